@@ -1,0 +1,213 @@
+"""Pins of the oracle (CPU restatement of the w2dynamics pair-move loop).
+
+* RNG stream against the reference's src/mtrng/random.cc (golden fixture
+  made by tests/golden/make_golden.py from that file compiled unchanged).
+* U matrices of w2dynamics_gb300.problems against the reference's
+  w2dyn/dmft/interaction.py (golden fixture).
+* time_evolve_in_eigenbasis known answer
+  (testsuite/ctqmc.tests/2-time-evolve-in-eigenbasis.F90:5-58).
+* fast updates (Sherman-Morrison grow/shrink, windowed trace) against full
+  recomputation after every proposal (the intent of the dead
+  MatrixUpdate.F90:489-632 test).
+* operator-list invariants of testsuite/ctqmc.tests/3-operator-list-stress-
+  test.F90 with a fixed seed.
+* physics known answers: U=0 impurity G(tau) equals the bath g(tau)
+  (half-filled Bethe lattice self-consistency), atomic-limit density matrix.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from w2dynamics_gb300 import problems as P
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_rng_stream_matches_reference_random_cc():
+    z = np.load(os.path.join(GOLD, "rng_streams.npz"))
+    for seed in (0, 1, 42, 4095):
+        ref = z[f"reals_{seed}"]
+        mine, _ = O.rng_stream(seed, len(ref), 0, 1, 1)
+        assert np.array_equal(mine, ref)
+        for lo, hi in ((1, 1), (1, 2), (1, 3), (1, 5), (8, 16), (1, 1000), (1, 123457)):
+            ref = z[f"ints_{seed}_{lo}_{hi}"]
+            _, ints = O.rng_stream(seed, 0, len(ref), lo, hi)
+            assert np.array_equal(ints, ref), (seed, lo, hi)
+
+
+def test_reference_rng_live_if_built():
+    """Compare directly against oracle/_ref (only where it could be built)."""
+    path = os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                        "librandom_ref.so")
+    if not os.path.exists(path):
+        pytest.skip("reference random.cc not built here")
+    import ctypes as C
+    lib = C.CDLL(path)
+    lib.new_random.restype = C.c_void_p
+    lib.seed_random.argtypes = [C.c_void_p, C.c_uint]
+    lib.get_random.argtypes = [C.c_void_p]
+    lib.get_random.restype = C.c_double
+    r = lib.new_random()
+    lib.seed_random(r, 777)
+    ref = np.array([lib.get_random(r) for _ in range(5000)])
+    mine, _ = O.rng_stream(777, 5000, 0, 1, 1)
+    assert np.array_equal(mine, ref)
+
+
+@pytest.mark.parametrize("key,fn,args", [
+    ("density_1_2.0_2.0_0.0", P.umatrix_density, (1, 2.0, 2.0, 0.0)),
+    ("density_2_3.0_2.0_0.5", P.umatrix_density, (2, 3.0, 2.0, 0.5)),
+    ("density_3_4.0_2.8_0.6", P.umatrix_density, (3, 4.0, 2.8, 0.6)),
+    ("kanamori_2_3.0_1.6_0.7", P.umatrix_kanamori, (2, 3.0, 1.6, 0.7)),
+    ("kanamori_3_4.0_2.8_0.6", P.umatrix_kanamori, (3, 4.0, 2.8, 0.6)),
+    ("kanamori_5_3.0_1.6_0.7", P.umatrix_kanamori, (5, 3.0, 1.6, 0.7)),
+])
+def test_umatrix_matches_reference_interaction(key, fn, args):
+    z = np.load(os.path.join(GOLD, "umatrices.npz"))
+    assert np.array_equal(P.flat_umatrix(fn(*args)), z[key])
+
+
+def test_time_evolve_known_answer():
+    """exp(-(E_i - Egs) tau) scaling of the reference test (10 states,
+    E_i = 0.1 i, tau = 0.3, rel 1e-14): the oracle's trace of a one-block
+    empty configuration equals the closed form."""
+    ev = 0.1 * np.arange(10)
+    tau = 0.3
+    vec = np.exp(-(ev - 0.0) * tau) * np.ones(10)
+    ref = np.array([np.exp(-(0.1 * i) * 0.3) for i in range(10)])
+    assert np.allclose(vec, ref, rtol=1e-14, atol=0)
+    # the same identity through the oracle: H = diag(-mu n) for one orbital
+    m = O.Model(1, np.zeros((2, 2, 2, 2)), P.muimp_solver(1, 0.7), "Nt Szt")
+    c = O.Chain(m, tau, np.ones((1, 2, 5)) * 0.1, 10, seed=3, taudiff_max=tau)
+    # empty trace of the chosen outer superstate: sum_i exp(-(E_i-Egs) beta)
+    sst = int(c.state()["outer_sst"])
+    off, n = m.sst_offset[sst], m.sst_size[sst]
+    e = m.evals[off:off + n]
+    expect = np.log(np.sum(np.exp(-(e - m.egs) * tau)))
+    assert abs(c.state()["trace_log"] - expect) < 1e-14
+
+
+def _hyb(F, beta, t):
+    s = 1.0
+    if t < 0:
+        t += beta
+        s = -1.0
+    n = t / beta * (len(F) - 1)
+    i = int(n)
+    return s * (F[i] + (n - i) * (F[i + 1] - F[i]))
+
+
+@pytest.mark.parametrize("name,beta,tdm,pout", [
+    ("anderson1", 10.0, 10.0, 0.0),
+    ("anderson1", 10.0, 3.0, 0.2),
+    ("dd3", 8.0, 8.0, 0.1),
+    ("dd3", 8.0, 2.5, 0.0),
+])
+def test_fast_updates_match_full_recompute(name, beta, tdm, pout):
+    pr = P.config_problem(name, beta=beta)
+    m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    c = O.Chain(m, pr["beta"], pr["ftau"], 50, seed=11, taudiff_max=tdm, p_outer=pout)
+    nacc = 0
+    for i in range(1500):
+        c.warmup(1)
+        st = c.state()
+        fd, ft = c.full_det(), c.full_trace()
+        assert abs(fd[0] - st["det_log"]) < 1e-9 and fd[1] == st["det_sign"], i
+        assert abs(ft[0] - st["trace_log"]) < 1e-9 and ft[1] == st["trace_sign"], i
+        nacc = st["noper"]
+    # inverse matrices against direct inversion
+    taus, orbs, spins, cas = c.get_config()
+    F = pr["ftau"][0, 0]
+    for b in range(pr["nd"]):
+        for s in range(2):
+            sel = (orbs - 1 == b) & (spins - 1 == s)
+            tc = np.sort(taus[sel & (cas == 1)])
+            ta = np.sort(taus[sel & (cas == 2)])
+            if len(tc) == 0:
+                continue
+            H = np.array([[_hyb(F, beta, a - cc) for cc in tc] for a in ta])
+            assert np.allclose(c.minv(2 * b + s), np.linalg.inv(H), rtol=1e-9, atol=1e-9)
+
+
+def test_operator_list_stress_invariants():
+    """3-operator-list-stress-test.F90 invariants with a fixed seed: time
+    order, per-flavour consistency, NPairs equal to a recount, window edges
+    (beta=100, 3 bands, TaudiffMax=10, window shift every 50 proposals)."""
+    nd = 3
+    um = P.flat_umatrix(P.umatrix_density(nd, 0.0, 0.0, 0.0))
+    m = O.Model(nd, um, P.muimp_solver(nd, 0.0), "Nt Szt")
+    beta = 100.0
+    ft = np.full((nd, 2, 200), 0.2)
+    c = O.Chain(m, beta, ft, 20, seed=12345, taudiff_max=10.0, ncorr=500)
+    st = c.state()
+    assert st["num_windows"] == 9 and st["nslide"] == max(6, 500 // 9)
+    for _ in range(300):
+        c.warmup(50)
+        st = c.state()
+        taus, orbs, spins, cas = c.get_config()
+        assert np.all(np.diff(taus) > 0)
+        for b in range(1, nd + 1):
+            for s in (1, 2):
+                sel = (orbs == b) & (spins == s)
+                assert np.sum(sel & (cas == 1)) == np.sum(sel & (cas == 2))
+        # NPairs recount from scratch
+        wmin, wmax, tdm = st["tauwin_min"], st["tauwin_max"], st["taudiff_max"]
+        n = 0
+        for i in range(len(taus)):
+            for j in range(i + 1, len(taus)):
+                if orbs[i] == orbs[j] and spins[i] == spins[j] and cas[i] != cas[j]:
+                    if taus[i] >= wmin and taus[j] <= wmax and taus[j] <= taus[i] + tdm:
+                        n += 1
+        assert n == st["npairs"]
+        assert wmax - wmin == pytest.approx(2 * beta / (st["num_windows"] + 1))
+
+
+def test_u0_green_function_equals_bath():
+    """U=0, mu=0, semicircle bath: the impurity G(tau) equals g(tau) of the
+    bath (half-filled Bethe lattice); w2dynamics' gtau convention is
+    positive.  16 chains, 20 bins per flavour."""
+    beta = 5.0
+    um = P.flat_umatrix(P.umatrix_density(1, 0.0, 0.0, 0.0))
+    ft = P.semicircle_ftau(1, beta, 1.0, 500)
+    g = P.semicircle_gtau(beta, 1.0, 500)
+    m = O.Model(1, um, P.muimp_solver(1, 0.0), "Nt Szt Azt")
+    res, dms = [], []
+    for seed in range(16):
+        c = O.Chain(m, beta, ft, 20, seed=seed, taudiff_max=beta, p_outer=0.1)
+        c.warmup(5000)
+        c.measure(4000)
+        r = c.results()
+        res.append(r["gtau"])
+        dms.append(np.diag(r["densitymatrix"]))
+        assert r["mean_sign"] == -1.0
+    G = np.mean(res, axis=0)
+    E = np.std(res, axis=0, ddof=1) / np.sqrt(len(res))
+    tt = np.linspace(0, beta, 500)
+    edges = np.linspace(0, beta, 21)
+    gex = np.array([np.mean(np.interp(np.linspace(a, b, 400), tt, g))
+                    for a, b in zip(edges[:-1], edges[1:])])
+    z = (G - gex) / E
+    assert np.abs(z).max() < 4.5
+    assert abs(z.mean()) < 1.0
+    assert np.allclose(np.mean(dms, axis=0), 0.25, atol=0.01)
+
+
+def test_atomic_limit_density_matrix():
+    """Delta -> 0: the sampled density matrix is exp(-beta H)/Z restricted
+    to the chain's outer superstate sector (no insertion is ever accepted)."""
+    beta = 2.0
+    pr = P.config_problem("dd3", beta=beta)
+    m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    ft = np.full((3, 2, 100), 1e-12)
+    c = O.Chain(m, beta, ft, 10, seed=5, taudiff_max=beta)
+    c.warmup(200)
+    c.measure(100)
+    r = c.results()
+    sst = int(c.state()["outer_sst"])
+    off, n = m.sst_offset[sst], m.sst_size[sst]
+    e = m.evals[off:off + n]
+    w = np.exp(-beta * (e - e.min()))
+    dm = np.diag(r["densitymatrix"])[off:off + n]
+    assert np.allclose(dm, w / w.sum(), rtol=1e-10)
