@@ -1,0 +1,165 @@
+/* cthyb_gpu.h -- C ABI of the GB300 CT-HYB pair-move engine.
+ *
+ * Drop-in boundary for the inner Monte Carlo loop of the w2dynamics Fortran
+ * module `ctqmc` (src/ctqmc_fortran/CTQMC.F90).  Plain C types only: a
+ * Fortran host binds these with iso_c_binding, Python with ctypes.  Every
+ * entry returns 0 on success and a negative code on failure; the message is
+ * available from cthyb_last_error().  Nothing in the library calls exit,
+ * abort or traps: the reference's `stop` conditions (CTQMC.F90:4062
+ * "DetRat too small in removal", Trace.F90:1777 "NPairs counting logic
+ * error") are reported as CTHYB_ERR_NUMERIC / CTHYB_ERR_INTERNAL.
+ *
+ * Conventions (as in the reference):
+ *   orbital b = 1..Nd, spin s = 1..2, ca = 1 (creator) / 2 (annihilator);
+ *   flavour index inside arrays f = 2*(b-1) + (s-1);
+ *   Fock bit of (b,s): (b-1) + Nd*(s-1) (Operator.F90:157);
+ *   U matrix (2Nd)^4 in Fortran order, flavour 2*(b-1)+s (Trace.F90:449);
+ *   muimp (Nd,2,Nd,2) Fortran order, solver sign (cthyb_solver.py:255);
+ *   F(tau) (Nd,2,Nftau) Fortran order on tau_j = j*beta/(Nftau-1).
+ */
+#ifndef CTHYB_GPU_H
+#define CTHYB_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CTHYB_OK 0
+#define CTHYB_ERR_ARG (-1)
+#define CTHYB_ERR_CUDA (-2)
+#define CTHYB_ERR_CAPACITY (-3)
+#define CTHYB_ERR_NUMERIC (-4)
+#define CTHYB_ERR_INTERNAL (-5)
+#define CTHYB_ERR_UNSUPPORTED (-6)
+
+typedef struct cthyb_model_s* cthyb_model_t;
+typedef struct cthyb_batch_s* cthyb_batch_t;
+
+/* Message of the last failed call on this thread. */
+const char* cthyb_last_error(void);
+
+/* Local problem: Fock space, superstates from the QuantumNumbers string,
+ * H_loc eigenbasis per superstate, c/c+ blocks in that eigenbasis.
+ * Replaces init_States / qns2substates / init_Psi / oneparticle_hamiltonian /
+ * u_hamiltonian / diag_Operator / transform_Psis called from init_solver
+ * (CTQMC.F90:7894-8000; States.F90:58-186; Operator.F90:115-300,482-546,
+ * 637-735,1042-1172). */
+int cthyb_model_create(int nd, const double* umatrix, const double* muimp,
+                       const char* quantum_numbers, cthyb_model_t* out);
+int cthyb_model_destroy(cthyb_model_t model);
+/* nsst, nstates, nsmax, monomial (1: every c/c+ block has one entry per
+ * column -- density-density models), egs */
+int cthyb_model_info(cthyb_model_t model, int* nsst, int* nstates, int* nsmax,
+                     int* monomial, double* egs);
+/* per superstate size/offset; per eigenstate the Fock state with the largest
+ * weight and the eigenvalue (StatesSuperstates / EigenstatesEnergies,
+ * CTQMC.F90:8040-8060) */
+int cthyb_model_states(cthyb_model_t model, int* sst_size, int* sst_offset,
+                       int* fock_state, double* evals);
+/* target superstate of operator (b,s,ca) acting on superstate sst, 1-based
+ * b, s, ca (the Connect table, States.F90:45), -1 if none */
+int cthyb_model_connect(cthyb_model_t model, int sst, int b, int s, int ca);
+
+/* One group of chains sharing beta and F(tau). */
+typedef struct {
+  double beta;
+  int32_t nftau;
+  int32_t ntau;          /* G(tau) bins (Ntau) */
+  const double* ftau;    /* (Nd,2,Nftau) Fortran order */
+  int32_t nchains;
+  int32_t seed0;         /* chain c is seeded with seed0 + c unless seeds */
+  const int32_t* seeds;  /* optional per-chain seeds (NULL: seed0 + c) */
+  double taudiff_max;    /* TaudiffMax parameter; <= 0: one window */
+  int32_t ncorr;         /* NCorr: proposals between measurements */
+  double p_outer;        /* PercentageOuterMove */
+  int32_t kcap;          /* max pairs per flavour (0: automatic) */
+  int32_t opcap;         /* max operators in a configuration (0: automatic) */
+  int32_t tree_levels;   /* time-bin tree depth, 2^levels leaves (0: automatic) */
+  int32_t maxhisto;      /* expansion-order histogram bins (MaxHisto) */
+  int32_t flags;         /* CTHYB_FLAG_* */
+} cthyb_group_desc;
+
+#define CTHYB_FLAG_DENSE 1  /* dense block trace even for monomial models */
+#define CTHYB_FLAG_NO_DM 2  /* skip the beta/2 density-matrix measurement */
+
+/* Create chains for all groups and initialise them like init_Trace
+ * (Trace.F90:340-701): window from TaudiffMax, outer superstate drawn with
+ * one uniform number in proportion to the empty trace, NSlide
+ * (CTQMC.F90:8069).  Chains are numbered consecutively over groups.
+ * Replaces init_solver's init_Trace / init_CTQMC for one process
+ * (one chain) or for a batch of independent chains. */
+int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc* groups,
+                       cthyb_batch_t* out);
+int cthyb_batch_destroy(cthyb_batch_t batch);
+int cthyb_batch_nchains(cthyb_batch_t batch);
+/* set_taudiffmax (CTQMC.F90:8180 -> init_window, Trace.F90:1608) */
+int cthyb_batch_set_taudiffmax(cthyb_batch_t batch, int group, double taudiff_max);
+/* ctqmc_warmup(N) for every chain (CTQMC.F90:8188-8263): N pair proposals */
+int cthyb_batch_warmup(cthyb_batch_t batch, int64_t nproposals);
+/* ctqmc_measure Z-space loop (CTQMC.F90:8355-8566): nmeas x NCorr
+ * proposals, measurements of sign, order histogram, density matrix at
+ * beta/2 and G(tau) (MeasGtauRem) after each NCorr block.  Accumulates
+ * across calls until cthyb_batch_reset_measurements. */
+int cthyb_batch_measure(cthyb_batch_t batch, int64_t nmeas);
+int cthyb_batch_reset_measurements(cthyb_batch_t batch);
+/* Wait for queued work; returns the first chain error if any. */
+int cthyb_batch_sync(cthyb_batch_t batch);
+/* CUDA stream the batch runs on (cudaStream_t as void*). */
+int cthyb_batch_stream(cthyb_batch_t batch, void** stream);
+/* Capture warmup/measure launches into CUDA graphs and replay them
+ * (1 = on, default off). */
+int cthyb_batch_use_graphs(cthyb_batch_t batch, int on);
+
+/* Normalised results of one chain (CTQMC.F90:8676-8760):
+ *   gtau (Nd,2,Ntau) Fortran order, mean_sign, densitymatrix in the
+ *   eigenbasis (nstates x nstates, column-major), histo (Nd,2,maxhisto)
+ *   Fortran order; counters[8] = try_add, acc_add, try_rem, acc_rem,
+ *   qn_add, qn_rem, cnt_meas, proposals.  Any output pointer may be NULL. */
+int cthyb_batch_results(cthyb_batch_t batch, int chain, double* gtau, double* mean_sign,
+                        double* densitymatrix, double* histo, int64_t* counters);
+/* Raw (unnormalised) accumulators summed over the chains of one group:
+ * gtau_sum[(Nd,2,Ntau)], sign_sum, cnt_meas. */
+int cthyb_batch_group_sums(cthyb_batch_t batch, int group, double* gtau_sum,
+                           double* sign_sum, int64_t* cnt_meas);
+/* Chain state: trace_log, trace_sign, det_log, det_sign, cfgsign, npairs,
+ * outer_sst, window_position, num_windows, noper, tauwin_min, tauwin_max,
+ * taudiff_max, nslide, status, pairs of flavour 0.. (16 doubles). */
+int cthyb_batch_state(cthyb_batch_t batch, int chain, double* out16);
+/* Configuration in the get_mc_config layout (CTQMC.F90:9367): returns the
+ * operator count in *n; arrays sized by the caller (opcap). */
+int cthyb_batch_get_config(cthyb_batch_t batch, int chain, int* n, double* taus,
+                           int* orbs, int* spins, int* cas, int* outer_sst);
+/* set_mc_config (CTQMC.F90:9378 -> Trace.F90:6872-7001): rebuild lists,
+ * full inverse hybridisation matrices by LU, trace and sign. */
+int cthyb_batch_set_config(cthyb_batch_t batch, int chain, int n, const double* taus,
+                           const int* orbs, const int* spins, const int* cas, int outer_sst);
+/* Inverse hybridisation matrix of one flavour f = 2(b-1)+(s-1) in time
+ * order (rows creators, columns annihilators, column-major k x k);
+ * returns k in *k. */
+int cthyb_batch_minv(cthyb_batch_t batch, int chain, int f, int* k, double* out);
+/* Full LU rebuild of every M of every chain (get_InvFullHybr,
+ * Trace.F90:2279-2336): max |M_fast - M_LU| over the batch in *maxdev;
+ * replace != 0 also installs the rebuilt matrices. */
+int cthyb_batch_refresh_minv(cthyb_batch_t batch, int replace, double* maxdev);
+
+/* Per-proposal records (layout cthyb_record below) for parity checks:
+ * cap records per chain; 0 disables. */
+int cthyb_batch_set_log(cthyb_batch_t batch, int64_t cap_per_chain);
+int cthyb_batch_get_log(cthyb_batch_t batch, int chain, void* records, int64_t* n);
+
+typedef struct {
+  int32_t move, outcome, orb, spin, change_outer, fpos_c, fpos_a, npairs, outer_sst, k_total;
+  double tau_c, tau_a, det_log, det_sign, tr_log, tr_sign, prob, rand;
+} cthyb_record;
+
+/* Device-side bookkeeping statistics for the roofline: bytes of M and
+ * operator arrays touched and flops of the determinant ratios and updates,
+ * summed over all chains since the last reset (8 int64). */
+int cthyb_batch_work_counters(cthyb_batch_t batch, int64_t* out8, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CTHYB_GPU_H */

@@ -1,0 +1,2576 @@
+// engine.cu -- GB300 (sm_103a) CT-HYB pair-move engine.
+//
+// One warp advances one Markov chain through the proposal loop of the
+// w2dynamics Fortran module (CTQMC.F90 ctqmc_warmup / ctqmc_measure ->
+// StepAdd / StepRem), so that a launch of N warps advances N independent
+// chains; a batch of one chain is the plain drop-in form.
+//
+// Per chain, in HBM:
+//   * a Mersenne-twister state that reproduces, draw for draw, the
+//     reference's std::mt19937 + uniform_real_distribution<double> +
+//     uniform_int_distribution<int> stream (src/mtrng/random.cc:35-78), so a
+//     chain seeded with s makes exactly the proposals of the reference run
+//     seeded with s;
+//   * the time-ordered operator array and, per flavour, the sorted creator
+//     and annihilator times (ranks = the FPos of Trace.F90:4275-4500);
+//   * per flavour the inverse hybridisation matrix M in "slot" order: rows
+//     and columns stay where they were appended, so the Sherman-Morrison
+//     grow/shrink of MatrixUpdate.F90:392-482 needs no row/column shifting;
+//   * a binary tree over 2^L equal time bins of [0, beta): each node holds,
+//     for every superstate, the superstate it is mapped to across the node's
+//     time span, and (density-density models) for every eigenstate the
+//     target state, log-weight and sign of the time-ordered product of
+//     propagators and c/c+ operators inside the span.  A pair move rebuilds
+//     at most two leaves and their ancestors (O(L) nodes) in the inactive
+//     half of a double buffer; acceptance flips the active bits.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/cthyb_gpu.h"
+#include "engine.cuh"
+#include "model.h"
+
+namespace cthyb {
+
+// ---------------------------------------------------------------------------
+// Chain context (all lanes hold the same values).
+struct Ctx {
+  const DModel* m;
+  const DGroup* g;
+  Hdr* h;
+  uint32_t* mt;
+  double* optau;
+  int* opcode;
+  double* srt_tau;
+  short* srt_slot;
+  double* slot_tau;
+  double* M;
+  char* tree;
+  unsigned char* act;
+  double* scr;
+  double* btau;
+  int* bcode;
+  double* gtau;
+  double* histo;
+  double* dm;
+  double* dense;
+  cthyb_record* log;
+  int lane, mti, mono, kcap, chain;
+};
+
+__device__ __forceinline__ double* srt_ptr(const Ctx& c, int f, int ca) {
+  return c.srt_tau + (size_t)(f * 2 + ca) * c.kcap;
+}
+__device__ __forceinline__ short* sslot_ptr(const Ctx& c, int f, int ca) {
+  return c.srt_slot + (size_t)(f * 2 + ca) * c.kcap;
+}
+__device__ __forceinline__ double* stau_ptr(const Ctx& c, int f, int ca) {
+  return c.slot_tau + (size_t)(f * 2 + ca) * c.kcap;
+}
+__device__ __forceinline__ double* M_ptr(const Ctx& c, int f) {
+  return c.M + (size_t)f * c.kcap * c.kcap;
+}
+
+__device__ __forceinline__ void set_status(Ctx& c, int st) {
+  if (c.lane == 0 && c.h->status == ST_OK) c.h->status = st;
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Warp reductions
+__device__ __forceinline__ double wsum(double x) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+  return x;
+}
+__device__ __forceinline__ double wmax(double x) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) x = fmax(x, __shfl_xor_sync(FULL, x, o));
+  return x;
+}
+__device__ __forceinline__ int wsumi(int x) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(FULL, x, o);
+  return x;
+}
+
+// ---------------------------------------------------------------------------
+// Mersenne twister MT19937 (Matsumoto & Nishimura 1998), warp-cooperative
+// state regeneration; the uniform double follows the C++ standard's
+// generate_canonical with two 32-bit draws, the bounded integer Lemire's
+// nearly-divisionless method (ACM TOMACS 29(1), 2019) -- the algorithms of
+// the standard library used by src/mtrng/random.cc.
+__device__ void mt_twist(uint32_t* mt, int lane) {
+  for (int base = 0; base < 624; base += 32) {
+    int i = base + lane;
+    bool on = i < 624;
+    uint32_t a = 0, b = 0, cc = 0;
+    if (on) {
+      a = mt[i];
+      b = mt[i + 1 < 624 ? i + 1 : 0];
+      cc = mt[i + 397 < 624 ? i + 397 : i + 397 - 624];
+    }
+    __syncwarp();
+    if (on) {
+      uint32_t y = (a & 0x80000000u) | (b & 0x7fffffffu);
+      mt[i] = cc ^ (y >> 1) ^ ((y & 1u) ? 0x9908b0dfu : 0u);
+    }
+    __syncwarp();
+  }
+}
+__device__ __forceinline__ uint32_t mt_next(Ctx& c) {
+  if (c.mti >= 624) {
+    mt_twist(c.mt, c.lane);
+    c.mti = 0;
+  }
+  uint32_t y = c.mt[c.mti];
+  c.mti++;
+  y ^= y >> 11;
+  y ^= (y << 7) & 0x9d2c5680u;
+  y ^= (y << 15) & 0xefc60000u;
+  y ^= y >> 18;
+  return y;
+}
+__device__ __forceinline__ double grnd(Ctx& c) {
+  uint32_t a = mt_next(c);
+  uint32_t b = mt_next(c);
+  double s = __dadd_rn((double)a, __dmul_rn((double)b, 4294967296.0));
+  double r = s * 0x1p-64;
+  if (r >= 1.0) r = 0x1.fffffffffffffp-1;
+  return r;
+}
+__device__ __forceinline__ int randint(Ctx& c, int lo, int hi) {
+  uint32_t range = (uint32_t)(hi - lo) + 1u;
+  uint64_t prod = (uint64_t)mt_next(c) * range;
+  uint32_t low = (uint32_t)prod;
+  if (low < range) {
+    uint32_t thr = (0u - range) % range;
+    int guard = 0;
+    while (low < thr) {
+      prod = (uint64_t)mt_next(c) * range;
+      low = (uint32_t)prod;
+      if (++guard > 256) {
+        set_status(c, ST_INTERNAL);
+        break;
+      }
+    }
+  }
+  return lo + (int)(prod >> 32);
+}
+__device__ void mt_seed(uint32_t* mt, uint32_t seed, int lane) {
+  if (lane == 0) {
+    mt[0] = seed;
+    for (int i = 1; i < 624; ++i) mt[i] = 1812433253u * (mt[i - 1] ^ (mt[i - 1] >> 30)) + (uint32_t)i;
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Warp 32-ary searches on sorted double arrays.
+// first index i in [0,n) with !(a[i] < x)   (lower bound)
+__device__ int wlb(const double* a, int n, double x, int lane) {
+  int lo = 0, hi = n;
+  while (hi - lo > 32) {
+    int step = (hi - lo + 31) >> 5;
+    int p = lo + lane * step;
+    bool pr = (p < hi) && (a[p] < x);
+    int cnt = __popc(__ballot_sync(FULL, pr));
+    if (cnt == 0) {
+      hi = lo;
+      break;
+    }
+    int pl = lo + (cnt - 1) * step, pn = lo + cnt * step;
+    lo = pl + 1;
+    hi = min(pn, hi);
+  }
+  if (hi > lo) {
+    int p = lo + lane;
+    bool pr = (p < hi) && (a[p] < x);
+    lo += __popc(__ballot_sync(FULL, pr));
+  }
+  return lo;
+}
+// first index i with a[i] > x   (upper bound)
+__device__ int wub(const double* a, int n, double x, int lane) {
+  int lo = 0, hi = n;
+  while (hi - lo > 32) {
+    int step = (hi - lo + 31) >> 5;
+    int p = lo + lane * step;
+    bool pr = (p < hi) && (a[p] <= x);
+    int cnt = __popc(__ballot_sync(FULL, pr));
+    if (cnt == 0) {
+      hi = lo;
+      break;
+    }
+    int pl = lo + (cnt - 1) * step, pn = lo + cnt * step;
+    lo = pl + 1;
+    hi = min(pn, hi);
+  }
+  if (hi > lo) {
+    int p = lo + lane;
+    bool pr = (p < hi) && (a[p] <= x);
+    lo += __popc(__ballot_sync(FULL, pr));
+  }
+  return lo;
+}
+// sequential (single-thread) versions for per-lane use
+__device__ __forceinline__ int slb(const double* a, int n, double x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ int sub(const double* a, int n, double x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (a[mid] <= x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Hybridisation function: get_HybrF, Trace.F90:1014-1033, with the
+// reference's operation order and no fused multiply-adds.
+__device__ __forceinline__ double hybrf(const Ctx& c, double tau, int f) {
+  const DGroup& g = *c.g;
+  double sig;
+  if (tau < 0.0) {
+    tau = __dadd_rn(tau, g.beta);
+    sig = -1.0;
+  } else {
+    sig = 1.0;
+  }
+  double n = __dmul_rn(__ddiv_rn(tau, g.beta), (double)(g.nftau - 1));
+  int i = (int)n;
+  if (i > g.nftau - 2) i = g.nftau - 2;
+  if (i < 0) i = 0;
+  const double* F = g.hybr + (size_t)f * g.nftau;
+  double f0 = F[i], f1 = F[i + 1];
+  return __dmul_rn(sig, __dadd_rn(f0, __dmul_rn(__dsub_rn(n, (double)(int)n), __dsub_rn(f1, f0))));
+}
+
+// ---------------------------------------------------------------------------
+// Window (Trace.F90:1608-1754)
+__device__ void set_window_bounds(Ctx& c) {
+  Hdr& h = *c.h;
+  if (c.lane == 0 && h.num_windows > 1) {
+    h.tauwin_min = __dmul_rn(__ddiv_rn((double)h.window_position, (double)(h.num_windows + 1)), c.g->beta);
+    h.tauwin_max = __dmul_rn(__ddiv_rn((double)(h.window_position + 2), (double)(h.num_windows + 1)), c.g->beta);
+  }
+  __syncwarp();
+}
+__device__ void init_window(Ctx& c, double tdm) {
+  Hdr& h = *c.h;
+  if (c.lane == 0) {
+    h.window_position = 0;
+    if (tdm > 0.0) {
+      h.taudiff_max = tdm;
+      int nw = (int)floor(c.g->beta / tdm) - 1;
+      h.num_windows = nw > 1 ? nw : 1;
+      h.tauwin_min = __dmul_rn(__ddiv_rn(0.0, (double)(h.num_windows + 1)), c.g->beta);
+      h.tauwin_max = __dmul_rn(__ddiv_rn(2.0, (double)(h.num_windows + 1)), c.g->beta);
+    } else {
+      h.taudiff_max = c.g->beta;
+      h.num_windows = 1;
+      h.tauwin_min = 0.0;
+      h.tauwin_max = c.g->beta;
+    }
+    h.npairs = -1;
+  }
+  __syncwarp();
+}
+__device__ void shift_window(Ctx& c) {
+  Hdr& h = *c.h;
+  if (h.num_windows > 1) {
+    if (c.lane == 0) {
+      h.window_position += 1;
+      if (h.window_position == h.num_windows) h.window_position = 0;
+      h.npairs = -1;
+    }
+    __syncwarp();
+    set_window_bounds(c);
+  } else {
+    if (c.lane == 0) h.window_position = 0;
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pair counting (ensure_valid_NPairs_diag / update_NPairs_diag,
+// Trace.F90:1756-1922) on the sorted per-flavour arrays.
+// Later partners of an operator at t: opposite-CA times u with
+// t < u <= min(win_max, t + tdm).
+__device__ __forceinline__ int cnt_later(const double* opp, int n, double t, double wmax, double tdm) {
+  double hi = fmin(wmax, __dadd_rn(t, tdm));
+  int a = sub(opp, n, t), b = sub(opp, n, hi);
+  return b > a ? b - a : 0;
+}
+// Earlier partners: max(win_min, t - tdm) <= u < t.
+__device__ __forceinline__ int cnt_earlier(const double* opp, int n, double t, double wmin, double tdm) {
+  double lo = fmax(wmin, __dsub_rn(t, tdm));
+  int a = slb(opp, n, lo), b = slb(opp, n, t);
+  return b > a ? b - a : 0;
+}
+__device__ int count_npairs(Ctx& c) {
+  Hdr& h = *c.h;
+  int K = h.K;
+  int start = wlb(c.optau, K, h.tauwin_min, c.lane);
+  int tot = 0;
+  for (int i = start + c.lane; i < K; i += 32) {
+    double t = c.optau[i];
+    if (t > h.tauwin_max) continue;
+    int code = c.opcode[i], f = code >> 1, ca = code & 1;
+    tot += cnt_later(srt_ptr(c, f, 1 - ca), h.k[f], t, h.tauwin_max, h.taudiff_max);
+  }
+  return wsumi(tot);
+}
+
+// ---------------------------------------------------------------------------
+// Configuration sign (get_Sign with get_BlockSign and get_permaltca,
+// Trace.F90:3479-3621).  BlockSign counts, for each operator, the
+// operators after it whose flavour index 2b+s is smaller; permaltca counts
+// for each creator the operators of its flavour after it, plus one if the
+// number of pairs is odd.
+__device__ double config_sign(Ctx& c) {
+  Hdr& h = *c.h;
+  const int K = h.K, nf = c.m->nf;
+  int chunk = (K + 31) >> 5;
+  int lo = min(K, c.lane * chunk), hi = min(K, lo + chunk);
+  int hist[NFMAX];
+#pragma unroll
+  for (int g = 0; g < NFMAX; ++g) hist[g] = 0;
+  for (int i = lo; i < hi; ++i) {
+    int f = c.opcode[i] >> 1;
+#pragma unroll
+    for (int g = 0; g < NFMAX; ++g) hist[g] += (f == g);
+  }
+  int pre[NFMAX], tot[NFMAX];
+#pragma unroll
+  for (int g = 0; g < NFMAX; ++g) {
+    int x = hist[g];
+    // inclusive scan
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(FULL, x, o);
+      if (c.lane >= o) x += y;
+    }
+    tot[g] = __shfl_sync(FULL, x, 31);
+    pre[g] = x - hist[g];
+  }
+  int inv = 0, alt = 0;
+  for (int i = lo; i < hi; ++i) {
+    int code = c.opcode[i], f = code >> 1, ca = code & 1;
+    // operators before i with a larger flavour index: inversions of the
+    // (time, flavour) order
+#pragma unroll
+    for (int g = 0; g < NFMAX; ++g)
+      if (g > f && g < nf) inv += pre[g];
+#pragma unroll
+    for (int g = 0; g < NFMAX; ++g)
+      if (g == f) pre[g] += 1;
+    if (ca == 0) {
+      int after = 0;
+#pragma unroll
+      for (int g = 0; g < NFMAX; ++g)
+        if (g == f) after = tot[g] - pre[g];
+      alt += after;
+    }
+  }
+  inv = wsumi(inv & 1) & 1;
+  alt = wsumi(alt & 1) & 1;
+  if ((K / 2) % 2 == 1) alt ^= 1;
+  double bs = inv ? -1.0 : 1.0, pa = alt ? -1.0 : 1.0;
+  return h.trace_sign * h.det_sign * bs * pa;
+}
+
+// ---------------------------------------------------------------------------
+// Time-bin tree
+struct Mod {
+  int type;         // 0 none, 1 insert, 2 remove
+  double t1, t2;    // inserted times (t1 < t2)
+  int c1, c2;       // inserted codes
+  int ix, iy;       // removed indices (ix < iy)
+  int b1, b2;       // affected leaves
+};
+
+__device__ __forceinline__ double bin_edge(const Ctx& c, int j) {
+  return __dmul_rn(c.g->beta, ldexp((double)j, -c.g->L));
+}
+__device__ __forceinline__ int bin_of(const Ctx& c, double t) {
+  const int nb = 1 << c.g->L;
+  int j = (int)(t / c.g->beta * (double)nb);
+  if (j < 0) j = 0;
+  if (j > nb - 1) j = nb - 1;
+  while (j < nb - 1 && bin_edge(c, j + 1) <= t) ++j;
+  while (j > 0 && bin_edge(c, j) > t) --j;
+  return j;
+}
+__device__ __forceinline__ char* node_base(const Ctx& c, int n, int slot) {
+  return c.tree + ((size_t)n * 2 + slot) * c.g->node_bytes;
+}
+__device__ __forceinline__ double* node_lw(const Ctx& c, int n, int slot) {
+  return (double*)node_base(c, n, slot);
+}
+__device__ __forceinline__ uint16_t* node_tg(const Ctx& c, int n, int slot) {
+  return (uint16_t*)(node_base(c, n, slot) + (size_t)c.m->ns * 8);
+}
+__device__ __forceinline__ int16_t* node_ss(const Ctx& c, int n, int slot) {
+  return (int16_t*)(node_base(c, n, slot) + (c.mono ? (size_t)c.m->ns * 10 : 0));
+}
+__device__ __forceinline__ bool node_mod(const Ctx& c, const Mod& md, int n) {
+  if (md.type == 0) return false;
+  int L = c.g->L;
+  int d = 31 - __clz(n);
+  int n1 = ((1 << L) + md.b1) >> (L - d), n2 = ((1 << L) + md.b2) >> (L - d);
+  return n == n1 || n == n2;
+}
+// slot holding the proposed content of node n
+__device__ __forceinline__ int node_slot(const Ctx& c, const Mod& md, int n) {
+  int a = c.act[n];
+  return node_mod(c, md, n) ? 1 - a : a;
+}
+
+// Gather the operators of bin b of the proposed configuration into
+// btau/bcode; returns their number.
+__device__ int gather_bin(Ctx& c, const Mod& md, int b) {
+  const int K = c.h->K;
+  const int nb = 1 << c.g->L;
+  double e0 = bin_edge(c, b), e1 = b + 1 < nb ? bin_edge(c, b + 1) : 0.0;
+  int lo = wlb(c.optau, K, e0, c.lane);
+  int hi = b + 1 < nb ? wlb(c.optau, K, e1, c.lane) : K;
+  bool in1 = false, in2 = false;
+  if (md.type == 1) {
+    in1 = bin_of(c, md.t1) == b;
+    in2 = bin_of(c, md.t2) == b;
+  }
+  int nrem = 0;
+  if (md.type == 2) nrem = (md.ix >= lo && md.ix < hi) + (md.iy >= lo && md.iy < hi);
+  for (int j = lo + c.lane; j < hi; j += 32) {
+    double t = c.optau[j];
+    int code = c.opcode[j];
+    int r = j - lo;
+    if (md.type == 1) {
+      r += (in1 && md.t1 < t) + (in2 && md.t2 < t);
+    } else if (md.type == 2) {
+      if (j == md.ix || j == md.iy) continue;
+      r -= (md.ix >= lo && md.ix < j) + (md.iy >= lo && md.iy < j);
+    }
+    c.btau[r] = t;
+    c.bcode[r] = code;
+  }
+  int n = hi - lo - nrem;
+  if (md.type == 1) {
+    // positions of the inserted operators
+    int p1 = 0, p2 = 0;
+    if (in1) p1 = wlb(c.optau + lo, hi - lo, md.t1, c.lane);
+    if (in2) p2 = wlb(c.optau + lo, hi - lo, md.t2, c.lane) + (in1 ? 1 : 0);
+    if (c.lane == 0) {
+      if (in1) {
+        c.btau[p1] = md.t1;
+        c.bcode[p1] = md.c1;
+      }
+      if (in2) {
+        c.btau[p2] = md.t2;
+        c.bcode[p2] = md.c2;
+      }
+    }
+    n += in1 + in2;
+  }
+  __syncwarp();
+  return n;
+}
+
+// Leaf of bin b from the gathered operators (n of them), written to `slot`.
+__device__ void build_leaf(Ctx& c, int b, int n, int slot, bool states) {
+  const DModel& m = *c.m;
+  const int L = c.g->L, nb = 1 << L, node = nb + b;
+  int16_t* ss = node_ss(c, node, slot);
+  for (int s = c.lane; s < m.nss; s += 32) {
+    int cur = s;
+    for (int j = 0; j < n && cur >= 0; ++j) {
+      int code = c.bcode[j];
+      cur = m.connect[((size_t)cur * m.nf + (code >> 1)) * 2 + (code & 1)];
+    }
+    ss[s] = (int16_t)cur;
+  }
+  if (states && c.mono) {
+    double t0 = bin_edge(c, b), t1 = b + 1 < nb ? bin_edge(c, b + 1) : c.g->beta;
+    double* lw = node_lw(c, node, slot);
+    uint16_t* tg = node_tg(c, node, slot);
+    for (int s = c.lane; s < m.ns; s += 32) {
+      int cur = s;
+      double l = 0.0, t = t0;
+      int neg = 0;
+      for (int j = 0; j < n; ++j) {
+        double tj = c.btau[j];
+        l -= (m.eval[cur] - m.egs) * (tj - t);
+        size_t idx = (size_t)c.bcode[j] * m.ns + cur;
+        int nx = m.mono_tgt[idx];
+        if (nx < 0) {
+          cur = -1;
+          break;
+        }
+        l += m.mono_lv[idx];
+        neg ^= m.mono_neg[idx];
+        cur = nx;
+        t = tj;
+      }
+      if (cur >= 0) {
+        l -= (m.eval[cur] - m.egs) * (t1 - t);
+        tg[s] = (uint16_t)(cur | (neg << 15));
+        lw[s] = l;
+      } else {
+        tg[s] = 0x7fff;
+        lw[s] = -DHUGE;
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// Combine the children of node n into `slot` of n.
+__device__ void combine(Ctx& c, int n, int sl, int sr, int slot, bool states) {
+  const DModel& m = *c.m;
+  const int16_t* ssl = node_ss(c, 2 * n, sl);
+  const int16_t* ssr = node_ss(c, 2 * n + 1, sr);
+  int16_t* ss = node_ss(c, n, slot);
+  for (int s = c.lane; s < m.nss; s += 32) {
+    int a = ssl[s];
+    ss[s] = a < 0 ? (int16_t)-1 : ssr[a];
+  }
+  if (states && c.mono) {
+    const double* lwl = node_lw(c, 2 * n, sl);
+    const uint16_t* tgl = node_tg(c, 2 * n, sl);
+    const double* lwr = node_lw(c, 2 * n + 1, sr);
+    const uint16_t* tgr = node_tg(c, 2 * n + 1, sr);
+    double* lw = node_lw(c, n, slot);
+    uint16_t* tg = node_tg(c, n, slot);
+    for (int s = c.lane; s < m.ns; s += 32) {
+      uint16_t a = tgl[s];
+      int mid = a & 0x7fff;
+      if (mid == 0x7fff) {
+        tg[s] = 0x7fff;
+        lw[s] = -DHUGE;
+        continue;
+      }
+      uint16_t b = tgr[mid];
+      if ((b & 0x7fff) == 0x7fff) {
+        tg[s] = 0x7fff;
+        lw[s] = -DHUGE;
+        continue;
+      }
+      tg[s] = (uint16_t)((b & 0x7fff) | ((a ^ b) & 0x8000));
+      lw[s] = lwl[s] + lwr[mid];
+    }
+  }
+  __syncwarp();
+}
+
+// Rebuild the leaves of a proposal and their ancestors in the inactive slots.
+__device__ void tree_propose(Ctx& c, const Mod& md, bool states) {
+  const int L = c.g->L, nb = 1 << L;
+  int n = gather_bin(c, md, md.b1);
+  build_leaf(c, md.b1, n, 1 - c.act[nb + md.b1], states);
+  if (md.b2 != md.b1) {
+    n = gather_bin(c, md, md.b2);
+    build_leaf(c, md.b2, n, 1 - c.act[nb + md.b2], states);
+  }
+  for (int d = L - 1; d >= 0; --d) {
+    int n1 = (nb + md.b1) >> (L - d), n2 = (nb + md.b2) >> (L - d);
+    combine(c, n1, node_slot(c, md, 2 * n1), node_slot(c, md, 2 * n1 + 1), 1 - c.act[n1], states);
+    if (n2 != n1) combine(c, n2, node_slot(c, md, 2 * n2), node_slot(c, md, 2 * n2 + 1), 1 - c.act[n2], states);
+  }
+  if (c.lane == 0) c.h->w_nodes += 2 * (L + 1);
+}
+__device__ void tree_accept(Ctx& c, const Mod& md) {
+  const int L = c.g->L, nb = 1 << L;
+  if (c.lane == 0) {
+    for (int d = L; d >= 0; --d) {
+      int n1 = (nb + md.b1) >> (L - d), n2 = (nb + md.b2) >> (L - d);
+      c.act[n1] ^= 1;
+      if (n2 != n1) c.act[n2] ^= 1;
+    }
+  }
+  __syncwarp();
+}
+// Full build from the current operator array into slot 0.
+__device__ void tree_build_all(Ctx& c) {
+  const int L = c.g->L, nb = 1 << L;
+  Mod md;
+  md.type = 0;
+  for (int b = 0; b < nb; ++b) {
+    int n = gather_bin(c, md, b);
+    build_leaf(c, b, n, 0, true);
+  }
+  for (int n = nb - 1; n >= 1; --n) combine(c, n, 0, 0, 0, true);
+  for (int i = c.lane; i < 2 * nb; i += 32) c.act[i] = 0;
+  __syncwarp();
+}
+
+// Superstate just before time t in the current configuration, starting from
+// s at tau = 0.
+__device__ int old_prefix(Ctx& c, int s, double t) {
+  const int L = c.g->L, nb = 1 << L;
+  const DModel& m = *c.m;
+  int b = bin_of(c, t);
+  int node = 1, lo = 0, span = nb;
+  for (int d = 0; d < L && s >= 0; ++d) {
+    int half = span >> 1;
+    if (b >= lo + half) {
+      s = node_ss(c, 2 * node, c.act[2 * node])[s];
+      node = 2 * node + 1;
+      lo += half;
+    } else {
+      node = 2 * node;
+    }
+    span = half;
+  }
+  if (s < 0) return -1;
+  int K = c.h->K;
+  int j0 = wlb(c.optau, K, bin_edge(c, b), c.lane);
+  int j1 = wlb(c.optau, K, t, c.lane);
+  for (int j = j0; j < j1 && s >= 0; ++j) {
+    int code = c.opcode[j];
+    s = m.connect[((size_t)s * m.nf + (code >> 1)) * 2 + (code & 1)];
+  }
+  return s;
+}
+// Superstate at beta reached from superstate s just before time t through
+// the proposed configuration's operators at times >= t.
+__device__ int new_suffix(Ctx& c, const Mod& md, int s, double t) {
+  const int L = c.g->L, nb = 1 << L;
+  const DModel& m = *c.m;
+  int b = bin_of(c, t);
+  int n = gather_bin(c, md, b);
+  for (int j = 0; j < n && s >= 0; ++j) {
+    if (c.btau[j] < t) continue;
+    int code = c.bcode[j];
+    s = m.connect[((size_t)s * m.nf + (code >> 1)) * 2 + (code & 1)];
+  }
+  // right siblings along the root-to-leaf path, deepest first
+  int path[24];
+  int np = 0;
+  int node = 1, lo = 0, span = nb;
+  for (int d = 0; d < L; ++d) {
+    int half = span >> 1;
+    if (b >= lo + half) {
+      node = 2 * node + 1;
+      lo += half;
+    } else {
+      path[np++] = 2 * node + 1;
+      node = 2 * node;
+    }
+    span = half;
+  }
+  for (int i = np - 1; i >= 0 && s >= 0; --i) s = node_ss(c, path[i], node_slot(c, md, path[i]))[s];
+  return s;
+}
+
+// Trace of superstate s0 from the root state map in `slot`:
+// sum over states i of s0 mapped onto themselves of sign*exp(lw).
+__device__ void root_trace(Ctx& c, int slot, int s0, double& lg, double& sg) {
+  const DModel& m = *c.m;
+  const double* lw = node_lw(c, 1, slot);
+  const uint16_t* tg = node_tg(c, 1, slot);
+  int off = m.sst_off[s0], n0 = m.sst_n[s0];
+  double mx = -DHUGE;
+  for (int i = c.lane; i < n0; i += 32) {
+    int st = off + i;
+    if ((tg[st] & 0x7fff) == st) mx = fmax(mx, lw[st]);
+  }
+  mx = wmax(mx);
+  if (mx == -DHUGE) {
+    lg = -DHUGE;
+    sg = 0.0;
+    return;
+  }
+  double sum = 0.0;
+  for (int i = c.lane; i < n0; i += 32) {
+    int st = off + i;
+    uint16_t t = tg[st];
+    if ((t & 0x7fff) == st) sum += ((t & 0x8000) ? -1.0 : 1.0) * exp(lw[st] - mx);
+  }
+  sum = wsum(sum);
+  lg = mx + log(fabs(sum));
+  sg = sum >= 0.0 ? 1.0 : -1.0;
+}
+
+// ---------------------------------------------------------------------------
+// Dense-block trace: time-ordered product of exp(-dtau (E-Egs)) and c/c+
+// blocks for the outer superstate s0, recomputed over the whole proposed
+// configuration (get_Trace_EB_fullmatrix, Trace.F90:5734-6100, evaluated as
+// a matrix over all outer states at once with one log scale).
+struct OpIter {
+  int j, K, stage;  // stage: number of inserted ops consumed
+};
+__device__ __forceinline__ bool next_op(const Ctx& c, const Mod& md, OpIter& it, double& t, int& code) {
+  while (true) {
+    while (md.type == 2 && it.j < it.K && (it.j == md.ix || it.j == md.iy)) it.j++;
+    bool haveOld = it.j < it.K;
+    double to = haveOld ? c.optau[it.j] : 0.0;
+    if (md.type == 1 && it.stage < 2) {
+      double tn = it.stage == 0 ? md.t1 : md.t2;
+      if (!haveOld || tn < to) {
+        t = tn;
+        code = it.stage == 0 ? md.c1 : md.c2;
+        it.stage++;
+        return true;
+      }
+    }
+    if (!haveOld) return false;
+    t = to;
+    code = c.opcode[it.j];
+    it.j++;
+    return true;
+  }
+}
+__device__ void dense_trace(Ctx& c, const Mod& md, int s0, double& lg, double& sg) {
+  const DModel& m = *c.m;
+  const int ld = m.nsmax;
+  double* X = c.dense;
+  double* Y = c.dense + (size_t)ld * ld;
+  int n0 = m.sst_n[s0];
+  for (int e = c.lane; e < n0 * n0; e += 32) {
+    int r = e % n0, col = e / n0;
+    X[(size_t)col * ld + r] = (r == col) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  int cur = s0, ncur = n0;
+  double t = 0.0, l = 0.0;
+  OpIter it{0, c.h->K, 0};
+  double tau;
+  int code;
+  bool zero = false;
+  while (next_op(c, md, it, tau, code)) {
+    int f = code >> 1, ca = code & 1;
+    int nxt = m.connect[((size_t)cur * m.nf + f) * 2 + ca];
+    if (nxt < 0) {
+      zero = true;
+      break;
+    }
+    double dt = tau - t;
+    const double* E = m.eval + m.sst_off[cur];
+    double e0 = E[0];
+    for (int e = c.lane; e < ncur * n0; e += 32) {
+      int r = e % ncur, col = e / ncur;
+      X[(size_t)col * ld + r] *= exp(-(E[r] - e0) * dt);
+    }
+    l += -(e0 - m.egs) * dt;
+    __syncwarp();
+    int nn = m.sst_n[nxt];
+    const double* B = m.blk + m.blk_off[((size_t)cur * m.nf + f) * 2 + ca];
+    double mx = 0.0;
+    for (int e = c.lane; e < nn * n0; e += 32) {
+      int i = e % nn, col = e / nn;
+      double acc = 0.0;
+      for (int r = 0; r < ncur; ++r) acc += B[(size_t)r * nn + i] * X[(size_t)col * ld + r];
+      Y[(size_t)col * ld + i] = acc;
+      mx = fmax(mx, fabs(acc));
+    }
+    mx = wmax(mx);
+    __syncwarp();
+    if (mx == 0.0) {
+      zero = true;
+      break;
+    }
+    double inv = 1.0 / mx;
+    for (int e = c.lane; e < nn * n0; e += 32) {
+      int i = e % nn, col = e / nn;
+      Y[(size_t)col * ld + i] *= inv;
+    }
+    l += log(mx);
+    __syncwarp();
+    double* T = X;
+    X = Y;
+    Y = T;
+    cur = nxt;
+    ncur = nn;
+    t = tau;
+  }
+  if (zero || cur != s0) {
+    lg = -DHUGE;
+    sg = 0.0;
+    return;
+  }
+  double dt = c.g->beta - t;
+  const double* E = m.eval + m.sst_off[cur];
+  double e0 = E[0];
+  l += -(e0 - m.egs) * dt;
+  double tr = 0.0;
+  for (int i = c.lane; i < n0; i += 32) tr += exp(-(E[i] - e0) * dt) * X[(size_t)i * ld + i];
+  tr = wsum(tr);
+  lg = l + log(fabs(tr));
+  sg = tr >= 0.0 ? 1.0 : -1.0;
+}
+
+// ---------------------------------------------------------------------------
+// Shifts of the sorted arrays
+
+// insert value/slot at position p of a sorted array with n entries
+__device__ void arr_insert(Ctx& c, double* a, short* sl, int n, int p, double v, short s) {
+  for (int base = n - 1; base >= p; base -= 32) {
+    int i = base - c.lane;
+    bool on = i >= p;
+    double x = 0;
+    short y = 0;
+    if (on) {
+      x = a[i];
+      y = sl[i];
+    }
+    __syncwarp();
+    if (on) {
+      a[i + 1] = x;
+      sl[i + 1] = y;
+    }
+    __syncwarp();
+  }
+  if (c.lane == 0) {
+    a[p] = v;
+    sl[p] = s;
+  }
+  __syncwarp();
+}
+__device__ void arr_remove(Ctx& c, double* a, short* sl, int n, int p) {
+  for (int base = p + 1; base < n; base += 32) {
+    int i = base + c.lane;
+    bool on = i < n;
+    double x = 0;
+    short y = 0;
+    if (on) {
+      x = a[i];
+      y = sl[i];
+    }
+    __syncwarp();
+    if (on) {
+      a[i - 1] = x;
+      sl[i - 1] = y;
+    }
+    __syncwarp();
+  }
+}
+// global operator array: insert t1 (before old index p1) and t2 (before old
+// index p2, p2 >= p1)
+__device__ void ops_insert2(Ctx& c, int p1, int p2, double t1, int c1, double t2, int c2) {
+  int K = c.h->K;
+  for (int base = K - 1; base >= p1; base -= 32) {
+    int i = base - c.lane;
+    bool on = i >= p1;
+    double x = 0;
+    int y = 0;
+    if (on) {
+      x = c.optau[i];
+      y = c.opcode[i];
+    }
+    __syncwarp();
+    if (on) {
+      int d = i + (i >= p2 ? 2 : 1);
+      c.optau[d] = x;
+      c.opcode[d] = y;
+    }
+    __syncwarp();
+  }
+  if (c.lane == 0) {
+    c.optau[p1] = t1;
+    c.opcode[p1] = c1;
+    c.optau[p2 + 1] = t2;
+    c.opcode[p2 + 1] = c2;
+  }
+  __syncwarp();
+}
+__device__ void ops_remove2(Ctx& c, int ix, int iy) {
+  int K = c.h->K;
+  for (int base = ix + 1; base < K; base += 32) {
+    int i = base + c.lane;
+    bool on = i < K && i != iy;
+    double x = 0;
+    int y = 0;
+    if (on) {
+      x = c.optau[i];
+      y = c.opcode[i];
+    }
+    __syncwarp();
+    if (on) {
+      int d = i - (i > iy ? 2 : 1);
+      c.optau[d] = x;
+      c.opcode[d] = y;
+    }
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Proposal log record
+__device__ void write_record(Ctx& c, const cthyb_record& r) {
+  if (c.log && c.lane == 0) {
+    Hdr& h = *c.h;
+    if (h.logn < c.g->logcap) c.log[h.logn] = r;
+    h.logn++;
+  }
+  __syncwarp();
+}
+
+// Trace of the proposed configuration for outer superstate s0.
+__device__ void proposed_trace(Ctx& c, const Mod& md, int s0, double& lg, double& sg) {
+  if (c.mono) {
+    tree_propose(c, md, true);
+    root_trace(c, 1 - c.act[1], s0, lg, sg);
+  } else {
+    dense_trace(c, md, s0, lg, sg);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// StepAdd, CTQMC.F90:3353-3613 (diagonal hybridisation).
+__device__ void step_add(Ctx& c, bool change_outer) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  if (c.lane == 0) h.try_add++;
+  __syncwarp();
+  cthyb_record r;
+  memset(&r, 0, sizeof(r));
+  r.move = 0;
+  r.change_outer = change_outer;
+  // pair_OperAdd, Trace.F90:3657-3702
+  double u1 = grnd(c);
+  int orb = randint(c, 1, m.nd);
+  int spin = randint(c, 1, 2);
+  double u2 = grnd(c);
+  double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  double tau_width = __dsub_rn(wmax, wmin);
+  double tau_a = __dadd_rn(wmin, __dmul_rn(tau_width, u1));
+  double tdf = __dmul_rn(1.0, tau_width);
+  double tau_min = fmax(__dsub_rn(tau_a, tdm), wmin);
+  double tau_w2 = __dsub_rn(fmin(__dadd_rn(tau_a, tdm), wmax), tau_min);
+  double tau_c = __dadd_rn(tau_min, __dmul_rn(tau_w2, u2));
+  tdf = __dmul_rn(tdf, tau_w2);
+  const int f = 2 * (orb - 1) + (spin - 1);
+  const int k = h.k[f];
+  const int K = h.K;
+  r.orb = orb;
+  r.spin = spin;
+  r.tau_c = tau_c;
+  r.tau_a = tau_a;
+  r.outer_sst = h.outer_sst;
+  r.k_total = K;
+  // process_OperAdd: equal times are rejected (Trace.F90:4292-4407)
+  int pa = wlb(c.optau, K, tau_a, c.lane);
+  int pc = wlb(c.optau, K, tau_c, c.lane);
+  bool eq = (tau_a == tau_c) || (pa < K && c.optau[pa] == tau_a) || (pc < K && c.optau[pc] == tau_c);
+  if (eq) {
+    if (c.lane == 0) h.qn_add++;
+    r.outcome = 0;
+    write_record(c, r);
+    return;
+  }
+  const double* sc = srt_ptr(c, f, 0);
+  const double* sa = srt_ptr(c, f, 1);
+  int fpos_c = wlb(sc, k, tau_c, c.lane) + 1;
+  int fpos_a = wlb(sa, k, tau_a, c.lane) + 1;
+  r.fpos_c = fpos_c;
+  r.fpos_a = fpos_a;
+  Mod md;
+  md.type = 1;
+  bool a_first = tau_a < tau_c;
+  md.t1 = a_first ? tau_a : tau_c;
+  md.c1 = a_first ? 2 * f + 1 : 2 * f;
+  md.t2 = a_first ? tau_c : tau_a;
+  md.c2 = a_first ? 2 * f : 2 * f + 1;
+  md.ix = md.iy = -1;
+  md.b1 = bin_of(c, md.t1);
+  md.b2 = bin_of(c, md.t2);
+  int p1 = a_first ? pa : pc, p2 = a_first ? pc : pa;
+  // quantum-number check (CTQMC.F90:3421-3470)
+  tree_propose(c, md, false);
+  int root_new = 1 - c.act[1];
+  int s0 = h.outer_sst, snew = s0;
+  bool ok;
+  if (!change_outer) {
+    ok = node_ss(c, 1, root_new)[s0] == s0;
+  } else {
+    int inside = old_prefix(c, s0, md.t2);
+    snew = inside >= 0 ? new_suffix(c, md, inside, md.t2) : -1;
+    ok = snew >= 0 && node_ss(c, 1, root_new)[snew] == snew;
+  }
+  if (!ok) {
+    if (c.lane == 0) h.qn_add++;
+    r.outcome = 1;
+    write_record(c, r);
+    return;
+  }
+  // determinant ratio (get_LogDetRatPairAdd / get_DetRatAdd)
+  double* Q = c.scr;
+  double* R = c.scr + c.kcap;
+  double* v = c.scr + 2 * c.kcap;
+  double* w = c.scr + 3 * c.kcap;
+  const double* tcs = stau_ptr(c, f, 0);
+  const double* tas = stau_ptr(c, f, 1);
+  for (int i = c.lane; i < k; i += 32) {
+    Q[i] = hybrf(c, __dsub_rn(tas[i], tau_c), f);
+    R[i] = hybrf(c, __dsub_rn(tau_a, tcs[i]), f);
+  }
+  double S = hybrf(c, __dsub_rn(tau_a, tau_c), f);
+  __syncwarp();
+  const double* Mf = M_ptr(c, f);
+  double part = 0.0;
+  for (int i = c.lane; i < k; i += 32) {
+    double acc = 0.0;
+    for (int j = 0; j < k; ++j) acc = fma(Mf[(size_t)j * c.kcap + i], Q[j], acc);
+    v[i] = acc;
+    part = fma(R[i], acc, part);
+  }
+  double ratio = S - wsum(part);
+  __syncwarp();
+  double sig = ((fpos_c - fpos_a) & 1) ? -1.0 : 1.0;
+  double det_log = log(fabs(ratio));
+  double det_sign = (ratio >= 0.0 ? 1.0 : -1.0) * sig;
+  if (c.lane == 0) {
+    h.w_mbytes += 8ll * k * k + 32ll * k;
+    h.w_mflops += 2ll * k * k + 2ll * k;
+  }
+  // trace
+  double tr_lg, tr_sg;
+  proposed_trace(c, md, snew, tr_lg, tr_sg);
+  double rnd = grnd(c);
+  // NPairs of the proposed configuration
+  int np;
+  if (h.npairs == -1) {
+    // full recount including the new pair
+    int tot = 0;
+    int start = wlb(c.optau, K, wmin, c.lane);
+    for (int i = start + c.lane; i < K; i += 32) {
+      double t = c.optau[i];
+      if (t > wmax) continue;
+      int cd = c.opcode[i], ff = cd >> 1, cc = cd & 1;
+      const double* opp = srt_ptr(c, ff, 1 - cc);
+      int n = cnt_later(opp, h.k[ff], t, wmax, tdm);
+      if (ff == f) {
+        // partner among the new operators
+        double tn = cc == 0 ? tau_a : tau_c;
+        if (tn > t && tn <= fmin(wmax, __dadd_rn(t, tdm))) n++;
+      }
+      tot += n;
+    }
+    tot = wsumi(tot);
+    // pairs with a new operator as the earlier member
+    double tearly = md.t1;
+    int cde = md.c1 & 1;
+    if (tearly >= wmin && tearly <= wmax) {
+      const double* opp = srt_ptr(c, f, 1 - cde);
+      int n = 0;
+      if (c.lane == 0) n = cnt_later(opp, k, tearly, wmax, tdm);
+      tot += __shfl_sync(FULL, n, 0);
+      double tl = md.t2;
+      if (tl <= fmin(wmax, __dadd_rn(tearly, tdm))) tot += 1;
+    }
+    {
+      double tlate = md.t2;
+      int cdl = md.c2 & 1;
+      if (tlate >= wmin && tlate <= wmax) {
+        const double* opp = srt_ptr(c, f, 1 - cdl);
+        int n = 0;
+        if (c.lane == 0) n = cnt_later(opp, k, tlate, wmax, tdm);
+        tot += __shfl_sync(FULL, n, 0);
+      }
+    }
+    np = tot;
+  } else {
+    // update_NPairs(+1): partners of both new operators
+    int n = 0;
+    if (c.lane == 0) {
+      const double* opp1 = srt_ptr(c, f, 1 - (md.c1 & 1));
+      const double* opp2 = srt_ptr(c, f, 1 - (md.c2 & 1));
+      n += cnt_later(opp1, k, md.t1, wmax, tdm) + cnt_earlier(opp1, k, md.t1, wmin, tdm);
+      if (md.t2 <= wmax && md.t2 <= __dadd_rn(md.t1, tdm)) n += 1;
+      n += cnt_later(opp2, k, md.t2, wmax, tdm) + cnt_earlier(opp2, k, md.t2, wmin, tdm);
+    }
+    np = h.npairs + __shfl_sync(FULL, n, 0);
+  }
+  double trr_log = tr_lg - h.trace_log;
+  double wr = exp(__dadd_rn(trr_log, det_log));
+  double x = __dmul_rn(1.0, tdf);
+  x = __dmul_rn(x, (double)(2 * m.nd));
+  x = __ddiv_rn(x, (double)np);
+  x = __dmul_rn(x, wr);
+  double prob = fabs(x);
+  r.det_log = det_log;
+  r.det_sign = det_sign;
+  r.tr_log = tr_lg;
+  r.tr_sign = tr_sg;
+  r.prob = prob;
+  r.rand = rnd;
+  r.npairs = np;
+  bool accept = rnd < prob;
+  if (accept) {
+    if (k + 1 > c.kcap || K + 2 > c.g->opcap) {
+      set_status(c, ST_CAPACITY);
+      return;
+    }
+    // get_MatAdd in slot order: w = R^T M, rank-one update, new row/column
+    double* Mw = M_ptr(c, f);
+    for (int j = c.lane; j < k; j += 32) {
+      double acc = 0.0;
+      const double* col = Mw + (size_t)j * c.kcap;
+      for (int i = 0; i < k; ++i) acc = fma(R[i], col[i], acc);
+      w[j] = acc;
+    }
+    __syncwarp();
+    double invS = 1.0 / ratio;
+    for (int i = c.lane; i < k; i += 32) {
+      double vi = v[i] * invS;
+      for (int j = 0; j < k; ++j) Mw[(size_t)j * c.kcap + i] = fma(vi, w[j], Mw[(size_t)j * c.kcap + i]);
+      Mw[(size_t)k * c.kcap + i] = -vi;
+    }
+    for (int j = c.lane; j < k; j += 32) Mw[(size_t)j * c.kcap + k] = -w[j] * invS;
+    if (c.lane == 0) {
+      Mw[(size_t)k * c.kcap + k] = invS;
+      h.w_mbytes += 16ll * k * k + 16ll * k;
+      h.w_mflops += 4ll * k * k;
+    }
+    __syncwarp();
+    // slots and sorted arrays
+    if (c.lane == 0) {
+      stau_ptr(c, f, 0)[k] = tau_c;
+      stau_ptr(c, f, 1)[k] = tau_a;
+    }
+    __syncwarp();
+    arr_insert(c, srt_ptr(c, f, 0), sslot_ptr(c, f, 0), k, fpos_c - 1, tau_c, (short)k);
+    arr_insert(c, srt_ptr(c, f, 1), sslot_ptr(c, f, 1), k, fpos_a - 1, tau_a, (short)k);
+    ops_insert2(c, p1, p2, md.t1, md.c1, md.t2, md.c2);
+    if (c.mono) tree_accept(c, md);
+    else {
+      tree_accept(c, md);
+    }
+    if (c.lane == 0) {
+      h.k[f] = k + 1;
+      h.K = K + 2;
+      h.det_log = det_log + h.det_log;
+      h.det_sign = det_sign * h.det_sign;
+      h.trace_log = tr_lg;
+      h.trace_sign = tr_sg;
+      h.npairs = np;
+      h.outer_sst = snew;
+      h.acc_add++;
+      h.w_opbytes += 24ll * (K - p1) + 40ll * k;
+    }
+    __syncwarp();
+    double sgn = config_sign(c);
+    if (c.lane == 0) h.cfgsign = -sgn;
+    __syncwarp();
+    r.outcome = 4;
+  } else {
+    r.outcome = 3;
+  }
+  r.outer_sst = h.outer_sst;
+  r.k_total = h.K;
+  write_record(c, r);
+}
+
+// ---------------------------------------------------------------------------
+// StepRem, CTQMC.F90:3892-4151 (diagonal hybridisation).
+__device__ void step_rem(Ctx& c, bool change_outer) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  if (c.lane == 0) h.try_rem++;
+  __syncwarp();
+  cthyb_record r;
+  memset(&r, 0, sizeof(r));
+  r.move = 1;
+  r.change_outer = change_outer;
+  r.outer_sst = h.outer_sst;
+  r.k_total = h.K;
+  // gen_OperRemove, Trace.F90:4851-4960
+  if (h.npairs == -1) {
+    int np = count_npairs(c);
+    if (c.lane == 0) h.npairs = np;
+    __syncwarp();
+  }
+  if (h.npairs <= 0) {
+    if (c.lane == 0) h.qn_rem++;
+    r.outcome = 2;
+    write_record(c, r);
+    return;
+  }
+  const int K = h.K;
+  const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  int target = randint(c, 1, h.npairs);
+  int start = wlb(c.optau, K, wmin, c.lane);
+  int ix = -1, yrank = -1;
+  for (int base = start; base < K; base += 32) {
+    int i = base + c.lane;
+    int cnt = 0, cd = 0, ff = 0, cc = 0, lb = 0;
+    double t = 0;
+    if (i < K) {
+      t = c.optau[i];
+      cd = c.opcode[i];
+      ff = cd >> 1;
+      cc = cd & 1;
+      const double* opp = srt_ptr(c, ff, 1 - cc);
+      double hi = fmin(wmax, __dadd_rn(t, tdm));
+      lb = sub(opp, h.k[ff], t);
+      int ub = sub(opp, h.k[ff], hi);
+      cnt = ub > lb ? ub - lb : 0;
+    }
+    int cum = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(FULL, cum, o);
+      if (c.lane >= o) cum += y;
+    }
+    int total = __shfl_sync(FULL, cum, 31);
+    if (target <= total) {
+      unsigned bal = __ballot_sync(FULL, cum >= target);
+      int L0 = __ffs(bal) - 1;
+      int before = __shfl_sync(FULL, cum - cnt, L0);
+      ix = base + L0;
+      yrank = __shfl_sync(FULL, lb, L0) + (target - before) - 1;
+      break;
+    }
+    target -= total;
+  }
+  if (ix < 0) {
+    set_status(c, ST_INTERNAL);
+    return;
+  }
+  const double tx = c.optau[ix];
+  const int cx = c.opcode[ix], f = cx >> 1, cax = cx & 1;
+  const int k = h.k[f];
+  if (yrank < 0 || yrank >= k) {
+    set_status(c, ST_INTERNAL);
+    return;
+  }
+  const double ty = srt_ptr(c, f, 1 - cax)[yrank];
+  const int iy = wlb(c.optau, K, ty, c.lane);
+  const int xrank = wlb(srt_ptr(c, f, cax), k, tx, c.lane);
+  if (iy <= ix || iy >= K || c.optau[iy] != ty || xrank >= k || srt_ptr(c, f, cax)[xrank] != tx) {
+    set_status(c, ST_INTERNAL);
+    return;
+  }
+  const double tau_c = cax == 0 ? tx : ty, tau_a = cax == 0 ? ty : tx;
+  const int rank_c = cax == 0 ? xrank : yrank, rank_a = cax == 0 ? yrank : xrank;
+  const int fpos_c = rank_c + 1, fpos_a = rank_a + 1;
+  const int slot_c = sslot_ptr(c, f, 0)[rank_c], slot_a = sslot_ptr(c, f, 1)[rank_a];
+  double hprf = __ddiv_rn((double)h.npairs,
+                          __dmul_rn(__dsub_rn(wmax, wmin),
+                                    __dsub_rn(fmin(__dadd_rn(tau_a, tdm), wmax), fmax(__dsub_rn(tau_a, tdm), wmin))));
+  r.orb = f / 2 + 1;
+  r.spin = f % 2 + 1;
+  r.tau_c = tau_c;
+  r.tau_a = tau_a;
+  r.fpos_c = fpos_c;
+  r.fpos_a = fpos_a;
+  r.npairs = h.npairs;
+  Mod md;
+  md.type = 2;
+  md.ix = ix;
+  md.iy = iy;
+  md.t1 = tx;
+  md.t2 = ty;
+  md.c1 = md.c2 = 0;
+  md.b1 = bin_of(c, tx);
+  md.b2 = bin_of(c, ty);
+  tree_propose(c, md, false);
+  int root_new = 1 - c.act[1];
+  int s0 = h.outer_sst, snew = s0;
+  bool ok;
+  if (!change_outer) {
+    ok = node_ss(c, 1, root_new)[s0] == s0;
+  } else {
+    int inside = old_prefix(c, s0, ty);
+    snew = inside >= 0 ? new_suffix(c, md, inside, ty) : -1;
+    ok = snew >= 0 && node_ss(c, 1, root_new)[snew] == snew;
+  }
+  if (!ok) {
+    if (c.lane == 0) h.qn_rem++;
+    r.outcome = 1;
+    write_record(c, r);
+    return;
+  }
+  const double* Mf = M_ptr(c, f);
+  double dr = Mf[(size_t)slot_a * c.kcap + slot_c];
+  double sig = ((fpos_c - fpos_a) & 1) ? -1.0 : 1.0;
+  double det_log = log(fabs(dr));
+  double det_sign = (dr >= 0.0 ? 1.0 : -1.0) * sig;
+  double tr_lg, tr_sg;
+  proposed_trace(c, md, snew, tr_lg, tr_sg);
+  double trr_log = tr_lg - h.trace_log;
+  double wr = exp(__dadd_rn(trr_log, det_log));
+  double x = __dmul_rn(1.0, hprf);
+  x = __ddiv_rn(x, (double)(2 * m.nd));
+  x = __dmul_rn(x, wr);
+  double prob = fabs(x);
+  double rnd = grnd(c);
+  r.det_log = det_log;
+  r.det_sign = det_sign;
+  r.tr_log = tr_lg;
+  r.tr_sign = tr_sg;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    if (fabs(dr * sig) < 1e-12) {  // CTQMC.F90:4062
+      set_status(c, ST_NUMERIC);
+      return;
+    }
+    // get_MatRem in slot order, then move the last row/column into the gap
+    double* Mw = M_ptr(c, f);
+    double* col = c.scr;             // column slot_a
+    double* row = c.scr + c.kcap;    // row slot_c
+    for (int i = c.lane; i < k; i += 32) {
+      col[i] = Mw[(size_t)slot_a * c.kcap + i];
+      row[i] = Mw[(size_t)i * c.kcap + slot_c];
+    }
+    __syncwarp();
+    double inv = 1.0 / dr;
+    for (int i = c.lane; i < k; i += 32) {
+      double ci = col[i] * inv;
+      for (int j = 0; j < k; ++j) Mw[(size_t)j * c.kcap + i] = fma(-ci, row[j], Mw[(size_t)j * c.kcap + i]);
+    }
+    __syncwarp();
+    const int last = k - 1;
+    if (slot_c != last) {
+      for (int j = c.lane; j < k; j += 32) Mw[(size_t)j * c.kcap + slot_c] = Mw[(size_t)j * c.kcap + last];
+    }
+    __syncwarp();
+    if (slot_a != last) {
+      for (int i = c.lane; i < k; i += 32) Mw[(size_t)slot_a * c.kcap + i] = Mw[(size_t)last * c.kcap + i];
+    }
+    __syncwarp();
+    if (c.lane == 0) {
+      h.w_mbytes += 16ll * k * k;
+      h.w_mflops += 2ll * k * k;
+    }
+    // slot bookkeeping: slot `last` moves into the freed slots
+    arr_remove(c, srt_ptr(c, f, 0), sslot_ptr(c, f, 0), k, rank_c);
+    arr_remove(c, srt_ptr(c, f, 1), sslot_ptr(c, f, 1), k, rank_a);
+    if (slot_c != last) {
+      short* ss = sslot_ptr(c, f, 0);
+      for (int i = c.lane; i < k - 1; i += 32)
+        if (ss[i] == last) ss[i] = (short)slot_c;
+      if (c.lane == 0) stau_ptr(c, f, 0)[slot_c] = stau_ptr(c, f, 0)[last];
+    }
+    if (slot_a != last) {
+      short* ss = sslot_ptr(c, f, 1);
+      for (int i = c.lane; i < k - 1; i += 32)
+        if (ss[i] == last) ss[i] = (short)slot_a;
+      if (c.lane == 0) stau_ptr(c, f, 1)[slot_a] = stau_ptr(c, f, 1)[last];
+    }
+    __syncwarp();
+    ops_remove2(c, ix, iy);
+    tree_accept(c, md);
+    if (c.lane == 0) {
+      h.k[f] = k - 1;
+      h.K = K - 2;
+      h.det_log = det_log + h.det_log;
+      h.det_sign = det_sign * h.det_sign;
+      h.trace_log = tr_lg;
+      h.trace_sign = tr_sg;
+      h.outer_sst = snew;
+      h.acc_rem++;
+      h.w_opbytes += 24ll * (K - ix) + 40ll * k;
+    }
+    __syncwarp();
+    // update_NPairs(-1): the pair and the partners of its members
+    int n = 0;
+    if (c.lane == 0) {
+      const double* oppx = srt_ptr(c, f, 1 - cax);
+      const double* oppy = srt_ptr(c, f, cax);
+      n = 1 + cnt_later(oppx, k - 1, tx, wmax, tdm) + cnt_earlier(oppx, k - 1, tx, wmin, tdm) +
+          cnt_later(oppy, k - 1, ty, wmax, tdm) + cnt_earlier(oppy, k - 1, ty, wmin, tdm);
+      h.npairs -= n;
+    }
+    __syncwarp();
+    double sgn = config_sign(c);
+    if (c.lane == 0) h.cfgsign = -sgn;
+    __syncwarp();
+    r.outcome = 4;
+  } else {
+    r.outcome = 3;
+  }
+  r.outer_sst = h.outer_sst;
+  r.k_total = h.K;
+  write_record(c, r);
+}
+
+// One proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250),
+// percentages of global, tau-shift and 4-operator moves zero.
+__device__ void one_step(Ctx& c) {
+  Hdr& h = *c.h;
+  for (int f = 0; f < c.m->nf; ++f)
+    if (h.k[f] + 1 > c.kcap) {
+      set_status(c, ST_CAPACITY);
+      return;
+    }
+  if (h.K + 2 > c.g->opcap) {
+    set_status(c, ST_CAPACITY);
+    return;
+  }
+  double rn = grnd(c);
+  if (rn < 0.5) {
+    grnd(c);  // Percentage4OperatorMove draw
+    bool co = grnd(c) < c.g->p_outer;
+    step_add(c, co);
+  } else {
+    grnd(c);
+    bool co = grnd(c) < c.g->p_outer;
+    step_rem(c, co);
+  }
+  if (c.lane == 0) h.nprop++;
+  __syncwarp();
+  if (h.nprop % h.nslide == 0) shift_window(c);
+}
+
+// ---------------------------------------------------------------------------
+// Measurements after each NCorr block (CTQMC.F90:8541-8566)
+__device__ void measure(Ctx& c) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  const DGroup& g = *c.g;
+  if (c.lane == 0) {
+    h.cnt_meas++;
+    h.meas_sign += h.cfgsign;  // MeasSign
+  }
+  // MeasExpOrder
+  for (int f = c.lane; f < m.nf; f += 32) {
+    int k = h.k[f];
+    int hm = g.maxhisto;
+    c.histo[(size_t)f * hm + (k < hm - 1 ? k : hm - 1)] += 1.0;
+  }
+  __syncwarp();
+  // MeasDensityMatrix_beta_half from the two children of the root
+  if (g.meas_dm && c.mono) {
+    int s0 = h.outer_sst;
+    int off = m.sst_off[s0], n0 = m.sst_n[s0];
+    const double* lwl = node_lw(c, 2, c.act[2]);
+    const uint16_t* tgl = node_tg(c, 2, c.act[2]);
+    const double* lwr = node_lw(c, 3, c.act[3]);
+    const uint16_t* tgr = node_tg(c, 3, c.act[3]);
+    for (int i = c.lane; i < n0; i += 32) {
+      int st = off + i;
+      uint16_t a = tgl[st];
+      int mid = a & 0x7fff;
+      if (mid == 0x7fff) continue;
+      uint16_t b = tgr[mid];
+      if ((b & 0x7fff) != st) continue;
+      double sgn = ((a ^ b) & 0x8000) ? -1.0 : 1.0;
+      double val = sgn * exp(lwl[st] + lwr[mid] - h.trace_log) * h.trace_sign * (-h.cfgsign);
+      c.dm[mid] += val;
+    }
+    __syncwarp();
+  }
+  // MeasGtauRem(.false.): M elements binned by tau_a - tau_c
+  const int nt = g.ntau;
+  for (int f = 0; f < m.nf; ++f) {
+    int k = h.k[f];
+    const double* Mf = M_ptr(c, f);
+    const double* tcs = stau_ptr(c, f, 0);
+    const double* tas = stau_ptr(c, f, 1);
+    double* G = c.gtau + (size_t)f * nt;
+    for (int i = c.lane; i < k; i += 32) {
+      double tc = tcs[i];
+      for (int j = 0; j < k; ++j) {
+        double Mv = Mf[(size_t)j * c.kcap + i];
+        double ta = tas[j];
+        int idt;
+        if (ta - tc > 0.0) {
+          idt = (int)((ta - tc) / g.beta * (double)nt) + 1;
+        } else {
+          idt = (int)((g.beta + ta - tc) / g.beta * (double)nt) + 1;
+          Mv = -Mv;
+        }
+        Mv = Mv * h.cfgsign;
+        if (idt > nt) idt = nt;
+        atomicAdd(&G[idt - 1], Mv);
+      }
+    }
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+__device__ Ctx make_ctx(const DModel* m, const DGroup* g, Hdr* hsm, int chain) {
+  Ctx c;
+  c.m = m;
+  c.g = g;
+  c.h = hsm;
+  c.lane = threadIdx.x & 31;
+  c.chain = chain;
+  char* b = g->base + (size_t)chain * g->stride;
+  c.mt = (uint32_t*)(b + g->o_mt);
+  c.optau = (double*)(b + g->o_optau);
+  c.opcode = (int*)(b + g->o_opcode);
+  c.srt_tau = (double*)(b + g->o_srt_tau);
+  c.srt_slot = (short*)(b + g->o_srt_slot);
+  c.slot_tau = (double*)(b + g->o_slot_tau);
+  c.M = (double*)(b + g->o_M);
+  c.tree = b + g->o_tree;
+  c.act = (unsigned char*)(b + g->o_act);
+  c.scr = (double*)(b + g->o_scr);
+  c.btau = c.scr + 4 * g->kcap;
+  c.bcode = (int*)(c.btau + g->opcap + 2);
+  c.gtau = (double*)(b + g->o_gtau);
+  c.histo = (double*)(b + g->o_histo);
+  c.dm = (double*)(b + g->o_dm);
+  c.dense = (double*)(b + g->o_dense);
+  c.log = g->logcap > 0 ? (cthyb_record*)(b + g->o_log) : nullptr;
+  c.kcap = g->kcap;
+  c.mono = m->monomial && !g->dense;
+  return c;
+}
+
+constexpr int WPB = 4;  // warps (chains) per block
+
+__device__ __forceinline__ void load_hdr(Hdr* dst, const Hdr* src, int lane) {
+  const int n = sizeof(Hdr) / 4;
+  for (int i = lane; i < n; i += 32) ((int*)dst)[i] = ((const int*)src)[i];
+  __syncwarp();
+}
+__device__ __forceinline__ void store_hdr(Hdr* dst, const Hdr* src, int lane) {
+  __syncwarp();
+  const int n = sizeof(Hdr) / 4;
+  for (int i = lane; i < n; i += 32) ((int*)dst)[i] = ((const int*)src)[i];
+  __syncwarp();
+}
+
+// init_Trace (Trace.F90:340-701) for every chain of a group.
+__global__ void __launch_bounds__(WPB * 32) k_init(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
+                                                  const int* seeds, const double* tdm, int ncorr) {
+  __shared__ Hdr hs[WPB];
+  int warp = threadIdx.x >> 5;
+  int chain = blockIdx.x * WPB + warp;
+  if (chain >= g.nchains) return;
+  Ctx c = make_ctx(&m, &g, &hs[warp], chain);
+  Hdr& h = *c.h;
+  if (c.lane == 0) {
+    memset(&h, 0, sizeof(Hdr));
+    h.det_log = 0.0;
+    h.det_sign = 1.0;
+    h.cfgsign = -1.0;
+    h.trace_sign = 1.0;
+  }
+  __syncwarp();
+  mt_seed(c.mt, (uint32_t)seeds[chain], c.lane);
+  c.mti = 624;
+  init_window(c, *tdm);
+  if (c.lane == 0) {
+    h.npairs = 0;
+    int nsl = (int)floor((double)ncorr / (double)h.num_windows);
+    h.nslide = nsl > 2 * m.nd ? nsl : 2 * m.nd;
+  }
+  __syncwarp();
+  // outer superstate in proportion to the empty trace
+  double rnd = grnd(c);
+  if (c.lane == 0) {
+    double acc = 0.0;
+    for (int s = 0; s < m.nss; ++s) {
+      h.outer_sst = s;
+      acc += g.empty_w[s];
+      if (acc >= rnd && g.empty_w[s] != 0.0) break;
+    }
+  }
+  __syncwarp();
+  // empty configuration
+  if (c.lane == 0) h.K = 0;
+  __syncwarp();
+  tree_build_all(c);
+  double lg, sg;
+  if (c.mono) root_trace(c, 0, h.outer_sst, lg, sg);
+  else {
+    Mod md;
+    md.type = 0;
+    dense_trace(c, md, h.outer_sst, lg, sg);
+  }
+  if (c.lane == 0) {
+    h.trace_log = lg;
+    h.trace_sign = sg;
+    h.mt_idx = c.mti;
+  }
+  store_hdr((Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr), &h, c.lane);
+}
+
+__global__ void __launch_bounds__(WPB * 32) k_sweep(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
+                                                   long long nprop, int nmeas, int reset) {
+  __shared__ Hdr hs[WPB];
+  int warp = threadIdx.x >> 5;
+  int chain = blockIdx.x * WPB + warp;
+  if (chain >= g.nchains) return;
+  Ctx c = make_ctx(&m, &g, &hs[warp], chain);
+  Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
+  load_hdr(c.h, gh, c.lane);
+  Hdr& h = *c.h;
+  c.mti = h.mt_idx;
+  if (reset && c.lane == 0) {  // init_counters, CTQMC.F90:847-899
+    h.try_add = h.acc_add = h.try_rem = h.acc_rem = h.qn_add = h.qn_rem = 0;
+    h.nprop = 0;
+  }
+  __syncwarp();
+  if (h.status == ST_OK) {
+    if (nmeas <= 0) {
+      for (long long i = 0; i < nprop && h.status == ST_OK; ++i) one_step(c);
+    } else {
+      for (int im = 0; im < nmeas && h.status == ST_OK; ++im) {
+        for (int ic = 0; ic < g.ncorr && h.status == ST_OK; ++ic) one_step(c);
+        if (h.status == ST_OK) measure(c);
+      }
+    }
+  }
+  if (c.lane == 0) {
+    h.mt_idx = c.mti;
+    if (h.status != ST_OK) atomicMax(g.err_flag, h.status);
+  }
+  store_hdr(gh, c.h, c.lane);
+}
+
+// set_mc_config: operator arrays from a time-ordered list already written
+// into optau/opcode by the host (K in the header); rebuilds the sorted
+// arrays, the tree, the trace, and the inverse hybridisation matrices by
+// Gauss-Jordan elimination with partial pivoting (get_InvFullHybr,
+// Trace.F90:2279-2336), in rank order (slot = rank).
+__device__ void rebuild_minv(Ctx& c, double* maxdev, bool replace, double& dlog, double& dsign) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  dlog = 0.0;
+  dsign = 1.0;
+  double* A = c.dense;  // needs kcap*kcap*2 doubles of scratch
+  for (int f = 0; f < m.nf; ++f) {
+    int k = h.k[f];
+    if (k == 0) continue;
+    const int ld = c.kcap;
+    double* H = A;
+    double* I = A + (size_t)ld * ld;
+    // H(a_rank, c_rank) = Delta(tau_a - tau_c), inverse as M(c_rank, a_rank)
+    const double* sc = srt_ptr(c, f, 0);
+    const double* sa = srt_ptr(c, f, 1);
+    for (int e = c.lane; e < k * k; e += 32) {
+      int ia = e % k, ic = e / k;
+      H[(size_t)ic * ld + ia] = hybrf(c, __dsub_rn(sa[ia], sc[ic]), f);
+      I[(size_t)ic * ld + ia] = (ia == ic) ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    bool sing = false;
+    for (int j = 0; j < k; ++j) {
+      // pivot: first maximal |H(i,j)|, i >= j
+      double best = -1.0;
+      int bi = j;
+      for (int i = j + c.lane; i < k; i += 32) {
+        double a = fabs(H[(size_t)j * ld + i]);
+        if (a > best) {
+          best = a;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) {
+        double ob = __shfl_xor_sync(FULL, best, o);
+        int oi = __shfl_xor_sync(FULL, bi, o);
+        if (ob > best || (ob == best && oi < bi)) {
+          best = ob;
+          bi = oi;
+        }
+      }
+      if (best <= 0.0) {
+        sing = true;
+        break;
+      }
+      if (bi != j) {
+        for (int col = c.lane; col < k; col += 32) {
+          double t = H[(size_t)col * ld + j];
+          H[(size_t)col * ld + j] = H[(size_t)col * ld + bi];
+          H[(size_t)col * ld + bi] = t;
+          t = I[(size_t)col * ld + j];
+          I[(size_t)col * ld + j] = I[(size_t)col * ld + bi];
+          I[(size_t)col * ld + bi] = t;
+        }
+        dsign = -dsign;
+      }
+      __syncwarp();
+      double piv = H[(size_t)j * ld + j];
+      dlog += log(fabs(piv));
+      if (piv < 0) dsign = -dsign;
+      double ip = 1.0 / piv;
+      for (int col = c.lane; col < k; col += 32) {
+        H[(size_t)col * ld + j] *= ip;
+        I[(size_t)col * ld + j] *= ip;
+      }
+      __syncwarp();
+      for (int col = 0; col < k; ++col) {
+        double hj = H[(size_t)col * ld + j];
+        double ij = I[(size_t)col * ld + j];
+        for (int i = c.lane; i < k; i += 32) {
+          if (i == j) continue;
+          double fct = H[(size_t)j * ld + i];
+          if (col == j) continue;
+          H[(size_t)col * ld + i] -= fct * hj;
+          I[(size_t)col * ld + i] -= fct * ij;
+        }
+      }
+      __syncwarp();
+      for (int i = c.lane; i < k; i += 32)
+        if (i != j) {
+          I[(size_t)j * ld + i] -= H[(size_t)j * ld + i] * I[(size_t)j * ld + j];
+          H[(size_t)j * ld + i] = 0.0;
+        }
+      __syncwarp();
+    }
+    if (sing) {
+      dlog = -DHUGE;
+      dsign = 0.0;
+      continue;
+    }
+    // I = H^{-1}: rows are c ranks, columns a ranks.  Compare / install in
+    // slot order: M[slot_a][slot_c] = Inv(rank_c, rank_a)
+    const short* slc = sslot_ptr(c, f, 0);
+    const short* sla = sslot_ptr(c, f, 1);
+    double* Mf = M_ptr(c, f);
+    double dev = 0.0;
+    for (int e = c.lane; e < k * k; e += 32) {
+      int rc = e % k, ra = e / k;
+      double val = I[(size_t)ra * ld + rc];
+      size_t idx = (size_t)sla[ra] * ld + slc[rc];
+      dev = fmax(dev, fabs(Mf[idx] - val));
+      if (replace) Mf[idx] = val;
+    }
+    dev = wmax(dev);
+    if (maxdev && c.lane == 0) *maxdev = fmax(*maxdev, dev);
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(WPB * 32) k_set_config(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
+                                                        int chain, int outer_sst) {
+  __shared__ Hdr hs[WPB];
+  int warp = threadIdx.x >> 5;
+  if (warp != 0) return;
+  Ctx c = make_ctx(&m, &g, &hs[0], chain);
+  Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
+  load_hdr(c.h, gh, c.lane);
+  Hdr& h = *c.h;
+  c.mti = h.mt_idx;
+  const int K = h.K;
+  // per-flavour sorted arrays, slot = rank
+  for (int f = 0; f < m.nf; ++f) {
+    for (int ca = 0; ca < 2; ++ca) {
+      double* st = srt_ptr(c, f, ca);
+      short* ss = sslot_ptr(c, f, ca);
+      double* tt = stau_ptr(c, f, ca);
+      int n = 0;
+      for (int base = 0; base < K; base += 32) {
+        int i = base + c.lane;
+        bool is = i < K && c.opcode[i] == 2 * f + ca;
+        unsigned bal = __ballot_sync(FULL, is);
+        int pos = n + __popc(bal & ((1u << c.lane) - 1u));
+        if (is && pos < c.kcap) {
+          st[pos] = c.optau[i];
+          ss[pos] = (short)pos;
+          tt[pos] = c.optau[i];
+        }
+        n += __popc(bal);
+      }
+      if (ca == 0 && c.lane == 0) h.k[f] = n;
+    }
+  }
+  __syncwarp();
+  if (c.lane == 0) h.outer_sst = outer_sst;
+  __syncwarp();
+  tree_build_all(c);
+  double lg, sg;
+  if (c.mono) root_trace(c, 0, h.outer_sst, lg, sg);
+  else {
+    Mod md;
+    md.type = 0;
+    dense_trace(c, md, h.outer_sst, lg, sg);
+  }
+  double dlog, dsign;
+  rebuild_minv(c, nullptr, true, dlog, dsign);
+  if (c.lane == 0) {
+    h.trace_log = lg;
+    h.trace_sign = sg;
+    h.det_log = dlog;
+    h.det_sign = dsign;
+    h.npairs = -1;
+  }
+  __syncwarp();
+  double sgn = config_sign(c);
+  if (c.lane == 0) h.cfgsign = -sgn;
+  store_hdr(gh, c.h, c.lane);
+}
+
+__global__ void __launch_bounds__(WPB * 32) k_refresh(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
+                                                     int replace, double* maxdev) {
+  __shared__ Hdr hs[WPB];
+  int warp = threadIdx.x >> 5;
+  int chain = blockIdx.x * WPB + warp;
+  if (chain >= g.nchains) return;
+  Ctx c = make_ctx(&m, &g, &hs[warp], chain);
+  Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
+  load_hdr(c.h, gh, c.lane);
+  double dlog, dsign;
+  __shared__ double dev[WPB];
+  if (c.lane == 0) dev[warp] = 0.0;
+  __syncwarp();
+  rebuild_minv(c, &dev[warp], replace != 0, dlog, dsign);
+  if (c.lane == 0) {
+    unsigned long long* p = (unsigned long long*)maxdev;
+    unsigned long long v = __double_as_longlong(dev[warp]);
+    atomicMax(p, v);  // non-negative doubles order like their bit patterns
+  }
+}
+
+__global__ void k_set_window(const __grid_constant__ DModel m, const __grid_constant__ DGroup g, double tdm) {
+  __shared__ Hdr hs[WPB];
+  int warp = threadIdx.x >> 5;
+  int chain = blockIdx.x * WPB + warp;
+  if (chain >= g.nchains) return;
+  Ctx c = make_ctx(&m, &g, &hs[warp], chain);
+  Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
+  load_hdr(c.h, gh, c.lane);
+  init_window(c, tdm);
+  store_hdr(gh, c.h, c.lane);
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+namespace {
+thread_local std::string g_err;
+int fail(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+#define CK(x)                                                                                     \
+  do {                                                                                            \
+    cudaError_t e_ = (x);                                                                         \
+    if (e_ != cudaSuccess) return fail(CTHYB_ERR_CUDA, std::string(#x ": ") + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+T* dev_upload(const std::vector<T>& v, cudaError_t& err) {
+  T* p = nullptr;
+  size_t n = std::max<size_t>(v.size(), 1) * sizeof(T);
+  err = cudaMalloc(&p, n);
+  if (err != cudaSuccess) return nullptr;
+  if (!v.empty()) err = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  return p;
+}
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+}  // namespace
+
+}  // namespace cthyb
+
+using namespace cthyb;
+
+struct cthyb_model_s {
+  HostModel hm;
+  DModel dm;
+  std::vector<void*> allocs;
+  bool uploaded = false;
+};
+
+struct GroupHost {
+  cthyb_group_desc desc;
+  DGroup g;
+  std::vector<double> hybr;
+  double* d_hybr = nullptr;
+  double* d_empty = nullptr;
+  int* d_seeds = nullptr;
+  double* d_tdm = nullptr;
+  int chain0 = 0;
+};
+
+struct cthyb_batch_s {
+  cthyb_model_t model;
+  std::vector<GroupHost> groups;
+  char* slab = nullptr;
+  int* d_err = nullptr;
+  double* d_dev = nullptr;
+  cudaStream_t stream = nullptr;
+  int nchains = 0;
+  int use_graphs = 0;
+  long long logcap = 0;
+  bool counters_reset_pending = false;
+};
+
+extern "C" {
+
+const char* cthyb_last_error(void) { return g_err.c_str(); }
+
+int cthyb_model_create(int nd, const double* umatrix, const double* muimp, const char* qns,
+                       cthyb_model_t* out) {
+  if (!umatrix || !muimp || !out) return fail(CTHYB_ERR_ARG, "null argument");
+  cthyb_model_s* M = new cthyb_model_s;
+  std::string err;
+  if (!build_model(nd, umatrix, muimp, qns, M->hm, err)) {
+    delete M;
+    return fail(CTHYB_ERR_ARG, err);
+  }
+  if (M->hm.nf > NFMAX) {
+    delete M;
+    return fail(CTHYB_ERR_UNSUPPORTED, "too many flavours");
+  }
+  *out = M;
+  return CTHYB_OK;
+}
+
+// Device copy of the model tables, made on first use by a batch.
+static int model_upload(cthyb_model_t M) {
+  if (M->uploaded) return CTHYB_OK;
+  HostModel& hm = M->hm;
+  DModel& d = M->dm;
+  d.nd = hm.nd;
+  d.nf = hm.nf;
+  d.ns = hm.ns;
+  d.nss = hm.nss;
+  d.nsmax = hm.nsmax;
+  d.monomial = hm.monomial;
+  d.egs = hm.egs;
+  cudaError_t e = cudaSuccess;
+  auto up = [&](auto& vec) {
+    auto* p = dev_upload(vec, e);
+    M->allocs.push_back((void*)p);
+    return p;
+  };
+  d.sst_n = up(hm.sst_n);
+  d.sst_off = up(hm.sst_off);
+  d.connect = up(hm.connect);
+  d.eval = up(hm.eval);
+  d.mono_tgt = up(hm.mono_tgt);
+  d.mono_lv = up(hm.mono_lv);
+  d.mono_neg = up(hm.mono_neg);
+  d.blk_off = up(hm.blk_off);
+  d.blk = up(hm.blk);
+  d.dm_off = up(hm.dm_off);
+  d.dm_size = hm.dm_size;
+  if (e != cudaSuccess) {
+    for (void* p : M->allocs) cudaFree(p);
+    M->allocs.clear();
+    return fail(CTHYB_ERR_CUDA, std::string("model upload: ") + cudaGetErrorString(e));
+  }
+  M->uploaded = true;
+  return CTHYB_OK;
+}
+
+int cthyb_model_destroy(cthyb_model_t m) {
+  if (!m) return CTHYB_OK;
+  for (void* p : m->allocs) cudaFree(p);
+  delete m;
+  return CTHYB_OK;
+}
+
+int cthyb_model_info(cthyb_model_t m, int* nsst, int* nstates, int* nsmax, int* monomial, double* egs) {
+  if (!m) return fail(CTHYB_ERR_ARG, "null model");
+  if (nsst) *nsst = m->hm.nss;
+  if (nstates) *nstates = m->hm.ns;
+  if (nsmax) *nsmax = m->hm.nsmax;
+  if (monomial) *monomial = m->hm.monomial;
+  if (egs) *egs = m->hm.egs;
+  return CTHYB_OK;
+}
+
+int cthyb_model_states(cthyb_model_t m, int* sst_size, int* sst_offset, int* fock_state, double* evals) {
+  if (!m) return fail(CTHYB_ERR_ARG, "null model");
+  const HostModel& h = m->hm;
+  for (int s = 0; s < h.nss; ++s) {
+    if (sst_size) sst_size[s] = h.sst_n[s];
+    if (sst_offset) sst_offset[s] = h.sst_off[s];
+  }
+  for (int i = 0; i < h.ns; ++i) {
+    if (fock_state) fock_state[i] = h.fock_of[i];
+    if (evals) evals[i] = h.eval[i];
+  }
+  return CTHYB_OK;
+}
+
+int cthyb_model_connect(cthyb_model_t m, int sst, int b, int s, int ca) {
+  if (!m) return fail(CTHYB_ERR_ARG, "null model");
+  const HostModel& h = m->hm;
+  if (sst < 0 || sst >= h.nss || b < 1 || b > h.nd || s < 1 || s > 2 || ca < 1 || ca > 2) return -1;
+  return h.connect[((size_t)sst * h.nf + 2 * (b - 1) + (s - 1)) * 2 + (ca - 1)];
+}
+
+static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
+  const HostModel& hm = B->model->hm;
+  DGroup& g = G.g;
+  const cthyb_group_desc& d = G.desc;
+  const int nf = hm.nf;
+  g.nchains = d.nchains;
+  g.beta = d.beta;
+  g.nftau = d.nftau;
+  g.ntau = d.ntau;
+  g.ncorr = d.ncorr > 0 ? d.ncorr : 100;
+  g.maxhisto = d.maxhisto > 1 ? d.maxhisto : 500;
+  g.p_outer = d.p_outer;
+  g.dense = (d.flags & CTHYB_FLAG_DENSE) ? 1 : 0;
+  g.meas_dm = (d.flags & CTHYB_FLAG_NO_DM) ? 0 : 1;
+  int kcap = d.kcap > 0 ? d.kcap : std::max(32, (int)std::min(4096.0, 32.0 * std::ceil(d.beta * 1.0 / 32.0 + 1.0)));
+  kcap = (kcap + 3) / 4 * 4;
+  int opcap = d.opcap > 0 ? d.opcap : std::max(64, std::min(nf * kcap * 2, (int)(64 + 16 * d.beta)));
+  g.kcap = kcap;
+  g.opcap = opcap;
+  int L = d.tree_levels;
+  if (L <= 0) {
+    L = 1;
+    while ((1 << L) < opcap / 4 && L < 12) ++L;
+  }
+  if (L > 16) L = 16;
+  g.L = L;
+  const bool mono = hm.monomial && !g.dense;
+  size_t nb = mono ? (size_t)hm.ns * 10 : 0;
+  nb += (size_t)hm.nss * 2;
+  g.node_bytes = align_up(nb, 16);
+  size_t nodes = (size_t)2 << L;  // heap indices 0 .. 2^(L+1)-1
+  size_t off = 0;
+  g.o_hdr = off;
+  off = align_up(off + sizeof(Hdr), 256);
+  g.o_mt = off;
+  off = align_up(off + 624 * 4, 256);
+  g.o_optau = off;
+  off = align_up(off + (size_t)(opcap + 2) * 8, 256);
+  g.o_opcode = off;
+  off = align_up(off + (size_t)(opcap + 2) * 4, 256);
+  g.o_srt_tau = off;
+  off = align_up(off + (size_t)nf * 2 * kcap * 8, 256);
+  g.o_srt_slot = off;
+  off = align_up(off + (size_t)nf * 2 * kcap * 2, 256);
+  g.o_slot_tau = off;
+  off = align_up(off + (size_t)nf * 2 * kcap * 8, 256);
+  g.o_M = off;
+  off = align_up(off + (size_t)nf * kcap * kcap * 8, 256);
+  g.o_tree = off;
+  off = align_up(off + nodes * 2 * g.node_bytes, 256);
+  g.o_act = off;
+  off = align_up(off + nodes, 256);
+  g.o_scr = off;
+  off = align_up(off + (size_t)(4 * kcap + opcap + 2) * 8 + (size_t)(opcap + 2) * 4, 256);
+  g.o_gtau = off;
+  off = align_up(off + (size_t)nf * d.ntau * 8, 256);
+  g.o_histo = off;
+  off = align_up(off + (size_t)nf * g.maxhisto * 8, 256);
+  g.o_dm = off;
+  off = align_up(off + (size_t)hm.ns * 8, 256);
+  g.o_dense = off;
+  size_t dense = std::max((size_t)2 * hm.nsmax * hm.nsmax, (size_t)2 * kcap * kcap) * 8;
+  off = align_up(off + dense, 256);
+  g.o_log = off;
+  g.logcap = logcap;
+  off = align_up(off + (size_t)logcap * sizeof(cthyb_record), 256);
+  g.stride = off;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc* groups, cthyb_batch_t* out) {
+  if (!model || ngroups < 1 || !groups || !out) return fail(CTHYB_ERR_ARG, "bad arguments");
+  {
+    int rc = model_upload(model);
+    if (rc) return rc;
+  }
+  cthyb_batch_s* B = new cthyb_batch_s;
+  B->model = model;
+  const HostModel& hm = model->hm;
+  B->groups.resize(ngroups);
+  size_t total = 0;
+  for (int i = 0; i < ngroups; ++i) {
+    GroupHost& G = B->groups[i];
+    G.desc = groups[i];
+    if (G.desc.nchains < 1 || G.desc.nftau < 2 || G.desc.ntau < 1 || !(G.desc.beta > 0) || !G.desc.ftau) {
+      delete B;
+      return fail(CTHYB_ERR_ARG, "bad group description");
+    }
+    layout_group(B, G, 0);
+    G.chain0 = B->nchains;
+    B->nchains += G.desc.nchains;
+    total += (size_t)G.desc.nchains * G.g.stride;
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&B->slab, total);
+  if (e == cudaSuccess) e = cudaMemsetAsync(B->slab, 0, total, B->stream);
+  if (e == cudaSuccess) e = cudaMalloc(&B->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(B->d_err, 0, sizeof(int), B->stream);
+  if (e == cudaSuccess) e = cudaMalloc(&B->d_dev, sizeof(double));
+  if (e != cudaSuccess) {
+    cthyb_batch_destroy(B);
+    return fail(CTHYB_ERR_CUDA, std::string("batch allocation: ") + cudaGetErrorString(e));
+  }
+  size_t off = 0;
+  for (int i = 0; i < ngroups; ++i) {
+    GroupHost& G = B->groups[i];
+    const cthyb_group_desc& d = G.desc;
+    G.g.base = B->slab + off;
+    off += (size_t)d.nchains * G.g.stride;
+    G.g.err_flag = B->d_err;
+    // F(tau) re-laid out per flavour f = 2b+s
+    G.hybr.resize((size_t)hm.nf * d.nftau);
+    for (int b = 0; b < hm.nd; ++b)
+      for (int s = 0; s < 2; ++s)
+        for (int t = 0; t < d.nftau; ++t)
+          G.hybr[(size_t)(2 * b + s) * d.nftau + t] = d.ftau[b + hm.nd * (s + 2 * (size_t)t)];
+    G.d_hybr = dev_upload(G.hybr, e);
+    G.g.hybr = G.d_hybr;
+    std::vector<double> w;
+    empty_trace_weights(hm, d.beta, w);
+    G.d_empty = dev_upload(w, e);
+    G.g.empty_w = G.d_empty;
+    std::vector<int> seeds(d.nchains);
+    for (int c = 0; c < d.nchains; ++c) seeds[c] = d.seeds ? d.seeds[c] : d.seed0 + c;
+    G.d_seeds = dev_upload(seeds, e);
+    std::vector<double> tdm(1, d.taudiff_max);
+    G.d_tdm = dev_upload(tdm, e);
+    if (e != cudaSuccess) {
+      cthyb_batch_destroy(B);
+      return fail(CTHYB_ERR_CUDA, std::string("group upload: ") + cudaGetErrorString(e));
+    }
+    int nblk = (d.nchains + WPB - 1) / WPB;
+    k_init<<<nblk, WPB * 32, 0, B->stream>>>(model->dm, G.g, G.d_seeds, G.d_tdm, G.g.ncorr);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      cthyb_batch_destroy(B);
+      return fail(CTHYB_ERR_CUDA, std::string("init launch: ") + cudaGetErrorString(e));
+    }
+  }
+  e = cudaStreamSynchronize(B->stream);
+  if (e != cudaSuccess) {
+    cthyb_batch_destroy(B);
+    return fail(CTHYB_ERR_CUDA, std::string("init: ") + cudaGetErrorString(e));
+  }
+  *out = B;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_destroy(cthyb_batch_t B) {
+  if (!B) return CTHYB_OK;
+  if (B->stream) cudaStreamSynchronize(B->stream);
+  for (GroupHost& G : B->groups) {
+    cudaFree(G.d_hybr);
+    cudaFree(G.d_empty);
+    cudaFree(G.d_seeds);
+    cudaFree(G.d_tdm);
+  }
+  cudaFree(B->slab);
+  cudaFree(B->d_err);
+  cudaFree(B->d_dev);
+  if (B->stream) cudaStreamDestroy(B->stream);
+  delete B;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_nchains(cthyb_batch_t B) { return B ? B->nchains : 0; }
+
+int cthyb_batch_stream(cthyb_batch_t B, void** s) {
+  if (!B || !s) return fail(CTHYB_ERR_ARG, "null");
+  *s = (void*)B->stream;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_use_graphs(cthyb_batch_t B, int on) {
+  if (!B) return fail(CTHYB_ERR_ARG, "null");
+  B->use_graphs = on;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_set_taudiffmax(cthyb_batch_t B, int group, double tdm) {
+  if (!B || group < 0 || group >= (int)B->groups.size()) return fail(CTHYB_ERR_ARG, "bad group");
+  GroupHost& G = B->groups[group];
+  int nblk = (G.desc.nchains + WPB - 1) / WPB;
+  k_set_window<<<nblk, WPB * 32, 0, B->stream>>>(B->model->dm, G.g, tdm);
+  CK(cudaGetLastError());
+  return CTHYB_OK;
+}
+
+static int launch_sweeps(cthyb_batch_t B, long long nprop, int nmeas, int reset) {
+  for (GroupHost& G : B->groups) {
+    int nblk = (G.desc.nchains + WPB - 1) / WPB;
+    k_sweep<<<nblk, WPB * 32, 0, B->stream>>>(B->model->dm, G.g, nprop, nmeas, reset);
+    CK(cudaGetLastError());
+  }
+  return CTHYB_OK;
+}
+
+int cthyb_batch_warmup(cthyb_batch_t B, int64_t n) {
+  if (!B || n < 0) return fail(CTHYB_ERR_ARG, "bad arguments");
+  // chunks keep single launches short
+  const long long chunk = 20000;
+  int reset = 1;
+  for (long long done = 0; done < n; done += chunk) {
+    long long m = std::min<long long>(chunk, n - done);
+    int rc = launch_sweeps(B, m, 0, reset);
+    if (rc) return rc;
+    reset = 0;
+  }
+  if (n == 0) return launch_sweeps(B, 0, 0, 1);
+  return CTHYB_OK;
+}
+
+int cthyb_batch_measure(cthyb_batch_t B, int64_t nmeas) {
+  if (!B || nmeas < 0) return fail(CTHYB_ERR_ARG, "bad arguments");
+  const long long chunk = 200;
+  int reset = 1;
+  for (long long done = 0; done < nmeas; done += chunk) {
+    int m = (int)std::min<long long>(chunk, nmeas - done);
+    int rc = launch_sweeps(B, 0, m, reset);
+    if (rc) return rc;
+    reset = 0;
+  }
+  return CTHYB_OK;
+}
+
+int cthyb_batch_reset_measurements(cthyb_batch_t B) {
+  if (!B) return fail(CTHYB_ERR_ARG, "null");
+  for (GroupHost& G : B->groups) {
+    for (int c = 0; c < G.desc.nchains; ++c) {
+      char* base = G.g.base + (size_t)c * G.g.stride;
+      CK(cudaMemsetAsync(base + G.g.o_gtau, 0, G.g.o_dense - G.g.o_gtau, B->stream));
+      // header measurement fields: cnt_meas, meas_sign
+      Hdr hz;
+      CK(cudaMemcpyAsync(&hz, base + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost, B->stream));
+      CK(cudaStreamSynchronize(B->stream));
+      hz.cnt_meas = 0;
+      hz.meas_sign = 0.0;
+      CK(cudaMemcpyAsync(base + G.g.o_hdr, &hz, sizeof(Hdr), cudaMemcpyHostToDevice, B->stream));
+      CK(cudaStreamSynchronize(B->stream));
+    }
+  }
+  return CTHYB_OK;
+}
+
+int cthyb_batch_sync(cthyb_batch_t B) {
+  if (!B) return fail(CTHYB_ERR_ARG, "null");
+  CK(cudaStreamSynchronize(B->stream));
+  int flag = 0;
+  CK(cudaMemcpy(&flag, B->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (flag == ST_CAPACITY) return fail(CTHYB_ERR_CAPACITY, "a chain reached its operator capacity (kcap/opcap)");
+  if (flag == ST_NUMERIC) return fail(CTHYB_ERR_NUMERIC, "DetRat too small in removal");
+  if (flag == ST_INTERNAL) return fail(CTHYB_ERR_INTERNAL, "pair bookkeeping inconsistency");
+  if (flag) return fail(CTHYB_ERR_INTERNAL, "chain error");
+  return CTHYB_OK;
+}
+
+static int find_chain(cthyb_batch_t B, int chain, GroupHost** G, int* local) {
+  if (!B || chain < 0 || chain >= B->nchains) return fail(CTHYB_ERR_ARG, "bad chain index");
+  for (GroupHost& g : B->groups)
+    if (chain >= g.chain0 && chain < g.chain0 + g.desc.nchains) {
+      *G = &g;
+      *local = chain - g.chain0;
+      return CTHYB_OK;
+    }
+  return fail(CTHYB_ERR_ARG, "bad chain index");
+}
+
+static int read_hdr(cthyb_batch_t B, GroupHost* G, int c, Hdr& h) {
+  CK(cudaStreamSynchronize(B->stream));
+  CK(cudaMemcpy(&h, G->g.base + (size_t)c * G->g.stride + G->g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost));
+  return CTHYB_OK;
+}
+
+int cthyb_batch_state(cthyb_batch_t B, int chain, double* o) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  o[0] = h.trace_log;
+  o[1] = h.trace_sign;
+  o[2] = h.det_log;
+  o[3] = h.det_sign;
+  o[4] = h.cfgsign;
+  o[5] = h.npairs;
+  o[6] = h.outer_sst;
+  o[7] = h.window_position;
+  o[8] = h.num_windows;
+  o[9] = h.K;
+  o[10] = h.tauwin_min;
+  o[11] = h.tauwin_max;
+  o[12] = h.taudiff_max;
+  o[13] = h.nslide;
+  o[14] = h.status;
+  o[15] = h.k[0];
+  return CTHYB_OK;
+}
+
+int cthyb_batch_results(cthyb_batch_t B, int chain, double* gtau, double* mean_sign, double* dmat,
+                        double* histo, int64_t* counters) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  const HostModel& hm = B->model->hm;
+  char* base = G->g.base + (size_t)c * G->g.stride;
+  const int nt = G->g.ntau, nf = hm.nf;
+  double ms = h.cnt_meas ? h.meas_sign / (double)h.cnt_meas : 0.0;
+  if (mean_sign) *mean_sign = ms;
+  if (gtau) {
+    std::vector<double> raw((size_t)nf * nt);
+    CK(cudaMemcpy(raw.data(), base + G->g.o_gtau, raw.size() * 8, cudaMemcpyDeviceToHost));
+    for (int f = 0; f < nf; ++f) {
+      int b = f / 2, s = f % 2;
+      for (int t = 0; t < nt; ++t) {
+        double v = h.cnt_meas ? -(raw[(size_t)f * nt + t] / (double)h.cnt_meas) / (-ms) * (double)nt /
+                                    (G->g.beta * G->g.beta)
+                              : 0.0;
+        gtau[b + hm.nd * (s + 2 * (size_t)t)] = v;
+      }
+    }
+  }
+  if (dmat) {
+    std::vector<double> d(hm.ns);
+    CK(cudaMemcpy(d.data(), base + G->g.o_dm, d.size() * 8, cudaMemcpyDeviceToHost));
+    double zs = h.cnt_meas ? -1.0 / ((double)h.cnt_meas * ms) : 0.0;
+    std::memset(dmat, 0, sizeof(double) * (size_t)hm.ns * hm.ns);
+    for (int i = 0; i < hm.ns; ++i) dmat[(size_t)i * hm.ns + i] = d[i] * zs;
+  }
+  if (histo) {
+    const int hmx = G->g.maxhisto;
+    std::vector<double> hh((size_t)nf * hmx);
+    CK(cudaMemcpy(hh.data(), base + G->g.o_histo, hh.size() * 8, cudaMemcpyDeviceToHost));
+    for (int f = 0; f < nf; ++f)
+      for (int k = 0; k < hmx; ++k)
+        histo[(f / 2) + hm.nd * ((f % 2) + 2 * (size_t)k)] =
+            h.cnt_meas ? hh[(size_t)f * hmx + k] / (double)h.cnt_meas : 0.0;
+  }
+  if (counters) {
+    counters[0] = h.try_add;
+    counters[1] = h.acc_add;
+    counters[2] = h.try_rem;
+    counters[3] = h.acc_rem;
+    counters[4] = h.qn_add;
+    counters[5] = h.qn_rem;
+    counters[6] = h.cnt_meas;
+    counters[7] = h.nprop;
+  }
+  return CTHYB_OK;
+}
+
+int cthyb_batch_group_sums(cthyb_batch_t B, int group, double* gsum, double* sign_sum, int64_t* cnt) {
+  if (!B || group < 0 || group >= (int)B->groups.size()) return fail(CTHYB_ERR_ARG, "bad group");
+  GroupHost& G = B->groups[group];
+  const HostModel& hm = B->model->hm;
+  CK(cudaStreamSynchronize(B->stream));
+  const int nt = G.g.ntau, nf = hm.nf;
+  std::vector<double> raw((size_t)nf * nt);
+  if (gsum) std::memset(gsum, 0, sizeof(double) * raw.size());
+  double ss = 0;
+  long long cn = 0;
+  for (int c = 0; c < G.desc.nchains; ++c) {
+    char* base = G.g.base + (size_t)c * G.g.stride;
+    Hdr h;
+    CK(cudaMemcpy(&h, base + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost));
+    ss += h.meas_sign;
+    cn += h.cnt_meas;
+    if (gsum) {
+      CK(cudaMemcpy(raw.data(), base + G.g.o_gtau, raw.size() * 8, cudaMemcpyDeviceToHost));
+      for (int f = 0; f < nf; ++f)
+        for (int t = 0; t < nt; ++t) gsum[(f / 2) + hm.nd * ((f % 2) + 2 * (size_t)t)] += raw[(size_t)f * nt + t];
+    }
+  }
+  if (sign_sum) *sign_sum = ss;
+  if (cnt) *cnt = cn;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_get_config(cthyb_batch_t B, int chain, int* n, double* taus, int* orbs, int* spins, int* cas,
+                           int* outer) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  char* base = G->g.base + (size_t)c * G->g.stride;
+  std::vector<double> t(h.K);
+  std::vector<int> code(h.K);
+  if (h.K) {
+    CK(cudaMemcpy(t.data(), base + G->g.o_optau, h.K * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(code.data(), base + G->g.o_opcode, h.K * 4, cudaMemcpyDeviceToHost));
+  }
+  *n = h.K;
+  for (int i = 0; i < h.K; ++i) {
+    if (taus) taus[i] = t[i];
+    int f = code[i] >> 1;
+    if (orbs) orbs[i] = f / 2 + 1;
+    if (spins) spins[i] = f % 2 + 1;
+    if (cas) cas[i] = (code[i] & 1) + 1;
+  }
+  if (outer) *outer = h.outer_sst;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_set_config(cthyb_batch_t B, int chain, int n, const double* taus, const int* orbs,
+                           const int* spins, const int* cas, int outer_sst) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  const HostModel& hm = B->model->hm;
+  if (n < 0 || n > G->g.opcap || outer_sst < 0 || outer_sst >= hm.nss)
+    return fail(CTHYB_ERR_ARG, "configuration exceeds capacity or bad superstate");
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return taus[a] < taus[b]; });
+  std::vector<double> t(n);
+  std::vector<int> code(n);
+  std::vector<int> per(hm.nf * 2, 0);
+  for (int i = 0; i < n; ++i) {
+    int j = idx[i];
+    if (orbs[j] < 1 || orbs[j] > hm.nd || spins[j] < 1 || spins[j] > 2 || cas[j] < 1 || cas[j] > 2)
+      return fail(CTHYB_ERR_ARG, "bad operator");
+    t[i] = taus[j];
+    int f = 2 * (orbs[j] - 1) + (spins[j] - 1);
+    code[i] = 2 * f + (cas[j] - 1);
+    per[code[i]]++;
+  }
+  for (int f = 0; f < hm.nf; ++f) {
+    if (per[2 * f] != per[2 * f + 1]) return fail(CTHYB_ERR_ARG, "unbalanced configuration");
+    if (per[2 * f] > G->g.kcap) return fail(CTHYB_ERR_CAPACITY, "configuration exceeds kcap");
+  }
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  h.K = n;
+  char* base = G->g.base + (size_t)c * G->g.stride;
+  if (n) {
+    CK(cudaMemcpy(base + G->g.o_optau, t.data(), n * 8, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(base + G->g.o_opcode, code.data(), n * 4, cudaMemcpyHostToDevice));
+  }
+  CK(cudaMemcpy(base + G->g.o_hdr, &h, sizeof(Hdr), cudaMemcpyHostToDevice));
+  k_set_config<<<1, 32, 0, B->stream>>>(B->model->dm, G->g, c, outer_sst);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(B->stream));
+  return CTHYB_OK;
+}
+
+int cthyb_batch_minv(cthyb_batch_t B, int chain, int f, int* kout, double* out) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  const int kcap = G->g.kcap, k = h.k[f];
+  *kout = k;
+  if (!out) return CTHYB_OK;
+  char* base = G->g.base + (size_t)c * G->g.stride;
+  std::vector<double> Mf((size_t)kcap * kcap);
+  std::vector<short> sc(kcap), sa(kcap);
+  CK(cudaMemcpy(Mf.data(), base + G->g.o_M + (size_t)f * kcap * kcap * 8, Mf.size() * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(sc.data(), base + G->g.o_srt_slot + (size_t)(2 * f) * kcap * 2, kcap * 2, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(sa.data(), base + G->g.o_srt_slot + (size_t)(2 * f + 1) * kcap * 2, kcap * 2,
+                cudaMemcpyDeviceToHost));
+  for (int ra = 0; ra < k; ++ra)
+    for (int rcn = 0; rcn < k; ++rcn) out[(size_t)ra * k + rcn] = Mf[(size_t)sa[ra] * kcap + sc[rcn]];
+  return CTHYB_OK;
+}
+
+int cthyb_batch_refresh_minv(cthyb_batch_t B, int replace, double* maxdev) {
+  if (!B) return fail(CTHYB_ERR_ARG, "null");
+  CK(cudaMemsetAsync(B->d_dev, 0, sizeof(double), B->stream));
+  for (GroupHost& G : B->groups) {
+    if (2 * G.g.kcap * G.g.kcap > 2 * B->model->hm.nsmax * B->model->hm.nsmax &&
+        (size_t)2 * G.g.kcap * G.g.kcap * 8 > G.g.o_log - G.g.o_dense)
+      return fail(CTHYB_ERR_INTERNAL, "refresh scratch too small");
+    int nblk = (G.desc.nchains + WPB - 1) / WPB;
+    k_refresh<<<nblk, WPB * 32, 0, B->stream>>>(B->model->dm, G.g, replace, B->d_dev);
+    CK(cudaGetLastError());
+  }
+  double d = 0;
+  CK(cudaMemcpyAsync(&d, B->d_dev, sizeof(double), cudaMemcpyDeviceToHost, B->stream));
+  CK(cudaStreamSynchronize(B->stream));
+  if (maxdev) *maxdev = d;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_set_log(cthyb_batch_t B, int64_t cap) {
+  if (!B || cap < 0) return fail(CTHYB_ERR_ARG, "bad arguments");
+  // re-layout is only possible right after creation: the log area is the
+  // last region of each chain block, so grow the slab by copying chains.
+  CK(cudaStreamSynchronize(B->stream));
+  std::vector<DGroup> oldg;
+  for (GroupHost& G : B->groups) oldg.push_back(G.g);
+  size_t total = 0;
+  for (GroupHost& G : B->groups) {
+    DGroup save = G.g;
+    layout_group(B, G, cap);
+    G.g.base = save.base;
+    G.g.hybr = save.hybr;
+    G.g.empty_w = save.empty_w;
+    G.g.err_flag = save.err_flag;
+    total += (size_t)G.desc.nchains * G.g.stride;
+  }
+  char* slab = nullptr;
+  CK(cudaMalloc(&slab, total));
+  CK(cudaMemset(slab, 0, total));
+  size_t off = 0;
+  for (size_t gi = 0; gi < B->groups.size(); ++gi) {
+    GroupHost& G = B->groups[gi];
+    char* nb = slab + off;
+    size_t keep = std::min(oldg[gi].o_log, G.g.o_log);
+    for (int c = 0; c < G.desc.nchains; ++c)
+      CK(cudaMemcpy(nb + (size_t)c * G.g.stride, oldg[gi].base + (size_t)c * oldg[gi].stride, keep,
+                    cudaMemcpyDeviceToDevice));
+    G.g.base = nb;
+    off += (size_t)G.desc.nchains * G.g.stride;
+    // reset the per-chain log counters
+    for (int c = 0; c < G.desc.nchains; ++c) {
+      Hdr h;
+      CK(cudaMemcpy(&h, nb + (size_t)c * G.g.stride + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost));
+      h.logn = 0;
+      CK(cudaMemcpy(nb + (size_t)c * G.g.stride + G.g.o_hdr, &h, sizeof(Hdr), cudaMemcpyHostToDevice));
+    }
+  }
+  cudaFree(B->slab);
+  B->slab = slab;
+  B->logcap = cap;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_get_log(cthyb_batch_t B, int chain, void* rec, int64_t* n) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  long long m = std::min<long long>(h.logn, G->g.logcap);
+  *n = h.logn;
+  if (rec && m > 0)
+    CK(cudaMemcpy(rec, G->g.base + (size_t)c * G->g.stride + G->g.o_log, (size_t)m * sizeof(cthyb_record),
+                  cudaMemcpyDeviceToHost));
+  return CTHYB_OK;
+}
+
+int cthyb_batch_work_counters(cthyb_batch_t B, int64_t* out8, int reset) {
+  if (!B || !out8) return fail(CTHYB_ERR_ARG, "null");
+  CK(cudaStreamSynchronize(B->stream));
+  for (int i = 0; i < 8; ++i) out8[i] = 0;
+  for (GroupHost& G : B->groups)
+    for (int c = 0; c < G.desc.nchains; ++c) {
+      char* p = G.g.base + (size_t)c * G.g.stride + G.g.o_hdr;
+      Hdr h;
+      CK(cudaMemcpy(&h, p, sizeof(Hdr), cudaMemcpyDeviceToHost));
+      out8[0] += h.w_mbytes;
+      out8[1] += h.w_mflops;
+      out8[2] += h.w_opbytes;
+      out8[3] += h.w_nodes;
+      out8[4] += h.try_add + h.try_rem;
+      out8[5] += h.acc_add + h.acc_rem;
+      if (reset) {
+        h.w_mbytes = h.w_mflops = h.w_opbytes = h.w_nodes = 0;
+        CK(cudaMemcpy(p, &h, sizeof(Hdr), cudaMemcpyHostToDevice));
+      }
+    }
+  return CTHYB_OK;
+}
+
+}  // extern "C"

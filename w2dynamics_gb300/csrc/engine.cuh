@@ -1,0 +1,69 @@
+// engine.cuh -- device data layout and warp-level primitives of the CT-HYB
+// pair-move engine (one warp advances one Markov chain).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cthyb {
+
+constexpr int NFMAX = 14;  // flavours (Nd <= 7)
+constexpr unsigned FULL = 0xffffffffu;
+constexpr double DHUGE = 1.7976931348623157e308;
+
+// status codes stored in the chain header
+enum : int {
+  ST_OK = 0,
+  ST_CAPACITY = 1,     // a proposal would exceed kcap/opcap (state untouched)
+  ST_INTERNAL = 2,     // bookkeeping inconsistency (NPairs count, search)
+  ST_NUMERIC = 3,      // DetRat too small on an accepted removal (CTQMC.F90:4062)
+  ST_UNSUPPORTED = 4,  // move type outside the implemented set
+};
+
+struct DModel {
+  int nd, nf, ns, nss, nsmax, monomial;
+  double egs;
+  const int* sst_n;            // [nss]
+  const int* sst_off;          // [nss]
+  const int* connect;          // [nss][nf][2]
+  const double* eval;          // [ns]
+  const int* mono_tgt;         // [2nf][ns]
+  const double* mono_lv;       // [2nf][ns]
+  const unsigned char* mono_neg;
+  const long long* blk_off;    // [nss][nf][2]
+  const double* blk;
+  const long long* dm_off;     // [nss]
+  long long dm_size;
+};
+
+// Per-chain header (kept in shared memory while a warp works on the chain).
+struct Hdr {
+  double trace_log, trace_sign, det_log, det_sign, cfgsign;
+  double tauwin_min, tauwin_max, taudiff_max;
+  double meas_sign;
+  int num_windows, window_position, npairs, outer_sst;
+  int K, mt_idx, status, nslide;
+  long long nprop, try_add, acc_add, try_rem, acc_rem, qn_add, qn_rem, cnt_meas, logn;
+  int k[NFMAX];
+  // work counters for the roofline: M bytes, M flops, op-array bytes, tree node updates
+  long long w_mbytes, w_mflops, w_opbytes, w_nodes;
+};
+
+struct DGroup {
+  int nchains;
+  double beta;
+  int nftau;
+  const double* hybr;  // [nf][nftau]
+  int ntau, ncorr, maxhisto;
+  double p_outer;
+  int kcap, opcap, L, dense, meas_dm;
+  char* base;          // chain c at base + c*stride
+  size_t stride;
+  size_t o_hdr, o_mt, o_optau, o_opcode, o_srt_tau, o_srt_slot, o_slot_tau, o_M, o_tree, o_act,
+      o_scr, o_gtau, o_histo, o_dm, o_dense, o_log;
+  size_t node_bytes;   // bytes of one node slot
+  long long logcap;
+  const double* empty_w;  // [nss] normalised empty-trace weights
+  int* err_flag;
+};
+
+}  // namespace cthyb

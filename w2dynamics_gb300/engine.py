@@ -1,0 +1,328 @@
+"""ctypes bindings of the GB300 CT-HYB engine (include/cthyb_gpu.h).
+
+The shared library is built in-tree by w2dynamics_gb300.build; there is no
+CPU fallback: if it is missing or no GPU is present, every entry point
+raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+RECORD_DTYPE = np.dtype([
+    ("move", "<i4"), ("outcome", "<i4"), ("orb", "<i4"), ("spin", "<i4"),
+    ("change_outer", "<i4"), ("fpos_c", "<i4"), ("fpos_a", "<i4"),
+    ("npairs", "<i4"), ("outer_sst", "<i4"), ("k_total", "<i4"),
+    ("tau_c", "<f8"), ("tau_a", "<f8"), ("det_log", "<f8"), ("det_sign", "<f8"),
+    ("tr_log", "<f8"), ("tr_sign", "<f8"), ("prob", "<f8"), ("rand", "<f8"),
+])
+
+FLAG_DENSE = 1
+FLAG_NO_DM = 2
+
+EXPORTS = (
+    "cthyb_last_error", "cthyb_model_create", "cthyb_model_destroy", "cthyb_model_info",
+    "cthyb_model_states", "cthyb_model_connect", "cthyb_batch_create", "cthyb_batch_destroy",
+    "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
+    "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
+    "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_results",
+    "cthyb_batch_group_sums", "cthyb_batch_state", "cthyb_batch_get_config",
+    "cthyb_batch_set_config", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
+    "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
+)
+
+
+class GroupDesc(C.Structure):
+    _fields_ = [("beta", C.c_double), ("nftau", C.c_int32), ("ntau", C.c_int32),
+                ("ftau", C.POINTER(C.c_double)), ("nchains", C.c_int32), ("seed0", C.c_int32),
+                ("seeds", C.POINTER(C.c_int32)), ("taudiff_max", C.c_double),
+                ("ncorr", C.c_int32), ("p_outer", C.c_double), ("kcap", C.c_int32),
+                ("opcap", C.c_int32), ("tree_levels", C.c_int32), ("maxhisto", C.c_int32),
+                ("flags", C.c_int32)]
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=False):
+    """Load libcthyb_gpu.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(path):
+        raise EngineError(f"{path} not built: run `python -m w2dynamics_gb300.build`")
+    L = C.CDLL(path)
+    vp, dp, ip, i64 = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int), C.c_int64
+    L.cthyb_last_error.restype = C.c_char_p
+    L.cthyb_model_create.argtypes = [C.c_int, dp, dp, C.c_char_p, C.POINTER(vp)]
+    L.cthyb_model_destroy.argtypes = [vp]
+    L.cthyb_model_info.argtypes = [vp, ip, ip, ip, ip, dp]
+    L.cthyb_model_states.argtypes = [vp, ip, ip, ip, dp]
+    L.cthyb_model_connect.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.cthyb_batch_create.argtypes = [vp, C.c_int, C.POINTER(GroupDesc), C.POINTER(vp)]
+    L.cthyb_batch_destroy.argtypes = [vp]
+    L.cthyb_batch_nchains.argtypes = [vp]
+    L.cthyb_batch_set_taudiffmax.argtypes = [vp, C.c_int, C.c_double]
+    L.cthyb_batch_warmup.argtypes = [vp, i64]
+    L.cthyb_batch_measure.argtypes = [vp, i64]
+    L.cthyb_batch_reset_measurements.argtypes = [vp]
+    L.cthyb_batch_sync.argtypes = [vp]
+    L.cthyb_batch_stream.argtypes = [vp, C.POINTER(vp)]
+    L.cthyb_batch_use_graphs.argtypes = [vp, C.c_int]
+    L.cthyb_batch_results.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.POINTER(i64)]
+    L.cthyb_batch_group_sums.argtypes = [vp, C.c_int, dp, dp, C.POINTER(i64)]
+    L.cthyb_batch_state.argtypes = [vp, C.c_int, dp]
+    L.cthyb_batch_get_config.argtypes = [vp, C.c_int, ip, dp, ip, ip, ip, ip]
+    L.cthyb_batch_set_config.argtypes = [vp, C.c_int, C.c_int, dp, ip, ip, ip, C.c_int]
+    L.cthyb_batch_minv.argtypes = [vp, C.c_int, C.c_int, ip, dp]
+    L.cthyb_batch_refresh_minv.argtypes = [vp, C.c_int, dp]
+    L.cthyb_batch_set_log.argtypes = [vp, i64]
+    L.cthyb_batch_get_log.argtypes = [vp, C.c_int, C.c_void_p, C.POINTER(i64)]
+    L.cthyb_batch_work_counters.argtypes = [vp, C.POINTER(i64), C.c_int]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise EngineError(f"cthyb error {rc}: {load().cthyb_last_error().decode()}")
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+class Model:
+    """Local problem on the device (cthyb_model_create)."""
+
+    def __init__(self, nd, umatrix, muimp, quantum_numbers):
+        L = load()
+        self.nd = nd
+        self._u = np.asfortranarray(np.asarray(umatrix, np.float64).reshape((2 * nd,) * 4))
+        self._mu = np.asfortranarray(np.asarray(muimp, np.float64).reshape(nd, 2, nd, 2))
+        h = C.c_void_p()
+        _check(L.cthyb_model_create(nd, _dp(self._u.ravel(order="F")),
+                                    _dp(self._mu.ravel(order="F")),
+                                    quantum_numbers.encode(), C.byref(h)))
+        self.h = h
+        a, b, c, d = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        e = C.c_double()
+        _check(L.cthyb_model_info(h, C.byref(a), C.byref(b), C.byref(c), C.byref(d), C.byref(e)))
+        self.nsst, self.nstates, self.nsmax, self.monomial, self.egs = (
+            a.value, b.value, c.value, d.value, e.value)
+        n = np.zeros(self.nsst, np.int32)
+        o = np.zeros(self.nsst, np.int32)
+        fk = np.zeros(self.nstates, np.int32)
+        ev = np.zeros(self.nstates)
+        _check(L.cthyb_model_states(h, _ip(n), _ip(o), _ip(fk), _dp(ev)))
+        self.sst_size, self.sst_offset, self.fock_states, self.evals = n, o, fk, ev
+
+    def connect(self, sst, b, s, ca):
+        return load().cthyb_model_connect(self.h, sst, b, s, ca)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().cthyb_model_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Group:
+    """Parameters of one group of chains (one beta / one F(tau))."""
+
+    def __init__(self, beta, ftau, ntau, nchains=1, seed0=0, seeds=None, taudiff_max=-1.0,
+                 ncorr=100, p_outer=0.0, kcap=0, opcap=0, tree_levels=0, maxhisto=500,
+                 dense=False, measure_dm=True):
+        self.beta = float(beta)
+        self.ftau = np.asfortranarray(np.asarray(ftau, np.float64))
+        self.ntau = int(ntau)
+        self.nchains = int(nchains)
+        self.seed0 = int(seed0)
+        self.seeds = None if seeds is None else np.ascontiguousarray(seeds, np.int32)
+        self.taudiff_max = float(taudiff_max)
+        self.ncorr = int(ncorr)
+        self.p_outer = float(p_outer)
+        self.kcap, self.opcap, self.tree_levels = int(kcap), int(opcap), int(tree_levels)
+        self.maxhisto = int(maxhisto)
+        self.flags = (FLAG_DENSE if dense else 0) | (0 if measure_dm else FLAG_NO_DM)
+
+    def desc(self):
+        d = GroupDesc()
+        d.beta = self.beta
+        d.nftau = self.ftau.shape[2]
+        d.ntau = self.ntau
+        self._fl = self.ftau.ravel(order="F")
+        d.ftau = _dp(self._fl)
+        d.nchains = self.nchains
+        d.seed0 = self.seed0
+        d.seeds = self.seeds.ctypes.data_as(C.POINTER(C.c_int32)) if self.seeds is not None else None
+        d.taudiff_max = self.taudiff_max
+        d.ncorr = self.ncorr
+        d.p_outer = self.p_outer
+        d.kcap, d.opcap, d.tree_levels = self.kcap, self.opcap, self.tree_levels
+        d.maxhisto = self.maxhisto
+        d.flags = self.flags
+        return d
+
+
+class Batch:
+    """A batch of independent chains (one chain = the plain drop-in form)."""
+
+    def __init__(self, model, groups):
+        L = load()
+        self.model = model
+        self.groups = list(groups)
+        descs = (GroupDesc * len(self.groups))(*[g.desc() for g in self.groups])
+        h = C.c_void_p()
+        _check(L.cthyb_batch_create(model.h, len(self.groups), descs, C.byref(h)))
+        self.h = h
+        self.nchains = L.cthyb_batch_nchains(h)
+        self._group_of = []
+        for gi, g in enumerate(self.groups):
+            self._group_of += [gi] * g.nchains
+
+    # --- loop entry points
+    def set_taudiffmax(self, group, tdm):
+        _check(load().cthyb_batch_set_taudiffmax(self.h, group, tdm))
+
+    def warmup(self, n):
+        _check(load().cthyb_batch_warmup(self.h, int(n)))
+
+    def measure(self, nmeas):
+        _check(load().cthyb_batch_measure(self.h, int(nmeas)))
+
+    def reset_measurements(self):
+        _check(load().cthyb_batch_reset_measurements(self.h))
+
+    def sync(self):
+        _check(load().cthyb_batch_sync(self.h))
+
+    def stream(self):
+        s = C.c_void_p()
+        _check(load().cthyb_batch_stream(self.h, C.byref(s)))
+        return s.value
+
+    def use_graphs(self, on=True):
+        _check(load().cthyb_batch_use_graphs(self.h, 1 if on else 0))
+
+    # --- results
+    def results(self, chain):
+        g = self.groups[self._group_of[chain]]
+        nd, ns = self.model.nd, self.model.nstates
+        gt = np.zeros(nd * 2 * g.ntau)
+        ms = np.zeros(1)
+        dm = np.zeros(ns * ns)
+        hi = np.zeros(nd * 2 * g.maxhisto)
+        cnt = np.zeros(8, np.int64)
+        _check(load().cthyb_batch_results(self.h, chain, _dp(gt), _dp(ms), _dp(dm), _dp(hi),
+                                          cnt.ctypes.data_as(C.POINTER(C.c_int64))))
+        return dict(gtau=gt.reshape((nd, 2, g.ntau), order="F"), mean_sign=float(ms[0]),
+                    densitymatrix=dm.reshape((ns, ns), order="F"),
+                    histo=hi.reshape((nd, 2, g.maxhisto), order="F"),
+                    counters=dict(zip(("try_add", "acc_add", "try_rem", "acc_rem", "qn_add",
+                                       "qn_rem", "cnt_meas", "proposals"), cnt.tolist())))
+
+    def group_sums(self, group):
+        g = self.groups[group]
+        nd = self.model.nd
+        gs = np.zeros(nd * 2 * g.ntau)
+        ss = np.zeros(1)
+        cn = np.zeros(1, np.int64)
+        _check(load().cthyb_batch_group_sums(self.h, group, _dp(gs), _dp(ss),
+                                             cn.ctypes.data_as(C.POINTER(C.c_int64))))
+        return gs.reshape((nd, 2, g.ntau), order="F"), float(ss[0]), int(cn[0])
+
+    def state(self, chain):
+        out = np.zeros(16)
+        _check(load().cthyb_batch_state(self.h, chain, _dp(out)))
+        keys = ("trace_log", "trace_sign", "det_log", "det_sign", "cfgsign", "npairs",
+                "outer_sst", "window_position", "num_windows", "noper", "tauwin_min",
+                "tauwin_max", "taudiff_max", "nslide", "status", "k0")
+        return dict(zip(keys, out.tolist()))
+
+    def get_config(self, chain):
+        g = self.groups[self._group_of[chain]]
+        cap = max(1, int(self.state(chain)["noper"]))
+        t = np.zeros(cap)
+        o = np.zeros(cap, np.int32)
+        s = np.zeros(cap, np.int32)
+        c = np.zeros(cap, np.int32)
+        n = C.c_int()
+        out = C.c_int()
+        _check(load().cthyb_batch_get_config(self.h, chain, C.byref(n), _dp(t), _ip(o), _ip(s),
+                                             _ip(c), C.byref(out)))
+        k = n.value
+        return t[:k], o[:k], s[:k], c[:k], out.value
+
+    def set_config(self, chain, taus, orbs, spins, cas, outer_sst):
+        t = np.ascontiguousarray(taus, np.float64)
+        o = np.ascontiguousarray(orbs, np.int32)
+        s = np.ascontiguousarray(spins, np.int32)
+        c = np.ascontiguousarray(cas, np.int32)
+        _check(load().cthyb_batch_set_config(self.h, chain, len(t), _dp(t), _ip(o), _ip(s),
+                                             _ip(c), int(outer_sst)))
+
+    def minv(self, chain, f):
+        k = C.c_int()
+        _check(load().cthyb_batch_minv(self.h, chain, f, C.byref(k), None))
+        out = np.zeros(max(k.value, 1) ** 2)
+        _check(load().cthyb_batch_minv(self.h, chain, f, C.byref(k), _dp(out)))
+        return out[:k.value ** 2].reshape((k.value, k.value), order="F")
+
+    def refresh_minv(self, replace=False):
+        d = np.zeros(1)
+        _check(load().cthyb_batch_refresh_minv(self.h, 1 if replace else 0, _dp(d)))
+        return float(d[0])
+
+    def set_log(self, cap):
+        _check(load().cthyb_batch_set_log(self.h, int(cap)))
+        self._logcap = int(cap)
+
+    def log(self, chain):
+        n = C.c_int64()
+        _check(load().cthyb_batch_get_log(self.h, chain, None, C.byref(n)))
+        m = min(n.value, self._logcap)
+        rec = np.zeros(m, RECORD_DTYPE)
+        if m:
+            _check(load().cthyb_batch_get_log(self.h, chain, rec.ctypes.data, C.byref(n)))
+        return rec
+
+    def work_counters(self, reset=False):
+        out = np.zeros(8, np.int64)
+        _check(load().cthyb_batch_work_counters(self.h, out.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                1 if reset else 0))
+        return dict(zip(("m_bytes", "m_flops", "op_bytes", "tree_nodes", "proposals",
+                         "accepted", "r6", "r7"), out.tolist()))
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().cthyb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -153,5 +153,5 @@ def config_problem(name, beta=None):
 
 # Chemical potentials fixed by hand for the named fillings (the reference
 # driver refuses a mu search in single-shot mode, cthyb:125-126).
-DD3_MU = 1.3
-K5_MU = 8.0
+DD3_MU = 3.3
+K5_MU = 9.8
