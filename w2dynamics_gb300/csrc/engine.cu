@@ -1824,6 +1824,29 @@ __global__ void __launch_bounds__(WPB * 32) k_refresh(const __grid_constant__ DM
   }
 }
 
+// Sum of the G(tau) accumulators, signs and measurement counts over the
+// chains of a group (one thread per bin, chains strided).
+__global__ void k_group_sum(const __grid_constant__ DGroup g, int nbins, double* out, double* sign_out,
+                            long long* cnt_out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < nbins) {
+    double acc = 0.0;
+    for (int c = 0; c < g.nchains; ++c) acc += ((const double*)(g.base + (size_t)c * g.stride + g.o_gtau))[i];
+    out[i] = acc;
+  }
+  if (i == 0) {
+    double ss = 0.0;
+    long long cn = 0;
+    for (int c = 0; c < g.nchains; ++c) {
+      const Hdr* h = (const Hdr*)(g.base + (size_t)c * g.stride + g.o_hdr);
+      ss += h->meas_sign;
+      cn += h->cnt_meas;
+    }
+    *sign_out = ss;
+    *cnt_out = cn;
+  }
+}
+
 __global__ void k_set_window(const __grid_constant__ DModel m, const __grid_constant__ DGroup g, double tdm) {
   __shared__ Hdr hs[WPB];
   int warp = threadIdx.x >> 5;
@@ -1895,6 +1918,8 @@ struct cthyb_batch_s {
   int use_graphs = 0;
   long long logcap = 0;
   bool counters_reset_pending = false;
+  double* d_red = nullptr;
+  std::vector<double> red_host;
 };
 
 extern "C" {
@@ -2154,6 +2179,7 @@ int cthyb_batch_destroy(cthyb_batch_t B) {
   cudaFree(B->slab);
   cudaFree(B->d_err);
   cudaFree(B->d_dev);
+  if (B->d_red) cudaFree(B->d_red);
   if (B->stream) cudaStreamDestroy(B->stream);
   delete B;
   return CTHYB_OK;
@@ -2354,25 +2380,25 @@ int cthyb_batch_group_sums(cthyb_batch_t B, int group, double* gsum, double* sig
   if (!B || group < 0 || group >= (int)B->groups.size()) return fail(CTHYB_ERR_ARG, "bad group");
   GroupHost& G = B->groups[group];
   const HostModel& hm = B->model->hm;
-  CK(cudaStreamSynchronize(B->stream));
-  const int nt = G.g.ntau, nf = hm.nf;
-  std::vector<double> raw((size_t)nf * nt);
-  if (gsum) std::memset(gsum, 0, sizeof(double) * raw.size());
-  double ss = 0;
-  long long cn = 0;
-  for (int c = 0; c < G.desc.nchains; ++c) {
-    char* base = G.g.base + (size_t)c * G.g.stride;
-    Hdr h;
-    CK(cudaMemcpy(&h, base + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost));
-    ss += h.meas_sign;
-    cn += h.cnt_meas;
-    if (gsum) {
-      CK(cudaMemcpy(raw.data(), base + G.g.o_gtau, raw.size() * 8, cudaMemcpyDeviceToHost));
-      for (int f = 0; f < nf; ++f)
-        for (int t = 0; t < nt; ++t) gsum[(f / 2) + hm.nd * ((f % 2) + 2 * (size_t)t)] += raw[(size_t)f * nt + t];
-    }
+  const int nt = G.g.ntau, nf = hm.nf, nbins = nf * nt;
+  if ((int)B->red_host.size() < nbins + 2) {
+    if (B->d_red) cudaFree(B->d_red);
+    B->d_red = nullptr;
+    CK(cudaMalloc(&B->d_red, (size_t)(nbins + 2) * 8));
+    B->red_host.assign(nbins + 2, 0.0);
   }
-  if (sign_sum) *sign_sum = ss;
+  k_group_sum<<<(nbins + 255) / 256, 256, 0, B->stream>>>(G.g, nbins, B->d_red, B->d_red + nbins,
+                                                          (long long*)(B->d_red + nbins + 1));
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(B->red_host.data(), B->d_red, (size_t)(nbins + 2) * 8, cudaMemcpyDeviceToHost, B->stream));
+  CK(cudaStreamSynchronize(B->stream));
+  const double* raw = B->red_host.data();
+  if (gsum)
+    for (int f = 0; f < nf; ++f)
+      for (int t = 0; t < nt; ++t) gsum[(f / 2) + hm.nd * ((f % 2) + 2 * (size_t)t)] = raw[(size_t)f * nt + t];
+  if (sign_sum) *sign_sum = raw[nbins];
+  long long cn;
+  std::memcpy(&cn, &raw[nbins + 1], 8);
   if (cnt) *cnt = cn;
   return CTHYB_OK;
 }
