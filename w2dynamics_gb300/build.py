@@ -35,19 +35,23 @@ def _stale():
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False):
-    if not force and not _stale():
+def build(force=False, verbose=False, out=None, defines=()):
+    """Compile the engine; `out`/`defines` build a variant (e.g. another
+    SWEEP_MIN_BLOCKS register budget) next to the default library."""
+    lib = out or LIB
+    if out is None and not force and not _stale():
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nvcc(), "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo",
            "-std=c++17", "-Xcompiler", "-fPIC", "-shared", "-o", tmp,
+           *[f"-D{d}" for d in defines],
            os.path.join(CSRC, "engine.cu"), os.path.join(CSRC, "model.cpp")]
     if verbose:
         print(" ".join(cmd))
     subprocess.check_call(cmd)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

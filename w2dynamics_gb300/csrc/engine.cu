@@ -52,13 +52,14 @@ struct Ctx {
   char* tree;
   unsigned char* act;
   double* scr;
-  double* btau;
-  int* bcode;
+  double* btau[2];
+  int* bcode[2];
   double* gtau;
   double* histo;
   double* dm;
   double* dense;
   cthyb_record* log;
+  cthyb_record* rec;  // per-warp record under construction (shared memory)
   int lane, mti, mono, kcap, chain;
 };
 
@@ -170,14 +171,23 @@ __device__ void mt_seed(uint32_t* mt, uint32_t seed, int lane) {
 }
 
 // ---------------------------------------------------------------------------
-// Warp 32-ary searches on sorted double arrays.
+// Warp 32-ary searches on sorted arrays of non-negative doubles.  For
+// x >= 0 the IEEE-754 order equals the order of the bit patterns read as
+// signed 64-bit integers, so the comparisons run on the integer pipes
+// (exact, and FP64 throughput on GB300 is scarce).
+__device__ __forceinline__ long long tkey(double x) {
+  long long b = __double_as_longlong(x);
+  return b == (long long)0x8000000000000000ll ? 0ll : b;  // -0.0 -> +0.0
+}
 // first index i in [0,n) with !(a[i] < x)   (lower bound)
-__device__ int wlb(const double* a, int n, double x, int lane) {
+__device__ int wlb(const double* ad, int n, double x, int lane) {
+  const long long* a = (const long long*)ad;
+  const long long xb = tkey(x);
   int lo = 0, hi = n;
   while (hi - lo > 32) {
     int step = (hi - lo + 31) >> 5;
     int p = lo + lane * step;
-    bool pr = (p < hi) && (a[p] < x);
+    bool pr = (p < hi) && (a[p] < xb);
     int cnt = __popc(__ballot_sync(FULL, pr));
     if (cnt == 0) {
       hi = lo;
@@ -189,18 +199,20 @@ __device__ int wlb(const double* a, int n, double x, int lane) {
   }
   if (hi > lo) {
     int p = lo + lane;
-    bool pr = (p < hi) && (a[p] < x);
+    bool pr = (p < hi) && (a[p] < xb);
     lo += __popc(__ballot_sync(FULL, pr));
   }
   return lo;
 }
 // first index i with a[i] > x   (upper bound)
-__device__ int wub(const double* a, int n, double x, int lane) {
+__device__ int wub(const double* ad, int n, double x, int lane) {
+  const long long* a = (const long long*)ad;
+  const long long xb = tkey(x);
   int lo = 0, hi = n;
   while (hi - lo > 32) {
     int step = (hi - lo + 31) >> 5;
     int p = lo + lane * step;
-    bool pr = (p < hi) && (a[p] <= x);
+    bool pr = (p < hi) && (a[p] <= xb);
     int cnt = __popc(__ballot_sync(FULL, pr));
     if (cnt == 0) {
       hi = lo;
@@ -212,30 +224,35 @@ __device__ int wub(const double* a, int n, double x, int lane) {
   }
   if (hi > lo) {
     int p = lo + lane;
-    bool pr = (p < hi) && (a[p] <= x);
+    bool pr = (p < hi) && (a[p] <= xb);
     lo += __popc(__ballot_sync(FULL, pr));
   }
   return lo;
 }
 // sequential (single-thread) versions for per-lane use
-__device__ __forceinline__ int slb(const double* a, int n, double x) {
+__device__ __forceinline__ int slb(const double* ad, int n, double x) {
+  const long long* a = (const long long*)ad;
+  const long long xb = tkey(x);
   int lo = 0, hi = n;
   while (lo < hi) {
     int mid = (lo + hi) >> 1;
-    if (a[mid] < x) lo = mid + 1;
+    if (a[mid] < xb) lo = mid + 1;
     else hi = mid;
   }
   return lo;
 }
-__device__ __forceinline__ int sub(const double* a, int n, double x) {
+__device__ __forceinline__ int sub(const double* ad, int n, double x) {
+  const long long* a = (const long long*)ad;
+  const long long xb = tkey(x);
   int lo = 0, hi = n;
   while (lo < hi) {
     int mid = (lo + hi) >> 1;
-    if (a[mid] <= x) lo = mid + 1;
+    if (a[mid] <= xb) lo = mid + 1;
     else hi = mid;
   }
   return lo;
 }
+__device__ __forceinline__ bool teq(double a, double b) { return tkey(a) == tkey(b); }
 
 // ---------------------------------------------------------------------------
 // Hybridisation function: get_HybrF, Trace.F90:1014-1033, with the
@@ -249,7 +266,7 @@ __device__ __forceinline__ double hybrf(const Ctx& c, double tau, int f) {
   } else {
     sig = 1.0;
   }
-  double n = __dmul_rn(__ddiv_rn(tau, g.beta), (double)(g.nftau - 1));
+  double n = tau * g.hscale;  // tau / beta * (Nftau - 1)
   int i = (int)n;
   if (i > g.nftau - 2) i = g.nftau - 2;
   if (i < 0) i = 0;
@@ -343,46 +360,26 @@ __device__ int count_npairs(Ctx& c) {
 __device__ double config_sign(Ctx& c) {
   Hdr& h = *c.h;
   const int K = h.K, nf = c.m->nf;
-  int chunk = (K + 31) >> 5;
-  int lo = min(K, c.lane * chunk), hi = min(K, lo + chunk);
-  int hist[NFMAX];
+  const unsigned lt = (1u << c.lane) - 1u;
+  int run[NFMAX];
 #pragma unroll
-  for (int g = 0; g < NFMAX; ++g) hist[g] = 0;
-  for (int i = lo; i < hi; ++i) {
-    int f = c.opcode[i] >> 1;
-#pragma unroll
-    for (int g = 0; g < NFMAX; ++g) hist[g] += (f == g);
-  }
-  int pre[NFMAX], tot[NFMAX];
-#pragma unroll
-  for (int g = 0; g < NFMAX; ++g) {
-    int x = hist[g];
-    // inclusive scan
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(FULL, x, o);
-      if (c.lane >= o) x += y;
-    }
-    tot[g] = __shfl_sync(FULL, x, 31);
-    pre[g] = x - hist[g];
-  }
+  for (int g = 0; g < NFMAX; ++g) run[g] = 0;
   int inv = 0, alt = 0;
-  for (int i = lo; i < hi; ++i) {
-    int code = c.opcode[i], f = code >> 1, ca = code & 1;
-    // operators before i with a larger flavour index: inversions of the
-    // (time, flavour) order
+  for (int base = 0; base < K; base += 32) {
+    int i = base + c.lane;
+    int code = i < K ? c.opcode[i] : -2;
+    int f = code >> 1;
+    bool cre = i < K && (code & 1) == 0;
 #pragma unroll
-    for (int g = 0; g < NFMAX; ++g)
-      if (g > f && g < nf) inv += pre[g];
-#pragma unroll
-    for (int g = 0; g < NFMAX; ++g)
-      if (g == f) pre[g] += 1;
-    if (ca == 0) {
-      int after = 0;
-#pragma unroll
-      for (int g = 0; g < NFMAX; ++g)
-        if (g == f) after = tot[g] - pre[g];
-      alt += after;
+    for (int g = 0; g < NFMAX; ++g) {
+      if (g >= nf) break;
+      unsigned msk = __ballot_sync(FULL, f == g);
+      int before = run[g] + __popc(msk & lt);  // operators of flavour g before i
+      if (i < K) {
+        if (g > f) inv += before;
+        if (g == f && cre) alt += 2 * h.k[g] - before - 1;  // of flavour g after i
+      }
+      run[g] += __popc(msk);
     }
   }
   inv = wsumi(inv & 1) & 1;
@@ -400,6 +397,7 @@ struct Mod {
   int c1, c2;       // inserted codes
   int ix, iy;       // removed indices (ix < iy)
   int b1, b2;       // affected leaves
+  int n1, n2;       // gathered operator counts of leaves b1, b2 (buffers 0, 1)
 };
 
 __device__ __forceinline__ double bin_edge(const Ctx& c, int j) {
@@ -407,11 +405,12 @@ __device__ __forceinline__ double bin_edge(const Ctx& c, int j) {
 }
 __device__ __forceinline__ int bin_of(const Ctx& c, double t) {
   const int nb = 1 << c.g->L;
-  int j = (int)(t / c.g->beta * (double)nb);
+  int j = (int)(t * c.g->binscale);  // first guess, corrected against the edges
   if (j < 0) j = 0;
   if (j > nb - 1) j = nb - 1;
-  while (j < nb - 1 && bin_edge(c, j + 1) <= t) ++j;
-  while (j > 0 && bin_edge(c, j) > t) --j;
+  const long long tb = tkey(t);
+  while (j < nb - 1 && tkey(bin_edge(c, j + 1)) <= tb) ++j;
+  while (j > 0 && tkey(bin_edge(c, j)) > tb) --j;
   return j;
 }
 __device__ __forceinline__ char* node_base(const Ctx& c, int n, int slot) {
@@ -441,7 +440,9 @@ __device__ __forceinline__ int node_slot(const Ctx& c, const Mod& md, int n) {
 
 // Gather the operators of bin b of the proposed configuration into
 // btau/bcode; returns their number.
-__device__ int gather_bin(Ctx& c, const Mod& md, int b) {
+__device__ int gather_bin(Ctx& c, const Mod& md, int b, int buf) {
+  double* btau = c.btau[buf];
+  int* bcode = c.bcode[buf];
   const int K = c.h->K;
   const int nb = 1 << c.g->L;
   double e0 = bin_edge(c, b), e1 = b + 1 < nb ? bin_edge(c, b + 1) : 0.0;
@@ -464,8 +465,8 @@ __device__ int gather_bin(Ctx& c, const Mod& md, int b) {
       if (j == md.ix || j == md.iy) continue;
       r -= (md.ix >= lo && md.ix < j) + (md.iy >= lo && md.iy < j);
     }
-    c.btau[r] = t;
-    c.bcode[r] = code;
+    btau[r] = t;
+    bcode[r] = code;
   }
   int n = hi - lo - nrem;
   if (md.type == 1) {
@@ -475,12 +476,12 @@ __device__ int gather_bin(Ctx& c, const Mod& md, int b) {
     if (in2) p2 = wlb(c.optau + lo, hi - lo, md.t2, c.lane) + (in1 ? 1 : 0);
     if (c.lane == 0) {
       if (in1) {
-        c.btau[p1] = md.t1;
-        c.bcode[p1] = md.c1;
+        btau[p1] = md.t1;
+        bcode[p1] = md.c1;
       }
       if (in2) {
-        c.btau[p2] = md.t2;
-        c.bcode[p2] = md.c2;
+        btau[p2] = md.t2;
+        bcode[p2] = md.c2;
       }
     }
     n += in1 + in2;
@@ -490,14 +491,16 @@ __device__ int gather_bin(Ctx& c, const Mod& md, int b) {
 }
 
 // Leaf of bin b from the gathered operators (n of them), written to `slot`.
-__device__ void build_leaf(Ctx& c, int b, int n, int slot, bool states) {
+__device__ void build_leaf(Ctx& c, int b, int n, int slot, bool states, int buf) {
   const DModel& m = *c.m;
+  const double* btau = c.btau[buf];
+  const int* bcode = c.bcode[buf];
   const int L = c.g->L, nb = 1 << L, node = nb + b;
   int16_t* ss = node_ss(c, node, slot);
   for (int s = c.lane; s < m.nss; s += 32) {
     int cur = s;
     for (int j = 0; j < n && cur >= 0; ++j) {
-      int code = c.bcode[j];
+      int code = bcode[j];
       cur = m.connect[((size_t)cur * m.nf + (code >> 1)) * 2 + (code & 1)];
     }
     ss[s] = (int16_t)cur;
@@ -511,9 +514,9 @@ __device__ void build_leaf(Ctx& c, int b, int n, int slot, bool states) {
       double l = 0.0, t = t0;
       int neg = 0;
       for (int j = 0; j < n; ++j) {
-        double tj = c.btau[j];
+        double tj = btau[j];
         l -= (m.eval[cur] - m.egs) * (tj - t);
-        size_t idx = (size_t)c.bcode[j] * m.ns + cur;
+        size_t idx = (size_t)bcode[j] * m.ns + cur;
         int nx = m.mono_tgt[idx];
         if (nx < 0) {
           cur = -1;
@@ -576,14 +579,14 @@ __device__ void combine(Ctx& c, int n, int sl, int sr, int slot, bool states) {
 }
 
 // Rebuild the leaves of a proposal and their ancestors in the inactive slots.
-__device__ void tree_propose(Ctx& c, const Mod& md, bool states) {
+__device__ void tree_propose(Ctx& c, Mod& md, bool states, bool gather) {
   const int L = c.g->L, nb = 1 << L;
-  int n = gather_bin(c, md, md.b1);
-  build_leaf(c, md.b1, n, 1 - c.act[nb + md.b1], states);
-  if (md.b2 != md.b1) {
-    n = gather_bin(c, md, md.b2);
-    build_leaf(c, md.b2, n, 1 - c.act[nb + md.b2], states);
+  if (gather) {
+    md.n1 = gather_bin(c, md, md.b1, 0);
+    md.n2 = md.b2 != md.b1 ? gather_bin(c, md, md.b2, 1) : md.n1;
   }
+  build_leaf(c, md.b1, md.n1, 1 - c.act[nb + md.b1], states, 0);
+  if (md.b2 != md.b1) build_leaf(c, md.b2, md.n2, 1 - c.act[nb + md.b2], states, 1);
   for (int d = L - 1; d >= 0; --d) {
     int n1 = (nb + md.b1) >> (L - d), n2 = (nb + md.b2) >> (L - d);
     combine(c, n1, node_slot(c, md, 2 * n1), node_slot(c, md, 2 * n1 + 1), 1 - c.act[n1], states);
@@ -608,8 +611,8 @@ __device__ void tree_build_all(Ctx& c) {
   Mod md;
   md.type = 0;
   for (int b = 0; b < nb; ++b) {
-    int n = gather_bin(c, md, b);
-    build_leaf(c, b, n, 0, true);
+    int n = gather_bin(c, md, b, 0);
+    build_leaf(c, b, n, 0, true, 0);
   }
   for (int n = nb - 1; n >= 1; --n) combine(c, n, 0, 0, 0, true);
   for (int i = c.lane; i < 2 * nb; i += 32) c.act[i] = 0;
@@ -646,32 +649,28 @@ __device__ int old_prefix(Ctx& c, int s, double t) {
 }
 // Superstate at beta reached from superstate s just before time t through
 // the proposed configuration's operators at times >= t.
+// t is the later member of the proposal, so its leaf is md.b2 whose
+// operators tree_propose gathered already.
 __device__ int new_suffix(Ctx& c, const Mod& md, int s, double t) {
   const int L = c.g->L, nb = 1 << L;
   const DModel& m = *c.m;
-  int b = bin_of(c, t);
-  int n = gather_bin(c, md, b);
+  const int b = md.b2;
+  const int buf = md.b2 != md.b1 ? 1 : 0;
+  const int n = md.b2 != md.b1 ? md.n2 : md.n1;
+  const long long tb = tkey(t);
   for (int j = 0; j < n && s >= 0; ++j) {
-    if (c.btau[j] < t) continue;
-    int code = c.bcode[j];
+    if (tkey(c.btau[buf][j]) < tb) continue;
+    int code = c.bcode[buf][j];
     s = m.connect[((size_t)s * m.nf + (code >> 1)) * 2 + (code & 1)];
   }
-  // right siblings along the root-to-leaf path, deepest first
-  int path[24];
-  int np = 0;
-  int node = 1, lo = 0, span = nb;
-  for (int d = 0; d < L; ++d) {
-    int half = span >> 1;
-    if (b >= lo + half) {
-      node = 2 * node + 1;
-      lo += half;
-    } else {
-      path[np++] = 2 * node + 1;
-      node = 2 * node;
-    }
-    span = half;
+  // right siblings of the left-child nodes on the leaf-to-root path, deepest
+  // (earliest in time) first
+  for (int d = L; d >= 1 && s >= 0; --d) {
+    int node = (nb + b) >> (L - d);
+    if (node & 1) continue;
+    int sib = node | 1;
+    s = node_ss(c, sib, node_slot(c, md, sib))[s];
   }
-  for (int i = np - 1; i >= 0 && s >= 0; --i) s = node_ss(c, path[i], node_slot(c, md, path[i]))[s];
   return s;
 }
 
@@ -910,6 +909,7 @@ __device__ void ops_remove2(Ctx& c, int ix, int iy) {
 // ---------------------------------------------------------------------------
 // Proposal log record
 __device__ void write_record(Ctx& c, const cthyb_record& r) {
+  __syncwarp();
   if (c.log && c.lane == 0) {
     Hdr& h = *c.h;
     if (h.logn < c.g->logcap) c.log[h.logn] = r;
@@ -919,9 +919,9 @@ __device__ void write_record(Ctx& c, const cthyb_record& r) {
 }
 
 // Trace of the proposed configuration for outer superstate s0.
-__device__ void proposed_trace(Ctx& c, const Mod& md, int s0, double& lg, double& sg) {
+__device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& lg, double& sg) {
   if (c.mono) {
-    tree_propose(c, md, true);
+    tree_propose(c, md, true, false);
     root_trace(c, 1 - c.act[1], s0, lg, sg);
   } else {
     dense_trace(c, md, s0, lg, sg);
@@ -935,8 +935,9 @@ __device__ void step_add(Ctx& c, bool change_outer) {
   const DModel& m = *c.m;
   if (c.lane == 0) h.try_add++;
   __syncwarp();
-  cthyb_record r;
-  memset(&r, 0, sizeof(r));
+  cthyb_record& r = *c.rec;
+  for (int i = c.lane; i < (int)(sizeof(cthyb_record) / 4); i += 32) ((int*)&r)[i] = 0;
+  __syncwarp();
   r.move = 0;
   r.change_outer = change_outer;
   // pair_OperAdd, Trace.F90:3657-3702
@@ -964,7 +965,7 @@ __device__ void step_add(Ctx& c, bool change_outer) {
   // process_OperAdd: equal times are rejected (Trace.F90:4292-4407)
   int pa = wlb(c.optau, K, tau_a, c.lane);
   int pc = wlb(c.optau, K, tau_c, c.lane);
-  bool eq = (tau_a == tau_c) || (pa < K && c.optau[pa] == tau_a) || (pc < K && c.optau[pc] == tau_c);
+  bool eq = teq(tau_a, tau_c) || (pa < K && teq(c.optau[pa], tau_a)) || (pc < K && teq(c.optau[pc], tau_c));
   if (eq) {
     if (c.lane == 0) h.qn_add++;
     r.outcome = 0;
@@ -989,7 +990,7 @@ __device__ void step_add(Ctx& c, bool change_outer) {
   md.b2 = bin_of(c, md.t2);
   int p1 = a_first ? pa : pc, p2 = a_first ? pc : pa;
   // quantum-number check (CTQMC.F90:3421-3470)
-  tree_propose(c, md, false);
+  tree_propose(c, md, false, true);
   int root_new = 1 - c.act[1];
   int s0 = h.outer_sst, snew = s0;
   bool ok;
@@ -1181,8 +1182,9 @@ __device__ void step_rem(Ctx& c, bool change_outer) {
   const DModel& m = *c.m;
   if (c.lane == 0) h.try_rem++;
   __syncwarp();
-  cthyb_record r;
-  memset(&r, 0, sizeof(r));
+  cthyb_record& r = *c.rec;
+  for (int i = c.lane; i < (int)(sizeof(cthyb_record) / 4); i += 32) ((int*)&r)[i] = 0;
+  __syncwarp();
   r.move = 1;
   r.change_outer = change_outer;
   r.outer_sst = h.outer_sst;
@@ -1250,7 +1252,7 @@ __device__ void step_rem(Ctx& c, bool change_outer) {
   const double ty = srt_ptr(c, f, 1 - cax)[yrank];
   const int iy = wlb(c.optau, K, ty, c.lane);
   const int xrank = wlb(srt_ptr(c, f, cax), k, tx, c.lane);
-  if (iy <= ix || iy >= K || c.optau[iy] != ty || xrank >= k || srt_ptr(c, f, cax)[xrank] != tx) {
+  if (iy <= ix || iy >= K || !teq(c.optau[iy], ty) || xrank >= k || !teq(srt_ptr(c, f, cax)[xrank], tx)) {
     set_status(c, ST_INTERNAL);
     return;
   }
@@ -1277,7 +1279,7 @@ __device__ void step_rem(Ctx& c, bool change_outer) {
   md.c1 = md.c2 = 0;
   md.b1 = bin_of(c, tx);
   md.b2 = bin_of(c, ty);
-  tree_propose(c, md, false);
+  tree_propose(c, md, false, true);
   int root_new = 1 - c.act[1];
   int s0 = h.outer_sst, snew = s0;
   bool ok;
@@ -1496,8 +1498,9 @@ __device__ void measure(Ctx& c) {
 
 // ---------------------------------------------------------------------------
 // Kernels
-__device__ Ctx make_ctx(const DModel* m, const DGroup* g, Hdr* hsm, int chain) {
+__device__ Ctx make_ctx(const DModel* m, const DGroup* g, Hdr* hsm, int chain, cthyb_record* rec = nullptr) {
   Ctx c;
+  c.rec = rec;
   c.m = m;
   c.g = g;
   c.h = hsm;
@@ -1514,8 +1517,10 @@ __device__ Ctx make_ctx(const DModel* m, const DGroup* g, Hdr* hsm, int chain) {
   c.tree = b + g->o_tree;
   c.act = (unsigned char*)(b + g->o_act);
   c.scr = (double*)(b + g->o_scr);
-  c.btau = c.scr + 4 * g->kcap;
-  c.bcode = (int*)(c.btau + g->opcap + 2);
+  c.btau[0] = c.scr + 4 * g->kcap;
+  c.btau[1] = c.btau[0] + g->opcap + 2;
+  c.bcode[0] = (int*)(c.btau[1] + g->opcap + 2);
+  c.bcode[1] = c.bcode[0] + g->opcap + 2;
   c.gtau = (double*)(b + g->o_gtau);
   c.histo = (double*)(b + g->o_histo);
   c.dm = (double*)(b + g->o_dm);
@@ -1527,6 +1532,9 @@ __device__ Ctx make_ctx(const DModel* m, const DGroup* g, Hdr* hsm, int chain) {
 }
 
 constexpr int WPB = 4;  // warps (chains) per block
+#ifndef SWEEP_MIN_BLOCKS
+#define SWEEP_MIN_BLOCKS 8  // resident blocks per SM the register budget aims for
+#endif
 
 __device__ __forceinline__ void load_hdr(Hdr* dst, const Hdr* src, int lane) {
   const int n = sizeof(Hdr) / 4;
@@ -1596,13 +1604,20 @@ __global__ void __launch_bounds__(WPB * 32) k_init(const __grid_constant__ DMode
   store_hdr((Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr), &h, c.lane);
 }
 
-__global__ void __launch_bounds__(WPB * 32) k_sweep(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
-                                                   long long nprop, int nmeas, int reset) {
+// One launch advances every chain of every group: warp -> (group, chain).
+__global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
+    k_sweep(const __grid_constant__ DModel m, const DGroup* __restrict__ groups, int ngroups, int ntotal,
+            long long nprop, int nmeas, int reset) {
   __shared__ Hdr hs[WPB];
+  __shared__ cthyb_record recs[WPB];
   int warp = threadIdx.x >> 5;
-  int chain = blockIdx.x * WPB + warp;
-  if (chain >= g.nchains) return;
-  Ctx c = make_ctx(&m, &g, &hs[warp], chain);
+  int gchain = blockIdx.x * WPB + warp;
+  if (gchain >= ntotal) return;
+  int gi = 0;
+  while (gi + 1 < ngroups && gchain >= groups[gi + 1].chain0) ++gi;
+  const DGroup& g = groups[gi];
+  int chain = gchain - g.chain0;
+  Ctx c = make_ctx(&m, &g, &hs[warp], chain, &recs[warp]);
   Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
   load_hdr(c.h, gh, c.lane);
   Hdr& h = *c.h;
@@ -1920,7 +1935,16 @@ struct cthyb_batch_s {
   bool counters_reset_pending = false;
   double* d_red = nullptr;
   std::vector<double> red_host;
+  DGroup* d_groups = nullptr;
 };
+
+static int upload_groups(cthyb_batch_s* B) {
+  std::vector<DGroup> gs;
+  for (GroupHost& G : B->groups) gs.push_back(G.g);
+  if (!B->d_groups) CK(cudaMalloc(&B->d_groups, sizeof(DGroup) * gs.size()));
+  CK(cudaMemcpy(B->d_groups, gs.data(), sizeof(DGroup) * gs.size(), cudaMemcpyHostToDevice));
+  return CTHYB_OK;
+}
 
 extern "C" {
 
@@ -2026,6 +2050,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   const int nf = hm.nf;
   g.nchains = d.nchains;
   g.beta = d.beta;
+  g.hscale = (double)(d.nftau - 1) / d.beta;
   g.nftau = d.nftau;
   g.ntau = d.ntau;
   g.ncorr = d.ncorr > 0 ? d.ncorr : 100;
@@ -2045,6 +2070,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   }
   if (L > 16) L = 16;
   g.L = L;
+  g.binscale = (double)(1 << L) / d.beta;
   const bool mono = hm.monomial && !g.dense;
   size_t nb = mono ? (size_t)hm.ns * 10 : 0;
   nb += (size_t)hm.nss * 2;
@@ -2072,7 +2098,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.o_act = off;
   off = align_up(off + nodes, 256);
   g.o_scr = off;
-  off = align_up(off + (size_t)(4 * kcap + opcap + 2) * 8 + (size_t)(opcap + 2) * 4, 256);
+  off = align_up(off + (size_t)(4 * kcap + 2 * (opcap + 2)) * 8 + (size_t)2 * (opcap + 2) * 4, 256);
   g.o_gtau = off;
   off = align_up(off + (size_t)nf * d.ntau * 8, 256);
   g.o_histo = off;
@@ -2109,6 +2135,7 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
     }
     layout_group(B, G, 0);
     G.chain0 = B->nchains;
+    G.g.chain0 = G.chain0;
     B->nchains += G.desc.nchains;
     total += (size_t)G.desc.nchains * G.g.stride;
   }
@@ -2163,6 +2190,10 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
     cthyb_batch_destroy(B);
     return fail(CTHYB_ERR_CUDA, std::string("init: ") + cudaGetErrorString(e));
   }
+  if (int rc = upload_groups(B)) {
+    cthyb_batch_destroy(B);
+    return rc;
+  }
   *out = B;
   return CTHYB_OK;
 }
@@ -2180,6 +2211,7 @@ int cthyb_batch_destroy(cthyb_batch_t B) {
   cudaFree(B->d_err);
   cudaFree(B->d_dev);
   if (B->d_red) cudaFree(B->d_red);
+  if (B->d_groups) cudaFree(B->d_groups);
   if (B->stream) cudaStreamDestroy(B->stream);
   delete B;
   return CTHYB_OK;
@@ -2209,11 +2241,10 @@ int cthyb_batch_set_taudiffmax(cthyb_batch_t B, int group, double tdm) {
 }
 
 static int launch_sweeps(cthyb_batch_t B, long long nprop, int nmeas, int reset) {
-  for (GroupHost& G : B->groups) {
-    int nblk = (G.desc.nchains + WPB - 1) / WPB;
-    k_sweep<<<nblk, WPB * 32, 0, B->stream>>>(B->model->dm, G.g, nprop, nmeas, reset);
-    CK(cudaGetLastError());
-  }
+  int nblk = (B->nchains + WPB - 1) / WPB;
+  k_sweep<<<nblk, WPB * 32, 0, B->stream>>>(B->model->dm, B->d_groups, (int)B->groups.size(), B->nchains, nprop,
+                                            nmeas, reset);
+  CK(cudaGetLastError());
   return CTHYB_OK;
 }
 
@@ -2557,7 +2588,7 @@ int cthyb_batch_set_log(cthyb_batch_t B, int64_t cap) {
   cudaFree(B->slab);
   B->slab = slab;
   B->logcap = cap;
-  return CTHYB_OK;
+  return upload_groups(B);
 }
 
 int cthyb_batch_get_log(cthyb_batch_t B, int chain, void* rec, int64_t* n) {

@@ -49,8 +49,8 @@ struct Hdr {
 };
 
 struct DGroup {
-  int nchains;
-  double beta;
+  int nchains, chain0;
+  double beta, hscale, binscale;  // hscale = (nftau - 1) / beta, binscale = 2^L / beta
   int nftau;
   const double* hybr;  // [nf][nftau]
   int ntau, ncorr, maxhisto;

@@ -51,7 +51,7 @@ _lib = None
 
 
 def library_path():
-    return _build.LIB
+    return os.environ.get("CTHYB_GPU_LIB", _build.LIB)
 
 
 def load(build_if_missing=False):
@@ -59,8 +59,8 @@ def load(build_if_missing=False):
     global _lib
     if _lib is not None:
         return _lib
-    path = _build.LIB
-    if build_if_missing:
+    path = library_path()
+    if build_if_missing and path == _build.LIB:
         _build.build()
     if not os.path.exists(path):
         raise EngineError(f"{path} not built: run `python -m w2dynamics_gb300.build`")
