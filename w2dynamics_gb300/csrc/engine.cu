@@ -36,6 +36,15 @@
 
 namespace cthyb {
 
+// Code size of the proposal path decides performance: with ~30 warps per SM
+// at different points of a fully inlined path the instruction cache
+// thrashes, so the larger building blocks exist once.
+#ifdef CTHYB_INLINE_ALL
+#define NOINL __forceinline__
+#else
+#define NOINL __noinline__
+#endif
+
 // ---------------------------------------------------------------------------
 // Chain context (all lanes hold the same values).
 struct Ctx {
@@ -105,7 +114,7 @@ __device__ __forceinline__ int wsumi(int x) {
 // generate_canonical with two 32-bit draws, the bounded integer Lemire's
 // nearly-divisionless method (ACM TOMACS 29(1), 2019) -- the algorithms of
 // the standard library used by src/mtrng/random.cc.
-__device__ void mt_twist(uint32_t* mt, int lane) {
+__device__ NOINL void mt_twist(uint32_t* mt, int lane) {
   for (int base = 0; base < 624; base += 32) {
     int i = base + lane;
     bool on = i < 624;
@@ -180,7 +189,7 @@ __device__ __forceinline__ long long tkey(double x) {
   return b == (long long)0x8000000000000000ll ? 0ll : b;  // -0.0 -> +0.0
 }
 // first index i in [0,n) with !(a[i] < x)   (lower bound)
-__device__ int wlb(const double* ad, int n, double x, int lane) {
+__device__ NOINL int wlb(const double* ad, int n, double x, int lane) {
   const long long* a = (const long long*)ad;
   const long long xb = tkey(x);
   int lo = 0, hi = n;
@@ -205,7 +214,7 @@ __device__ int wlb(const double* ad, int n, double x, int lane) {
   return lo;
 }
 // first index i with a[i] > x   (upper bound)
-__device__ int wub(const double* ad, int n, double x, int lane) {
+__device__ NOINL int wub(const double* ad, int n, double x, int lane) {
   const long long* a = (const long long*)ad;
   const long long xb = tkey(x);
   int lo = 0, hi = n;
@@ -277,7 +286,7 @@ __device__ __forceinline__ double hybrf(const Ctx& c, double tau, int f) {
 
 // ---------------------------------------------------------------------------
 // Window (Trace.F90:1608-1754)
-__device__ void set_window_bounds(Ctx& c) {
+__device__ NOINL void set_window_bounds(Ctx& c) {
   Hdr& h = *c.h;
   if (c.lane == 0 && h.num_windows > 1) {
     h.tauwin_min = __dmul_rn(__ddiv_rn((double)h.window_position, (double)(h.num_windows + 1)), c.g->beta);
@@ -285,7 +294,7 @@ __device__ void set_window_bounds(Ctx& c) {
   }
   __syncwarp();
 }
-__device__ void init_window(Ctx& c, double tdm) {
+__device__ NOINL void init_window(Ctx& c, double tdm) {
   Hdr& h = *c.h;
   if (c.lane == 0) {
     h.window_position = 0;
@@ -305,7 +314,7 @@ __device__ void init_window(Ctx& c, double tdm) {
   }
   __syncwarp();
 }
-__device__ void shift_window(Ctx& c) {
+__device__ NOINL void shift_window(Ctx& c) {
   Hdr& h = *c.h;
   if (h.num_windows > 1) {
     if (c.lane == 0) {
@@ -337,7 +346,7 @@ __device__ __forceinline__ int cnt_earlier(const double* opp, int n, double t, d
   int a = slb(opp, n, lo), b = slb(opp, n, t);
   return b > a ? b - a : 0;
 }
-__device__ int count_npairs(Ctx& c) {
+__device__ NOINL int count_npairs(Ctx& c) {
   Hdr& h = *c.h;
   int K = h.K;
   int start = wlb(c.optau, K, h.tauwin_min, c.lane);
@@ -357,7 +366,7 @@ __device__ int count_npairs(Ctx& c) {
 // operators after it whose flavour index 2b+s is smaller; permaltca counts
 // for each creator the operators of its flavour after it, plus one if the
 // number of pairs is odd.
-__device__ double config_sign(Ctx& c) {
+__device__ NOINL double config_sign(Ctx& c) {
   Hdr& h = *c.h;
   const int K = h.K, nf = c.m->nf;
   const unsigned lt = (1u << c.lane) - 1u;
@@ -440,7 +449,7 @@ __device__ __forceinline__ int node_slot(const Ctx& c, const Mod& md, int n) {
 
 // Gather the operators of bin b of the proposed configuration into
 // btau/bcode; returns their number.
-__device__ int gather_bin(Ctx& c, const Mod& md, int b, int buf) {
+__device__ NOINL int gather_bin(Ctx& c, const Mod& md, int b, int buf) {
   double* btau = c.btau[buf];
   int* bcode = c.bcode[buf];
   const int K = c.h->K;
@@ -491,7 +500,7 @@ __device__ int gather_bin(Ctx& c, const Mod& md, int b, int buf) {
 }
 
 // Leaf of bin b from the gathered operators (n of them), written to `slot`.
-__device__ void build_leaf(Ctx& c, int b, int n, int slot, bool states, int buf) {
+__device__ NOINL void build_leaf(Ctx& c, int b, int n, int slot, bool states, int buf) {
   const DModel& m = *c.m;
   const double* btau = c.btau[buf];
   const int* bcode = c.bcode[buf];
@@ -515,7 +524,7 @@ __device__ void build_leaf(Ctx& c, int b, int n, int slot, bool states, int buf)
       int neg = 0;
       for (int j = 0; j < n; ++j) {
         double tj = btau[j];
-        l -= (m.eval[cur] - m.egs) * (tj - t);
+        l -= m.evs[cur] * (tj - t);
         size_t idx = (size_t)bcode[j] * m.ns + cur;
         int nx = m.mono_tgt[idx];
         if (nx < 0) {
@@ -528,7 +537,7 @@ __device__ void build_leaf(Ctx& c, int b, int n, int slot, bool states, int buf)
         t = tj;
       }
       if (cur >= 0) {
-        l -= (m.eval[cur] - m.egs) * (t1 - t);
+        l -= m.evs[cur] * (t1 - t);
         tg[s] = (uint16_t)(cur | (neg << 15));
         lw[s] = l;
       } else {
@@ -541,7 +550,7 @@ __device__ void build_leaf(Ctx& c, int b, int n, int slot, bool states, int buf)
 }
 
 // Combine the children of node n into `slot` of n.
-__device__ void combine(Ctx& c, int n, int sl, int sr, int slot, bool states) {
+__device__ NOINL void combine(Ctx& c, int n, int sl, int sr, int slot, bool states) {
   const DModel& m = *c.m;
   const int16_t* ssl = node_ss(c, 2 * n, sl);
   const int16_t* ssr = node_ss(c, 2 * n + 1, sr);
@@ -579,7 +588,7 @@ __device__ void combine(Ctx& c, int n, int sl, int sr, int slot, bool states) {
 }
 
 // Rebuild the leaves of a proposal and their ancestors in the inactive slots.
-__device__ void tree_propose(Ctx& c, Mod& md, bool states, bool gather) {
+__device__ NOINL void tree_propose(Ctx& c, Mod& md, bool states, bool gather) {
   const int L = c.g->L, nb = 1 << L;
   if (gather) {
     md.n1 = gather_bin(c, md, md.b1, 0);
@@ -621,7 +630,7 @@ __device__ void tree_build_all(Ctx& c) {
 
 // Superstate just before time t in the current configuration, starting from
 // s at tau = 0.
-__device__ int old_prefix(Ctx& c, int s, double t) {
+__device__ NOINL int old_prefix(Ctx& c, int s, double t) {
   const int L = c.g->L, nb = 1 << L;
   const DModel& m = *c.m;
   int b = bin_of(c, t);
@@ -651,7 +660,7 @@ __device__ int old_prefix(Ctx& c, int s, double t) {
 // the proposed configuration's operators at times >= t.
 // t is the later member of the proposal, so its leaf is md.b2 whose
 // operators tree_propose gathered already.
-__device__ int new_suffix(Ctx& c, const Mod& md, int s, double t) {
+__device__ NOINL int new_suffix(Ctx& c, const Mod& md, int s, double t) {
   const int L = c.g->L, nb = 1 << L;
   const DModel& m = *c.m;
   const int b = md.b2;
@@ -676,7 +685,7 @@ __device__ int new_suffix(Ctx& c, const Mod& md, int s, double t) {
 
 // Trace of superstate s0 from the root state map in `slot`:
 // sum over states i of s0 mapped onto themselves of sign*exp(lw).
-__device__ void root_trace(Ctx& c, int slot, int s0, double& lg, double& sg) {
+__device__ NOINL void root_trace(Ctx& c, int slot, int s0, double& lg, double& sg) {
   const DModel& m = *c.m;
   const double* lw = node_lw(c, 1, slot);
   const uint16_t* tg = node_tg(c, 1, slot);
@@ -732,7 +741,7 @@ __device__ __forceinline__ bool next_op(const Ctx& c, const Mod& md, OpIter& it,
     return true;
   }
 }
-__device__ void dense_trace(Ctx& c, const Mod& md, int s0, double& lg, double& sg) {
+__device__ NOINL void dense_trace(Ctx& c, const Mod& md, int s0, double& lg, double& sg) {
   const DModel& m = *c.m;
   const int ld = m.nsmax;
   double* X = c.dense;
@@ -815,7 +824,7 @@ __device__ void dense_trace(Ctx& c, const Mod& md, int s0, double& lg, double& s
 // Shifts of the sorted arrays
 
 // insert value/slot at position p of a sorted array with n entries
-__device__ void arr_insert(Ctx& c, double* a, short* sl, int n, int p, double v, short s) {
+__device__ NOINL void arr_insert(Ctx& c, double* a, short* sl, int n, int p, double v, short s) {
   for (int base = n - 1; base >= p; base -= 32) {
     int i = base - c.lane;
     bool on = i >= p;
@@ -838,7 +847,7 @@ __device__ void arr_insert(Ctx& c, double* a, short* sl, int n, int p, double v,
   }
   __syncwarp();
 }
-__device__ void arr_remove(Ctx& c, double* a, short* sl, int n, int p) {
+__device__ NOINL void arr_remove(Ctx& c, double* a, short* sl, int n, int p) {
   for (int base = p + 1; base < n; base += 32) {
     int i = base + c.lane;
     bool on = i < n;
@@ -858,7 +867,7 @@ __device__ void arr_remove(Ctx& c, double* a, short* sl, int n, int p) {
 }
 // global operator array: insert t1 (before old index p1) and t2 (before old
 // index p2, p2 >= p1)
-__device__ void ops_insert2(Ctx& c, int p1, int p2, double t1, int c1, double t2, int c2) {
+__device__ NOINL void ops_insert2(Ctx& c, int p1, int p2, double t1, int c1, double t2, int c2) {
   int K = c.h->K;
   for (int base = K - 1; base >= p1; base -= 32) {
     int i = base - c.lane;
@@ -885,7 +894,7 @@ __device__ void ops_insert2(Ctx& c, int p1, int p2, double t1, int c1, double t2
   }
   __syncwarp();
 }
-__device__ void ops_remove2(Ctx& c, int ix, int iy) {
+__device__ NOINL void ops_remove2(Ctx& c, int ix, int iy) {
   int K = c.h->K;
   for (int base = ix + 1; base < K; base += 32) {
     int i = base + c.lane;
@@ -908,7 +917,7 @@ __device__ void ops_remove2(Ctx& c, int ix, int iy) {
 
 // ---------------------------------------------------------------------------
 // Proposal log record
-__device__ void write_record(Ctx& c, const cthyb_record& r) {
+__device__ NOINL void write_record(Ctx& c, const cthyb_record& r) {
   __syncwarp();
   if (c.log && c.lane == 0) {
     Hdr& h = *c.h;
@@ -930,7 +939,7 @@ __device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& lg, double& sg) 
 
 // ---------------------------------------------------------------------------
 // StepAdd, CTQMC.F90:3353-3613 (diagonal hybridisation).
-__device__ void step_add(Ctx& c, bool change_outer) {
+__device__ NOINL void step_add(Ctx& c, bool change_outer) {
   Hdr& h = *c.h;
   const DModel& m = *c.m;
   if (c.lane == 0) h.try_add++;
@@ -1177,7 +1186,7 @@ __device__ void step_add(Ctx& c, bool change_outer) {
 
 // ---------------------------------------------------------------------------
 // StepRem, CTQMC.F90:3892-4151 (diagonal hybridisation).
-__device__ void step_rem(Ctx& c, bool change_outer) {
+__device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   Hdr& h = *c.h;
   const DModel& m = *c.m;
   if (c.lane == 0) h.try_rem++;
@@ -1431,7 +1440,7 @@ __device__ void one_step(Ctx& c) {
 
 // ---------------------------------------------------------------------------
 // Measurements after each NCorr block (CTQMC.F90:8541-8566)
-__device__ void measure(Ctx& c) {
+__device__ NOINL void measure(Ctx& c) {
   Hdr& h = *c.h;
   const DModel& m = *c.m;
   const DGroup& g = *c.g;
@@ -1482,9 +1491,9 @@ __device__ void measure(Ctx& c) {
         double ta = tas[j];
         int idt;
         if (ta - tc > 0.0) {
-          idt = (int)((ta - tc) / g.beta * (double)nt) + 1;
+          idt = (int)((ta - tc) * g.gscale) + 1;  // (ta - tc) / beta * Ntau
         } else {
-          idt = (int)((g.beta + ta - tc) / g.beta * (double)nt) + 1;
+          idt = (int)((g.beta + ta - tc) * g.gscale) + 1;
           Mv = -Mv;
         }
         Mv = Mv * h.cfgsign;
@@ -1989,6 +1998,11 @@ static int model_upload(cthyb_model_t M) {
   d.sst_off = up(hm.sst_off);
   d.connect = up(hm.connect);
   d.eval = up(hm.eval);
+  {
+    std::vector<double> evs(hm.ns);
+    for (int i = 0; i < hm.ns; ++i) evs[i] = hm.eval[i] - hm.egs;
+    d.evs = up(evs);
+  }
   d.mono_tgt = up(hm.mono_tgt);
   d.mono_lv = up(hm.mono_lv);
   d.mono_neg = up(hm.mono_neg);
@@ -2051,6 +2065,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.nchains = d.nchains;
   g.beta = d.beta;
   g.hscale = (double)(d.nftau - 1) / d.beta;
+  g.gscale = (double)d.ntau / d.beta;
   g.nftau = d.nftau;
   g.ntau = d.ntau;
   g.ncorr = d.ncorr > 0 ? d.ncorr : 100;

@@ -26,6 +26,7 @@ struct DModel {
   const int* sst_off;          // [nss]
   const int* connect;          // [nss][nf][2]
   const double* eval;          // [ns]
+  const double* evs;           // [ns] eval - egs
   const int* mono_tgt;         // [2nf][ns]
   const double* mono_lv;       // [2nf][ns]
   const unsigned char* mono_neg;
@@ -50,7 +51,7 @@ struct Hdr {
 
 struct DGroup {
   int nchains, chain0;
-  double beta, hscale, binscale;  // hscale = (nftau - 1) / beta, binscale = 2^L / beta
+  double beta, hscale, binscale, gscale;  // (nftau-1)/beta, 2^L/beta, ntau/beta
   int nftau;
   const double* hybr;  // [nf][nftau]
   int ntau, ncorr, maxhisto;
