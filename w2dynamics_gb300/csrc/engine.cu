@@ -62,6 +62,7 @@ struct Ctx {
   unsigned char* act;
   double* scr;
   double* btau[2];
+  double* bdt[2];  // time steps before each gathered operator and to the bin end
   int* bcode[2];
   double* gtau;
   double* histo;
@@ -69,7 +70,11 @@ struct Ctx {
   double* dense;
   cthyb_record* log;
   cthyb_record* rec;  // per-warp record under construction (shared memory)
-  int lane, mti, mono, kcap, chain;
+  int lane, mono, kcap, chain;
+  // next tempered generator outputs: lane i holds output mtbase + i;
+  // mtpos is the next unread position, mtcnt the valid count
+  uint32_t mtbuf;
+  int mtbase, mtpos, mtcnt;
 };
 
 __device__ __forceinline__ double* srt_ptr(const Ctx& c, int f, int ca) {
@@ -132,26 +137,45 @@ __device__ NOINL void mt_twist(uint32_t* mt, int lane) {
     __syncwarp();
   }
 }
-__device__ __forceinline__ uint32_t mt_next(Ctx& c) {
-  if (c.mti >= 624) {
-    mt_twist(c.mt, c.lane);
-    c.mti = 0;
-  }
-  uint32_t y = c.mt[c.mti];
-  c.mti++;
+__device__ __forceinline__ uint32_t mt_temper(uint32_t y) {
   y ^= y >> 11;
   y ^= (y << 7) & 0x9d2c5680u;
   y ^= (y << 15) & 0xefc60000u;
   y ^= y >> 18;
   return y;
 }
+// Load the 32 outputs starting at state index `from` (twisting first when
+// the state is exhausted) into the lanes' buffer.
+__device__ NOINL void mt_refill(Ctx& c, int from) {
+  if (from >= 624) {
+    mt_twist(c.mt, c.lane);
+    from = 0;
+  }
+  c.mtbase = from;
+  c.mtcnt = min(32, 624 - from);
+  c.mtpos = 0;
+  int i = from + c.lane;
+  c.mtbuf = i < 624 ? mt_temper(c.mt[i]) : 0u;
+}
+__device__ __forceinline__ uint32_t mt_next(Ctx& c) {
+  if (c.mtpos >= c.mtcnt) mt_refill(c, c.mtbase + c.mtcnt);
+  uint32_t y = __shfl_sync(FULL, c.mtbuf, c.mtpos);
+  c.mtpos++;
+  return y;
+}
+// generator position (index of the next output) for the chain header
+__device__ __forceinline__ int mt_index(const Ctx& c) { return c.mtbase + c.mtpos; }
 __device__ __forceinline__ double grnd(Ctx& c) {
   uint32_t a = mt_next(c);
   uint32_t b = mt_next(c);
-  double s = __dadd_rn((double)a, __dmul_rn((double)b, 4294967296.0));
-  double r = s * 0x1p-64;
-  if (r >= 1.0) r = 0x1.fffffffffffffp-1;
-  return r;
+  // generate_canonical: RN(a + b 2^32) / 2^64.  a + b 2^32 is the 64-bit
+  // integer v, so one correctly rounded u64->f64 conversion gives the sum,
+  // and the scaling by 2^-64 is an exponent shift (exact, v >= 1).
+  unsigned long long v = ((unsigned long long)b << 32) | a;
+  if (v == 0ull) return 0.0;
+  long long bits = __double_as_longlong(__ull2double_rn(v)) - (64ll << 52);
+  if (bits >= 0x3FF0000000000000ll) bits = 0x3FEFFFFFFFFFFFFFll;  // 1.0 -> nextafter(1, 0)
+  return __longlong_as_double(bits);
 }
 __device__ __forceinline__ int randint(Ctx& c, int lo, int hi) {
   uint32_t range = (uint32_t)(hi - lo) + 1u;
@@ -268,20 +292,18 @@ __device__ __forceinline__ bool teq(double a, double b) { return tkey(a) == tkey
 // reference's operation order and no fused multiply-adds.
 __device__ __forceinline__ double hybrf(const Ctx& c, double tau, int f) {
   const DGroup& g = *c.g;
-  double sig;
-  if (tau < 0.0) {
-    tau = __dadd_rn(tau, g.beta);
-    sig = -1.0;
-  } else {
-    sig = 1.0;
-  }
+  // tau is a difference of distinct times, never -0.0, so the sign bit
+  // decides the antiperiodic branch
+  const long long neg = __double_as_longlong(tau) & (long long)0x8000000000000000ll;
+  if (neg) tau = tau + g.beta;
   double n = tau * g.hscale;  // tau / beta * (Nftau - 1)
-  int i = (int)n;
-  if (i > g.nftau - 2) i = g.nftau - 2;
-  if (i < 0) i = 0;
+  int in = (int)n;
+  double fr = n - (double)in;
+  int i = min(max(in, 0), g.nftau - 2);
   const double* F = g.hybr + (size_t)f * g.nftau;
-  double f0 = F[i], f1 = F[i + 1];
-  return __dmul_rn(sig, __dadd_rn(f0, __dmul_rn(__dsub_rn(n, (double)(int)n), __dsub_rn(f1, f0))));
+  double f0 = __ldg(F + i), f1 = __ldg(F + i + 1);
+  double v = fma(fr, f1 - f0, f0);
+  return __longlong_as_double(__double_as_longlong(v) ^ neg);
 }
 
 // ---------------------------------------------------------------------------
@@ -496,17 +518,27 @@ __device__ NOINL int gather_bin(Ctx& c, const Mod& md, int b, int buf) {
     n += in1 + in2;
   }
   __syncwarp();
+  // time steps: before operator j from the previous one (bin start for j=0),
+  // and from the last operator to the bin end (index n)
+  double* bdt = c.bdt[buf];
+  double t1 = b + 1 < nb ? e1 : c.g->beta;
+  for (int j = c.lane; j <= n; j += 32) {
+    double prev = j > 0 ? btau[j - 1] : e0;
+    double cur = j < n ? btau[j] : t1;
+    bdt[j] = cur - prev;
+  }
+  __syncwarp();
   return n;
 }
 
-// Leaf of bin b from the gathered operators (n of them), written to `slot`.
-__device__ NOINL void build_leaf(Ctx& c, int b, int n, int slot, bool states, int buf) {
+// Leaf of bin b from the gathered operators (n of them), written to `slot`:
+// superstate map (do_ss) and/or state map (do_states).
+__device__ __forceinline__ void leaf_body(Ctx& c, int b, int n, int slot, bool do_ss, bool do_states, int buf) {
   const DModel& m = *c.m;
-  const double* btau = c.btau[buf];
   const int* bcode = c.bcode[buf];
   const int L = c.g->L, nb = 1 << L, node = nb + b;
   int16_t* ss = node_ss(c, node, slot);
-  for (int s = c.lane; s < m.nss; s += 32) {
+  for (int s = c.lane; do_ss && s < m.nss; s += 32) {
     int cur = s;
     for (int j = 0; j < n && cur >= 0; ++j) {
       int code = bcode[j];
@@ -514,17 +546,16 @@ __device__ NOINL void build_leaf(Ctx& c, int b, int n, int slot, bool states, in
     }
     ss[s] = (int16_t)cur;
   }
-  if (states && c.mono) {
-    double t0 = bin_edge(c, b), t1 = b + 1 < nb ? bin_edge(c, b + 1) : c.g->beta;
+  if (do_states && c.mono) {
+    const double* bdt = c.bdt[buf];
     double* lw = node_lw(c, node, slot);
     uint16_t* tg = node_tg(c, node, slot);
     for (int s = c.lane; s < m.ns; s += 32) {
       int cur = s;
-      double l = 0.0, t = t0;
+      double l = 0.0;
       int neg = 0;
       for (int j = 0; j < n; ++j) {
-        double tj = btau[j];
-        l -= m.evs[cur] * (tj - t);
+        l = fma(-m.evs[cur], bdt[j], l);
         size_t idx = (size_t)bcode[j] * m.ns + cur;
         int nx = m.mono_tgt[idx];
         if (nx < 0) {
@@ -534,10 +565,9 @@ __device__ NOINL void build_leaf(Ctx& c, int b, int n, int slot, bool states, in
         l += m.mono_lv[idx];
         neg ^= m.mono_neg[idx];
         cur = nx;
-        t = tj;
       }
       if (cur >= 0) {
-        l -= m.evs[cur] * (t1 - t);
+        l = fma(-m.evs[cur], bdt[n], l);
         tg[s] = (uint16_t)(cur | (neg << 15));
         lw[s] = l;
       } else {
@@ -550,16 +580,16 @@ __device__ NOINL void build_leaf(Ctx& c, int b, int n, int slot, bool states, in
 }
 
 // Combine the children of node n into `slot` of n.
-__device__ NOINL void combine(Ctx& c, int n, int sl, int sr, int slot, bool states) {
+__device__ __forceinline__ void combine_body(Ctx& c, int n, int sl, int sr, int slot, bool do_ss, bool do_states) {
   const DModel& m = *c.m;
   const int16_t* ssl = node_ss(c, 2 * n, sl);
   const int16_t* ssr = node_ss(c, 2 * n + 1, sr);
   int16_t* ss = node_ss(c, n, slot);
-  for (int s = c.lane; s < m.nss; s += 32) {
+  for (int s = c.lane; do_ss && s < m.nss; s += 32) {
     int a = ssl[s];
     ss[s] = a < 0 ? (int16_t)-1 : ssr[a];
   }
-  if (states && c.mono) {
+  if (do_states && c.mono) {
     const double* lwl = node_lw(c, 2 * n, sl);
     const uint16_t* tgl = node_tg(c, 2 * n, sl);
     const double* lwr = node_lw(c, 2 * n + 1, sr);
@@ -587,19 +617,33 @@ __device__ NOINL void combine(Ctx& c, int n, int sl, int sr, int slot, bool stat
   __syncwarp();
 }
 
-// Rebuild the leaves of a proposal and their ancestors in the inactive slots.
+// Rebuild the leaves of a proposal and their ancestors in the inactive
+// slots: the superstate maps (states = false, first pass, gathers the
+// leaves' operators) or the state maps (states = true).
 __device__ NOINL void tree_propose(Ctx& c, Mod& md, bool states, bool gather) {
   const int L = c.g->L, nb = 1 << L;
+  const int nleaf = md.b2 != md.b1 ? 2 : 1;
   if (gather) {
-    md.n1 = gather_bin(c, md, md.b1, 0);
-    md.n2 = md.b2 != md.b1 ? gather_bin(c, md, md.b2, 1) : md.n1;
+    for (int q = 0; q < nleaf; ++q) {
+      int n = gather_bin(c, md, q ? md.b2 : md.b1, q);
+      if (q) md.n2 = n;
+      else md.n1 = n;
+    }
+    if (nleaf == 1) md.n2 = md.n1;
   }
-  build_leaf(c, md.b1, md.n1, 1 - c.act[nb + md.b1], states, 0);
-  if (md.b2 != md.b1) build_leaf(c, md.b2, md.n2, 1 - c.act[nb + md.b2], states, 1);
+  for (int q = 0; q < nleaf; ++q) {
+    int b = q ? md.b2 : md.b1;
+    leaf_body(c, b, q ? md.n2 : md.n1, 1 - c.act[nb + b], !states, states, q);
+  }
+  int n1 = nb + md.b1, n2 = nb + md.b2;
   for (int d = L - 1; d >= 0; --d) {
-    int n1 = (nb + md.b1) >> (L - d), n2 = (nb + md.b2) >> (L - d);
-    combine(c, n1, node_slot(c, md, 2 * n1), node_slot(c, md, 2 * n1 + 1), 1 - c.act[n1], states);
-    if (n2 != n1) combine(c, n2, node_slot(c, md, 2 * n2), node_slot(c, md, 2 * n2 + 1), 1 - c.act[n2], states);
+    n1 >>= 1;
+    n2 >>= 1;
+    const int cnt = n2 != n1 ? 2 : 1;
+    for (int q = 0; q < cnt; ++q) {
+      int n = q ? n2 : n1;
+      combine_body(c, n, node_slot(c, md, 2 * n), node_slot(c, md, 2 * n + 1), 1 - c.act[n], !states, states);
+    }
   }
   if (c.lane == 0) c.h->w_nodes += 2 * (L + 1);
 }
@@ -621,9 +665,9 @@ __device__ void tree_build_all(Ctx& c) {
   md.type = 0;
   for (int b = 0; b < nb; ++b) {
     int n = gather_bin(c, md, b, 0);
-    build_leaf(c, b, n, 0, true, 0);
+    leaf_body(c, b, n, 0, true, true, 0);
   }
-  for (int n = nb - 1; n >= 1; --n) combine(c, n, 0, 0, 0, true);
+  for (int n = nb - 1; n >= 1; --n) combine_body(c, n, 0, 0, 0, true, true);
   for (int i = c.lane; i < 2 * nb; i += 32) c.act[i] = 0;
   __syncwarp();
 }
@@ -685,7 +729,9 @@ __device__ NOINL int new_suffix(Ctx& c, const Mod& md, int s, double t) {
 
 // Trace of superstate s0 from the root state map in `slot`:
 // sum over states i of s0 mapped onto themselves of sign*exp(lw).
-__device__ NOINL void root_trace(Ctx& c, int slot, int s0, double& lg, double& sg) {
+// lg/sg: log|trace| and its sign; mx/sum: trace = sum * exp(mx) (the
+// acceptance ratio uses these without a logarithm).
+__device__ NOINL void root_trace(Ctx& c, int slot, int s0, double& mx_out, double& sum_out) {
   const DModel& m = *c.m;
   const double* lw = node_lw(c, 1, slot);
   const uint16_t* tg = node_tg(c, 1, slot);
@@ -697,8 +743,8 @@ __device__ NOINL void root_trace(Ctx& c, int slot, int s0, double& lg, double& s
   }
   mx = wmax(mx);
   if (mx == -DHUGE) {
-    lg = -DHUGE;
-    sg = 0.0;
+    mx_out = -DHUGE;
+    sum_out = 0.0;
     return;
   }
   double sum = 0.0;
@@ -707,9 +753,29 @@ __device__ NOINL void root_trace(Ctx& c, int slot, int s0, double& lg, double& s
     uint16_t t = tg[st];
     if ((t & 0x7fff) == st) sum += ((t & 0x8000) ? -1.0 : 1.0) * exp(lw[st] - mx);
   }
-  sum = wsum(sum);
-  lg = mx + log(fabs(sum));
-  sg = sum >= 0.0 ? 1.0 : -1.0;
+  mx_out = mx;
+  sum_out = wsum(sum);
+}
+__device__ __forceinline__ void trace_log(double mx, double sum, double& lg, double& sg) {
+  if (mx == -DHUGE) {
+    lg = -DHUGE;
+    sg = 0.0;
+  } else {
+    lg = mx + log(fabs(sum));
+    sg = sum >= 0.0 ? 1.0 : -1.0;
+  }
+}
+// |weight ratio| = |trace_new/trace_old| * |det ratio| from the mantissa/
+// exponent split of the new trace; logarithms only where the plain
+// product could over- or underflow.
+__device__ __forceinline__ double weight_ratio(double mx, double sum, double old_log, double absdet) {
+  if (mx == -DHUGE || sum == 0.0) return 0.0;
+  double e = mx - old_log;
+  if (e > -600.0 && e < 600.0) {
+    double w = exp(e) * fabs(sum) * absdet;
+    if (w > 1e-290 && w < 1e290) return w;
+  }
+  return exp(e + log(fabs(sum)) + log(absdet));
 }
 
 // ---------------------------------------------------------------------------
@@ -928,12 +994,13 @@ __device__ NOINL void write_record(Ctx& c, const cthyb_record& r) {
 }
 
 // Trace of the proposed configuration for outer superstate s0.
-__device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& lg, double& sg) {
+// Trace of the proposed configuration as sum * exp(mx).
+__device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum) {
   if (c.mono) {
     tree_propose(c, md, true, false);
-    root_trace(c, 1 - c.act[1], s0, lg, sg);
+    root_trace(c, 1 - c.act[1], s0, mx, sum);
   } else {
-    dense_trace(c, md, s0, lg, sg);
+    dense_trace(c, md, s0, mx, sum);  // log|trace| and its sign
   }
 }
 
@@ -1040,15 +1107,14 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
   double ratio = S - wsum(part);
   __syncwarp();
   double sig = ((fpos_c - fpos_a) & 1) ? -1.0 : 1.0;
-  double det_log = log(fabs(ratio));
   double det_sign = (ratio >= 0.0 ? 1.0 : -1.0) * sig;
   if (c.lane == 0) {
     h.w_mbytes += 8ll * k * k + 32ll * k;
     h.w_mflops += 2ll * k * k + 2ll * k;
   }
   // trace
-  double tr_lg, tr_sg;
-  proposed_trace(c, md, snew, tr_lg, tr_sg);
+  double tr_mx, tr_sum;
+  proposed_trace(c, md, snew, tr_mx, tr_sum);
   double rnd = grnd(c);
   // NPairs of the proposed configuration
   int np;
@@ -1104,13 +1170,15 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
     }
     np = h.npairs + __shfl_sync(FULL, n, 0);
   }
-  double trr_log = tr_lg - h.trace_log;
-  double wr = exp(__dadd_rn(trr_log, det_log));
-  double x = __dmul_rn(1.0, tdf);
-  x = __dmul_rn(x, (double)(2 * m.nd));
-  x = __ddiv_rn(x, (double)np);
-  x = __dmul_rn(x, wr);
+  double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(ratio));
+  double x = tdf * (double)(2 * m.nd) / (double)np * wr;
   double prob = fabs(x);
+  bool accept = rnd < prob;
+  double det_log = 0.0, tr_lg = 0.0, tr_sg = 0.0;
+  if (accept || c.log) {
+    det_log = log(fabs(ratio));
+    trace_log(tr_mx, tr_sum, tr_lg, tr_sg);
+  }
   r.det_log = det_log;
   r.det_sign = det_sign;
   r.tr_log = tr_lg;
@@ -1118,7 +1186,6 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
   r.prob = prob;
   r.rand = rnd;
   r.npairs = np;
-  bool accept = rnd < prob;
   if (accept) {
     if (k + 1 > c.kcap || K + 2 > c.g->opcap) {
       set_status(c, ST_CAPACITY);
@@ -1308,17 +1375,18 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   const double* Mf = M_ptr(c, f);
   double dr = Mf[(size_t)slot_a * c.kcap + slot_c];
   double sig = ((fpos_c - fpos_a) & 1) ? -1.0 : 1.0;
-  double det_log = log(fabs(dr));
   double det_sign = (dr >= 0.0 ? 1.0 : -1.0) * sig;
-  double tr_lg, tr_sg;
-  proposed_trace(c, md, snew, tr_lg, tr_sg);
-  double trr_log = tr_lg - h.trace_log;
-  double wr = exp(__dadd_rn(trr_log, det_log));
-  double x = __dmul_rn(1.0, hprf);
-  x = __ddiv_rn(x, (double)(2 * m.nd));
-  x = __dmul_rn(x, wr);
+  double tr_mx, tr_sum;
+  proposed_trace(c, md, snew, tr_mx, tr_sum);
+  double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(dr));
+  double x = hprf / (double)(2 * m.nd) * wr;
   double prob = fabs(x);
   double rnd = grnd(c);
+  double det_log = 0.0, tr_lg = 0.0, tr_sg = 0.0;
+  if (rnd < prob || c.log) {
+    det_log = log(fabs(dr));
+    trace_log(tr_mx, tr_sum, tr_lg, tr_sg);
+  }
   r.det_log = det_log;
   r.det_sign = det_sign;
   r.tr_log = tr_lg;
@@ -1528,7 +1596,9 @@ __device__ Ctx make_ctx(const DModel* m, const DGroup* g, Hdr* hsm, int chain, c
   c.scr = (double*)(b + g->o_scr);
   c.btau[0] = c.scr + 4 * g->kcap;
   c.btau[1] = c.btau[0] + g->opcap + 2;
-  c.bcode[0] = (int*)(c.btau[1] + g->opcap + 2);
+  c.bdt[0] = c.btau[1] + g->opcap + 2;
+  c.bdt[1] = c.bdt[0] + g->opcap + 3;
+  c.bcode[0] = (int*)(c.bdt[1] + g->opcap + 3);
   c.bcode[1] = c.bcode[0] + g->opcap + 2;
   c.gtau = (double*)(b + g->o_gtau);
   c.histo = (double*)(b + g->o_histo);
@@ -1575,7 +1645,7 @@ __global__ void __launch_bounds__(WPB * 32) k_init(const __grid_constant__ DMode
   }
   __syncwarp();
   mt_seed(c.mt, (uint32_t)seeds[chain], c.lane);
-  c.mti = 624;
+  mt_refill(c, 624);
   init_window(c, *tdm);
   if (c.lane == 0) {
     h.npairs = 0;
@@ -1599,8 +1669,11 @@ __global__ void __launch_bounds__(WPB * 32) k_init(const __grid_constant__ DMode
   __syncwarp();
   tree_build_all(c);
   double lg, sg;
-  if (c.mono) root_trace(c, 0, h.outer_sst, lg, sg);
-  else {
+  if (c.mono) {
+    double mx, sum;
+    root_trace(c, 0, h.outer_sst, mx, sum);
+    trace_log(mx, sum, lg, sg);
+  } else {
     Mod md;
     md.type = 0;
     dense_trace(c, md, h.outer_sst, lg, sg);
@@ -1608,7 +1681,7 @@ __global__ void __launch_bounds__(WPB * 32) k_init(const __grid_constant__ DMode
   if (c.lane == 0) {
     h.trace_log = lg;
     h.trace_sign = sg;
-    h.mt_idx = c.mti;
+    h.mt_idx = mt_index(c);
   }
   store_hdr((Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr), &h, c.lane);
 }
@@ -1630,7 +1703,7 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
   Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
   load_hdr(c.h, gh, c.lane);
   Hdr& h = *c.h;
-  c.mti = h.mt_idx;
+  mt_refill(c, h.mt_idx);
   if (reset && c.lane == 0) {  // init_counters, CTQMC.F90:847-899
     h.try_add = h.acc_add = h.try_rem = h.acc_rem = h.qn_add = h.qn_rem = 0;
     h.nprop = 0;
@@ -1647,7 +1720,7 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
     }
   }
   if (c.lane == 0) {
-    h.mt_idx = c.mti;
+    h.mt_idx = mt_index(c);
     if (h.status != ST_OK) atomicMax(g.err_flag, h.status);
   }
   store_hdr(gh, c.h, c.lane);
@@ -1777,7 +1850,6 @@ __global__ void __launch_bounds__(WPB * 32) k_set_config(const __grid_constant__
   Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
   load_hdr(c.h, gh, c.lane);
   Hdr& h = *c.h;
-  c.mti = h.mt_idx;
   const int K = h.K;
   // per-flavour sorted arrays, slot = rank
   for (int f = 0; f < m.nf; ++f) {
@@ -1806,8 +1878,11 @@ __global__ void __launch_bounds__(WPB * 32) k_set_config(const __grid_constant__
   __syncwarp();
   tree_build_all(c);
   double lg, sg;
-  if (c.mono) root_trace(c, 0, h.outer_sst, lg, sg);
-  else {
+  if (c.mono) {
+    double mx, sum;
+    root_trace(c, 0, h.outer_sst, mx, sum);
+    trace_log(mx, sum, lg, sg);
+  } else {
     Mod md;
     md.type = 0;
     dense_trace(c, md, h.outer_sst, lg, sg);
@@ -2113,7 +2188,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.o_act = off;
   off = align_up(off + nodes, 256);
   g.o_scr = off;
-  off = align_up(off + (size_t)(4 * kcap + 2 * (opcap + 2)) * 8 + (size_t)2 * (opcap + 2) * 4, 256);
+  off = align_up(off + (size_t)(4 * kcap + 2 * (opcap + 2) + 2 * (opcap + 3)) * 8 + (size_t)2 * (opcap + 2) * 4, 256);
   g.o_gtau = off;
   off = align_up(off + (size_t)nf * d.ntau * 8, 256);
   g.o_histo = off;
