@@ -45,6 +45,23 @@ namespace cthyb {
 #define NOINL __noinline__
 #endif
 
+#ifdef CTHYB_PROFILE
+#define PROF_START() long long prof_t0_ = clock64()
+#define PROF_MARK(i)                                      \
+  do {                                                    \
+    long long t_ = clock64();                             \
+    if (c.lane == 0) c.h->prof[i] += t_ - prof_t0_;       \
+    prof_t0_ = t_;                                        \
+  } while (0)
+#else
+#define PROF_START() \
+  do {               \
+  } while (0)
+#define PROF_MARK(i) \
+  do {               \
+  } while (0)
+#endif
+
 // ---------------------------------------------------------------------------
 // Chain context (all lanes hold the same values).
 struct Ctx {
@@ -1009,6 +1026,7 @@ __device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum)
 __device__ NOINL void step_add(Ctx& c, bool change_outer) {
   Hdr& h = *c.h;
   const DModel& m = *c.m;
+  PROF_START();
   if (c.lane == 0) h.try_add++;
   __syncwarp();
   cthyb_record& r = *c.rec;
@@ -1065,6 +1083,7 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
   md.b1 = bin_of(c, md.t1);
   md.b2 = bin_of(c, md.t2);
   int p1 = a_first ? pa : pc, p2 = a_first ? pc : pa;
+  PROF_MARK(1);
   // quantum-number check (CTQMC.F90:3421-3470)
   tree_propose(c, md, false, true);
   int root_new = 1 - c.act[1];
@@ -1077,6 +1096,7 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
     snew = inside >= 0 ? new_suffix(c, md, inside, md.t2) : -1;
     ok = snew >= 0 && node_ss(c, 1, root_new)[snew] == snew;
   }
+  PROF_MARK(2);
   if (!ok) {
     if (c.lane == 0) h.qn_add++;
     r.outcome = 1;
@@ -1106,6 +1126,7 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
   }
   double ratio = S - wsum(part);
   __syncwarp();
+  PROF_MARK(3);
   double sig = ((fpos_c - fpos_a) & 1) ? -1.0 : 1.0;
   double det_sign = (ratio >= 0.0 ? 1.0 : -1.0) * sig;
   if (c.lane == 0) {
@@ -1115,6 +1136,7 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
   // trace
   double tr_mx, tr_sum;
   proposed_trace(c, md, snew, tr_mx, tr_sum);
+  PROF_MARK(4);
   double rnd = grnd(c);
   // NPairs of the proposed configuration
   int np;
@@ -1186,6 +1208,7 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
   r.prob = prob;
   r.rand = rnd;
   r.npairs = np;
+  PROF_MARK(5);
   if (accept) {
     if (k + 1 > c.kcap || K + 2 > c.g->opcap) {
       set_status(c, ST_CAPACITY);
@@ -1222,6 +1245,7 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
     arr_insert(c, srt_ptr(c, f, 0), sslot_ptr(c, f, 0), k, fpos_c - 1, tau_c, (short)k);
     arr_insert(c, srt_ptr(c, f, 1), sslot_ptr(c, f, 1), k, fpos_a - 1, tau_a, (short)k);
     ops_insert2(c, p1, p2, md.t1, md.c1, md.t2, md.c2);
+    PROF_MARK(6);
     if (c.mono) tree_accept(c, md);
     else {
       tree_accept(c, md);
@@ -1242,6 +1266,7 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
     double sgn = config_sign(c);
     if (c.lane == 0) h.cfgsign = -sgn;
     __syncwarp();
+    PROF_MARK(7);
     r.outcome = 4;
   } else {
     r.outcome = 3;
@@ -1256,6 +1281,7 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
 __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   Hdr& h = *c.h;
   const DModel& m = *c.m;
+  PROF_START();
   if (c.lane == 0) h.try_rem++;
   __syncwarp();
   cthyb_record& r = *c.rec;
@@ -1355,6 +1381,7 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   md.c1 = md.c2 = 0;
   md.b1 = bin_of(c, tx);
   md.b2 = bin_of(c, ty);
+  PROF_MARK(8);
   tree_propose(c, md, false, true);
   int root_new = 1 - c.act[1];
   int s0 = h.outer_sst, snew = s0;
@@ -1376,8 +1403,10 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   double dr = Mf[(size_t)slot_a * c.kcap + slot_c];
   double sig = ((fpos_c - fpos_a) & 1) ? -1.0 : 1.0;
   double det_sign = (dr >= 0.0 ? 1.0 : -1.0) * sig;
+  PROF_MARK(2);
   double tr_mx, tr_sum;
   proposed_trace(c, md, snew, tr_mx, tr_sum);
+  PROF_MARK(4);
   double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(dr));
   double x = hprf / (double)(2 * m.nd) * wr;
   double prob = fabs(x);
@@ -1443,6 +1472,7 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
     }
     __syncwarp();
     ops_remove2(c, ix, iy);
+    PROF_MARK(6);
     tree_accept(c, md);
     if (c.lane == 0) {
       h.k[f] = k - 1;
@@ -1469,6 +1499,7 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
     double sgn = config_sign(c);
     if (c.lane == 0) h.cfgsign = -sgn;
     __syncwarp();
+    PROF_MARK(7);
     r.outcome = 4;
   } else {
     r.outcome = 3;
@@ -1481,6 +1512,7 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
 // One proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250),
 // percentages of global, tau-shift and 4-operator moves zero.
 __device__ void one_step(Ctx& c) {
+  PROF_START();
   Hdr& h = *c.h;
   for (int f = 0; f < c.m->nf; ++f)
     if (h.k[f] + 1 > c.kcap) {
@@ -1495,10 +1527,12 @@ __device__ void one_step(Ctx& c) {
   if (rn < 0.5) {
     grnd(c);  // Percentage4OperatorMove draw
     bool co = grnd(c) < c.g->p_outer;
+    PROF_MARK(0);
     step_add(c, co);
   } else {
     grnd(c);
     bool co = grnd(c) < c.g->p_outer;
+    PROF_MARK(0);
     step_rem(c, co);
   }
   if (c.lane == 0) h.nprop++;
@@ -1715,7 +1749,9 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
     } else {
       for (int im = 0; im < nmeas && h.status == ST_OK; ++im) {
         for (int ic = 0; ic < g.ncorr && h.status == ST_OK; ++ic) one_step(c);
+        PROF_START();
         if (h.status == ST_OK) measure(c);
+        PROF_MARK(9);
       }
     }
   }
@@ -2694,6 +2730,20 @@ int cthyb_batch_get_log(cthyb_batch_t B, int chain, void* rec, int64_t* n) {
   if (rec && m > 0)
     CK(cudaMemcpy(rec, G->g.base + (size_t)c * G->g.stride + G->g.o_log, (size_t)m * sizeof(cthyb_record),
                   cudaMemcpyDeviceToHost));
+  return CTHYB_OK;
+}
+
+// Phase cycle counters (builds with -DCTHYB_PROFILE), summed over chains.
+int cthyb_debug_phase_cycles(cthyb_batch_t B, int64_t* out10) {
+  if (!B || !out10) return fail(CTHYB_ERR_ARG, "null");
+  CK(cudaStreamSynchronize(B->stream));
+  for (int i = 0; i < 10; ++i) out10[i] = 0;
+  for (GroupHost& G : B->groups)
+    for (int c = 0; c < G.desc.nchains; ++c) {
+      Hdr h;
+      CK(cudaMemcpy(&h, G.g.base + (size_t)c * G.g.stride + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost));
+      for (int i = 0; i < 10; ++i) out10[i] += h.prof[i];
+    }
   return CTHYB_OK;
 }
 

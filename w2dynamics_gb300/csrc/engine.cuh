@@ -47,6 +47,8 @@ struct Hdr {
   int k[NFMAX];
   // work counters for the roofline: M bytes, M flops, op-array bytes, tree node updates
   long long w_mbytes, w_mflops, w_opbytes, w_nodes;
+  // cycles per proposal phase (only with -DCTHYB_PROFILE)
+  long long prof[10];
 };
 
 struct DGroup {
