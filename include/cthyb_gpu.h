@@ -159,6 +159,25 @@ typedef struct {
  * summed over all chains since the last reset (8 int64). */
 int cthyb_batch_work_counters(cthyb_batch_t batch, int64_t* out8, int reset);
 
+/* Allocation-free inverse hybridisation matrix of one flavour -- no
+ * counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (a solver whose device memory was fixed at start-up, a process whose
+ * memory belongs to another allocator, code that must not allocate between
+ * capturing and replaying its work): the elimination's two k x k work
+ * matrices live in a static device array of the library (1 MiB on every GPU
+ * that loads it, kept until exit), so k is limited to 256 and larger k is
+ * rejected with CTHYB_ERR_CAPACITY.  All pointers are caller-owned device
+ * memory: tau_c[k], tau_a[k] creator/annihilator times, ftau[nftau] F(tau)
+ * of the flavour on tau_j = j*beta/(nftau-1); outputs minv[k*k] (column-
+ * major, rows creators, columns annihilators, in the order of the inputs)
+ * and logdet[2] = log|det H|, sign of H(a,c) = F(tau_a - tau_c).
+ * Asynchronous on `stream` (cudaStream_t, NULL for the default stream).
+ * The first call on a device resolves the array's device address with that
+ * device current and should come before any stream capture.  Calls share
+ * the array: calls whose kernels overlap on the GPU race. */
+int cthyb_minv_rebuild_noalloc(int k, const double* tau_c, const double* tau_a, const double* ftau,
+                               int nftau, double beta, double* minv, double* logdet, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

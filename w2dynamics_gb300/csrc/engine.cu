@@ -2771,3 +2771,165 @@ int cthyb_batch_work_counters(cthyb_batch_t B, int64_t* out8, int reset) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free inverse hybridisation matrix.
+//
+// For callers that cannot call cudaMalloc -- a host already running inside a
+// fixed device-memory budget (a Fortran solver whose arrays were sized at
+// start-up, a process that hands all device memory to another framework's
+// caching allocator, or code that must not allocate between the capture and
+// the replay of its own work).  The two k x k work matrices of the
+// elimination live in one file-scope device array instead of in a chain
+// slab, so every GPU that loads this library holds it until the process
+// exits.  All calls share it: calls whose kernels overlap on the GPU race on
+// it, and it keeps the last call's contents (every call writes the full
+// k x k region it reads, so nothing stale is ever used).
+namespace cthyb {
+constexpr int NOALLOC_KMAX = 256;  // largest k accepted (2 * 256^2 doubles = 1 MiB)
+static __device__ __align__(256) double g_noalloc_scratch[2 * NOALLOC_KMAX * NOALLOC_KMAX];
+
+// One warp: H(a, c) = F(tau_a - tau_c) with the reference's interpolation
+// (get_HybrF, Trace.F90:1014-1033), Gauss-Jordan elimination with partial
+// pivoting on [H | 1] in the scratch array, M = H^{-1} written with rows =
+// creators and columns = annihilators, log|det H| and its sign.
+__global__ void k_minv_noalloc(double* scratch, int k, const double* __restrict__ tau_c,
+                               const double* __restrict__ tau_a, const double* __restrict__ F, int nftau,
+                               double beta, double* __restrict__ minv, double* __restrict__ logdet) {
+  const int lane = threadIdx.x & 31;
+  const int ld = k;
+  double* H = scratch;
+  double* I = scratch + (size_t)k * k;
+  const double hs = (double)(nftau - 1) / beta;
+  for (int e = lane; e < k * k; e += 32) {
+    int ia = e % k, ic = e / k;
+    double tau = tau_a[ia] - tau_c[ic];
+    double sig = 1.0;
+    if (tau < 0.0) {
+      tau += beta;
+      sig = -1.0;
+    }
+    double n = tau * hs;
+    int in = (int)n;
+    int i = min(max(in, 0), nftau - 2);
+    H[(size_t)ic * ld + ia] = sig * (F[i] + (n - (double)in) * (F[i + 1] - F[i]));
+    I[(size_t)ic * ld + ia] = (ia == ic) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  double dlog = 0.0, dsign = 1.0;
+  for (int j = 0; j < k; ++j) {
+    double best = -1.0;
+    int bi = j;
+    for (int i = j + lane; i < k; i += 32) {
+      double a = fabs(H[(size_t)j * ld + i]);
+      if (a > best) {
+        best = a;
+        bi = i;
+      }
+    }
+    for (int o = 16; o; o >>= 1) {
+      double ob = __shfl_xor_sync(FULL, best, o);
+      int oi = __shfl_xor_sync(FULL, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (best <= 0.0) {  // singular
+      if (lane == 0) {
+        logdet[0] = -DHUGE;
+        logdet[1] = 0.0;
+      }
+      return;
+    }
+    if (bi != j) {
+      for (int col = lane; col < k; col += 32) {
+        double t = H[(size_t)col * ld + j];
+        H[(size_t)col * ld + j] = H[(size_t)col * ld + bi];
+        H[(size_t)col * ld + bi] = t;
+        t = I[(size_t)col * ld + j];
+        I[(size_t)col * ld + j] = I[(size_t)col * ld + bi];
+        I[(size_t)col * ld + bi] = t;
+      }
+      dsign = -dsign;
+    }
+    __syncwarp();
+    double piv = H[(size_t)j * ld + j];
+    dlog += log(fabs(piv));
+    if (piv < 0) dsign = -dsign;
+    double ip = 1.0 / piv;
+    for (int col = lane; col < k; col += 32) {
+      H[(size_t)col * ld + j] *= ip;
+      I[(size_t)col * ld + j] *= ip;
+    }
+    __syncwarp();
+    for (int col = 0; col < k; ++col) {
+      if (col == j) continue;
+      double hj = H[(size_t)col * ld + j];
+      double ij = I[(size_t)col * ld + j];
+      for (int i = lane; i < k; i += 32) {
+        if (i == j) continue;
+        double fct = H[(size_t)j * ld + i];
+        H[(size_t)col * ld + i] -= fct * hj;
+        I[(size_t)col * ld + i] -= fct * ij;
+      }
+    }
+    __syncwarp();
+    for (int i = lane; i < k; i += 32)
+      if (i != j) {
+        I[(size_t)j * ld + i] -= H[(size_t)j * ld + i] * I[(size_t)j * ld + j];
+        H[(size_t)j * ld + i] = 0.0;
+      }
+    __syncwarp();
+  }
+  // I(c, a) = H^{-1}: column-major k x k, rows creators, columns annihilators
+  for (int e = lane; e < k * k; e += 32) minv[e] = I[e];
+  if (lane == 0) {
+    logdet[0] = dlog;
+    logdet[1] = dsign;
+  }
+}
+
+namespace {
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[64] = {nullptr};
+}  // namespace
+}  // namespace cthyb
+
+extern "C" {
+
+// Allocation-free variant of the M rebuild (no counterpart in the
+// reference): see include/cthyb_gpu.h.  The first call on a device looks up
+// the device address of the scratch array with that device current (do it
+// before any stream capture); later calls on that device only launch.
+int cthyb_minv_rebuild_noalloc(int k, const double* tau_c, const double* tau_a, const double* ftau,
+                               int nftau, double beta, double* minv, double* logdet, void* stream) {
+  using namespace cthyb;
+  if (k < 0 || k > NOALLOC_KMAX)
+    return fail(CTHYB_ERR_CAPACITY, "cthyb_minv_rebuild_noalloc: k = " + std::to_string(k) +
+                                        " exceeds the static scratch limit of " +
+                                        std::to_string(NOALLOC_KMAX) + " operators per type");
+  if (nftau < 2 || !(beta > 0.0) || !logdet || (k > 0 && (!tau_c || !tau_a || !ftau || !minv)))
+    return fail(CTHYB_ERR_ARG, "cthyb_minv_rebuild_noalloc: bad arguments");
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(CTHYB_ERR_ARG, "cthyb_minv_rebuild_noalloc: device ordinal out of range");
+  double* scratch = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess)
+        return fail(CTHYB_ERR_CUDA, std::string("cthyb_minv_rebuild_noalloc: cudaGetSymbolAddress: ") +
+                                        cudaGetErrorString(e));
+      g_noalloc_ptr[dev] = (double*)p;
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  k_minv_noalloc<<<1, 32, 0, (cudaStream_t)stream>>>(scratch, k, tau_c, tau_a, ftau, nftau, beta, minv, logdet);
+  CK(cudaGetLastError());
+  return CTHYB_OK;
+}
+
+}  // extern "C"

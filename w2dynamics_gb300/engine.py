@@ -31,6 +31,7 @@ EXPORTS = (
     "cthyb_batch_group_sums", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
+    "cthyb_minv_rebuild_noalloc",
 )
 
 
@@ -92,6 +93,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_set_log.argtypes = [vp, i64]
     L.cthyb_batch_get_log.argtypes = [vp, C.c_int, C.c_void_p, C.POINTER(i64)]
     L.cthyb_batch_work_counters.argtypes = [vp, C.POINTER(i64), C.c_int]
+    L.cthyb_minv_rebuild_noalloc.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_double, vp, vp, vp]
     _lib = L
     return L
 
