@@ -197,39 +197,57 @@ def run_gpu(args):
     print(json.dumps(line))
 
 
-def _cpu_chain(args_tuple):
-    beta, seed, nprop = args_tuple
+_WORKER = {}
+
+
+def _worker_init(beta, seed, ftau):
+    """One oracle chain per process, built and thermalised once."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from w2dynamics_gb300 import problems as P
-    pr = P.config_problem("dd3", beta=beta)
-    m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
-    c = O.Chain(m, beta, pr["ftau"], NTAU, seed=seed, taudiff_max=TDM, ncorr=NCORR)
+    nd = 3
+    um = P.flat_umatrix(P.umatrix_density(nd, 4.0, 4.0 - 1.2, 0.6))
+    m = O.Model(nd, um, P.muimp_solver(nd, P.DD3_MU), "Nt Szt")
+    c = O.Chain(m, beta, ftau, NTAU, seed=seed, taudiff_max=TDM, ncorr=NCORR)
     c.warmup(THERMALIZE)
+    _WORKER["chain"], _WORKER["model"] = c, m
+
+
+def _worker_run(nmeas):
+    c = _WORKER["chain"]
     t0 = time.perf_counter()
-    c.measure(nprop // NCORR)
-    return time.perf_counter() - t0, (nprop // NCORR) * NCORR
+    c.measure(nmeas)
+    return time.perf_counter() - t0, nmeas * NCORR
 
 
 def run_reference(args):
-    """Oracle (C++ restatement of the Fortran loop) on all host cores."""
+    """Oracle (C++ restatement of the Fortran loop) on all host cores, one
+    chain per core; each step runs `ref_meas` measurement cycles per chain."""
     import multiprocessing as mp
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    from w2dynamics_gb300 import problems as P
     cores = os.cpu_count() or 1
-    nprop = args.ref_proposals
-    tasks = [(BETAS[i % len(BETAS)], i, nprop) for i in range(cores)]
+    ftaus = {b: P.semicircle_ftau(3, b, 1.0, NTAU) for b in BETAS}
     ctx = mp.get_context("spawn")
-    vals = []
-    with ctx.Pool(cores) as pool:
+    pools = []
+    for i in range(cores):
+        b = BETAS[i % len(BETAS)]
+        pools.append(ctx.Pool(1, initializer=_worker_init, initargs=(b, i, ftaus[b])))
+    try:
         for _ in range(args.warmup):
-            pool.map(_cpu_chain, tasks[:cores])
+            for r in [p.apply_async(_worker_run, (max(1, args.ref_meas // 4),)) for p in pools]:
+                r.get()
+        vals = []
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            res = pool.map(_cpu_chain, tasks)
+            res = [r.get() for r in [p.apply_async(_worker_run, (args.ref_meas,)) for p in pools]]
             vals.append(sum(n for _, n in res) / max(t for t, _ in res))
         wall = time.perf_counter() - t0
+    finally:
+        for p in pools:
+            p.terminate()
     value = float(np.median(vals))
     line = {
         "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": args.gpus,
@@ -239,7 +257,8 @@ def run_reference(args):
         "config": workload_desc(args.chains_per_beta), "impl": "reference",
         "cpu_baseline": {"value": value, "unit": "MC updates/s", "cores": cores, "kind": "port",
                          "sample": f"{cores} chains (one per core, beta cycling over {list(BETAS)}), "
-                                   f"{nprop} proposals each after {THERMALIZE} thermalisation"},
+                                   f"{args.ref_meas} measurement cycles of {NCORR} proposals per chain "
+                                   f"and step after {THERMALIZE} thermalisation proposals"},
         "e2e": {"value": value, "unit": "MC updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -253,7 +272,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--chains-per-beta", type=int, default=CHAINS_PER_BETA)
-    ap.add_argument("--ref-proposals", type=int, default=20000)
+    ap.add_argument("--ref-meas", type=int, default=100,
+                    help="measurement cycles per chain and step of the CPU reference arm")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -87,11 +87,12 @@ def semicircle_gtau(beta, half_bandwidth, ntau, nquad=4000):
     tau = np.linspace(0.0, beta, ntau)
     out = np.empty(ntau)
     pos = e >= 0
-    for i, t in enumerate(tau):
-        f = np.empty_like(e)
-        f[pos] = np.exp(-e[pos] * t) / (1.0 + np.exp(-beta * e[pos]))
-        f[~pos] = np.exp(e[~pos] * (beta - t)) / (1.0 + np.exp(beta * e[~pos]))
-        out[i] = np.dot(wt, f)
+    ep, en = e[pos], e[~pos]
+    dp = 1.0 / (1.0 + np.exp(-beta * ep))
+    dn = 1.0 / (1.0 + np.exp(beta * en))
+    for a in range(0, ntau, 256):
+        t = tau[a:a + 256, None]
+        out[a:a + 256] = (np.exp(-ep * t) * dp) @ wt[pos] + (np.exp(en * (beta - t)) * dn) @ wt[~pos]
     return out
 
 
