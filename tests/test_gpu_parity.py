@@ -165,6 +165,43 @@ def test_batched_chains_match_oracle_per_seed(lib):
         assert np.array_equal(t_o, t_g), c
 
 
+@pytest.mark.parametrize("warps", [7, 32])
+def test_phase_synchronous_schedule_matches_oracle(lib, warps):
+    """The phase-synchronous schedule (blocks of `warps` chains, a partial
+    last block) runs every chain as the reference chain of its own seed, and
+    its measurements equal the independent-warp schedule's: histogram and
+    sign exactly, G(tau) and the density matrix to 1e-12 relative (G(tau)
+    bins are summed with atomics, whose order is not fixed)."""
+    pr = P.config_problem("dd3", beta=10.0)
+    mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    n = 45
+    runs = []
+    for sched in (0, warps):
+        b = E.Batch(mg, [E.Group(10.0, pr["ftau"], 20, nchains=n, seed0=300, taudiff_max=5.0,
+                                 kcap=64, opcap=512, ncorr=50)])
+        b.set_schedule(sched)
+        b.warmup(2000)
+        b.measure(20)
+        b.sync()
+        runs.append(b)
+    mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    for c in (0, 6, 7, 44):
+        co = O.Chain(mo, 10.0, pr["ftau"], 20, seed=300 + c, taudiff_max=5.0, ncorr=50)
+        co.warmup(2000)
+        co.measure(20)
+        t_o, *_ = co.get_config()
+        t_g, *_ = runs[1].get_config(c)
+        assert np.array_equal(t_o, t_g), c
+    for c in range(n):
+        r0, r1 = runs[0].results(c), runs[1].results(c)
+        scale = np.abs(r0["gtau"]).max()
+        assert np.allclose(r0["gtau"], r1["gtau"], rtol=1e-12, atol=1e-12 * scale), c
+        assert r0["mean_sign"] == r1["mean_sign"]
+        assert np.array_equal(r0["histo"], r1["histo"])
+        assert np.allclose(r0["densitymatrix"], r1["densitymatrix"], rtol=1e-12, atol=1e-14)
+        assert r0["counters"] == r1["counters"]
+
+
 def test_set_config_and_refresh(lib):
     """set_mc_config: trace and determinant of a fixed configuration equal
     the oracle's; the LU refresh of fast-updated M shows only rounding drift."""

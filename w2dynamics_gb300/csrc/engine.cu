@@ -77,6 +77,7 @@ struct Ctx {
   double* M;
   char* tree;
   unsigned char* act;
+  int* bstart;  // [2^L + 1] index of the first operator of each time bin
   double* scr;
   double* btau[2];
   double* bdt[2];  // time steps before each gathered operator and to the bin end
@@ -491,11 +492,9 @@ __device__ __forceinline__ int node_slot(const Ctx& c, const Mod& md, int n) {
 __device__ NOINL int gather_bin(Ctx& c, const Mod& md, int b, int buf) {
   double* btau = c.btau[buf];
   int* bcode = c.bcode[buf];
-  const int K = c.h->K;
   const int nb = 1 << c.g->L;
   double e0 = bin_edge(c, b), e1 = b + 1 < nb ? bin_edge(c, b + 1) : 0.0;
-  int lo = wlb(c.optau, K, e0, c.lane);
-  int hi = b + 1 < nb ? wlb(c.optau, K, e1, c.lane) : K;
+  const int lo = c.bstart[b], hi = c.bstart[b + 1];
   bool in1 = false, in2 = false;
   if (md.type == 1) {
     in1 = bin_of(c, md.t1) == b;
@@ -635,9 +634,9 @@ __device__ __forceinline__ void combine_body(Ctx& c, int n, int sl, int sr, int 
 }
 
 // Rebuild the leaves of a proposal and their ancestors in the inactive
-// slots: the superstate maps (states = false, first pass, gathers the
-// leaves' operators) or the state maps (states = true).
-__device__ NOINL void tree_propose(Ctx& c, Mod& md, bool states, bool gather) {
+// slots: superstate maps (do_ss) and/or, for monomial models, state maps
+// (do_states) in one traversal; `gather` collects the leaves' operators.
+__device__ NOINL void tree_propose(Ctx& c, Mod& md, bool do_ss, bool do_states, bool gather) {
   const int L = c.g->L, nb = 1 << L;
   const int nleaf = md.b2 != md.b1 ? 2 : 1;
   if (gather) {
@@ -650,7 +649,7 @@ __device__ NOINL void tree_propose(Ctx& c, Mod& md, bool states, bool gather) {
   }
   for (int q = 0; q < nleaf; ++q) {
     int b = q ? md.b2 : md.b1;
-    leaf_body(c, b, q ? md.n2 : md.n1, 1 - c.act[nb + b], !states, states, q);
+    leaf_body(c, b, q ? md.n2 : md.n1, 1 - c.act[nb + b], do_ss, do_states, q);
   }
   int n1 = nb + md.b1, n2 = nb + md.b2;
   for (int d = L - 1; d >= 0; --d) {
@@ -659,7 +658,7 @@ __device__ NOINL void tree_propose(Ctx& c, Mod& md, bool states, bool gather) {
     const int cnt = n2 != n1 ? 2 : 1;
     for (int q = 0; q < cnt; ++q) {
       int n = q ? n2 : n1;
-      combine_body(c, n, node_slot(c, md, 2 * n), node_slot(c, md, 2 * n + 1), 1 - c.act[n], !states, states);
+      combine_body(c, n, node_slot(c, md, 2 * n), node_slot(c, md, 2 * n + 1), 1 - c.act[n], do_ss, do_states);
     }
   }
   if (c.lane == 0) c.h->w_nodes += 2 * (L + 1);
@@ -675,11 +674,30 @@ __device__ void tree_accept(Ctx& c, const Mod& md) {
   }
   __syncwarp();
 }
+// Bin starts from the current operator array.
+__device__ NOINL void bstart_build(Ctx& c) {
+  const int nb = 1 << c.g->L, K = c.h->K;
+  for (int b = c.lane; b <= nb; b += 32) c.bstart[b] = b == nb ? K : slb(c.optau, K, bin_edge(c, b));
+  __syncwarp();
+}
+// Operators entered (+1) or left (-1) bins ba and bb.
+__device__ __forceinline__ void bstart_shift(Ctx& c, int ba, int bb, int d) {
+  const int nb = 1 << c.g->L;
+  for (int b = c.lane; b <= nb; b += 32) c.bstart[b] += d * ((b > ba) + (b > bb));
+  __syncwarp();
+}
+// Position of time t in the operator array (lower bound), searched inside its bin.
+__device__ __forceinline__ int op_lower_bound(Ctx& c, int bin, double t) {
+  const int j0 = c.bstart[bin];
+  return j0 + wlb(c.optau + j0, c.bstart[bin + 1] - j0, t, c.lane);
+}
+
 // Full build from the current operator array into slot 0.
 __device__ void tree_build_all(Ctx& c) {
   const int L = c.g->L, nb = 1 << L;
   Mod md;
   md.type = 0;
+  bstart_build(c);
   for (int b = 0; b < nb; ++b) {
     int n = gather_bin(c, md, b, 0);
     leaf_body(c, b, n, 0, true, true, 0);
@@ -708,9 +726,8 @@ __device__ NOINL int old_prefix(Ctx& c, int s, double t) {
     span = half;
   }
   if (s < 0) return -1;
-  int K = c.h->K;
-  int j0 = wlb(c.optau, K, bin_edge(c, b), c.lane);
-  int j1 = wlb(c.optau, K, t, c.lane);
+  int j0 = c.bstart[b];
+  int j1 = j0 + wlb(c.optau + j0, c.bstart[b + 1] - j0, t, c.lane);
   for (int j = j0; j < j1 && s >= 0; ++j) {
     int code = c.opcode[j];
     s = m.connect[((size_t)s * m.nf + (code >> 1)) * 2 + (code & 1)];
@@ -1014,27 +1031,73 @@ __device__ NOINL void write_record(Ctx& c, const cthyb_record& r) {
 // Trace of the proposed configuration as sum * exp(mx).
 __device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum) {
   if (c.mono) {
-    tree_propose(c, md, true, false);
-    root_trace(c, 1 - c.act[1], s0, mx, sum);
+    root_trace(c, 1 - c.act[1], s0, mx, sum);  // tree rebuilt with the QN check
   } else {
     dense_trace(c, md, s0, mx, sum);  // log|trace| and its sign
   }
 }
 
 // ---------------------------------------------------------------------------
-// StepAdd, CTQMC.F90:3353-3613 (diagonal hybridisation).
-__device__ NOINL void step_add(Ctx& c, bool change_outer) {
-  Hdr& h = *c.h;
-  const DModel& m = *c.m;
-  PROF_START();
-  if (c.lane == 0) h.try_add++;
+// One proposal in phases.  StepAdd (CTQMC.F90:3353-3613) and StepRem
+// (CTQMC.F90:3892-4151) for diagonal hybridisation, split so that a block of
+// warps can execute each phase together (k_sweep_sync): draw, set-up,
+// superstate/state tree + QN check, determinant ratio, trace + Metropolis
+// decision, accepted-move updates, bookkeeping.  A warp whose proposal ended
+// early (equal times, no pairs, QN violation, rejection) idles in the later
+// phases.  The per-warp proposal state lives in shared memory.
+struct Prop {
+  int move, alive, co, f, k, K, fpos_c, fpos_a, p1, p2, snew, np, ix, iy, cax, rank_c, rank_a, slot_c, slot_a,
+      accept;
+  double tau_c, tau_a, tdf, hprf, ratio, det_sign, det_log, tr_log, tr_sign, tx, ty;
+  Mod md;
+};
+
+__device__ __forceinline__ void prop_end(Ctx& c, Prop& p, int outcome) {
+  c.rec->outcome = outcome;
+  p.alive = 0;
   __syncwarp();
+}
+
+// Phase 0: capacity check and the move-type draws (CTQMC.F90:8435-8476).
+__device__ NOINL void ph_draw(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  p.alive = 0;
+  p.accept = 0;
+  for (int f = 0; f < c.m->nf; ++f)
+    if (h.k[f] + 1 > c.kcap) {
+      set_status(c, ST_CAPACITY);
+      return;
+    }
+  if (h.K + 2 > c.g->opcap) {
+    set_status(c, ST_CAPACITY);
+    return;
+  }
+  double rn = grnd(c);
+  grnd(c);  // Percentage4OperatorMove draw
+  bool co = grnd(c) < c.g->p_outer;
   cthyb_record& r = *c.rec;
   for (int i = c.lane; i < (int)(sizeof(cthyb_record) / 4); i += 32) ((int*)&r)[i] = 0;
   __syncwarp();
-  r.move = 0;
-  r.change_outer = change_outer;
-  // pair_OperAdd, Trace.F90:3657-3702
+  p.move = rn < 0.5 ? 0 : 1;
+  p.co = co;
+  r.move = p.move;
+  r.change_outer = co;
+  r.outer_sst = h.outer_sst;
+  r.k_total = h.K;
+  if (c.lane == 0) {
+    if (p.move == 0) h.try_add++;
+    else h.try_rem++;
+  }
+  p.alive = 1;
+  __syncwarp();
+}
+
+// Phase 1, insertion: pair_OperAdd (Trace.F90:3657-3702) and
+// process_OperAdd's equal-time rejection and FPos (Trace.F90:4275-4500).
+__device__ NOINL void ph_setup_add(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  cthyb_record& r = *c.rec;
   double u1 = grnd(c);
   int orb = randint(c, 1, m.nd);
   int spin = randint(c, 1, 2);
@@ -1054,244 +1117,48 @@ __device__ NOINL void step_add(Ctx& c, bool change_outer) {
   r.spin = spin;
   r.tau_c = tau_c;
   r.tau_a = tau_a;
-  r.outer_sst = h.outer_sst;
-  r.k_total = K;
-  // process_OperAdd: equal times are rejected (Trace.F90:4292-4407)
-  int pa = wlb(c.optau, K, tau_a, c.lane);
-  int pc = wlb(c.optau, K, tau_c, c.lane);
+  const int ba = bin_of(c, tau_a), bc = bin_of(c, tau_c);
+  int pa = op_lower_bound(c, ba, tau_a);
+  int pc = op_lower_bound(c, bc, tau_c);
   bool eq = teq(tau_a, tau_c) || (pa < K && teq(c.optau[pa], tau_a)) || (pc < K && teq(c.optau[pc], tau_c));
   if (eq) {
     if (c.lane == 0) h.qn_add++;
-    r.outcome = 0;
-    write_record(c, r);
+    prop_end(c, p, 0);
     return;
   }
-  const double* sc = srt_ptr(c, f, 0);
-  const double* sa = srt_ptr(c, f, 1);
-  int fpos_c = wlb(sc, k, tau_c, c.lane) + 1;
-  int fpos_a = wlb(sa, k, tau_a, c.lane) + 1;
+  int fpos_c = wlb(srt_ptr(c, f, 0), k, tau_c, c.lane) + 1;
+  int fpos_a = wlb(srt_ptr(c, f, 1), k, tau_a, c.lane) + 1;
   r.fpos_c = fpos_c;
   r.fpos_a = fpos_a;
-  Mod md;
-  md.type = 1;
   bool a_first = tau_a < tau_c;
+  Mod& md = p.md;
+  md.type = 1;
   md.t1 = a_first ? tau_a : tau_c;
   md.c1 = a_first ? 2 * f + 1 : 2 * f;
   md.t2 = a_first ? tau_c : tau_a;
   md.c2 = a_first ? 2 * f : 2 * f + 1;
   md.ix = md.iy = -1;
-  md.b1 = bin_of(c, md.t1);
-  md.b2 = bin_of(c, md.t2);
-  int p1 = a_first ? pa : pc, p2 = a_first ? pc : pa;
-  PROF_MARK(1);
-  // quantum-number check (CTQMC.F90:3421-3470)
-  tree_propose(c, md, false, true);
-  int root_new = 1 - c.act[1];
-  int s0 = h.outer_sst, snew = s0;
-  bool ok;
-  if (!change_outer) {
-    ok = node_ss(c, 1, root_new)[s0] == s0;
-  } else {
-    int inside = old_prefix(c, s0, md.t2);
-    snew = inside >= 0 ? new_suffix(c, md, inside, md.t2) : -1;
-    ok = snew >= 0 && node_ss(c, 1, root_new)[snew] == snew;
-  }
-  PROF_MARK(2);
-  if (!ok) {
-    if (c.lane == 0) h.qn_add++;
-    r.outcome = 1;
-    write_record(c, r);
-    return;
-  }
-  // determinant ratio (get_LogDetRatPairAdd / get_DetRatAdd)
-  double* Q = c.scr;
-  double* R = c.scr + c.kcap;
-  double* v = c.scr + 2 * c.kcap;
-  double* w = c.scr + 3 * c.kcap;
-  const double* tcs = stau_ptr(c, f, 0);
-  const double* tas = stau_ptr(c, f, 1);
-  for (int i = c.lane; i < k; i += 32) {
-    Q[i] = hybrf(c, __dsub_rn(tas[i], tau_c), f);
-    R[i] = hybrf(c, __dsub_rn(tau_a, tcs[i]), f);
-  }
-  double S = hybrf(c, __dsub_rn(tau_a, tau_c), f);
+  md.b1 = a_first ? ba : bc;
+  md.b2 = a_first ? bc : ba;
+  p.p1 = a_first ? pa : pc;
+  p.p2 = a_first ? pc : pa;
+  p.f = f;
+  p.k = k;
+  p.K = K;
+  p.fpos_c = fpos_c;
+  p.fpos_a = fpos_a;
+  p.tau_c = tau_c;
+  p.tau_a = tau_a;
+  p.tdf = tdf;
   __syncwarp();
-  const double* Mf = M_ptr(c, f);
-  double part = 0.0;
-  for (int i = c.lane; i < k; i += 32) {
-    double acc = 0.0;
-    for (int j = 0; j < k; ++j) acc = fma(Mf[(size_t)j * c.kcap + i], Q[j], acc);
-    v[i] = acc;
-    part = fma(R[i], acc, part);
-  }
-  double ratio = S - wsum(part);
-  __syncwarp();
-  PROF_MARK(3);
-  double sig = ((fpos_c - fpos_a) & 1) ? -1.0 : 1.0;
-  double det_sign = (ratio >= 0.0 ? 1.0 : -1.0) * sig;
-  if (c.lane == 0) {
-    h.w_mbytes += 8ll * k * k + 32ll * k;
-    h.w_mflops += 2ll * k * k + 2ll * k;
-  }
-  // trace
-  double tr_mx, tr_sum;
-  proposed_trace(c, md, snew, tr_mx, tr_sum);
-  PROF_MARK(4);
-  double rnd = grnd(c);
-  // NPairs of the proposed configuration
-  int np;
-  if (h.npairs == -1) {
-    // full recount including the new pair
-    int tot = 0;
-    int start = wlb(c.optau, K, wmin, c.lane);
-    for (int i = start + c.lane; i < K; i += 32) {
-      double t = c.optau[i];
-      if (t > wmax) continue;
-      int cd = c.opcode[i], ff = cd >> 1, cc = cd & 1;
-      const double* opp = srt_ptr(c, ff, 1 - cc);
-      int n = cnt_later(opp, h.k[ff], t, wmax, tdm);
-      if (ff == f) {
-        // partner among the new operators
-        double tn = cc == 0 ? tau_a : tau_c;
-        if (tn > t && tn <= fmin(wmax, __dadd_rn(t, tdm))) n++;
-      }
-      tot += n;
-    }
-    tot = wsumi(tot);
-    // pairs with a new operator as the earlier member
-    double tearly = md.t1;
-    int cde = md.c1 & 1;
-    if (tearly >= wmin && tearly <= wmax) {
-      const double* opp = srt_ptr(c, f, 1 - cde);
-      int n = 0;
-      if (c.lane == 0) n = cnt_later(opp, k, tearly, wmax, tdm);
-      tot += __shfl_sync(FULL, n, 0);
-      double tl = md.t2;
-      if (tl <= fmin(wmax, __dadd_rn(tearly, tdm))) tot += 1;
-    }
-    {
-      double tlate = md.t2;
-      int cdl = md.c2 & 1;
-      if (tlate >= wmin && tlate <= wmax) {
-        const double* opp = srt_ptr(c, f, 1 - cdl);
-        int n = 0;
-        if (c.lane == 0) n = cnt_later(opp, k, tlate, wmax, tdm);
-        tot += __shfl_sync(FULL, n, 0);
-      }
-    }
-    np = tot;
-  } else {
-    // update_NPairs(+1): partners of both new operators
-    int n = 0;
-    if (c.lane == 0) {
-      const double* opp1 = srt_ptr(c, f, 1 - (md.c1 & 1));
-      const double* opp2 = srt_ptr(c, f, 1 - (md.c2 & 1));
-      n += cnt_later(opp1, k, md.t1, wmax, tdm) + cnt_earlier(opp1, k, md.t1, wmin, tdm);
-      if (md.t2 <= wmax && md.t2 <= __dadd_rn(md.t1, tdm)) n += 1;
-      n += cnt_later(opp2, k, md.t2, wmax, tdm) + cnt_earlier(opp2, k, md.t2, wmin, tdm);
-    }
-    np = h.npairs + __shfl_sync(FULL, n, 0);
-  }
-  double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(ratio));
-  double x = tdf * (double)(2 * m.nd) / (double)np * wr;
-  double prob = fabs(x);
-  bool accept = rnd < prob;
-  double det_log = 0.0, tr_lg = 0.0, tr_sg = 0.0;
-  if (accept || c.log) {
-    det_log = log(fabs(ratio));
-    trace_log(tr_mx, tr_sum, tr_lg, tr_sg);
-  }
-  r.det_log = det_log;
-  r.det_sign = det_sign;
-  r.tr_log = tr_lg;
-  r.tr_sign = tr_sg;
-  r.prob = prob;
-  r.rand = rnd;
-  r.npairs = np;
-  PROF_MARK(5);
-  if (accept) {
-    if (k + 1 > c.kcap || K + 2 > c.g->opcap) {
-      set_status(c, ST_CAPACITY);
-      return;
-    }
-    // get_MatAdd in slot order: w = R^T M, rank-one update, new row/column
-    double* Mw = M_ptr(c, f);
-    for (int j = c.lane; j < k; j += 32) {
-      double acc = 0.0;
-      const double* col = Mw + (size_t)j * c.kcap;
-      for (int i = 0; i < k; ++i) acc = fma(R[i], col[i], acc);
-      w[j] = acc;
-    }
-    __syncwarp();
-    double invS = 1.0 / ratio;
-    for (int i = c.lane; i < k; i += 32) {
-      double vi = v[i] * invS;
-      for (int j = 0; j < k; ++j) Mw[(size_t)j * c.kcap + i] = fma(vi, w[j], Mw[(size_t)j * c.kcap + i]);
-      Mw[(size_t)k * c.kcap + i] = -vi;
-    }
-    for (int j = c.lane; j < k; j += 32) Mw[(size_t)j * c.kcap + k] = -w[j] * invS;
-    if (c.lane == 0) {
-      Mw[(size_t)k * c.kcap + k] = invS;
-      h.w_mbytes += 16ll * k * k + 16ll * k;
-      h.w_mflops += 4ll * k * k;
-    }
-    __syncwarp();
-    // slots and sorted arrays
-    if (c.lane == 0) {
-      stau_ptr(c, f, 0)[k] = tau_c;
-      stau_ptr(c, f, 1)[k] = tau_a;
-    }
-    __syncwarp();
-    arr_insert(c, srt_ptr(c, f, 0), sslot_ptr(c, f, 0), k, fpos_c - 1, tau_c, (short)k);
-    arr_insert(c, srt_ptr(c, f, 1), sslot_ptr(c, f, 1), k, fpos_a - 1, tau_a, (short)k);
-    ops_insert2(c, p1, p2, md.t1, md.c1, md.t2, md.c2);
-    PROF_MARK(6);
-    if (c.mono) tree_accept(c, md);
-    else {
-      tree_accept(c, md);
-    }
-    if (c.lane == 0) {
-      h.k[f] = k + 1;
-      h.K = K + 2;
-      h.det_log = det_log + h.det_log;
-      h.det_sign = det_sign * h.det_sign;
-      h.trace_log = tr_lg;
-      h.trace_sign = tr_sg;
-      h.npairs = np;
-      h.outer_sst = snew;
-      h.acc_add++;
-      h.w_opbytes += 24ll * (K - p1) + 40ll * k;
-    }
-    __syncwarp();
-    double sgn = config_sign(c);
-    if (c.lane == 0) h.cfgsign = -sgn;
-    __syncwarp();
-    PROF_MARK(7);
-    r.outcome = 4;
-  } else {
-    r.outcome = 3;
-  }
-  r.outer_sst = h.outer_sst;
-  r.k_total = h.K;
-  write_record(c, r);
 }
 
-// ---------------------------------------------------------------------------
-// StepRem, CTQMC.F90:3892-4151 (diagonal hybridisation).
-__device__ NOINL void step_rem(Ctx& c, bool change_outer) {
+// Phase 1, removal: gen_OperRemove (Trace.F90:4851-4960): the NPair-th
+// eligible pair in (time of the earlier member, time of the later member)
+// order, FPos, and the proposal-probability factor.
+__device__ NOINL void ph_setup_rem(Ctx& c, Prop& p) {
   Hdr& h = *c.h;
-  const DModel& m = *c.m;
-  PROF_START();
-  if (c.lane == 0) h.try_rem++;
-  __syncwarp();
   cthyb_record& r = *c.rec;
-  for (int i = c.lane; i < (int)(sizeof(cthyb_record) / 4); i += 32) ((int*)&r)[i] = 0;
-  __syncwarp();
-  r.move = 1;
-  r.change_outer = change_outer;
-  r.outer_sst = h.outer_sst;
-  r.k_total = h.K;
-  // gen_OperRemove, Trace.F90:4851-4960
   if (h.npairs == -1) {
     int np = count_npairs(c);
     if (c.lane == 0) h.npairs = np;
@@ -1299,8 +1166,7 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   }
   if (h.npairs <= 0) {
     if (c.lane == 0) h.qn_rem++;
-    r.outcome = 2;
-    write_record(c, r);
+    prop_end(c, p, 2);
     return;
   }
   const int K = h.K;
@@ -1310,13 +1176,10 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   int ix = -1, yrank = -1;
   for (int base = start; base < K; base += 32) {
     int i = base + c.lane;
-    int cnt = 0, cd = 0, ff = 0, cc = 0, lb = 0;
-    double t = 0;
+    int cnt = 0, lb = 0;
     if (i < K) {
-      t = c.optau[i];
-      cd = c.opcode[i];
-      ff = cd >> 1;
-      cc = cd & 1;
+      double t = c.optau[i];
+      int cd = c.opcode[i], ff = cd >> 1, cc = cd & 1;
       const double* opp = srt_ptr(c, ff, 1 - cc);
       double hi = fmin(wmax, __dadd_rn(t, tdm));
       lb = sub(opp, h.k[ff], t);
@@ -1342,6 +1205,7 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   }
   if (ix < 0) {
     set_status(c, ST_INTERNAL);
+    p.alive = 0;
     return;
   }
   const double tx = c.optau[ix];
@@ -1349,30 +1213,31 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   const int k = h.k[f];
   if (yrank < 0 || yrank >= k) {
     set_status(c, ST_INTERNAL);
+    p.alive = 0;
     return;
   }
   const double ty = srt_ptr(c, f, 1 - cax)[yrank];
-  const int iy = wlb(c.optau, K, ty, c.lane);
+  const int by = bin_of(c, ty);
+  const int iy = op_lower_bound(c, by, ty);
   const int xrank = wlb(srt_ptr(c, f, cax), k, tx, c.lane);
   if (iy <= ix || iy >= K || !teq(c.optau[iy], ty) || xrank >= k || !teq(srt_ptr(c, f, cax)[xrank], tx)) {
     set_status(c, ST_INTERNAL);
+    p.alive = 0;
     return;
   }
   const double tau_c = cax == 0 ? tx : ty, tau_a = cax == 0 ? ty : tx;
   const int rank_c = cax == 0 ? xrank : yrank, rank_a = cax == 0 ? yrank : xrank;
-  const int fpos_c = rank_c + 1, fpos_a = rank_a + 1;
-  const int slot_c = sslot_ptr(c, f, 0)[rank_c], slot_a = sslot_ptr(c, f, 1)[rank_a];
-  double hprf = __ddiv_rn((double)h.npairs,
-                          __dmul_rn(__dsub_rn(wmax, wmin),
-                                    __dsub_rn(fmin(__dadd_rn(tau_a, tdm), wmax), fmax(__dsub_rn(tau_a, tdm), wmin))));
+  p.hprf = __ddiv_rn((double)h.npairs,
+                     __dmul_rn(__dsub_rn(wmax, wmin),
+                               __dsub_rn(fmin(__dadd_rn(tau_a, tdm), wmax), fmax(__dsub_rn(tau_a, tdm), wmin))));
   r.orb = f / 2 + 1;
   r.spin = f % 2 + 1;
   r.tau_c = tau_c;
   r.tau_a = tau_a;
-  r.fpos_c = fpos_c;
-  r.fpos_a = fpos_a;
+  r.fpos_c = rank_c + 1;
+  r.fpos_a = rank_a + 1;
   r.npairs = h.npairs;
-  Mod md;
+  Mod& md = p.md;
   md.type = 2;
   md.ix = ix;
   md.iy = iy;
@@ -1380,164 +1245,351 @@ __device__ NOINL void step_rem(Ctx& c, bool change_outer) {
   md.t2 = ty;
   md.c1 = md.c2 = 0;
   md.b1 = bin_of(c, tx);
-  md.b2 = bin_of(c, ty);
-  PROF_MARK(8);
-  tree_propose(c, md, false, true);
+  md.b2 = by;
+  p.f = f;
+  p.k = k;
+  p.K = K;
+  p.ix = ix;
+  p.iy = iy;
+  p.cax = cax;
+  p.tx = tx;
+  p.ty = ty;
+  p.tau_c = tau_c;
+  p.tau_a = tau_a;
+  p.rank_c = rank_c;
+  p.rank_a = rank_a;
+  p.fpos_c = rank_c + 1;
+  p.fpos_a = rank_a + 1;
+  p.slot_c = sslot_ptr(c, f, 0)[rank_c];
+  p.slot_a = sslot_ptr(c, f, 1)[rank_a];
+  __syncwarp();
+}
+
+// Phase 2: proposed tree and the quantum-number check
+// (check_sst_sequence, Trace.F90:1243-1304; CTQMC.F90:3421-3470 and
+// 3928-3976).
+__device__ NOINL void ph_tree_qn(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  Mod& md = p.md;
+  tree_propose(c, md, true, c.mono != 0, true);
   int root_new = 1 - c.act[1];
   int s0 = h.outer_sst, snew = s0;
   bool ok;
-  if (!change_outer) {
+  if (!p.co) {
     ok = node_ss(c, 1, root_new)[s0] == s0;
   } else {
-    int inside = old_prefix(c, s0, ty);
-    snew = inside >= 0 ? new_suffix(c, md, inside, ty) : -1;
+    int inside = old_prefix(c, s0, md.t2);
+    snew = inside >= 0 ? new_suffix(c, md, inside, md.t2) : -1;
     ok = snew >= 0 && node_ss(c, 1, root_new)[snew] == snew;
   }
+  p.snew = snew;
+  __syncwarp();
   if (!ok) {
-    if (c.lane == 0) h.qn_rem++;
-    r.outcome = 1;
-    write_record(c, r);
+    if (c.lane == 0) {
+      if (p.move == 0) h.qn_add++;
+      else h.qn_rem++;
+    }
+    prop_end(c, p, 1);
+  }
+}
+
+// Phase 3: determinant ratio.  Insertion: S - R.(M Q)
+// (get_LogDetRatPairAdd / get_DetRatAdd, Trace.F90:2775-2833,
+// MatrixUpdate.F90:392-407); removal: M(c, a) (Trace.F90:2937-2966).
+__device__ NOINL void ph_det(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const int f = p.f, k = p.k;
+  const double* Mf = M_ptr(c, f);
+  if (p.move == 1) {
+    double dr = Mf[(size_t)p.slot_a * c.kcap + p.slot_c];
+    double sig = ((p.fpos_c - p.fpos_a) & 1) ? -1.0 : 1.0;
+    p.ratio = dr;
+    p.det_sign = (dr >= 0.0 ? 1.0 : -1.0) * sig;
+    __syncwarp();
     return;
   }
-  const double* Mf = M_ptr(c, f);
-  double dr = Mf[(size_t)slot_a * c.kcap + slot_c];
-  double sig = ((fpos_c - fpos_a) & 1) ? -1.0 : 1.0;
-  double det_sign = (dr >= 0.0 ? 1.0 : -1.0) * sig;
-  PROF_MARK(2);
+  double* Q = c.scr;
+  double* R = c.scr + c.kcap;
+  double* v = c.scr + 2 * c.kcap;
+  const double* tcs = stau_ptr(c, f, 0);
+  const double* tas = stau_ptr(c, f, 1);
+  const double tau_c = p.tau_c, tau_a = p.tau_a;
+  for (int i = c.lane; i < k; i += 32) {
+    Q[i] = hybrf(c, __dsub_rn(tas[i], tau_c), f);
+    R[i] = hybrf(c, __dsub_rn(tau_a, tcs[i]), f);
+  }
+  double S = hybrf(c, __dsub_rn(tau_a, tau_c), f);
+  __syncwarp();
+  double part = 0.0;
+  for (int i = c.lane; i < k; i += 32) {
+    double acc = 0.0;
+    for (int j = 0; j < k; ++j) acc = fma(Mf[(size_t)j * c.kcap + i], Q[j], acc);
+    v[i] = acc;
+    part = fma(R[i], acc, part);
+  }
+  double ratio = S - wsum(part);
+  double sig = ((p.fpos_c - p.fpos_a) & 1) ? -1.0 : 1.0;
+  p.ratio = ratio;
+  p.det_sign = (ratio >= 0.0 ? 1.0 : -1.0) * sig;
+  if (c.lane == 0) {
+    h.w_mbytes += 8ll * k * k + 32ll * k;
+    h.w_mflops += 2ll * k * k + 2ll * k;
+  }
+  __syncwarp();
+}
+
+// Phase 4: trace of the proposed configuration, NPairs of the new
+// configuration (update_NPairs / ensure_valid_NPairs, Trace.F90:1756-1922)
+// and the Metropolis decision (CTQMC.F90:3508-3524, 4050-4058).
+__device__ NOINL void ph_decide(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  cthyb_record& r = *c.rec;
   double tr_mx, tr_sum;
-  proposed_trace(c, md, snew, tr_mx, tr_sum);
-  PROF_MARK(4);
-  double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(dr));
-  double x = hprf / (double)(2 * m.nd) * wr;
-  double prob = fabs(x);
-  double rnd = grnd(c);
+  proposed_trace(c, p.md, p.snew, tr_mx, tr_sum);
+  const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  const int f = p.f, k = p.k, K = p.K;
+  double prob, rnd;
+  if (p.move == 0) {
+    const Mod& md = p.md;
+    rnd = grnd(c);
+    int np;
+    if (h.npairs == -1) {
+      // full recount including the new pair
+      int tot = 0;
+      int start = wlb(c.optau, K, wmin, c.lane);
+      for (int i = start + c.lane; i < K; i += 32) {
+        double t = c.optau[i];
+        if (t > wmax) continue;
+        int cd = c.opcode[i], ff = cd >> 1, cc = cd & 1;
+        int n = cnt_later(srt_ptr(c, ff, 1 - cc), h.k[ff], t, wmax, tdm);
+        if (ff == f) {
+          double tn = cc == 0 ? p.tau_a : p.tau_c;  // partner among the new operators
+          if (tn > t && tn <= fmin(wmax, __dadd_rn(t, tdm))) n++;
+        }
+        tot += n;
+      }
+      tot = wsumi(tot);
+      int n = 0;
+      if (c.lane == 0) {
+        if (md.t1 >= wmin && md.t1 <= wmax) {  // pairs with a new operator as the earlier member
+          n += cnt_later(srt_ptr(c, f, 1 - (md.c1 & 1)), k, md.t1, wmax, tdm);
+          if (md.t2 <= fmin(wmax, __dadd_rn(md.t1, tdm))) n += 1;
+        }
+        if (md.t2 >= wmin && md.t2 <= wmax) n += cnt_later(srt_ptr(c, f, 1 - (md.c2 & 1)), k, md.t2, wmax, tdm);
+      }
+      np = tot + __shfl_sync(FULL, n, 0);
+    } else {
+      int n = 0;
+      if (c.lane == 0) {
+        const double* opp1 = srt_ptr(c, f, 1 - (md.c1 & 1));
+        const double* opp2 = srt_ptr(c, f, 1 - (md.c2 & 1));
+        n += cnt_later(opp1, k, md.t1, wmax, tdm) + cnt_earlier(opp1, k, md.t1, wmin, tdm);
+        if (md.t2 <= wmax && md.t2 <= __dadd_rn(md.t1, tdm)) n += 1;
+        n += cnt_later(opp2, k, md.t2, wmax, tdm) + cnt_earlier(opp2, k, md.t2, wmin, tdm);
+      }
+      np = h.npairs + __shfl_sync(FULL, n, 0);
+    }
+    double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(p.ratio));
+    prob = fabs(p.tdf * (double)(2 * m.nd) / (double)np * wr);
+    p.np = np;
+    r.npairs = np;
+  } else {
+    double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(p.ratio));
+    prob = fabs(p.hprf / (double)(2 * m.nd) * wr);
+    rnd = grnd(c);
+  }
+  bool accept = rnd < prob;
+  if (accept && p.move == 1 && fabs(p.ratio) < 1e-12) {  // CTQMC.F90:4062
+    set_status(c, ST_NUMERIC);
+    p.alive = 0;
+    return;
+  }
   double det_log = 0.0, tr_lg = 0.0, tr_sg = 0.0;
-  if (rnd < prob || c.log) {
-    det_log = log(fabs(dr));
+  if (accept || c.log) {
+    det_log = log(fabs(p.ratio));
     trace_log(tr_mx, tr_sum, tr_lg, tr_sg);
   }
   r.det_log = det_log;
-  r.det_sign = det_sign;
+  r.det_sign = p.det_sign;
   r.tr_log = tr_lg;
   r.tr_sign = tr_sg;
   r.prob = prob;
   r.rand = rnd;
-  if (rnd < prob) {
-    if (fabs(dr * sig) < 1e-12) {  // CTQMC.F90:4062
-      set_status(c, ST_NUMERIC);
-      return;
-    }
-    // get_MatRem in slot order, then move the last row/column into the gap
-    double* Mw = M_ptr(c, f);
-    double* col = c.scr;             // column slot_a
-    double* row = c.scr + c.kcap;    // row slot_c
-    for (int i = c.lane; i < k; i += 32) {
-      col[i] = Mw[(size_t)slot_a * c.kcap + i];
-      row[i] = Mw[(size_t)i * c.kcap + slot_c];
-    }
-    __syncwarp();
-    double inv = 1.0 / dr;
-    for (int i = c.lane; i < k; i += 32) {
-      double ci = col[i] * inv;
-      for (int j = 0; j < k; ++j) Mw[(size_t)j * c.kcap + i] = fma(-ci, row[j], Mw[(size_t)j * c.kcap + i]);
-    }
-    __syncwarp();
-    const int last = k - 1;
-    if (slot_c != last) {
-      for (int j = c.lane; j < k; j += 32) Mw[(size_t)j * c.kcap + slot_c] = Mw[(size_t)j * c.kcap + last];
-    }
-    __syncwarp();
-    if (slot_a != last) {
-      for (int i = c.lane; i < k; i += 32) Mw[(size_t)slot_a * c.kcap + i] = Mw[(size_t)last * c.kcap + i];
-    }
-    __syncwarp();
-    if (c.lane == 0) {
-      h.w_mbytes += 16ll * k * k;
-      h.w_mflops += 2ll * k * k;
-    }
-    // slot bookkeeping: slot `last` moves into the freed slots
-    arr_remove(c, srt_ptr(c, f, 0), sslot_ptr(c, f, 0), k, rank_c);
-    arr_remove(c, srt_ptr(c, f, 1), sslot_ptr(c, f, 1), k, rank_a);
-    if (slot_c != last) {
-      short* ss = sslot_ptr(c, f, 0);
-      for (int i = c.lane; i < k - 1; i += 32)
-        if (ss[i] == last) ss[i] = (short)slot_c;
-      if (c.lane == 0) stau_ptr(c, f, 0)[slot_c] = stau_ptr(c, f, 0)[last];
-    }
-    if (slot_a != last) {
-      short* ss = sslot_ptr(c, f, 1);
-      for (int i = c.lane; i < k - 1; i += 32)
-        if (ss[i] == last) ss[i] = (short)slot_a;
-      if (c.lane == 0) stau_ptr(c, f, 1)[slot_a] = stau_ptr(c, f, 1)[last];
-    }
-    __syncwarp();
-    ops_remove2(c, ix, iy);
-    PROF_MARK(6);
-    tree_accept(c, md);
-    if (c.lane == 0) {
-      h.k[f] = k - 1;
-      h.K = K - 2;
-      h.det_log = det_log + h.det_log;
-      h.det_sign = det_sign * h.det_sign;
-      h.trace_log = tr_lg;
-      h.trace_sign = tr_sg;
-      h.outer_sst = snew;
-      h.acc_rem++;
-      h.w_opbytes += 24ll * (K - ix) + 40ll * k;
-    }
-    __syncwarp();
-    // update_NPairs(-1): the pair and the partners of its members
-    int n = 0;
-    if (c.lane == 0) {
-      const double* oppx = srt_ptr(c, f, 1 - cax);
-      const double* oppy = srt_ptr(c, f, cax);
-      n = 1 + cnt_later(oppx, k - 1, tx, wmax, tdm) + cnt_earlier(oppx, k - 1, tx, wmin, tdm) +
-          cnt_later(oppy, k - 1, ty, wmax, tdm) + cnt_earlier(oppy, k - 1, ty, wmin, tdm);
-      h.npairs -= n;
-    }
-    __syncwarp();
-    double sgn = config_sign(c);
-    if (c.lane == 0) h.cfgsign = -sgn;
-    __syncwarp();
-    PROF_MARK(7);
-    r.outcome = 4;
-  } else {
-    r.outcome = 3;
-  }
-  r.outer_sst = h.outer_sst;
-  r.k_total = h.K;
-  write_record(c, r);
+  p.det_log = det_log;
+  p.tr_log = tr_lg;
+  p.tr_sign = tr_sg;
+  p.accept = accept;
+  __syncwarp();
+  if (!accept) prop_end(c, p, 3);
 }
 
-// One proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250),
-// percentages of global, tau-shift and 4-operator moves zero.
-__device__ void one_step(Ctx& c) {
-  PROF_START();
+// Phase 5: accepted insertion: get_MatAdd in slot order (w = R^T M, rank-one
+// update, new row and column), sorted and operator arrays, tree flip, sign.
+__device__ NOINL void ph_accept_add(Ctx& c, Prop& p) {
   Hdr& h = *c.h;
-  for (int f = 0; f < c.m->nf; ++f)
-    if (h.k[f] + 1 > c.kcap) {
-      set_status(c, ST_CAPACITY);
-      return;
-    }
-  if (h.K + 2 > c.g->opcap) {
-    set_status(c, ST_CAPACITY);
-    return;
+  const int f = p.f, k = p.k, K = p.K;
+  const Mod& md = p.md;
+  const double* R = c.scr + c.kcap;
+  const double* v = c.scr + 2 * c.kcap;
+  double* w = c.scr + 3 * c.kcap;
+  double* Mw = M_ptr(c, f);
+  for (int j = c.lane; j < k; j += 32) {
+    double acc = 0.0;
+    const double* col = Mw + (size_t)j * c.kcap;
+    for (int i = 0; i < k; ++i) acc = fma(R[i], col[i], acc);
+    w[j] = acc;
   }
-  double rn = grnd(c);
-  if (rn < 0.5) {
-    grnd(c);  // Percentage4OperatorMove draw
-    bool co = grnd(c) < c.g->p_outer;
-    PROF_MARK(0);
-    step_add(c, co);
-  } else {
-    grnd(c);
-    bool co = grnd(c) < c.g->p_outer;
-    PROF_MARK(0);
-    step_rem(c, co);
+  __syncwarp();
+  double invS = 1.0 / p.ratio;
+  for (int i = c.lane; i < k; i += 32) {
+    double vi = v[i] * invS;
+    for (int j = 0; j < k; ++j) Mw[(size_t)j * c.kcap + i] = fma(vi, w[j], Mw[(size_t)j * c.kcap + i]);
+    Mw[(size_t)k * c.kcap + i] = -vi;
   }
+  for (int j = c.lane; j < k; j += 32) Mw[(size_t)j * c.kcap + k] = -w[j] * invS;
+  if (c.lane == 0) {
+    Mw[(size_t)k * c.kcap + k] = invS;
+    h.w_mbytes += 16ll * k * k + 16ll * k;
+    h.w_mflops += 4ll * k * k;
+    stau_ptr(c, f, 0)[k] = p.tau_c;
+    stau_ptr(c, f, 1)[k] = p.tau_a;
+  }
+  __syncwarp();
+  arr_insert(c, srt_ptr(c, f, 0), sslot_ptr(c, f, 0), k, p.fpos_c - 1, p.tau_c, (short)k);
+  arr_insert(c, srt_ptr(c, f, 1), sslot_ptr(c, f, 1), k, p.fpos_a - 1, p.tau_a, (short)k);
+  ops_insert2(c, p.p1, p.p2, md.t1, md.c1, md.t2, md.c2);
+  bstart_shift(c, md.b1, md.b2, +1);
+  tree_accept(c, md);
+  if (c.lane == 0) {
+    h.k[f] = k + 1;
+    h.K = K + 2;
+    h.det_log = p.det_log + h.det_log;
+    h.det_sign = p.det_sign * h.det_sign;
+    h.trace_log = p.tr_log;
+    h.trace_sign = p.tr_sign;
+    h.npairs = p.np;
+    h.outer_sst = p.snew;
+    h.acc_add++;
+    h.w_opbytes += 24ll * (K - p.p1) + 40ll * k;
+  }
+  __syncwarp();
+  double sgn = config_sign(c);
+  if (c.lane == 0) h.cfgsign = -sgn;
+  c.rec->outcome = 4;
+  __syncwarp();
+}
+
+// Phase 5: accepted removal: get_MatRem in slot order, then the last row and
+// column move into the gap; arrays, tree flip, NPairs, sign.
+__device__ NOINL void ph_accept_rem(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const int f = p.f, k = p.k, K = p.K, slot_c = p.slot_c, slot_a = p.slot_a;
+  const Mod& md = p.md;
+  double* Mw = M_ptr(c, f);
+  double* col = c.scr;           // column slot_a
+  double* row = c.scr + c.kcap;  // row slot_c
+  for (int i = c.lane; i < k; i += 32) {
+    col[i] = Mw[(size_t)slot_a * c.kcap + i];
+    row[i] = Mw[(size_t)i * c.kcap + slot_c];
+  }
+  __syncwarp();
+  double inv = 1.0 / p.ratio;
+  for (int i = c.lane; i < k; i += 32) {
+    double ci = col[i] * inv;
+    for (int j = 0; j < k; ++j) Mw[(size_t)j * c.kcap + i] = fma(-ci, row[j], Mw[(size_t)j * c.kcap + i]);
+  }
+  __syncwarp();
+  const int last = k - 1;
+  if (slot_c != last)
+    for (int j = c.lane; j < k; j += 32) Mw[(size_t)j * c.kcap + slot_c] = Mw[(size_t)j * c.kcap + last];
+  __syncwarp();
+  if (slot_a != last)
+    for (int i = c.lane; i < k; i += 32) Mw[(size_t)slot_a * c.kcap + i] = Mw[(size_t)last * c.kcap + i];
+  __syncwarp();
+  if (c.lane == 0) {
+    h.w_mbytes += 16ll * k * k;
+    h.w_mflops += 2ll * k * k;
+  }
+  arr_remove(c, srt_ptr(c, f, 0), sslot_ptr(c, f, 0), k, p.rank_c);
+  arr_remove(c, srt_ptr(c, f, 1), sslot_ptr(c, f, 1), k, p.rank_a);
+  if (slot_c != last) {
+    short* ss = sslot_ptr(c, f, 0);
+    for (int i = c.lane; i < k - 1; i += 32)
+      if (ss[i] == last) ss[i] = (short)slot_c;
+    if (c.lane == 0) stau_ptr(c, f, 0)[slot_c] = stau_ptr(c, f, 0)[last];
+  }
+  if (slot_a != last) {
+    short* ss = sslot_ptr(c, f, 1);
+    for (int i = c.lane; i < k - 1; i += 32)
+      if (ss[i] == last) ss[i] = (short)slot_a;
+    if (c.lane == 0) stau_ptr(c, f, 1)[slot_a] = stau_ptr(c, f, 1)[last];
+  }
+  __syncwarp();
+  ops_remove2(c, p.ix, p.iy);
+  bstart_shift(c, md.b1, md.b2, -1);
+  tree_accept(c, md);
+  const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  if (c.lane == 0) {
+    h.k[f] = k - 1;
+    h.K = K - 2;
+    h.det_log = p.det_log + h.det_log;
+    h.det_sign = p.det_sign * h.det_sign;
+    h.trace_log = p.tr_log;
+    h.trace_sign = p.tr_sign;
+    h.outer_sst = p.snew;
+    h.acc_rem++;
+    h.w_opbytes += 24ll * (K - p.ix) + 40ll * k;
+    // update_NPairs(-1): the pair and the partners of its members
+    const double* oppx = srt_ptr(c, f, 1 - p.cax);
+    const double* oppy = srt_ptr(c, f, p.cax);
+    h.npairs -= 1 + cnt_later(oppx, k - 1, p.tx, wmax, tdm) + cnt_earlier(oppx, k - 1, p.tx, wmin, tdm) +
+                cnt_later(oppy, k - 1, p.ty, wmax, tdm) + cnt_earlier(oppy, k - 1, p.ty, wmin, tdm);
+  }
+  __syncwarp();
+  double sgn = config_sign(c);
+  if (c.lane == 0) h.cfgsign = -sgn;
+  c.rec->outcome = 4;
+  __syncwarp();
+}
+
+// Phase 6: record, proposal count and the window cadence
+// (CTQMC.F90:8531: shift every NSlide add/remove tries).
+__device__ NOINL void ph_finish(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  cthyb_record& r = *c.rec;
+  r.outer_sst = h.outer_sst;
+  r.k_total = h.K;
+  __syncwarp();
+  write_record(c, r);
   if (c.lane == 0) h.nprop++;
   __syncwarp();
   if (h.nprop % h.nslide == 0) shift_window(c);
+}
+
+// One proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250) with
+// the phases back to back.
+__device__ void one_step(Ctx& c, Prop& p) {
+  PROF_START();
+  ph_draw(c, p);
+  if (!p.alive) return;  // capacity
+  PROF_MARK(0);
+  if (p.move == 0) ph_setup_add(c, p);
+  else ph_setup_rem(c, p);
+  PROF_MARK(1);
+  if (p.alive) ph_tree_qn(c, p);
+  PROF_MARK(2);
+  if (p.alive) ph_det(c, p);
+  PROF_MARK(3);
+  if (p.alive) ph_decide(c, p);
+  PROF_MARK(4);
+  if (p.alive) {
+    if (p.move == 0) ph_accept_add(c, p);
+    else ph_accept_rem(c, p);
+  }
+  PROF_MARK(5);
+  if (c.h->status == ST_OK) ph_finish(c, p);
+  PROF_MARK(6);
 }
 
 // ---------------------------------------------------------------------------
@@ -1627,6 +1679,7 @@ __device__ Ctx make_ctx(const DModel* m, const DGroup* g, Hdr* hsm, int chain, c
   c.M = (double*)(b + g->o_M);
   c.tree = b + g->o_tree;
   c.act = (unsigned char*)(b + g->o_act);
+  c.bstart = (int*)(b + g->o_bstart);
   c.scr = (double*)(b + g->o_scr);
   c.btau[0] = c.scr + 4 * g->kcap;
   c.btau[1] = c.btau[0] + g->opcap + 2;
@@ -1723,9 +1776,11 @@ __global__ void __launch_bounds__(WPB * 32) k_init(const __grid_constant__ DMode
 // One launch advances every chain of every group: warp -> (group, chain).
 __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
     k_sweep(const __grid_constant__ DModel m, const DGroup* __restrict__ groups, int ngroups, int ntotal,
-            long long nprop, int nmeas, int reset) {
+            long long nprop, int nmeas, int reset, int actbytes) {
   __shared__ Hdr hs[WPB];
   __shared__ cthyb_record recs[WPB];
+  __shared__ Prop props[WPB];
+  extern __shared__ __align__(16) unsigned char dyn_act[];
   int warp = threadIdx.x >> 5;
   int gchain = blockIdx.x * WPB + warp;
   if (gchain >= ntotal) return;
@@ -1736,6 +1791,12 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
   Ctx c = make_ctx(&m, &g, &hs[warp], chain, &recs[warp]);
   Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
   load_hdr(c.h, gh, c.lane);
+  // the tree's active bits live in shared memory during the sweep
+  unsigned char* gact = c.act;
+  const int nact4 = (2 << g.L) / 4;
+  c.act = dyn_act + (size_t)warp * actbytes;
+  for (int i = c.lane; i < nact4; i += 32) ((uint32_t*)c.act)[i] = ((const uint32_t*)gact)[i];
+  __syncwarp();
   Hdr& h = *c.h;
   mt_refill(c, h.mt_idx);
   if (reset && c.lane == 0) {  // init_counters, CTQMC.F90:847-899
@@ -1745,10 +1806,10 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
   __syncwarp();
   if (h.status == ST_OK) {
     if (nmeas <= 0) {
-      for (long long i = 0; i < nprop && h.status == ST_OK; ++i) one_step(c);
+      for (long long i = 0; i < nprop && h.status == ST_OK; ++i) one_step(c, props[warp]);
     } else {
       for (int im = 0; im < nmeas && h.status == ST_OK; ++im) {
-        for (int ic = 0; ic < g.ncorr && h.status == ST_OK; ++ic) one_step(c);
+        for (int ic = 0; ic < g.ncorr && h.status == ST_OK; ++ic) one_step(c, props[warp]);
         PROF_START();
         if (h.status == ST_OK) measure(c);
         PROF_MARK(9);
@@ -1759,7 +1820,96 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
     h.mt_idx = mt_index(c);
     if (h.status != ST_OK) atomicMax(g.err_flag, h.status);
   }
+  __syncwarp();
+  for (int i = c.lane; i < nact4; i += 32) ((uint32_t*)gact)[i] = ((const uint32_t*)c.act)[i];
   store_hdr(gh, c.h, c.lane);
+}
+
+// Phase-synchronous sweep: the warps of a block (one chain each) run the
+// phases of their proposals together, with a block-wide barrier between
+// phases, so that the SM's instruction caches serve the code of one phase at
+// a time instead of every warp's own position in the proposal.  Per-warp
+// header, record, proposal state and tree active bits live in dynamic shared
+// memory.  Results are those of k_sweep: each chain's proposal sequence is
+// unchanged, only the interleaving of chains differs.
+__global__ void __launch_bounds__(1024, 1)
+    k_sweep_sync(const __grid_constant__ DModel m, const DGroup* __restrict__ groups, int ngroups, int ntotal,
+                 long long nprop, int nmeas, int reset, int actbytes) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Hdr* hs = (Hdr*)dyn;
+  cthyb_record* recs = (cthyb_record*)(hs + nw);
+  Prop* props = (Prop*)(recs + nw);
+  unsigned char* acts = (unsigned char*)(props + nw);
+  const int gchain = blockIdx.x * nw + warp;
+  const bool valid = gchain < ntotal;
+  Prop& p = props[warp];
+  Ctx c;
+  const DGroup* gp = nullptr;
+  unsigned char* gact = nullptr;
+  Hdr* gh = nullptr;
+  long long total = 0;
+  int nact4 = 0;
+  if (valid) {
+    int gi = 0;
+    while (gi + 1 < ngroups && gchain >= groups[gi + 1].chain0) ++gi;
+    gp = &groups[gi];
+    const int chain = gchain - gp->chain0;
+    c = make_ctx(&m, gp, &hs[warp], chain, &recs[warp]);
+    gh = (Hdr*)(gp->base + (size_t)chain * gp->stride + gp->o_hdr);
+    load_hdr(c.h, gh, lane);
+    gact = c.act;
+    nact4 = (2 << gp->L) / 4;
+    c.act = acts + (size_t)warp * actbytes;
+    for (int i = lane; i < nact4; i += 32) ((uint32_t*)c.act)[i] = ((const uint32_t*)gact)[i];
+    __syncwarp();
+    mt_refill(c, c.h->mt_idx);
+    if (reset && lane == 0) {  // init_counters, CTQMC.F90:847-899
+      Hdr& h = *c.h;
+      h.try_add = h.acc_add = h.try_rem = h.acc_rem = h.qn_add = h.qn_rem = 0;
+      h.nprop = 0;
+    }
+    __syncwarp();
+    total = nmeas <= 0 ? nprop : (long long)nmeas * gp->ncorr;
+  }
+  long long i = 0;
+  for (;;) {
+    const bool mine = valid && i < total && c.h->status == ST_OK;
+    if (!__syncthreads_or(mine)) break;
+    if (mine) ph_draw(c, p);
+    else if (lane == 0) p.alive = 0;
+    __syncthreads();
+    if (p.alive) {
+      if (p.move == 0) ph_setup_add(c, p);
+      else ph_setup_rem(c, p);
+    }
+    __syncthreads();
+    if (p.alive) ph_tree_qn(c, p);
+    __syncthreads();
+    if (p.alive) ph_det(c, p);
+    __syncthreads();
+    if (p.alive) ph_decide(c, p);
+    __syncthreads();
+    if (p.alive) {
+      if (p.move == 0) ph_accept_add(c, p);
+      else ph_accept_rem(c, p);
+    }
+    __syncthreads();
+    if (mine && c.h->status == ST_OK) {
+      ph_finish(c, p);
+      ++i;
+      if (nmeas > 0 && i % gp->ncorr == 0 && c.h->status == ST_OK) measure(c);
+    }
+  }
+  if (valid) {
+    if (lane == 0) {
+      c.h->mt_idx = mt_index(c);
+      if (c.h->status != ST_OK) atomicMax(gp->err_flag, c.h->status);
+    }
+    __syncwarp();
+    for (int i2 = lane; i2 < nact4; i2 += 32) ((uint32_t*)gact)[i2] = ((const uint32_t*)c.act)[i2];
+    store_hdr(gh, c.h, lane);
+  }
 }
 
 // set_mc_config: operator arrays from a time-ordered list already written
@@ -2051,6 +2201,7 @@ struct cthyb_batch_s {
   cudaStream_t stream = nullptr;
   int nchains = 0;
   int use_graphs = 0;
+  int sync_warps = 0;  // 0: independent warps (k_sweep); n: phase-synchronous blocks of n warps
   long long logcap = 0;
   bool counters_reset_pending = false;
   double* d_red = nullptr;
@@ -2194,7 +2345,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
     L = 1;
     while ((1 << L) < opcap / 4 && L < 12) ++L;
   }
-  if (L > 16) L = 16;
+  if (L > 10) L = 10;  // the sweep keeps 2^(L+1) active bits per chain in shared memory
   g.L = L;
   g.binscale = (double)(1 << L) / d.beta;
   const bool mono = hm.monomial && !g.dense;
@@ -2223,6 +2374,8 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   off = align_up(off + nodes * 2 * g.node_bytes, 256);
   g.o_act = off;
   off = align_up(off + nodes, 256);
+  g.o_bstart = off;
+  off = align_up(off + ((size_t)(1 << L) + 1) * 4, 256);
   g.o_scr = off;
   off = align_up(off + (size_t)(4 * kcap + 2 * (opcap + 2) + 2 * (opcap + 3)) * 8 + (size_t)2 * (opcap + 2) * 4, 256);
   g.o_gtau = off;
@@ -2367,10 +2520,29 @@ int cthyb_batch_set_taudiffmax(cthyb_batch_t B, int group, double tdm) {
 }
 
 static int launch_sweeps(cthyb_batch_t B, long long nprop, int nmeas, int reset) {
-  int nblk = (B->nchains + WPB - 1) / WPB;
-  k_sweep<<<nblk, WPB * 32, 0, B->stream>>>(B->model->dm, B->d_groups, (int)B->groups.size(), B->nchains, nprop,
-                                            nmeas, reset);
+  int Lmax = 1;
+  for (GroupHost& G : B->groups) Lmax = std::max(Lmax, G.g.L);
+  const int actbytes = 2 << Lmax;
+  if (B->sync_warps > 0) {
+    const int nw = B->sync_warps;
+    const int nblk = (B->nchains + nw - 1) / nw;
+    const size_t smem = (size_t)nw * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + actbytes);
+    if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_sweep_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_sweep_sync<<<nblk, nw * 32, smem, B->stream>>>(B->model->dm, B->d_groups, (int)B->groups.size(), B->nchains,
+                                                     nprop, nmeas, reset, actbytes);
+  } else {
+    const int nblk = (B->nchains + WPB - 1) / WPB;
+    k_sweep<<<nblk, WPB * 32, (size_t)WPB * actbytes, B->stream>>>(B->model->dm, B->d_groups,
+                                                                   (int)B->groups.size(), B->nchains, nprop, nmeas,
+                                                                   reset, actbytes);
+  }
   CK(cudaGetLastError());
+  return CTHYB_OK;
+}
+
+int cthyb_batch_set_schedule(cthyb_batch_t B, int warps_per_block) {
+  if (!B || warps_per_block < 0 || warps_per_block > 32) return fail(CTHYB_ERR_ARG, "warps_per_block must be 0..32");
+  B->sync_warps = warps_per_block;
   return CTHYB_OK;
 }
 

@@ -61,7 +61,7 @@ struct DGroup {
   int kcap, opcap, L, dense, meas_dm;
   char* base;          // chain c at base + c*stride
   size_t stride;
-  size_t o_hdr, o_mt, o_optau, o_opcode, o_srt_tau, o_srt_slot, o_slot_tau, o_M, o_tree, o_act,
+  size_t o_hdr, o_mt, o_optau, o_opcode, o_srt_tau, o_srt_slot, o_slot_tau, o_M, o_tree, o_act, o_bstart,
       o_scr, o_gtau, o_histo, o_dm, o_dense, o_log;
   size_t node_bytes;   // bytes of one node slot
   long long logcap;

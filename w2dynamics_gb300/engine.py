@@ -27,7 +27,7 @@ EXPORTS = (
     "cthyb_model_states", "cthyb_model_connect", "cthyb_batch_create", "cthyb_batch_destroy",
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
-    "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_results",
+    "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_results",
     "cthyb_batch_group_sums", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
@@ -83,6 +83,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_sync.argtypes = [vp]
     L.cthyb_batch_stream.argtypes = [vp, C.POINTER(vp)]
     L.cthyb_batch_use_graphs.argtypes = [vp, C.c_int]
+    L.cthyb_batch_set_schedule.argtypes = [vp, C.c_int]
     L.cthyb_batch_results.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_group_sums.argtypes = [vp, C.c_int, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_state.argtypes = [vp, C.c_int, dp]
@@ -228,6 +229,10 @@ class Batch:
 
     def use_graphs(self, on=True):
         _check(load().cthyb_batch_use_graphs(self.h, 1 if on else 0))
+
+    def set_schedule(self, warps_per_block):
+        """0: independent warps; n (1..32): phase-synchronous blocks of n chains."""
+        _check(load().cthyb_batch_set_schedule(self.h, int(warps_per_block)))
 
     # --- results
     def results(self, chain):
