@@ -112,10 +112,11 @@ int cthyb_batch_stream(cthyb_batch_t batch, void** stream);
  * (1 = on, default off). */
 int cthyb_batch_use_graphs(cthyb_batch_t batch, int on);
 /* How the sweep kernel schedules chains (no reference counterpart: the
- * Fortran code runs one chain per process).  0 (default) = independent
- * warps, four chains per block; n in 1..32 = phase-synchronous blocks of n
- * chains whose proposals advance phase by phase together.  Per-chain
- * results do not depend on the schedule. */
+ * Fortran code runs one chain per process).  -1 (default) = automatic
+ * (phase-synchronous, two blocks per multiprocessor, at most 16 chains a
+ * block); 0 = independent warps, four chains per block; n in 1..32 =
+ * phase-synchronous blocks of n chains whose proposals advance phase by
+ * phase together.  Per-chain results do not depend on the schedule. */
 int cthyb_batch_set_schedule(cthyb_batch_t batch, int warps_per_block);
 
 /* Normalised results of one chain (CTQMC.F90:8676-8760):

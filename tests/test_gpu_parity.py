@@ -165,7 +165,7 @@ def test_batched_chains_match_oracle_per_seed(lib):
         assert np.array_equal(t_o, t_g), c
 
 
-@pytest.mark.parametrize("warps", [7, 32])
+@pytest.mark.parametrize("warps", [-1, 7, 32])
 def test_phase_synchronous_schedule_matches_oracle(lib, warps):
     """The phase-synchronous schedule (blocks of `warps` chains, a partial
     last block) runs every chain as the reference chain of its own seed, and

@@ -566,29 +566,66 @@ __device__ __forceinline__ void leaf_body(Ctx& c, int b, int n, int slot, bool d
     const double* bdt = c.bdt[buf];
     double* lw = node_lw(c, node, slot);
     uint16_t* tg = node_tg(c, node, slot);
-    for (int s = c.lane; s < m.ns; s += 32) {
-      int cur = s;
-      double l = 0.0;
-      int neg = 0;
-      for (int j = 0; j < n; ++j) {
-        l = fma(-m.evs[cur], bdt[j], l);
-        size_t idx = (size_t)bcode[j] * m.ns + cur;
-        int nx = m.mono_tgt[idx];
-        if (nx < 0) {
-          cur = -1;
-          break;
+    if (m.ns <= 16 * c.kcap) {
+      // Integer walk first (target state and sign of every start state),
+      // then the log weights of the surviving start states only, one per
+      // lane: the FP64 work scales with the survivors, not with the states.
+      int16_t* surv = (int16_t*)c.scr;  // the determinant scratch is idle here
+      int nsurv = 0;
+      for (int s0 = 0; s0 < m.ns; s0 += 32) {
+        const int s = s0 + c.lane;
+        int cur = s < m.ns ? s : -1, neg = 0;
+        for (int j = 0; j < n && cur >= 0; ++j) {
+          const size_t idx = (size_t)bcode[j] * m.ns + cur;
+          neg ^= m.mono_neg[idx];
+          cur = m.mono_tgt[idx];
         }
-        l += m.mono_lv[idx];
-        neg ^= m.mono_neg[idx];
-        cur = nx;
+        if (s < m.ns) {
+          tg[s] = cur >= 0 ? (uint16_t)(cur | (neg << 15)) : (uint16_t)0x7fff;
+          if (cur < 0) lw[s] = -DHUGE;
+        }
+        const unsigned bal = __ballot_sync(FULL, cur >= 0);
+        if (cur >= 0) surv[nsurv + __popc(bal & ((1u << c.lane) - 1u))] = (int16_t)s;
+        nsurv += __popc(bal);
       }
-      if (cur >= 0) {
-        l = fma(-m.evs[cur], bdt[n], l);
-        tg[s] = (uint16_t)(cur | (neg << 15));
-        lw[s] = l;
-      } else {
-        tg[s] = 0x7fff;
-        lw[s] = -DHUGE;
+      __syncwarp();
+      for (int q = c.lane; q < nsurv; q += 32) {
+        const int s = surv[q];
+        int cur = s;
+        double l = 0.0;
+        for (int j = 0; j < n; ++j) {
+          l = fma(-m.evs[cur], bdt[j], l);
+          const size_t idx = (size_t)bcode[j] * m.ns + cur;
+          if (!m.mono_lv0) l += m.mono_lv[idx];
+          cur = m.mono_tgt[idx];
+        }
+        lw[s] = fma(-m.evs[cur], bdt[n], l);
+      }
+    } else {
+      for (int s = c.lane; s < m.ns; s += 32) {
+        int cur = s;
+        double l = 0.0;
+        int neg = 0;
+        for (int j = 0; j < n; ++j) {
+          l = fma(-m.evs[cur], bdt[j], l);
+          size_t idx = (size_t)bcode[j] * m.ns + cur;
+          int nx = m.mono_tgt[idx];
+          if (nx < 0) {
+            cur = -1;
+            break;
+          }
+          l += m.mono_lv[idx];
+          neg ^= m.mono_neg[idx];
+          cur = nx;
+        }
+        if (cur >= 0) {
+          l = fma(-m.evs[cur], bdt[n], l);
+          tg[s] = (uint16_t)(cur | (neg << 15));
+          lw[s] = l;
+        } else {
+          tg[s] = 0x7fff;
+          lw[s] = -DHUGE;
+        }
       }
     }
   }
@@ -1031,7 +1068,7 @@ __device__ NOINL void write_record(Ctx& c, const cthyb_record& r) {
 // Trace of the proposed configuration as sum * exp(mx).
 __device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum) {
   if (c.mono) {
-    root_trace(c, 1 - c.act[1], s0, mx, sum);  // tree rebuilt with the QN check
+    root_trace(c, 1 - c.act[1], s0, mx, sum);  // state tree rebuilt after the QN check
   } else {
     dense_trace(c, md, s0, mx, sum);  // log|trace| and its sign
   }
@@ -1048,7 +1085,7 @@ __device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum)
 struct Prop {
   int move, alive, co, f, k, K, fpos_c, fpos_a, p1, p2, snew, np, ix, iy, cax, rank_c, rank_a, slot_c, slot_a,
       accept;
-  double tau_c, tau_a, tdf, hprf, ratio, det_sign, det_log, tr_log, tr_sign, tx, ty;
+  double tau_c, tau_a, tdf, hprf, ratio, det_sign, det_log, tr_log, tr_sign, tr_mx, tr_sum, tx, ty;
   Mod md;
 };
 
@@ -1268,10 +1305,10 @@ __device__ NOINL void ph_setup_rem(Ctx& c, Prop& p) {
 // Phase 2: proposed tree and the quantum-number check
 // (check_sst_sequence, Trace.F90:1243-1304; CTQMC.F90:3421-3470 and
 // 3928-3976).
-__device__ NOINL void ph_tree_qn(Ctx& c, Prop& p) {
+__device__ NOINL void ph_tree_ss(Ctx& c, Prop& p) {
   Hdr& h = *c.h;
   Mod& md = p.md;
-  tree_propose(c, md, true, c.mono != 0, true);
+  tree_propose(c, md, true, false, true);  // superstate maps (integer only)
   int root_new = 1 - c.act[1];
   int s0 = h.outer_sst, snew = s0;
   bool ok;
@@ -1291,6 +1328,12 @@ __device__ NOINL void ph_tree_qn(Ctx& c, Prop& p) {
     }
     prop_end(c, p, 1);
   }
+}
+
+// Phase 2b: state maps and log weights of the proposed tree (monomial
+// models), only for proposals that passed the QN check.
+__device__ NOINL void ph_tree_states(Ctx& c, Prop& p) {
+  if (c.mono) tree_propose(c, p.md, false, true, false);
 }
 
 // Phase 3: determinant ratio.  Insertion: S - R.(M Q)
@@ -1341,12 +1384,18 @@ __device__ NOINL void ph_det(Ctx& c, Prop& p) {
 // Phase 4: trace of the proposed configuration, NPairs of the new
 // configuration (update_NPairs / ensure_valid_NPairs, Trace.F90:1756-1922)
 // and the Metropolis decision (CTQMC.F90:3508-3524, 4050-4058).
+__device__ NOINL void ph_trace(Ctx& c, Prop& p) {
+  double tr_mx, tr_sum;
+  proposed_trace(c, p.md, p.snew, tr_mx, tr_sum);
+  p.tr_mx = tr_mx;
+  p.tr_sum = tr_sum;
+  __syncwarp();
+}
 __device__ NOINL void ph_decide(Ctx& c, Prop& p) {
   Hdr& h = *c.h;
   const DModel& m = *c.m;
   cthyb_record& r = *c.rec;
-  double tr_mx, tr_sum;
-  proposed_trace(c, p.md, p.snew, tr_mx, tr_sum);
+  const double tr_mx = p.tr_mx, tr_sum = p.tr_sum;
   const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
   const int f = p.f, k = p.k, K = p.K;
   double prob, rnd;
@@ -1577,10 +1626,12 @@ __device__ void one_step(Ctx& c, Prop& p) {
   if (p.move == 0) ph_setup_add(c, p);
   else ph_setup_rem(c, p);
   PROF_MARK(1);
-  if (p.alive) ph_tree_qn(c, p);
+  if (p.alive) ph_tree_ss(c, p);
+  if (p.alive) ph_tree_states(c, p);
   PROF_MARK(2);
   if (p.alive) ph_det(c, p);
   PROF_MARK(3);
+  if (p.alive) ph_trace(c, p);
   if (p.alive) ph_decide(c, p);
   PROF_MARK(4);
   if (p.alive) {
@@ -1872,35 +1923,53 @@ __global__ void __launch_bounds__(1024, 1)
     __syncwarp();
     total = nmeas <= 0 ? nprop : (long long)nmeas * gp->ncorr;
   }
+  // One barrier after each phase: draw, set-up, superstate tree + QN check,
+  // state tree, determinant, trace, decision, accepted-move updates,
+  // bookkeeping and measurement.  A warp with nothing to do in a phase
+  // (proposal ended, chain finished, no chain) only meets the barrier.
   long long i = 0;
+#ifdef CTHYB_PROFILE
+  // prof[k]: work of phase k (0..8, phase 8 = bookkeeping); prof[9]: waits
+#define SPROF(k)  \
+  if (valid) {    \
+    PROF_MARK(k); \
+  }
+  PROF_START();
+#else
+#define SPROF(k)
+#endif
+#define PHASE(k, stmt) \
+  if (p.alive) {       \
+    stmt;              \
+  }                    \
+  SPROF(k);            \
+  __syncthreads();     \
+  SPROF(9);
   for (;;) {
     const bool mine = valid && i < total && c.h->status == ST_OK;
     if (!__syncthreads_or(mine)) break;
+    SPROF(9);
     if (mine) ph_draw(c, p);
     else if (lane == 0) p.alive = 0;
+    SPROF(0);
     __syncthreads();
-    if (p.alive) {
-      if (p.move == 0) ph_setup_add(c, p);
-      else ph_setup_rem(c, p);
-    }
-    __syncthreads();
-    if (p.alive) ph_tree_qn(c, p);
-    __syncthreads();
-    if (p.alive) ph_det(c, p);
-    __syncthreads();
-    if (p.alive) ph_decide(c, p);
-    __syncthreads();
-    if (p.alive) {
-      if (p.move == 0) ph_accept_add(c, p);
-      else ph_accept_rem(c, p);
-    }
-    __syncthreads();
+    SPROF(9);
+    PHASE(1, if (p.move == 0) ph_setup_add(c, p); else ph_setup_rem(c, p))
+    PHASE(2, ph_tree_ss(c, p))
+    PHASE(3, ph_tree_states(c, p))
+    PHASE(4, ph_det(c, p))
+    PHASE(5, ph_trace(c, p))
+    PHASE(6, ph_decide(c, p))
+    PHASE(7, if (p.move == 0) ph_accept_add(c, p); else ph_accept_rem(c, p))
     if (mine && c.h->status == ST_OK) {
       ph_finish(c, p);
       ++i;
       if (nmeas > 0 && i % gp->ncorr == 0 && c.h->status == ST_OK) measure(c);
     }
+    SPROF(8);
   }
+#undef PHASE
+#undef SPROF
   if (valid) {
     if (lane == 0) {
       c.h->mt_idx = mt_index(c);
@@ -2201,7 +2270,8 @@ struct cthyb_batch_s {
   cudaStream_t stream = nullptr;
   int nchains = 0;
   int use_graphs = 0;
-  int sync_warps = 0;  // 0: independent warps (k_sweep); n: phase-synchronous blocks of n warps
+  int sync_warps = -1;  // -1: automatic; 0: independent warps (k_sweep); n: phase-synchronous blocks of n warps
+  int nsm = 0;          // multiprocessors of the device
   long long logcap = 0;
   bool counters_reset_pending = false;
   double* d_red = nullptr;
@@ -2249,6 +2319,9 @@ static int model_upload(cthyb_model_t M) {
   d.nss = hm.nss;
   d.nsmax = hm.nsmax;
   d.monomial = hm.monomial;
+  d.mono_lv0 = 1;
+  for (double x : hm.mono_lv)
+    if (x != 0.0) d.mono_lv0 = 0;
   d.egs = hm.egs;
   cudaError_t e = cudaSuccess;
   auto up = [&](auto& vec) {
@@ -2340,10 +2413,14 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   int opcap = d.opcap > 0 ? d.opcap : std::max(64, std::min(nf * kcap * 2, (int)(64 + 16 * d.beta)));
   g.kcap = kcap;
   g.opcap = opcap;
+  // Default depth: two leaves up to 512 operators, then one level more per
+  // factor four (measured optimum of the proposal rate for density-density
+  // models: the leaf rebuild grows with the operators of a bin, the combine
+  // steps with the depth).
   int L = d.tree_levels;
   if (L <= 0) {
     L = 1;
-    while ((1 << L) < opcap / 4 && L < 12) ++L;
+    while ((512ll << (2 * (L - 1))) < opcap && L < 10) ++L;
   }
   if (L > 10) L = 10;  // the sweep keeps 2^(L+1) active bits per chain in shared memory
   g.L = L;
@@ -2424,6 +2501,11 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
   if (e == cudaSuccess) e = cudaMalloc(&B->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemsetAsync(B->d_err, 0, sizeof(int), B->stream);
   if (e == cudaSuccess) e = cudaMalloc(&B->d_dev, sizeof(double));
+  if (e == cudaSuccess) {
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, dev);
+  }
   if (e != cudaSuccess) {
     cthyb_batch_destroy(B);
     return fail(CTHYB_ERR_CUDA, std::string("batch allocation: ") + cudaGetErrorString(e));
@@ -2523,8 +2605,12 @@ static int launch_sweeps(cthyb_batch_t B, long long nprop, int nmeas, int reset)
   int Lmax = 1;
   for (GroupHost& G : B->groups) Lmax = std::max(Lmax, G.g.L);
   const int actbytes = 2 << Lmax;
-  if (B->sync_warps > 0) {
-    const int nw = B->sync_warps;
+  // Automatic schedule: phase-synchronous blocks, two per multiprocessor,
+  // chains spread evenly over the multiprocessors (at 64 registers a thread
+  // an SM holds 32 chain warps).
+  int nw = B->sync_warps;
+  if (nw < 0) nw = std::min(16, std::max(1, (B->nchains + 2 * B->nsm - 1) / (2 * std::max(B->nsm, 1))));
+  if (nw > 0) {
     const int nblk = (B->nchains + nw - 1) / nw;
     const size_t smem = (size_t)nw * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + actbytes);
     if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_sweep_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -2541,7 +2627,7 @@ static int launch_sweeps(cthyb_batch_t B, long long nprop, int nmeas, int reset)
 }
 
 int cthyb_batch_set_schedule(cthyb_batch_t B, int warps_per_block) {
-  if (!B || warps_per_block < 0 || warps_per_block > 32) return fail(CTHYB_ERR_ARG, "warps_per_block must be 0..32");
+  if (!B || warps_per_block < -1 || warps_per_block > 32) return fail(CTHYB_ERR_ARG, "warps_per_block must be -1..32");
   B->sync_warps = warps_per_block;
   return CTHYB_OK;
 }

@@ -21,6 +21,7 @@ enum : int {
 
 struct DModel {
   int nd, nf, ns, nss, nsmax, monomial;
+  int mono_lv0;                // every monomial log|value| is zero (density-density models)
   double egs;
   const int* sst_n;            // [nss]
   const int* sst_off;          // [nss]

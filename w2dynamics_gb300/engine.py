@@ -231,7 +231,7 @@ class Batch:
         _check(load().cthyb_batch_use_graphs(self.h, 1 if on else 0))
 
     def set_schedule(self, warps_per_block):
-        """0: independent warps; n (1..32): phase-synchronous blocks of n chains."""
+        """-1: automatic; 0: independent warps; n (1..32): phase-synchronous blocks of n chains."""
         _check(load().cthyb_batch_set_schedule(self.h, int(warps_per_block)))
 
     # --- results
