@@ -58,6 +58,14 @@ int cthyb_model_info(cthyb_model_t model, int* nsst, int* nstates, int* nsmax,
  * CTQMC.F90:8040-8060) */
 int cthyb_model_states(cthyb_model_t model, int* sst_size, int* sst_offset,
                        int* fock_state, double* evals);
+/* Occupation basis and eigenvectors: occ_fock[i] = Fock state (bit
+ * (b-1)+Nd*(s-1) set when occupied) of basis vector i in superstate order
+ * (States of each superstate, States.F90:58-186; OccbasisMapping,
+ * CTQMC.F90:8061); evec (nstates x nstates, column-major, block diagonal)
+ * holds the H_loc eigenvectors in that basis, the Evec of
+ * Transform_DensityMatrix_EB_to_OCCB (CTQMC.F90:3163-3179).  Either
+ * pointer may be NULL. */
+int cthyb_model_basis(cthyb_model_t model, int* occ_fock, double* evec);
 /* target superstate of operator (b,s,ca) acting on superstate sst, 1-based
  * b, s, ca (the Connect table, States.F90:45), -1 if none */
 int cthyb_model_connect(cthyb_model_t model, int sst, int b, int s, int ca);

@@ -1,0 +1,107 @@
+"""The mctqmc drop-in module: parameter-string rules (Parameters.F90:281-320,
+77-160) and rejection of unsupported modes on the CPU; a full solve through
+the module's entry points against the oracle on the GPU."""
+import numpy as np
+import pytest
+
+import oracle as O
+from w2dynamics_gb300 import estimators as ES
+from w2dynamics_gb300 import mctqmc as ctqmc
+from w2dynamics_gb300 import problems as P
+
+
+def pstring(d):
+    # the driver's config_to_pstring (cthyb_solver.py:765-767)
+    return "".join("%s = %s #\n" % (k, v) for k, v in sorted(d.items()))
+
+
+BASE = {"beta": 10.0, "Nd": 3, "Ntau": 40, "NCorr": 50, "Nmeas": 60, "Nwarmups": 2000,
+        "MaxHisto": 60, "TaudiffMax": 5.0, "QuantumNumbers": "Nt Szt",
+        "PercentageGlobalMove": 0.0, "PercentageTauShiftMove": 0.0,
+        "Percentage4OperatorMove": 0.0, "PercentageOuterMove": 0.1,
+        "PercentageWormInsert": 0.0, "segment": 0, "offdiag": 0, "statesampling": 0,
+        "MeasDensityMatrix": 1, "Eigenbasis": 1, "NLegMax": 10}
+
+
+def test_parameter_string_rules():
+    ctqmc.init_paras("# comment line\nNCorr = 1e2 # trailing\nbeta=\t25.5\nNd = 3\n"
+                     "QuantumNumbers = Nt Szt #\nSymMove01 = 1,2\n")
+    assert ctqmc._int("NCorr") == 100          # integer given in scientific notation
+    assert ctqmc._real("beta") == 25.5         # tabs are blanks
+    assert ctqmc._str("QuantumNumbers") == "Nt Szt"
+    assert ctqmc._raw("SymMove01") == "1 2"     # commas are blanks
+    assert ctqmc._int("N") == 100               # prefix match: first name starting with "N"
+    with pytest.raises(KeyError):
+        ctqmc._int("Nmeas")
+    with pytest.raises(ValueError):
+        ctqmc.init_paras("NCorr = 1.5\n")
+        ctqmc._int("NCorr")
+    ctqmc.dest_paras()
+
+
+@pytest.mark.parametrize("key,val", [("PercentageGlobalMove", 0.005),
+                                     ("PercentageTauShiftMove", 0.005),
+                                     ("Percentage4OperatorMove", 0.1), ("segment", 1),
+                                     ("offdiag", 1), ("statesampling", 1)])
+def test_unsupported_modes_are_rejected(key, val):
+    ctqmc.init_paras(pstring(dict(BASE, **{key: val})))
+    with pytest.raises(NotImplementedError, match=key):
+        ctqmc._check_supported()
+    ctqmc.dest_paras()
+
+
+def test_supported_configuration_passes_the_check():
+    ctqmc.init_paras(pstring(BASE))
+    ctqmc._check_supported()
+    ctqmc.dest_paras()
+
+
+@pytest.mark.gpu
+def test_solve_through_the_module_matches_the_oracle():
+    """init_rnd/init_paras/init_solver/set_taudiffmax/ctqmc_warmup/
+    ctqmc_measure as cthyb_solver.py calls them; the results equal the
+    oracle chain of the same seed (identical proposal streams)."""
+    pr = P.config_problem("dd3", beta=10.0)
+    nd, ntau = 3, BASE["Ntau"]
+    ftau = pr["ftau"]
+    ftau_full = np.zeros((nd, 2, nd, 2, ftau.shape[-1]))
+    for b in range(nd):
+        for s in range(2):
+            ftau_full[b, s, b, s] = ftau[b, s]
+    umat = np.asarray(pr["umatrix"]).reshape((2 * nd,) * 4)
+    ctqmc.init_rnd(11)
+    ctqmc.init_paras(pstring(BASE))
+    ctqmc.init_solver(umat, ftau_full, pr["muimp"], np.zeros_like(ftau_full), 1)
+    ctqmc.set_taudiffmax(BASE["TaudiffMax"])
+    ctqmc.ctqmc_warmup(BASE["Nwarmups"])
+    ctqmc.ctqmc_measure(1, 1)
+    mo = O.Model(nd, pr["umatrix"], pr["muimp"], "Nt Szt")
+    co = O.Chain(mo, 10.0, ftau, ntau, seed=11, taudiff_max=5.0, ncorr=BASE["NCorr"],
+                 p_outer=0.1, maxhisto=BASE["MaxHisto"] + 1)
+    co.set_taudiffmax(5.0)
+    co.warmup(BASE["Nwarmups"])
+    co.measure(BASE["Nmeas"])
+    ro = co.results()
+    assert ctqmc.mean_sign == ro["mean_sign"]
+    gg = np.stack([ctqmc.gtau[f // 2, f % 2] for f in range(2 * nd)])
+    assert np.allclose(gg, ro["gtau"], rtol=1e-9, atol=1e-12)
+    hg = np.stack([ctqmc.histo[f // 2, f % 2] for f in range(2 * nd)])
+    assert np.array_equal(hg, ro["histo"])
+    evec = np.zeros((mo.nstates, mo.nstates))
+    for s in range(len(mo.sst_size)):
+        o, n = mo.sst_offset[s], mo.sst_size[s]
+        evec[o:o + n, o:o + n] = mo.evec(s)
+    ref = ES.from_density_matrix(nd, mo.fock_states, evec, ro["densitymatrix"])
+    assert np.allclose(ctqmc.densitymatrix, ref["densitymatrix"], atol=1e-10)
+    assert np.allclose(ctqmc.occ, ref["occ"], atol=1e-10)
+    assert np.allclose(ctqmc.rho1, ref["rho1"], atol=1e-10)
+    assert ctqmc.gtau_full.shape == (nd, 2, nd, 2, ntau)
+    assert ctqmc.occbasismapping.shape == (mo.nstates, nd, 2)
+    cnt = co.counters()
+    assert ctqmc.accadd[0] == cnt["acc_add"] / cnt["try_add"]
+    n, outer, _ = ctqmc.get_mc_config_scalars()
+    taus, orbs, spins, cas, hashybs, outer2, _ = ctqmc.get_mc_config(n)
+    t_o, *_ = co.get_config()
+    assert np.array_equal(taus, t_o) and outer2 == outer
+    ctqmc.dest_ctqmc()
+    ctqmc.dest_paras()

@@ -1883,7 +1883,11 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
 // header, record, proposal state and tree active bits live in dynamic shared
 // memory.  Results are those of k_sweep: each chain's proposal sequence is
 // unchanged, only the interleaving of chains differs.
-__global__ void __launch_bounds__(1024, 1)
+#ifndef SYNC_MAX_THREADS
+#define SYNC_MAX_THREADS 1024  // register budget: 64 per thread, 32 chain warps per SM
+#define SYNC_MIN_BLOCKS 1
+#endif
+__global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
     k_sweep_sync(const __grid_constant__ DModel m, const DGroup* __restrict__ groups, int ngroups, int ntotal,
                  long long nprop, int nmeas, int reset, int actbytes) {
   extern __shared__ __align__(16) unsigned char dyn[];
@@ -2381,6 +2385,23 @@ int cthyb_model_states(cthyb_model_t m, int* sst_size, int* sst_offset, int* foc
   for (int i = 0; i < h.ns; ++i) {
     if (fock_state) fock_state[i] = h.fock_of[i];
     if (evals) evals[i] = h.eval[i];
+  }
+  return CTHYB_OK;
+}
+
+int cthyb_model_basis(cthyb_model_t m, int* occ_fock, double* evec) {
+  if (!m) return fail(CTHYB_ERR_ARG, "null model");
+  const HostModel& h = m->hm;
+  if (occ_fock)
+    for (int i = 0; i < h.ns; ++i) occ_fock[i] = h.occ_fock[i];
+  if (evec) {
+    std::fill(evec, evec + (size_t)h.ns * h.ns, 0.0);
+    for (int s = 0; s < h.nss; ++s) {
+      const int n = h.sst_n[s], o = h.sst_off[s];
+      const double* v = h.evec.data() + h.evec_off[s];
+      for (int k = 0; k < n; ++k)
+        for (int i = 0; i < n; ++i) evec[(size_t)(o + k) * h.ns + (o + i)] = v[(size_t)k * n + i];
+    }
   }
   return CTHYB_OK;
 }

@@ -260,6 +260,15 @@ bool build_model(int nd, const double* umat, const double* muimp, const char* qn
     for (int i = 0; i < n; ++i) m.eval[m.sst_off[s] + i] = w[i];
     m.egs = std::min(m.egs, w[0]);
   }
+  // occupation basis and eigenvectors (Evec of Transform_DensityMatrix_EB_to_OCCB)
+  m.occ_fock.resize(ns);
+  m.evec_off.assign(nss, 0);
+  m.evec.clear();
+  for (int s = 0; s < nss; ++s) {
+    for (int i = 0; i < m.sst_n[s]; ++i) m.occ_fock[m.sst_off[s] + i] = (int)members[s][i];
+    m.evec_off[s] = (long long)m.evec.size();
+    m.evec.insert(m.evec.end(), V[s].begin(), V[s].end());
+  }
   // dominant Fock state per eigenstate
   m.fock_of.resize(ns);
   m.state_sst.resize(ns);

@@ -13,6 +13,9 @@ struct HostModel {
   std::vector<int> connect;               // [nss][nf][2], flavour f = 2b+s, ca 0=c+ 1=c
   std::vector<double> eval;               // [ns] eigenvalues, superstate-major, ascending
   std::vector<int> fock_of, state_sst;    // [ns]
+  std::vector<int> occ_fock;              // [ns] Fock state of occupation-basis vector i (superstate order)
+  std::vector<double> evec;               // per superstate n x n column-major eigenvectors, at sst_off^2 offsets
+  std::vector<long long> evec_off;        // [nss]
   std::vector<long long> blk_off;         // [nss][nf][2] offset into blk or -1
   std::vector<double> blk;                // dense blocks n_target x n_source, column-major
   std::vector<int> mono_tgt;              // [2nf][ns]

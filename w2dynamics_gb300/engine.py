@@ -24,7 +24,8 @@ FLAG_NO_DM = 2
 
 EXPORTS = (
     "cthyb_last_error", "cthyb_model_create", "cthyb_model_destroy", "cthyb_model_info",
-    "cthyb_model_states", "cthyb_model_connect", "cthyb_batch_create", "cthyb_batch_destroy",
+    "cthyb_model_states", "cthyb_model_basis", "cthyb_model_connect", "cthyb_batch_create",
+    "cthyb_batch_destroy",
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
     "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_results",
@@ -73,6 +74,7 @@ def load(build_if_missing=False):
     L.cthyb_model_info.argtypes = [vp, ip, ip, ip, ip, dp]
     L.cthyb_model_states.argtypes = [vp, ip, ip, ip, dp]
     L.cthyb_model_connect.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+    L.cthyb_model_basis.argtypes = [vp, ip, dp]
     L.cthyb_batch_create.argtypes = [vp, C.c_int, C.POINTER(GroupDesc), C.POINTER(vp)]
     L.cthyb_batch_destroy.argtypes = [vp]
     L.cthyb_batch_nchains.argtypes = [vp]
@@ -139,6 +141,14 @@ class Model:
 
     def connect(self, sst, b, s, ca):
         return load().cthyb_model_connect(self.h, sst, b, s, ca)
+
+    def basis(self):
+        """(occ_fock, evec): Fock state of each occupation-basis vector in
+        superstate order and the block-diagonal eigenvector matrix."""
+        fk = np.zeros(self.nstates, np.int32)
+        ev = np.zeros(self.nstates * self.nstates)
+        _check(load().cthyb_model_basis(self.h, _ip(fk), _dp(ev)))
+        return fk, ev.reshape((self.nstates, self.nstates), order="F")
 
     def close(self):
         if getattr(self, "h", None):

@@ -1,0 +1,318 @@
+"""Drop-in for the f2py module ``w2dyn.auxiliaries.CTQMC.mctqmc`` on the
+pair-move path.
+
+The reference's Python driver (w2dyn/dmft/cthyb_solver.py:21,113-114,
+240-241,323-345,397-398,947-1035) talks to the Fortran module only through
+these procedures and module variables:
+
+  init_rnd(Nseed)                         CTQMC.F90:9404
+  init_paras(parastr) / dest_paras()      CTQMC.F90:9412 / 9420
+  init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no)
+                                          CTQMC.F90:7894-8086
+  set_taudiffmax(x)                       CTQMC.F90:8180
+  ctqmc_warmup(N)                         CTQMC.F90:8188-8263
+  ctqmc_measure(iSector, iComponent)      CTQMC.F90:8355-8760
+  init_counters()                         CTQMC.F90:847-899
+  get_mc_config_scalars(), get_mc_config(N), set_mc_config(...),
+  set_empty_mc_config(sst, state)         CTQMC.F90:9358-9392
+  dest_ctqmc()                            CTQMC.F90:901
+  gtau, gtau_full, histo, occ, rho1, rho2, densitymatrix, mean_sign,
+  statessuperstates, eigenstatesenergies, occbasismapping, accadd, accrem,
+  time_warmup, time_sim, time_sim_steps, aborted, ...
+
+so ``import w2dynamics_gb300.mctqmc as ctqmc`` in place of the f2py import
+runs the same solve on the GPU engine.  The module keeps the reference's
+singleton semantics (one solver per process).  Parameters are read from the
+parameter string with the reference's rules (Parameters.F90:281-320: one
+``key = value`` per line, text after ``#`` ignored, commas as blanks, a key
+matches the first parameter whose name starts with it).
+
+Beyond the reference: ``GPUChains = n`` in the parameter string runs n
+independent chains (seeds Nseed .. Nseed+n-1) in one batch and combines
+their measurements as one longer run would (sign-weighted), the form in
+which the GPU is used efficiently.
+
+Parameters selecting moves or modes outside the engine (global and tau-shift
+moves, 4-operator and worm moves, segment, off-diagonal hybridisation,
+state sampling, retarded interactions) raise NotImplementedError at
+init_solver.  Estimators that the engine does not measure (Legendre G_l,
+outer-state trace contributions, the trace-recomputation histograms
+lhisto/rhisto) are returned as zeros.  Each init_solver seeds the chains
+from Nseed; the reference continues one global random stream across
+solves, so solves after the first draw different (equally valid) streams.
+"""
+import time
+
+import numpy as np
+
+from . import engine as E
+from . import estimators as ES
+
+NWormSectors = 16  # CTQMC.F90:111
+
+_seed = 0
+_params = []          # (key, value) in input order
+_model = None
+_batch = None
+_nd = 0
+_beta = 0.0
+_nchains = 1
+
+# module variables read by the driver (reset by dest_ctqmc)
+gtau = gtau_full = histo = occ = rho1 = rho2 = densitymatrix = None
+gleg = gleg_full = None
+statessuperstates = eigenstatesenergies = occbasismapping = None
+outersuperstatehisto = outerstatehisto = signhistosuperstates = signhistostates = None
+tracecontribsuperstates = tracecontribstates = None
+lhisto = rhisto = None
+mean_sign = 0.0
+accadd = np.zeros(NWormSectors)
+accrem = np.zeros(NWormSectors)
+accadd4 = accrem4 = accglob = accshift = accflavc = 0.0
+accpair = accpairtau = None
+time_warmup = time_sim = time_sim_steps = 0.0
+aborted = 0
+simid = 0
+fancy_prog = False
+fourpnt = 0
+
+
+# --------------------------------------------------------------- parameters
+def init_rnd(Nseed):
+    """Seed of the random stream (init_rnd, CTQMC.F90:9404)."""
+    global _seed
+    _seed = int(Nseed)
+
+
+def init_paras(parastr):
+    """Parse the parameter string (read_ParameterString, Parameters.F90:281)."""
+    global _params
+    _params = []
+    for line in str(parastr).split("\n"):
+        line = line.replace("\t", " ")
+        if line.startswith("#"):
+            continue
+        if "#" in line:
+            line = line[:line.index("#")]
+        if "=" not in line:
+            continue
+        key, val = line.split("=", 1)
+        _params.append((key.strip(), val.strip().replace(",", " ")))
+
+
+def dest_paras():
+    global _params
+    _params = []
+
+
+def _raw(key):
+    for k, v in _params:  # get_*_Parameter: first name that starts with key
+        if k.startswith(key):
+            return v
+    raise KeyError(f"{key} not found in parameter list")
+
+
+def _int(key, default=None):
+    try:
+        v = _raw(key)
+    except KeyError:
+        if default is None:
+            raise
+        return default
+    try:
+        return int(v.split()[0])
+    except ValueError:
+        r = float(v.split()[0])
+        if r != int(r):
+            raise ValueError(f"{key} is not an integer")
+        return int(r)
+
+
+def _real(key, default=None):
+    try:
+        return float(_raw(key).split()[0])
+    except KeyError:
+        if default is None:
+            raise
+        return default
+
+
+def _str(key, default=None):
+    try:
+        return _raw(key)
+    except KeyError:
+        if default is None:
+            raise
+        return default
+
+
+def _check_supported():
+    bad = []
+    for key in ("PercentageGlobalMove", "PercentageTauShiftMove", "Percentage4OperatorMove",
+                "PercentageWormInsert"):
+        if _real(key, 0.0) != 0.0:
+            bad.append(f"{key} = {_real(key)}")
+    for key in ("segment", "offdiag", "statesampling", "Phonon", "Screening", "Uw", "NSymMove"):
+        if _int(key, 0) != 0:
+            bad.append(f"{key} = {_int(key)}")
+    if _int("Eigenbasis", 1) == 0:
+        bad.append("Eigenbasis = 0")
+    if "All" in _str("QuantumNumbers", "").split():
+        bad.append("QuantumNumbers = All")
+    if bad:
+        raise NotImplementedError("outside the GPU pair-move engine: " + ", ".join(bad))
+
+
+# ------------------------------------------------------------------- solver
+def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
+    """Model and chain(s) for one solve (init_solver, CTQMC.F90:7894-8086)."""
+    global _model, _batch, _nd, _beta, _nchains
+    global statessuperstates, eigenstatesenergies, occbasismapping
+    _check_supported()
+    ftau_full = np.asarray(Ftau_full, np.float64)
+    nd = ftau_full.shape[0]
+    nftau = ftau_full.shape[-1]
+    ftau = np.empty((nd, 2, nftau))
+    for b in range(nd):  # Ftau(ib,is,:) = Ftau_full(ib,is,ib,is,:)
+        for s in range(2):
+            ftau[b, s] = ftau_full[b, s, b, s]
+    mu = np.asarray(muimp_full, np.float64).reshape(nd, 2, nd, 2)
+    um = np.asarray(u_matrix, np.float64).reshape((2 * nd,) * 4)
+    qns = _str("QuantumNumbers", "Nt Szt")
+    dest_ctqmc()
+    _nd, _beta = nd, _real("beta")
+    _nchains = max(1, _int("GPUChains", 1))
+    _model = E.Model(nd, um, mu, qns)
+    group = E.Group(_beta, ftau, _int("Ntau"), nchains=_nchains, seed0=_seed,
+                    taudiff_max=_real("TaudiffMax", -1.0), ncorr=_int("NCorr"),
+                    p_outer=_real("PercentageOuterMove", 0.0), maxhisto=_int("MaxHisto", 500) + 1,
+                    measure_dm=_int("MeasDensityMatrix", 1) != 0)
+    _batch = E.Batch(_model, [group])
+    ns = _model.nstates
+    statessuperstates = np.zeros(ns, np.int32)
+    for s in range(_model.nsst):
+        o, n = _model.sst_offset[s], _model.sst_size[s]
+        statessuperstates[o:o + n] = s
+    eigenstatesenergies = np.array(_model.evals)
+    fk, _ = _model.basis()
+    occbasismapping = np.zeros((ns, nd, 2), np.int32)
+    for b in range(nd):
+        for s in range(2):
+            occbasismapping[:, b, s] = (fk >> (b + s * nd)) & 1
+
+
+def set_taudiffmax(x):
+    _batch.set_taudiffmax(0, float(x))
+
+
+def ctqmc_warmup(N):
+    global time_warmup
+    t0 = time.perf_counter()
+    _batch.warmup(int(N))
+    _batch.sync()
+    time_warmup = time.perf_counter() - t0
+
+
+def init_counters():
+    """Counters restart with every measurement call of the engine."""
+
+
+def ctqmc_measure(iSector=1, iComponent=1):
+    """Z-space loop and normalised results (CTQMC.F90:8355-8760)."""
+    global time_sim, time_sim_steps
+    if iSector != 1:
+        raise NotImplementedError("worm sectors are outside the GPU pair-move engine")
+    t0 = time.perf_counter()
+    _batch.reset_measurements()
+    _batch.measure(_int("Nmeas"))
+    _batch.sync()
+    time_sim = time_sim_steps = time.perf_counter() - t0
+    _collect()
+
+
+def _collect():
+    global gtau, gtau_full, histo, occ, rho1, rho2, densitymatrix, mean_sign, gleg, gleg_full
+    global accadd, accrem, outersuperstatehisto, outerstatehisto, signhistosuperstates
+    global signhistostates, tracecontribsuperstates, tracecontribstates, lhisto, rhisto
+    nd, ns, nf = _nd, _model.nstates, 2 * _nd
+    res = [_batch.results(c) for c in range(_nchains)]
+    signs = np.array([r["mean_sign"] for r in res])
+    wsum = signs.sum()
+    # the per-chain results are normalised by their own mean sign; one
+    # combined run is the sign-weighted average
+    gtau = sum(r["gtau"] * s for r, s in zip(res, signs)) / wsum
+    dm_eigen = sum(r["densitymatrix"] * s for r, s in zip(res, signs)) / wsum
+    mean_sign = float(signs.mean())
+    histo = sum(r["histo"] for r in res) / _nchains
+    cnt = {k: sum(r["counters"][k] for r in res) for k in res[0]["counters"]}
+    accadd = np.zeros(NWormSectors)
+    accrem = np.zeros(NWormSectors)
+    accadd[0] = cnt["acc_add"] / max(cnt["try_add"], 1)
+    accrem[0] = cnt["acc_rem"] / max(cnt["try_rem"], 1)
+    gtau_full = np.zeros((nd, 2, nd, 2, gtau.shape[-1]))
+    for b in range(nd):
+        for s in range(2):
+            gtau_full[b, s, b, s] = gtau[b, s]
+    if _int("MeasDensityMatrix", 1) != 0:
+        fk, evec = _model.basis()
+        est = ES.from_density_matrix(nd, fk, evec, dm_eigen)
+        densitymatrix, occ, rho1, rho2 = (est["densitymatrix"], est["occ"], est["rho1"],
+                                          est["rho2"])
+    else:
+        densitymatrix = np.zeros((ns, ns))
+        occ = np.zeros((nd, 2, nd, 2))
+        rho1 = np.zeros((nf, nf))
+        rho2 = np.zeros((nf,) * 4)
+    nleg = _int("NLegMax", 100)
+    gleg = np.zeros((nd, 2, nleg))
+    gleg_full = np.zeros((nd, 2, nd, 2, nleg))
+    nss = _model.nsst
+    outersuperstatehisto = np.zeros(nss)
+    outerstatehisto = np.zeros(ns)
+    signhistosuperstates = np.zeros(nss)
+    signhistostates = np.zeros(ns)
+    tracecontribsuperstates = np.zeros(nss)
+    tracecontribstates = np.zeros(ns)
+    lhisto = np.zeros(1)
+    rhisto = np.zeros(1)
+
+
+# ------------------------------------------------------ configuration access
+def get_mc_config_scalars():
+    """(number of operators, outer superstate, outer state)."""
+    taus, *_ , outer = _batch.get_config(0)
+    return len(taus), outer, 1
+
+
+def get_mc_config(N):
+    """(taus, orbs, spins, cas, hashybs, outer_sst, outer_state), 1-based
+    orbital/spin/ca as in get_mc_config (CTQMC.F90:9367)."""
+    taus, orbs, spins, cas, outer = _batch.get_config(0)
+    n = int(N)
+    return (np.array(taus[:n]), np.array(orbs[:n]), np.array(spins[:n]), np.array(cas[:n]),
+            np.ones(n, np.int32), outer, 1)
+
+
+def set_mc_config(N, taus, orbs, spins, cas, hashybs, outer_sst, outer_state):
+    n = int(N)
+    if np.any(np.asarray(hashybs)[:n] == 0):
+        raise NotImplementedError("operators without hybridisation (worms) are not supported")
+    for c in range(_nchains):
+        _batch.set_config(c, np.asarray(taus)[:n], np.asarray(orbs)[:n], np.asarray(spins)[:n],
+                          np.asarray(cas)[:n], int(outer_sst))
+
+
+def set_empty_mc_config(outer_sst, outer_state):
+    for c in range(_nchains):
+        _batch.set_config(c, np.zeros(0), np.zeros(0, np.int32), np.zeros(0, np.int32),
+                          np.zeros(0, np.int32), int(outer_sst))
+
+
+def dest_ctqmc():
+    """Free the solver (dest_ctqmc, CTQMC.F90:901)."""
+    global _model, _batch
+    if _batch is not None:
+        _batch.close()
+    if _model is not None:
+        _model.close()
+    _batch = _model = None
