@@ -87,6 +87,9 @@ typedef struct {
   int32_t tree_levels;   /* time-bin tree depth, 2^levels leaves (0: automatic) */
   int32_t maxhisto;      /* expansion-order histogram bins (MaxHisto) */
   int32_t flags;         /* CTHYB_FLAG_* */
+  double p_global;       /* PercentageGlobalMove: spin flip, CA flip, random
+                            flavour permutation (StepGlob, CTQMC.F90:4433-4554) */
+  double p_shift;        /* PercentageTauShiftMove (StepShiftTau, CTQMC.F90:4557-4835) */
 } cthyb_group_desc;
 
 #define CTHYB_FLAG_DENSE 1  /* dense block trace even for monomial models */
@@ -126,6 +129,11 @@ int cthyb_batch_use_graphs(cthyb_batch_t batch, int on);
  * phase-synchronous blocks of n chains whose proposals advance phase by
  * phase together.  Per-chain results do not depend on the schedule. */
 int cthyb_batch_set_schedule(cthyb_batch_t batch, int warps_per_block);
+
+/* Global and tau-shift move counters of one chain since the last warmup or
+ * measure call: TryGlob, AccGlob, AccQNGlob, TryShift, AccShift
+ * (CTQMC.F90:134-136). */
+int cthyb_batch_move_counters(cthyb_batch_t batch, int chain, int64_t* counters5);
 
 /* Normalised results of one chain (CTQMC.F90:8676-8760):
  *   gtau (Nd,2,Ntau) Fortran order, mean_sign, densitymatrix in the

@@ -90,6 +90,7 @@ struct Model {
   std::vector<Block> ham, evec;                // per superstate
   std::vector<std::vector<double>> eval;       // ascending per superstate
   double egs = 0;
+  bool has_szt = false;  // glob_has_Szt, CTQMC.F90:317-321
   int cidx(int sst, int b, int s, int ca) const { return ((sst * nd + b) * 2 + s) * 2 + ca; }
   int conn(int sst, int b, int s, int ca) const { return connect[cidx(sst, b, s, ca)]; }
   const Block& peb(int sst, int b, int s, int ca) const { return psis_eb[cidx(sst, b, s, ca)]; }
@@ -229,6 +230,7 @@ static Model* build_model(int nd, const double* umat, const double* muimp, const
     return nullptr;
   }
   bool useNt = q.find("Nt") != std::string::npos, useSzt = q.find("Szt") != std::string::npos;
+  m->has_szt = useSzt;
   bool useQzt = q.find("Qzt") != std::string::npos, useAzt = q.find("Azt") != std::string::npos;
   bool useLzt = q.find("Lzt") != std::string::npos, useJzt = q.find("Jzt") != std::string::npos;
   // qns2substates, States.F90:149-186
@@ -428,6 +430,7 @@ struct Chain {
   int kv = -1, bv = 1 << 30;
   // counters
   long long try_add = 0, try_rem = 0, acc_add = 0, acc_rem = 0, accqn_add = 0, accqn_rem = 0;
+  long long try_glob = 0, acc_glob = 0, accqn_glob = 0, try_shift = 0, acc_shift = 0;
   // measurements
   long long cnt_meas = 0;
   double meas_sign = 0;
@@ -1280,6 +1283,309 @@ static void step_rem(Chain& c, bool change_outer) {
   record(c, r);
 }
 
+// Per-flavour sorted lists of an operator list.
+static void flavour_lists(const Chain& c, const std::vector<Op>& ops, std::vector<std::vector<double>>& tc,
+                          std::vector<std::vector<double>>& ta) {
+  tc.assign(c.nf, {});
+  ta.assign(c.nf, {});
+  for (const Op& o : ops) (o.ca == 0 ? tc : ta)[c.fi(o.b, o.s)].push_back(o.tau);
+}
+
+// Number of superstates s with s -> s under the whole list, their list
+// (check_qn_all_ssts, Trace.F90:1399-1433; -1 for those that fail).
+static int fixed_ssts(const Chain& c, const std::vector<Op>& ops, std::vector<int>& ssts) {
+  ssts.assign(c.m->nss, -1);
+  int n = 0;
+  for (int s = 0; s < c.m->nss; ++s)
+    if (walk(c, ops, s, 0, (int)ops.size()) == s) {
+      ssts[s] = s;
+      ++n;
+    }
+  return n;
+}
+
+enum { GLOB_RANDPERM = 1, GLOB_USERSYM = 2, GLOB_SPINFLIP = 3, GLOB_CAFLIP = 4 };
+enum { MOVE_GLOB = 2, MOVE_SHIFT = 3, MOVE_OUTER = 4 };
+
+// StepGlob, CTQMC.F90:4433-4554 (diagonal hybridisation; no user symmetry
+// moves): gen_SpinFlipUpdate / gen_CAFlip / gen_GlobalUpdate_new
+// (Trace.F90:1103-1198), the QN checks perform_spinflip_check_qn /
+// perform_global_check_qn (Trace.F90:1306-1394), globalUpdate
+// (Trace.F90:2126-2188), get_InvFullHybr and get_FullLogDet
+// (Trace.F90:2279-2336, 2665-2685), full trace, Metropolis with wrat.
+static void step_glob(Chain& c) {
+  c.try_glob++;
+  Record r{};
+  r.move = MOVE_GLOB;
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  if (c.ops.empty()) {
+    r.outcome = OUT_NOPAIRS;
+    record(c, r);
+    return;
+  }
+  const int nd = c.nd, n2 = 2 * nd;
+  // gu(0): CA flip; gu(i), i = 1..2Nd: flavour (b-1)+Nd*(s-1)+1 -> gu(i)
+  std::vector<int> gu(n2 + 1, 0);
+  int type;
+  double rand = c.rng.grnd();
+  if (rand < 0.3) {
+    type = GLOB_SPINFLIP;
+    for (int i = 1; i <= nd; ++i) gu[i] = i + nd;
+    for (int i = nd + 1; i <= n2; ++i) gu[i] = i - nd;
+  } else if (rand < 0.6) {
+    type = GLOB_CAFLIP;
+    gu[0] = 1;
+    for (int i = 1; i <= n2; ++i) gu[i] = i;
+  } else {
+    type = GLOB_RANDPERM;  // rand_perm (Trace.F90:1083-1099) + randint(0,1)
+    for (int i = 1; i <= n2; ++i) gu[i] = i;
+    for (int j = 1; j <= n2; ++j) {
+      int i = c.rng.randint(j, n2);
+      std::swap(gu[j], gu[i]);
+    }
+    gu[0] = c.rng.randint(0, 1);
+  }
+  r.orb = type;
+  r.spin = gu[0];
+  std::vector<Op> nops = c.ops;
+  for (Op& o : nops) {
+    int i = o.b + nd * o.s + 1;
+    o.b = (gu[i] - 1) % nd;
+    o.s = (gu[i] - 1) / nd;
+    if (gu[0] != 0) o.ca = 1 - o.ca;
+  }
+  double sst_factor;
+  int new_outer;
+  if (type == GLOB_SPINFLIP && c.m->has_szt) {
+    int old_state = c.m->states[c.outer_sst][0];
+    int down = old_state & ((1 << nd) - 1), up = (old_state >> nd) & ((1 << nd) - 1);
+    new_outer = c.m->sst_of_state[up | (down << nd)];
+    sst_factor = walk(c, nops, new_outer, 0, (int)nops.size()) == new_outer ? 1.0 : 0.0;
+  } else {
+    std::vector<int> so, sn;
+    int n_old = fixed_ssts(c, c.ops, so);
+    int n_new = fixed_ssts(c, nops, sn);
+    new_outer = c.outer_sst;
+    if (n_new <= 0) {
+      sst_factor = 0.0;
+    } else {
+      sst_factor = double(n_new) / n_old;
+      int k = c.rng.randint(1, n_new);
+      for (int i = 0; i < c.m->nss; ++i)
+        if (sn[i] != -1 && --k <= 0) {
+          new_outer = sn[i];
+          break;
+        }
+    }
+  }
+  r.fpos_c = new_outer;
+  r.tau_c = sst_factor;
+  if (sst_factor == 0.0) {
+    c.accqn_glob++;
+    r.outcome = OUT_QN;
+    record(c, r);
+    return;
+  }
+  // new inverse matrices and determinant; determinant of the current
+  // inverse matrices by LU (get_FullLogDet)
+  std::vector<std::vector<double>> tc, ta, minv_old = c.minv, tc_old = c.tau_c, ta_old = c.tau_a;
+  flavour_lists(c, nops, tc, ta);
+  c.tau_c = tc;
+  c.tau_a = ta;
+  LogVal det_new = rebuild_minv(c);
+  std::vector<std::vector<double>> minv_new = c.minv;
+  LogVal det_minv_old{0.0, 1.0};
+  for (int f = 0; f < c.nf; ++f) {
+    int k = (int)tc_old[f].size();
+    if (k == 0) continue;
+    std::vector<double> A = minv_old[f];
+    bool sing;
+    det_minv_old = lmul(lu_logdet_inverse(A, k, sing), det_minv_old);
+  }
+  LogVal detrat = lmul(det_new, det_minv_old);
+  // full trace of the new configuration
+  std::vector<Op> ops_old = c.ops;
+  int outer_old = c.outer_sst;
+  c.ops = nops;
+  c.outer_sst = new_outer;
+  std::vector<LogVal> part;
+  LogVal trnew = full_trace(c, &part);
+  LogVal trrat = ldiv(trnew, c.trace);
+  double prob = std::fabs(std::exp(trrat.log + detrat.log) * sst_factor);
+  double rnd = c.rng.grnd();
+  r.det_log = detrat.log;
+  r.det_sign = detrat.sign;
+  r.tr_log = trnew.log;
+  r.tr_sign = trnew.sign;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    c.det = det_new;
+    c.trace = trnew;
+    c.parttrace = part;
+    c.minv = minv_new;
+    c.cfgsign = -config_sign(c);
+    c.acc_glob++;
+    r.outcome = OUT_ACCEPT;
+  } else {
+    c.ops = ops_old;
+    c.outer_sst = outer_old;
+    c.tau_c = tc_old;
+    c.tau_a = ta_old;
+    c.minv = minv_old;
+    reset_caches(c);
+    r.outcome = OUT_REJECT;
+  }
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  record(c, r);
+}
+
+// StepChangeOuter, CTQMC.F90:4570-4638 (no state sampling): new outer
+// superstate in proportion to the empty trace; always accepted.
+static void step_change_outer(Chain& c) {
+  Record r{};
+  r.move = MOVE_OUTER;
+  for (;;) {
+    std::vector<double> etv(c.m->nss);
+    double sum = 0.0;
+    for (int s = 0; s < c.m->nss; ++s) {
+      c.outer_sst = s;
+      LogVal t = full_trace(c, nullptr);
+      etv[s] = t.sign * std::exp(t.log);
+    }
+    for (int s = 0; s < c.m->nss; ++s) sum += etv[s];
+    for (int s = 0; s < c.m->nss; ++s) etv[s] = etv[s] / sum;
+    double rnd = c.rng.grnd();
+    double acc = 0.0;
+    for (int s = 0; s < c.m->nss; ++s) {
+      c.outer_sst = s;
+      acc += etv[s];
+      if (acc >= rnd && etv[s] != 0.0) break;
+    }
+    r.rand = rnd;
+    c.trace = full_trace(c, &c.parttrace);
+    if (!(c.trace.log < -HUGE_D)) break;
+  }
+  c.cfgsign = -config_sign(c);
+  r.outcome = OUT_ACCEPT;
+  r.tr_log = c.trace.log;
+  r.tr_sign = c.trace.sign;
+  r.outer_sst = c.outer_sst;
+  record(c, r);
+}
+
+// StepShiftTau_proper, CTQMC.F90:4641-4835, with
+// update_InvFullHybrShiftTau_diag (Trace.F90:2355-2452): all times shifted
+// by -DeltaTau cyclically, the outer superstate becomes the one entering
+// the new first operator, the window keeps its place relative to the
+// operators, M rows/columns of wrapped operators rotate to the end with a
+// sign change.
+static void step_shift(Chain& c) {
+  if (c.ops.empty()) {
+    step_change_outer(c);
+    return;
+  }
+  Record r{};
+  r.move = MOVE_SHIFT;
+  double dtau = c.rng.grnd() * c.p.beta;
+  r.tau_c = dtau;
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  if (dtau == 0.0 || dtau == c.p.beta) {
+    r.outcome = OUT_NOPAIRS;
+    record(c, r);
+    return;
+  }
+  c.try_shift++;
+  const int K = (int)c.ops.size();
+  std::vector<int> wr_c(c.nf, 0), wr_a(c.nf, 0);
+  int first = K;  // index of the first operator with tau >= dtau
+  for (int i = K - 1; i >= 0; --i)
+    if (c.ops[i].tau >= dtau) first = i;
+  for (int i = 0; i < first; ++i) (c.ops[i].ca == 0 ? wr_c : wr_a)[c.fi(c.ops[i].b, c.ops[i].s)]++;
+  auto shifted = [&](double t) {  // modulo(tau - DeltaTau, beta)
+    double x = t - dtau;
+    return x - std::floor(x / c.p.beta) * c.p.beta;
+  };
+  std::vector<Op> nops;
+  for (int i = first; i < K; ++i) nops.push_back(c.ops[i]);
+  for (int i = 0; i < first; ++i) nops.push_back(c.ops[i]);
+  for (Op& o : nops) o.tau = shifted(o.tau);
+  // outer superstate: the one entering the new first operator
+  int new_outer = first < K ? walk(c, c.ops, c.outer_sst, 0, first) : c.outer_sst;
+  double factor = 1.0;
+  std::vector<Op> ops_old = c.ops;
+  int outer_old = c.outer_sst, wp_old = c.window_position, np_old = c.npairs;
+  double wmin_old = c.tauwin_min, wmax_old = c.tauwin_max;
+  c.ops = nops;
+  c.outer_sst = new_outer;
+  int nw = c.num_windows;
+  int d = (int)std::floor((dtau / c.p.beta) * double(nw + 1));
+  c.window_position = ((wp_old - (((d % nw) + nw) % nw)) % nw + nw) % nw;
+  c.npairs = -1;
+  set_window_bounds(c);
+  std::vector<LogVal> part;
+  LogVal trnew = full_trace(c, &part);
+  LogVal trrat = ldiv(trnew, c.trace);
+  double prob = std::fabs(factor * (trrat.sign * std::exp(trrat.log)));
+  double rnd = c.rng.grnd();
+  r.fpos_c = new_outer;
+  r.tr_log = trnew.log;
+  r.tr_sign = trnew.sign;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    c.trace = trnew;
+    c.parttrace = part;
+    double detrat = 1.0;
+    for (int f = 0; f < c.nf; ++f) {
+      int k = (int)c.tau_c[f].size();
+      int w1 = wr_c[f], w2 = wr_a[f];
+      std::vector<double> nc, na;
+      for (int i = w1; i < k; ++i) nc.push_back(shifted(c.tau_c[f][i]));
+      for (int i = 0; i < w1; ++i) nc.push_back(shifted(c.tau_c[f][i]));
+      for (int i = w2; i < k; ++i) na.push_back(shifted(c.tau_a[f][i]));
+      for (int i = 0; i < w2; ++i) na.push_back(shifted(c.tau_a[f][i]));
+      c.tau_c[f] = nc;
+      c.tau_a[f] = na;
+      if (!((w1 == 0 && w2 == 0) || (w1 == k && w2 == k))) {
+        const std::vector<double>& M = c.minv[f];
+        std::vector<double> N((size_t)k * k);
+        auto at = [&](int i, int j) { return M[(size_t)j * k + i]; };
+        for (int j = 0; j < k; ++j)
+          for (int i = 0; i < k; ++i) {
+            // new (i, j) <- old row i+w1 (mod k), column j+w2 (mod k), negated
+            // when exactly one of the two wrapped
+            int oi = (i + w1) % k, oj = (j + w2) % k;
+            bool ri = i >= k - w1, cj = j >= k - w2;
+            double v = at(oi, oj);
+            N[(size_t)j * k + i] = (ri != cj) ? -v : v;
+          }
+        c.minv[f] = N;
+      }
+      if ((k % 2) != 0 && ((w1 + w2) % 2) != 0) detrat = -detrat;
+    }
+    c.det.sign = c.det.sign * detrat;
+    c.cfgsign = -config_sign(c);
+    c.acc_shift++;
+    r.outcome = OUT_ACCEPT;
+  } else {
+    c.ops = ops_old;
+    c.outer_sst = outer_old;
+    c.window_position = wp_old;
+    c.tauwin_min = wmin_old;
+    c.tauwin_max = wmax_old;
+    c.npairs = np_old;
+    reset_caches(c);
+    r.outcome = OUT_REJECT;
+  }
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  record(c, r);
+}
+
 // one proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250)
 static int one_step(Chain& c) {
   double rand_num = c.rng.grnd();
@@ -1298,8 +1604,10 @@ static int one_step(Chain& c) {
     } else {
       return -2;
     }
+  } else if (rand_num <= 1.0 - c.p.p_shift) {
+    step_glob(c);
   } else {
-    return -3;  // global / tau-shift moves are outside this restatement
+    step_shift(c);
   }
   if ((c.try_add + c.try_rem) % c.nslide == 0) shift_window(c);
   return 0;
@@ -1307,6 +1615,7 @@ static int one_step(Chain& c) {
 
 static void init_counters(Chain& c) {
   c.try_add = c.try_rem = c.acc_add = c.acc_rem = c.accqn_add = c.accqn_rem = 0;
+  c.try_glob = c.acc_glob = c.accqn_glob = c.try_shift = c.acc_shift = 0;
 }
 
 // MeasGtauRem(.false.), CTQMC.F90:2252-2440 (tau bins only)
@@ -1545,6 +1854,11 @@ void orc_chain_counters(void* cc, long long* out) {
   out[4] = c.accqn_add;
   out[5] = c.accqn_rem;
   out[6] = c.cnt_meas;
+  out[7] = c.try_glob;
+  out[8] = c.acc_glob;
+  out[9] = c.accqn_glob;
+  out[10] = c.try_shift;
+  out[11] = c.acc_shift;
 }
 
 // state: trace(log,sign), det(log,sign), cfgsign, npairs, outer_sst,

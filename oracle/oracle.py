@@ -142,7 +142,7 @@ class Chain:
     """One Markov chain of the restated reference loop."""
 
     def __init__(self, model, beta, ftau, ntau, seed, taudiff_max=-1.0, ncorr=100,
-                 p_outer=0.0, maxhisto=500, meas_dm=1):
+                 p_outer=0.0, maxhisto=500, meas_dm=1, p_global=0.0, p_shift=0.0):
         L = lib()
         self.model = model
         nd = model.nd
@@ -153,7 +153,7 @@ class Chain:
         self.ntau = ntau
         self.maxhisto = maxhisto
         p = Params(beta=beta, nftau=self.nftau, ntau=ntau, ncorr=ncorr, seed=seed,
-                   taudiff_max=taudiff_max, p_global=0.0, p_shift=0.0, p_4op=0.0,
+                   taudiff_max=taudiff_max, p_global=p_global, p_shift=p_shift, p_4op=0.0,
                    p_outer=p_outer, maxhisto=maxhisto, meas_dm=meas_dm)
         self.params = p
         self.h = L.orc_chain_create(model.h, C.byref(p), _dp(self._ftau.ravel(order="F")))
@@ -193,10 +193,11 @@ class Chain:
                     histo=hi.reshape(nf, self.maxhisto))
 
     def counters(self):
-        out = (C.c_longlong * 7)()
+        out = (C.c_longlong * 12)()
         lib().orc_chain_counters(self.h, out)
         return dict(zip(("try_add", "acc_add", "try_rem", "acc_rem", "qn_add", "qn_rem",
-                         "cnt_meas"), list(out)))
+                         "cnt_meas", "try_glob", "acc_glob", "qn_glob", "try_shift",
+                         "acc_shift"), list(out)))
 
     def state(self):
         out = np.zeros(14)

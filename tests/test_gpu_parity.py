@@ -26,17 +26,20 @@ def lib():
     return E.load(build_if_missing=True)
 
 
-def run_pair(name, beta, tdm, p_outer, nprop, seed, dense=False, qns=None, ntau=50):
+def run_pair(name, beta, tdm, p_outer, nprop, seed, dense=False, qns=None, ntau=50, p_global=0.0,
+             p_shift=0.0):
     pr = P.config_problem(name, beta=beta)
     q = qns or pr["quantum_numbers"]
     mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
-    co = O.Chain(mo, beta, pr["ftau"], ntau, seed=seed, taudiff_max=tdm, p_outer=p_outer)
+    co = O.Chain(mo, beta, pr["ftau"], ntau, seed=seed, taudiff_max=tdm, p_outer=p_outer,
+                 p_global=p_global, p_shift=p_shift)
     co.start_log(nprop)
     co.warmup(nprop)
     ref = co.log()
     mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
     grp = E.Group(beta, pr["ftau"], ntau, nchains=1, seed0=seed, taudiff_max=tdm,
-                  p_outer=p_outer, dense=dense, kcap=64, opcap=512)
+                  p_outer=p_outer, dense=dense, kcap=64, opcap=512, p_global=p_global,
+                  p_shift=p_shift)
     b = E.Batch(mg, [grp])
     b.set_log(nprop)
     b.warmup(nprop)
@@ -93,6 +96,44 @@ CASES = [
     ("dd3", 8.0, 8.0, 0.0, 3000, 5, False, "Nt"),
     ("kanamori5", 2.0, 2.0, 0.0, 300, 4, False, None),
 ]
+
+
+GLOBAL_CASES = [
+    ("anderson1", 10.0, 3.0, 0.1, 20000, 12, False, None),
+    ("dd3", 10.0, 4.0, 0.1, 8000, 13, False, None),
+    ("dd3", 25.0, 5.0, 0.0, 6000, 14, False, None),
+    ("dd3", 10.0, 4.0, 0.1, 2000, 15, True, None),
+    ("dd3", 8.0, 8.0, 0.0, 3000, 16, False, "Nt"),
+]
+
+
+@pytest.mark.parametrize("name,beta,tdm,pout,nprop,seed,dense,qns", GLOBAL_CASES)
+def test_global_and_shift_move_parity(lib, name, beta, tdm, pout, nprop, seed, dense, qns):
+    """Global moves (StepGlob) and tau-shift moves (StepShiftTau) at 5 %
+    each, proposal by proposal; the final state and inverse matrices."""
+    ref, got, co, b = run_pair(name, beta, tdm, pout, nprop, seed, dense=dense, qns=qns,
+                               p_global=0.05, p_shift=0.05)
+    F = P.config_problem(name, beta=beta)["ftau"][0, 0]
+    compare_logs(ref, got, F, beta)
+    for mv in (2, 3):
+        assert np.sum((ref["move"] == mv) & (ref["outcome"] == 4)) > 0, mv
+    mc = b.move_counters(0)
+    oc = co.counters()
+    for key in ("try_glob", "acc_glob", "qn_glob", "try_shift", "acc_shift"):
+        assert mc[key] == oc[key], key
+    so, sg = co.state(), b.state(0)
+    assert so["noper"] == sg["noper"] and so["outer_sst"] == sg["outer_sst"]
+    assert so["cfgsign"] == sg["cfgsign"] and so["det_sign"] == sg["det_sign"]
+    assert abs(so["det_log"] - sg["det_log"]) < 1e-8
+    assert so["window_position"] == sg["window_position"]
+    t_o, *_ = co.get_config()
+    t_g, *_ = b.get_config(0)
+    assert np.array_equal(t_o, t_g)
+    for f in range(2 * co.model.nd):
+        mo_, mg_ = co.minv(f), b.minv(0, f)
+        assert mo_.shape == mg_.shape
+        if mo_.size:
+            assert np.allclose(mg_, mo_, rtol=1e-9, atol=1e-9 * np.abs(mo_).max())
 
 
 @pytest.mark.parametrize("name,beta,tdm,pout,nprop,seed,dense,qns", CASES)
@@ -168,7 +209,8 @@ def test_batched_chains_match_oracle_per_seed(lib):
 @pytest.mark.parametrize("warps", [-1, 7, 32])
 def test_phase_synchronous_schedule_matches_oracle(lib, warps):
     """The phase-synchronous schedule (blocks of `warps` chains, a partial
-    last block) runs every chain as the reference chain of its own seed, and
+    last block; global and tau-shift moves at 2 % each) runs every chain as
+    the reference chain of its own seed, and
     its measurements equal the independent-warp schedule's: histogram and
     sign exactly, G(tau) and the density matrix to 1e-12 relative (G(tau)
     bins are summed with atomics, whose order is not fixed)."""
@@ -178,7 +220,7 @@ def test_phase_synchronous_schedule_matches_oracle(lib, warps):
     runs = []
     for sched in (0, warps):
         b = E.Batch(mg, [E.Group(10.0, pr["ftau"], 20, nchains=n, seed0=300, taudiff_max=5.0,
-                                 kcap=64, opcap=512, ncorr=50)])
+                                 kcap=64, opcap=512, ncorr=50, p_global=0.02, p_shift=0.02)])
         b.set_schedule(sched)
         b.warmup(2000)
         b.measure(20)
@@ -186,7 +228,8 @@ def test_phase_synchronous_schedule_matches_oracle(lib, warps):
         runs.append(b)
     mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
     for c in (0, 6, 7, 44):
-        co = O.Chain(mo, 10.0, pr["ftau"], 20, seed=300 + c, taudiff_max=5.0, ncorr=50)
+        co = O.Chain(mo, 10.0, pr["ftau"], 20, seed=300 + c, taudiff_max=5.0, ncorr=50,
+                     p_global=0.02, p_shift=0.02)
         co.warmup(2000)
         co.measure(20)
         t_o, *_ = co.get_config()

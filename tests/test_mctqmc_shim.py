@@ -17,7 +17,7 @@ def pstring(d):
 
 BASE = {"beta": 10.0, "Nd": 3, "Ntau": 40, "NCorr": 50, "Nmeas": 60, "Nwarmups": 2000,
         "MaxHisto": 60, "TaudiffMax": 5.0, "QuantumNumbers": "Nt Szt",
-        "PercentageGlobalMove": 0.0, "PercentageTauShiftMove": 0.0,
+        "PercentageGlobalMove": 0.005, "PercentageTauShiftMove": 0.005,
         "Percentage4OperatorMove": 0.0, "PercentageOuterMove": 0.1,
         "PercentageWormInsert": 0.0, "segment": 0, "offdiag": 0, "statesampling": 0,
         "MeasDensityMatrix": 1, "Eigenbasis": 1, "NLegMax": 10}
@@ -39,9 +39,8 @@ def test_parameter_string_rules():
     ctqmc.dest_paras()
 
 
-@pytest.mark.parametrize("key,val", [("PercentageGlobalMove", 0.005),
-                                     ("PercentageTauShiftMove", 0.005),
-                                     ("Percentage4OperatorMove", 0.1), ("segment", 1),
+@pytest.mark.parametrize("key,val", [("Percentage4OperatorMove", 0.1), ("segment", 1),
+                                     ("NSymMove", 1), ("PercentageWormInsert", 0.1),
                                      ("offdiag", 1), ("statesampling", 1)])
 def test_unsupported_modes_are_rejected(key, val):
     ctqmc.init_paras(pstring(dict(BASE, **{key: val})))
@@ -59,8 +58,9 @@ def test_supported_configuration_passes_the_check():
 @pytest.mark.gpu
 def test_solve_through_the_module_matches_the_oracle():
     """init_rnd/init_paras/init_solver/set_taudiffmax/ctqmc_warmup/
-    ctqmc_measure as cthyb_solver.py calls them; the results equal the
-    oracle chain of the same seed (identical proposal streams)."""
+    ctqmc_measure as cthyb_solver.py calls them, with the default global and
+    tau-shift move percentages; the results equal the oracle chain of the
+    same seed (identical proposal streams)."""
     pr = P.config_problem("dd3", beta=10.0)
     nd, ntau = 3, BASE["Ntau"]
     ftau = pr["ftau"]
@@ -77,7 +77,7 @@ def test_solve_through_the_module_matches_the_oracle():
     ctqmc.ctqmc_measure(1, 1)
     mo = O.Model(nd, pr["umatrix"], pr["muimp"], "Nt Szt")
     co = O.Chain(mo, 10.0, ftau, ntau, seed=11, taudiff_max=5.0, ncorr=BASE["NCorr"],
-                 p_outer=0.1, maxhisto=BASE["MaxHisto"] + 1)
+                 p_outer=0.1, maxhisto=BASE["MaxHisto"] + 1, p_global=0.005, p_shift=0.005)
     co.set_taudiffmax(5.0)
     co.warmup(BASE["Nwarmups"])
     co.measure(BASE["Nmeas"])

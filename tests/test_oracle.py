@@ -131,6 +131,66 @@ def test_fast_updates_match_full_recompute(name, beta, tdm, pout):
             assert np.allclose(c.minv(2 * b + s), np.linalg.inv(H), rtol=1e-9, atol=1e-9)
 
 
+@pytest.mark.parametrize("name,beta,tdm", [("anderson1", 10.0, 3.0), ("dd3", 8.0, 2.5),
+                                            ("dd3", 8.0, 8.0)])
+def test_global_and_shift_moves_keep_state_consistent(name, beta, tdm):
+    """Global moves (spin flip, CA flip, random permutation) and tau-shift
+    moves at 10 % each: trace, determinant and inverse matrices stay equal to
+    a full recompute after every step, and both move kinds are accepted."""
+    pr = P.config_problem(name, beta=beta)
+    m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    c = O.Chain(m, pr["beta"], pr["ftau"], 50, seed=23, taudiff_max=tdm, p_outer=0.1,
+                p_global=0.1, p_shift=0.1)
+    acc = {"acc_glob": 0, "acc_shift": 0}
+    for i in range(1500):
+        c.warmup(1)  # counters restart with every call
+        for k in acc:
+            acc[k] += c.counters()[k]
+        st = c.state()
+        fd, ft = c.full_det(), c.full_trace()
+        assert abs(fd[0] - st["det_log"]) < 1e-9 and fd[1] == st["det_sign"], i
+        assert abs(ft[0] - st["trace_log"]) < 1e-9 and ft[1] == st["trace_sign"], i
+    assert acc["acc_glob"] > 0 and acc["acc_shift"] > 0, acc
+    taus, orbs, spins, cas = c.get_config()
+    assert np.all(np.diff(taus) > 0) and taus.min() >= 0 and taus.max() < beta
+    F = pr["ftau"][0, 0]
+    for b in range(pr["nd"]):
+        for s in range(2):
+            sel = (orbs - 1 == b) & (spins - 1 == s)
+            tc = np.sort(taus[sel & (cas == 1)])
+            ta = np.sort(taus[sel & (cas == 2)])
+            if len(tc) == 0:
+                continue
+            H = np.array([[_hyb(F, beta, a - cc) for cc in tc] for a in ta])
+            assert np.allclose(c.minv(2 * b + s), np.linalg.inv(H), rtol=1e-9, atol=1e-9)
+
+
+def test_u0_green_function_with_global_and_shift_moves():
+    """The U=0 known answer of the bath G(tau) holds with global and
+    tau-shift moves switched on (detailed balance of the added moves)."""
+    beta = 5.0
+    um = P.flat_umatrix(P.umatrix_density(1, 0.0, 0.0, 0.0))
+    ft = P.semicircle_ftau(1, beta, 1.0, 500)
+    g = P.semicircle_gtau(beta, 1.0, 500)
+    m = O.Model(1, um, P.muimp_solver(1, 0.0), "Nt Szt Azt")
+    res = []
+    for seed in range(16):
+        c = O.Chain(m, beta, ft, 20, seed=100 + seed, taudiff_max=beta, p_global=0.1,
+                    p_shift=0.1)
+        c.warmup(5000)
+        c.measure(4000)
+        res.append(c.results()["gtau"])
+    G = np.mean(res, axis=0)
+    E = np.std(res, axis=0, ddof=1) / np.sqrt(len(res))
+    tt = np.linspace(0, beta, 500)
+    edges = np.linspace(0, beta, 21)
+    gex = np.array([np.mean(np.interp(np.linspace(a, b, 400), tt, g))
+                    for a, b in zip(edges[:-1], edges[1:])])
+    z = (G - gex) / E
+    assert np.abs(z).max() < 4.5
+    assert abs(z.mean()) < 1.0
+
+
 def test_operator_list_stress_invariants():
     """3-operator-list-stress-test.F90 invariants with a fixed seed: time
     order, per-flavour consistency, NPairs equal to a recount, window edges

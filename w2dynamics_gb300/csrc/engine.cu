@@ -1083,8 +1083,8 @@ __device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum)
 // early (equal times, no pairs, QN violation, rejection) idles in the later
 // phases.  The per-warp proposal state lives in shared memory.
 struct Prop {
-  int move, alive, co, f, k, K, fpos_c, fpos_a, p1, p2, snew, np, ix, iy, cax, rank_c, rank_a, slot_c, slot_a,
-      accept;
+  int move, alive, rare, co, f, k, K, fpos_c, fpos_a, p1, p2, snew, np, ix, iy, cax, rank_c, rank_a, slot_c,
+      slot_a, accept;
   double tau_c, tau_a, tdf, hprf, ratio, det_sign, det_log, tr_log, tr_sign, tr_mx, tr_sum, tx, ty;
   Mod md;
 };
@@ -1099,6 +1099,7 @@ __device__ __forceinline__ void prop_end(Ctx& c, Prop& p, int outcome) {
 __device__ NOINL void ph_draw(Ctx& c, Prop& p) {
   Hdr& h = *c.h;
   p.alive = 0;
+  p.rare = 0;
   p.accept = 0;
   for (int f = 0; f < c.m->nf; ++f)
     if (h.k[f] + 1 > c.kcap) {
@@ -1109,20 +1110,33 @@ __device__ NOINL void ph_draw(Ctx& c, Prop& p) {
     set_status(c, ST_CAPACITY);
     return;
   }
-  double rn = grnd(c);
-  grnd(c);  // Percentage4OperatorMove draw
-  bool co = grnd(c) < c.g->p_outer;
+  // move thresholds of the Z-space loop (PercentageWormInsert = 0)
+  const double rn = grnd(c);
+  const double pair = __dsub_rn(__dsub_rn(1.0, c.g->p_shift), c.g->p_global);
+  int move;
+  if (rn < __ddiv_rn(pair, 2.0)) move = 0;
+  else if (rn <= pair) move = 1;
+  else if (rn <= __dsub_rn(1.0, c.g->p_shift)) move = 2;
+  else move = 3;
   cthyb_record& r = *c.rec;
   for (int i = c.lane; i < (int)(sizeof(cthyb_record) / 4); i += 32) ((int*)&r)[i] = 0;
   __syncwarp();
-  p.move = rn < 0.5 ? 0 : 1;
-  p.co = co;
-  r.move = p.move;
-  r.change_outer = co;
+  p.move = move;
+  r.move = move;
   r.outer_sst = h.outer_sst;
   r.k_total = h.K;
+  if (move >= 2) {  // global or tau-shift move
+    p.rare = 1;
+    __syncwarp();
+    return;
+  }
+  p.rare = 0;
+  grnd(c);  // Percentage4OperatorMove draw
+  bool co = grnd(c) < c.g->p_outer;
+  p.co = co;
+  r.change_outer = co;
   if (c.lane == 0) {
-    if (p.move == 0) h.try_add++;
+    if (move == 0) h.try_add++;
     else h.try_rem++;
   }
   p.alive = 1;
@@ -1613,7 +1627,585 @@ __device__ NOINL void ph_finish(Ctx& c, Prop& p) {
   write_record(c, r);
   if (c.lane == 0) h.nprop++;
   __syncwarp();
-  if (h.nprop % h.nslide == 0) shift_window(c);
+  // after every move, whatever its kind (CTQMC.F90:8531-8533)
+  if ((h.try_add + h.try_rem) % h.nslide == 0) shift_window(c);
+}
+
+// ---------------------------------------------------------------------------
+// Global and tau-shift moves.  Rare (PercentageGlobalMove and
+// PercentageTauShiftMove default to 0.5 % each); each rebuilds the whole
+// tree into the inactive node slots, so a rejection leaves the active tree
+// untouched and an acceptance flips every node.  Work space per chain
+// (o_glob): the new inverse matrices, the new sorted time lists, a copy of
+// the operator arrays.
+__device__ __forceinline__ double* glob_minv(const Ctx& c) {
+  return (double*)(c.g->base + (size_t)c.chain * c.g->stride + c.g->o_glob);
+}
+__device__ __forceinline__ double* glob_srt(const Ctx& c) {
+  return glob_minv(c) + (size_t)c.m->nf * c.kcap * c.kcap;
+}
+__device__ __forceinline__ double* glob_optau(const Ctx& c) { return glob_srt(c) + (size_t)c.m->nf * 2 * c.kcap; }
+__device__ __forceinline__ int* glob_opcode(const Ctx& c) { return (int*)(glob_optau(c) + c.g->opcap + 2); }
+
+__device__ NOINL void tree_build_inactive(Ctx& c, bool do_ss, bool do_states) {
+  const int L = c.g->L, nb = 1 << L;
+  Mod md;
+  md.type = 0;
+  for (int b = 0; b < nb; ++b) {
+    const int n = gather_bin(c, md, b, 0);
+    leaf_body(c, b, n, 1 - c.act[nb + b], do_ss, do_states, 0);
+  }
+  for (int n = nb - 1; n >= 1; --n)
+    combine_body(c, n, 1 - c.act[2 * n], 1 - c.act[2 * n + 1], 1 - c.act[n], do_ss, do_states);
+  if (c.lane == 0) c.h->w_nodes += 2 * nb;
+}
+__device__ __forceinline__ void tree_flip_all(Ctx& c) {
+  for (int i = c.lane; i < (2 << c.g->L); i += 32) c.act[i] ^= 1;
+  __syncwarp();
+}
+
+// Gauss-Jordan inverse with partial pivoting (first maximal pivot) of
+// H(a_rank, c_rank) = Delta(tau_a - tau_c) for the sorted time lists sc/sa
+// of flavour f (get_InvFullHybr, Trace.F90:2279-2336); log|det| and sign are
+// accumulated into dlog/dsign (get_MatLogDetFull, MatrixUpdate.F90:41-99).
+// On return work + kcap^2 holds the inverse, element (c_rank, a_rank) at
+// [a_rank * kcap + c_rank].  Returns false for a singular matrix.
+__device__ NOINL bool gj_inverse(Ctx& c, int f, int k, const double* sc, const double* sa, double* work,
+                                 double& dlog, double& dsign) {
+  const int ld = c.kcap;
+  double* H = work;
+  double* I = work + (size_t)ld * ld;
+  for (int e = c.lane; e < k * k; e += 32) {
+    int ia = e % k, ic = e / k;
+    H[(size_t)ic * ld + ia] = hybrf(c, __dsub_rn(sa[ia], sc[ic]), f);
+    I[(size_t)ic * ld + ia] = (ia == ic) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  for (int j = 0; j < k; ++j) {
+    double best = -1.0;
+    int bi = j;
+    for (int i = j + c.lane; i < k; i += 32) {
+      double a = fabs(H[(size_t)j * ld + i]);
+      if (a > best) {
+        best = a;
+        bi = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      double ob = __shfl_xor_sync(FULL, best, o);
+      int oi = __shfl_xor_sync(FULL, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (best <= 0.0) return false;
+    if (bi != j) {
+      for (int col = c.lane; col < k; col += 32) {
+        double t = H[(size_t)col * ld + j];
+        H[(size_t)col * ld + j] = H[(size_t)col * ld + bi];
+        H[(size_t)col * ld + bi] = t;
+        t = I[(size_t)col * ld + j];
+        I[(size_t)col * ld + j] = I[(size_t)col * ld + bi];
+        I[(size_t)col * ld + bi] = t;
+      }
+      dsign = -dsign;
+    }
+    __syncwarp();
+    double piv = H[(size_t)j * ld + j];
+    dlog += log(fabs(piv));
+    if (piv < 0) dsign = -dsign;
+    double ip = 1.0 / piv;
+    for (int col = c.lane; col < k; col += 32) {
+      H[(size_t)col * ld + j] *= ip;
+      I[(size_t)col * ld + j] *= ip;
+    }
+    __syncwarp();
+    for (int col = 0; col < k; ++col) {
+      double hj = H[(size_t)col * ld + j];
+      double ij = I[(size_t)col * ld + j];
+      for (int i = c.lane; i < k; i += 32) {
+        if (i == j) continue;
+        double fct = H[(size_t)j * ld + i];
+        if (col == j) continue;
+        H[(size_t)col * ld + i] -= fct * hj;
+        I[(size_t)col * ld + i] -= fct * ij;
+      }
+    }
+    __syncwarp();
+    for (int i = c.lane; i < k; i += 32)
+      if (i != j) {
+        I[(size_t)j * ld + i] -= H[(size_t)j * ld + i] * I[(size_t)j * ld + j];
+        H[(size_t)j * ld + i] = 0.0;
+      }
+    __syncwarp();
+  }
+  return true;
+}
+
+// log|det| and sign of the current inverse matrix of flavour f in rank order
+// by LU with partial pivoting (first maximal pivot), accumulated into
+// dlog/dsign (get_FullLogDet, Trace.F90:2665-2685, via get_LogDetFull).
+__device__ NOINL void lu_logdet_minv(Ctx& c, int f, double* work, double& dlog, double& dsign) {
+  const int k = c.h->k[f], ld = c.kcap;
+  if (k == 0) return;
+  const short* slc = sslot_ptr(c, f, 0);
+  const short* sla = sslot_ptr(c, f, 1);
+  const double* Mf = M_ptr(c, f);
+  double* A = work;  // A(rc, ra) at [ra * ld + rc]
+  for (int e = c.lane; e < k * k; e += 32) {
+    const int rc = e % k, ra = e / k;
+    A[(size_t)ra * ld + rc] = Mf[(size_t)sla[ra] * ld + slc[rc]];
+  }
+  __syncwarp();
+  for (int j = 0; j < k; ++j) {
+    double best = -1.0;
+    int bi = j;
+    for (int i = j + c.lane; i < k; i += 32) {
+      const double a = fabs(A[(size_t)j * ld + i]);
+      if (a > best) {
+        best = a;
+        bi = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const double ob = __shfl_xor_sync(FULL, best, o);
+      const int oi = __shfl_xor_sync(FULL, bi, o);
+      if (ob > best || (ob == best && oi < bi)) {
+        best = ob;
+        bi = oi;
+      }
+    }
+    if (best <= 0.0) {
+      dlog = -DHUGE;
+      dsign = 0.0;
+      return;
+    }
+    if (bi != j) {
+      for (int col = c.lane; col < k; col += 32) {
+        const double t = A[(size_t)col * ld + j];
+        A[(size_t)col * ld + j] = A[(size_t)col * ld + bi];
+        A[(size_t)col * ld + bi] = t;
+      }
+      dsign = -dsign;
+    }
+    __syncwarp();
+    const double piv = A[(size_t)j * ld + j];
+    dlog += log(fabs(piv));
+    if (piv < 0) dsign = -dsign;
+    for (int i = j + 1 + c.lane; i < k; i += 32) A[(size_t)j * ld + i] /= piv;
+    __syncwarp();
+    for (int col = j + 1; col < k; ++col) {
+      const double ajc = A[(size_t)col * ld + j];
+      for (int i = j + 1 + c.lane; i < k; i += 32) A[(size_t)col * ld + i] -= A[(size_t)j * ld + i] * ajc;
+    }
+    __syncwarp();
+  }
+}
+
+// Per-flavour sorted time lists of the current operator arrays into
+// dst[(2f + ca) * kcap + rank]; counts into k (lane-uniform).
+__device__ NOINL void sorted_lists(Ctx& c, double* dst, int* k) {
+  const int K = c.h->K;
+  for (int f = 0; f < c.m->nf; ++f)
+    for (int ca = 0; ca < 2; ++ca) {
+      double* st = dst + (size_t)(2 * f + ca) * c.kcap;
+      int n = 0;
+      for (int base = 0; base < K; base += 32) {
+        const int i = base + c.lane;
+        const bool is = i < K && c.opcode[i] == 2 * f + ca;
+        const unsigned bal = __ballot_sync(FULL, is);
+        const int pos = n + __popc(bal & ((1u << c.lane) - 1u));
+        if (is && pos < c.kcap) st[pos] = c.optau[i];
+        n += __popc(bal);
+      }
+      if (ca == 0) k[f] = n;
+    }
+  __syncwarp();
+}
+
+// Trace of the configuration in the operator arrays with outer superstate
+// s0, from the inactive tree slots (monomial models: state maps rebuilt
+// there first) or the dense product.
+__device__ NOINL void rebuilt_trace(Ctx& c, int s0, double& lg, double& sg) {
+  if (c.mono) {
+    tree_build_inactive(c, false, true);
+    double mx, sum;
+    root_trace(c, 1 - c.act[1], s0, mx, sum);
+    trace_log(mx, sum, lg, sg);
+  } else {
+    Mod md;
+    md.type = 0;
+    dense_trace(c, md, s0, lg, sg);
+  }
+}
+
+// StepGlob, CTQMC.F90:4433-4554, without user symmetry moves: spin flip
+// (30 %, gen_SpinFlipUpdate), creator/annihilator flip (30 %, gen_CAFlip),
+// random flavour permutation with random CA flip (gen_GlobalUpdate_new,
+// rand_perm) (Trace.F90:1083-1198); QN checks perform_spinflip_check_qn /
+// perform_global_check_qn (Trace.F90:1306-1394); full inverse and
+// determinant (get_InvFullHybr) times the LU determinant of the current
+// inverse matrices (get_FullLogDet); weight exp(dlog tr + log detrat) * sst
+// factor.
+__device__ NOINL void ph_global(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  cthyb_record& r = *c.rec;
+  if (c.lane == 0) h.try_glob++;
+  __syncwarp();
+  const int K = h.K, nd = m.nd, n2 = 2 * nd;
+  if (K == 0) {
+    r.outcome = 2;
+    __syncwarp();
+    return;
+  }
+  int gu[NFMAX + 1];
+  int type;
+  const double u = grnd(c);
+  if (u < 0.3) {
+    type = 3;  // spin flip
+    gu[0] = 0;
+    for (int i = 1; i <= n2; ++i) gu[i] = i <= nd ? i + nd : i - nd;
+  } else if (u < 0.6) {
+    type = 4;  // CA flip
+    gu[0] = 1;
+    for (int i = 1; i <= n2; ++i) gu[i] = i;
+  } else {
+    type = 1;  // random permutation (Green 1963) and random CA flip
+    for (int i = 1; i <= n2; ++i) gu[i] = i;
+    for (int j = 1; j <= n2; ++j) {
+      const int i = randint(c, j, n2);
+      const int t = gu[j];
+      gu[j] = gu[i];
+      gu[i] = t;
+    }
+    gu[0] = randint(c, 0, 1);
+  }
+  // flavour f = 2b + s -> reference index b + Nd*s + 1 -> gu -> new flavour
+  int fmap[NFMAX];
+  for (int f = 0; f < m.nf; ++f) {
+    const int g = gu[(f >> 1) + nd * (f & 1) + 1] - 1;
+    fmap[f] = 2 * (g % nd) + g / nd;
+  }
+  const int flip = gu[0] != 0;
+  int* opc_old = glob_opcode(c);
+  for (int i = c.lane; i < K; i += 32) {
+    const int code = c.opcode[i];
+    opc_old[i] = code;
+    c.opcode[i] = 2 * fmap[code >> 1] + (flip ? 1 - (code & 1) : (code & 1));
+  }
+  __syncwarp();
+  // QN check on the superstate maps of the rebuilt tree
+  tree_build_inactive(c, true, false);
+  const int16_t* ss_new = node_ss(c, 1, 1 - c.act[1]);
+  const int16_t* ss_old = node_ss(c, 1, c.act[1]);
+  int new_outer = h.outer_sst;
+  double factor;
+  if (type == 3 && m.has_szt) {
+    new_outer = m.sflip_sst[h.outer_sst];
+    factor = ss_new[new_outer] == new_outer ? 1.0 : 0.0;
+  } else {
+    int n_old = 0, n_new = 0;
+    for (int s = c.lane; s < m.nss; s += 32) {
+      n_old += ss_old[s] == s;
+      n_new += ss_new[s] == s;
+    }
+    n_old = wsumi(n_old);
+    n_new = wsumi(n_new);
+    if (n_old <= 0) {
+      set_status(c, ST_INTERNAL);  // "impossible old configuration"
+      return;
+    }
+    if (n_new <= 0) {
+      factor = 0.0;
+    } else {
+      factor = __ddiv_rn((double)n_new, (double)n_old);
+      int kk = randint(c, 1, n_new);
+      if (c.lane == 0)
+        for (int s = 0; s < m.nss; ++s)
+          if (ss_new[s] == s && --kk <= 0) {
+            new_outer = s;
+            break;
+          }
+      new_outer = __shfl_sync(FULL, new_outer, 0);
+    }
+  }
+  r.orb = type;
+  r.spin = gu[0];
+  r.fpos_c = new_outer;
+  r.tau_c = factor;
+  if (factor == 0.0) {
+    for (int i = c.lane; i < K; i += 32) c.opcode[i] = opc_old[i];
+    if (c.lane == 0) h.qn_glob++;
+    r.outcome = 1;
+    __syncwarp();
+    return;
+  }
+  // new sorted lists and inverse matrices
+  double* srt_new = glob_srt(c);
+  double* minv_new = glob_minv(c);
+  int knew[NFMAX];
+  sorted_lists(c, srt_new, knew);
+  double dlog = 0.0, dsign = 1.0;
+  bool singular = false;
+  for (int f = 0; f < m.nf && !singular; ++f) {
+    const int k = knew[f];
+    if (k == 0) continue;
+    const double* sc = srt_new + (size_t)(2 * f) * c.kcap;
+    if (!gj_inverse(c, f, k, sc, sc + c.kcap, c.dense, dlog, dsign)) {
+      singular = true;
+      break;
+    }
+    const double* I = c.dense + (size_t)c.kcap * c.kcap;
+    double* Mf = minv_new + (size_t)f * c.kcap * c.kcap;
+    for (int e = c.lane; e < k * k; e += 32) {
+      const int rc = e % k, ra = e / k;
+      Mf[(size_t)ra * c.kcap + rc] = I[(size_t)ra * c.kcap + rc];
+    }
+    __syncwarp();
+  }
+  // DetRat = DetNew * det(current inverse matrices)
+  double olog = 0.0, osign = 1.0;
+  if (!singular)
+    for (int f = 0; f < m.nf; ++f) lu_logdet_minv(c, f, c.dense, olog, osign);
+  double tr_lg = -DHUGE, tr_sg = 0.0, prob = 0.0;
+  const double det_lg = singular ? -DHUGE : dlog + olog;
+  const double det_sg = singular ? 0.0 : dsign * osign;
+  if (!singular) {
+    rebuilt_trace(c, new_outer, tr_lg, tr_sg);
+    prob = fabs(exp(__dsub_rn(tr_lg, h.trace_log) + det_lg) * factor);
+  }
+  const double rnd = grnd(c);
+  r.det_log = det_lg;
+  r.det_sign = det_sg;
+  r.tr_log = tr_lg;
+  r.tr_sign = tr_sg;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    for (int f = 0; f < m.nf; ++f) {
+      const int k = knew[f];
+      const double* src = minv_new + (size_t)f * c.kcap * c.kcap;
+      double* Mf = M_ptr(c, f);
+      for (int e = c.lane; e < k * k; e += 32) {
+        const size_t idx = (size_t)(e / k) * c.kcap + (e % k);
+        Mf[idx] = src[idx];
+      }
+      for (int ca = 0; ca < 2; ++ca) {
+        const double* st = srt_new + (size_t)(2 * f + ca) * c.kcap;
+        for (int i = c.lane; i < k; i += 32) {
+          srt_ptr(c, f, ca)[i] = st[i];
+          sslot_ptr(c, f, ca)[i] = (short)i;
+          stau_ptr(c, f, ca)[i] = st[i];
+        }
+      }
+    }
+    __syncwarp();
+    tree_flip_all(c);
+    if (c.lane == 0) {
+      for (int f = 0; f < m.nf; ++f) h.k[f] = knew[f];
+      h.det_log = dlog;
+      h.det_sign = dsign;
+      h.trace_log = tr_lg;
+      h.trace_sign = tr_sg;
+      h.outer_sst = new_outer;
+      h.acc_glob++;
+    }
+    __syncwarp();
+    const double sgn = config_sign(c);
+    if (c.lane == 0) h.cfgsign = -sgn;
+    r.outcome = 4;
+  } else {
+    for (int i = c.lane; i < K; i += 32) c.opcode[i] = opc_old[i];
+    r.outcome = 3;
+  }
+  __syncwarp();
+}
+
+// StepChangeOuter, CTQMC.F90:4570-4638 (no state sampling): new outer
+// superstate in proportion to the normalised empty-trace weights; always
+// accepted.
+__device__ NOINL void ph_change_outer(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  cthyb_record& r = *c.rec;
+  r.move = 4;
+  double lg = -DHUGE, sg = 0.0;
+  int s0 = h.outer_sst;
+  for (int tries = 0; tries < 64 && !(lg > -DHUGE); ++tries) {
+    const double rnd = grnd(c);
+    r.rand = rnd;
+    if (c.lane == 0) {
+      double acc = 0.0;
+      for (int s = 0; s < c.m->nss; ++s) {
+        s0 = s;
+        acc += c.g->empty_w[s];
+        if (acc >= rnd && c.g->empty_w[s] != 0.0) break;
+      }
+    }
+    s0 = __shfl_sync(FULL, s0, 0);
+    if (c.mono) {
+      double mx, sum;
+      root_trace(c, c.act[1], s0, mx, sum);
+      trace_log(mx, sum, lg, sg);
+    } else {
+      Mod md;
+      md.type = 0;
+      dense_trace(c, md, s0, lg, sg);
+    }
+  }
+  if (!(lg > -DHUGE)) {
+    set_status(c, ST_INTERNAL);
+    return;
+  }
+  if (c.lane == 0) {
+    h.outer_sst = s0;
+    h.trace_log = lg;
+    h.trace_sign = sg;
+  }
+  __syncwarp();
+  const double sgn = config_sign(c);
+  if (c.lane == 0) h.cfgsign = -sgn;
+  r.outcome = 4;
+  r.tr_log = lg;
+  r.tr_sign = sg;
+  __syncwarp();
+}
+
+// StepShiftTau_proper, CTQMC.F90:4641-4835, and
+// update_InvFullHybrShiftTau_diag (Trace.F90:2355-2452): every time moves by
+// -DeltaTau cyclically; the operators that wrap go to the end of the list;
+// the outer superstate becomes the one entering the new first operator; the
+// window keeps its place relative to the operators.  On acceptance M keeps
+// its entries (slot order), negated where exactly one of the creator and
+// the annihilator wrapped, and the determinant sign flips for an odd
+// dimension with an odd number of wrapped rows and columns.
+__device__ NOINL void ph_shift(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  cthyb_record& r = *c.rec;
+  const int K = h.K;
+  if (K == 0) {
+    ph_change_outer(c, p);
+    return;
+  }
+  const double beta = c.g->beta;
+  const double dtau = __dmul_rn(grnd(c), beta);
+  r.tau_c = dtau;
+  if (dtau == 0.0 || dtau == beta) {
+    r.outcome = 2;
+    __syncwarp();
+    return;
+  }
+  if (c.lane == 0) h.try_shift++;
+  __syncwarp();
+  const int first = wlb(c.optau, K, dtau, c.lane);  // first operator with tau >= DeltaTau
+  const int new_outer = first < K ? old_prefix(c, h.outer_sst, dtau) : h.outer_sst;
+  double* tau_old = glob_optau(c);
+  int* opc_old = glob_opcode(c);
+  for (int i = c.lane; i < K; i += 32) {
+    tau_old[i] = c.optau[i];
+    opc_old[i] = c.opcode[i];
+  }
+  __syncwarp();
+  for (int i = c.lane; i < K; i += 32) {
+    const int j = i + first < K ? i + first : i + first - K;
+    const double x = __dsub_rn(tau_old[j], dtau);  // modulo(tau - DeltaTau, beta)
+    c.optau[i] = x < 0.0 ? __dadd_rn(x, beta) : x;
+    c.opcode[i] = opc_old[j];
+  }
+  __syncwarp();
+  bstart_build(c);
+  const int wp_old = h.window_position, np_old = h.npairs;
+  const double wmin_old = h.tauwin_min, wmax_old = h.tauwin_max;
+  {
+    const int nw = h.num_windows;
+    const int d = (int)floor(__dmul_rn(__ddiv_rn(dtau, beta), (double)(nw + 1)));
+    const int dm = ((d % nw) + nw) % nw;
+    if (c.lane == 0) {
+      h.window_position = (((wp_old - dm) % nw) + nw) % nw;
+      h.npairs = -1;
+    }
+    __syncwarp();
+    set_window_bounds(c);
+  }
+  tree_build_inactive(c, true, false);
+  double tr_lg, tr_sg;
+  rebuilt_trace(c, new_outer, tr_lg, tr_sg);
+  const double prob = fabs(exp(__dsub_rn(tr_lg, h.trace_log)));
+  const double rnd = grnd(c);
+  r.fpos_c = new_outer;
+  r.tr_log = tr_lg;
+  r.tr_sign = tr_sg;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    double detrat = 1.0;
+    double* tmp = glob_srt(c);
+    short* tmps = (short*)glob_minv(c);
+    for (int f = 0; f < m.nf; ++f) {
+      const int k = h.k[f];
+      if (k == 0) continue;
+      const double* tc = stau_ptr(c, f, 0);
+      const double* ta = stau_ptr(c, f, 1);
+      double* Mf = M_ptr(c, f);
+      for (int e = c.lane; e < k * k; e += 32) {
+        const int sc = e % k, sa = e / k;
+        if ((tc[sc] < dtau) != (ta[sa] < dtau)) Mf[(size_t)sa * c.kcap + sc] = -Mf[(size_t)sa * c.kcap + sc];
+      }
+      int w[2];
+      for (int ca = 0; ca < 2; ++ca) {
+        double* st = srt_ptr(c, f, ca);
+        short* sl = sslot_ptr(c, f, ca);
+        double* sv = stau_ptr(c, f, ca);
+        w[ca] = wlb(st, k, dtau, c.lane);
+        for (int i = c.lane; i < k; i += 32) {
+          const int j = i + w[ca] < k ? i + w[ca] : i + w[ca] - k;
+          const double x = __dsub_rn(st[j], dtau);
+          tmp[i] = x < 0.0 ? __dadd_rn(x, beta) : x;
+          tmps[i] = sl[j];
+        }
+        __syncwarp();
+        for (int i = c.lane; i < k; i += 32) {
+          st[i] = tmp[i];
+          sl[i] = tmps[i];
+          const double x = __dsub_rn(sv[i], dtau);
+          sv[i] = x < 0.0 ? __dadd_rn(x, beta) : x;
+        }
+        __syncwarp();
+      }
+      if ((k & 1) && ((w[0] + w[1]) & 1)) detrat = -detrat;
+    }
+    tree_flip_all(c);
+    if (c.lane == 0) {
+      h.trace_log = tr_lg;
+      h.trace_sign = tr_sg;
+      h.outer_sst = new_outer;
+      h.det_sign = h.det_sign * detrat;
+      h.acc_shift++;
+    }
+    __syncwarp();
+    const double sgn = config_sign(c);
+    if (c.lane == 0) h.cfgsign = -sgn;
+    r.outcome = 4;
+  } else {
+    for (int i = c.lane; i < K; i += 32) {
+      c.optau[i] = tau_old[i];
+      c.opcode[i] = opc_old[i];
+    }
+    __syncwarp();
+    bstart_build(c);
+    if (c.lane == 0) {
+      h.window_position = wp_old;
+      h.tauwin_min = wmin_old;
+      h.tauwin_max = wmax_old;
+      h.npairs = np_old;
+    }
+    r.outcome = 3;
+  }
+  __syncwarp();
 }
 
 // One proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250) with
@@ -1621,6 +2213,12 @@ __device__ NOINL void ph_finish(Ctx& c, Prop& p) {
 __device__ void one_step(Ctx& c, Prop& p) {
   PROF_START();
   ph_draw(c, p);
+  if (p.rare) {
+    if (p.move == 2) ph_global(c, p);
+    else ph_shift(c, p);
+    if (c.h->status == ST_OK) ph_finish(c, p);
+    return;
+  }
   if (!p.alive) return;  // capacity
   PROF_MARK(0);
   if (p.move == 0) ph_setup_add(c, p);
@@ -1852,6 +2450,7 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
   mt_refill(c, h.mt_idx);
   if (reset && c.lane == 0) {  // init_counters, CTQMC.F90:847-899
     h.try_add = h.acc_add = h.try_rem = h.acc_rem = h.qn_add = h.qn_rem = 0;
+    h.try_glob = h.acc_glob = h.qn_glob = h.try_shift = h.acc_shift = 0;
     h.nprop = 0;
   }
   __syncwarp();
@@ -1922,6 +2521,7 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
     if (reset && lane == 0) {  // init_counters, CTQMC.F90:847-899
       Hdr& h = *c.h;
       h.try_add = h.acc_add = h.try_rem = h.acc_rem = h.qn_add = h.qn_rem = 0;
+      h.try_glob = h.acc_glob = h.qn_glob = h.try_shift = h.acc_shift = 0;
       h.nprop = 0;
     }
     __syncwarp();
@@ -1953,8 +2553,12 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
     const bool mine = valid && i < total && c.h->status == ST_OK;
     if (!__syncthreads_or(mine)) break;
     SPROF(9);
-    if (mine) ph_draw(c, p);
-    else if (lane == 0) p.alive = 0;
+    if (mine) {
+      ph_draw(c, p);
+    } else if (lane == 0) {
+      p.alive = 0;
+      p.rare = 0;
+    }
     SPROF(0);
     __syncthreads();
     SPROF(9);
@@ -1965,6 +2569,13 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
     PHASE(5, ph_trace(c, p))
     PHASE(6, ph_decide(c, p))
     PHASE(7, if (p.move == 0) ph_accept_add(c, p); else ph_accept_rem(c, p))
+    if (__syncthreads_or(p.rare)) {  // global and tau-shift moves, rare
+      if (p.rare) {
+        if (p.move == 2) ph_global(c, p);
+        else ph_shift(c, p);
+      }
+      __syncthreads();
+    }
     if (mine && c.h->status == ST_OK) {
       ph_finish(c, p);
       ++i;
@@ -2000,83 +2611,8 @@ __device__ void rebuild_minv(Ctx& c, double* maxdev, bool replace, double& dlog,
     int k = h.k[f];
     if (k == 0) continue;
     const int ld = c.kcap;
-    double* H = A;
-    double* I = A + (size_t)ld * ld;
-    // H(a_rank, c_rank) = Delta(tau_a - tau_c), inverse as M(c_rank, a_rank)
-    const double* sc = srt_ptr(c, f, 0);
-    const double* sa = srt_ptr(c, f, 1);
-    for (int e = c.lane; e < k * k; e += 32) {
-      int ia = e % k, ic = e / k;
-      H[(size_t)ic * ld + ia] = hybrf(c, __dsub_rn(sa[ia], sc[ic]), f);
-      I[(size_t)ic * ld + ia] = (ia == ic) ? 1.0 : 0.0;
-    }
-    __syncwarp();
-    bool sing = false;
-    for (int j = 0; j < k; ++j) {
-      // pivot: first maximal |H(i,j)|, i >= j
-      double best = -1.0;
-      int bi = j;
-      for (int i = j + c.lane; i < k; i += 32) {
-        double a = fabs(H[(size_t)j * ld + i]);
-        if (a > best) {
-          best = a;
-          bi = i;
-        }
-      }
-#pragma unroll
-      for (int o = 16; o; o >>= 1) {
-        double ob = __shfl_xor_sync(FULL, best, o);
-        int oi = __shfl_xor_sync(FULL, bi, o);
-        if (ob > best || (ob == best && oi < bi)) {
-          best = ob;
-          bi = oi;
-        }
-      }
-      if (best <= 0.0) {
-        sing = true;
-        break;
-      }
-      if (bi != j) {
-        for (int col = c.lane; col < k; col += 32) {
-          double t = H[(size_t)col * ld + j];
-          H[(size_t)col * ld + j] = H[(size_t)col * ld + bi];
-          H[(size_t)col * ld + bi] = t;
-          t = I[(size_t)col * ld + j];
-          I[(size_t)col * ld + j] = I[(size_t)col * ld + bi];
-          I[(size_t)col * ld + bi] = t;
-        }
-        dsign = -dsign;
-      }
-      __syncwarp();
-      double piv = H[(size_t)j * ld + j];
-      dlog += log(fabs(piv));
-      if (piv < 0) dsign = -dsign;
-      double ip = 1.0 / piv;
-      for (int col = c.lane; col < k; col += 32) {
-        H[(size_t)col * ld + j] *= ip;
-        I[(size_t)col * ld + j] *= ip;
-      }
-      __syncwarp();
-      for (int col = 0; col < k; ++col) {
-        double hj = H[(size_t)col * ld + j];
-        double ij = I[(size_t)col * ld + j];
-        for (int i = c.lane; i < k; i += 32) {
-          if (i == j) continue;
-          double fct = H[(size_t)j * ld + i];
-          if (col == j) continue;
-          H[(size_t)col * ld + i] -= fct * hj;
-          I[(size_t)col * ld + i] -= fct * ij;
-        }
-      }
-      __syncwarp();
-      for (int i = c.lane; i < k; i += 32)
-        if (i != j) {
-          I[(size_t)j * ld + i] -= H[(size_t)j * ld + i] * I[(size_t)j * ld + j];
-          H[(size_t)j * ld + i] = 0.0;
-        }
-      __syncwarp();
-    }
-    if (sing) {
+    const double* I = A + (size_t)ld * ld;
+    if (!gj_inverse(c, f, k, srt_ptr(c, f, 0), srt_ptr(c, f, 1), A, dlog, dsign)) {
       dlog = -DHUGE;
       dsign = 0.0;
       continue;
@@ -2342,6 +2878,20 @@ static int model_upload(cthyb_model_t M) {
     for (int i = 0; i < hm.ns; ++i) evs[i] = hm.eval[i] - hm.egs;
     d.evs = up(evs);
   }
+  d.has_szt = hm.has_szt;
+  {
+    // superstate of the spin-flipped first basis state of each superstate
+    std::vector<int> sst_of_fock((size_t)1 << hm.nf, -1), sflip(hm.nss, 0);
+    for (int s = 0; s < hm.nss; ++s)
+      for (int i = 0; i < hm.sst_n[s]; ++i) sst_of_fock[hm.occ_fock[hm.sst_off[s] + i]] = s;
+    for (int s = 0; s < hm.nss; ++s) {
+      const int st = hm.occ_fock[hm.sst_off[s]];
+      const int down = st & ((1 << hm.nd) - 1), upb = (st >> hm.nd) & ((1 << hm.nd) - 1);
+      const int t = sst_of_fock[upb | (down << hm.nd)];
+      sflip[s] = t >= 0 ? t : s;
+    }
+    d.sflip_sst = up(sflip);
+  }
   d.mono_tgt = up(hm.mono_tgt);
   d.mono_lv = up(hm.mono_lv);
   d.mono_neg = up(hm.mono_neg);
@@ -2427,6 +2977,8 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.ncorr = d.ncorr > 0 ? d.ncorr : 100;
   g.maxhisto = d.maxhisto > 1 ? d.maxhisto : 500;
   g.p_outer = d.p_outer;
+  g.p_global = d.p_global;
+  g.p_shift = d.p_shift;
   g.dense = (d.flags & CTHYB_FLAG_DENSE) ? 1 : 0;
   g.meas_dm = (d.flags & CTHYB_FLAG_NO_DM) ? 0 : 1;
   int kcap = d.kcap > 0 ? d.kcap : std::max(32, (int)std::min(4096.0, 32.0 * std::ceil(d.beta * 1.0 / 32.0 + 1.0)));
@@ -2488,6 +3040,15 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.o_log = off;
   g.logcap = logcap;
   off = align_up(off + (size_t)logcap * sizeof(cthyb_record), 256);
+  // work space of global and tau-shift moves: new inverse matrices, new
+  // sorted lists, copy of the operator arrays
+  g.o_glob = 0;
+  if (d.p_global > 0.0 || d.p_shift > 0.0) {
+    g.o_glob = off;
+    off = align_up(off + ((size_t)nf * kcap * kcap + (size_t)nf * 2 * kcap + (opcap + 2)) * 8 +
+                             (size_t)(opcap + 2) * 4,
+                   256);
+  }
   g.stride = off;
   return CTHYB_OK;
 }
@@ -3023,6 +3584,23 @@ int cthyb_debug_phase_cycles(cthyb_batch_t B, int64_t* out10) {
       CK(cudaMemcpy(&h, G.g.base + (size_t)c * G.g.stride + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost));
       for (int i = 0; i < 10; ++i) out10[i] += h.prof[i];
     }
+  return CTHYB_OK;
+}
+
+int cthyb_batch_move_counters(cthyb_batch_t B, int chain, int64_t* out5) {
+  if (!out5) return fail(CTHYB_ERR_ARG, "null");
+  GroupHost* G;
+  int lc;
+  int rc = find_chain(B, chain, &G, &lc);
+  if (rc) return rc;
+  Hdr h;
+  rc = read_hdr(B, G, lc, h);
+  if (rc) return rc;
+  out5[0] = h.try_glob;
+  out5[1] = h.acc_glob;
+  out5[2] = h.qn_glob;
+  out5[3] = h.try_shift;
+  out5[4] = h.acc_shift;
   return CTHYB_OK;
 }
 

@@ -22,6 +22,8 @@ enum : int {
 struct DModel {
   int nd, nf, ns, nss, nsmax, monomial;
   int mono_lv0;                // every monomial log|value| is zero (density-density models)
+  int has_szt;                 // spin flips map superstates to superstates (glob_has_Szt)
+  const int* sflip_sst;        // [nss] superstate of the spin-flipped first state (perform_spinflip_check_qn)
   double egs;
   const int* sst_n;            // [nss]
   const int* sst_off;          // [nss]
@@ -45,6 +47,7 @@ struct Hdr {
   int num_windows, window_position, npairs, outer_sst;
   int K, mt_idx, status, nslide;
   long long nprop, try_add, acc_add, try_rem, acc_rem, qn_add, qn_rem, cnt_meas, logn;
+  long long try_glob, acc_glob, qn_glob, try_shift, acc_shift;
   int k[NFMAX];
   // work counters for the roofline: M bytes, M flops, op-array bytes, tree node updates
   long long w_mbytes, w_mflops, w_opbytes, w_nodes;
@@ -58,12 +61,12 @@ struct DGroup {
   int nftau;
   const double* hybr;  // [nf][nftau]
   int ntau, ncorr, maxhisto;
-  double p_outer;
+  double p_outer, p_global, p_shift;  // PercentageOuterMove, PercentageGlobalMove, PercentageTauShiftMove
   int kcap, opcap, L, dense, meas_dm;
   char* base;          // chain c at base + c*stride
   size_t stride;
   size_t o_hdr, o_mt, o_optau, o_opcode, o_srt_tau, o_srt_slot, o_slot_tau, o_M, o_tree, o_act, o_bstart,
-      o_scr, o_gtau, o_histo, o_dm, o_dense, o_log;
+      o_scr, o_gtau, o_histo, o_dm, o_dense, o_log, o_glob;  // o_glob: 0 when no global/shift moves
   size_t node_bytes;   // bytes of one node slot
   long long logcap;
   const double* empty_w;  // [nss] normalised empty-trace weights

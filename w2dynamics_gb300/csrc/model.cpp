@@ -133,6 +133,7 @@ bool build_model(int nd, const double* umat, const double* muimp, const char* qn
   QN qf;
   qf.nt = q.find("Nt") != std::string::npos;
   qf.szt = q.find("Szt") != std::string::npos;
+  m.has_szt = qf.szt ? 1 : 0;
   qf.qzt = q.find("Qzt") != std::string::npos;
   qf.azt = q.find("Azt") != std::string::npos;
   qf.lzt = q.find("Lzt") != std::string::npos;

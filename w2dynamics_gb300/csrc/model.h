@@ -8,6 +8,7 @@ namespace cthyb {
 
 struct HostModel {
   int nd = 0, nf = 0, ns = 0, nss = 0, nsmax = 0, monomial = 0;
+  int has_szt = 0;                        // QuantumNumbers contains Szt (glob_has_Szt, CTQMC.F90:317-321)
   double egs = 0;
   std::vector<int> sst_n, sst_off;        // per superstate
   std::vector<int> connect;               // [nss][nf][2], flavour f = 2b+s, ca 0=c+ 1=c

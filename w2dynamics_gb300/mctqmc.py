@@ -32,9 +32,9 @@ independent chains (seeds Nseed .. Nseed+n-1) in one batch and combines
 their measurements as one longer run would (sign-weighted), the form in
 which the GPU is used efficiently.
 
-Parameters selecting moves or modes outside the engine (global and tau-shift
-moves, 4-operator and worm moves, segment, off-diagonal hybridisation,
-state sampling, retarded interactions) raise NotImplementedError at
+Parameters selecting moves or modes outside the engine (4-operator and worm
+moves, user symmetry moves, segment, off-diagonal hybridisation, state
+sampling, retarded interactions) raise NotImplementedError at
 init_solver.  Estimators that the engine does not measure (Legendre G_l,
 outer-state trace contributions, the trace-recomputation histograms
 lhisto/rhisto) are returned as zeros.  Each init_solver seeds the chains
@@ -148,8 +148,7 @@ def _str(key, default=None):
 
 def _check_supported():
     bad = []
-    for key in ("PercentageGlobalMove", "PercentageTauShiftMove", "Percentage4OperatorMove",
-                "PercentageWormInsert"):
+    for key in ("Percentage4OperatorMove", "PercentageWormInsert"):
         if _real(key, 0.0) != 0.0:
             bad.append(f"{key} = {_real(key)}")
     for key in ("segment", "offdiag", "statesampling", "Phonon", "Screening", "Uw", "NSymMove"):
@@ -186,7 +185,9 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
     group = E.Group(_beta, ftau, _int("Ntau"), nchains=_nchains, seed0=_seed,
                     taudiff_max=_real("TaudiffMax", -1.0), ncorr=_int("NCorr"),
                     p_outer=_real("PercentageOuterMove", 0.0), maxhisto=_int("MaxHisto", 500) + 1,
-                    measure_dm=_int("MeasDensityMatrix", 1) != 0)
+                    measure_dm=_int("MeasDensityMatrix", 1) != 0,
+                    p_global=_real("PercentageGlobalMove", 0.0),
+                    p_shift=_real("PercentageTauShiftMove", 0.0))
     _batch = E.Batch(_model, [group])
     ns = _model.nstates
     statessuperstates = np.zeros(ns, np.int32)
@@ -232,7 +233,7 @@ def ctqmc_measure(iSector=1, iComponent=1):
 
 def _collect():
     global gtau, gtau_full, histo, occ, rho1, rho2, densitymatrix, mean_sign, gleg, gleg_full
-    global accadd, accrem, outersuperstatehisto, outerstatehisto, signhistosuperstates
+    global accadd, accrem, accglob, accshift, outersuperstatehisto, outerstatehisto, signhistosuperstates
     global signhistostates, tracecontribsuperstates, tracecontribstates, lhisto, rhisto
     nd, ns, nf = _nd, _model.nstates, 2 * _nd
     res = [_batch.results(c) for c in range(_nchains)]
@@ -245,10 +246,14 @@ def _collect():
     mean_sign = float(signs.mean())
     histo = sum(r["histo"] for r in res) / _nchains
     cnt = {k: sum(r["counters"][k] for r in res) for k in res[0]["counters"]}
+    mc = [_batch.move_counters(c) for c in range(_nchains)]
+    mcnt = {k: sum(x[k] for x in mc) for k in mc[0]}
     accadd = np.zeros(NWormSectors)
     accrem = np.zeros(NWormSectors)
     accadd[0] = cnt["acc_add"] / max(cnt["try_add"], 1)
     accrem[0] = cnt["acc_rem"] / max(cnt["try_rem"], 1)
+    accglob = mcnt["acc_glob"] / mcnt["try_glob"] if mcnt["try_glob"] else float("nan")
+    accshift = mcnt["acc_shift"] / mcnt["try_shift"] if mcnt["try_shift"] else float("nan")
     gtau_full = np.zeros((nd, 2, nd, 2, gtau.shape[-1]))
     for b in range(nd):
         for s in range(2):
