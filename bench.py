@@ -1,8 +1,8 @@
 """Benchmark: MC updates/sec of the CT-HYB pair-move loop on one GB300.
 
-Workload (the batched configuration): 4864 independent chains of the
+Workload (the batched configuration): 4096 independent chains of the
 3-orbital density-density model (U=4, J=0.6, U'=U-2J, mu=3.3 for filling
-2/6, QuantumNumbers "Nt Szt"), 1216 chains at each beta in {10,25,50,100},
+2/6, QuantumNumbers "Nt Szt"), 1024 chains at each beta in {10,25,50,100},
 semicircular bath (D=1) with F(tau) on Ntau=Nftau=2000 points, seed = chain
 index, TaudiffMax=5, NCorr=100.  One step = one measurement cycle of every
 chain: NCorr pair proposals (StepAdd/StepRem, CTQMC.F90:8428-8476) and the
@@ -29,15 +29,18 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 BETAS = (10.0, 25.0, 50.0, 100.0)
-CHAINS_PER_BETA = 1216  # 4864 chains: 32 chain warps on each of the 152 SMs
+CHAINS_PER_BETA = 1024  # 4096 chains, 1024 at each beta
 NTAU = 2000
 NCORR = 100
 TDM = 5.0
 THERMALIZE = 2000  # proposals per chain before timing (not timed)
+TUNE = 200         # of them, per candidate schedule of the autotuner (10 candidates)
 METRIC = "MC updates/sec on 1 GB300, batched vs one-chain form, at equal G(tau) error"
-# DRAM bytes (read + write) per sweep launch of the bench workload, from the
-# ncu capture summarised in profiles/ (None until captured).
-TRAFFIC_PER_LAUNCH = None
+# From one ncu capture (--set full) of a timed sweep launch of this workload:
+# DRAM bytes read + written, FP64-pipe and issue utilisation.
+TRAFFIC_PER_LAUNCH = 349.6e6
+NCU_FP64_PIPE = 0.477
+NCU_ISSUE_ACTIVE = 0.211
 
 
 def workload_desc(chains_per_beta):
@@ -132,7 +135,9 @@ def run_gpu(args):
     cpb = args.chains_per_beta
     probs = problems()
     model, groups, batch, _ = build_batch(E, probs, cpb)
-    batch.warmup(THERMALIZE)
+    sched = batch.autotune(TUNE)  # thermalisation doubles as schedule tuning
+    batch.warmup(THERMALIZE - 10 * TUNE)
+    batch.use_graphs(True)
     batch.sync()
     stream = torch.cuda.ExternalStream(batch.stream())
     for _ in range(args.warmup):
@@ -164,7 +169,9 @@ def run_gpu(args):
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     model2, groups2, b2, h2d = build_batch(E, probs, cpb)
-    b2.warmup(THERMALIZE)
+    b2.autotune(TUNE)
+    b2.warmup(THERMALIZE - 10 * TUNE)
+    b2.use_graphs(True)
     d2h = 0
     for _ in range(args.steps):
         b2.measure(1)
@@ -200,15 +207,20 @@ def run_gpu(args):
                 "h2d_bytes_per_step": int(h2d) // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps,
                 "timed": f"model+batch creation from host arrays, {THERMALIZE} thermalisation "
-                         f"proposals per chain, {args.steps} steps each with G(tau) sums read back",
+                         f"proposals per chain (schedule autotuning included), {args.steps} steps "
+                         f"each with G(tau) sums read back",
                 "wall_s": t_e2e},
         "one_chain_form": {"value": single_value, "unit": "MC updates/s",
                            "batched_over_one_chain": value / single_value},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                      "frac": achieved / hbm, "traffic": TRAFFIC_PER_LAUNCH, "peak_kind": peak_kind,
                      "note": "algorithmic bytes of M and operator arrays per sweep launch; "
-                             "the kernel is bound by instruction issue and the FP64 pipe, not HBM"},
+                             "the kernel is bound by barrier waits, load latency and the FP64 "
+                             "pipe, not HBM",
+                     "ncu": {"fp64_pipe_busy": NCU_FP64_PIPE, "issue_active": NCU_ISSUE_ACTIVE}},
         "work": wc,
+        "schedule": {"warps_per_block": sched, "chosen_by": "autotuner (cthyb_batch_autotune)",
+                     "cuda_graphs": True},
         "gpu_launches": args.steps,
         "clocks": clocks.summary(),
     }

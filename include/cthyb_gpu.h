@@ -119,8 +119,8 @@ int cthyb_batch_reset_measurements(cthyb_batch_t batch);
 int cthyb_batch_sync(cthyb_batch_t batch);
 /* CUDA stream the batch runs on (cudaStream_t as void*). */
 int cthyb_batch_stream(cthyb_batch_t batch, void** stream);
-/* Capture warmup/measure launches into CUDA graphs and replay them
- * (1 = on, default off). */
+/* Capture the launch sequence of warmup(n) / measure(n) into a CUDA graph
+ * once per n and schedule and replay it (1 = on, default off). */
 int cthyb_batch_use_graphs(cthyb_batch_t batch, int on);
 /* How the sweep kernel schedules chains (no reference counterpart: the
  * Fortran code runs one chain per process).  -1 (default) = automatic
@@ -129,6 +129,11 @@ int cthyb_batch_use_graphs(cthyb_batch_t batch, int on);
  * phase-synchronous blocks of n chains whose proposals advance phase by
  * phase together.  Per-chain results do not depend on the schedule. */
 int cthyb_batch_set_schedule(cthyb_batch_t batch, int warps_per_block);
+/* Time `nprop` warmup proposals per chain under each schedule (independent
+ * warps; phase-synchronous blocks of 4..32 chains) and keep the fastest;
+ * the proposals are real warmup steps of the chains (no reference
+ * counterpart).  *best receives the chosen warps per block. */
+int cthyb_batch_autotune(cthyb_batch_t batch, int64_t nprop, int* best);
 
 /* Global and tau-shift move counters of one chain since the last warmup or
  * measure call: TryGlob, AccGlob, AccQNGlob, TryShift, AccShift

@@ -245,6 +245,40 @@ def test_phase_synchronous_schedule_matches_oracle(lib, warps):
         assert r0["counters"] == r1["counters"]
 
 
+def test_graph_replay_and_autotune_keep_the_chains():
+    """Warmup/measure through captured CUDA graphs give the same chains and
+    measurements as direct launches; the schedule autotuner's proposals are
+    ordinary warmup steps (the chains stay the oracle chains of their seeds)."""
+    pr = P.config_problem("dd3", beta=10.0)
+    mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    runs = []
+    for graphs in (False, True):
+        b = E.Batch(mg, [E.Group(10.0, pr["ftau"], 20, nchains=40, seed0=500, taudiff_max=5.0,
+                                 kcap=64, opcap=512, ncorr=50, p_global=0.02, p_shift=0.02)])
+        b.use_graphs(graphs)
+        for _ in range(2):
+            b.warmup(300)
+            b.measure(4)
+        b.sync()
+        runs.append(b)
+    for c in range(40):
+        assert np.array_equal(runs[0].get_config(c)[0], runs[1].get_config(c)[0])
+        r0, r1 = runs[0].results(c), runs[1].results(c)
+        assert r0["counters"] == r1["counters"]
+        assert np.allclose(r0["gtau"], r1["gtau"], rtol=1e-12, atol=1e-12 * np.abs(r0["gtau"]).max())
+    b = E.Batch(mg, [E.Group(10.0, pr["ftau"], 20, nchains=40, seed0=600, taudiff_max=5.0,
+                             kcap=64, opcap=512)])
+    best = b.autotune(50)
+    assert best in (0, 4, 8, 12, 14, 16, 20, 24, 28, 32)
+    b.sync()
+    mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    for c in (0, 39):
+        co = O.Chain(mo, 10.0, pr["ftau"], 20, seed=600 + c, taudiff_max=5.0)
+        for _ in range(10):  # one warmup call per candidate schedule
+            co.warmup(50)
+        assert np.array_equal(co.get_config()[0], b.get_config(c)[0])
+
+
 def test_set_config_and_refresh(lib):
     """set_mc_config: trace and determinant of a fixed configuration equal
     the oracle's; the LU refresh of fast-updated M shows only rounding drift."""

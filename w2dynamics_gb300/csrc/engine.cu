@@ -2811,6 +2811,14 @@ struct cthyb_batch_s {
   int nchains = 0;
   int use_graphs = 0;
   int sync_warps = -1;  // -1: automatic; 0: independent warps (k_sweep); n: phase-synchronous blocks of n warps
+  size_t sync_smem = 48 * 1024;  // dynamic shared memory the sync kernel is opted in for
+  // captured launch sequences of warmup(n) / measure(n), replayed while n and
+  // the schedule stay the same
+  struct Graph {
+    long long n = -1;
+    int sched = -2;
+    cudaGraphExec_t exec = nullptr;
+  } gwarm, gmeas;
   int nsm = 0;          // multiprocessors of the device
   long long logcap = 0;
   bool counters_reset_pending = false;
@@ -3155,6 +3163,8 @@ int cthyb_batch_destroy(cthyb_batch_t B) {
   cudaFree(B->d_dev);
   if (B->d_red) cudaFree(B->d_red);
   if (B->d_groups) cudaFree(B->d_groups);
+  if (B->gwarm.exec) cudaGraphExecDestroy(B->gwarm.exec);
+  if (B->gmeas.exec) cudaGraphExecDestroy(B->gmeas.exec);
   if (B->stream) cudaStreamDestroy(B->stream);
   delete B;
   return CTHYB_OK;
@@ -3183,19 +3193,28 @@ int cthyb_batch_set_taudiffmax(cthyb_batch_t B, int group, double tdm) {
   return CTHYB_OK;
 }
 
+// Warps per block of the sweep: the set value, or the automatic choice --
+// phase-synchronous blocks, two per multiprocessor, chains spread evenly
+// over the multiprocessors (at 64 registers a thread an SM holds 32 chain
+// warps).
+static int schedule_of(cthyb_batch_t B) {
+  int nw = B->sync_warps;
+  if (nw < 0) nw = std::min(16, std::max(1, (B->nchains + 2 * B->nsm - 1) / (2 * std::max(B->nsm, 1))));
+  return nw;
+}
+
 static int launch_sweeps(cthyb_batch_t B, long long nprop, int nmeas, int reset) {
   int Lmax = 1;
   for (GroupHost& G : B->groups) Lmax = std::max(Lmax, G.g.L);
   const int actbytes = 2 << Lmax;
-  // Automatic schedule: phase-synchronous blocks, two per multiprocessor,
-  // chains spread evenly over the multiprocessors (at 64 registers a thread
-  // an SM holds 32 chain warps).
-  int nw = B->sync_warps;
-  if (nw < 0) nw = std::min(16, std::max(1, (B->nchains + 2 * B->nsm - 1) / (2 * std::max(B->nsm, 1))));
+  const int nw = schedule_of(B);
   if (nw > 0) {
     const int nblk = (B->nchains + nw - 1) / nw;
     const size_t smem = (size_t)nw * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + actbytes);
-    if (smem > 48 * 1024) CK(cudaFuncSetAttribute(k_sweep_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (smem > B->sync_smem) {
+      CK(cudaFuncSetAttribute(k_sweep_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      B->sync_smem = smem;
+    }
     k_sweep_sync<<<nblk, nw * 32, smem, B->stream>>>(B->model->dm, B->d_groups, (int)B->groups.size(), B->nchains,
                                                      nprop, nmeas, reset, actbytes);
   } else {
@@ -3214,32 +3233,99 @@ int cthyb_batch_set_schedule(cthyb_batch_t B, int warps_per_block) {
   return CTHYB_OK;
 }
 
-int cthyb_batch_warmup(cthyb_batch_t B, int64_t n) {
-  if (!B || n < 0) return fail(CTHYB_ERR_ARG, "bad arguments");
-  // chunks keep single launches short
-  const long long chunk = 20000;
+// The launches of warmup(n) (meas = false) or measure(n); chunks keep single
+// launches short.
+static int issue_sweeps(cthyb_batch_t B, long long n, bool meas) {
+  const long long chunk = meas ? 200 : 20000;
   int reset = 1;
   for (long long done = 0; done < n; done += chunk) {
-    long long m = std::min<long long>(chunk, n - done);
-    int rc = launch_sweeps(B, m, 0, reset);
+    const long long m = std::min<long long>(chunk, n - done);
+    int rc = meas ? launch_sweeps(B, 0, (int)m, reset) : launch_sweeps(B, m, 0, reset);
     if (rc) return rc;
     reset = 0;
   }
-  if (n == 0) return launch_sweeps(B, 0, 0, 1);
+  if (n == 0 && !meas) return launch_sweeps(B, 0, 0, 1);
   return CTHYB_OK;
+}
+
+// Capture the launch sequence once per (n, schedule) and replay it.
+static int graph_sweeps(cthyb_batch_t B, cthyb_batch_s::Graph& G, long long n, bool meas) {
+  const int sched = schedule_of(B);
+  if (!G.exec || G.n != n || G.sched != sched) {
+    if (G.exec) {
+      CK(cudaGraphExecDestroy(G.exec));
+      G.exec = nullptr;
+    }
+    // kernel attributes are set outside the capture
+    int Lmax = 1;
+    for (GroupHost& g : B->groups) Lmax = std::max(Lmax, g.g.L);
+    const size_t smem = (size_t)sched * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + (2 << Lmax));
+    if (sched > 0 && smem > B->sync_smem) {
+      CK(cudaFuncSetAttribute(k_sweep_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      B->sync_smem = smem;
+    }
+    CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = issue_sweeps(B, n, meas);
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(B->stream, &graph);
+    if (rc) {
+      if (graph) cudaGraphDestroy(graph);
+      return rc;
+    }
+    CK(e);
+    e = cudaGraphInstantiate(&G.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(e);
+    G.n = n;
+    G.sched = sched;
+  }
+  CK(cudaGraphLaunch(G.exec, B->stream));
+  return CTHYB_OK;
+}
+
+int cthyb_batch_warmup(cthyb_batch_t B, int64_t n) {
+  if (!B || n < 0) return fail(CTHYB_ERR_ARG, "bad arguments");
+  return B->use_graphs ? graph_sweeps(B, B->gwarm, n, false) : issue_sweeps(B, n, false);
 }
 
 int cthyb_batch_measure(cthyb_batch_t B, int64_t nmeas) {
   if (!B || nmeas < 0) return fail(CTHYB_ERR_ARG, "bad arguments");
-  const long long chunk = 200;
-  int reset = 1;
-  for (long long done = 0; done < nmeas; done += chunk) {
-    int m = (int)std::min<long long>(chunk, nmeas - done);
-    int rc = launch_sweeps(B, 0, m, reset);
-    if (rc) return rc;
-    reset = 0;
+  if (nmeas == 0) return CTHYB_OK;
+  return B->use_graphs ? graph_sweeps(B, B->gmeas, nmeas, true) : issue_sweeps(B, nmeas, true);
+}
+
+int cthyb_batch_autotune(cthyb_batch_t B, int64_t nprop, int* best_out) {
+  if (!B || nprop < 1) return fail(CTHYB_ERR_ARG, "bad arguments");
+  const int cands[] = {0, 4, 8, 12, 14, 16, 20, 24, 28, 32};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const int saved = B->sync_warps;
+  int best = saved;
+  float best_ms = 3.4e38f;
+  int rc = CTHYB_OK;
+  for (int nw : cands) {
+    B->sync_warps = nw;
+    cudaEventRecord(e0, B->stream);
+    rc = issue_sweeps(B, nprop, false);
+    if (rc) break;
+    cudaEventRecord(e1, B->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      rc = fail(CTHYB_ERR_CUDA, "autotune launch failed");
+      break;
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = nw;
+    }
   }
-  return CTHYB_OK;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  B->sync_warps = rc ? saved : best;
+  if (best_out) *best_out = B->sync_warps;
+  return rc;
 }
 
 int cthyb_batch_reset_measurements(cthyb_batch_t B) {

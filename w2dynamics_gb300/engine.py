@@ -28,7 +28,7 @@ EXPORTS = (
     "cthyb_batch_destroy",
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
-    "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_results",
+    "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_autotune", "cthyb_batch_results",
     "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
@@ -86,6 +86,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_stream.argtypes = [vp, C.POINTER(vp)]
     L.cthyb_batch_use_graphs.argtypes = [vp, C.c_int]
     L.cthyb_batch_set_schedule.argtypes = [vp, C.c_int]
+    L.cthyb_batch_autotune.argtypes = [vp, i64, C.POINTER(C.c_int)]
     L.cthyb_batch_results.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_move_counters.argtypes = [vp, C.c_int, C.POINTER(i64)]
     L.cthyb_batch_group_sums.argtypes = [vp, C.c_int, dp, dp, C.POINTER(i64)]
@@ -246,6 +247,13 @@ class Batch:
     def set_schedule(self, warps_per_block):
         """-1: automatic; 0: independent warps; n (1..32): phase-synchronous blocks of n chains."""
         _check(load().cthyb_batch_set_schedule(self.h, int(warps_per_block)))
+
+    def autotune(self, nprop):
+        """Pick the fastest schedule on `nprop` warmup proposals per candidate;
+        returns the chosen warps per block (0: independent warps)."""
+        best = C.c_int()
+        _check(load().cthyb_batch_autotune(self.h, int(nprop), C.byref(best)))
+        return best.value
 
     # --- results
     def results(self, chain):
