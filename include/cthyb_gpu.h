@@ -90,6 +90,7 @@ typedef struct {
   double p_global;       /* PercentageGlobalMove: spin flip, CA flip, random
                             flavour permutation (StepGlob, CTQMC.F90:4433-4554) */
   double p_shift;        /* PercentageTauShiftMove (StepShiftTau, CTQMC.F90:4557-4835) */
+  int32_t nleg;          /* NLegMax: Legendre coefficients of G measured (0: none) */
 } cthyb_group_desc;
 
 #define CTHYB_FLAG_DENSE 1  /* dense block trace even for monomial models */
@@ -134,6 +135,17 @@ int cthyb_batch_set_schedule(cthyb_batch_t batch, int warps_per_block);
  * the proposals are real warmup steps of the chains (no reference
  * counterpart).  *best receives the chosen warps per block. */
 int cthyb_batch_autotune(cthyb_batch_t batch, int64_t nprop, int* best);
+
+/* The remaining Z-space estimators of one chain, normalised as in
+ * CTQMC.F90:8740-8760: gleg (Nd,2,nleg) Fortran order (MeasGtauRem's
+ * Legendre part, CTQMC.F90:2368-2389), and from MeasOuterHistograms
+ * (CTQMC.F90:3285-3341) the outer superstate/state visit histograms
+ * (nsst / nstates), their mean signs and their mean trace contributions.
+ * Trace contributions are measured for monomial models only (zero
+ * otherwise).  Any pointer may be NULL. */
+int cthyb_batch_results_extra(cthyb_batch_t batch, int chain, double* gleg, double* outer_sst_histo,
+                              double* outer_state_histo, double* sign_sst, double* sign_state,
+                              double* contrib_sst, double* contrib_state);
 
 /* Global and tau-shift move counters of one chain since the last warmup or
  * measure call: TryGlob, AccGlob, AccQNGlob, TryShift, AccShift

@@ -389,6 +389,7 @@ struct Params {
   double taudiff_max;  // TaudiffMax parameter (<=0: one window of width beta)
   double p_global, p_shift, p_4op, p_outer;
   int32_t maxhisto, meas_dm;
+  int32_t nleg;  // NLegMax (0: no Legendre measurement)
 };
 
 struct Op {
@@ -438,6 +439,9 @@ struct Chain {
   std::vector<double> histo;  // [f][maxhisto]
   std::vector<double> dm;     // ns x ns eigenbasis (offsets)
   std::vector<double> outer_histo;
+  std::vector<double> gleg;                                   // [f][nleg]
+  std::vector<double> sign_sst, contrib_sst;                  // [nss]
+  std::vector<double> state_histo, sign_state, contrib_state;  // [ns]
   double mean_sign = 0;
   // logging
   Record* log = nullptr;
@@ -1637,8 +1641,43 @@ static void meas_gtau(Chain& c) {
         M = M * c.cfgsign;
         if (idt > nt) idt = nt;
         c.gtau[(size_t)f * nt + (idt - 1)] += M;
+        // Legendre coefficients (CTQMC.F90:2368-2389)
+        if (c.p.nleg > 0) {
+          double x = ta - tc > 0.0 ? 2.0 / c.p.beta * (ta - tc) - 1.0 : 2.0 / c.p.beta * (c.p.beta + ta - tc) - 1.0;
+          double plx = 0.0, plm1x = 0.0, plp1x;
+          for (int l = 0; l < c.p.nleg; ++l) {
+            if (l == 0) {
+              plp1x = 1.0;
+            } else if (l == 1) {
+              plp1x = x;
+            } else {
+              int ll = l - 1;
+              plp1x = (2.0 * double(ll) + 1.0) / double(ll + 1) * x * plx - double(ll) / double(ll + 1) * plm1x;
+            }
+            c.gleg[(size_t)f * c.p.nleg + l] += M * plp1x;
+            plm1x = plx;
+            plx = plp1x;
+          }
+        }
       }
   }
+}
+
+// MeasOuterHistograms, CTQMC.F90:3285-3341 (no state sampling)
+static void meas_outer(Chain& c) {
+  const Model& m = *c.m;
+  int s0 = c.outer_sst, off = m.offset[s0], n = m.nst[s0];
+  c.outer_histo[s0] += 1.0;
+  c.sign_sst[s0] += c.cfgsign;
+  double sum = 0.0;
+  for (int i = 0; i < n; ++i) {
+    c.state_histo[off + i] += 1.0;
+    c.sign_state[off + i] += c.trace.sign * c.parttrace[i].sign * c.cfgsign;
+    double e = std::exp(c.parttrace[i].log);
+    sum += e;
+    c.contrib_state[off + i] += e;
+  }
+  c.contrib_sst[s0] += sum;
 }
 
 // MeasDensityMatrix_beta_half (CTQMC.F90:3088-3150) with the beta/2 states
@@ -1779,6 +1818,12 @@ void* orc_chain_create(void* model, const Params* p, const double* hybr_fortran)
   c->histo.assign((size_t)c->nf * std::max(p->maxhisto, 1), 0.0);
   c->dm.assign((size_t)m->ns * m->ns, 0.0);
   c->outer_histo.assign(m->nss, 0.0);
+  c->sign_sst.assign(m->nss, 0.0);
+  c->contrib_sst.assign(m->nss, 0.0);
+  c->state_histo.assign(m->ns, 0.0);
+  c->sign_state.assign(m->ns, 0.0);
+  c->contrib_state.assign(m->ns, 0.0);
+  c->gleg.assign((size_t)c->nf * std::max(p->nleg, 0), 0.0);
   return c;
 }
 void orc_chain_destroy(void* c) { delete (Chain*)c; }
@@ -1816,7 +1861,7 @@ int orc_chain_measure(void* cc, long long nmeas) {
     }
     c.cnt_meas++;
     c.meas_sign += c.cfgsign;  // MeasSign
-    c.outer_histo[c.outer_sst] += 1.0;
+    meas_outer(c);
     for (int f = 0; f < c.nf; ++f) {  // MeasExpOrder
       int k = (int)c.tau_c[f].size();
       int hmax = std::max(c.p.maxhisto, 1);
@@ -1843,6 +1888,30 @@ void orc_chain_results(void* cc, double* gtau, double* mean_sign, double* dm, do
     for (size_t i = 0; i < c.dm.size(); ++i) dm[i] = c.dm[i] * zs;
   if (histo)
     for (size_t i = 0; i < c.histo.size(); ++i) histo[i] = c.histo[i] / double(c.cnt_meas);
+}
+
+// gleg [f][nleg] and the outer histograms, normalised as CTQMC.F90:8740-8760
+void orc_chain_results_extra(void* cc, double* gleg, double* sst_histo, double* state_histo, double* sign_sst,
+                             double* sign_state, double* contrib_sst, double* contrib_state) {
+  Chain& c = *(Chain*)cc;
+  double cnt = double(c.cnt_meas);
+  double ms = c.meas_sign / cnt;
+  double zs = -1.0 / (cnt * ms);
+  for (int f = 0; f < c.nf; ++f)
+    for (int l = 0; l < c.p.nleg; ++l) {
+      double v = c.gleg[(size_t)f * c.p.nleg + l] * std::sqrt(double(2 * l) + 1.0) / c.p.beta;
+      gleg[(size_t)f * c.p.nleg + l] = -v * zs;
+    }
+  for (int s = 0; s < c.m->nss; ++s) {
+    sign_sst[s] = c.sign_sst[s] / c.outer_histo[s];
+    sst_histo[s] = c.outer_histo[s] / cnt;
+    contrib_sst[s] = c.contrib_sst[s] / cnt;
+  }
+  for (int i = 0; i < c.m->ns; ++i) {
+    sign_state[i] = c.sign_state[i] / c.state_histo[i];
+    state_histo[i] = c.state_histo[i] / cnt;
+    contrib_state[i] = c.contrib_state[i] / cnt;
+  }
 }
 
 void orc_chain_counters(void* cc, long long* out) {

@@ -27,7 +27,8 @@ class Params(C.Structure):
     _fields_ = [("beta", C.c_double), ("nftau", C.c_int32), ("ntau", C.c_int32),
                 ("ncorr", C.c_int32), ("seed", C.c_int32), ("taudiff_max", C.c_double),
                 ("p_global", C.c_double), ("p_shift", C.c_double), ("p_4op", C.c_double),
-                ("p_outer", C.c_double), ("maxhisto", C.c_int32), ("meas_dm", C.c_int32)]
+                ("p_outer", C.c_double), ("maxhisto", C.c_int32), ("meas_dm", C.c_int32),
+                ("nleg", C.c_int32)]
 
 
 _lib = None
@@ -68,6 +69,7 @@ def lib():
         L.orc_chain_measure.argtypes = [vp, C.c_longlong]
         L.orc_chain_results.argtypes = [vp, dp, dp, dp, dp]
         L.orc_chain_counters.argtypes = [vp, C.POINTER(C.c_longlong)]
+        L.orc_chain_results_extra.argtypes = [vp, dp, dp, dp, dp, dp, dp, dp]
         L.orc_chain_state.argtypes = [vp, dp]
         L.orc_chain_get_config.argtypes = [vp, dp, ip, ip, ip]
         L.orc_chain_set_config.argtypes = [vp, C.c_int, dp, ip, ip, ip, C.c_int]
@@ -142,7 +144,7 @@ class Chain:
     """One Markov chain of the restated reference loop."""
 
     def __init__(self, model, beta, ftau, ntau, seed, taudiff_max=-1.0, ncorr=100,
-                 p_outer=0.0, maxhisto=500, meas_dm=1, p_global=0.0, p_shift=0.0):
+                 p_outer=0.0, maxhisto=500, meas_dm=1, p_global=0.0, p_shift=0.0, nleg=0):
         L = lib()
         self.model = model
         nd = model.nd
@@ -154,7 +156,7 @@ class Chain:
         self.maxhisto = maxhisto
         p = Params(beta=beta, nftau=self.nftau, ntau=ntau, ncorr=ncorr, seed=seed,
                    taudiff_max=taudiff_max, p_global=p_global, p_shift=p_shift, p_4op=0.0,
-                   p_outer=p_outer, maxhisto=maxhisto, meas_dm=meas_dm)
+                   p_outer=p_outer, maxhisto=maxhisto, meas_dm=meas_dm, nleg=nleg)
         self.params = p
         self.h = L.orc_chain_create(model.h, C.byref(p), _dp(self._ftau.ravel(order="F")))
         self._log = None
@@ -191,6 +193,18 @@ class Chain:
         return dict(gtau=g.reshape(nf, self.ntau), mean_sign=float(ms[0]),
                     densitymatrix=dm.reshape(ns, ns, order="F"),
                     histo=hi.reshape(nf, self.maxhisto))
+
+    def results_extra(self):
+        nf, ns, nss = 2 * self.model.nd, self.model.nstates, len(self.model.sst_size)
+        nleg = self.params.nleg
+        gl = np.zeros(max(1, nf * nleg))
+        arrs = [np.zeros(nss), np.zeros(ns), np.zeros(nss), np.zeros(ns), np.zeros(nss), np.zeros(ns)]
+        lib().orc_chain_results_extra(self.h, _dp(gl), *[_dp(a) for a in arrs])
+        keys = ("outer_sst_histo", "outer_state_histo", "sign_sst", "sign_state", "contrib_sst",
+                "contrib_state")
+        out = dict(zip(keys, arrs))
+        out["gleg"] = gl[:nf * nleg].reshape(nf, nleg)
+        return out
 
     def counters(self):
         out = (C.c_longlong * 12)()

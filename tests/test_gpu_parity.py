@@ -163,17 +163,20 @@ def test_proposal_stream_parity(lib, name, beta, tdm, pout, nprop, seed, dense, 
 
 
 def test_measurement_parity(lib):
-    """G(tau), sign, histogram and density matrix of one chain equal the
-    oracle's to rounding (identical proposal streams)."""
+    """G(tau), sign, histogram, density matrix, Legendre G_l and the outer
+    superstate/state histograms of one chain (global and tau-shift moves at
+    1 % each) equal the oracle's to rounding (identical proposal streams)."""
     pr = P.config_problem("dd3", beta=10.0)
     mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
-    co = O.Chain(mo, 10.0, pr["ftau"], 40, seed=9, taudiff_max=5.0, p_outer=0.1, ncorr=50)
+    co = O.Chain(mo, 10.0, pr["ftau"], 40, seed=9, taudiff_max=5.0, p_outer=0.1, ncorr=50,
+                 p_global=0.01, p_shift=0.01, nleg=12)
     co.warmup(2000)
     co.measure(300)
     ro = co.results()
     mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
     b = E.Batch(mg, [E.Group(10.0, pr["ftau"], 40, nchains=1, seed0=9, taudiff_max=5.0,
-                             p_outer=0.1, ncorr=50, kcap=64, opcap=512)])
+                             p_outer=0.1, ncorr=50, kcap=64, opcap=512, p_global=0.01,
+                             p_shift=0.01, nleg=12)])
     b.warmup(2000)
     b.measure(300)
     b.sync()
@@ -186,6 +189,16 @@ def test_measurement_parity(lib):
     ho = ro["histo"]
     hg = np.stack([rg["histo"][f // 2, f % 2] for f in range(6)])
     assert np.array_equal(hg[:, :ho.shape[1]], ho)
+    # Legendre coefficients and outer-state histograms
+    xo, xg = co.results_extra(), b.results_extra(0)
+    gl = np.stack([xg["gleg"][f // 2, f % 2] for f in range(6)])
+    assert np.allclose(gl, xo["gleg"], rtol=1e-9, atol=1e-12 * np.abs(xo["gleg"]).max())
+    for key in ("outer_sst_histo", "outer_state_histo"):
+        assert np.array_equal(xg[key], xo[key]), key
+    for key in ("sign_sst", "sign_state"):
+        assert np.allclose(xg[key], xo[key], rtol=1e-12, atol=1e-12, equal_nan=True), key
+    for key in ("contrib_sst", "contrib_state"):
+        assert np.allclose(xg[key], xo[key], rtol=1e-9, atol=1e-300), key
 
 
 def test_batched_chains_match_oracle_per_seed(lib):

@@ -77,7 +77,8 @@ def test_solve_through_the_module_matches_the_oracle():
     ctqmc.ctqmc_measure(1, 1)
     mo = O.Model(nd, pr["umatrix"], pr["muimp"], "Nt Szt")
     co = O.Chain(mo, 10.0, ftau, ntau, seed=11, taudiff_max=5.0, ncorr=BASE["NCorr"],
-                 p_outer=0.1, maxhisto=BASE["MaxHisto"] + 1, p_global=0.005, p_shift=0.005)
+                 p_outer=0.1, maxhisto=BASE["MaxHisto"] + 1, p_global=0.005, p_shift=0.005,
+                 nleg=BASE["NLegMax"])
     co.set_taudiffmax(5.0)
     co.warmup(BASE["Nwarmups"])
     co.measure(BASE["Nmeas"])
@@ -96,6 +97,11 @@ def test_solve_through_the_module_matches_the_oracle():
     assert np.allclose(ctqmc.occ, ref["occ"], atol=1e-10)
     assert np.allclose(ctqmc.rho1, ref["rho1"], atol=1e-10)
     assert ctqmc.gtau_full.shape == (nd, 2, nd, 2, ntau)
+    xo = co.results_extra()
+    gl = np.stack([ctqmc.gleg[f // 2, f % 2] for f in range(2 * nd)])
+    assert np.allclose(gl, xo["gleg"], rtol=1e-9, atol=1e-12 * np.abs(xo["gleg"]).max())
+    assert np.array_equal(ctqmc.outersuperstatehisto, xo["outer_sst_histo"])
+    assert np.allclose(ctqmc.signhistosuperstates, xo["sign_sst"], equal_nan=True)
     assert ctqmc.occbasismapping.shape == (mo.nstates, nd, 2)
     cnt = co.counters()
     assert ctqmc.accadd[0] == cnt["acc_add"] / cnt["try_add"]

@@ -165,6 +165,54 @@ def test_global_and_shift_moves_keep_state_consistent(name, beta, tdm):
             assert np.allclose(c.minv(2 * b + s), np.linalg.inv(H), rtol=1e-9, atol=1e-9)
 
 
+def test_legendre_coefficients_u0_known_answer_and_sum_rule():
+    """Legendre G_l (MeasGtauRem, CTQMC.F90:2368-2389): at U = 0 equal to
+    sqrt(2l+1) * int_0^beta P_l(2 tau/beta - 1) g(tau) dtau of the bath; and
+    G_0 = (beta/Ntau) * sum of the G(tau) bins in the same run (both sum the
+    same M elements)."""
+    from numpy.polynomial import legendre as npl
+    beta, nleg = 5.0, 8
+    um = P.flat_umatrix(P.umatrix_density(1, 0.0, 0.0, 0.0))
+    ft = P.semicircle_ftau(1, beta, 1.0, 500)
+    g = P.semicircle_gtau(beta, 1.0, 500)
+    m = O.Model(1, um, P.muimp_solver(1, 0.0), "Nt Szt Azt")
+    gls = []
+    for seed in range(16):
+        c = O.Chain(m, beta, ft, 20, seed=200 + seed, taudiff_max=beta, nleg=nleg)
+        c.warmup(3000)
+        c.measure(3000)
+        r, x = c.results(), c.results_extra()
+        for f in range(2):
+            assert abs(x["gleg"][f, 0] - r["gtau"][f].sum() * beta / 20) < 1e-12
+        gls.append(x["gleg"])
+    G = np.mean(gls, axis=0)
+    E = np.std(gls, axis=0, ddof=1) / np.sqrt(len(gls))
+    tt = np.linspace(0, beta, 20001)
+    gg = np.interp(tt, np.linspace(0, beta, 500), g)
+    exact = np.array([np.sqrt(2 * l + 1) * np.trapezoid(npl.legval(2 * tt / beta - 1, [0] * l + [1]) * gg, tt)
+                      for l in range(nleg)])
+    z = (G - exact[None, :]) / E
+    assert np.abs(z).max() < 4.5, z
+
+
+def test_outer_histograms_sum_rules():
+    """MeasOuterHistograms: superstate visit frequencies sum to one, state
+    visits add up to their superstate's size, signs are within [-1, 1] and
+    the trace contributions of the states add up to their superstate's."""
+    pr = P.config_problem("dd3", beta=8.0)
+    m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    c = O.Chain(m, 8.0, pr["ftau"], 20, seed=3, taudiff_max=4.0, ncorr=20, p_global=0.05, p_shift=0.05)
+    c.warmup(2000)
+    c.measure(300)
+    x = c.results_extra()
+    assert abs(x["outer_sst_histo"].sum() - 1.0) < 1e-12
+    for s, (o, n) in enumerate(zip(m.sst_offset, m.sst_size)):
+        assert np.allclose(x["outer_state_histo"][o:o + n], x["outer_sst_histo"][s])
+        assert abs(x["contrib_state"][o:o + n].sum() - x["contrib_sst"][s]) <= 1e-12 * max(1, x["contrib_sst"][s])
+    visited = x["outer_sst_histo"] > 0
+    assert np.all(np.abs(x["sign_sst"][visited]) <= 1.0)
+
+
 def test_u0_green_function_with_global_and_shift_moves():
     """The U=0 known answer of the bath G(tau) holds with global and
     tau-shift moves switched on (detailed balance of the added moves)."""

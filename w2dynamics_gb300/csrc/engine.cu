@@ -2279,30 +2279,102 @@ __device__ NOINL void measure(Ctx& c) {
     }
     __syncwarp();
   }
-  // MeasGtauRem(.false.): M elements binned by tau_a - tau_c
-  const int nt = g.ntau;
+  // MeasOuterHistograms (CTQMC.F90:3285-3341, no state sampling); the
+  // per-state trace contributions come from the root of the state tree
+  {
+    const int s0 = h.outer_sst, off = m.sst_off[s0], n0 = m.sst_n[s0];
+    double* oh = (double*)((char*)c.gtau - g.o_gtau + g.o_outer);
+    // [0,nss) superstate visits, [nss,2nss) superstate signs, [2nss,3nss)
+    // superstate contributions, then the same three for states
+    double* st_visit = oh + 3 * m.nss;
+    double* st_sign = st_visit + m.ns;
+    double* st_contr = st_sign + m.ns;
+    double csum = 0.0;
+    const double* lw = c.mono ? node_lw(c, 1, c.act[1]) : nullptr;
+    const uint16_t* tg = c.mono ? node_tg(c, 1, c.act[1]) : nullptr;
+    for (int i = c.lane; i < n0; i += 32) {
+      const int st = off + i;
+      double psign = 1.0, contr = 0.0;
+      if (c.mono && (tg[st] & 0x7fff) == st) {
+        psign = (tg[st] & 0x8000) ? -1.0 : 1.0;
+        contr = exp(lw[st]);
+      }
+      st_visit[st] += 1.0;
+      st_sign[st] += h.trace_sign * psign * h.cfgsign;
+      st_contr[st] += contr;
+      csum += contr;
+    }
+    csum = wsum(csum);
+    if (c.lane == 0) {
+      oh[s0] += 1.0;
+      oh[m.nss + s0] += h.cfgsign;
+      oh[2 * m.nss + s0] += csum;
+    }
+    __syncwarp();
+  }
+  // MeasGtauRem(.false.): M elements binned by tau_a - tau_c, and their
+  // Legendre coefficients (CTQMC.F90:2252-2440)
+  const int nt = g.ntau, nleg = g.nleg;
+  double* lsum = nleg > 0 ? (double*)((char*)c.gtau - g.o_gtau + g.o_glscr) + (size_t)c.lane * nleg : nullptr;
   for (int f = 0; f < m.nf; ++f) {
     int k = h.k[f];
     const double* Mf = M_ptr(c, f);
     const double* tcs = stau_ptr(c, f, 0);
     const double* tas = stau_ptr(c, f, 1);
     double* G = c.gtau + (size_t)f * nt;
+    for (int l = 0; l < nleg; ++l) lsum[l] = 0.0;
     for (int i = c.lane; i < k; i += 32) {
       double tc = tcs[i];
       for (int j = 0; j < k; ++j) {
         double Mv = Mf[(size_t)j * c.kcap + i];
         double ta = tas[j];
-        int idt;
+        double dt;
         if (ta - tc > 0.0) {
-          idt = (int)((ta - tc) * g.gscale) + 1;  // (ta - tc) / beta * Ntau
+          dt = ta - tc;
         } else {
-          idt = (int)((g.beta + ta - tc) * g.gscale) + 1;
+          dt = g.beta + ta - tc;
           Mv = -Mv;
         }
+        // idt = int(dt / beta * Ntau) + 1, evaluated exactly as written
+        // where dt * (Ntau / beta) lies close to a bin edge
+        const double q = dt * g.gscale;
+        int idt = (int)q;
+        const double fr = q - (double)idt;
+        if (fr < 1e-9 || fr > 1.0 - 1e-9) idt = (int)__dmul_rn(__ddiv_rn(dt, g.beta), (double)nt);
+        idt += 1;
         Mv = Mv * h.cfgsign;
         if (idt > nt) idt = nt;
         atomicAdd(&G[idt - 1], Mv);
+        if (nleg > 0) {
+          // P_l by the three-term recurrence, as evaluated in the reference
+          const double x = __dsub_rn(__dmul_rn(__ddiv_rn(2.0, g.beta), dt), 1.0);
+          double plx = 0.0, plm1 = 0.0;
+          for (int l = 0; l < nleg; ++l) {
+            double p;
+            if (l == 0) {
+              p = 1.0;
+            } else if (l == 1) {
+              p = x;
+            } else {
+              const int ll = l - 1;
+              p = __dsub_rn(__dmul_rn(__dmul_rn(__ddiv_rn(2.0 * ll + 1.0, (double)(ll + 1)), x), plx),
+                            __dmul_rn(__ddiv_rn((double)ll, (double)(ll + 1)), plm1));
+            }
+            lsum[l] = __dadd_rn(lsum[l], __dmul_rn(Mv, p));
+            plm1 = plx;
+            plx = p;
+          }
+        }
       }
+    }
+    if (nleg > 0) {
+      __syncwarp();
+      double* GL = (double*)((char*)c.gtau - g.o_gtau + g.o_gleg) + (size_t)f * nleg;
+      for (int l = 0; l < nleg; ++l) {
+        const double v = wsum(lsum[l]);
+        if (c.lane == 0) GL[l] += v;
+      }
+      __syncwarp();
     }
   }
   __syncwarp();
@@ -3042,12 +3114,22 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   off = align_up(off + (size_t)nf * g.maxhisto * 8, 256);
   g.o_dm = off;
   off = align_up(off + (size_t)hm.ns * 8, 256);
+  g.nleg = d.nleg > 0 ? d.nleg : 0;
+  g.o_gleg = off;
+  off = align_up(off + (size_t)nf * g.nleg * 8, 256);
+  g.o_outer = off;  // outer superstate/state histograms, signs, trace contributions
+  off = align_up(off + (size_t)3 * (hm.nss + hm.ns) * 8, 256);
   g.o_dense = off;
   size_t dense = std::max((size_t)2 * hm.nsmax * hm.nsmax, (size_t)2 * kcap * kcap) * 8;
   off = align_up(off + dense, 256);
   g.o_log = off;
   g.logcap = logcap;
   off = align_up(off + (size_t)logcap * sizeof(cthyb_record), 256);
+  g.o_glscr = 0;
+  if (g.nleg > 0) {
+    g.o_glscr = off;
+    off = align_up(off + (size_t)32 * g.nleg * 8, 256);
+  }
   // work space of global and tau-shift moves: new inverse matrices, new
   // sorted lists, copy of the operator arrays
   g.o_glob = 0;
@@ -3400,6 +3482,55 @@ int cthyb_batch_state(cthyb_batch_t B, int chain, double* o) {
   o[13] = h.nslide;
   o[14] = h.status;
   o[15] = h.k[0];
+  return CTHYB_OK;
+}
+
+int cthyb_batch_results_extra(cthyb_batch_t B, int chain, double* gleg, double* outer_sst_histo,
+                              double* outer_state_histo, double* sign_sst, double* sign_state,
+                              double* contrib_sst, double* contrib_state) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  const HostModel& hm = B->model->hm;
+  char* base = G->g.base + (size_t)c * G->g.stride;
+  const int nf = hm.nf, nleg = G->g.nleg, nss = hm.nss, ns = hm.ns;
+  const double cnt = (double)h.cnt_meas;
+  const double ms = h.cnt_meas ? h.meas_sign / cnt : 0.0;
+  if (gleg && nleg > 0) {
+    std::vector<double> raw((size_t)nf * nleg);
+    CK(cudaMemcpy(raw.data(), base + G->g.o_gleg, raw.size() * 8, cudaMemcpyDeviceToHost));
+    const double zs = h.cnt_meas ? -1.0 / (cnt * ms) : 0.0;
+    for (int f = 0; f < nf; ++f)
+      for (int l = 0; l < nleg; ++l) {
+        // GLeg * sqrt(2l+1)/beta, then -GLeg * zScaling (CTQMC.F90:8755-8760)
+        const double v = raw[(size_t)f * nleg + l] * std::sqrt(2.0 * l + 1.0) / G->g.beta;
+        gleg[(f / 2) + hm.nd * ((f % 2) + 2 * (size_t)l)] = -v * zs;
+      }
+  }
+  std::vector<double> o((size_t)3 * (nss + ns));
+  CK(cudaMemcpy(o.data(), base + G->g.o_outer, o.size() * 8, cudaMemcpyDeviceToHost));
+  const double* sv = o.data();
+  const double* ss = sv + nss;
+  const double* sc = ss + nss;
+  const double* tv = sc + nss;
+  const double* ts = tv + ns;
+  const double* tc = ts + ns;
+  // SignHisto /= visits (0/0 stays NaN as in the reference), histograms and
+  // contributions / CntMeas (CTQMC.F90:8740-8752)
+  for (int s = 0; s < nss; ++s) {
+    if (sign_sst) sign_sst[s] = ss[s] / sv[s];
+    if (outer_sst_histo) outer_sst_histo[s] = sv[s] / cnt;
+    if (contrib_sst) contrib_sst[s] = sc[s] / cnt;
+  }
+  for (int i = 0; i < ns; ++i) {
+    if (sign_state) sign_state[i] = ts[i] / tv[i];
+    if (outer_state_histo) outer_state_histo[i] = tv[i] / cnt;
+    if (contrib_state) contrib_state[i] = tc[i] / cnt;
+  }
   return CTHYB_OK;
 }
 

@@ -61,12 +61,14 @@ struct DGroup {
   int nftau;
   const double* hybr;  // [nf][nftau]
   int ntau, ncorr, maxhisto;
+  int nleg;            // Legendre coefficients of G measured (NLegMax; 0: none)
   double p_outer, p_global, p_shift;  // PercentageOuterMove, PercentageGlobalMove, PercentageTauShiftMove
   int kcap, opcap, L, dense, meas_dm;
   char* base;          // chain c at base + c*stride
   size_t stride;
   size_t o_hdr, o_mt, o_optau, o_opcode, o_srt_tau, o_srt_slot, o_slot_tau, o_M, o_tree, o_act, o_bstart,
-      o_scr, o_gtau, o_histo, o_dm, o_dense, o_log, o_glob;  // o_glob: 0 when no global/shift moves
+      o_scr, o_gtau, o_histo, o_dm, o_gleg, o_outer, o_dense, o_log, o_glob,  // o_glob: 0 without global/shift moves
+      o_glscr;  // per-lane Legendre partial sums (0 when nleg == 0)
   size_t node_bytes;   // bytes of one node slot
   long long logcap;
   const double* empty_w;  // [nss] normalised empty-trace weights

@@ -29,7 +29,7 @@ EXPORTS = (
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
     "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_autotune", "cthyb_batch_results",
-    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_state", "cthyb_batch_get_config",
+    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_results_extra", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
     "cthyb_minv_rebuild_noalloc",
@@ -42,7 +42,8 @@ class GroupDesc(C.Structure):
                 ("seeds", C.POINTER(C.c_int32)), ("taudiff_max", C.c_double),
                 ("ncorr", C.c_int32), ("p_outer", C.c_double), ("kcap", C.c_int32),
                 ("opcap", C.c_int32), ("tree_levels", C.c_int32), ("maxhisto", C.c_int32),
-                ("flags", C.c_int32), ("p_global", C.c_double), ("p_shift", C.c_double)]
+                ("flags", C.c_int32), ("p_global", C.c_double), ("p_shift", C.c_double),
+                ("nleg", C.c_int32)]
 
 
 class EngineError(RuntimeError):
@@ -89,6 +90,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_autotune.argtypes = [vp, i64, C.POINTER(C.c_int)]
     L.cthyb_batch_results.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_move_counters.argtypes = [vp, C.c_int, C.POINTER(i64)]
+    L.cthyb_batch_results_extra.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp]
     L.cthyb_batch_group_sums.argtypes = [vp, C.c_int, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_state.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_get_config.argtypes = [vp, C.c_int, ip, dp, ip, ip, ip, ip]
@@ -169,7 +171,7 @@ class Group:
 
     def __init__(self, beta, ftau, ntau, nchains=1, seed0=0, seeds=None, taudiff_max=-1.0,
                  ncorr=100, p_outer=0.0, kcap=0, opcap=0, tree_levels=0, maxhisto=500,
-                 dense=False, measure_dm=True, p_global=0.0, p_shift=0.0):
+                 dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0):
         self.beta = float(beta)
         self.ftau = np.asfortranarray(np.asarray(ftau, np.float64))
         self.ntau = int(ntau)
@@ -180,6 +182,7 @@ class Group:
         self.ncorr = int(ncorr)
         self.p_outer = float(p_outer)
         self.p_global, self.p_shift = float(p_global), float(p_shift)
+        self.nleg = int(nleg)
         self.kcap, self.opcap, self.tree_levels = int(kcap), int(opcap), int(tree_levels)
         self.maxhisto = int(maxhisto)
         self.flags = (FLAG_DENSE if dense else 0) | (0 if measure_dm else FLAG_NO_DM)
@@ -201,6 +204,7 @@ class Group:
         d.maxhisto = self.maxhisto
         d.flags = self.flags
         d.p_global, d.p_shift = self.p_global, self.p_shift
+        d.nleg = self.nleg
         return d
 
 
@@ -271,6 +275,19 @@ class Batch:
                     histo=hi.reshape((nd, 2, g.maxhisto), order="F"),
                     counters=dict(zip(("try_add", "acc_add", "try_rem", "acc_rem", "qn_add",
                                        "qn_rem", "cnt_meas", "proposals"), cnt.tolist())))
+
+    def results_extra(self, chain):
+        """Legendre G_l (Nd,2,nleg) and the outer superstate/state histograms."""
+        g = self.groups[self._group_of[chain]]
+        nd, ns, nss = self.model.nd, self.model.nstates, self.model.nsst
+        gl = np.zeros(max(1, nd * 2 * g.nleg))
+        arrs = [np.zeros(nss), np.zeros(ns), np.zeros(nss), np.zeros(ns), np.zeros(nss), np.zeros(ns)]
+        _check(load().cthyb_batch_results_extra(self.h, chain, _dp(gl), *[_dp(a) for a in arrs]))
+        keys = ("outer_sst_histo", "outer_state_histo", "sign_sst", "sign_state", "contrib_sst",
+                "contrib_state")
+        out = dict(zip(keys, arrs))
+        out["gleg"] = gl[:nd * 2 * g.nleg].reshape((nd, 2, g.nleg), order="F")
+        return out
 
     def move_counters(self, chain):
         """Global and tau-shift move counters since the last warmup/measure call."""

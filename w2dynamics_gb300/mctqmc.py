@@ -35,9 +35,9 @@ which the GPU is used efficiently.
 Parameters selecting moves or modes outside the engine (4-operator and worm
 moves, user symmetry moves, segment, off-diagonal hybridisation, state
 sampling, retarded interactions) raise NotImplementedError at
-init_solver.  Estimators that the engine does not measure (Legendre G_l,
-outer-state trace contributions, the trace-recomputation histograms
-lhisto/rhisto) are returned as zeros.  Each init_solver seeds the chains
+init_solver.  The trace-recomputation histograms lhisto/rhisto describe the
+reference's list-walking implementation and are returned as zeros; outer
+trace contributions are measured for density-density (monomial) models.  Each init_solver seeds the chains
 from Nseed; the reference continues one global random stream across
 solves, so solves after the first draw different (equally valid) streams.
 """
@@ -187,7 +187,7 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
                     p_outer=_real("PercentageOuterMove", 0.0), maxhisto=_int("MaxHisto", 500) + 1,
                     measure_dm=_int("MeasDensityMatrix", 1) != 0,
                     p_global=_real("PercentageGlobalMove", 0.0),
-                    p_shift=_real("PercentageTauShiftMove", 0.0))
+                    p_shift=_real("PercentageTauShiftMove", 0.0), nleg=_int("NLegMax", 100))
     _batch = E.Batch(_model, [group])
     ns = _model.nstates
     statessuperstates = np.zeros(ns, np.int32)
@@ -268,16 +268,23 @@ def _collect():
         occ = np.zeros((nd, 2, nd, 2))
         rho1 = np.zeros((nf, nf))
         rho2 = np.zeros((nf,) * 4)
-    nleg = _int("NLegMax", 100)
-    gleg = np.zeros((nd, 2, nleg))
+    ext = [_batch.results_extra(c) for c in range(_nchains)]
+    gleg = sum(x["gleg"] * s for x, s in zip(ext, signs)) / wsum
+    nleg = gleg.shape[-1]
     gleg_full = np.zeros((nd, 2, nd, 2, nleg))
-    nss = _model.nsst
-    outersuperstatehisto = np.zeros(nss)
-    outerstatehisto = np.zeros(ns)
-    signhistosuperstates = np.zeros(nss)
-    signhistostates = np.zeros(ns)
-    tracecontribsuperstates = np.zeros(nss)
-    tracecontribstates = np.zeros(ns)
+    for b in range(nd):
+        for s in range(2):
+            gleg_full[b, s, b, s] = gleg[b, s]
+    outersuperstatehisto = sum(x["outer_sst_histo"] for x in ext) / _nchains
+    outerstatehisto = sum(x["outer_state_histo"] for x in ext) / _nchains
+    with np.errstate(invalid="ignore", divide="ignore"):
+        # per-chain signs are normalised by their own visit counts
+        signhistosuperstates = (sum(np.nan_to_num(x["sign_sst"]) * x["outer_sst_histo"] for x in ext)
+                                / (outersuperstatehisto * _nchains))
+        signhistostates = (sum(np.nan_to_num(x["sign_state"]) * x["outer_state_histo"] for x in ext)
+                           / (outerstatehisto * _nchains))
+    tracecontribsuperstates = sum(x["contrib_sst"] for x in ext) / _nchains
+    tracecontribstates = sum(x["contrib_state"] for x in ext) / _nchains
     lhisto = np.zeros(1)
     rhisto = np.zeros(1)
 
