@@ -114,27 +114,29 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def build_batch(E, probs, cpb):
-    """Model and one group of `cpb` chains per beta, from host arrays."""
+def build_batch(E, probs, cpb, rank=0):
+    """Model and `cpb` chains per beta for one GPU, from host arrays; seed =
+    chain index of the whole job (rank r holds chains r*4*cpb ...)."""
     pr0 = probs[0]
     model = E.Model(pr0["nd"], pr0["umatrix"], pr0["muimp"], pr0["quantum_numbers"])
     groups = []
     for i, pr in enumerate(probs):
         groups.append(E.Group(pr["beta"], pr["ftau"], pr["ntau"], nchains=cpb,
-                              seed0=i * cpb, taudiff_max=TDM, ncorr=NCORR,
+                              seed0=(rank * len(probs) + i) * cpb, taudiff_max=TDM, ncorr=NCORR,
                               kcap=32 if pr["beta"] <= 25 else 64,
                               opcap=256 if pr["beta"] <= 25 else (512 if pr["beta"] <= 50 else 1024)))
     h2d = sum(g.ftau.nbytes for g in groups) + pr0["umatrix"].nbytes + pr0["muimp"].nbytes
     return model, groups, E.Batch(model, groups), h2d
 
 
-def run_gpu(args):
+def run_gpu(args, rank=0, world=1):
     import torch
     from w2dynamics_gb300 import engine as E
+    from w2dynamics_gb300 import shard
 
     cpb = args.chains_per_beta
     probs = problems()
-    model, groups, batch, _ = build_batch(E, probs, cpb)
+    model, groups, batch, _ = build_batch(E, probs, cpb, rank)
     sched = batch.autotune(TUNE)  # thermalisation doubles as schedule tuning
     batch.warmup(THERMALIZE - 10 * TUNE)
     batch.use_graphs(True)
@@ -146,7 +148,10 @@ def run_gpu(args):
     batch.work_counters(reset=True)
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
-    nchains = batch.nchains
+    nchains = world * len(BETAS) * cpb  # the whole job (weak scaling: fixed chains per GPU)
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
     with ClockSampler() as clocks:
         torch.cuda.synchronize()
         with torch.cuda.stream(stream):
@@ -156,7 +161,7 @@ def run_gpu(args):
             stop.record(stream)
         stop.synchronize()
     batch.sync()
-    ms = start.elapsed_time(stop)
+    ms = shard.max_over_ranks(start.elapsed_time(stop))
     props = nchains * NCORR * args.steps
     value = props / (ms / 1e3)
     wc = batch.work_counters(reset=False)
@@ -167,8 +172,10 @@ def run_gpu(args):
     # device->host read of every group's G(tau) and sign sums.  All proposals
     # of the call (thermalisation included) count as updates.
     torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
     t0 = time.perf_counter()
-    model2, groups2, b2, h2d = build_batch(E, probs, cpb)
+    model2, groups2, b2, h2d = build_batch(E, probs, cpb, rank)
     b2.autotune(TUNE)
     b2.warmup(THERMALIZE - 10 * TUNE)
     b2.use_graphs(True)
@@ -179,9 +186,11 @@ def run_gpu(args):
             gs, ss, cn = b2.group_sums(gi)
             d2h += gs.nbytes + 16
     b2.sync()
-    t_e2e = time.perf_counter() - t0
+    t_e2e = shard.max_over_ranks(time.perf_counter() - t0)
     b2.close()
     e2e_value = nchains * (THERMALIZE + NCORR * args.steps) / t_e2e
+    if rank != 0:
+        return
     # plain one-chain drop-in form on the same model (beta=50 problem)
     single = E.Batch(model, [E.Group(probs[2]["beta"], probs[2]["ftau"], NTAU, nchains=1, seed0=0,
                                      taudiff_max=TDM, ncorr=NCORR, kcap=64, opcap=512)])
@@ -198,7 +207,7 @@ def run_gpu(args):
     bytes_per_launch = (wc["m_bytes"] + wc["op_bytes"]) / max(1, args.steps)
     achieved = bytes_per_launch / (ms / 1e3 / args.steps) / 1e9
     line = {
-        "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": 1,
+        "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (semicircular bath, seeded chains)",
@@ -309,12 +318,15 @@ def main():
         run_reference(args)
         return
     rank = int(os.environ.get("RANK", "0"))
-    if args.gpus > 1:
-        # independent replicas: each rank runs the same batch on its own GPU
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if world > 1:
+        # every rank runs its own chains (seeds offset by rank); the only
+        # exchange is the host-side max of the step times over a gloo group
         import torch
+        import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-    if rank == 0 or args.gpus == 1:
-        run_gpu(args)
+        dist.init_process_group("gloo")
+    run_gpu(args, rank, world)
 
 
 if __name__ == "__main__":

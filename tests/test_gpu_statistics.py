@@ -1,0 +1,104 @@
+"""Statistical checks of the GPU engine.
+
+1. G(tau), occupancies and double occupancies of a batch of GPU chains fall
+   within the statistical error of an oracle (CPU) run with the same total
+   number of samples but different seeds.
+2. Equal error at equal samples: the G(tau) error of a batch of n chains and
+   of one chain run n times longer agree, so MC updates/s of the two forms
+   compare at equal statistical error.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from w2dynamics_gb300 import engine as E
+from w2dynamics_gb300 import estimators as ES
+from w2dynamics_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+BETA, NTAU, NCORR, NCH, NMEAS, NWARM = 10.0, 20, 50, 16, 400, 3000
+
+
+def _occ(model_like, nd, dm, fock, evec):
+    est = ES.from_density_matrix(nd, fock, evec, dm)
+    return np.array([est["occ"][f // 2, f % 2, f // 2, f % 2] for f in range(2 * nd)]), est["occ"]
+
+
+def test_gpu_batch_agrees_with_cpu_run_within_errors():
+    pr = P.config_problem("dd3", beta=BETA)
+    nd = pr["nd"]
+    mg = E.Model(nd, pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    fk, evec = mg.basis()
+    b = E.Batch(mg, [E.Group(BETA, pr["ftau"], NTAU, nchains=NCH, seed0=1000, taudiff_max=5.0,
+                             ncorr=NCORR, kcap=64, opcap=512, p_outer=0.1, p_global=0.005,
+                             p_shift=0.005)])
+    b.warmup(NWARM)
+    b.measure(NMEAS)
+    b.sync()
+    gpu_g, gpu_n, gpu_d = [], [], []
+    for c in range(NCH):
+        r = b.results(c)
+        gpu_g.append(np.stack([r["gtau"][f // 2, f % 2] for f in range(2 * nd)]))
+        n, occ = _occ(mg, nd, r["densitymatrix"], fk, evec)
+        gpu_n.append(n)
+        gpu_d.append(occ[0, 0, 0, 1])  # double occupancy of orbital 1
+    mo = O.Model(nd, pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    ev = np.zeros((mo.nstates, mo.nstates))
+    for s in range(len(mo.sst_size)):
+        o, n_ = mo.sst_offset[s], mo.sst_size[s]
+        ev[o:o + n_, o:o + n_] = mo.evec(s)
+    cpu_g, cpu_n, cpu_d = [], [], []
+    for c in range(NCH):
+        co = O.Chain(mo, BETA, pr["ftau"], NTAU, seed=5000 + c, taudiff_max=5.0, ncorr=NCORR,
+                     p_outer=0.1, p_global=0.005, p_shift=0.005)
+        co.warmup(NWARM)
+        co.measure(NMEAS)
+        r = co.results()
+        cpu_g.append(r["gtau"])
+        n, occ = _occ(mo, nd, r["densitymatrix"], mo.fock_states, ev)
+        cpu_n.append(n)
+        cpu_d.append(occ[0, 0, 0, 1])
+
+    def z(a, b_):
+        a, b_ = np.asarray(a), np.asarray(b_)
+        se = np.sqrt(a.var(axis=0, ddof=1) / len(a) + b_.var(axis=0, ddof=1) / len(b_))
+        return (a.mean(axis=0) - b_.mean(axis=0)) / se
+
+    zg = z(gpu_g, cpu_g)
+    assert np.mean(np.abs(zg) < 2.0) > 0.85 and np.abs(zg).max() < 4.5, zg
+    zn = z(gpu_n, cpu_n)
+    assert np.abs(zn).max() < 4.0, zn
+    assert abs(z(gpu_d, cpu_d)) < 4.0
+
+
+def test_equal_error_batched_and_one_chain_forms():
+    pr = P.config_problem("dd3", beta=BETA)
+    nd = pr["nd"]
+    mg = E.Model(nd, pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    # outer-superstate, global and tau-shift moves make each chain ergodic
+    # over the superstate sectors (pair moves alone keep a chain in the
+    # sector it starts in)
+    moves = dict(p_outer=0.1, p_global=0.005, p_shift=0.005)
+    b = E.Batch(mg, [E.Group(BETA, pr["ftau"], NTAU, nchains=NCH, seed0=2000, taudiff_max=5.0,
+                             ncorr=NCORR, kcap=64, opcap=512, **moves)])
+    b.warmup(NWARM)
+    b.measure(NMEAS)
+    b.sync()
+    batched = np.array([b.results(c)["gtau"] for c in range(NCH)])
+    one = E.Batch(mg, [E.Group(BETA, pr["ftau"], NTAU, nchains=1, seed0=3000, taudiff_max=5.0,
+                               ncorr=NCORR, kcap=64, opcap=512, **moves)])
+    one.warmup(NWARM)
+    blocks = []
+    for _ in range(NCH):  # the same total samples, in NCH consecutive blocks
+        one.reset_measurements()
+        one.measure(NMEAS)
+        one.sync()
+        blocks.append(one.results(0)["gtau"])
+    blocks = np.array(blocks)
+    err_b = batched.std(axis=0, ddof=1) / np.sqrt(NCH)
+    err_1 = blocks.std(axis=0, ddof=1) / np.sqrt(NCH)
+    ratio = np.median(err_1 / err_b)
+    assert 0.5 < ratio < 2.0, ratio
+    zz = (batched.mean(axis=0) - blocks.mean(axis=0)) / np.sqrt(err_b ** 2 + err_1 ** 2)
+    assert np.abs(zz).max() < 4.5
