@@ -201,6 +201,46 @@ def test_measurement_parity(lib):
         assert np.allclose(xg[key], xo[key], rtol=1e-9, atol=1e-300), key
 
 
+@pytest.mark.parametrize("name,beta,dense,nprop", [("dd3", 10.0, True, 1500), ("kanamori5", 2.0, False, 200)])
+def test_dense_block_trace_and_density_matrix(lib, name, beta, dense, nprop):
+    """Dense-block models (block products with bin-edge checkpoints): the
+    proposal stream, G(tau) and the full density matrix (superstate blocks,
+    compared in the occupation basis) equal the oracle's."""
+    pr = P.config_problem(name, beta=beta)
+    q = pr["quantum_numbers"]
+    mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
+    co = O.Chain(mo, beta, pr["ftau"], 30, seed=31, taudiff_max=beta / 2, ncorr=20, p_outer=0.1,
+                 p_global=0.02, p_shift=0.02)
+    co.start_log(nprop + 20 * 30)
+    co.warmup(nprop)
+    co.measure(30)
+    ref = co.log()
+    mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
+    b = E.Batch(mg, [E.Group(beta, pr["ftau"], 30, nchains=1, seed0=31, taudiff_max=beta / 2, ncorr=20,
+                             p_outer=0.1, dense=dense, kcap=64, opcap=512, p_global=0.02,
+                             p_shift=0.02, tree_levels=3)])
+    b.set_log(nprop + 20 * 30)
+    b.warmup(nprop)
+    b.measure(30)
+    b.sync()
+    got = b.log(0)
+    F = pr["ftau"][0, 0]
+    compare_logs(ref, got, F, beta)
+    ro, rg = co.results(), b.results(0)
+    nf = 2 * pr["nd"]
+    gg = np.stack([rg["gtau"][f // 2, f % 2] for f in range(nf)])
+    assert np.allclose(gg, ro["gtau"], rtol=1e-9, atol=1e-12 * max(1.0, np.abs(ro["gtau"]).max()))
+    fk, ev_g = mg.basis()
+    ev_o = np.zeros_like(ev_g)
+    for s in range(len(mo.sst_size)):
+        o, n = mo.sst_offset[s], mo.sst_size[s]
+        ev_o[o:o + n, o:o + n] = mo.evec(s)
+    dm_g = ev_g @ rg["densitymatrix"] @ ev_g.T
+    dm_o = ev_o @ ro["densitymatrix"] @ ev_o.T
+    assert np.allclose(dm_g, dm_o, rtol=1e-8, atol=1e-10)
+    assert abs(np.trace(dm_g) - 1.0) < 1e-9
+
+
 def test_batched_chains_match_oracle_per_seed(lib):
     """Every chain of a batch is the reference chain of its own seed."""
     pr = P.config_problem("dd3", beta=10.0)

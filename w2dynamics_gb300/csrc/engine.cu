@@ -958,6 +958,259 @@ __device__ NOINL void dense_trace(Ctx& c, const Mod& md, int s0, double& lg, dou
 }
 
 // ---------------------------------------------------------------------------
+// Dense-block trace with checkpoints at the bin edges: the reference's
+// cached kets/bras with lazy extension (get_Trace_EB, Trace.F90:5354-5546,
+// and the R/L loops of get_Trace_EB_fullmatrix, Trace.F90:5734-6100), kept at
+// the 2^L + 1 time-bin edges.  Ket checkpoint j: every outer state
+// propagated from tau = 0 through the operators before edge j and evolved to
+// the edge; bra checkpoint j: from beta through the operators after edge j.
+// A pair move in bins b1 <= b2 needs kets up to b1 and bras from b2 + 1 and
+// recomputes only bins b1..b2; acceptance keeps those checkpoints.  Each
+// column (outer state) carries its own log scale.
+struct ChkHead {
+  int sst, rows, cols, pad;
+};
+__device__ __forceinline__ ChkHead* chk_head(const Ctx& c, int dir, int j) {
+  return (ChkHead*)(c.g->base + (size_t)c.chain * c.g->stride + c.g->o_chk +
+                    ((size_t)dir * ((1 << c.g->L) + 1) + j) * c.g->chk_bytes);
+}
+__device__ __forceinline__ double* chk_lg(ChkHead* p) { return (double*)(p + 1); }
+__device__ __forceinline__ double* chk_v(const Ctx& c, ChkHead* p) { return chk_lg(p) + c.m->nsmax; }
+
+__device__ __forceinline__ double* dwork(const Ctx& c, int i) {
+  const size_t n2 = (size_t)c.m->nsmax * c.m->nsmax;
+  return i < 2 ? c.dense + i * n2 : c.dense + 2 * n2 + (size_t)(i - 2) * c.m->nsmax;
+}
+// column-wise split_log (Trace.F90:5341-5348): scale each column to max 1
+__device__ void col_split(Ctx& c, int rows, int cols, double* v, double* lg) {
+  const int ld = c.m->nsmax;
+  for (int col = c.lane; col < cols; col += 32) {
+    double mx = 0.0;
+    for (int i = 0; i < rows; ++i) mx = fmax(mx, fabs(v[(size_t)col * ld + i]));
+    if (mx > 0.0) {
+      const double inv = 1.0 / mx;
+      for (int i = 0; i < rows; ++i) v[(size_t)col * ld + i] *= inv;
+    }
+    lg[col] += log(mx);
+  }
+  __syncwarp();
+}
+// exp(-(E - E0) dt) on the rows of superstate sst, E0 - Egs into the logs
+__device__ void col_evolve(Ctx& c, int sst, int rows, int cols, double* v, double* lg, double dt) {
+  const DModel& m = *c.m;
+  const int ld = m.nsmax;
+  const double* E = m.eval + m.sst_off[sst];
+  const double e0 = E[0];
+  if (rows > 1) {
+    double* fac = dwork(c, 3);  // one exponential per row, shared by the columns
+    for (int i = c.lane; i < rows; i += 32) fac[i] = exp(-(E[i] - e0) * dt);
+    __syncwarp();
+    for (int e = c.lane; e < rows * cols; e += 32) {
+      const int i = e % rows, col = e / rows;
+      v[(size_t)col * ld + i] *= fac[i];
+    }
+  }
+  for (int col = c.lane; col < cols; col += 32) lg[col] += -(e0 - m.egs) * dt;
+  __syncwarp();
+  if (rows > 1) col_split(c, rows, cols, v, lg);
+}
+// One operator: evolve by dt in superstate *sst, apply the block of
+// (code, ca-flip for bras) into `out`, split.  Returns false when the
+// superstate sequence breaks.
+__device__ bool col_step(Ctx& c, int& sst, int& rows, int cols, double*& v, double*& out, double* lg, int code,
+                         bool bra, double dt) {
+  const DModel& m = *c.m;
+  const int ld = m.nsmax;
+  const int f = code >> 1, ca = bra ? 1 - (code & 1) : (code & 1);
+  const int nxt = m.connect[((size_t)sst * m.nf + f) * 2 + ca];
+  if (nxt < 0) return false;
+  col_evolve(c, sst, rows, cols, v, lg, dt);
+  const int nn = m.sst_n[nxt];
+  const double* B = m.blk + m.blk_off[((size_t)sst * m.nf + f) * 2 + ca];
+  for (int e = c.lane; e < nn * cols; e += 32) {
+    const int i = e % nn, col = e / nn;
+    double acc = 0.0;
+    for (int r = 0; r < rows; ++r) acc = fma(B[(size_t)r * nn + i], v[(size_t)col * ld + r], acc);
+    out[(size_t)col * ld + i] = acc;
+  }
+  __syncwarp();
+  if (nn > 1 || rows > 1) col_split(c, nn, cols, out, lg);
+  double* t = v;
+  v = out;
+  out = t;
+  sst = nxt;
+  rows = nn;
+  return true;
+}
+__device__ void chk_load(Ctx& c, ChkHead* h, int& sst, int& rows, int& cols, double* v, double* lg) {
+  sst = h->sst;
+  rows = h->rows;
+  cols = h->cols;
+  const int ld = c.m->nsmax;
+  const double* src = chk_v(c, h);
+  for (int e = c.lane; e < rows * cols; e += 32) v[(size_t)(e / rows) * ld + e % rows] = src[(size_t)(e / rows) * ld + e % rows];
+  for (int col = c.lane; col < cols; col += 32) lg[col] = chk_lg(h)[col];
+  __syncwarp();
+}
+__device__ void chk_store(Ctx& c, ChkHead* h, int sst, int rows, int cols, const double* v, const double* lg) {
+  const int ld = c.m->nsmax;
+  double* dst = chk_v(c, h);
+  for (int e = c.lane; e < rows * cols; e += 32) dst[(size_t)(e / rows) * ld + e % rows] = v[(size_t)(e / rows) * ld + e % rows];
+  for (int col = c.lane; col < cols; col += 32) chk_lg(h)[col] = lg[col];
+  if (c.lane == 0) {
+    h->sst = sst;
+    h->rows = rows;
+    h->cols = cols;
+  }
+  __syncwarp();
+}
+__device__ void chk_identity(Ctx& c, ChkHead* h, int s0) {
+  const int ld = c.m->nsmax, n0 = c.m->sst_n[s0];
+  double* dst = chk_v(c, h);
+  for (int e = c.lane; e < n0 * n0; e += 32) dst[(size_t)(e / n0) * ld + e % n0] = (e / n0 == e % n0) ? 1.0 : 0.0;
+  for (int col = c.lane; col < n0; col += 32) chk_lg(h)[col] = 0.0;
+  if (c.lane == 0) {
+    h->sst = s0;
+    h->rows = n0;
+    h->cols = n0;
+  }
+  __syncwarp();
+}
+// Kets valid up to edge `upto` (current configuration).
+__device__ NOINL bool ensure_kets(Ctx& c, int upto) {
+  Hdr& h = *c.h;
+  if (h.kv < 0) {
+    chk_identity(c, chk_head(c, 0, 0), h.outer_sst);
+    if (c.lane == 0) h.kv = 0;
+    __syncwarp();
+  }
+  double *v = dwork(c, 0), *o = dwork(c, 1), *lg = dwork(c, 2);
+  while (h.kv < upto) {
+    const int j = h.kv;
+    int sst, rows, cols;
+    chk_load(c, chk_head(c, 0, j), sst, rows, cols, v, lg);
+    double t = bin_edge(c, j);
+    for (int i = c.bstart[j]; i < c.bstart[j + 1]; ++i) {
+      const double tau = c.optau[i];
+      if (!col_step(c, sst, rows, cols, v, o, lg, c.opcode[i], false, tau - t)) return false;
+      t = tau;
+    }
+    col_evolve(c, sst, rows, cols, v, lg, bin_edge(c, j + 1) - t);
+    chk_store(c, chk_head(c, 0, j + 1), sst, rows, cols, v, lg);
+    if (c.lane == 0) h.kv = j + 1;
+    __syncwarp();
+  }
+  return true;
+}
+// Bras valid from edge `from` (current configuration).
+__device__ NOINL bool ensure_bras(Ctx& c, int from) {
+  Hdr& h = *c.h;
+  const int nb = 1 << c.g->L;
+  if (h.bv > nb) {
+    chk_identity(c, chk_head(c, 1, nb), h.outer_sst);
+    if (c.lane == 0) h.bv = nb;
+    __syncwarp();
+  }
+  double *v = dwork(c, 0), *o = dwork(c, 1), *lg = dwork(c, 2);
+  while (h.bv > from) {
+    const int j = h.bv;
+    int sst, rows, cols;
+    chk_load(c, chk_head(c, 1, j), sst, rows, cols, v, lg);
+    double t = bin_edge(c, j);
+    for (int i = c.bstart[j] - 1; i >= c.bstart[j - 1]; --i) {
+      const double tau = c.optau[i];
+      if (!col_step(c, sst, rows, cols, v, o, lg, c.opcode[i], true, t - tau)) return false;
+      t = tau;
+    }
+    col_evolve(c, sst, rows, cols, v, lg, t - bin_edge(c, j - 1));
+    chk_store(c, chk_head(c, 1, j - 1), sst, rows, cols, v, lg);
+    if (c.lane == 0) h.bv = j - 1;
+    __syncwarp();
+  }
+  return true;
+}
+// <bra|ket> per column at one edge, summed over the outer states in log
+// form (addLogTr, Trace.F90:298-309).
+__device__ void chk_close(Ctx& c, int sst, int rows, int cols, const double* v, const double* lg, ChkHead* bh,
+                          double& out_lg, double& out_sg) {
+  out_lg = -DHUGE;
+  out_sg = 0.0;
+  if (bh->sst != sst) return;
+  const int ld = c.m->nsmax;
+  const double* bv = chk_v(c, bh);
+  const double* blg = chk_lg(bh);
+  for (int col = 0; col < cols; ++col) {
+    double part = 0.0;
+    for (int i = c.lane; i < rows; i += 32) part = fma(v[(size_t)col * ld + i], bv[(size_t)col * ld + i], part);
+    const double bk = wsum(part);
+    if (bk == 0.0) continue;
+    const double l = lg[col] + blg[col] + log(fabs(bk));
+    const double sg = bk >= 0.0 ? 1.0 : -1.0;
+    if (out_sg == 0.0) {
+      out_lg = l;
+      out_sg = sg;
+    } else if (out_lg >= l) {
+      out_lg = out_lg + log(1.0 + out_sg * sg * exp(l - out_lg));
+    } else {
+      const double nl = l + log(1.0 + out_sg * sg * exp(out_lg - l));
+      out_lg = nl;
+      out_sg = sg;
+    }
+  }
+}
+// Trace of a proposed pair move for the current outer superstate from the
+// checkpoints: kets at edge b1, the proposed operators of bins b1..b2 (the
+// gathered leaves for b1/b2, the current lists in between), bras at b2 + 1.
+__device__ NOINL void chk_trace(Ctx& c, const Mod& md, double& out_lg, double& out_sg) {
+  out_lg = -DHUGE;
+  out_sg = 0.0;
+  const int b1 = md.b1, b2 = md.b2;
+  if (!ensure_kets(c, b1) || !ensure_bras(c, b2 + 1)) {
+    set_status(c, ST_INTERNAL);
+    return;
+  }
+  double *v = dwork(c, 0), *o = dwork(c, 1), *lg = dwork(c, 2);
+  int sst, rows, cols;
+  chk_load(c, chk_head(c, 0, b1), sst, rows, cols, v, lg);
+  double t = bin_edge(c, b1);
+  for (int b = b1; b <= b2; ++b) {
+    const bool gathered = b == b1 || b == b2;
+    const int buf = b == b1 ? 0 : 1;
+    const int n = !gathered ? c.bstart[b + 1] - c.bstart[b] : (buf == 0 ? md.n1 : md.n2);
+    for (int q = 0; q < n; ++q) {
+      const double tau = gathered ? c.btau[buf][q] : c.optau[c.bstart[b] + q];
+      const int code = gathered ? c.bcode[buf][q] : c.opcode[c.bstart[b] + q];
+      if (!col_step(c, sst, rows, cols, v, o, lg, code, false, tau - t)) return;
+      t = tau;
+    }
+    col_evolve(c, sst, rows, cols, v, lg, bin_edge(c, b + 1) - t);
+    t = bin_edge(c, b + 1);
+  }
+  chk_close(c, sst, rows, cols, v, lg, chk_head(c, 1, b2 + 1), out_lg, out_sg);
+}
+__device__ __forceinline__ void chk_invalidate(Ctx& c) {
+  if (c.lane == 0) {
+    c.h->kv = -1;
+    c.h->bv = (1 << c.g->L) + 1;
+  }
+  __syncwarp();
+}
+// After an accepted pair move in bins md.b1..md.b2: checkpoints outside the
+// changed bins stay valid unless the outer superstate changed.
+__device__ __forceinline__ void chk_keep(Ctx& c, const Mod& md, int new_outer) {
+  if (!c.g->o_chk) return;
+  if (new_outer != c.h->outer_sst) {
+    chk_invalidate(c);
+    return;
+  }
+  if (c.lane == 0) {
+    if (c.h->kv > md.b1) c.h->kv = md.b1;
+    if (c.h->bv < md.b2 + 1) c.h->bv = md.b2 + 1;
+  }
+  __syncwarp();
+}
+
+// ---------------------------------------------------------------------------
 // Shifts of the sorted arrays
 
 // insert value/slot at position p of a sorted array with n entries
@@ -1069,8 +1322,10 @@ __device__ NOINL void write_record(Ctx& c, const cthyb_record& r) {
 __device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum) {
   if (c.mono) {
     root_trace(c, 1 - c.act[1], s0, mx, sum);  // state tree rebuilt after the QN check
+  } else if (s0 == c.h->outer_sst && c.g->o_chk) {
+    chk_trace(c, md, mx, sum);  // log|trace| and its sign from the checkpoints
   } else {
-    dense_trace(c, md, s0, mx, sum);  // log|trace| and its sign
+    dense_trace(c, md, s0, mx, sum);  // new outer superstate: from scratch
   }
 }
 
@@ -1524,6 +1779,7 @@ __device__ NOINL void ph_accept_add(Ctx& c, Prop& p) {
   ops_insert2(c, p.p1, p.p2, md.t1, md.c1, md.t2, md.c2);
   bstart_shift(c, md.b1, md.b2, +1);
   tree_accept(c, md);
+  chk_keep(c, md, p.snew);
   if (c.lane == 0) {
     h.k[f] = k + 1;
     h.K = K + 2;
@@ -1592,6 +1848,7 @@ __device__ NOINL void ph_accept_rem(Ctx& c, Prop& p) {
   ops_remove2(c, p.ix, p.iy);
   bstart_shift(c, md.b1, md.b2, -1);
   tree_accept(c, md);
+  chk_keep(c, md, p.snew);
   const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
   if (c.lane == 0) {
     h.k[f] = k - 1;
@@ -2005,6 +2262,7 @@ __device__ NOINL void ph_global(Ctx& c, Prop& p) {
     }
     __syncwarp();
     tree_flip_all(c);
+    if (c.g->o_chk) chk_invalidate(c);
     if (c.lane == 0) {
       for (int f = 0; f < m.nf; ++f) h.k[f] = knew[f];
       h.det_log = dlog;
@@ -2066,6 +2324,7 @@ __device__ NOINL void ph_change_outer(Ctx& c, Prop& p) {
     h.trace_sign = sg;
   }
   __syncwarp();
+  if (c.g->o_chk) chk_invalidate(c);
   const double sgn = config_sign(c);
   if (c.lane == 0) h.cfgsign = -sgn;
   r.outcome = 4;
@@ -2179,6 +2438,7 @@ __device__ NOINL void ph_shift(Ctx& c, Prop& p) {
       if ((k & 1) && ((w[0] + w[1]) & 1)) detrat = -detrat;
     }
     tree_flip_all(c);
+    if (c.g->o_chk) chk_invalidate(c);
     if (c.lane == 0) {
       h.trace_log = tr_lg;
       h.trace_sign = tr_sg;
@@ -2311,6 +2571,33 @@ __device__ NOINL void measure(Ctx& c) {
       oh[2 * m.nss + s0] += csum;
     }
     __syncwarp();
+  }
+  // MeasDensityMatrix_beta_half for dense-block models: kets and bras at the
+  // middle edge (beta/2), rho(s1, s2) += bra(s1) ket(s2) / trace per outer
+  // state (CTQMC.F90:3088-3150)
+  if (g.meas_dm && !c.mono && g.o_chk) {
+    const int mid = 1 << (g.L - 1);
+    if (ensure_kets(c, mid) && ensure_bras(c, mid)) {
+      ChkHead* kh = chk_head(c, 0, mid);
+      ChkHead* bh = chk_head(c, 1, mid);
+      if (kh->sst == bh->sst) {
+        const int sst = kh->sst, n = kh->rows, cols = kh->cols, ld = m.nsmax;
+        const double* kv = chk_v(c, kh);
+        const double* bv = chk_v(c, bh);
+        const double* klg = chk_lg(kh);
+        const double* blg = chk_lg(bh);
+        double* D = c.dm + m.dm_off[sst];
+        const double sgn = h.trace_sign * (-h.cfgsign);
+        for (int e = c.lane; e < n * n; e += 32) {
+          const int s1 = e % n, s2 = e / n;
+          double acc = 0.0;
+          for (int col = 0; col < cols; ++col)
+            acc += bv[(size_t)col * ld + s1] * kv[(size_t)col * ld + s2] * exp(klg[col] + blg[col] - h.trace_log);
+          D[(size_t)s2 * n + s1] += acc * sgn;
+        }
+        __syncwarp();
+      }
+    }
   }
   // MeasGtauRem(.false.): M elements binned by tau_a - tau_c, and their
   // Legendre coefficients (CTQMC.F90:2252-2440)
@@ -2476,6 +2763,7 @@ __global__ void __launch_bounds__(WPB * 32) k_init(const __grid_constant__ DMode
   if (c.lane == 0) h.K = 0;
   __syncwarp();
   tree_build_all(c);
+  chk_invalidate(c);
   double lg, sg;
   if (c.mono) {
     double mx, sum;
@@ -2744,6 +3032,7 @@ __global__ void __launch_bounds__(WPB * 32) k_set_config(const __grid_constant__
   if (c.lane == 0) h.outer_sst = outer_sst;
   __syncwarp();
   tree_build_all(c);
+  chk_invalidate(c);
   double lg, sg;
   if (c.mono) {
     double mx, sum;
@@ -3112,19 +3401,26 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   off = align_up(off + (size_t)nf * d.ntau * 8, 256);
   g.o_histo = off;
   off = align_up(off + (size_t)nf * g.maxhisto * 8, 256);
-  g.o_dm = off;
-  off = align_up(off + (size_t)hm.ns * 8, 256);
+  g.o_dm = off;  // diagonal (monomial models) or the superstate blocks of rho
+  off = align_up(off + (size_t)(mono ? hm.ns : hm.dm_size) * 8, 256);
   g.nleg = d.nleg > 0 ? d.nleg : 0;
   g.o_gleg = off;
   off = align_up(off + (size_t)nf * g.nleg * 8, 256);
   g.o_outer = off;  // outer superstate/state histograms, signs, trace contributions
   off = align_up(off + (size_t)3 * (hm.nss + hm.ns) * 8, 256);
   g.o_dense = off;
-  size_t dense = std::max((size_t)2 * hm.nsmax * hm.nsmax, (size_t)2 * kcap * kcap) * 8;
+  size_t dense = std::max((size_t)2 * hm.nsmax * hm.nsmax + 2 * hm.nsmax, (size_t)2 * kcap * kcap) * 8;
   off = align_up(off + dense, 256);
   g.o_log = off;
   g.logcap = logcap;
   off = align_up(off + (size_t)logcap * sizeof(cthyb_record), 256);
+  g.o_chk = 0;
+  g.chk_bytes = 0;
+  if (!mono) {
+    g.chk_bytes = align_up(16 + (size_t)8 * hm.nsmax + (size_t)8 * hm.nsmax * hm.nsmax, 16);
+    g.o_chk = off;
+    off = align_up(off + (size_t)2 * ((1u << L) + 1) * g.chk_bytes, 256);
+  }
   g.o_glscr = 0;
   if (g.nleg > 0) {
     g.o_glscr = off;
@@ -3562,11 +3858,21 @@ int cthyb_batch_results(cthyb_batch_t B, int chain, double* gtau, double* mean_s
     }
   }
   if (dmat) {
-    std::vector<double> d(hm.ns);
+    const bool blocks = G->g.o_chk != 0;
+    std::vector<double> d(blocks ? hm.dm_size : hm.ns);
     CK(cudaMemcpy(d.data(), base + G->g.o_dm, d.size() * 8, cudaMemcpyDeviceToHost));
     double zs = h.cnt_meas ? -1.0 / ((double)h.cnt_meas * ms) : 0.0;
     std::memset(dmat, 0, sizeof(double) * (size_t)hm.ns * hm.ns);
-    for (int i = 0; i < hm.ns; ++i) dmat[(size_t)i * hm.ns + i] = d[i] * zs;
+    if (!blocks) {
+      for (int i = 0; i < hm.ns; ++i) dmat[(size_t)i * hm.ns + i] = d[i] * zs;
+    } else {
+      for (int sst = 0; sst < hm.nss; ++sst) {
+        const int n = hm.sst_n[sst], o = hm.sst_off[sst];
+        for (int s2 = 0; s2 < n; ++s2)
+          for (int s1 = 0; s1 < n; ++s1)
+            dmat[(size_t)(o + s2) * hm.ns + (o + s1)] = d[hm.dm_off[sst] + (size_t)s2 * n + s1] * zs;
+      }
+    }
   }
   if (histo) {
     const int hmx = G->g.maxhisto;

@@ -46,6 +46,7 @@ struct Hdr {
   double meas_sign;
   int num_windows, window_position, npairs, outer_sst;
   int K, mt_idx, status, nslide;
+  int kv, bv;  // dense-block models: ket checkpoints 0..kv and bra checkpoints bv..2^L are valid
   long long nprop, try_add, acc_add, try_rem, acc_rem, qn_add, qn_rem, cnt_meas, logn;
   long long try_glob, acc_glob, qn_glob, try_shift, acc_shift;
   int k[NFMAX];
@@ -68,7 +69,9 @@ struct DGroup {
   size_t stride;
   size_t o_hdr, o_mt, o_optau, o_opcode, o_srt_tau, o_srt_slot, o_slot_tau, o_M, o_tree, o_act, o_bstart,
       o_scr, o_gtau, o_histo, o_dm, o_gleg, o_outer, o_dense, o_log, o_glob,  // o_glob: 0 without global/shift moves
-      o_glscr;  // per-lane Legendre partial sums (0 when nleg == 0)
+      o_glscr,  // per-lane Legendre partial sums (0 when nleg == 0)
+      o_chk;    // dense-block models: ket and bra checkpoints at the 2^L + 1 bin edges
+  size_t chk_bytes;  // bytes of one checkpoint
   size_t node_bytes;   // bytes of one node slot
   long long logcap;
   const double* empty_w;  // [nss] normalised empty-trace weights
