@@ -147,6 +147,22 @@ int cthyb_batch_results_extra(cthyb_batch_t batch, int chain, double* gleg, doub
                               double* outer_state_histo, double* sign_sst, double* sign_state,
                               double* contrib_sst, double* contrib_state);
 
+/* Per-configuration gradients of log|w| = log|det H| + log|trace| of every
+ * chain's current configuration (no reference counterpart: the reference
+ * has no derivatives).
+ *   grad_delta  (nchains, Nd, 2, Nftau), each chain Fortran order:
+ *               d log|det H| / d F(b, s, tau_j), F entering H through the
+ *               linear interpolation of get_HybrF (Trace.F90:1014-1033);
+ *   grad_params (nchains, nparams): d log|trace| / d theta_p for parameter
+ *               directions given by per-eigenstate energy derivatives
+ *               dE (nparams x nstates, row-major, p slowest) -- monomial
+ *               (density-density) models only, nparams <= 32;
+ *   log_weights (nchains, 2): log|det H| and the absolute log|trace|
+ *               (energies not shifted by the ground-state energy).
+ * grad_params/dE may be NULL with nparams = 0. */
+int cthyb_batch_gradients(cthyb_batch_t batch, int nparams, const double* dE, double* grad_delta,
+                          double* grad_params, double* log_weights);
+
 /* Global and tau-shift move counters of one chain since the last warmup or
  * measure call: TryGlob, AccGlob, AccQNGlob, TryShift, AccShift
  * (CTQMC.F90:134-136). */

@@ -2956,6 +2956,99 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
   }
 }
 
+// Gradients of log|w| of each chain's current configuration (no reference
+// counterpart).  Determinant part: d log|det H| / dH(a, c) = M(c, a), and
+// H(a, c) = Delta_f(tau_a - tau_c) interpolates the grid linearly
+// (get_HybrF, Trace.F90:1014-1033), so M(c, a) * sign * (1 - frac) goes to
+// grid point i and M(c, a) * sign * frac to i + 1.  Trace part (monomial
+// models): each surviving outer state's log weight is minus the sum over
+// segments of E(state) * length; along a parameter direction with per-state
+// energy derivatives dE it changes by the same sum with dE, and d log|tr| is
+// the average of those over the states weighted by their signed
+// contributions.  One warp per chain; the walk is O(K) per state.
+constexpr int NPARMAX = 32;
+__global__ void __launch_bounds__(WPB * 32) k_grad(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
+                                                  const double* __restrict__ dE, int npar, double* gdelta,
+                                                  double* gpar, double* logw) {
+  __shared__ Hdr hs[WPB];
+  const int warp = threadIdx.x >> 5;
+  const int chain = blockIdx.x * WPB + warp;
+  if (chain >= g.nchains) return;
+  Ctx c = make_ctx(&m, &g, &hs[warp], chain);
+  load_hdr(c.h, (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr), c.lane);
+  Hdr& h = *c.h;
+  const int nft = g.nftau;
+  double* gd = gdelta + (size_t)chain * m.nf * nft;
+  for (int f = 0; f < m.nf; ++f) {
+    const int k = h.k[f];
+    const double* Mf = M_ptr(c, f);
+    const double* tcs = stau_ptr(c, f, 0);
+    const double* tas = stau_ptr(c, f, 1);
+    for (int e = c.lane; e < k * k; e += 32) {
+      const int sc = e % k, sa = e / k;
+      const double Mv = Mf[(size_t)sa * c.kcap + sc];
+      double dt = tas[sa] - tcs[sc], sig = 1.0;
+      if (dt < 0.0) {
+        dt = dt + g.beta;
+        sig = -1.0;
+      }
+      const double n = dt / g.beta * (double)(nft - 1);
+      int i = (int)n;
+      const double fr = n - (double)(int)n;
+      if (i > nft - 2) i = nft - 2;
+      atomicAdd(&gd[(size_t)f * nft + i], Mv * sig * (1.0 - fr));
+      atomicAdd(&gd[(size_t)f * nft + i + 1], Mv * sig * fr);
+    }
+  }
+  __syncwarp();
+  if (c.lane == 0) logw[2 * (size_t)chain] = h.det_log;
+  if (!c.mono || npar <= 0) return;
+  const int s0 = h.outer_sst, off = m.sst_off[s0], n0 = m.sst_n[s0], K = h.K;
+  double mx = -DHUGE, S = 0.0, D[NPARMAX];
+  for (int p = 0; p < npar; ++p) D[p] = 0.0;
+  for (int q = c.lane; q < n0; q += 32) {
+    int cur = off + q, neg = 0;
+    double l = 0.0, dl[NPARMAX], t = 0.0;
+    for (int p = 0; p < npar; ++p) dl[p] = 0.0;
+    for (int j = 0; j < K && cur >= 0; ++j) {
+      const double tau = c.optau[j], dt = tau - t;
+      l -= m.evs[cur] * dt;
+      for (int p = 0; p < npar; ++p) dl[p] -= dE[(size_t)p * m.ns + cur] * dt;
+      const size_t idx = (size_t)c.opcode[j] * m.ns + cur;
+      const int nx = m.mono_tgt[idx];
+      if (nx >= 0) {
+        l += m.mono_lv[idx];
+        neg ^= m.mono_neg[idx];
+      }
+      cur = nx;
+      t = tau;
+    }
+    if (cur != off + q) continue;
+    const double dt = g.beta - t;
+    l -= m.evs[cur] * dt;
+    for (int p = 0; p < npar; ++p) dl[p] -= dE[(size_t)p * m.ns + cur] * dt;
+    const double sg = neg ? -1.0 : 1.0;
+    if (l > mx) {  // rescale the running sums to the new maximum
+      const double r = mx == -DHUGE ? 0.0 : exp(mx - l);
+      S *= r;
+      for (int p = 0; p < npar; ++p) D[p] *= r;
+      mx = l;
+    }
+    const double w = sg * exp(l - mx);
+    S += w;
+    for (int p = 0; p < npar; ++p) D[p] += w * dl[p];
+  }
+  const double gmx = wmax(mx);
+  const double r = mx == -DHUGE ? 0.0 : exp(mx - gmx);
+  S = wsum(S * r);
+  for (int p = 0; p < npar; ++p) {
+    const double v = wsum(D[p] * r);
+    if (c.lane == 0) gpar[(size_t)chain * npar + p] = v / S;
+  }
+  // absolute log|trace| (the stored trace is relative to exp(-beta Egs))
+  if (c.lane == 0) logw[2 * (size_t)chain + 1] = gmx + log(fabs(S)) - g.beta * m.egs;
+}
+
 // set_mc_config: operator arrays from a time-ordered list already written
 // into optau/opcode by the host (K in the header); rebuilds the sorted
 // arrays, the tree, the trace, and the inverse hybridisation matrices by
@@ -4018,6 +4111,62 @@ int cthyb_batch_minv(cthyb_batch_t B, int chain, int f, int* kout, double* out) 
   return CTHYB_OK;
 }
 
+int cthyb_batch_gradients(cthyb_batch_t B, int nparams, const double* dE, double* grad_delta, double* grad_params,
+                          double* log_weights) {
+  if (!B || nparams < 0 || nparams > NPARMAX || (nparams > 0 && (!dE || !grad_params)))
+    return fail(CTHYB_ERR_ARG, "bad arguments (nparams must be 0..32)");
+  const HostModel& hm = B->model->hm;
+  if (nparams > 0)
+    for (GroupHost& G : B->groups)
+      if (G.g.o_chk) return fail(CTHYB_ERR_UNSUPPORTED, "trace gradients need a monomial (density-density) model");
+  CK(cudaStreamSynchronize(B->stream));
+  double* d_dE = nullptr;
+  if (nparams > 0) {
+    CK(cudaMalloc(&d_dE, sizeof(double) * (size_t)nparams * hm.ns));
+    CK(cudaMemcpy(d_dE, dE, sizeof(double) * (size_t)nparams * hm.ns, cudaMemcpyHostToDevice));
+  }
+  int rc = CTHYB_OK;
+  for (GroupHost& G : B->groups) {
+    const int n = G.desc.nchains, nft = G.g.nftau, nf = hm.nf;
+    double *gd = nullptr, *gp = nullptr, *lw = nullptr;
+    cudaError_t e = cudaMalloc(&gd, sizeof(double) * (size_t)n * nf * nft);
+    if (e == cudaSuccess) e = cudaMalloc(&gp, sizeof(double) * (size_t)n * std::max(nparams, 1));
+    if (e == cudaSuccess) e = cudaMalloc(&lw, sizeof(double) * (size_t)n * 2);
+    if (e == cudaSuccess) e = cudaMemsetAsync(gd, 0, sizeof(double) * (size_t)n * nf * nft, B->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(lw, 0, sizeof(double) * (size_t)n * 2, B->stream);
+    if (e == cudaSuccess) {
+      k_grad<<<(n + WPB - 1) / WPB, WPB * 32, 0, B->stream>>>(B->model->dm, G.g, d_dE, nparams, gd, gp, lw);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+    if (e == cudaSuccess) {
+      std::vector<double> h((size_t)n * nf * nft);
+      e = cudaMemcpy(h.data(), gd, h.size() * 8, cudaMemcpyDeviceToHost);
+      // per chain (Nd, 2, Nftau) Fortran order
+      if (e == cudaSuccess && grad_delta)
+        for (int ch = 0; ch < n; ++ch)
+          for (int f = 0; f < nf; ++f)
+            for (int j = 0; j < nft; ++j)
+              grad_delta[(size_t)(G.chain0 + ch) * nf * nft + (f / 2) + hm.nd * ((f % 2) + 2 * (size_t)j)] =
+                  h[((size_t)ch * nf + f) * nft + j];
+    }
+    if (e == cudaSuccess && nparams > 0)
+      e = cudaMemcpy(grad_params + (size_t)G.chain0 * nparams, gp, sizeof(double) * (size_t)n * nparams,
+                     cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && log_weights)
+      e = cudaMemcpy(log_weights + (size_t)G.chain0 * 2, lw, sizeof(double) * (size_t)n * 2, cudaMemcpyDeviceToHost);
+    cudaFree(gd);
+    cudaFree(gp);
+    cudaFree(lw);
+    if (e != cudaSuccess) {
+      rc = fail(CTHYB_ERR_CUDA, std::string("gradients: ") + cudaGetErrorString(e));
+      break;
+    }
+  }
+  if (d_dE) cudaFree(d_dE);
+  return rc;
+}
+
 int cthyb_batch_refresh_minv(cthyb_batch_t B, int replace, double* maxdev) {
   if (!B) return fail(CTHYB_ERR_ARG, "null");
   CK(cudaMemsetAsync(B->d_dev, 0, sizeof(double), B->stream));
@@ -4071,6 +4220,8 @@ int cthyb_batch_set_log(cthyb_batch_t B, int64_t cap) {
       Hdr h;
       CK(cudaMemcpy(&h, nb + (size_t)c * G.g.stride + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost));
       h.logn = 0;
+      h.kv = -1;  // regions after the log (checkpoints, scratch) start empty
+      h.bv = (1 << G.g.L) + 1;
       CK(cudaMemcpy(nb + (size_t)c * G.g.stride + G.g.o_hdr, &h, sizeof(Hdr), cudaMemcpyHostToDevice));
     }
   }

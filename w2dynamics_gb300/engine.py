@@ -29,7 +29,7 @@ EXPORTS = (
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
     "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_autotune", "cthyb_batch_results",
-    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_results_extra", "cthyb_batch_state", "cthyb_batch_get_config",
+    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
     "cthyb_minv_rebuild_noalloc",
@@ -91,6 +91,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_results.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_move_counters.argtypes = [vp, C.c_int, C.POINTER(i64)]
     L.cthyb_batch_results_extra.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp]
+    L.cthyb_batch_gradients.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.cthyb_batch_group_sums.argtypes = [vp, C.c_int, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_state.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_get_config.argtypes = [vp, C.c_int, ip, dp, ip, ip, ip, ip]
@@ -288,6 +289,25 @@ class Batch:
         out = dict(zip(keys, arrs))
         out["gleg"] = gl[:nd * 2 * g.nleg].reshape((nd, 2, g.nleg), order="F")
         return out
+
+    def gradients(self, dE=None):
+        """d log|w| of every chain's current configuration: grad_delta
+        (nchains, Nd, 2, Nftau) w.r.t. the F(tau) grid, grad_params
+        (nchains, nparams) along the parameter directions dE (nparams,
+        nstates), log_weights (nchains, 2) = (log|det|, log|trace|)."""
+        nd = self.model.nd
+        nft = self.groups[0].ftau.shape[2]
+        if any(g.ftau.shape[2] != nft for g in self.groups):
+            raise ValueError("gradients need one Nftau for all groups")
+        npar = 0 if dE is None else int(np.asarray(dE).shape[0])
+        dEc = None if dE is None else np.ascontiguousarray(dE, np.float64)
+        gd = np.zeros((self.nchains, nd * 2 * nft))
+        gp = np.zeros((self.nchains, max(npar, 1)))
+        lw = np.zeros((self.nchains, 2))
+        _check(load().cthyb_batch_gradients(self.h, npar, _dp(dEc) if dEc is not None else None, _dp(gd),
+                                            _dp(gp), _dp(lw)))
+        gd = gd.reshape((self.nchains, nft, 2, nd)).transpose(0, 3, 2, 1)
+        return gd, gp[:, :npar], lw
 
     def move_counters(self, chain):
         """Global and tau-shift move counters since the last warmup/measure call."""
