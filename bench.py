@@ -129,6 +129,50 @@ def build_batch(E, probs, cpb, rank=0):
     return model, groups, E.Batch(model, groups), h2d
 
 
+def measure_backward(E, model, pr, args):
+    """The differentiation configuration: 2048 chains of the same model at
+    beta = 50; one forward step (NCorr proposals + measurement) against one
+    backward pass (d log|w| of every chain w.r.t. the F(tau) grid and the
+    2Nd + 2 parameters eps_f, U, J), both device-timed with CUDA events on the
+    batch's stream."""
+    import torch
+    from w2dynamics_gb300 import gradients as GR
+    n = 2048
+    b = E.Batch(model, [E.Group(pr["beta"], pr["ftau"], pr["ntau"], nchains=n, seed0=0, taudiff_max=TDM,
+                                ncorr=NCORR, kcap=64, opcap=512)])
+    b.autotune(TUNE)
+    b.warmup(THERMALIZE - 10 * TUNE)
+    b.sync()
+    dev = torch.device("cuda")
+    dE = torch.tensor(GR.density_density_directions(model.nd, model.fock_states), dtype=torch.float64, device=dev)
+    nf, nft = 2 * model.nd, pr["ftau"].shape[2]
+    gd = torch.empty((n, nf, nft), dtype=torch.float64, device=dev)
+    gp = torch.empty((n, dE.shape[0]), dtype=torch.float64, device=dev)
+    lw = torch.empty((n, 2), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()  # dE copied on torch's stream before the batch's stream reads it
+    stream = torch.cuda.ExternalStream(b.stream())
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    reps = max(3, args.steps // 4)
+    for _ in range(2):  # warm-up
+        b.measure(1)
+        b.gradients_device(dE, gd, gp, lw)
+    b.sync()
+    ev[0].record(stream)
+    for _ in range(reps):
+        b.measure(1)
+    ev[1].record(stream)
+    for _ in range(reps):
+        b.gradients_device(dE, gd, gp, lw)
+    ev[2].record(stream)
+    ev[2].synchronize()
+    fwd = ev[0].elapsed_time(ev[1]) / reps
+    bwd = ev[1].elapsed_time(ev[2]) / reps
+    b.close()
+    return {"config": "2048 chains, beta=50, 3-orbital density-density; d log|w| w.r.t. "
+                      f"F(tau) ({nf}x{nft}) and {dE.shape[0]} H_loc parameters",
+            "forward_step_ms": fwd, "backward_ms": bwd, "backward_over_forward": bwd / fwd}
+
+
 def run_gpu(args, rank=0, world=1):
     import torch
     from w2dynamics_gb300 import engine as E
@@ -203,6 +247,7 @@ def run_gpu(args, rank=0, world=1):
     single.sync()
     s_time = time.perf_counter() - s0
     single_value = s_steps * NCORR / s_time
+    backward = measure_backward(E, model, probs[2], args)
     hbm, peak_kind = measured_peaks()
     bytes_per_launch = (wc["m_bytes"] + wc["op_bytes"]) / max(1, args.steps)
     achieved = bytes_per_launch / (ms / 1e3 / args.steps) / 1e9
@@ -227,6 +272,7 @@ def run_gpu(args, rank=0, world=1):
                              "the kernel is bound by barrier waits, load latency and the FP64 "
                              "pipe, not HBM",
                      "ncu": {"fp64_pipe_busy": NCU_FP64_PIPE, "issue_active": NCU_ISSUE_ACTIVE}},
+        "backward": backward,
         "work": wc,
         "schedule": {"warps_per_block": sched, "chosen_by": "autotuner (cthyb_batch_autotune)",
                      "cuda_graphs": True},

@@ -91,6 +91,9 @@ typedef struct {
                             flavour permutation (StepGlob, CTQMC.F90:4433-4554) */
   double p_shift;        /* PercentageTauShiftMove (StepShiftTau, CTQMC.F90:4557-4835) */
   int32_t nleg;          /* NLegMax: Legendre coefficients of G measured (0: none) */
+  int32_t nscore;        /* parameter directions for the score-function dG(tau)/dtheta (0: none;
+                            monomial models only, <= 32) */
+  const double* score_dE; /* nscore x nstates energy derivatives per eigenstate (row-major) */
 } cthyb_group_desc;
 
 #define CTHYB_FLAG_DENSE 1  /* dense block trace even for monomial models */
@@ -162,6 +165,22 @@ int cthyb_batch_results_extra(cthyb_batch_t batch, int chain, double* gleg, doub
  * grad_params/dE may be NULL with nparams = 0. */
 int cthyb_batch_gradients(cthyb_batch_t batch, int nparams, const double* dE, double* grad_delta,
                           double* grad_params, double* log_weights);
+
+/* The same with every array in device memory owned by the caller and no
+ * host copies (the form a torch.autograd.Function uses): grad_delta_dev
+ * (nchains, 2Nd, Nftau) row-major with flavour f = 2(b-1) + (s-1),
+ * grad_params_dev (nchains, nparams), log_weights_dev (nchains, 2),
+ * dE_dev (nparams, nstates).  Enqueued on `stream` (NULL: the batch's
+ * stream) after the batch's queued work; returns without synchronising. */
+int cthyb_batch_gradients_device(cthyb_batch_t batch, int nparams, const double* dE_dev, double* grad_delta_dev,
+                                 double* grad_params_dev, double* log_weights_dev, void* stream);
+
+/* Score-function estimate of dG(tau)/dtheta_p for the group's parameter
+ * directions (nscore > 0): dgtau (nscore, Nd, 2, Ntau), each direction in
+ * Fortran order, = <G g_p> - <G><g_p> with g_p = d log|trace| / dtheta_p of
+ * the measured configuration, normalised like G(tau); mean_score (nscore)
+ * = <g_p>.  Assumes a sign-free model (configuration sign constant). */
+int cthyb_batch_results_score(cthyb_batch_t batch, int chain, double* dgtau, double* mean_score);
 
 /* Global and tau-shift move counters of one chain since the last warmup or
  * measure call: TryGlob, AccGlob, AccQNGlob, TryShift, AccShift

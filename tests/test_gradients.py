@@ -108,3 +108,69 @@ def test_autograd_function_applies_the_chain_rule():
     assert np.allclose(logw.detach().numpy(), lw.sum(axis=1))
     assert np.allclose(ftau.grad.numpy(), np.tensordot(np.arange(1, 5), gd, axes=1))
     assert np.allclose(theta.grad.numpy(), np.arange(1, 5) @ gp)
+
+
+@pytest.mark.gpu
+def test_score_function_dG_dU_matches_finite_differences():
+    """dG(tau)/dU from the score-function estimator <G g> - <G><g> (g = d
+    log|trace|/dU of each measured configuration) against central
+    differences of G(tau) from independent runs at U +- dU, single-orbital
+    Anderson model, 2048 chains per run."""
+    from w2dynamics_gb300 import engine as E
+    beta, nd, u0, du, n, nt = 10.0, 1, 2.0, 0.1, 2048, 10
+    ft = P.semicircle_ftau(nd, beta, 1.0, 1000)
+    mu = P.muimp_solver(nd, u0 / 2)
+
+    def run(u, seed0, score):
+        um = P.flat_umatrix(P.umatrix_density(nd, u, u, 0.0))
+        mg = E.Model(nd, um, mu, "Nt Szt Azt")
+        dE = GR.density_density_directions(nd, mg.fock_states)[2:3] if score else None
+        b = E.Batch(mg, [E.Group(beta, ft, nt, nchains=n, seed0=seed0, taudiff_max=beta, ncorr=20,
+                                 p_shift=0.01, score_dE=dE)])
+        b.warmup(4000)
+        b.measure(400)
+        b.sync()
+        G = np.array([b.results(c)["gtau"][0, 0] for c in range(n)])
+        dG = np.array([b.results_score(c)[0][0, 0, 0] for c in range(n)]) if score else None
+        return G, dG
+
+    _, dG = run(u0, 0, True)
+    Gp, _ = run(u0 + du, 10000, False)
+    Gm, _ = run(u0 - du, 20000, False)
+    fd = (Gp.mean(0) - Gm.mean(0)) / (2 * du)
+    efd = np.sqrt(Gp.var(0, ddof=1) / n + Gm.var(0, ddof=1) / n) / (2 * du)
+    sf = dG.mean(0)
+    esf = dG.std(0, ddof=1) / np.sqrt(n)
+    z = (sf - fd) / np.sqrt(efd ** 2 + esf ** 2)
+    assert np.abs(z).max() < 4.5, (z, sf, fd)
+    assert np.mean(np.abs(z) < 2.5) >= 0.8
+    assert np.abs(sf).max() > 5 * esf.max()  # the derivative is resolved
+
+
+@pytest.mark.gpu
+def test_device_gradients_equal_host_gradients():
+    torch = pytest.importorskip("torch")
+    from w2dynamics_gb300 import engine as E
+    beta, nd = 10.0, 3
+    pr = P.config_problem("dd3", beta=beta)
+    mg = E.Model(nd, pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    b = E.Batch(mg, [E.Group(beta, pr["ftau"], 20, nchains=6, seed0=90, taudiff_max=5.0,
+                             kcap=64, opcap=512)])
+    b.warmup(1500)
+    b.sync()
+    dE = GR.density_density_directions(nd, mg.fock_states)
+    gd, gp, lw = b.gradients(dE)
+    dev = torch.device("cuda")
+    nft = pr["ftau"].shape[2]
+    t_gd = torch.empty((6, 2 * nd, nft), dtype=torch.float64, device=dev)
+    t_gp = torch.empty((6, dE.shape[0]), dtype=torch.float64, device=dev)
+    t_lw = torch.empty((6, 2), dtype=torch.float64, device=dev)
+    t_dE = torch.tensor(dE, device=dev)
+    torch.cuda.synchronize()
+    b.gradients_device(t_dE, t_gd, t_gp, t_lw)
+    b.sync()
+    g = t_gd.cpu().numpy()
+    assert np.allclose(np.stack([g[:, f] for f in range(2 * nd)], 1),
+                       np.stack([gd[:, f // 2, f % 2] for f in range(2 * nd)], 1))
+    assert np.allclose(t_gp.cpu().numpy(), gp)
+    assert np.allclose(t_lw.cpu().numpy(), lw)

@@ -2501,6 +2501,57 @@ __device__ void one_step(Ctx& c, Prop& p) {
   PROF_MARK(6);
 }
 
+// d log|trace| / dtheta_p of the current configuration (monomial models):
+// every outer state is walked through the operators; its log weight is
+// -sum E(state) * segment, its derivative the same sum with dE_p; the
+// derivatives are averaged with the states' signed contributions.  Also
+// returns log|trace| (relative to exp(-beta Egs)).  Lane-uniform results.
+constexpr int NPARMAX = 32;
+__device__ NOINL void trace_score(Ctx& c, const double* __restrict__ dE, int npar, double* score, double& logtr) {
+  const DModel& m = *c.m;
+  const Hdr& h = *c.h;
+  const int s0 = h.outer_sst, off = m.sst_off[s0], n0 = m.sst_n[s0], K = h.K;
+  double mx = -DHUGE, S = 0.0, D[NPARMAX];
+  for (int p = 0; p < npar; ++p) D[p] = 0.0;
+  for (int q = c.lane; q < n0; q += 32) {
+    int cur = off + q, neg = 0;
+    double l = 0.0, dl[NPARMAX], t = 0.0;
+    for (int p = 0; p < npar; ++p) dl[p] = 0.0;
+    for (int j = 0; j < K && cur >= 0; ++j) {
+      const double tau = c.optau[j], dt = tau - t;
+      l -= m.evs[cur] * dt;
+      for (int p = 0; p < npar; ++p) dl[p] -= dE[(size_t)p * m.ns + cur] * dt;
+      const size_t idx = (size_t)c.opcode[j] * m.ns + cur;
+      const int nx = m.mono_tgt[idx];
+      if (nx >= 0) {
+        l += m.mono_lv[idx];
+        neg ^= m.mono_neg[idx];
+      }
+      cur = nx;
+      t = tau;
+    }
+    if (cur != off + q) continue;
+    const double dt = c.g->beta - t;
+    l -= m.evs[cur] * dt;
+    for (int p = 0; p < npar; ++p) dl[p] -= dE[(size_t)p * m.ns + cur] * dt;
+    const double sg = neg ? -1.0 : 1.0;
+    if (l > mx) {  // rescale the running sums to the new maximum
+      const double r = mx == -DHUGE ? 0.0 : exp(mx - l);
+      S *= r;
+      for (int p = 0; p < npar; ++p) D[p] *= r;
+      mx = l;
+    }
+    const double w = sg * exp(l - mx);
+    S += w;
+    for (int p = 0; p < npar; ++p) D[p] += w * dl[p];
+  }
+  const double gmx = wmax(mx);
+  const double r = mx == -DHUGE ? 0.0 : exp(mx - gmx);
+  S = wsum(S * r);
+  for (int p = 0; p < npar; ++p) score[p] = wsum(D[p] * r) / S;
+  logtr = gmx + log(fabs(S));
+}
+
 // ---------------------------------------------------------------------------
 // Measurements after each NCorr block (CTQMC.F90:8541-8566)
 __device__ NOINL void measure(Ctx& c) {
@@ -2599,6 +2650,17 @@ __device__ NOINL void measure(Ctx& c) {
       }
     }
   }
+  // score-function dG/dtheta: d log|trace| / dtheta of this configuration
+  const int nsc = g.nscore;
+  double score[NPARMAX];
+  double* sacc = nsc > 0 ? (double*)((char*)c.gtau - g.o_gtau + g.o_score) : nullptr;
+  if (nsc > 0) {
+    double ltr;
+    trace_score(c, g.score_dE, nsc, score, ltr);
+    if (c.lane == 0)
+      for (int p = 0; p < nsc; ++p) sacc[p] += score[p];
+    __syncwarp();
+  }
   // MeasGtauRem(.false.): M elements binned by tau_a - tau_c, and their
   // Legendre coefficients (CTQMC.F90:2252-2440)
   const int nt = g.ntau, nleg = g.nleg;
@@ -2632,6 +2694,7 @@ __device__ NOINL void measure(Ctx& c) {
         Mv = Mv * h.cfgsign;
         if (idt > nt) idt = nt;
         atomicAdd(&G[idt - 1], Mv);
+        for (int p = 0; p < nsc; ++p) atomicAdd(&sacc[nsc + ((size_t)p * m.nf + f) * nt + idt - 1], Mv * score[p]);
         if (nleg > 0) {
           // P_l by the three-term recurrence, as evaluated in the reference
           const double x = __dsub_rn(__dmul_rn(__ddiv_rn(2.0, g.beta), dt), 1.0);
@@ -2966,7 +3029,6 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
 // energy derivatives dE it changes by the same sum with dE, and d log|tr| is
 // the average of those over the states weighted by their signed
 // contributions.  One warp per chain; the walk is O(K) per state.
-constexpr int NPARMAX = 32;
 __global__ void __launch_bounds__(WPB * 32) k_grad(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
                                                   const double* __restrict__ dE, int npar, double* gdelta,
                                                   double* gpar, double* logw) {
@@ -3003,50 +3065,12 @@ __global__ void __launch_bounds__(WPB * 32) k_grad(const __grid_constant__ DMode
   __syncwarp();
   if (c.lane == 0) logw[2 * (size_t)chain] = h.det_log;
   if (!c.mono || npar <= 0) return;
-  const int s0 = h.outer_sst, off = m.sst_off[s0], n0 = m.sst_n[s0], K = h.K;
-  double mx = -DHUGE, S = 0.0, D[NPARMAX];
-  for (int p = 0; p < npar; ++p) D[p] = 0.0;
-  for (int q = c.lane; q < n0; q += 32) {
-    int cur = off + q, neg = 0;
-    double l = 0.0, dl[NPARMAX], t = 0.0;
-    for (int p = 0; p < npar; ++p) dl[p] = 0.0;
-    for (int j = 0; j < K && cur >= 0; ++j) {
-      const double tau = c.optau[j], dt = tau - t;
-      l -= m.evs[cur] * dt;
-      for (int p = 0; p < npar; ++p) dl[p] -= dE[(size_t)p * m.ns + cur] * dt;
-      const size_t idx = (size_t)c.opcode[j] * m.ns + cur;
-      const int nx = m.mono_tgt[idx];
-      if (nx >= 0) {
-        l += m.mono_lv[idx];
-        neg ^= m.mono_neg[idx];
-      }
-      cur = nx;
-      t = tau;
-    }
-    if (cur != off + q) continue;
-    const double dt = g.beta - t;
-    l -= m.evs[cur] * dt;
-    for (int p = 0; p < npar; ++p) dl[p] -= dE[(size_t)p * m.ns + cur] * dt;
-    const double sg = neg ? -1.0 : 1.0;
-    if (l > mx) {  // rescale the running sums to the new maximum
-      const double r = mx == -DHUGE ? 0.0 : exp(mx - l);
-      S *= r;
-      for (int p = 0; p < npar; ++p) D[p] *= r;
-      mx = l;
-    }
-    const double w = sg * exp(l - mx);
-    S += w;
-    for (int p = 0; p < npar; ++p) D[p] += w * dl[p];
-  }
-  const double gmx = wmax(mx);
-  const double r = mx == -DHUGE ? 0.0 : exp(mx - gmx);
-  S = wsum(S * r);
-  for (int p = 0; p < npar; ++p) {
-    const double v = wsum(D[p] * r);
-    if (c.lane == 0) gpar[(size_t)chain * npar + p] = v / S;
-  }
+  double score[NPARMAX], ltr;
+  trace_score(c, dE, npar, score, ltr);
+  if (c.lane == 0)
+    for (int p = 0; p < npar; ++p) gpar[(size_t)chain * npar + p] = score[p];
   // absolute log|trace| (the stored trace is relative to exp(-beta Egs))
-  if (c.lane == 0) logw[2 * (size_t)chain + 1] = gmx + log(fabs(S)) - g.beta * m.egs;
+  if (c.lane == 0) logw[2 * (size_t)chain + 1] = ltr - g.beta * m.egs;
 }
 
 // set_mc_config: operator arrays from a time-ordered list already written
@@ -3250,6 +3274,7 @@ struct GroupHost {
   std::vector<double> hybr;
   double* d_hybr = nullptr;
   double* d_empty = nullptr;
+  double* d_score = nullptr;
   int* d_seeds = nullptr;
   double* d_tdm = nullptr;
   int chain0 = 0;
@@ -3501,6 +3526,9 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   off = align_up(off + (size_t)nf * g.nleg * 8, 256);
   g.o_outer = off;  // outer superstate/state histograms, signs, trace contributions
   off = align_up(off + (size_t)3 * (hm.nss + hm.ns) * 8, 256);
+  g.nscore = (d.nscore > 0 && d.score_dE && mono) ? std::min(d.nscore, 32) : 0;
+  g.o_score = off;
+  off = align_up(off + (size_t)g.nscore * (1 + (size_t)nf * d.ntau) * 8, 256);
   g.o_dense = off;
   size_t dense = std::max((size_t)2 * hm.nsmax * hm.nsmax + 2 * hm.nsmax, (size_t)2 * kcap * kcap) * 8;
   off = align_up(off + dense, 256);
@@ -3590,6 +3618,12 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
     empty_trace_weights(hm, d.beta, w);
     G.d_empty = dev_upload(w, e);
     G.g.empty_w = G.d_empty;
+    G.g.score_dE = nullptr;
+    if (G.g.nscore > 0) {
+      std::vector<double> dE(d.score_dE, d.score_dE + (size_t)G.g.nscore * hm.ns);
+      G.d_score = dev_upload(dE, e);
+      G.g.score_dE = G.d_score;
+    }
     std::vector<int> seeds(d.nchains);
     for (int c = 0; c < d.nchains; ++c) seeds[c] = d.seeds ? d.seeds[c] : d.seed0 + c;
     G.d_seeds = dev_upload(seeds, e);
@@ -3626,6 +3660,7 @@ int cthyb_batch_destroy(cthyb_batch_t B) {
   for (GroupHost& G : B->groups) {
     cudaFree(G.d_hybr);
     cudaFree(G.d_empty);
+    cudaFree(G.d_score);
     cudaFree(G.d_seeds);
     cudaFree(G.d_tdm);
   }
@@ -3923,6 +3958,41 @@ int cthyb_batch_results_extra(cthyb_batch_t B, int chain, double* gleg, double* 
   return CTHYB_OK;
 }
 
+int cthyb_batch_results_score(cthyb_batch_t B, int chain, double* dgtau, double* mean_score) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  const int ns = G->g.nscore;
+  if (ns <= 0) return fail(CTHYB_ERR_ARG, "the group has no score directions");
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  const HostModel& hm = B->model->hm;
+  const int nf = hm.nf, nt = G->g.ntau;
+  std::vector<double> acc((size_t)ns * (1 + (size_t)nf * nt)), gt((size_t)nf * nt);
+  char* base = G->g.base + (size_t)c * G->g.stride;
+  CK(cudaMemcpy(acc.data(), base + G->g.o_score, acc.size() * 8, cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(gt.data(), base + G->g.o_gtau, gt.size() * 8, cudaMemcpyDeviceToHost));
+  const double cnt = (double)h.cnt_meas;
+  if (cnt <= 0) return fail(CTHYB_ERR_ARG, "no measurements");
+  // G = -(raw/cnt)/(-mean_sign) * Ntau/beta^2 (CTQMC.F90:8730); the sign is
+  // constant (+-1) in a sign-free model
+  const double ms = h.meas_sign / cnt;
+  const double norm = (double)nt / (G->g.beta * G->g.beta) / ms;
+  for (int p = 0; p < ns; ++p) {
+    const double gmean = acc[p] / cnt;
+    if (mean_score) mean_score[p] = gmean;
+    if (!dgtau) continue;
+    for (int f = 0; f < nf; ++f)
+      for (int t = 0; t < nt; ++t) {
+        const double cov = acc[ns + ((size_t)p * nf + f) * nt + t] / cnt - gt[(size_t)f * nt + t] / cnt * gmean;
+        dgtau[(size_t)p * nf * nt + (f / 2) + hm.nd * ((f % 2) + 2 * (size_t)t)] = cov * norm;
+      }
+  }
+  return CTHYB_OK;
+}
+
 int cthyb_batch_results(cthyb_batch_t B, int chain, double* gtau, double* mean_sign, double* dmat,
                         double* histo, int64_t* counters) {
   GroupHost* G;
@@ -4165,6 +4235,38 @@ int cthyb_batch_gradients(cthyb_batch_t B, int nparams, const double* dE, double
   }
   if (d_dE) cudaFree(d_dE);
   return rc;
+}
+
+int cthyb_batch_gradients_device(cthyb_batch_t B, int nparams, const double* dE_dev, double* grad_delta_dev,
+                                 double* grad_params_dev, double* log_weights_dev, void* stream) {
+  if (!B || nparams < 0 || nparams > NPARMAX || !grad_delta_dev || !log_weights_dev ||
+      (nparams > 0 && (!dE_dev || !grad_params_dev)))
+    return fail(CTHYB_ERR_ARG, "bad arguments (nparams must be 0..32)");
+  if (nparams > 0)
+    for (GroupHost& G : B->groups)
+      if (G.g.o_chk) return fail(CTHYB_ERR_UNSUPPORTED, "trace gradients need a monomial (density-density) model");
+  const int nft = B->groups[0].g.nftau, nf = B->model->hm.nf;
+  for (GroupHost& G : B->groups)
+    if (G.g.nftau != nft) return fail(CTHYB_ERR_ARG, "gradients need one Nftau for all groups");
+  cudaStream_t st = stream ? (cudaStream_t)stream : B->stream;
+  if (st != B->stream) {  // order after the batch's queued sweeps
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev, B->stream));
+    CK(cudaStreamWaitEvent(st, ev, 0));
+    CK(cudaEventDestroy(ev));
+  }
+  CK(cudaMemsetAsync(grad_delta_dev, 0, sizeof(double) * (size_t)B->nchains * nf * nft, st));
+  for (GroupHost& G : B->groups) {
+    const int n = G.desc.nchains;
+    k_grad<<<(n + WPB - 1) / WPB, WPB * 32, 0, st>>>(B->model->dm, G.g, dE_dev, nparams,
+                                                     grad_delta_dev + (size_t)G.chain0 * nf * nft,
+                                                     grad_params_dev ? grad_params_dev + (size_t)G.chain0 * nparams
+                                                                     : nullptr,
+                                                     log_weights_dev + (size_t)G.chain0 * 2);
+    CK(cudaGetLastError());
+  }
+  return CTHYB_OK;
 }
 
 int cthyb_batch_refresh_minv(cthyb_batch_t B, int replace, double* maxdev) {

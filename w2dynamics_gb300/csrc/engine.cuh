@@ -63,6 +63,8 @@ struct DGroup {
   const double* hybr;  // [nf][nftau]
   int ntau, ncorr, maxhisto;
   int nleg;            // Legendre coefficients of G measured (NLegMax; 0: none)
+  int nscore;          // parameter directions of the score-function dG/dtheta (0: none)
+  const double* score_dE;  // [nscore][ns]
   double p_outer, p_global, p_shift;  // PercentageOuterMove, PercentageGlobalMove, PercentageTauShiftMove
   int kcap, opcap, L, dense, meas_dm;
   char* base;          // chain c at base + c*stride
@@ -70,7 +72,8 @@ struct DGroup {
   size_t o_hdr, o_mt, o_optau, o_opcode, o_srt_tau, o_srt_slot, o_slot_tau, o_M, o_tree, o_act, o_bstart,
       o_scr, o_gtau, o_histo, o_dm, o_gleg, o_outer, o_dense, o_log, o_glob,  // o_glob: 0 without global/shift moves
       o_glscr,  // per-lane Legendre partial sums (0 when nleg == 0)
-      o_chk;    // dense-block models: ket and bra checkpoints at the 2^L + 1 bin edges
+      o_chk,    // dense-block models: ket and bra checkpoints at the 2^L + 1 bin edges
+      o_score;  // score sums [nscore] and G * score sums [nscore][nf][ntau]
   size_t chk_bytes;  // bytes of one checkpoint
   size_t node_bytes;   // bytes of one node slot
   long long logcap;

@@ -29,7 +29,7 @@ EXPORTS = (
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
     "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_autotune", "cthyb_batch_results",
-    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_state", "cthyb_batch_get_config",
+    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
     "cthyb_minv_rebuild_noalloc",
@@ -43,7 +43,7 @@ class GroupDesc(C.Structure):
                 ("ncorr", C.c_int32), ("p_outer", C.c_double), ("kcap", C.c_int32),
                 ("opcap", C.c_int32), ("tree_levels", C.c_int32), ("maxhisto", C.c_int32),
                 ("flags", C.c_int32), ("p_global", C.c_double), ("p_shift", C.c_double),
-                ("nleg", C.c_int32)]
+                ("nleg", C.c_int32), ("nscore", C.c_int32), ("score_dE", C.POINTER(C.c_double))]
 
 
 class EngineError(RuntimeError):
@@ -92,6 +92,8 @@ def load(build_if_missing=False):
     L.cthyb_batch_move_counters.argtypes = [vp, C.c_int, C.POINTER(i64)]
     L.cthyb_batch_results_extra.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp]
     L.cthyb_batch_gradients.argtypes = [vp, C.c_int, dp, dp, dp, dp]
+    L.cthyb_batch_results_score.argtypes = [vp, C.c_int, dp, dp]
+    L.cthyb_batch_gradients_device.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp]
     L.cthyb_batch_group_sums.argtypes = [vp, C.c_int, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_state.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_get_config.argtypes = [vp, C.c_int, ip, dp, ip, ip, ip, ip]
@@ -172,7 +174,7 @@ class Group:
 
     def __init__(self, beta, ftau, ntau, nchains=1, seed0=0, seeds=None, taudiff_max=-1.0,
                  ncorr=100, p_outer=0.0, kcap=0, opcap=0, tree_levels=0, maxhisto=500,
-                 dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0):
+                 dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0, score_dE=None):
         self.beta = float(beta)
         self.ftau = np.asfortranarray(np.asarray(ftau, np.float64))
         self.ntau = int(ntau)
@@ -184,6 +186,7 @@ class Group:
         self.p_outer = float(p_outer)
         self.p_global, self.p_shift = float(p_global), float(p_shift)
         self.nleg = int(nleg)
+        self.score_dE = None if score_dE is None else np.ascontiguousarray(score_dE, np.float64)
         self.kcap, self.opcap, self.tree_levels = int(kcap), int(opcap), int(tree_levels)
         self.maxhisto = int(maxhisto)
         self.flags = (FLAG_DENSE if dense else 0) | (0 if measure_dm else FLAG_NO_DM)
@@ -206,6 +209,8 @@ class Group:
         d.flags = self.flags
         d.p_global, d.p_shift = self.p_global, self.p_shift
         d.nleg = self.nleg
+        d.nscore = 0 if self.score_dE is None else self.score_dE.shape[0]
+        d.score_dE = _dp(self.score_dE) if self.score_dE is not None else None
         return d
 
 
@@ -289,6 +294,24 @@ class Batch:
         out = dict(zip(keys, arrs))
         out["gleg"] = gl[:nd * 2 * g.nleg].reshape((nd, 2, g.nleg), order="F")
         return out
+
+    def gradients_device(self, dE_dev, grad_delta, grad_params, log_weights, stream=None):
+        """Device-memory form of `gradients` (torch CUDA tensors or raw
+        pointers): grad_delta (nchains, 2Nd, Nftau), grad_params (nchains,
+        nparams), log_weights (nchains, 2); enqueued, not synchronised."""
+        ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr() if hasattr(t, "data_ptr") else int(t))
+        npar = 0 if dE_dev is None else int(dE_dev.shape[0])
+        _check(load().cthyb_batch_gradients_device(self.h, npar, ptr(dE_dev), ptr(grad_delta), ptr(grad_params),
+                                                   ptr(log_weights), C.c_void_p(stream) if stream else None))
+
+    def results_score(self, chain):
+        """Score-function dG(tau)/dtheta (nscore, Nd, 2, Ntau) and <g> (nscore)."""
+        g = self.groups[self._group_of[chain]]
+        nd, ns = self.model.nd, g.score_dE.shape[0]
+        dg = np.zeros(ns * nd * 2 * g.ntau)
+        ms = np.zeros(ns)
+        _check(load().cthyb_batch_results_score(self.h, chain, _dp(dg), _dp(ms)))
+        return dg.reshape((ns, g.ntau, 2, nd)).transpose(0, 3, 2, 1), ms
 
     def gradients(self, dE=None):
         """d log|w| of every chain's current configuration: grad_delta
