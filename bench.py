@@ -35,6 +35,10 @@ NCORR = 100
 TDM = 5.0
 THERMALIZE = 2000  # proposals per chain before timing (not timed)
 TUNE = 200         # of them, per candidate schedule of the autotuner (10 candidates)
+CPU_SAMPLE_MEAS = 100  # measurement cycles per host core and round of the bounded CPU sample
+# dense-block workload (--workload kanamori5): 5-orbital Kanamori with
+# spin-flip and pair hopping, 1024 chains, one window (TaudiffMax <= 0)
+K5_BETA, K5_CHAINS, K5_THERM = 40.0, 1024, 2000
 METRIC = "MC updates/sec on 1 GB300, batched vs one-chain form, at equal G(tau) error"
 # From one ncu capture (--set full) of a timed sweep launch of this workload:
 # DRAM bytes read + written, FP64-pipe and issue utilisation.
@@ -173,6 +177,54 @@ def measure_backward(E, model, pr, args):
             "forward_step_ms": fwd, "backward_ms": bwd, "backward_over_forward": bwd / fwd}
 
 
+def run_gpu_k5(args):
+    """Dense-block workload: 1024 chains of the 5-orbital Kanamori model
+    (U=3, J=0.7, crystal field, beta=40, 1024 states in 36 (N,Sz) blocks up
+    to 100x100), Ntau = Nftau = 4000, NCorr = 100, seed = chain index.  The
+    chains are thermalised for K5_THERM proposals only (orders still
+    growing); the CPU sample runs the oracle on the same footing."""
+    import torch
+    from w2dynamics_gb300 import engine as E
+    from w2dynamics_gb300 import problems as P
+    pr = P.config_problem("kanamori5", beta=K5_BETA)
+    model = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    b = E.Batch(model, [E.Group(K5_BETA, pr["ftau"], pr["ntau"], nchains=K5_CHAINS, seed0=0, taudiff_max=-1.0,
+                                ncorr=NCORR, kcap=64, opcap=1024, tree_levels=4)])
+    b.warmup(K5_THERM)
+    b.sync()
+    stream = torch.cuda.ExternalStream(b.stream())
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(args.warmup):
+        b.measure(1)
+    b.sync()
+    with ClockSampler() as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            b.measure(1)
+        stop.record(stream)
+        stop.synchronize()
+    ms = start.elapsed_time(stop)
+    value = K5_CHAINS * NCORR * args.steps / (ms / 1e3)
+    korder = float(np.mean([b.state(c)["noper"] for c in range(0, K5_CHAINS, 64)]))
+    b.close()
+    cores = os.cpu_count() or 1
+    cpu_value, cpu_wall = oracle_rate(cores, 2, 2, 0, workload="kanamori5")
+    line = {
+        "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (semicircular bath D=2, seeded chains)",
+        "config": {"workload": f"{K5_CHAINS} chains, 5-orbital Kanamori U=3 J=0.7 crystal field +-0.2, "
+                               f"beta={K5_BETA}, Ntau=Nftau=4000, Nt Szt blocks, NCorr={NCORR}, "
+                               f"{K5_THERM} thermalisation proposals",
+                   "mean_operators_per_chain": korder},
+        "cpu_baseline": {"value": cpu_value, "unit": "MC updates/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} chains (one per host core), {K5_THERM} thermalisation "
+                                   f"proposals, 2 rounds of 2 x {NCORR} proposals ({cpu_wall:.1f} s)"},
+        "gpu_launches": args.steps, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line))
+
+
 def run_gpu(args, rank=0, world=1):
     import torch
     from w2dynamics_gb300 import engine as E
@@ -248,6 +300,8 @@ def run_gpu(args, rank=0, world=1):
     s_time = time.perf_counter() - s0
     single_value = s_steps * NCORR / s_time
     backward = measure_backward(E, model, probs[2], args)
+    cores = os.cpu_count() or 1
+    cpu_value, cpu_wall = oracle_rate(cores, CPU_SAMPLE_MEAS, 3, 1)
     hbm, peak_kind = measured_peaks()
     bytes_per_launch = (wc["m_bytes"] + wc["op_bytes"]) / max(1, args.steps)
     achieved = bytes_per_launch / (ms / 1e3 / args.steps) / 1e9
@@ -272,6 +326,11 @@ def run_gpu(args, rank=0, world=1):
                              "the kernel is bound by barrier waits, load latency and the FP64 "
                              "pipe, not HBM",
                      "ncu": {"fp64_pipe_busy": NCU_FP64_PIPE, "issue_active": NCU_ISSUE_ACTIVE}},
+        "cpu_baseline": {"value": cpu_value, "unit": "MC updates/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} chains (one per host core, beta cycling over {list(BETAS)}), "
+                                   f"{THERMALIZE} thermalisation proposals, then 3 rounds of "
+                                   f"{CPU_SAMPLE_MEAS} measurement cycles x {NCORR} proposals per chain "
+                                   f"({cpu_wall:.1f} s wall)"},
         "backward": backward,
         "work": wc,
         "schedule": {"warps_per_block": sched, "chosen_by": "autotuner (cthyb_batch_autotune)",
@@ -285,16 +344,16 @@ def run_gpu(args, rank=0, world=1):
 _WORKER = {}
 
 
-def _worker_init(beta, seed, ftau):
+def _worker_init(name, beta, seed, ftau, therm):
     """One oracle chain per process, built and thermalised once."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from w2dynamics_gb300 import problems as P
-    nd = 3
-    um = P.flat_umatrix(P.umatrix_density(nd, 4.0, 4.0 - 1.2, 0.6))
-    m = O.Model(nd, um, P.muimp_solver(nd, P.DD3_MU), "Nt Szt")
-    c = O.Chain(m, beta, ftau, NTAU, seed=seed, taudiff_max=TDM, ncorr=NCORR)
-    c.warmup(THERMALIZE)
+    pr = P.config_problem(name, beta=beta)
+    m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    tdm = TDM if name == "dd3" else -1.0
+    c = O.Chain(m, beta, ftau, 100, seed=seed, taudiff_max=tdm, ncorr=NCORR)
+    c.warmup(therm)
     _WORKER["chain"], _WORKER["model"] = c, m
 
 
@@ -305,35 +364,47 @@ def _worker_run(nmeas):
     return time.perf_counter() - t0, nmeas * NCORR
 
 
-def run_reference(args):
-    """Oracle (C++ restatement of the Fortran loop) on all host cores, one
-    chain per core; each step runs `ref_meas` measurement cycles per chain."""
+def oracle_rate(cores, meas, rounds, warm_rounds, workload="batched"):
+    """MC updates/s of the oracle (C++ restatement of the Fortran loop) on
+    `cores` host cores, one chain per core (beta cycling over the groups of
+    the batched workload), each round `meas` measurement cycles per chain;
+    median over rounds."""
     import multiprocessing as mp
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
     from w2dynamics_gb300 import problems as P
-    cores = os.cpu_count() or 1
-    ftaus = {b: P.semicircle_ftau(3, b, 1.0, NTAU) for b in BETAS}
+    if workload == "kanamori5":
+        specs = [("kanamori5", K5_BETA, P.config_problem("kanamori5", beta=K5_BETA)["ftau"], K5_THERM)]
+    else:
+        specs = [("dd3", b, P.semicircle_ftau(3, b, 1.0, NTAU), THERMALIZE) for b in BETAS]
     ctx = mp.get_context("spawn")
     pools = []
     for i in range(cores):
-        b = BETAS[i % len(BETAS)]
-        pools.append(ctx.Pool(1, initializer=_worker_init, initargs=(b, i, ftaus[b])))
+        name, b, ft, th = specs[i % len(specs)]
+        pools.append(ctx.Pool(1, initializer=_worker_init, initargs=(name, b, i, ft, th)))
     try:
-        for _ in range(args.warmup):
-            for r in [p.apply_async(_worker_run, (max(1, args.ref_meas // 4),)) for p in pools]:
+        for _ in range(warm_rounds):
+            for r in [p.apply_async(_worker_run, (max(1, meas // 4),)) for p in pools]:
                 r.get()
         vals = []
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            res = [r.get() for r in [p.apply_async(_worker_run, (args.ref_meas,)) for p in pools]]
+        for _ in range(rounds):
+            res = [r.get() for r in [p.apply_async(_worker_run, (meas,)) for p in pools]]
             vals.append(sum(n for _, n in res) / max(t for t, _ in res))
         wall = time.perf_counter() - t0
     finally:
         for p in pools:
             p.terminate()
-    value = float(np.median(vals))
+    return float(np.median(vals)), wall
+
+
+def run_reference(args):
+    """Oracle (C++ restatement of the Fortran loop) on all host cores, one
+    chain per core; each step runs `ref_meas` measurement cycles per chain."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    value, wall = oracle_rate(cores, args.ref_meas if args.workload == "batched" else 2, args.steps,
+                              args.warmup, workload=args.workload)
     line = {
         "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
@@ -357,11 +428,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--chains-per-beta", type=int, default=CHAINS_PER_BETA)
+    ap.add_argument("--workload", default="batched", choices=("batched", "kanamori5"),
+                    help="batched: the 4096-chain benchmark; kanamori5: dense-block 5-orbital model")
     ap.add_argument("--ref-meas", type=int, default=100,
                     help="measurement cycles per chain and step of the CPU reference arm")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "kanamori5":
+        run_gpu_k5(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
