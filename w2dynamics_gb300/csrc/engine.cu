@@ -191,7 +191,15 @@ __device__ __forceinline__ double grnd(Ctx& c) {
   // and the scaling by 2^-64 is an exponent shift (exact, v >= 1).
   unsigned long long v = ((unsigned long long)b << 32) | a;
   if (v == 0ull) return 0.0;
-  long long bits = __double_as_longlong(__ull2double_rn(v)) - (64ll << 52);
+  // round v to 53 bits (to nearest, ties to even) with integer operations
+  // and build the double v * 2^-64 directly: exponent -1 - lz, carry of the
+  // rounding into the exponent field included (keeps the FP64 pipe free)
+  const int lz = __clzll(v);
+  const unsigned long long m = v << lz;  // leading one at bit 63
+  unsigned long long mant = m >> 11;     // 53 bits with the hidden one
+  const unsigned long long rest = m & 0x7FFull;
+  if (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) ++mant;
+  long long bits = (long long)(((unsigned long long)(1022 - lz) << 52) + (mant - (1ull << 52)));
   if (bits >= 0x3FF0000000000000ll) bits = 0x3FEFFFFFFFFFFFFFll;  // 1.0 -> nextafter(1, 0)
   return __longlong_as_double(bits);
 }
@@ -449,18 +457,19 @@ struct Mod {
   int n1, n2;       // gathered operator counts of leaves b1, b2 (buffers 0, 1)
 };
 
-__device__ __forceinline__ double bin_edge(const Ctx& c, int j) {
-  return __dmul_rn(c.g->beta, ldexp((double)j, -c.g->L));
-}
+// Bin edges beta * j / 2^L (tabulated per group) and the bin of a time by
+// an integer search over their order keys (no FP64 work).
+__device__ __forceinline__ double bin_edge(const Ctx& c, int j) { return c.g->edges[j]; }
 __device__ __forceinline__ int bin_of(const Ctx& c, double t) {
-  const int nb = 1 << c.g->L;
-  int j = (int)(t * c.g->binscale);  // first guess, corrected against the edges
-  if (j < 0) j = 0;
-  if (j > nb - 1) j = nb - 1;
   const long long tb = tkey(t);
-  while (j < nb - 1 && tkey(bin_edge(c, j + 1)) <= tb) ++j;
-  while (j > 0 && tkey(bin_edge(c, j)) > tb) --j;
-  return j;
+  const long long* ek = c.g->ekeys;
+  int lo = 0, hi = 1 << c.g->L;  // the bin is the last j in [lo, hi) with ek[j] <= tb
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (ek[mid] <= tb) lo = mid;
+    else hi = mid;
+  }
+  return lo;
 }
 __device__ __forceinline__ char* node_base(const Ctx& c, int n, int slot) {
   return c.tree + ((size_t)n * 2 + slot) * c.g->node_bytes;
@@ -802,11 +811,35 @@ __device__ NOINL int new_suffix(Ctx& c, const Mod& md, int s, double t) {
 // sum over states i of s0 mapped onto themselves of sign*exp(lw).
 // lg/sg: log|trace| and its sign; mx/sum: trace = sum * exp(mx) (the
 // acceptance ratio uses these without a logarithm).
-__device__ NOINL void root_trace(Ctx& c, int slot, int s0, double& mx_out, double& sum_out) {
+__device__ NOINL void root_trace(Ctx& c, int slot, int s0, double& mx_out, double& sum_out,
+                                 double ref = -DHUGE) {
   const DModel& m = *c.m;
   const double* lw = node_lw(c, 1, slot);
   const uint16_t* tg = node_tg(c, 1, slot);
   int off = m.sst_off[s0], n0 = m.sst_n[s0];
+  if (ref > -DHUGE) {
+    // relative to a known log scale (the current trace): one exponential
+    // per state and no separate scale pass; falls back when a term could
+    // overflow or all underflow
+    double sum = 0.0;
+    bool big = false;
+    for (int i = c.lane; i < n0; i += 32) {
+      const int st = off + i;
+      const uint16_t t = tg[st];
+      if ((t & 0x7fff) != st) continue;
+      const double d = lw[st] - ref;
+      if (d > 600.0) big = true;
+      else sum += ((t & 0x8000) ? -1.0 : 1.0) * exp(d);
+    }
+    if (!__any_sync(FULL, big)) {
+      sum = wsum(sum);
+      if (sum != 0.0) {
+        mx_out = ref;
+        sum_out = sum;
+        return;
+      }
+    }
+  }
   double mx = -DHUGE;
   for (int i = c.lane; i < n0; i += 32) {
     int st = off + i;
@@ -841,6 +874,10 @@ __device__ __forceinline__ void trace_log(double mx, double sum, double& lg, dou
 // product could over- or underflow.
 __device__ __forceinline__ double weight_ratio(double mx, double sum, double old_log, double absdet) {
   if (mx == -DHUGE || sum == 0.0) return 0.0;
+  if (mx == old_log) {  // trace already relative to the current one
+    const double w = fabs(sum) * absdet;
+    if (w > 1e-290 && w < 1e290) return w;
+  }
   double e = mx - old_log;
   if (e > -600.0 && e < 600.0) {
     double w = exp(e) * fabs(sum) * absdet;
@@ -1321,7 +1358,7 @@ __device__ NOINL void write_record(Ctx& c, const cthyb_record& r) {
 // Trace of the proposed configuration as sum * exp(mx).
 __device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum) {
   if (c.mono) {
-    root_trace(c, 1 - c.act[1], s0, mx, sum);  // state tree rebuilt after the QN check
+    root_trace(c, 1 - c.act[1], s0, mx, sum, c.h->trace_log);  // state tree rebuilt after the QN check
   } else if (s0 == c.h->outer_sst && c.g->o_chk) {
     chk_trace(c, md, mx, sum);  // log|trace| and its sign from the checkpoints
   } else {
@@ -3275,6 +3312,8 @@ struct GroupHost {
   double* d_hybr = nullptr;
   double* d_empty = nullptr;
   double* d_score = nullptr;
+  double* d_edges = nullptr;
+  long long* d_ekeys = nullptr;
   int* d_seeds = nullptr;
   double* d_tdm = nullptr;
   int chain0 = 0;
@@ -3618,6 +3657,19 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
     empty_trace_weights(hm, d.beta, w);
     G.d_empty = dev_upload(w, e);
     G.g.empty_w = G.d_empty;
+    {
+      const int nbins = 1 << G.g.L;
+      std::vector<double> edges(nbins + 1);
+      std::vector<long long> keys(nbins + 1);
+      for (int j = 0; j <= nbins; ++j) {
+        edges[j] = d.beta * std::ldexp((double)j, -G.g.L);  // exact scaling, one rounding
+        std::memcpy(&keys[j], &edges[j], 8);
+      }
+      G.d_edges = dev_upload(edges, e);
+      G.d_ekeys = dev_upload(keys, e);
+      G.g.edges = G.d_edges;
+      G.g.ekeys = G.d_ekeys;
+    }
     G.g.score_dE = nullptr;
     if (G.g.nscore > 0) {
       std::vector<double> dE(d.score_dE, d.score_dE + (size_t)G.g.nscore * hm.ns);
@@ -3661,6 +3713,8 @@ int cthyb_batch_destroy(cthyb_batch_t B) {
     cudaFree(G.d_hybr);
     cudaFree(G.d_empty);
     cudaFree(G.d_score);
+    cudaFree(G.d_edges);
+    cudaFree(G.d_ekeys);
     cudaFree(G.d_seeds);
     cudaFree(G.d_tdm);
   }
@@ -4302,6 +4356,9 @@ int cthyb_batch_set_log(cthyb_batch_t B, int64_t cap) {
     G.g.hybr = save.hybr;
     G.g.empty_w = save.empty_w;
     G.g.err_flag = save.err_flag;
+    G.g.edges = save.edges;
+    G.g.ekeys = save.ekeys;
+    G.g.score_dE = save.score_dE;
     total += (size_t)G.desc.nchains * G.g.stride;
   }
   char* slab = nullptr;

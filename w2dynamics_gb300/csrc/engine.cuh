@@ -78,6 +78,8 @@ struct DGroup {
   size_t node_bytes;   // bytes of one node slot
   long long logcap;
   const double* empty_w;  // [nss] normalised empty-trace weights
+  const double* edges;    // [2^L + 1] time-bin edges beta * j / 2^L
+  const long long* ekeys; // [2^L + 1] their order keys (bit patterns)
   int* err_flag;
 };
 
