@@ -1018,17 +1018,32 @@ __device__ __forceinline__ double* dwork(const Ctx& c, int i) {
   const size_t n2 = (size_t)c.m->nsmax * c.m->nsmax;
   return i < 2 ? c.dense + i * n2 : c.dense + 2 * n2 + (size_t)(i - 2) * c.m->nsmax;
 }
-// column-wise split_log (Trace.F90:5341-5348): scale each column to max 1
+// Column-wise renormalisation, the role of split_log (Trace.F90:5341-5348):
+// each column is scaled by the power of two at or below its largest
+// magnitude (exact), whose exponent goes into the column's log.  One column
+// at a time, warp-parallel over its rows; the maximum is taken on the bit
+// patterns (order-preserving for magnitudes), so no FP64 compares.
 __device__ void col_split(Ctx& c, int rows, int cols, double* v, double* lg) {
   const int ld = c.m->nsmax;
-  for (int col = c.lane; col < cols; col += 32) {
-    double mx = 0.0;
-    for (int i = 0; i < rows; ++i) mx = fmax(mx, fabs(v[(size_t)col * ld + i]));
-    if (mx > 0.0) {
-      const double inv = 1.0 / mx;
-      for (int i = 0; i < rows; ++i) v[(size_t)col * ld + i] *= inv;
+  for (int col = 0; col < cols; ++col) {
+    double* vc = v + (size_t)col * ld;
+    long long mk = 0;
+    for (int i = c.lane; i < rows; i += 32) {
+      const long long k = __double_as_longlong(vc[i]) & 0x7FFFFFFFFFFFFFFFll;
+      mk = k > mk ? k : mk;
     }
-    lg[col] += log(mx);
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      const long long y = __shfl_xor_sync(FULL, mk, o);
+      mk = y > mk ? y : mk;
+    }
+    const int ef = (int)(mk >> 52);  // biased exponent of the maximum
+    if (mk == 0 || ef == 0 || ef == 0x7FF) continue;  // zero, subnormal or non-finite column: left as is
+    const int e = ef - 1023 > 1022 ? 1022 : ef - 1023;  // keep 2^-e a normal number
+    if (e == 0) continue;
+    const double sc = __longlong_as_double((long long)(1023 - e) << 52);  // 2^-e
+    for (int i = c.lane; i < rows; i += 32) vc[i] *= sc;
+    if (c.lane == 0) lg[col] += (double)e * 0.69314718055994530942;  // e ln 2
   }
   __syncwarp();
 }
