@@ -94,6 +94,9 @@ typedef struct {
   int32_t nscore;        /* parameter directions for the score-function dG(tau)/dtheta (0: none;
                             monomial models only, <= 32) */
   const double* score_dE; /* nscore x nstates energy derivatives per eigenstate (row-major) */
+  int32_t nsym;          /* NSymMove: user symmetry moves for StepGlob (0: none) */
+  const int32_t* symmoves; /* nsym x 2Nd, row i = SymMove(i+1): 1-based target flavour of flavour
+                              (b-1) + Nd*(s-1) + 1 (Trace.F90:471-477) */
 } cthyb_group_desc;
 
 #define CTHYB_FLAG_DENSE 1  /* dense block trace even for monomial models */

@@ -390,6 +390,8 @@ struct Params {
   double p_global, p_shift, p_4op, p_outer;
   int32_t maxhisto, meas_dm;
   int32_t nleg;  // NLegMax (0: no Legendre measurement)
+  int32_t nsym;  // NSymMove
+  const int32_t* symmoves;  // nsym x 2Nd, SymMoveNN lists (1-based targets)
 };
 
 struct Op {
@@ -440,6 +442,7 @@ struct Chain {
   std::vector<double> dm;     // ns x ns eigenbasis (offsets)
   std::vector<double> outer_histo;
   std::vector<double> gleg;                                   // [f][nleg]
+  std::vector<std::vector<int>> symmoves;                     // SymMoves(2 NSymMove, 2 Nd), Trace.F90:471-477
   std::vector<double> sign_sst, contrib_sst;                  // [nss]
   std::vector<double> state_histo, sign_state, contrib_state;  // [ns]
   double mean_sign = 0;
@@ -1311,8 +1314,8 @@ static int fixed_ssts(const Chain& c, const std::vector<Op>& ops, std::vector<in
 enum { GLOB_RANDPERM = 1, GLOB_USERSYM = 2, GLOB_SPINFLIP = 3, GLOB_CAFLIP = 4 };
 enum { MOVE_GLOB = 2, MOVE_SHIFT = 3, MOVE_OUTER = 4 };
 
-// StepGlob, CTQMC.F90:4433-4554 (diagonal hybridisation; no user symmetry
-// moves): gen_SpinFlipUpdate / gen_CAFlip / gen_GlobalUpdate_new
+// StepGlob, CTQMC.F90:4433-4554 (diagonal hybridisation):
+// gen_SpinFlipUpdate / gen_CAFlip / gen_SymUpdate / gen_GlobalUpdate_new
 // (Trace.F90:1103-1198), the QN checks perform_spinflip_check_qn /
 // perform_global_check_qn (Trace.F90:1306-1394), globalUpdate
 // (Trace.F90:2126-2188), get_InvFullHybr and get_FullLogDet
@@ -1341,6 +1344,10 @@ static void step_glob(Chain& c) {
     type = GLOB_CAFLIP;
     gu[0] = 1;
     for (int i = 1; i <= n2; ++i) gu[i] = i;
+  } else if (rand < 0.8 && !c.symmoves.empty()) {
+    type = GLOB_USERSYM;  // gen_SymUpdate, Trace.F90:1170-1182
+    int isym = c.rng.randint(1, (int)c.symmoves.size());
+    for (int i = 1; i <= n2; ++i) gu[i] = c.symmoves[isym - 1][i - 1];
   } else {
     type = GLOB_RANDPERM;  // rand_perm (Trace.F90:1083-1099) + randint(0,1)
     for (int i = 1; i <= n2; ++i) gu[i] = i;
@@ -1824,6 +1831,16 @@ void* orc_chain_create(void* model, const Params* p, const double* hybr_fortran)
   c->sign_state.assign(m->ns, 0.0);
   c->contrib_state.assign(m->ns, 0.0);
   c->gleg.assign((size_t)c->nf * std::max(p->nleg, 0), 0.0);
+  if (p->nsym > 0 && p->symmoves) {  // the moves and their inverses
+    int n2 = c->nf;
+    c->symmoves.assign(2 * p->nsym, std::vector<int>(n2, 0));
+    for (int i = 0; i < p->nsym; ++i)
+      for (int j = 0; j < n2; ++j) {
+        int t = p->symmoves[(size_t)i * n2 + j];
+        c->symmoves[i][j] = t;
+        if (t >= 1 && t <= n2) c->symmoves[p->nsym + i][t - 1] = j + 1;
+      }
+  }
   return c;
 }
 void orc_chain_destroy(void* c) { delete (Chain*)c; }

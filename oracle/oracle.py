@@ -28,7 +28,7 @@ class Params(C.Structure):
                 ("ncorr", C.c_int32), ("seed", C.c_int32), ("taudiff_max", C.c_double),
                 ("p_global", C.c_double), ("p_shift", C.c_double), ("p_4op", C.c_double),
                 ("p_outer", C.c_double), ("maxhisto", C.c_int32), ("meas_dm", C.c_int32),
-                ("nleg", C.c_int32)]
+                ("nleg", C.c_int32), ("nsym", C.c_int32), ("symmoves", C.POINTER(C.c_int32))]
 
 
 _lib = None
@@ -144,7 +144,8 @@ class Chain:
     """One Markov chain of the restated reference loop."""
 
     def __init__(self, model, beta, ftau, ntau, seed, taudiff_max=-1.0, ncorr=100,
-                 p_outer=0.0, maxhisto=500, meas_dm=1, p_global=0.0, p_shift=0.0, nleg=0):
+                 p_outer=0.0, maxhisto=500, meas_dm=1, p_global=0.0, p_shift=0.0, nleg=0,
+                 symmoves=None):
         L = lib()
         self.model = model
         nd = model.nd
@@ -157,6 +158,11 @@ class Chain:
         p = Params(beta=beta, nftau=self.nftau, ntau=ntau, ncorr=ncorr, seed=seed,
                    taudiff_max=taudiff_max, p_global=p_global, p_shift=p_shift, p_4op=0.0,
                    p_outer=p_outer, maxhisto=maxhisto, meas_dm=meas_dm, nleg=nleg)
+        self._sym = None
+        if symmoves is not None:
+            self._sym = np.ascontiguousarray(np.atleast_2d(symmoves), np.int32)
+            p.nsym = self._sym.shape[0]
+            p.symmoves = self._sym.ctypes.data_as(C.POINTER(C.c_int32))
         self.params = p
         self.h = L.orc_chain_create(model.h, C.byref(p), _dp(self._ftau.ravel(order="F")))
         self._log = None

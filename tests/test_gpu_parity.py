@@ -27,19 +27,19 @@ def lib():
 
 
 def run_pair(name, beta, tdm, p_outer, nprop, seed, dense=False, qns=None, ntau=50, p_global=0.0,
-             p_shift=0.0):
+             p_shift=0.0, symmoves=None):
     pr = P.config_problem(name, beta=beta)
     q = qns or pr["quantum_numbers"]
     mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
     co = O.Chain(mo, beta, pr["ftau"], ntau, seed=seed, taudiff_max=tdm, p_outer=p_outer,
-                 p_global=p_global, p_shift=p_shift)
+                 p_global=p_global, p_shift=p_shift, symmoves=symmoves)
     co.start_log(nprop)
     co.warmup(nprop)
     ref = co.log()
     mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
     grp = E.Group(beta, pr["ftau"], ntau, nchains=1, seed0=seed, taudiff_max=tdm,
                   p_outer=p_outer, dense=dense, kcap=64, opcap=512, p_global=p_global,
-                  p_shift=p_shift)
+                  p_shift=p_shift, symmoves=symmoves)
     b = E.Batch(mg, [grp])
     b.set_log(nprop)
     b.warmup(nprop)
@@ -111,12 +111,16 @@ GLOBAL_CASES = [
 def test_global_and_shift_move_parity(lib, name, beta, tdm, pout, nprop, seed, dense, qns):
     """Global moves (StepGlob) and tau-shift moves (StepShiftTau) at 5 %
     each, proposal by proposal; the final state and inverse matrices."""
+    # user symmetry moves for the 3-orbital model: a cyclic orbital permutation
+    sym = [[2, 3, 1, 5, 6, 4], [2, 1, 3, 5, 4, 6]] if name == "dd3" else None
     ref, got, co, b = run_pair(name, beta, tdm, pout, nprop, seed, dense=dense, qns=qns,
-                               p_global=0.05, p_shift=0.05)
+                               p_global=0.05, p_shift=0.05, symmoves=sym)
     F = P.config_problem(name, beta=beta)["ftau"][0, 0]
     compare_logs(ref, got, F, beta)
     for mv in (2, 3):
         assert np.sum((ref["move"] == mv) & (ref["outcome"] == 4)) > 0, mv
+    if sym is not None:
+        assert np.sum((ref["move"] == 2) & (ref["orb"] == 2)) > 0  # user symmetry moves drawn
     mc = b.move_counters(0)
     oc = co.counters()
     for key in ("try_glob", "acc_glob", "qn_glob", "try_shift", "acc_shift"):

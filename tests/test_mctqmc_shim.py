@@ -20,7 +20,8 @@ BASE = {"beta": 10.0, "Nd": 3, "Ntau": 40, "NCorr": 50, "Nmeas": 60, "Nwarmups":
         "PercentageGlobalMove": 0.005, "PercentageTauShiftMove": 0.005,
         "Percentage4OperatorMove": 0.0, "PercentageOuterMove": 0.1,
         "PercentageWormInsert": 0.0, "segment": 0, "offdiag": 0, "statesampling": 0,
-        "MeasDensityMatrix": 1, "Eigenbasis": 1, "NLegMax": 10}
+        "MeasDensityMatrix": 1, "Eigenbasis": 1, "NLegMax": 10,
+        "NSymMove": 1, "SymMove01": "2 3 1 5 6 4"}
 
 
 def test_parameter_string_rules():
@@ -40,7 +41,7 @@ def test_parameter_string_rules():
 
 
 @pytest.mark.parametrize("key,val", [("Percentage4OperatorMove", 0.1), ("segment", 1),
-                                     ("NSymMove", 1), ("PercentageWormInsert", 0.1),
+                                     ("PercentageWormInsert", 0.1),
                                      ("offdiag", 1), ("statesampling", 1)])
 def test_unsupported_modes_are_rejected(key, val):
     ctqmc.init_paras(pstring(dict(BASE, **{key: val})))
@@ -78,7 +79,7 @@ def test_solve_through_the_module_matches_the_oracle():
     mo = O.Model(nd, pr["umatrix"], pr["muimp"], "Nt Szt")
     co = O.Chain(mo, 10.0, ftau, ntau, seed=11, taudiff_max=5.0, ncorr=BASE["NCorr"],
                  p_outer=0.1, maxhisto=BASE["MaxHisto"] + 1, p_global=0.005, p_shift=0.005,
-                 nleg=BASE["NLegMax"])
+                 nleg=BASE["NLegMax"], symmoves=[[2, 3, 1, 5, 6, 4]])
     co.set_taudiffmax(5.0)
     co.warmup(BASE["Nwarmups"])
     co.measure(BASE["Nmeas"])

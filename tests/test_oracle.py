@@ -134,13 +134,16 @@ def test_fast_updates_match_full_recompute(name, beta, tdm, pout):
 @pytest.mark.parametrize("name,beta,tdm", [("anderson1", 10.0, 3.0), ("dd3", 8.0, 2.5),
                                             ("dd3", 8.0, 8.0)])
 def test_global_and_shift_moves_keep_state_consistent(name, beta, tdm):
-    """Global moves (spin flip, CA flip, random permutation) and tau-shift
-    moves at 10 % each: trace, determinant and inverse matrices stay equal to
-    a full recompute after every step, and both move kinds are accepted."""
+    """Global moves (spin flip, CA flip, user symmetry moves, random
+    permutation) and tau-shift moves at 10 % each: trace, determinant and
+    inverse matrices stay equal to a full recompute after every step, and
+    both move kinds are accepted."""
     pr = P.config_problem(name, beta=beta)
     m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    # a cyclic orbital permutation (its inverse differs) for the 3-orbital model
+    sym = [[2, 3, 1, 5, 6, 4]] if pr["nd"] == 3 else None
     c = O.Chain(m, pr["beta"], pr["ftau"], 50, seed=23, taudiff_max=tdm, p_outer=0.1,
-                p_global=0.1, p_shift=0.1)
+                p_global=0.1, p_shift=0.1, symmoves=sym)
     acc = {"acc_glob": 0, "acc_shift": 0}
     for i in range(1500):
         c.warmup(1)  # counters restart with every call

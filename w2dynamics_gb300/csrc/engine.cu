@@ -2151,9 +2151,10 @@ __device__ NOINL void rebuilt_trace(Ctx& c, int s0, double& lg, double& sg) {
   }
 }
 
-// StepGlob, CTQMC.F90:4433-4554, without user symmetry moves: spin flip
-// (30 %, gen_SpinFlipUpdate), creator/annihilator flip (30 %, gen_CAFlip),
-// random flavour permutation with random CA flip (gen_GlobalUpdate_new,
+// StepGlob, CTQMC.F90:4433-4554: spin flip (30 %, gen_SpinFlipUpdate),
+// creator/annihilator flip (30 %, gen_CAFlip), a user symmetry move or its
+// inverse (20 % when NSymMove > 0, gen_SymUpdate), otherwise a random
+// flavour permutation with random CA flip (gen_GlobalUpdate_new,
 // rand_perm) (Trace.F90:1083-1198); QN checks perform_spinflip_check_qn /
 // perform_global_check_qn (Trace.F90:1306-1394); full inverse and
 // determinant (get_InvFullHybr) times the LU determinant of the current
@@ -2182,6 +2183,11 @@ __device__ NOINL void ph_global(Ctx& c, Prop& p) {
     type = 4;  // CA flip
     gu[0] = 1;
     for (int i = 1; i <= n2; ++i) gu[i] = i;
+  } else if (u < 0.8 && c.g->nsym > 0) {
+    type = 2;  // user symmetry move or its inverse (gen_SymUpdate)
+    const int isym = randint(c, 1, 2 * c.g->nsym);
+    gu[0] = 0;
+    for (int i = 1; i <= n2; ++i) gu[i] = c.g->symmoves[(size_t)(isym - 1) * n2 + (i - 1)];
   } else {
     type = 1;  // random permutation (Green 1963) and random CA flip
     for (int i = 1; i <= n2; ++i) gu[i] = i;
@@ -3329,6 +3335,7 @@ struct GroupHost {
   double* d_score = nullptr;
   double* d_edges = nullptr;
   long long* d_ekeys = nullptr;
+  int* d_sym = nullptr;
   int* d_seeds = nullptr;
   double* d_tdm = nullptr;
   int chain0 = 0;
@@ -3685,6 +3692,22 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
       G.g.edges = G.d_edges;
       G.g.ekeys = G.d_ekeys;
     }
+    G.g.nsym = 0;
+    G.g.symmoves = nullptr;
+    if (d.nsym > 0 && d.symmoves) {
+      // the moves and their inverses, SymMoves(NSymMove + i, SymMoves(i, j)) = j
+      const int n2 = hm.nf;
+      std::vector<int> sm((size_t)2 * d.nsym * n2);
+      for (int i = 0; i < d.nsym; ++i)
+        for (int j = 0; j < n2; ++j) {
+          const int t = d.symmoves[(size_t)i * n2 + j];
+          sm[(size_t)i * n2 + j] = t;
+          if (t >= 1 && t <= n2) sm[(size_t)(d.nsym + i) * n2 + (t - 1)] = j + 1;
+        }
+      G.d_sym = dev_upload(sm, e);
+      G.g.symmoves = G.d_sym;
+      G.g.nsym = d.nsym;
+    }
     G.g.score_dE = nullptr;
     if (G.g.nscore > 0) {
       std::vector<double> dE(d.score_dE, d.score_dE + (size_t)G.g.nscore * hm.ns);
@@ -3730,6 +3753,7 @@ int cthyb_batch_destroy(cthyb_batch_t B) {
     cudaFree(G.d_score);
     cudaFree(G.d_edges);
     cudaFree(G.d_ekeys);
+    cudaFree(G.d_sym);
     cudaFree(G.d_seeds);
     cudaFree(G.d_tdm);
   }
@@ -4374,6 +4398,8 @@ int cthyb_batch_set_log(cthyb_batch_t B, int64_t cap) {
     G.g.edges = save.edges;
     G.g.ekeys = save.ekeys;
     G.g.score_dE = save.score_dE;
+    G.g.nsym = save.nsym;
+    G.g.symmoves = save.symmoves;
     total += (size_t)G.desc.nchains * G.g.stride;
   }
   char* slab = nullptr;

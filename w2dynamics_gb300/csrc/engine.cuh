@@ -80,6 +80,8 @@ struct DGroup {
   const double* empty_w;  // [nss] normalised empty-trace weights
   const double* edges;    // [2^L + 1] time-bin edges beta * j / 2^L
   const long long* ekeys; // [2^L + 1] their order keys (bit patterns)
+  int nsym;               // user symmetry moves (with their inverses: 2 * nsym rows)
+  const int* symmoves;    // [2 nsym][2 Nd] 1-based target flavours in the reference's order
   int* err_flag;
 };
 

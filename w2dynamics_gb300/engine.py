@@ -43,7 +43,8 @@ class GroupDesc(C.Structure):
                 ("ncorr", C.c_int32), ("p_outer", C.c_double), ("kcap", C.c_int32),
                 ("opcap", C.c_int32), ("tree_levels", C.c_int32), ("maxhisto", C.c_int32),
                 ("flags", C.c_int32), ("p_global", C.c_double), ("p_shift", C.c_double),
-                ("nleg", C.c_int32), ("nscore", C.c_int32), ("score_dE", C.POINTER(C.c_double))]
+                ("nleg", C.c_int32), ("nscore", C.c_int32), ("score_dE", C.POINTER(C.c_double)),
+                ("nsym", C.c_int32), ("symmoves", C.POINTER(C.c_int32))]
 
 
 class EngineError(RuntimeError):
@@ -174,7 +175,8 @@ class Group:
 
     def __init__(self, beta, ftau, ntau, nchains=1, seed0=0, seeds=None, taudiff_max=-1.0,
                  ncorr=100, p_outer=0.0, kcap=0, opcap=0, tree_levels=0, maxhisto=500,
-                 dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0, score_dE=None):
+                 dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0, score_dE=None,
+                 symmoves=None):
         self.beta = float(beta)
         self.ftau = np.asfortranarray(np.asarray(ftau, np.float64))
         self.ntau = int(ntau)
@@ -187,6 +189,9 @@ class Group:
         self.p_global, self.p_shift = float(p_global), float(p_shift)
         self.nleg = int(nleg)
         self.score_dE = None if score_dE is None else np.ascontiguousarray(score_dE, np.float64)
+        # user symmetry moves: rows of 1-based target flavours in the reference's
+        # flavour order (b-1) + Nd*(s-1) + 1
+        self.symmoves = None if symmoves is None else np.ascontiguousarray(np.atleast_2d(symmoves), np.int32)
         self.kcap, self.opcap, self.tree_levels = int(kcap), int(opcap), int(tree_levels)
         self.maxhisto = int(maxhisto)
         self.flags = (FLAG_DENSE if dense else 0) | (0 if measure_dm else FLAG_NO_DM)
@@ -211,6 +216,8 @@ class Group:
         d.nleg = self.nleg
         d.nscore = 0 if self.score_dE is None else self.score_dE.shape[0]
         d.score_dE = _dp(self.score_dE) if self.score_dE is not None else None
+        d.nsym = 0 if self.symmoves is None else self.symmoves.shape[0]
+        d.symmoves = self.symmoves.ctypes.data_as(C.POINTER(C.c_int32)) if self.symmoves is not None else None
         return d
 
 

@@ -33,9 +33,8 @@ their measurements as one longer run would (sign-weighted), the form in
 which the GPU is used efficiently.
 
 Parameters selecting moves or modes outside the engine (4-operator and worm
-moves, user symmetry moves, segment, off-diagonal hybridisation, state
-sampling, retarded interactions) raise NotImplementedError at
-init_solver.  The trace-recomputation histograms lhisto/rhisto describe the
+moves, segment, off-diagonal hybridisation, state sampling, retarded
+interactions) raise NotImplementedError at init_solver.  The trace-recomputation histograms lhisto/rhisto describe the
 reference's list-walking implementation and are returned as zeros; outer
 trace contributions are measured for density-density (monomial) models.  Each init_solver seeds the chains
 from Nseed; the reference continues one global random stream across
@@ -151,7 +150,7 @@ def _check_supported():
     for key in ("Percentage4OperatorMove", "PercentageWormInsert"):
         if _real(key, 0.0) != 0.0:
             bad.append(f"{key} = {_real(key)}")
-    for key in ("segment", "offdiag", "statesampling", "Phonon", "Screening", "Uw", "NSymMove"):
+    for key in ("segment", "offdiag", "statesampling", "Phonon", "Screening", "Uw"):
         if _int(key, 0) != 0:
             bad.append(f"{key} = {_int(key)}")
     if _int("Eigenbasis", 1) == 0:
@@ -188,6 +187,10 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
                     measure_dm=_int("MeasDensityMatrix", 1) != 0,
                     p_global=_real("PercentageGlobalMove", 0.0),
                     p_shift=_real("PercentageTauShiftMove", 0.0), nleg=_int("NLegMax", 100))
+    nsym = _int("NSymMove", 0)
+    if nsym > 0:  # SymMove01 ... (Trace.F90:471-477)
+        group.symmoves = np.array([[int(x) for x in _raw("SymMove%02d" % (i + 1)).split()]
+                                   for i in range(nsym)], np.int32)
     _batch = E.Batch(_model, [group])
     ns = _model.nstates
     statessuperstates = np.zeros(ns, np.int32)
