@@ -392,3 +392,36 @@ def test_ratios_against_dense_lu(lib):
         worst = max(worst, err / (1e-10 + 2e-14 * C[i]))
         if r["outcome"] == 4:
             cfg[f] = (tc2, ta2)
+
+
+def test_capacity_limit_and_invalid_configurations(lib):
+    """Edge cases: a chain that outgrows kcap stops with CTHYB_ERR_CAPACITY
+    reported by sync (no fault, the other chains' results stay readable);
+    set_mc_config rejects unbalanced, out-of-range, colliding (equal-time)
+    and over-capacity configurations with an error code; the empty
+    configuration is accepted."""
+    pr = P.config_problem("dd3", beta=50.0)
+    mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    b = E.Batch(mg, [E.Group(50.0, pr["ftau"], 20, nchains=8, seed0=1, taudiff_max=5.0, kcap=4,
+                             opcap=64)])
+    b.warmup(5000)
+    with pytest.raises(E.EngineError, match="capacity"):
+        b.sync()
+    r = b.results(0)
+    assert r["gtau"].shape == (3, 2, 20)
+    b2 = E.Batch(mg, [E.Group(10.0, P.config_problem("dd3", beta=10.0)["ftau"], 20, nchains=1, seed0=1,
+                              taudiff_max=10.0, kcap=4, opcap=64)])
+    bad = [
+        ([1.0, 2.0], [1, 1], [1, 1], [1, 1], 0),          # unbalanced (two creators)
+        ([1.0, 12.0], [1, 1], [1, 1], [1, 2], 0),         # time beyond beta
+        ([1.0, 1.0], [1, 1], [1, 1], [1, 2], 0),          # equal times
+        ([1.0, 2.0], [4, 4], [1, 1], [1, 2], 0),          # orbital out of range
+        (list(np.arange(1, 11) * 0.9), [1] * 10, [1] * 10, [1, 2] * 5, 0),  # 5 pairs > kcap 4
+    ]
+    for taus, orbs, spins, cas, outer in bad:
+        with pytest.raises(E.EngineError):
+            b2.set_config(0, taus, orbs, spins, cas, outer)
+    b2.set_config(0, [], [], [], [], 0)
+    assert b2.state(0)["noper"] == 0
+    b2.warmup(100)
+    b2.sync()

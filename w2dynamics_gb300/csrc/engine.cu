@@ -4231,6 +4231,9 @@ int cthyb_batch_set_config(cthyb_batch_t B, int chain, int n, const double* taus
     code[i] = 2 * f + (cas[j] - 1);
     per[code[i]]++;
   }
+  for (int i = 0; i < n; ++i)  // times in [0, beta), pairwise distinct
+    if (!(t[i] >= 0.0 && t[i] < G->g.beta) || (i > 0 && !(t[i] > t[i - 1])))
+      return fail(CTHYB_ERR_ARG, "operator times must be distinct and in [0, beta)");
   for (int f = 0; f < hm.nf; ++f) {
     if (per[2 * f] != per[2 * f + 1]) return fail(CTHYB_ERR_ARG, "unbalanced configuration");
     if (per[2 * f] > G->g.kcap) return fail(CTHYB_ERR_CAPACITY, "configuration exceeds kcap");
