@@ -34,6 +34,7 @@ NTAU = 2000
 NCORR = 100
 TDM = 5.0
 THERMALIZE = 2000  # proposals per chain before timing (not timed)
+E2E_WARMUP = 1000  # re-thermalisation proposals per chain of the warm-started end-to-end solve
 TUNE = 200         # of them, per candidate schedule of the autotuner (10 candidates)
 CPU_SAMPLE_MEAS = 100  # measurement cycles per host core and round of the bounded CPU sample
 # dense-block workload (--workload kanamori5): 5-orbital Kanamori with
@@ -42,9 +43,9 @@ K5_BETA, K5_CHAINS, K5_THERM = 40.0, 1024, 2000
 METRIC = "MC updates/sec on 1 GB300, batched vs one-chain form, at equal G(tau) error"
 # From one ncu capture (--set full) of a timed sweep launch of this workload:
 # DRAM bytes read + written, FP64-pipe and issue utilisation.
-TRAFFIC_PER_LAUNCH = 349.6e6
-NCU_FP64_PIPE = 0.477
-NCU_ISSUE_ACTIVE = 0.211
+TRAFFIC_PER_LAUNCH = 383.5e6
+NCU_FP64_PIPE = 0.368
+NCU_ISSUE_ACTIVE = 0.225
 
 
 def workload_desc(chains_per_beta):
@@ -65,37 +66,49 @@ def problems():
 
 
 class ClockSampler:
-    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks/throttle reasons sampled during the timed region:
+    one `nvidia-smi -lms 50` process whose lines a thread collects; entering
+    waits for its first line so that sampling is live when timing starts."""
 
-    def __init__(self):
+    def __init__(self, interval_ms=50):
         self.samples = []
-        self._stop = threading.Event()
+        self.interval_ms = interval_ms
+        self._proc = None
         self._t = None
+        self._first = threading.Event()
 
     def _run(self):
+        for line in self._proc.stdout:
+            v = [x.strip() for x in line.strip().split(",")]
+            if len(v) >= 7:
+                self.samples.append(v)
+                self._first.set()
+        self._first.set()
+
+    def __enter__(self):
         q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
              "clocks_event_reasons.sw_power_cap")
-        while not self._stop.is_set():
-            try:
-                r = subprocess.run(["nvidia-smi", "-i", "0", f"--query-gpu={q}",
-                                    "--format=csv,noheader,nounits"],
-                                   capture_output=True, text=True, timeout=5)
-                v = [x.strip() for x in r.stdout.strip().split(",")]
-                if len(v) >= 7:
-                    self.samples.append(v)
-            except Exception:
-                pass
-            self._stop.wait(0.2)
-
-    def __enter__(self):
+        try:
+            self._proc = subprocess.Popen(["nvidia-smi", "-i", "0", f"--query-gpu={q}",
+                                           "--format=csv,noheader,nounits", f"-lms={self.interval_ms}"],
+                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self._proc = None
+            return self
         self._t = threading.Thread(target=self._run, daemon=True)
         self._t.start()
+        self._first.wait(timeout=10)
         return self
 
     def __exit__(self, *a):
-        self._stop.set()
-        self._t.join(timeout=10)
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=10)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+            self._t.join(timeout=10)
 
     def summary(self):
         if not self.samples:
@@ -261,18 +274,25 @@ def run_gpu(args, rank=0, world=1):
     props = nchains * NCORR * args.steps
     value = props / (ms / 1e3)
     wc = batch.work_counters(reset=False)
+    # the thermalised configurations: what one DMFT iteration hands the next
+    # through mc_config_inout (cthyb_solver.py:329-345)
+    cfg = batch.get_configs()
     batch.close()
-    # End to end through the public API: one solver call as a DMFT iteration
-    # makes it -- model and chains from host arrays (U, mu, F(tau) copied to
-    # the device), thermalisation, then every step a measurement cycle and the
-    # device->host read of every group's G(tau) and sign sums.  All proposals
-    # of the call (thermalisation included) count as updates.
+    # End to end through the public API: one warm-started solver call as a
+    # DMFT iteration makes it -- model and chains from host arrays (U, mu,
+    # F(tau) copied to the device), the previous configurations uploaded in
+    # one call, E2E_WARMUP re-thermalisation proposals per chain, then every
+    # step a measurement cycle and the device->host read of every group's
+    # G(tau) and sign sums, and at the end the configurations read back.  All
+    # proposals of the call count as updates (all at the thermalised order).
     torch.cuda.synchronize()
     if world > 1:
         dist.barrier()
     t0 = time.perf_counter()
     model2, groups2, b2, h2d = build_batch(E, probs, cpb, rank)
-    b2.warmup(THERMALIZE)  # automatic schedule (the autotuner's choice above on this workload)
+    b2.set_configs(*cfg)
+    h2d += sum(a.nbytes for a in cfg)
+    b2.warmup(E2E_WARMUP)  # automatic schedule (the autotuner's choice above on this workload)
     b2.use_graphs(True)
     d2h = 0
     for _ in range(args.steps):
@@ -280,10 +300,12 @@ def run_gpu(args, rank=0, world=1):
         for gi in range(len(groups2)):
             gs, ss, cn = b2.group_sums(gi)
             d2h += gs.nbytes + 16
+    cfg_out = b2.get_configs()
+    d2h += sum(a.nbytes for a in cfg_out)
     b2.sync()
     t_e2e = shard.max_over_ranks(time.perf_counter() - t0)
     b2.close()
-    e2e_value = nchains * (THERMALIZE + NCORR * args.steps) / t_e2e
+    e2e_value = nchains * (E2E_WARMUP + NCORR * args.steps) / t_e2e
     if rank != 0:
         return
     # plain one-chain drop-in form on the same model (beta=50 problem)
@@ -313,8 +335,10 @@ def run_gpu(args, rank=0, world=1):
         "e2e": {"value": e2e_value, "unit": "MC updates/s",
                 "h2d_bytes_per_step": int(h2d) // args.steps,
                 "d2h_bytes_per_step": d2h // args.steps,
-                "timed": f"model+batch creation from host arrays, {THERMALIZE} thermalisation "
-                         f"proposals per chain, {args.steps} steps each with G(tau) sums read back",
+                "timed": f"warm-started solve: model+batch creation from host arrays, upload of "
+                         f"the thermalised configurations, {E2E_WARMUP} re-thermalisation proposals "
+                         f"per chain, {args.steps} steps each with G(tau) sums read back, "
+                         f"configurations read back; bytes per step = per-call bytes / steps",
                 "wall_s": t_e2e},
         "one_chain_form": {"value": single_value, "unit": "MC updates/s",
                            "batched_over_one_chain": value / single_value},

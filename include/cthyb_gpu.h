@@ -213,6 +213,23 @@ int cthyb_batch_get_config(cthyb_batch_t batch, int chain, int* n, double* taus,
  * full inverse hybridisation matrices by LU, trace and sign. */
 int cthyb_batch_set_config(cthyb_batch_t batch, int chain, int n, const double* taus,
                            const int* orbs, const int* spins, const int* cas, int outer_sst);
+/* set_mc_config for the chains chain0 .. chain0 + nset - 1 in one call (the
+ * warm start of cthyb_solver.py:329-332 with mc_config_inout, for a whole
+ * batch): the operators of chain chain0 + i are entries offsets[i] ..
+ * offsets[i + 1] - 1 (offsets[0] = 0) of taus/orbs/spins/cas, its outer
+ * superstate outer_sst[i].  Every configuration is checked before the
+ * first one is written; one upload and one kernel launch per group. */
+int cthyb_batch_set_configs(cthyb_batch_t batch, int chain0, int nset, const int* offsets,
+                            const double* taus, const int* orbs, const int* spins,
+                            const int* cas, const int* outer_sst);
+/* get_mc_config for the chains chain0 .. chain0 + nget - 1 (the
+ * mc_config_inout read-back, cthyb_solver.py:344-345): fills offsets
+ * (nget + 1 entries, as in cthyb_batch_set_configs) and outer_sst (nget,
+ * may be NULL); with all four operator arrays NULL only those, else the
+ * operators, cap being the arrays' length (CTHYB_ERR_CAPACITY if the
+ * total operator count exceeds it). */
+int cthyb_batch_get_configs(cthyb_batch_t batch, int chain0, int nget, int* offsets, int cap,
+                            double* taus, int* orbs, int* spins, int* cas, int* outer_sst);
 /* Inverse hybridisation matrix of one flavour f = 2(b-1)+(s-1) in time
  * order (rows creators, columns annihilators, column-major k x k);
  * returns k in *k. */

@@ -361,6 +361,75 @@ def test_set_config_and_refresh(lib):
     assert dev < 1e-9
 
 
+def test_bulk_configs_warm_start(lib):
+    """cthyb_batch_get_configs / cthyb_batch_set_configs (the mc_config_inout
+    warm start for a whole batch): the bulk read equals the per-chain
+    get_mc_config; configurations moved into a fresh batch of two groups
+    (a range across the group boundary) carry the trace and determinant of
+    the oracle's full rebuild; an invalid chain in the middle of a bulk
+    write is rejected before any chain is written; the warm-started chains
+    keep running with only rounding drift in M."""
+    betas = (10.0, 25.0)
+    pr = {b: P.config_problem("dd3", beta=b) for b in betas}
+    q = pr[10.0]["quantum_numbers"]
+    mg = E.Model(3, pr[10.0]["umatrix"], pr[10.0]["muimp"], q)
+
+    def batch(seed0):
+        return E.Batch(mg, [E.Group(b, pr[b]["ftau"], 20, nchains=6, seed0=seed0 + 100 * i,
+                                    taudiff_max=5.0, kcap=64, opcap=512, p_outer=0.1)
+                            for i, b in enumerate(betas)])
+
+    a = batch(1)
+    a.warmup(3000)
+    a.sync()
+    offs, t, o, s, c, outer = a.get_configs()
+    assert len(offs) == 13 and offs[-1] > 0
+    for ch in range(12):
+        tg, og, sg_, cg, outg = a.get_config(ch)
+        sl = slice(offs[ch], offs[ch + 1])
+        assert np.array_equal(tg, t[sl]) and np.array_equal(og, o[sl])
+        assert np.array_equal(sg_, s[sl]) and np.array_equal(cg, c[sl]) and outg == outer[ch]
+    b = batch(7)
+    b.set_configs(offs, t, o, s, c, outer)
+    o2 = b.get_configs()
+    for x, y in zip(o2, (offs, t, o, s, c, outer)):
+        assert np.array_equal(x, y)
+    mo = O.Model(3, pr[10.0]["umatrix"], pr[10.0]["muimp"], q)
+    for ch in range(12):
+        beta = betas[ch // 6]
+        co = O.Chain(mo, beta, pr[beta]["ftau"], 20, seed=0, taudiff_max=5.0)
+        sl = slice(offs[ch], offs[ch + 1])
+        co.set_config(t[sl], o[sl], s[sl], c[sl], int(outer[ch]))
+        ft, fd = co.full_trace(), co.full_det()
+        st = b.state(ch)
+        assert abs(st["trace_log"] - ft[0]) < 1e-10 * max(1, abs(ft[0])) and st["trace_sign"] == ft[1]
+        assert abs(st["det_log"] - fd[0]) < 1e-10 * max(1, abs(fd[0])) and st["det_sign"] == fd[1]
+        sa = a.state(ch)
+        assert st["cfgsign"] == sa["cfgsign"] and st["noper"] == sa["noper"]
+    # chains 4..9 (groups 0 and 1) with chain 7's configuration made invalid
+    sub = slice(offs[4], offs[10])
+    t_bad = t[sub].copy()
+    k7 = offs[7] - offs[4]
+    n7 = offs[8] - offs[7]
+    before = b.get_configs()
+    if n7 >= 2:
+        t_bad[k7 + 1] = t_bad[k7]  # two operators at one time
+    else:
+        t_bad[k7] = betas[1] + 1.0  # beyond beta
+    with pytest.raises(E.EngineError):
+        b.set_configs(offs[4:11] - offs[4], t_bad, o[sub], s[sub], c[sub], outer[4:10], chain0=4)
+    after = b.get_configs()
+    for x, y in zip(after, before):
+        assert np.array_equal(x, y)
+    # the same range, valid: written across the group boundary in one call
+    b.set_configs(offs[4:11] - offs[4], t[sub], o[sub], s[sub], c[sub], outer[4:10], chain0=4)
+    for x, y in zip(b.get_configs(), (offs, t, o, s, c, outer)):
+        assert np.array_equal(x, y)
+    b.warmup(2000)
+    b.sync()
+    assert b.refresh_minv(replace=False) < 1e-9
+
+
 def test_ratios_against_dense_lu(lib):
     """Every determinant ratio of a GPU run against det(H_new)/det(H_old)
     from dense LU (numpy.linalg.slogdet) of the rebuilt hybridisation
@@ -410,13 +479,13 @@ def test_capacity_limit_and_invalid_configurations(lib):
     r = b.results(0)
     assert r["gtau"].shape == (3, 2, 20)
     b2 = E.Batch(mg, [E.Group(10.0, P.config_problem("dd3", beta=10.0)["ftau"], 20, nchains=1, seed0=1,
-                              taudiff_max=10.0, kcap=4, opcap=64)])
+                              taudiff_max=10.0, kcap=16, opcap=64)])
     bad = [
         ([1.0, 2.0], [1, 1], [1, 1], [1, 1], 0),          # unbalanced (two creators)
         ([1.0, 12.0], [1, 1], [1, 1], [1, 2], 0),         # time beyond beta
         ([1.0, 1.0], [1, 1], [1, 1], [1, 2], 0),          # equal times
         ([1.0, 2.0], [4, 4], [1, 1], [1, 2], 0),          # orbital out of range
-        (list(np.arange(1, 11) * 0.9), [1] * 10, [1] * 10, [1, 2] * 5, 0),  # 5 pairs > kcap 4
+        (list(np.arange(1, 35) * 0.25), [1] * 34, [1] * 34, [1, 2] * 17, 0),  # 17 pairs > kcap 16
     ]
     for taus, orbs, spins, cas, outer in bad:
         with pytest.raises(E.EngineError):

@@ -3171,16 +3171,32 @@ __device__ void rebuild_minv(Ctx& c, double* maxdev, bool replace, double& dlog,
   }
 }
 
-__global__ void __launch_bounds__(WPB * 32) k_set_config(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
-                                                        int chain, int outer_sst) {
+// set_mc_config for chains chain0 .. chain0 + nset - 1 of a group, one warp
+// per chain: chain chain0 + w takes the time-ordered operators
+// offs[w] .. offs[w + 1] (codes 2f + ca) and outer superstate outers[w] from
+// the staging arrays, then rebuilds the per-flavour lists, the tree, the
+// trace, the inverse hybridisation matrices and the sign.
+__global__ void __launch_bounds__(WPB * 32) k_set_configs(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
+                                                         int chain0, int nset, const int* __restrict__ offs,
+                                                         const double* __restrict__ taus,
+                                                         const int* __restrict__ codes,
+                                                         const int* __restrict__ outers) {
   __shared__ Hdr hs[WPB];
-  int warp = threadIdx.x >> 5;
-  if (warp != 0) return;
-  Ctx c = make_ctx(&m, &g, &hs[0], chain);
+  const int warp = threadIdx.x >> 5;
+  const int w = blockIdx.x * WPB + warp;
+  if (w >= nset) return;
+  const int chain = chain0 + w;
+  Ctx c = make_ctx(&m, &g, &hs[warp], chain);
   Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
   load_hdr(c.h, gh, c.lane);
   Hdr& h = *c.h;
-  const int K = h.K;
+  const int o0 = offs[w], K = offs[w + 1] - o0, outer_sst = outers[w];
+  for (int i = c.lane; i < K; i += 32) {
+    c.optau[i] = taus[o0 + i];
+    c.opcode[i] = codes[o0 + i];
+  }
+  if (c.lane == 0) h.K = K;
+  __syncwarp();
   // per-flavour sorted arrays, slot = rank
   for (int f = 0; f < m.nf; ++f) {
     for (int ca = 0; ca < 2; ++ca) {
@@ -3231,6 +3247,35 @@ __global__ void __launch_bounds__(WPB * 32) k_set_config(const __grid_constant__
   double sgn = config_sign(c);
   if (c.lane == 0) h.cfgsign = -sgn;
   store_hdr(gh, c.h, c.lane);
+}
+
+// get_mc_config for chains chain0 .. chain0 + n - 1 of a group, one warp per
+// chain: with offs == nullptr the operator counts and outer superstates,
+// else the time-ordered operators of chain chain0 + w into
+// taus/codes[offs[w] ..].
+__global__ void __launch_bounds__(WPB * 32) k_get_configs(const __grid_constant__ DGroup g, int chain0, int n,
+                                                         const int* __restrict__ offs, int* __restrict__ counts,
+                                                         int* __restrict__ outers, double* __restrict__ taus,
+                                                         int* __restrict__ codes) {
+  const int w = blockIdx.x * WPB + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const char* base = g.base + (size_t)(chain0 + w) * g.stride;
+  const Hdr* gh = (const Hdr*)(base + g.o_hdr);
+  const int K = gh->K;
+  if (!offs) {
+    if (lane == 0) {
+      counts[w] = K;
+      outers[w] = gh->outer_sst;
+    }
+    return;
+  }
+  const double* ot = (const double*)(base + g.o_optau);
+  const int* oc = (const int*)(base + g.o_opcode);
+  const int o0 = offs[w];
+  for (int i = lane; i < K; i += 32) {
+    taus[o0 + i] = ot[i];
+    codes[o0 + i] = oc[i];
+  }
 }
 
 __global__ void __launch_bounds__(WPB * 32) k_refresh(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
@@ -4207,50 +4252,171 @@ int cthyb_batch_get_config(cthyb_batch_t B, int chain, int* n, double* taus, int
   return CTHYB_OK;
 }
 
-int cthyb_batch_set_config(cthyb_batch_t B, int chain, int n, const double* taus, const int* orbs,
-                           const int* spins, const int* cas, int outer_sst) {
-  GroupHost* G;
-  int c;
-  int rc = find_chain(B, chain, &G, &c);
-  if (rc) return rc;
+// Checks one chain's configuration (get_mc_config layout, 1-based orbital,
+// spin and creator/annihilator indices) and appends it, time ordered, as
+// operator codes 2f + ca to the staging arrays.
+static int stage_config(cthyb_batch_t B, const GroupHost* G, int n, const double* taus, const int* orbs,
+                        const int* spins, const int* cas, int outer_sst, std::vector<double>& t,
+                        std::vector<int>& code) {
   const HostModel& hm = B->model->hm;
   if (n < 0 || n > G->g.opcap || outer_sst < 0 || outer_sst >= hm.nss)
     return fail(CTHYB_ERR_ARG, "configuration exceeds capacity or bad superstate");
   std::vector<int> idx(n);
   for (int i = 0; i < n; ++i) idx[i] = i;
   std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return taus[a] < taus[b]; });
-  std::vector<double> t(n);
-  std::vector<int> code(n);
   std::vector<int> per(hm.nf * 2, 0);
+  const size_t o = t.size();
   for (int i = 0; i < n; ++i) {
     int j = idx[i];
     if (orbs[j] < 1 || orbs[j] > hm.nd || spins[j] < 1 || spins[j] > 2 || cas[j] < 1 || cas[j] > 2)
       return fail(CTHYB_ERR_ARG, "bad operator");
-    t[i] = taus[j];
-    int f = 2 * (orbs[j] - 1) + (spins[j] - 1);
-    code[i] = 2 * f + (cas[j] - 1);
-    per[code[i]]++;
-  }
-  for (int i = 0; i < n; ++i)  // times in [0, beta), pairwise distinct
-    if (!(t[i] >= 0.0 && t[i] < G->g.beta) || (i > 0 && !(t[i] > t[i - 1])))
+    const double tj = taus[j];
+    if (!(tj >= 0.0 && tj < G->g.beta) || (i > 0 && !(tj > t[o + i - 1])))  // in [0, beta), distinct
       return fail(CTHYB_ERR_ARG, "operator times must be distinct and in [0, beta)");
+    t.push_back(tj);
+    int f = 2 * (orbs[j] - 1) + (spins[j] - 1);
+    code.push_back(2 * f + (cas[j] - 1));
+    per[code.back()]++;
+  }
   for (int f = 0; f < hm.nf; ++f) {
     if (per[2 * f] != per[2 * f + 1]) return fail(CTHYB_ERR_ARG, "unbalanced configuration");
     if (per[2 * f] > G->g.kcap) return fail(CTHYB_ERR_CAPACITY, "configuration exceeds kcap");
   }
-  Hdr h;
-  rc = read_hdr(B, G, c, h);
-  if (rc) return rc;
-  h.K = n;
-  char* base = G->g.base + (size_t)c * G->g.stride;
-  if (n) {
-    CK(cudaMemcpy(base + G->g.o_optau, t.data(), n * 8, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(base + G->g.o_opcode, code.data(), n * 4, cudaMemcpyHostToDevice));
+  return CTHYB_OK;
+}
+
+// Uploads the staged configurations of chains c0 .. c0 + n - 1 of one group
+// (one copy per array) and rebuilds them with k_set_configs.
+static int upload_configs(cthyb_batch_t B, GroupHost* G, int c0, int n, const std::vector<int>& offs,
+                          const std::vector<double>& t, const std::vector<int>& code,
+                          const std::vector<int>& outer) {
+  const size_t nop = t.size();
+  const size_t bytes = (offs.size() + outer.size() + nop) * 4 + nop * 8 + 16;
+  char* d = nullptr;
+  CK(cudaMalloc(&d, bytes));
+  double* dt = (double*)d;
+  int* dcode = (int*)(d + nop * 8);
+  int* doffs = dcode + nop;
+  int* douter = doffs + offs.size();
+  cudaError_t e = cudaSuccess;
+  if (nop) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dt, t.data(), nop * 8, cudaMemcpyHostToDevice, B->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dcode, code.data(), nop * 4, cudaMemcpyHostToDevice, B->stream);
   }
-  CK(cudaMemcpy(base + G->g.o_hdr, &h, sizeof(Hdr), cudaMemcpyHostToDevice));
-  k_set_config<<<1, 32, 0, B->stream>>>(B->model->dm, G->g, c, outer_sst);
-  CK(cudaGetLastError());
+  if (e == cudaSuccess) e = cudaMemcpyAsync(doffs, offs.data(), offs.size() * 4, cudaMemcpyHostToDevice, B->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(douter, outer.data(), outer.size() * 4, cudaMemcpyHostToDevice, B->stream);
+  if (e == cudaSuccess) {
+    k_set_configs<<<(n + WPB - 1) / WPB, WPB * 32, 0, B->stream>>>(B->model->dm, G->g, c0, n, doffs, dt, dcode, douter);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+  cudaFree(d);
+  CK(e);
+  return CTHYB_OK;
+}
+
+int cthyb_batch_get_configs(cthyb_batch_t B, int chain0, int nget, int* offsets, int cap, double* taus,
+                            int* orbs, int* spins, int* cas, int* outer_sst) {
+  if (!B || nget < 0 || chain0 < 0 || chain0 + nget > B->nchains || !offsets)
+    return fail(CTHYB_ERR_ARG, "bad chain range or offsets");
   CK(cudaStreamSynchronize(B->stream));
+  // segments of consecutive chains in one group
+  struct Seg { GroupHost* G; int c0, i0, n; };
+  std::vector<Seg> segs;
+  for (int i = 0; i < nget; ++i) {
+    GroupHost* G;
+    int c;
+    int rc = find_chain(B, chain0 + i, &G, &c);
+    if (rc) return rc;
+    if (segs.empty() || segs.back().G != G) segs.push_back(Seg{G, c, i, 0});
+    segs.back().n++;
+  }
+  std::vector<int> cnt(nget), out(nget);
+  int* d = nullptr;
+  CK(cudaMalloc(&d, (size_t)(2 * nget + 2) * 4));
+  cudaError_t e = cudaSuccess;
+  for (const Seg& sg : segs) {
+    if (e != cudaSuccess) break;
+    k_get_configs<<<(sg.n + WPB - 1) / WPB, WPB * 32, 0, B->stream>>>(sg.G->g, sg.c0, sg.n, nullptr, d + sg.i0,
+                                                                      d + nget + sg.i0, nullptr, nullptr);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(cnt.data(), d, (size_t)nget * 4, cudaMemcpyDeviceToHost, B->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out.data(), d + nget, (size_t)nget * 4, cudaMemcpyDeviceToHost, B->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+  cudaFree(d);
+  CK(e);
+  offsets[0] = 0;
+  for (int i = 0; i < nget; ++i) offsets[i + 1] = offsets[i] + cnt[i];
+  if (outer_sst)
+    for (int i = 0; i < nget; ++i) outer_sst[i] = out[i];
+  if (!taus && !orbs && !spins && !cas) return CTHYB_OK;
+  const int nop = offsets[nget];
+  if (nop > cap) return fail(CTHYB_ERR_CAPACITY, "output arrays smaller than the operator count");
+  if (nop == 0) return CTHYB_OK;
+  std::vector<double> t(nop);
+  std::vector<int> code(nop);
+  char* db = nullptr;
+  CK(cudaMalloc(&db, (size_t)nop * 12 + (size_t)(nget + 1) * 4 + 16));
+  double* dt = (double*)db;
+  int* dc = (int*)(db + (size_t)nop * 8);
+  int* doffs = dc + nop;
+  e = cudaMemcpyAsync(doffs, offsets, (size_t)(nget + 1) * 4, cudaMemcpyHostToDevice, B->stream);
+  for (const Seg& sg : segs) {
+    if (e != cudaSuccess) break;
+    k_get_configs<<<(sg.n + WPB - 1) / WPB, WPB * 32, 0, B->stream>>>(sg.G->g, sg.c0, sg.n, doffs + sg.i0, nullptr,
+                                                                      nullptr, dt, dc);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(t.data(), dt, (size_t)nop * 8, cudaMemcpyDeviceToHost, B->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(code.data(), dc, (size_t)nop * 4, cudaMemcpyDeviceToHost, B->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+  cudaFree(db);
+  CK(e);
+  for (int i = 0; i < nop; ++i) {
+    if (taus) taus[i] = t[i];
+    const int f = code[i] >> 1;
+    if (orbs) orbs[i] = f / 2 + 1;
+    if (spins) spins[i] = f % 2 + 1;
+    if (cas) cas[i] = (code[i] & 1) + 1;
+  }
+  return CTHYB_OK;
+}
+
+int cthyb_batch_set_config(cthyb_batch_t B, int chain, int n, const double* taus, const int* orbs,
+                           const int* spins, const int* cas, int outer_sst) {
+  const int offs[2] = {0, n};
+  return cthyb_batch_set_configs(B, chain, 1, offs, taus, orbs, spins, cas, &outer_sst);
+}
+
+int cthyb_batch_set_configs(cthyb_batch_t B, int chain0, int nset, const int* offsets, const double* taus,
+                            const int* orbs, const int* spins, const int* cas, const int* outer_sst) {
+  if (!B || nset < 0 || chain0 < 0 || chain0 + nset > B->nchains || !offsets || !outer_sst || offsets[0] != 0)
+    return fail(CTHYB_ERR_ARG, "bad chain range or offsets");
+  for (int i = 0; i < nset; ++i)
+    if (offsets[i + 1] < offsets[i]) return fail(CTHYB_ERR_ARG, "offsets must not decrease");
+  if (offsets[nset] > 0 && (!taus || !orbs || !spins || !cas)) return fail(CTHYB_ERR_ARG, "null operator arrays");
+  // check every configuration before the first device write
+  struct Seg { GroupHost* G; int c0, i0, n; std::vector<double> t; std::vector<int> code, offs, outer; };
+  std::vector<Seg> segs;
+  for (int i = 0; i < nset; ++i) {
+    GroupHost* G;
+    int c;
+    int rc = find_chain(B, chain0 + i, &G, &c);
+    if (rc) return rc;
+    if (segs.empty() || segs.back().G != G) segs.push_back(Seg{G, c, i, 0, {}, {}, {0}, {}});
+    Seg& sg = segs.back();
+    const int o = offsets[i], n = offsets[i + 1] - offsets[i];
+    rc = stage_config(B, G, n, taus + o, orbs + o, spins + o, cas + o, outer_sst[i], sg.t, sg.code);
+    if (rc) return rc;
+    sg.offs.push_back((int)sg.t.size());
+    sg.outer.push_back(outer_sst[i]);
+    sg.n++;
+  }
+  for (Seg& sg : segs) {
+    int rc = upload_configs(B, sg.G, sg.c0, sg.n, sg.offs, sg.t, sg.code, sg.outer);
+    if (rc) return rc;
+  }
   return CTHYB_OK;
 }
 

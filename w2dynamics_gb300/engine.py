@@ -30,7 +30,7 @@ EXPORTS = (
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
     "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_autotune", "cthyb_batch_results",
     "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
-    "cthyb_batch_set_config", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
+    "cthyb_batch_set_config", "cthyb_batch_set_configs", "cthyb_batch_get_configs", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
     "cthyb_minv_rebuild_noalloc",
 )
@@ -99,6 +99,8 @@ def load(build_if_missing=False):
     L.cthyb_batch_state.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_get_config.argtypes = [vp, C.c_int, ip, dp, ip, ip, ip, ip]
     L.cthyb_batch_set_config.argtypes = [vp, C.c_int, C.c_int, dp, ip, ip, ip, C.c_int]
+    L.cthyb_batch_set_configs.argtypes = [vp, C.c_int, C.c_int, ip, dp, ip, ip, ip, ip]
+    L.cthyb_batch_get_configs.argtypes = [vp, C.c_int, C.c_int, ip, C.c_int, dp, ip, ip, ip, ip]
     L.cthyb_batch_minv.argtypes = [vp, C.c_int, C.c_int, ip, dp]
     L.cthyb_batch_refresh_minv.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_set_log.argtypes = [vp, i64]
@@ -384,6 +386,35 @@ class Batch:
         c = np.ascontiguousarray(cas, np.int32)
         _check(load().cthyb_batch_set_config(self.h, chain, len(t), _dp(t), _ip(o), _ip(s),
                                              _ip(c), int(outer_sst)))
+
+    def get_configs(self, chain0=0, n=None):
+        """Configurations of chains chain0 .. chain0 + n - 1 in one call:
+        (offsets, taus, orbs, spins, cas, outer_sst) with chain chain0 + i's
+        operators at offsets[i] .. offsets[i + 1] - 1 (1-based orbitals,
+        spins and creator/annihilator flags as get_mc_config)."""
+        n = self.nchains - chain0 if n is None else int(n)
+        offs = np.zeros(n + 1, np.int32)
+        outer = np.zeros(max(n, 1), np.int32)
+        _check(load().cthyb_batch_get_configs(self.h, chain0, n, _ip(offs), 0, None, None, None, None,
+                                              _ip(outer)))
+        nop = int(offs[-1])
+        t = np.zeros(max(nop, 1))
+        o, s, c = (np.zeros(max(nop, 1), np.int32) for _ in range(3))
+        _check(load().cthyb_batch_get_configs(self.h, chain0, n, _ip(offs), len(t), _dp(t), _ip(o),
+                                              _ip(s), _ip(c), _ip(outer)))
+        return offs, t[:nop], o[:nop], s[:nop], c[:nop], outer[:n]
+
+    def set_configs(self, offsets, taus, orbs, spins, cas, outer_sst, chain0=0):
+        """set_mc_config of chains chain0 .. chain0 + len(outer_sst) - 1 in
+        one call, in the layout get_configs returns."""
+        offs = np.ascontiguousarray(offsets, np.int32)
+        outer = np.ascontiguousarray(outer_sst, np.int32)
+        if len(offs) != len(outer) + 1:
+            raise ValueError("offsets must have one entry more than outer_sst")
+        t = np.ascontiguousarray(taus, np.float64)
+        o, s, c = (np.ascontiguousarray(a, np.int32) for a in (orbs, spins, cas))
+        _check(load().cthyb_batch_set_configs(self.h, chain0, len(outer), _ip(offs), _dp(t), _ip(o),
+                                              _ip(s), _ip(c), _ip(outer)))
 
     def minv(self, chain, f):
         k = C.c_int()
