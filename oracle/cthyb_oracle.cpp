@@ -1759,14 +1759,18 @@ void orc_model_sst(void* mm, int* nst, int* offset, int* states, double* evals) 
     }
   }
 }
+static bool model_args_ok(const Model* m, int sst, int b, int s, int ca) {
+  return sst >= 0 && sst < (int)m->nst.size() && b >= 0 && b < m->nd && s >= 0 && s < 2 && ca >= 0 && ca < 2;
+}
 int orc_model_connect(void* mm, int sst, int b, int s, int ca) {
   Model* m = (Model*)mm;
+  if (!model_args_ok(m, sst, b, s, ca)) return -1;
   return m->conn(sst, b, s, ca);
 }
 // c/c+ block in the eigenbasis (column-major rows x cols); returns 0 or -1
 int orc_model_psis_eb(void* mm, int sst, int b, int s, int ca, double* out, int* rows, int* cols) {
   Model* m = (Model*)mm;
-  if (m->conn(sst, b, s, ca) < 0) return -1;
+  if (!model_args_ok(m, sst, b, s, ca) || m->conn(sst, b, s, ca) < 0) return -1;
   const Block& B = m->peb(sst, b, s, ca);
   *rows = B.rows;
   *cols = B.cols;
@@ -1775,6 +1779,7 @@ int orc_model_psis_eb(void* mm, int sst, int b, int s, int ca, double* out, int*
 }
 int orc_model_evec(void* mm, int sst, double* out) {
   Model* m = (Model*)mm;
+  if (sst < 0 || sst >= (int)m->evec.size()) return -1;
   std::memcpy(out, m->evec[sst].a.data(), m->evec[sst].a.size() * sizeof(double));
   return 0;
 }

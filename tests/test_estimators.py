@@ -57,7 +57,8 @@ def _block_formulas(nd, mo, dm):
     for s in range(len(size)):
         evec[off[s]:off[s] + size[s], off[s]:off[s] + size[s]] = mo.evec(s)
     rho2_some = {}
-    for (f4, f3, f2, f1) in ((0, 1, 1, 0), (1, 0, 1, 0), (2, 3, 3, 2), (0, 2, 2, 0)):
+    picks = ((0, 1, 1, 0), (1, 0, 1, 0), (2, 3, 3, 2), (0, 2, 2, 0))
+    for (f4, f3, f2, f1) in (p for p in picks if max(p) < nf):
         acc = 0.0
         for s in range(len(size)):
             n1 = conn(s, f1, 1)
@@ -112,3 +113,71 @@ def test_ladder_tables_anticommute():
         for g in range(4):
             ac = mat(f, 1) @ mat(g, 0) + mat(g, 0) @ mat(f, 1)
             assert np.allclose(ac, np.eye(ns) * (f == g))
+
+
+def _s2_block_formula(nd, mo, dm):
+    """<S^2> per electron number the reference's way: S^2 = S+S-/2 + S-S+/2
+    + Sz^2 built block by block from the eigenbasis ladder operators along
+    the superstate connections (Operator.F90:548-633), then the trace of
+    rho_block S^2_block per superstate (CTQMC.F90:2811-2838)."""
+    off, size = mo.sst_offset, mo.sst_size
+    ssq = np.zeros(2 * nd + 1)
+
+    def walk(s, ops):
+        """Matrix of the product `ops` ((f, ca), last first) from block s
+        back to block s, or None if it leaves the block or is forbidden."""
+        cur, mat = s, np.eye(size[s])
+        for f, ca in reversed(ops):
+            nxt = mo.connect(cur, f // 2, f % 2, ca)
+            if nxt < 0:
+                return None
+            mat = mo.psis_eb(cur, f // 2, f % 2, ca) @ mat
+            cur = nxt
+        return mat if cur == s else None
+
+    for s in range(len(size)):
+        s2 = np.zeros((size[s], size[s]))
+        for b in range(nd):
+            for b2 in range(nd):
+                up, dn, up2, dn2 = 2 * b, 2 * b + 1, 2 * b2, 2 * b2 + 1
+                for ops in ([(up, 0), (dn, 1), (dn2, 0), (up2, 1)],
+                            [(dn, 0), (up, 1), (up2, 0), (dn2, 1)]):
+                    m = walk(s, ops)
+                    if m is not None:
+                        s2 += 0.5 * m
+                for ops, w in (([(up, 0), (up, 1), (up2, 0), (up2, 1)], 0.25),
+                               ([(dn, 0), (dn, 1), (dn2, 0), (dn2, 1)], 0.25),
+                               ([(up, 0), (up, 1), (dn2, 0), (dn2, 1)], -0.25),
+                               ([(dn, 0), (dn, 1), (up2, 0), (up2, 1)], -0.25)):
+                    m = walk(s, ops)
+                    if m is not None:
+                        s2 += w * m
+        ne = bin(int(mo.fock_states[off[s]])).count("1")
+        blk = dm[off[s]:off[s] + size[s], off[s]:off[s] + size[s]]
+        ssq[ne] += float(np.trace(blk @ s2))
+    return ssq
+
+
+@pytest.mark.parametrize("name", ["anderson1", "dd3"])
+def test_spin_square_matches_block_formula(name):
+    """ssquare from the occupation-basis density matrix equals the
+    reference's eigenbasis block evaluation on an oracle-measured density
+    matrix; the S^2 operator has eigenvalues S(S+1) and its infinite-
+    temperature mean is 3 Nd / 8."""
+    pr, mo, dm = _oracle_dm(name, 10.0, 400)
+    nd = pr["nd"]
+    evec = np.zeros_like(dm)
+    for s in range(len(mo.sst_size)):
+        o, n = mo.sst_offset[s], mo.sst_size[s]
+        evec[o:o + n, o:o + n] = mo.evec(s)
+    rho = evec @ dm @ evec.T
+    ssq, op = ES.spin_square(nd, mo.fock_states, mo.sst_size, mo.sst_offset, rho)
+    ref = _s2_block_formula(nd, mo, dm)
+    assert np.allclose(ssq, ref, atol=1e-12)
+    assert ssq.sum() > 0.0
+    ev = np.linalg.eigvalsh(op)
+    twice_s = -1.0 + np.sqrt(1.0 + 4.0 * ev)
+    assert np.allclose(twice_s, np.round(twice_s), atol=1e-9)
+    flat, _ = ES.spin_square(nd, mo.fock_states, mo.sst_size, mo.sst_offset,
+                             np.eye(mo.nstates) / mo.nstates)
+    assert abs(flat.sum() - 3.0 * nd / 8.0) < 1e-12

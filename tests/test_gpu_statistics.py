@@ -3,13 +3,17 @@
 1. G(tau), occupancies and double occupancies of a batch of GPU chains fall
    within the statistical error of an oracle (CPU) run with the same total
    number of samples but different seeds.
-2. Equal error at equal samples: the G(tau) error of a batch of n chains and
+2. Detailed balance: the expansion-order histogram and occupations of GPU
+   chains on a single-orbital impurity with a discrete asymmetric bath equal
+   exact diagonalisation of impurity + bath.
+3. Equal error at equal samples: the G(tau) error of a batch of n chains and
    of one chain run n times longer agree, so MC updates/s of the two forms
    compare at equal statistical error.
 """
 import numpy as np
 import pytest
 
+import exact_bath as XB
 import oracle as O
 from w2dynamics_gb300 import engine as E
 from w2dynamics_gb300 import estimators as ES
@@ -102,3 +106,37 @@ def test_equal_error_batched_and_one_chain_forms():
     assert 0.5 < ratio < 2.0, ratio
     zz = (batched.mean(axis=0) - blocks.mean(axis=0)) / np.sqrt(err_b ** 2 + err_1 ** 2)
     assert np.abs(zz).max() < 4.5
+
+
+def test_detailed_balance_against_exact_diagonalisation():
+    """64 GPU chains (sliding windows, outer-superstate, global and tau-shift
+    moves) of the single-orbital impurity with two bath levels: per-flavour
+    order histogram and occupations within 4.5 standard errors of the exact
+    values (tests/exact_bath.py)."""
+    beta, mu, u, eps, v = 4.0, 1.3, 2.0, [-0.6, 0.9], [0.6, 0.8]
+    pex = XB.order_marginal(beta, mu, u, eps, v)[:30]
+    nup, ndn, dbl = XB.occupations(beta, mu, u, eps, v)
+    um = P.flat_umatrix(P.umatrix_density(1, u, u, 0.0))
+    f = XB.ftau_bath(beta, eps, v, 2000)
+    mg = E.Model(1, um, P.muimp_solver(1, mu), "Nt Szt Azt")
+    fk, evec = mg.basis()
+    n = 64
+    b = E.Batch(mg, [E.Group(beta, np.broadcast_to(f, (1, 2, 2000)).copy(), 20, nchains=n, seed0=500,
+                             taudiff_max=1.0, ncorr=20, kcap=32, opcap=128, maxhisto=30, p_outer=0.1,
+                             p_global=0.01, p_shift=0.01)])
+    b.warmup(2000)
+    b.measure(5000)
+    b.sync()
+    hist, occ = [], []
+    for c in range(n):
+        r = b.results(c)
+        h = r["histo"].reshape(2, -1)
+        hist.append(h / h.sum(axis=1, keepdims=True))
+        o = ES.from_density_matrix(1, fk, evec, r["densitymatrix"])["occ"]
+        occ.append([o[0, 0, 0, 0], o[0, 1, 0, 1], o[0, 0, 0, 1]])
+    hist, occ = np.array(hist), np.array(occ)
+    sel = pex > 1e-3
+    z = (hist.mean(0)[:, sel] - pex[sel]) / (hist.std(0, ddof=1)[:, sel] / np.sqrt(n))
+    assert np.abs(z).max() < 4.5, z
+    zo = (occ.mean(0) - [nup, ndn, dbl]) / (occ.std(0, ddof=1) / np.sqrt(n))
+    assert np.abs(zo).max() < 4.5, zo

@@ -20,7 +20,7 @@ BASE = {"beta": 10.0, "Nd": 3, "Ntau": 40, "NCorr": 50, "Nmeas": 60, "Nwarmups":
         "PercentageGlobalMove": 0.005, "PercentageTauShiftMove": 0.005,
         "Percentage4OperatorMove": 0.0, "PercentageOuterMove": 0.1,
         "PercentageWormInsert": 0.0, "segment": 0, "offdiag": 0, "statesampling": 0,
-        "MeasDensityMatrix": 1, "Eigenbasis": 1, "NLegMax": 10,
+        "MeasDensityMatrix": 1, "MeasSsquare": 1, "Eigenbasis": 1, "NLegMax": 10,
         "NSymMove": 1, "SymMove01": "2 3 1 5 6 4"}
 
 
@@ -97,6 +97,9 @@ def test_solve_through_the_module_matches_the_oracle():
     assert np.allclose(ctqmc.densitymatrix, ref["densitymatrix"], atol=1e-10)
     assert np.allclose(ctqmc.occ, ref["occ"], atol=1e-10)
     assert np.allclose(ctqmc.rho1, ref["rho1"], atol=1e-10)
+    ssq, _ = ES.spin_square(nd, mo.fock_states, mo.sst_size, mo.sst_offset, ref["densitymatrix"])
+    assert np.allclose(ctqmc.ssquare, ssq, atol=1e-10)
+    assert ctqmc.ssquare_operator.shape == (mo.nstates, mo.nstates)
     assert ctqmc.gtau_full.shape == (nd, 2, nd, 2, ntau)
     xo = co.results_extra()
     gl = np.stack([ctqmc.gleg[f // 2, f % 2] for f in range(2 * nd)])

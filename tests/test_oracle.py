@@ -12,14 +12,19 @@
 * operator-list invariants of testsuite/ctqmc.tests/3-operator-list-stress-
   test.F90 with a fixed seed.
 * physics known answers: U=0 impurity G(tau) equals the bath g(tau)
-  (half-filled Bethe lattice self-consistency), atomic-limit density matrix.
+  (half-filled Bethe lattice self-consistency), atomic-limit density matrix,
+  and detailed balance: the sampled expansion-order distribution and
+  occupations of a single-orbital impurity with a discrete asymmetric bath
+  equal exact diagonalisation of impurity + bath (tests/exact_bath.py).
 """
 import os
 
 import numpy as np
 import pytest
 
+import exact_bath as XB
 import oracle as O
+from w2dynamics_gb300 import estimators as ES
 from w2dynamics_gb300 import problems as P
 
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
@@ -322,3 +327,56 @@ def test_atomic_limit_density_matrix():
     w = np.exp(-beta * (e - e.min()))
     dm = np.diag(r["densitymatrix"])[off:off + n]
     assert np.allclose(dm, w / w.sum(), rtol=1e-10)
+
+
+# single-orbital impurity, two bath levels, away from particle-hole symmetry
+BATH = dict(beta=4.0, mu=1.3, u=2.0, eps=[-0.6, 0.9], v=[0.6, 0.8])
+
+
+def bath_problem(nftau=2000):
+    b = BATH
+    um = P.flat_umatrix(P.umatrix_density(1, b["u"], b["u"], 0.0))
+    f = XB.ftau_bath(b["beta"], b["eps"], b["v"], nftau)
+    return um, P.muimp_solver(1, b["mu"]), np.broadcast_to(f, (1, 2, nftau)).copy()
+
+
+def test_detailed_balance_order_distribution_and_occupations():
+    """Exact answer for the whole sampler (acceptance factors, NPairs,
+    sliding windows, outer-superstate, global and tau-shift moves): the
+    per-flavour expansion-order histogram and the occupations from the
+    density matrix of 16 chains agree with exact diagonalisation of
+    impurity + discrete bath within 4.5 standard errors; F(tau) follows the
+    reference's bath-site formula, and swapping the bath energies' sign
+    (the other time convention) is detected at > 5 standard errors."""
+    b = BATH
+    pex = XB.order_marginal(b["beta"], b["mu"], b["u"], b["eps"], b["v"])[:30]
+    nup, ndn, dbl = XB.occupations(b["beta"], b["mu"], b["u"], b["eps"], b["v"])
+    um, muimp, ft = bath_problem()
+    m = O.Model(1, um, muimp, "Nt Szt Azt")
+    ev = np.eye(m.nstates)
+    hist, occ = [], []
+    for seed in range(16):
+        c = O.Chain(m, b["beta"], ft, 20, seed=seed, taudiff_max=1.0, ncorr=20, p_outer=0.1,
+                    p_global=0.01, p_shift=0.01, maxhisto=30)
+        c.warmup(2000)
+        c.measure(10000)
+        r = c.results()
+        hist.append(r["histo"] / r["histo"].sum(axis=1, keepdims=True))
+        o = ES.from_density_matrix(1, m.fock_states, ev, r["densitymatrix"])["occ"]
+        occ.append([o[0, 0, 0, 0], o[0, 1, 0, 1], o[0, 0, 0, 1]])
+    hist, occ = np.array(hist), np.array(occ)
+    sel = pex > 1e-3
+    mean, se = hist.mean(0)[:, sel], hist.std(0, ddof=1)[:, sel] / 4.0
+    z = (mean - pex[sel]) / se
+    assert np.abs(z).max() < 4.5, z
+    zo = (occ.mean(0) - [nup, ndn, dbl]) / (occ.std(0, ddof=1) / 4.0)
+    assert np.abs(zo).max() < 4.5, zo
+    # the same sampler with the bath energies reflected is a different model
+    flip = XB.ftau_bath(b["beta"], -np.array(b["eps"]), b["v"], 2000)
+    c = O.Chain(m, b["beta"], np.broadcast_to(flip, (1, 2, 2000)).copy(), 20, seed=99,
+                taudiff_max=1.0, ncorr=20, maxhisto=30)
+    c.warmup(2000)
+    c.measure(40000)
+    h = c.results()["histo"]
+    h = h / h.sum(axis=1, keepdims=True)
+    assert np.abs(h[:, 0] - pex[0]).max() > 5 * se[:, 0].max()

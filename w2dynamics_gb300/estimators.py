@@ -8,6 +8,9 @@ After the Z-space loop the reference turns the density matrix at beta/2
                                                        CTQMC.F90:2945-3017
   occ(b1,s1,b2,s2)      = Tr(rho n_f2 n_f1)            MeasDoubleOcc_from_Densitymatrix,
                                                        CTQMC.F90:2884-2942
+  ssquare(N)            = sum over superstates of N electrons of Tr(rho S^2)
+                                                       MeasureS2_from_densitymatrix,
+                                                       CTQMC.F90:2811-2838
 and finally rotates rho to the occupation basis (Transform_DensityMatrix_EB_to_OCCB,
 CTQMC.F90:3163-3179).  The reference evaluates each trace block by block in
 the eigenbasis with DGEMM/DDOT; traces do not depend on the basis, so here
@@ -82,3 +85,55 @@ def from_density_matrix(nd, occ_fock, evec, dm_eigen):
                 for f1 in range(nf):
                     rho2[f4, f3, f2, f1] = _trace(rho, tgt, sgn, [(f4, 0), (f3, 0), (f2, 1), (f1, 1)])
     return dict(densitymatrix=rho, occ=occ, rho1=rho1, rho2=rho2)
+
+
+def _apply(tgt, sgn, ops):
+    """The product of `ops` ((f, ca), last acting first) on every basis
+    vector: (target index or -1, amplitude)."""
+    ns = tgt.shape[2]
+    cur = np.arange(ns)
+    amp = np.ones(ns)
+    for f, ca in reversed(ops):
+        alive = cur >= 0
+        c = np.where(alive, cur, 0)
+        amp = np.where(alive, amp * sgn[f, ca, c], 0.0)
+        cur = np.where(alive, tgt[f, ca, c], -1)
+    return cur, amp
+
+
+def spin_square(nd, occ_fock, sst_size, sst_offset, rho):
+    """(ssquare, ssquare_operator).
+
+    ssquare_operator: S^2 = S+S-/2 + S-S+/2 + Sz^2 summed over all orbitals
+    (init_S2alt2, Operator.F90:548-633), S+ = sum_b c+_{b,up} c_{b,dn}, kept on
+    the superstate blocks only and in the occupation basis of the states
+    (create_ssquare_full, CTQMC.F90:2769-2806).  ssquare(N), N = 0 .. 2Nd:
+    Tr(rho S^2) over the blocks of the superstates with N electrons
+    (MeasureS2_from_densitymatrix, CTQMC.F90:2811-2838), with `rho` the
+    normalised occupation-basis density matrix (the trace of a block does
+    not depend on the basis)."""
+    occ_fock = np.asarray(occ_fock, np.int64)
+    ns = len(occ_fock)
+    tgt, sgn = ladder_tables(nd, occ_fock)
+    s2 = np.zeros((ns, ns))
+    cols = np.arange(ns)
+    for b in range(nd):
+        for b2 in range(nd):
+            up, dn, up2, dn2 = 2 * b, 2 * b + 1, 2 * b2, 2 * b2 + 1
+            for ops in ([(up, 0), (dn, 1), (dn2, 0), (up2, 1)],    # S+_b S-_b2
+                        [(dn, 0), (up, 1), (up2, 0), (dn2, 1)]):   # S-_b S+_b2
+                cur, amp = _apply(tgt, sgn, ops)
+                ok = cur >= 0
+                np.add.at(s2, (cur[ok], cols[ok]), 0.5 * amp[ok])
+    nup = sum((occ_fock >> b) & 1 for b in range(nd))
+    ndn = sum((occ_fock >> (nd + b)) & 1 for b in range(nd))
+    s2[cols, cols] += (0.5 * (nup - ndn)) ** 2
+    block = np.full(ns, -1)
+    for i, (o, n) in enumerate(zip(sst_offset, sst_size)):
+        block[o:o + n] = i
+    s2 = np.where(block[:, None] == block[None, :], s2, 0.0)
+    ssq = np.zeros(2 * nd + 1)
+    for o, n in zip(sst_offset, sst_size):
+        ne = bin(int(occ_fock[o])).count("1")
+        ssq[ne] += float(np.sum(rho[o:o + n, o:o + n] * s2[o:o + n, o:o + n].T))
+    return ssq, s2

@@ -64,6 +64,7 @@ statessuperstates = eigenstatesenergies = occbasismapping = None
 outersuperstatehisto = outerstatehisto = signhistosuperstates = signhistostates = None
 tracecontribsuperstates = tracecontribstates = None
 lhisto = rhisto = None
+ssquare = ssquare_operator = None
 mean_sign = 0.0
 accadd = np.zeros(NWormSectors)
 accrem = np.zeros(NWormSectors)
@@ -238,6 +239,7 @@ def _collect():
     global gtau, gtau_full, histo, occ, rho1, rho2, densitymatrix, mean_sign, gleg, gleg_full
     global accadd, accrem, accglob, accshift, outersuperstatehisto, outerstatehisto, signhistosuperstates
     global signhistostates, tracecontribsuperstates, tracecontribstates, lhisto, rhisto
+    global ssquare, ssquare_operator
     nd, ns, nf = _nd, _model.nstates, 2 * _nd
     res = [_batch.results(c) for c in range(_nchains)]
     signs = np.array([r["mean_sign"] for r in res])
@@ -266,6 +268,9 @@ def _collect():
         est = ES.from_density_matrix(nd, fk, evec, dm_eigen)
         densitymatrix, occ, rho1, rho2 = (est["densitymatrix"], est["occ"], est["rho1"],
                                           est["rho2"])
+        if _int("MeasSsquare", 0) != 0:
+            ssquare, ssquare_operator = ES.spin_square(nd, fk, _model.sst_size, _model.sst_offset,
+                                                       densitymatrix)
     else:
         densitymatrix = np.zeros((ns, ns))
         occ = np.zeros((nd, 2, nd, 2))
