@@ -434,6 +434,7 @@ struct Chain {
   // counters
   long long try_add = 0, try_rem = 0, acc_add = 0, acc_rem = 0, accqn_add = 0, accqn_rem = 0;
   long long try_glob = 0, acc_glob = 0, accqn_glob = 0, try_shift = 0, acc_shift = 0;
+  long long try_add4 = 0, acc_add4 = 0, try_rem4 = 0, acc_rem4 = 0;
   // measurements
   long long cnt_meas = 0;
   double meas_sign = 0;
@@ -1312,7 +1313,7 @@ static int fixed_ssts(const Chain& c, const std::vector<Op>& ops, std::vector<in
 }
 
 enum { GLOB_RANDPERM = 1, GLOB_USERSYM = 2, GLOB_SPINFLIP = 3, GLOB_CAFLIP = 4 };
-enum { MOVE_GLOB = 2, MOVE_SHIFT = 3, MOVE_OUTER = 4 };
+enum { MOVE_GLOB = 2, MOVE_SHIFT = 3, MOVE_OUTER = 4, MOVE_ADD4 = 5, MOVE_REM4 = 6 };
 
 // StepGlob, CTQMC.F90:4433-4554 (diagonal hybridisation):
 // gen_SpinFlipUpdate / gen_CAFlip / gen_SymUpdate / gen_GlobalUpdate_new
@@ -1597,6 +1598,306 @@ static void step_shift(Chain& c) {
   record(c, r);
 }
 
+// ---------------------------------------------------------------------------
+// 4-operator moves (StepAdd4 / StepRem4, CTQMC.F90:3615-3890, 4153-4431),
+// diagonal hybridisation.  Both rebuild every inverse matrix
+// (get_InvFullHybr) and the whole trace like StepGlob.
+
+// Removable pairs of a time-ordered list, skipping the entries whose index
+// is in `skip` (ensure_valid_NPairs_diag, Trace.F90:1762-1803, on the list
+// without them); the incremental update_NPairs_diag (Trace.F90:1862-1922)
+// gives the same count for operators inside the window.
+static int count_pairs_list(const Chain& c, const std::vector<Op>& ops, const std::vector<int>& skip) {
+  auto skipped = [&](int i) { return std::find(skip.begin(), skip.end(), i) != skip.end(); };
+  int n = 0;
+  const int K = (int)ops.size();
+  for (int i = 0; i < K; ++i) {
+    if (skipped(i)) continue;
+    const Op& x = ops[i];
+    if (x.tau < c.tauwin_min) continue;
+    if (x.tau > c.tauwin_max) break;
+    for (int j = i + 1; j < K; ++j) {
+      const Op& y = ops[j];
+      if (y.tau > c.tauwin_max || y.tau > x.tau + c.taudiff_max) break;
+      if (skipped(j)) continue;
+      if (y.b == x.b && y.s == x.s && y.ca != x.ca) ++n;
+    }
+  }
+  return n;
+}
+
+// The npair-th removable pair of `ops` without the `skip` entries, in the
+// scan order of gen_OperRemove (Trace.F90:4880-4910): indices (ix < iy).
+static void select_pair(const Chain& c, const std::vector<Op>& ops, const std::vector<int>& skip, int npair,
+                        int& ix, int& iy) {
+  auto skipped = [&](int i) { return std::find(skip.begin(), skip.end(), i) != skip.end(); };
+  const int K = (int)ops.size();
+  ix = iy = -1;
+  for (int i = 0; i < K; ++i) {
+    if (skipped(i)) continue;
+    const Op& x = ops[i];
+    if (x.tau < c.tauwin_min) continue;
+    for (int j = i + 1; j < K; ++j) {
+      const Op& y = ops[j];
+      if (y.tau > c.tauwin_max || y.tau > x.tau + c.taudiff_max) break;
+      if (skipped(j) || y.b != x.b || y.s != x.s || y.ca == x.ca) continue;
+      if (--npair <= 0) {
+        ix = i;
+        iy = j;
+        return;
+      }
+    }
+  }
+}
+
+// is_rempair_diag (Trace.F90:2006-2030)
+static bool is_rempair(const Chain& c, const Op& x, const Op& y) {
+  return x.b == y.b && x.s == y.s && x.ca != y.ca && x.tau >= c.tauwin_min && x.tau <= c.tauwin_max &&
+         y.tau >= c.tauwin_min && y.tau <= c.tauwin_max && std::fabs(x.tau - y.tau) <= c.taudiff_max;
+}
+
+// hybpairremfactor of gen_OperRemove (Trace.F90:4942-4948): np over the
+// window width times the creator range around the annihilator.
+static double rem_factor(const Chain& c, int np, const Op& x, const Op& y) {
+  const Op& a = x.ca == 1 ? x : y;
+  return double(np) / ((c.tauwin_max - c.tauwin_min) *
+                       (std::min(a.tau + c.taudiff_max, c.tauwin_max) - std::max(a.tau - c.taudiff_max, c.tauwin_min)));
+}
+
+// Determinant ratio and trace of the proposed list nops (full rebuild), the
+// Metropolis draw, and installation on acceptance.  Returns the outcome.
+static int full_rebuild_step(Chain& c, std::vector<Op>& nops, double factor, Record& r, int npairs_new) {
+  std::vector<std::vector<double>> tc, ta, minv_old = c.minv, tc_old = c.tau_c, ta_old = c.tau_a;
+  flavour_lists(c, nops, tc, ta);
+  c.tau_c = tc;
+  c.tau_a = ta;
+  LogVal det_new = rebuild_minv(c);
+  std::vector<std::vector<double>> minv_new = c.minv;
+  LogVal det_minv_old{0.0, 1.0};
+  for (int f = 0; f < c.nf; ++f) {
+    int k = (int)tc_old[f].size();
+    if (k == 0) continue;
+    std::vector<double> A = minv_old[f];
+    bool sing;
+    det_minv_old = lmul(lu_logdet_inverse(A, k, sing), det_minv_old);
+  }
+  LogVal detrat = lmul(det_new, det_minv_old);
+  std::vector<Op> ops_old = c.ops;
+  c.ops = nops;
+  std::vector<LogVal> part;
+  LogVal trnew = full_trace(c, &part);
+  LogVal trrat = ldiv(trnew, c.trace);
+  double prob = std::fabs(factor * std::exp(trrat.log + detrat.log));
+  double rnd = c.rng.grnd();
+  r.det_log = detrat.log;
+  r.det_sign = detrat.sign;
+  r.tr_log = trnew.log;
+  r.tr_sign = trnew.sign;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    c.det = det_new;
+    c.trace = trnew;
+    c.parttrace = part;
+    c.minv = minv_new;
+    c.npairs = npairs_new;
+    c.cfgsign = -config_sign(c);
+    return OUT_ACCEPT;
+  }
+  c.ops = ops_old;
+  c.tau_c = tc_old;
+  c.tau_a = ta_old;
+  c.minv = minv_old;
+  reset_caches(c);
+  return OUT_REJECT;
+}
+
+// Index of the first operator of `ops` with tau >= t.
+static int lower_index(const std::vector<Op>& ops, double t) {
+  return (int)(std::lower_bound(ops.begin(), ops.end(), t, [](const Op& e, double v) { return e.tau < v; }) -
+               ops.begin());
+}
+
+// StepAdd4, CTQMC.F90:3615-3890.
+static void step_add4(Chain& c) {
+  c.try_add4++;
+  Record r{};
+  r.move = MOVE_ADD4;
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  // pair_OperAdd with N = 4, force_diagonal (Trace.F90:3657-3702): per
+  // pair the annihilator at tau_ref in the window, orbital and spin, the
+  // creator within TaudiffMax; process_OperAdd puts each pair in time order
+  Op nw[4];
+  double tdf = 1.0;
+  for (int pr = 0; pr < 2; ++pr) {
+    const double w = c.tauwin_max - c.tauwin_min;
+    const double tau_ref = c.tauwin_min + w * c.rng.grnd();
+    tdf = tdf * w;
+    const int orb = c.rng.randint(1, c.nd);
+    const int spin = c.rng.randint(1, 2);
+    const double tmin = std::max(tau_ref - c.taudiff_max, c.tauwin_min);
+    const double w2 = std::min(tau_ref + c.taudiff_max, c.tauwin_max) - tmin;
+    const double tcr = tmin + w2 * c.rng.grnd();
+    tdf = tdf * w2;
+    Op a{tau_ref, orb - 1, spin - 1, 1}, cr{tcr, orb - 1, spin - 1, 0};
+    nw[2 * pr] = a.tau < cr.tau ? a : cr;
+    nw[2 * pr + 1] = a.tau < cr.tau ? cr : a;
+  }
+  r.orb = c.fi(nw[0].b, nw[0].s) + 1;
+  r.spin = c.fi(nw[2].b, nw[2].s) + 1;
+  r.tau_c = nw[0].tau;
+  r.tau_a = nw[1].tau;
+  // equal times among the new operators or with present ones
+  bool equal = false;
+  for (int i = 0; i < 4; ++i) {
+    for (int j = i + 1; j < 4; ++j)
+      if (nw[i].tau == nw[j].tau) equal = true;
+    for (const Op& e : c.ops)
+      if (e.tau == nw[i].tau) equal = true;
+  }
+  if (c.npairs == -1) c.npairs = count_pairs_list(c, c.ops, {});  // ensure_valid_NPairs
+  if (equal) {
+    r.outcome = OUT_EQUALTIME;
+    record(c, r);
+    return;
+  }
+  // proposed list and the indices of the new operators in it
+  std::vector<Op> all = c.ops;
+  for (int i = 0; i < 4; ++i) all.insert(all.begin() + lower_index(all, nw[i].tau), nw[i]);
+  int q[4];
+  for (int i = 0; i < 4; ++i) q[i] = lower_index(all, nw[i].tau);
+  const int np_12 = count_pairs_list(c, all, {q[2], q[3]});
+  const int np_34 = count_pairs_list(c, all, {q[0], q[1]});
+  const int np_all = count_pairs_list(c, all, {});
+  double rf;
+  int branch = 0;
+  if (is_rempair(c, nw[0], nw[3]) && is_rempair(c, nw[1], nw[2])) {
+    branch = 1;
+    const int np_23 = count_pairs_list(c, all, {q[0], q[3]});
+    const int np_14 = count_pairs_list(c, all, {q[1], q[2]});
+    rf = (1.0 / double(np_all)) * (1.0 / double(np_12) + 1.0 / double(np_34) + 1.0 / double(np_14) + 1.0 / double(np_23));
+    tdf = tdf / 4.0;
+  } else if (is_rempair(c, nw[0], nw[2]) && is_rempair(c, nw[1], nw[3])) {
+    branch = 2;
+    const int np_23 = count_pairs_list(c, all, {q[0], q[2]});
+    const int np_14 = count_pairs_list(c, all, {q[1], q[3]});
+    rf = (1.0 / double(np_all)) * (1.0 / double(np_12) + 1.0 / double(np_34) + 1.0 / double(np_14) + 1.0 / double(np_23));
+    tdf = tdf / 4.0;
+  } else {
+    rf = (1.0 / double(np_all)) * (1.0 / double(np_12) + 1.0 / double(np_34));
+    tdf = tdf / 2.0;
+  }
+  r.change_outer = branch;
+  r.fpos_c = np_12;
+  r.fpos_a = np_34;
+  r.npairs = np_all;
+  // check_sst_sequence from the operator before the earliest new one to the
+  // operator after the latest (get_current_ssts, Trace.F90:1220-1304)
+  const int first = std::min(q[0], q[2]), last = std::max(q[1], q[3]);
+  const double t_first = all[first].tau, t_last = all[last].tau;
+  const int bs = sector_before(c, lower_index(c.ops, t_first));
+  const int es = sector_before(c, lower_index(c.ops, t_last));
+  const int w = bs < 0 ? -1 : walk(c, all, bs, first, last + 1);
+  if (bs < 0 || w < 0 || w != es) {
+    r.outcome = OUT_QN;
+    record(c, r);
+    return;
+  }
+  const double n2 = 2.0 * c.nd;
+  r.outcome = full_rebuild_step(c, all, tdf * n2 * n2 * rf, r, np_all);
+  if (r.outcome == OUT_ACCEPT) c.acc_add4++;
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  record(c, r);
+}
+
+// StepRem4, CTQMC.F90:4153-4431.
+static void step_rem4(Chain& c) {
+  c.try_rem4++;
+  Record r{};
+  r.move = MOVE_REM4;
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  if (c.npairs == -1) c.npairs = count_pairs_list(c, c.ops, {});
+  const int np_old = c.npairs;
+  if (np_old <= 0) {
+    r.outcome = OUT_NOPAIRS;
+    record(c, r);
+    return;
+  }
+  // first pair (gen_OperRemove on the present list)
+  int a1, a2;
+  select_pair(c, c.ops, {}, c.rng.randint(1, np_old), a1, a2);
+  const double f1 = rem_factor(c, np_old, c.ops[a1], c.ops[a2]);
+  const int np_34 = count_pairs_list(c, c.ops, {a1, a2});
+  if (np_34 <= 0) {
+    r.outcome = OUT_NOPAIRS;
+    record(c, r);
+    return;
+  }
+  // second pair (gen_OperRemove on the list without the first)
+  int b1, b2;
+  select_pair(c, c.ops, {a1, a2}, c.rng.randint(1, np_34), b1, b2);
+  const double f2 = rem_factor(c, np_34, c.ops[b1], c.ops[b2]);
+  double tdf = double(np_old) * double(np_34) / f1 / f2;
+  const int np_12 = count_pairs_list(c, c.ops, {b1, b2});
+  const Op& o1 = c.ops[a1];
+  const Op& o2 = c.ops[a2];
+  const Op& o3 = c.ops[b1];
+  const Op& o4 = c.ops[b2];
+  double rf;
+  int branch = 0;
+  if (is_rempair(c, o1, o4) && is_rempair(c, o2, o3)) {
+    branch = 1;
+    const int np_23 = count_pairs_list(c, c.ops, {a1, b2});
+    const int np_14 = count_pairs_list(c, c.ops, {a2, b1});
+    rf = (1.0 / double(np_old)) * (1.0 / double(np_12) + 1.0 / double(np_34) + 1.0 / double(np_14) + 1.0 / double(np_23));
+    tdf = tdf / 4.0;
+  } else if (is_rempair(c, o1, o3) && is_rempair(c, o2, o4)) {
+    branch = 2;
+    const int np_23 = count_pairs_list(c, c.ops, {a1, b1});
+    const int np_14 = count_pairs_list(c, c.ops, {a2, b2});
+    rf = (1.0 / double(np_old)) * (1.0 / double(np_12) + 1.0 / double(np_34) + 1.0 / double(np_14) + 1.0 / double(np_23));
+    tdf = tdf / 4.0;
+  } else {
+    rf = (1.0 / double(np_old)) * (1.0 / double(np_12) + 1.0 / double(np_34));
+    tdf = tdf / 2.0;
+  }
+  r.orb = c.fi(o1.b, o1.s) + 1;
+  r.spin = c.fi(o3.b, o3.s) + 1;
+  r.tau_c = o1.tau;
+  r.tau_a = o2.tau;
+  r.change_outer = branch;
+  r.fpos_c = np_12;
+  r.fpos_a = np_34;
+  const std::vector<int> gone = {a1, a2, b1, b2};
+  const int np_new = count_pairs_list(c, c.ops, gone);
+  r.npairs = np_new;
+  std::vector<Op> nops;
+  nops.reserve(c.ops.size() - 4);
+  for (int i = 0; i < (int)c.ops.size(); ++i)
+    if (std::find(gone.begin(), gone.end(), i) == gone.end()) nops.push_back(c.ops[i]);
+  // check_sst_sequence over the operators left between the earliest and
+  // the latest removed one
+  const int first = std::min(a1, b1), last = std::max(a2, b2);
+  const int bs = sector_before(c, first);
+  const int es = sector_before(c, last + 1);
+  const int from = lower_index(nops, c.ops[first].tau), to = lower_index(nops, c.ops[last].tau);
+  const int w = bs < 0 ? -1 : walk(c, nops, bs, from, to);
+  if (bs < 0 || w < 0 || w != es) {
+    r.outcome = OUT_QN;
+    record(c, r);
+    return;
+  }
+  const double n2 = 2.0 * c.nd;
+  r.outcome = full_rebuild_step(c, nops, 1.0 / (n2 * n2) / tdf / rf, r, np_new);
+  if (r.outcome == OUT_ACCEPT) c.acc_rem4++;
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  record(c, r);
+}
+
 // one proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250)
 static int one_step(Chain& c) {
   double rand_num = c.rng.grnd();
@@ -1606,14 +1907,14 @@ static int one_step(Chain& c) {
       bool co = c.rng.grnd() < c.p.p_outer;
       step_add(c, co);
     } else {
-      return -2;  // 4-operator moves are outside this restatement
+      step_add4(c);
     }
   } else if (rand_num <= 1.0 - c.p.p_shift - c.p.p_global) {
     if (c.rng.grnd() >= c.p.p_4op) {
       bool co = c.rng.grnd() < c.p.p_outer;
       step_rem(c, co);
     } else {
-      return -2;
+      step_rem4(c);
     }
   } else if (rand_num <= 1.0 - c.p.p_shift) {
     step_glob(c);
@@ -1627,6 +1928,7 @@ static int one_step(Chain& c) {
 static void init_counters(Chain& c) {
   c.try_add = c.try_rem = c.acc_add = c.acc_rem = c.accqn_add = c.accqn_rem = 0;
   c.try_glob = c.acc_glob = c.accqn_glob = c.try_shift = c.acc_shift = 0;
+  c.try_add4 = c.acc_add4 = c.try_rem4 = c.acc_rem4 = 0;
 }
 
 // MeasGtauRem(.false.), CTQMC.F90:2252-2440 (tau bins only)
@@ -1950,6 +2252,10 @@ void orc_chain_counters(void* cc, long long* out) {
   out[9] = c.accqn_glob;
   out[10] = c.try_shift;
   out[11] = c.acc_shift;
+  out[12] = c.try_add4;
+  out[13] = c.acc_add4;
+  out[14] = c.try_rem4;
+  out[15] = c.acc_rem4;
 }
 
 // state: trace(log,sign), det(log,sign), cfgsign, npairs, outer_sst,

@@ -145,7 +145,7 @@ class Chain:
 
     def __init__(self, model, beta, ftau, ntau, seed, taudiff_max=-1.0, ncorr=100,
                  p_outer=0.0, maxhisto=500, meas_dm=1, p_global=0.0, p_shift=0.0, nleg=0,
-                 symmoves=None):
+                 symmoves=None, p_4op=0.0):
         L = lib()
         self.model = model
         nd = model.nd
@@ -156,7 +156,7 @@ class Chain:
         self.ntau = ntau
         self.maxhisto = maxhisto
         p = Params(beta=beta, nftau=self.nftau, ntau=ntau, ncorr=ncorr, seed=seed,
-                   taudiff_max=taudiff_max, p_global=p_global, p_shift=p_shift, p_4op=0.0,
+                   taudiff_max=taudiff_max, p_global=p_global, p_shift=p_shift, p_4op=p_4op,
                    p_outer=p_outer, maxhisto=maxhisto, meas_dm=meas_dm, nleg=nleg)
         self._sym = None
         if symmoves is not None:
@@ -213,11 +213,11 @@ class Chain:
         return out
 
     def counters(self):
-        out = (C.c_longlong * 12)()
+        out = (C.c_longlong * 16)()
         lib().orc_chain_counters(self.h, out)
         return dict(zip(("try_add", "acc_add", "try_rem", "acc_rem", "qn_add", "qn_rem",
                          "cnt_meas", "try_glob", "acc_glob", "qn_glob", "try_shift",
-                         "acc_shift"), list(out)))
+                         "acc_shift", "try_add4", "acc_add4", "try_rem4", "acc_rem4"), list(out)))
 
     def state(self):
         out = np.zeros(14)

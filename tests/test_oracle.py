@@ -140,16 +140,17 @@ def test_fast_updates_match_full_recompute(name, beta, tdm, pout):
                                             ("dd3", 8.0, 8.0)])
 def test_global_and_shift_moves_keep_state_consistent(name, beta, tdm):
     """Global moves (spin flip, CA flip, user symmetry moves, random
-    permutation) and tau-shift moves at 10 % each: trace, determinant and
-    inverse matrices stay equal to a full recompute after every step, and
-    both move kinds are accepted."""
+    permutation) and tau-shift moves at 10 % each, 4-operator moves at 30 %
+    of the insertions and removals: trace, determinant and inverse matrices
+    stay equal to a full recompute after every step, and every move kind is
+    accepted."""
     pr = P.config_problem(name, beta=beta)
     m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
     # a cyclic orbital permutation (its inverse differs) for the 3-orbital model
     sym = [[2, 3, 1, 5, 6, 4]] if pr["nd"] == 3 else None
     c = O.Chain(m, pr["beta"], pr["ftau"], 50, seed=23, taudiff_max=tdm, p_outer=0.1,
-                p_global=0.1, p_shift=0.1, symmoves=sym)
-    acc = {"acc_glob": 0, "acc_shift": 0}
+                p_global=0.1, p_shift=0.1, symmoves=sym, p_4op=0.3)
+    acc = {"acc_glob": 0, "acc_shift": 0, "acc_add4": 0, "acc_rem4": 0}
     for i in range(1500):
         c.warmup(1)  # counters restart with every call
         for k in acc:
@@ -340,14 +341,17 @@ def bath_problem(nftau=2000):
     return um, P.muimp_solver(1, b["mu"]), np.broadcast_to(f, (1, 2, nftau)).copy()
 
 
-def test_detailed_balance_order_distribution_and_occupations():
+@pytest.mark.parametrize("p_4op", [0.0, 0.5])
+def test_detailed_balance_order_distribution_and_occupations(p_4op):
     """Exact answer for the whole sampler (acceptance factors, NPairs,
     sliding windows, outer-superstate, global and tau-shift moves): the
     per-flavour expansion-order histogram and the occupations from the
     density matrix of 16 chains agree with exact diagonalisation of
     impurity + discrete bath within 4.5 standard errors; F(tau) follows the
     reference's bath-site formula, and swapping the bath energies' sign
-    (the other time convention) is detected at > 5 standard errors."""
+    (the other time convention) is detected at > 5 standard errors.  With
+    p_4op = 0.5 half of the insertions and removals are 4-operator moves
+    (StepAdd4 / StepRem4)."""
     b = BATH
     pex = XB.order_marginal(b["beta"], b["mu"], b["u"], b["eps"], b["v"])[:30]
     nup, ndn, dbl = XB.occupations(b["beta"], b["mu"], b["u"], b["eps"], b["v"])
@@ -357,7 +361,7 @@ def test_detailed_balance_order_distribution_and_occupations():
     hist, occ = [], []
     for seed in range(16):
         c = O.Chain(m, b["beta"], ft, 20, seed=seed, taudiff_max=1.0, ncorr=20, p_outer=0.1,
-                    p_global=0.01, p_shift=0.01, maxhisto=30)
+                    p_global=0.01, p_shift=0.01, maxhisto=30, p_4op=p_4op)
         c.warmup(2000)
         c.measure(10000)
         r = c.results()
