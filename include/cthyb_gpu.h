@@ -97,6 +97,8 @@ typedef struct {
   int32_t nsym;          /* NSymMove: user symmetry moves for StepGlob (0: none) */
   const int32_t* symmoves; /* nsym x 2Nd, row i = SymMove(i+1): 1-based target flavour of flavour
                               (b-1) + Nd*(s-1) + 1 (Trace.F90:471-477) */
+  double p_4op;          /* Percentage4OperatorMove: share of insertions and removals made as
+                            4-operator moves (StepAdd4 / StepRem4, CTQMC.F90:3615-3890, 4153-4431) */
 } cthyb_group_desc;
 
 #define CTHYB_FLAG_DENSE 1  /* dense block trace even for monomial models */
@@ -189,6 +191,9 @@ int cthyb_batch_results_score(cthyb_batch_t batch, int chain, double* dgtau, dou
  * measure call: TryGlob, AccGlob, AccQNGlob, TryShift, AccShift
  * (CTQMC.F90:134-136). */
 int cthyb_batch_move_counters(cthyb_batch_t batch, int chain, int64_t* counters5);
+/* 4-operator move counters since the last warmup/measure call:
+ * TryAdd4, AccAdd4, TryRem4, AccRem4 (CTQMC.F90:134-136). */
+int cthyb_batch_move_counters4(cthyb_batch_t batch, int chain, int64_t* out4);
 
 /* Normalised results of one chain (CTQMC.F90:8676-8760):
  *   gtau (Nd,2,Ntau) Fortran order, mean_sign, densitymatrix in the

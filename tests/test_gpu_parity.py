@@ -27,19 +27,19 @@ def lib():
 
 
 def run_pair(name, beta, tdm, p_outer, nprop, seed, dense=False, qns=None, ntau=50, p_global=0.0,
-             p_shift=0.0, symmoves=None):
+             p_shift=0.0, symmoves=None, p_4op=0.0):
     pr = P.config_problem(name, beta=beta)
     q = qns or pr["quantum_numbers"]
     mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
     co = O.Chain(mo, beta, pr["ftau"], ntau, seed=seed, taudiff_max=tdm, p_outer=p_outer,
-                 p_global=p_global, p_shift=p_shift, symmoves=symmoves)
+                 p_global=p_global, p_shift=p_shift, symmoves=symmoves, p_4op=p_4op)
     co.start_log(nprop)
     co.warmup(nprop)
     ref = co.log()
     mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
     grp = E.Group(beta, pr["ftau"], ntau, nchains=1, seed0=seed, taudiff_max=tdm,
                   p_outer=p_outer, dense=dense, kcap=64, opcap=512, p_global=p_global,
-                  p_shift=p_shift, symmoves=symmoves)
+                  p_shift=p_shift, symmoves=symmoves, p_4op=p_4op)
     b = E.Batch(mg, [grp])
     b.set_log(nprop)
     b.warmup(nprop)
@@ -130,6 +130,47 @@ def test_global_and_shift_move_parity(lib, name, beta, tdm, pout, nprop, seed, d
     assert so["cfgsign"] == sg["cfgsign"] and so["det_sign"] == sg["det_sign"]
     assert abs(so["det_log"] - sg["det_log"]) < 1e-8
     assert so["window_position"] == sg["window_position"]
+    t_o, *_ = co.get_config()
+    t_g, *_ = b.get_config(0)
+    assert np.array_equal(t_o, t_g)
+    for f in range(2 * co.model.nd):
+        mo_, mg_ = co.minv(f), b.minv(0, f)
+        assert mo_.shape == mg_.shape
+        if mo_.size:
+            assert np.allclose(mg_, mo_, rtol=1e-9, atol=1e-9 * np.abs(mo_).max())
+
+
+FOUR_CASES = [
+    ("anderson1", 10.0, 3.0, 0.1, 20000, 31, False),
+    ("dd3", 10.0, 4.0, 0.1, 6000, 32, False),
+    ("dd3", 25.0, 5.0, 0.0, 4000, 33, False),
+    ("dd3", 10.0, 4.0, 0.1, 2000, 34, True),
+    ("kanamori5", 2.0, 2.0, 0.0, 400, 35, False),
+]
+
+
+@pytest.mark.parametrize("name,beta,tdm,pout,nprop,seed,dense", FOUR_CASES)
+def test_four_operator_move_parity(lib, name, beta, tdm, pout, nprop, seed, dense):
+    """4-operator moves (StepAdd4 / StepRem4) at 30 % of the insertions and
+    removals, with global and tau-shift moves at 2 % each, proposal by
+    proposal (the first pair's times, both flavours, the removable-pair
+    counts of each proposal, outcome, ratios); the final configuration,
+    state, move counters and inverse matrices."""
+    ref, got, co, b = run_pair(name, beta, tdm, pout, nprop, seed, dense=dense,
+                               p_global=0.02, p_shift=0.02, p_4op=0.3)
+    F = P.config_problem(name, beta=beta)["ftau"][0, 0]
+    compare_logs(ref, got, F, beta)
+    for mv in (5, 6):
+        assert np.sum((ref["move"] == mv) & (ref["outcome"] == 4)) > 0, mv
+    mc = b.move_counters(0)
+    oc = co.counters()
+    for key in ("try_add4", "acc_add4", "try_rem4", "acc_rem4", "try_glob", "acc_glob"):
+        assert mc[key] == oc[key], key
+    so, sg = co.state(), b.state(0)
+    assert so["noper"] == sg["noper"] and so["outer_sst"] == sg["outer_sst"]
+    assert so["cfgsign"] == sg["cfgsign"] and so["det_sign"] == sg["det_sign"]
+    assert so["npairs"] == sg["npairs"] or so["npairs"] == -1 or sg["npairs"] == -1
+    assert abs(so["det_log"] - sg["det_log"]) < 1e-8
     t_o, *_ = co.get_config()
     t_g, *_ = b.get_config(0)
     assert np.array_equal(t_o, t_g)

@@ -108,11 +108,13 @@ def test_equal_error_batched_and_one_chain_forms():
     assert np.abs(zz).max() < 4.5
 
 
-def test_detailed_balance_against_exact_diagonalisation():
+@pytest.mark.parametrize("p_4op", [0.0, 0.5])
+def test_detailed_balance_against_exact_diagonalisation(p_4op):
     """64 GPU chains (sliding windows, outer-superstate, global and tau-shift
-    moves) of the single-orbital impurity with two bath levels: per-flavour
-    order histogram and occupations within 4.5 standard errors of the exact
-    values (tests/exact_bath.py)."""
+    moves, and with p_4op = 0.5 half of the insertions and removals as
+    4-operator moves) of the single-orbital impurity with two bath levels:
+    per-flavour order histogram and occupations within 4.5 standard errors
+    of the exact values (tests/exact_bath.py)."""
     beta, mu, u, eps, v = 4.0, 1.3, 2.0, [-0.6, 0.9], [0.6, 0.8]
     pex = XB.order_marginal(beta, mu, u, eps, v)[:30]
     nup, ndn, dbl = XB.occupations(beta, mu, u, eps, v)
@@ -123,7 +125,7 @@ def test_detailed_balance_against_exact_diagonalisation():
     n = 64
     b = E.Batch(mg, [E.Group(beta, np.broadcast_to(f, (1, 2, 2000)).copy(), 20, nchains=n, seed0=500,
                              taudiff_max=1.0, ncorr=20, kcap=32, opcap=128, maxhisto=30, p_outer=0.1,
-                             p_global=0.01, p_shift=0.01)])
+                             p_global=0.01, p_shift=0.01, p_4op=p_4op)])
     b.warmup(2000)
     b.measure(5000)
     b.sync()

@@ -18,7 +18,7 @@ def pstring(d):
 BASE = {"beta": 10.0, "Nd": 3, "Ntau": 40, "NCorr": 50, "Nmeas": 60, "Nwarmups": 2000,
         "MaxHisto": 60, "TaudiffMax": 5.0, "QuantumNumbers": "Nt Szt",
         "PercentageGlobalMove": 0.005, "PercentageTauShiftMove": 0.005,
-        "Percentage4OperatorMove": 0.0, "PercentageOuterMove": 0.1,
+        "Percentage4OperatorMove": 0.1, "PercentageOuterMove": 0.1,
         "PercentageWormInsert": 0.0, "segment": 0, "offdiag": 0, "statesampling": 0,
         "MeasDensityMatrix": 1, "MeasSsquare": 1, "Eigenbasis": 1, "NLegMax": 10,
         "NSymMove": 1, "SymMove01": "2 3 1 5 6 4"}
@@ -40,7 +40,7 @@ def test_parameter_string_rules():
     ctqmc.dest_paras()
 
 
-@pytest.mark.parametrize("key,val", [("Percentage4OperatorMove", 0.1), ("segment", 1),
+@pytest.mark.parametrize("key,val", [("flavourchange_moves", 1), ("segment", 1),
                                      ("PercentageWormInsert", 0.1),
                                      ("offdiag", 1), ("statesampling", 1)])
 def test_unsupported_modes_are_rejected(key, val):
@@ -79,7 +79,7 @@ def test_solve_through_the_module_matches_the_oracle():
     mo = O.Model(nd, pr["umatrix"], pr["muimp"], "Nt Szt")
     co = O.Chain(mo, 10.0, ftau, ntau, seed=11, taudiff_max=5.0, ncorr=BASE["NCorr"],
                  p_outer=0.1, maxhisto=BASE["MaxHisto"] + 1, p_global=0.005, p_shift=0.005,
-                 nleg=BASE["NLegMax"], symmoves=[[2, 3, 1, 5, 6, 4]])
+                 nleg=BASE["NLegMax"], symmoves=[[2, 3, 1, 5, 6, 4]], p_4op=0.1)
     co.set_taudiffmax(5.0)
     co.warmup(BASE["Nwarmups"])
     co.measure(BASE["Nmeas"])
@@ -109,6 +109,7 @@ def test_solve_through_the_module_matches_the_oracle():
     assert ctqmc.occbasismapping.shape == (mo.nstates, nd, 2)
     cnt = co.counters()
     assert ctqmc.accadd[0] == cnt["acc_add"] / cnt["try_add"]
+    assert ctqmc.accadd4 == cnt["acc_add4"] / cnt["try_add4"] and cnt["acc_add4"] > 0
     n, outer, _ = ctqmc.get_mc_config_scalars()
     taus, orbs, spins, cas, hashybs, outer2, _ = ctqmc.get_mc_config(n)
     t_o, *_ = co.get_config()

@@ -1437,8 +1437,14 @@ __device__ NOINL void ph_draw(Ctx& c, Prop& p) {
     __syncwarp();
     return;
   }
+  if (!(grnd(c) >= c.g->p_4op)) {  // 4-operator move (StepAdd4 / StepRem4), no outer draw
+    p.move = move + 5;
+    r.move = move + 5;
+    p.rare = 1;
+    __syncwarp();
+    return;
+  }
   p.rare = 0;
-  grnd(c);  // Percentage4OperatorMove draw
   bool co = grnd(c) < c.g->p_outer;
   p.co = co;
   r.change_outer = co;
@@ -2526,6 +2532,499 @@ __device__ NOINL void ph_shift(Ctx& c, Prop& p) {
   __syncwarp();
 }
 
+// ---------------------------------------------------------------------------
+// 4-operator moves (StepAdd4 / StepRem4, CTQMC.F90:3615-3890, 4153-4431),
+// diagonal hybridisation.  Rare like global moves: the proposed operator
+// arrays are written in place (the old ones saved in the o_glob work space),
+// the changed flavours' inverse matrices are rebuilt by Gauss-Jordan and the
+// tree into the inactive slots; a rejection restores the arrays.  The
+// reference rebuilds every flavour's matrix; for the unchanged flavours the
+// ratio of the rebuilt and the present determinant is one, so only the
+// changed flavours enter here.
+
+// Removable pairs of the operator arrays (time order, K entries) without the
+// entries skip[0..3] (-1: unused) (ensure_valid_NPairs_diag,
+// Trace.F90:1762-1803, on the list without them).
+__device__ NOINL int count_pairs_skip(Ctx& c, const double* tau, const int* code, int K, const int* skip) {
+  const Hdr& h = *c.h;
+  const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  int tot = 0;
+  for (int i = c.lane; i < K; i += 32) {
+    if (i == skip[0] || i == skip[1] || i == skip[2] || i == skip[3]) continue;
+    const double x = tau[i];
+    if (x < wmin || x > wmax) continue;
+    const int cx = code[i];
+    const double hi = fmin(wmax, __dadd_rn(x, tdm));
+    for (int j = i + 1; j < K; ++j) {
+      if (tau[j] > hi) break;
+      if (j == skip[0] || j == skip[1] || j == skip[2] || j == skip[3]) continue;
+      const int cy = code[j];
+      tot += ((cy >> 1) == (cx >> 1)) && ((cy & 1) != (cx & 1));
+    }
+  }
+  return wsumi(tot);
+}
+
+// The target-th removable pair (1-based) in the scan order of
+// gen_OperRemove (Trace.F90:4880-4910) without the skip entries: indices
+// ix < iy, lane-uniform; false if there is none.
+__device__ NOINL bool select_pair_skip(Ctx& c, const double* tau, const int* code, int K, const int* skip,
+                                       int target, int& ix, int& iy) {
+  const Hdr& h = *c.h;
+  const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  const int start = wlb(tau, K, wmin, c.lane);
+  for (int base = start; base < K; base += 32) {
+    const int i = base + c.lane;
+    int cnt = 0;
+    if (i < K && i != skip[0] && i != skip[1] && i != skip[2] && i != skip[3]) {
+      const double x = tau[i];
+      const int cx = code[i];
+      const double hi = fmin(wmax, __dadd_rn(x, tdm));
+      for (int j = i + 1; j < K; ++j) {
+        if (tau[j] > hi) break;
+        if (j == skip[0] || j == skip[1] || j == skip[2] || j == skip[3]) continue;
+        const int cy = code[j];
+        cnt += ((cy >> 1) == (cx >> 1)) && ((cy & 1) != (cx & 1));
+      }
+    }
+    int cum = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL, cum, o);
+      if (c.lane >= o) cum += y;
+    }
+    const int total = __shfl_sync(FULL, cum, 31);
+    if (target <= total) {
+      const unsigned bal = __ballot_sync(FULL, cum >= target);
+      const int L0 = __ffs(bal) - 1;
+      const int before = __shfl_sync(FULL, cum - cnt, L0);
+      int want = target - before, jy = -1;
+      if (c.lane == L0) {
+        const double x = tau[i];
+        const int cx = code[i];
+        const double hi = fmin(wmax, __dadd_rn(x, tdm));
+        for (int j = i + 1; j < K; ++j) {
+          if (tau[j] > hi) break;
+          if (j == skip[0] || j == skip[1] || j == skip[2] || j == skip[3]) continue;
+          const int cy = code[j];
+          if (((cy >> 1) == (cx >> 1)) && ((cy & 1) != (cx & 1)) && --want <= 0) {
+            jy = j;
+            break;
+          }
+        }
+      }
+      ix = base + L0;
+      iy = __shfl_sync(FULL, jy, L0);
+      return iy > ix;
+    }
+    target -= total;
+  }
+  return false;
+}
+
+// is_rempair_diag (Trace.F90:2006-2030) for (time, code) operators.
+__device__ __forceinline__ bool rempair4(const Hdr& h, double tx, int cx, double ty, int cy) {
+  return (cx >> 1) == (cy >> 1) && (cx & 1) != (cy & 1) && tx >= h.tauwin_min && tx <= h.tauwin_max &&
+         ty >= h.tauwin_min && ty <= h.tauwin_max && fabs(__dsub_rn(tx, ty)) <= h.taudiff_max;
+}
+
+// hybpairremfactor of gen_OperRemove (Trace.F90:4942-4948); ta is the
+// annihilator's time.
+__device__ __forceinline__ double remfac4(const Hdr& h, int np, double ta) {
+  return __ddiv_rn((double)np, __dmul_rn(__dsub_rn(h.tauwin_max, h.tauwin_min),
+                                         __dsub_rn(fmin(__dadd_rn(ta, h.taudiff_max), h.tauwin_max),
+                                                   fmax(__dsub_rn(ta, h.taudiff_max), h.tauwin_min))));
+}
+
+// Superstate walk over operators j0 .. j1-1 of the present arrays, skipping
+// the entries in skip[0..3], from superstate s (lane 0 walks; lane-uniform).
+__device__ NOINL int walk_ops(Ctx& c, int s, int j0, int j1, const int* skip) {
+  const DModel& m = *c.m;
+  if (c.lane == 0)
+    for (int j = j0; j < j1 && s >= 0; ++j) {
+      if (j == skip[0] || j == skip[1] || j == skip[2] || j == skip[3]) continue;
+      const int code = c.opcode[j];
+      s = m.connect[((size_t)s * m.nf + (code >> 1)) * 2 + (code & 1)];
+    }
+  return __shfl_sync(FULL, s, 0);
+}
+
+// Determinant ratio of the proposed arrays for the changed flavours fa, fb
+// (new sorted lists in srt_new, counts in knew, new inverses in the o_glob
+// matrices), the trace from the rebuilt tree, the Metropolis draw and the
+// installation on acceptance.  `factor` multiplies the weight ratio; the
+// old arrays are in glob_optau/glob_opcode (K_old entries).  Returns the
+// outcome (3 rejected, 4 accepted).
+__device__ NOINL int rebuild4_decide(Ctx& c, int fa, int fb, double factor, int K_old, int np_new) {
+  Hdr& h = *c.h;
+  cthyb_record& r = *c.rec;
+  double* srt_new = glob_srt(c);
+  double* minv_new = glob_minv(c);
+  int knew[NFMAX];
+  bstart_build(c);
+  tree_build_inactive(c, true, false);
+  sorted_lists(c, srt_new, knew);
+  double dlog = 0.0, dsign = 1.0, olog = 0.0, osign = 1.0;
+  bool singular = false;
+  for (int q = 0; q < 2 && !singular; ++q) {
+    const int f = q == 0 ? fa : fb;
+    if (q == 1 && fb == fa) break;
+    const int k = knew[f];
+    if (k > 0) {
+      const double* sc = srt_new + (size_t)(2 * f) * c.kcap;
+      if (!gj_inverse(c, f, k, sc, sc + c.kcap, c.dense, dlog, dsign)) {
+        singular = true;
+        break;
+      }
+      const double* I = c.dense + (size_t)c.kcap * c.kcap;
+      double* Mf = minv_new + (size_t)f * c.kcap * c.kcap;
+      for (int e = c.lane; e < k * k; e += 32) {
+        const int rc = e % k, ra = e / k;
+        Mf[(size_t)ra * c.kcap + rc] = I[(size_t)ra * c.kcap + rc];
+      }
+      __syncwarp();
+    }
+    lu_logdet_minv(c, f, c.dense, olog, osign);
+  }
+  double tr_lg = -DHUGE, tr_sg = 0.0, prob = 0.0;
+  const double det_lg = singular ? -DHUGE : dlog + olog;
+  const double det_sg = singular ? 0.0 : dsign * osign;
+  if (!singular) {
+    rebuilt_trace(c, h.outer_sst, tr_lg, tr_sg);
+    prob = fabs(__dmul_rn(factor, exp(__dsub_rn(tr_lg, h.trace_log) + det_lg)));
+  }
+  const double rnd = grnd(c);
+  r.det_log = det_lg;
+  r.det_sign = det_sg;
+  r.tr_log = tr_lg;
+  r.tr_sign = tr_sg;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    for (int q = 0; q < 2; ++q) {
+      const int f = q == 0 ? fa : fb;
+      if (q == 1 && fb == fa) break;
+      const int k = knew[f];
+      const double* src = minv_new + (size_t)f * c.kcap * c.kcap;
+      double* Mf = M_ptr(c, f);
+      for (int e = c.lane; e < k * k; e += 32) {
+        const size_t idx = (size_t)(e / k) * c.kcap + (e % k);
+        Mf[idx] = src[idx];
+      }
+      for (int ca = 0; ca < 2; ++ca) {
+        const double* st = srt_new + (size_t)(2 * f + ca) * c.kcap;
+        for (int i = c.lane; i < k; i += 32) {
+          srt_ptr(c, f, ca)[i] = st[i];
+          sslot_ptr(c, f, ca)[i] = (short)i;
+          stau_ptr(c, f, ca)[i] = st[i];
+        }
+      }
+    }
+    __syncwarp();
+    tree_flip_all(c);
+    if (c.g->o_chk) chk_invalidate(c);
+    if (c.lane == 0) {
+      h.k[fa] = knew[fa];
+      h.k[fb] = knew[fb];
+      h.det_log = h.det_log + det_lg;
+      h.det_sign = h.det_sign * det_sg;
+      h.trace_log = tr_lg;
+      h.trace_sign = tr_sg;
+      h.npairs = np_new;
+    }
+    __syncwarp();
+    const double sgn = config_sign(c);
+    if (c.lane == 0) h.cfgsign = -sgn;
+    __syncwarp();
+    return 4;
+  }
+  // restore the present arrays
+  const double* tau_old = glob_optau(c);
+  const int* opc_old = glob_opcode(c);
+  for (int i = c.lane; i < K_old; i += 32) {
+    c.optau[i] = tau_old[i];
+    c.opcode[i] = opc_old[i];
+  }
+  if (c.lane == 0) h.K = K_old;
+  __syncwarp();
+  bstart_build(c);
+  return 3;
+}
+
+// StepAdd4, CTQMC.F90:3615-3890.
+__device__ NOINL void ph_add4(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  cthyb_record& r = *c.rec;
+  if (c.lane == 0) h.try_add4++;
+  __syncwarp();
+  const int K = h.K;
+  const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  // pair_OperAdd with N = 4, force_diagonal (Trace.F90:3657-3702); each
+  // pair in time order (process_OperAdd)
+  double nt[4];
+  int nc[4];
+  double tdf = 1.0;
+  for (int pr = 0; pr < 2; ++pr) {
+    const double w = __dsub_rn(wmax, wmin);
+    const double tref = __dadd_rn(wmin, __dmul_rn(w, grnd(c)));
+    tdf = __dmul_rn(tdf, w);
+    const int orb = randint(c, 1, m.nd);
+    const int spin = randint(c, 1, 2);
+    const double tmin = fmax(__dsub_rn(tref, tdm), wmin);
+    const double w2 = __dsub_rn(fmin(__dadd_rn(tref, tdm), wmax), tmin);
+    const double tcr = __dadd_rn(tmin, __dmul_rn(w2, grnd(c)));
+    tdf = __dmul_rn(tdf, w2);
+    const int f = 2 * (orb - 1) + (spin - 1);
+    const bool afirst = tref < tcr;
+    nt[2 * pr] = afirst ? tref : tcr;
+    nc[2 * pr] = 2 * f + (afirst ? 1 : 0);
+    nt[2 * pr + 1] = afirst ? tcr : tref;
+    nc[2 * pr + 1] = 2 * f + (afirst ? 0 : 1);
+  }
+  const int fa = nc[0] >> 1, fb = nc[2] >> 1;
+  r.orb = fa + 1;
+  r.spin = fb + 1;
+  r.tau_c = nt[0];
+  r.tau_a = nt[1];
+  const int dk = fa == fb ? 2 : 1;
+  if (K + 4 > c.g->opcap || h.k[fa] + dk > c.kcap || h.k[fb] + dk > c.kcap) {
+    set_status(c, ST_CAPACITY);
+    return;
+  }
+  // equal times among the new operators or with present ones
+  bool equal = nt[0] == nt[1] || nt[0] == nt[2] || nt[0] == nt[3] || nt[1] == nt[2] || nt[1] == nt[3] ||
+               nt[2] == nt[3];
+  for (int i = c.lane; i < K; i += 32) {
+    const double t = c.optau[i];
+    equal = equal || t == nt[0] || t == nt[1] || t == nt[2] || t == nt[3];
+  }
+  equal = __any_sync(FULL, equal);
+  if (h.npairs == -1) {  // ensure_valid_NPairs
+    const int np = count_npairs(c);
+    if (c.lane == 0) h.npairs = np;
+    __syncwarp();
+  }
+  if (equal) {
+    r.outcome = 0;
+    __syncwarp();
+    return;
+  }
+  // superstates around the changed segment in the present configuration
+  const double t_first = fmin(nt[0], nt[2]), t_last = fmax(nt[1], nt[3]);
+  const int bs = old_prefix(c, h.outer_sst, t_first);
+  const int es = old_prefix(c, h.outer_sst, t_last);
+  // proposed arrays: merge the four operators in
+  double* tau_old = glob_optau(c);
+  int* opc_old = glob_opcode(c);
+  for (int i = c.lane; i < K; i += 32) {
+    tau_old[i] = c.optau[i];
+    opc_old[i] = c.opcode[i];
+  }
+  __syncwarp();
+  int q[4];
+  for (int j = 0; j < 4; ++j) {
+    int rank = 0;
+    for (int l = 0; l < 4; ++l) rank += nt[l] < nt[j];
+    q[j] = wlb(tau_old, K, nt[j], c.lane) + rank;
+  }
+  for (int i = c.lane; i < K; i += 32) {
+    const double t = tau_old[i];
+    const int d = (nt[0] < t) + (nt[1] < t) + (nt[2] < t) + (nt[3] < t);
+    c.optau[i + d] = t;
+    c.opcode[i + d] = opc_old[i];
+  }
+  if (c.lane < 4) {
+    c.optau[q[c.lane]] = nt[c.lane];
+    c.opcode[q[c.lane]] = nc[c.lane];
+  }
+  if (c.lane == 0) h.K = K + 4;
+  __syncwarp();
+  const int Kn = K + 4;
+  const int none[4] = {-1, -1, -1, -1};
+  const int s12[4] = {q[2], q[3], -1, -1}, s34[4] = {q[0], q[1], -1, -1};
+  const int np_12 = count_pairs_skip(c, c.optau, c.opcode, Kn, s12);
+  const int np_34 = count_pairs_skip(c, c.optau, c.opcode, Kn, s34);
+  const int np_all = count_pairs_skip(c, c.optau, c.opcode, Kn, none);
+  double rf;
+  int branch = 0;
+  if (rempair4(h, nt[0], nc[0], nt[3], nc[3]) && rempair4(h, nt[1], nc[1], nt[2], nc[2])) {
+    branch = 1;
+    const int sa[4] = {q[0], q[3], -1, -1}, sb[4] = {q[1], q[2], -1, -1};
+    const int np_23 = count_pairs_skip(c, c.optau, c.opcode, Kn, sa);
+    const int np_14 = count_pairs_skip(c, c.optau, c.opcode, Kn, sb);
+    rf = __dmul_rn(__ddiv_rn(1.0, (double)np_all),
+                   __dadd_rn(__dadd_rn(__dadd_rn(__ddiv_rn(1.0, (double)np_12), __ddiv_rn(1.0, (double)np_34)),
+                                       __ddiv_rn(1.0, (double)np_14)),
+                             __ddiv_rn(1.0, (double)np_23)));
+    tdf = __ddiv_rn(tdf, 4.0);
+  } else if (rempair4(h, nt[0], nc[0], nt[2], nc[2]) && rempair4(h, nt[1], nc[1], nt[3], nc[3])) {
+    branch = 2;
+    const int sa[4] = {q[0], q[2], -1, -1}, sb[4] = {q[1], q[3], -1, -1};
+    const int np_23 = count_pairs_skip(c, c.optau, c.opcode, Kn, sa);
+    const int np_14 = count_pairs_skip(c, c.optau, c.opcode, Kn, sb);
+    rf = __dmul_rn(__ddiv_rn(1.0, (double)np_all),
+                   __dadd_rn(__dadd_rn(__dadd_rn(__ddiv_rn(1.0, (double)np_12), __ddiv_rn(1.0, (double)np_34)),
+                                       __ddiv_rn(1.0, (double)np_14)),
+                             __ddiv_rn(1.0, (double)np_23)));
+    tdf = __ddiv_rn(tdf, 4.0);
+  } else {
+    rf = __dmul_rn(__ddiv_rn(1.0, (double)np_all),
+                   __dadd_rn(__ddiv_rn(1.0, (double)np_12), __ddiv_rn(1.0, (double)np_34)));
+    tdf = __ddiv_rn(tdf, 2.0);
+  }
+  r.change_outer = branch;
+  r.fpos_c = np_12;
+  r.fpos_a = np_34;
+  r.npairs = np_all;
+  // check_sst_sequence over the merged arrays from the earliest to the
+  // latest new operator
+  const int first = min(q[0], q[2]), last = max(q[1], q[3]);
+  const int w = bs < 0 ? -1 : walk_ops(c, bs, first, last + 1, none);
+  if (bs < 0 || w < 0 || w != es) {
+    for (int i = c.lane; i < K; i += 32) {
+      c.optau[i] = tau_old[i];
+      c.opcode[i] = opc_old[i];
+    }
+    if (c.lane == 0) h.K = K;
+    __syncwarp();
+    r.outcome = 1;
+    __syncwarp();
+    return;
+  }
+  const double n2 = 2.0 * m.nd;
+  const double factor = __dmul_rn(__dmul_rn(__dmul_rn(tdf, n2), n2), rf);
+  r.outcome = rebuild4_decide(c, fa, fb, factor, K, np_all);
+  if (r.outcome == 4 && c.lane == 0) h.acc_add4++;
+  r.outer_sst = h.outer_sst;
+  r.k_total = h.K;
+  __syncwarp();
+}
+
+// StepRem4, CTQMC.F90:4153-4431.
+__device__ NOINL void ph_rem4(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  cthyb_record& r = *c.rec;
+  if (c.lane == 0) h.try_rem4++;
+  __syncwarp();
+  const int K = h.K;
+  if (h.npairs == -1) {
+    const int np = count_npairs(c);
+    if (c.lane == 0) h.npairs = np;
+    __syncwarp();
+  }
+  const int np_old = h.npairs;
+  if (np_old <= 0) {
+    r.outcome = 2;
+    __syncwarp();
+    return;
+  }
+  const int none[4] = {-1, -1, -1, -1};
+  int a1, a2;
+  if (!select_pair_skip(c, c.optau, c.opcode, K, none, randint(c, 1, np_old), a1, a2)) {
+    set_status(c, ST_INTERNAL);
+    return;
+  }
+  const double ta1 = c.optau[a1], ta2 = c.optau[a2];
+  const int ca1 = c.opcode[a1], ca2 = c.opcode[a2];
+  const double f1 = remfac4(h, np_old, (ca1 & 1) ? ta1 : ta2);
+  const int sA[4] = {a1, a2, -1, -1};
+  const int np_34 = count_pairs_skip(c, c.optau, c.opcode, K, sA);
+  if (np_34 <= 0) {
+    r.outcome = 2;
+    __syncwarp();
+    return;
+  }
+  int b1, b2;
+  if (!select_pair_skip(c, c.optau, c.opcode, K, sA, randint(c, 1, np_34), b1, b2)) {
+    set_status(c, ST_INTERNAL);
+    return;
+  }
+  const double tb1 = c.optau[b1], tb2 = c.optau[b2];
+  const int cb1 = c.opcode[b1], cb2 = c.opcode[b2];
+  const double f2 = remfac4(h, np_34, (cb1 & 1) ? tb1 : tb2);
+  double tdf = __ddiv_rn(__ddiv_rn(__dmul_rn((double)np_old, (double)np_34), f1), f2);
+  const int sB[4] = {b1, b2, -1, -1};
+  const int np_12 = count_pairs_skip(c, c.optau, c.opcode, K, sB);
+  double rf;
+  int branch = 0;
+  if (rempair4(h, ta1, ca1, tb2, cb2) && rempair4(h, ta2, ca2, tb1, cb1)) {
+    branch = 1;
+    const int sa[4] = {a1, b2, -1, -1}, sb[4] = {a2, b1, -1, -1};
+    const int np_23 = count_pairs_skip(c, c.optau, c.opcode, K, sa);
+    const int np_14 = count_pairs_skip(c, c.optau, c.opcode, K, sb);
+    rf = __dmul_rn(__ddiv_rn(1.0, (double)np_old),
+                   __dadd_rn(__dadd_rn(__dadd_rn(__ddiv_rn(1.0, (double)np_12), __ddiv_rn(1.0, (double)np_34)),
+                                       __ddiv_rn(1.0, (double)np_14)),
+                             __ddiv_rn(1.0, (double)np_23)));
+    tdf = __ddiv_rn(tdf, 4.0);
+  } else if (rempair4(h, ta1, ca1, tb1, cb1) && rempair4(h, ta2, ca2, tb2, cb2)) {
+    branch = 2;
+    const int sa[4] = {a1, b1, -1, -1}, sb[4] = {a2, b2, -1, -1};
+    const int np_23 = count_pairs_skip(c, c.optau, c.opcode, K, sa);
+    const int np_14 = count_pairs_skip(c, c.optau, c.opcode, K, sb);
+    rf = __dmul_rn(__ddiv_rn(1.0, (double)np_old),
+                   __dadd_rn(__dadd_rn(__dadd_rn(__ddiv_rn(1.0, (double)np_12), __ddiv_rn(1.0, (double)np_34)),
+                                       __ddiv_rn(1.0, (double)np_14)),
+                             __ddiv_rn(1.0, (double)np_23)));
+    tdf = __ddiv_rn(tdf, 4.0);
+  } else {
+    rf = __dmul_rn(__ddiv_rn(1.0, (double)np_old),
+                   __dadd_rn(__ddiv_rn(1.0, (double)np_12), __ddiv_rn(1.0, (double)np_34)));
+    tdf = __ddiv_rn(tdf, 2.0);
+  }
+  const int fa = ca1 >> 1, fb = cb1 >> 1;
+  r.orb = fa + 1;
+  r.spin = fb + 1;
+  r.tau_c = ta1;
+  r.tau_a = ta2;
+  r.change_outer = branch;
+  r.fpos_c = np_12;
+  r.fpos_a = np_34;
+  const int gone[4] = {a1, a2, b1, b2};
+  const int np_new = count_pairs_skip(c, c.optau, c.opcode, K, gone);
+  r.npairs = np_new;
+  // check_sst_sequence over the operators left between the earliest and the
+  // latest removed one
+  const int first = min(a1, b1), last = max(a2, b2);
+  const int bs = old_prefix(c, h.outer_sst, c.optau[first]);
+  int es = old_prefix(c, h.outer_sst, c.optau[last]);
+  if (es >= 0) {
+    const int code = c.opcode[last];
+    es = m.connect[((size_t)es * m.nf + (code >> 1)) * 2 + (code & 1)];
+  }
+  const int w = bs < 0 ? -1 : walk_ops(c, bs, first + 1, last, gone);
+  if (bs < 0 || es < 0 || w < 0 || w != es) {
+    r.outcome = 1;
+    __syncwarp();
+    return;
+  }
+  // proposed arrays without the four operators
+  double* tau_old = glob_optau(c);
+  int* opc_old = glob_opcode(c);
+  for (int i = c.lane; i < K; i += 32) {
+    tau_old[i] = c.optau[i];
+    opc_old[i] = c.opcode[i];
+  }
+  __syncwarp();
+  for (int i = c.lane; i < K; i += 32) {
+    if (i == a1 || i == a2 || i == b1 || i == b2) continue;
+    const int d = (a1 < i) + (a2 < i) + (b1 < i) + (b2 < i);
+    c.optau[i - d] = tau_old[i];
+    c.opcode[i - d] = opc_old[i];
+  }
+  if (c.lane == 0) h.K = K - 4;
+  __syncwarp();
+  const double n2 = 2.0 * m.nd;
+  const double factor = __ddiv_rn(__ddiv_rn(__ddiv_rn(1.0, __dmul_rn(n2, n2)), tdf), rf);
+  r.outcome = rebuild4_decide(c, fa, fb, factor, K, np_new);
+  if (r.outcome == 4 && c.lane == 0) h.acc_rem4++;
+  r.outer_sst = h.outer_sst;
+  r.k_total = h.K;
+  __syncwarp();
+}
+
 // One proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250) with
 // the phases back to back.
 __device__ void one_step(Ctx& c, Prop& p) {
@@ -2533,7 +3032,9 @@ __device__ void one_step(Ctx& c, Prop& p) {
   ph_draw(c, p);
   if (p.rare) {
     if (p.move == 2) ph_global(c, p);
-    else ph_shift(c, p);
+    else if (p.move == 3) ph_shift(c, p);
+    else if (p.move == 5) ph_add4(c, p);
+    else ph_rem4(c, p);
     if (c.h->status == ST_OK) ph_finish(c, p);
     return;
   }
@@ -2932,6 +3433,7 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
   if (reset && c.lane == 0) {  // init_counters, CTQMC.F90:847-899
     h.try_add = h.acc_add = h.try_rem = h.acc_rem = h.qn_add = h.qn_rem = 0;
     h.try_glob = h.acc_glob = h.qn_glob = h.try_shift = h.acc_shift = 0;
+    h.try_add4 = h.acc_add4 = h.try_rem4 = h.acc_rem4 = 0;
     h.nprop = 0;
   }
   __syncwarp();
@@ -3003,6 +3505,8 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
       Hdr& h = *c.h;
       h.try_add = h.acc_add = h.try_rem = h.acc_rem = h.qn_add = h.qn_rem = 0;
       h.try_glob = h.acc_glob = h.qn_glob = h.try_shift = h.acc_shift = 0;
+      h.try_add4 = h.acc_add4 = h.try_rem4 = h.acc_rem4 = 0;
+    h.try_add4 = h.acc_add4 = h.try_rem4 = h.acc_rem4 = 0;
       h.nprop = 0;
     }
     __syncwarp();
@@ -3053,7 +3557,9 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
     if (__syncthreads_or(p.rare)) {  // global and tau-shift moves, rare
       if (p.rare) {
         if (p.move == 2) ph_global(c, p);
-        else ph_shift(c, p);
+        else if (p.move == 3) ph_shift(c, p);
+        else if (p.move == 5) ph_add4(c, p);
+        else ph_rem4(c, p);
       }
       __syncthreads();
     }
@@ -3572,6 +4078,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.p_outer = d.p_outer;
   g.p_global = d.p_global;
   g.p_shift = d.p_shift;
+  g.p_4op = d.p_4op;
   g.dense = (d.flags & CTHYB_FLAG_DENSE) ? 1 : 0;
   g.meas_dm = (d.flags & CTHYB_FLAG_NO_DM) ? 0 : 1;
   int kcap = d.kcap > 0 ? d.kcap : std::max(32, (int)std::min(4096.0, 32.0 * std::ceil(d.beta * 1.0 / 32.0 + 1.0)));
@@ -3653,10 +4160,10 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
     g.o_glscr = off;
     off = align_up(off + (size_t)32 * g.nleg * 8, 256);
   }
-  // work space of global and tau-shift moves: new inverse matrices, new
-  // sorted lists, copy of the operator arrays
+  // work space of global, tau-shift and 4-operator moves: new inverse
+  // matrices, new sorted lists, copy of the operator arrays
   g.o_glob = 0;
-  if (d.p_global > 0.0 || d.p_shift > 0.0) {
+  if (d.p_global > 0.0 || d.p_shift > 0.0 || d.p_4op > 0.0) {
     g.o_glob = off;
     off = align_up(off + ((size_t)nf * kcap * kcap + (size_t)nf * 2 * kcap + (opcap + 2)) * 8 +
                              (size_t)(opcap + 2) * 4,
@@ -4627,6 +5134,22 @@ int cthyb_debug_phase_cycles(cthyb_batch_t B, int64_t* out10) {
       CK(cudaMemcpy(&h, G.g.base + (size_t)c * G.g.stride + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost));
       for (int i = 0; i < 10; ++i) out10[i] += h.prof[i];
     }
+  return CTHYB_OK;
+}
+
+int cthyb_batch_move_counters4(cthyb_batch_t B, int chain, int64_t* out4) {
+  if (!out4) return fail(CTHYB_ERR_ARG, "null");
+  GroupHost* G;
+  int lc;
+  int rc = find_chain(B, chain, &G, &lc);
+  if (rc) return rc;
+  Hdr h;
+  rc = read_hdr(B, G, lc, h);
+  if (rc) return rc;
+  out4[0] = h.try_add4;
+  out4[1] = h.acc_add4;
+  out4[2] = h.try_rem4;
+  out4[3] = h.acc_rem4;
   return CTHYB_OK;
 }
 

@@ -49,6 +49,7 @@ struct Hdr {
   int kv, bv;  // dense-block models: ket checkpoints 0..kv and bra checkpoints bv..2^L are valid
   long long nprop, try_add, acc_add, try_rem, acc_rem, qn_add, qn_rem, cnt_meas, logn;
   long long try_glob, acc_glob, qn_glob, try_shift, acc_shift;
+  long long try_add4, acc_add4, try_rem4, acc_rem4;
   int k[NFMAX];
   // work counters for the roofline: M bytes, M flops, op-array bytes, tree node updates
   long long w_mbytes, w_mflops, w_opbytes, w_nodes;
@@ -66,6 +67,7 @@ struct DGroup {
   int nscore;          // parameter directions of the score-function dG/dtheta (0: none)
   const double* score_dE;  // [nscore][ns]
   double p_outer, p_global, p_shift;  // PercentageOuterMove, PercentageGlobalMove, PercentageTauShiftMove
+  double p_4op;                       // Percentage4OperatorMove
   int kcap, opcap, L, dense, meas_dm;
   char* base;          // chain c at base + c*stride
   size_t stride;

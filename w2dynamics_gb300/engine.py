@@ -29,7 +29,7 @@ EXPORTS = (
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
     "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_autotune", "cthyb_batch_results",
-    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
+    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_move_counters4", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_set_configs", "cthyb_batch_get_configs", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
     "cthyb_minv_rebuild_noalloc",
@@ -44,7 +44,7 @@ class GroupDesc(C.Structure):
                 ("opcap", C.c_int32), ("tree_levels", C.c_int32), ("maxhisto", C.c_int32),
                 ("flags", C.c_int32), ("p_global", C.c_double), ("p_shift", C.c_double),
                 ("nleg", C.c_int32), ("nscore", C.c_int32), ("score_dE", C.POINTER(C.c_double)),
-                ("nsym", C.c_int32), ("symmoves", C.POINTER(C.c_int32))]
+                ("nsym", C.c_int32), ("symmoves", C.POINTER(C.c_int32)), ("p_4op", C.c_double)]
 
 
 class EngineError(RuntimeError):
@@ -91,6 +91,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_autotune.argtypes = [vp, i64, C.POINTER(C.c_int)]
     L.cthyb_batch_results.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_move_counters.argtypes = [vp, C.c_int, C.POINTER(i64)]
+    L.cthyb_batch_move_counters4.argtypes = [vp, C.c_int, C.POINTER(i64)]
     L.cthyb_batch_results_extra.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp]
     L.cthyb_batch_gradients.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.cthyb_batch_results_score.argtypes = [vp, C.c_int, dp, dp]
@@ -178,7 +179,7 @@ class Group:
     def __init__(self, beta, ftau, ntau, nchains=1, seed0=0, seeds=None, taudiff_max=-1.0,
                  ncorr=100, p_outer=0.0, kcap=0, opcap=0, tree_levels=0, maxhisto=500,
                  dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0, score_dE=None,
-                 symmoves=None):
+                 symmoves=None, p_4op=0.0):
         self.beta = float(beta)
         self.ftau = np.asfortranarray(np.asarray(ftau, np.float64))
         self.ntau = int(ntau)
@@ -189,6 +190,7 @@ class Group:
         self.ncorr = int(ncorr)
         self.p_outer = float(p_outer)
         self.p_global, self.p_shift = float(p_global), float(p_shift)
+        self.p_4op = float(p_4op)
         self.nleg = int(nleg)
         self.score_dE = None if score_dE is None else np.ascontiguousarray(score_dE, np.float64)
         # user symmetry moves: rows of 1-based target flavours in the reference's
@@ -215,6 +217,7 @@ class Group:
         d.maxhisto = self.maxhisto
         d.flags = self.flags
         d.p_global, d.p_shift = self.p_global, self.p_shift
+        d.p_4op = self.p_4op
         d.nleg = self.nleg
         d.nscore = 0 if self.score_dE is None else self.score_dE.shape[0]
         d.score_dE = _dp(self.score_dE) if self.score_dE is not None else None
@@ -342,10 +345,15 @@ class Batch:
         return gd, gp[:, :npar], lw
 
     def move_counters(self, chain):
-        """Global and tau-shift move counters since the last warmup/measure call."""
+        """Global, tau-shift and 4-operator move counters since the last
+        warmup/measure call."""
         out = np.zeros(5, np.int64)
         _check(load().cthyb_batch_move_counters(self.h, chain, out.ctypes.data_as(C.POINTER(C.c_int64))))
-        return dict(zip(("try_glob", "acc_glob", "qn_glob", "try_shift", "acc_shift"), out.tolist()))
+        d = dict(zip(("try_glob", "acc_glob", "qn_glob", "try_shift", "acc_shift"), out.tolist()))
+        out4 = np.zeros(4, np.int64)
+        _check(load().cthyb_batch_move_counters4(self.h, chain, out4.ctypes.data_as(C.POINTER(C.c_int64))))
+        d.update(zip(("try_add4", "acc_add4", "try_rem4", "acc_rem4"), out4.tolist()))
+        return d
 
     def group_sums(self, group):
         g = self.groups[group]

@@ -148,10 +148,10 @@ def _str(key, default=None):
 
 def _check_supported():
     bad = []
-    for key in ("Percentage4OperatorMove", "PercentageWormInsert"):
-        if _real(key, 0.0) != 0.0:
-            bad.append(f"{key} = {_real(key)}")
-    for key in ("segment", "offdiag", "statesampling", "Phonon", "Screening", "Uw"):
+    if _real("PercentageWormInsert", 0.0) != 0.0:
+        bad.append(f"PercentageWormInsert = {_real('PercentageWormInsert')}")
+    for key in ("segment", "offdiag", "statesampling", "Phonon", "Screening", "Uw",
+                "flavourchange_moves"):
         if _int(key, 0) != 0:
             bad.append(f"{key} = {_int(key)}")
     if _int("Eigenbasis", 1) == 0:
@@ -187,7 +187,8 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
                     p_outer=_real("PercentageOuterMove", 0.0), maxhisto=_int("MaxHisto", 500) + 1,
                     measure_dm=_int("MeasDensityMatrix", 1) != 0,
                     p_global=_real("PercentageGlobalMove", 0.0),
-                    p_shift=_real("PercentageTauShiftMove", 0.0), nleg=_int("NLegMax", 100))
+                    p_shift=_real("PercentageTauShiftMove", 0.0), nleg=_int("NLegMax", 100),
+                    p_4op=_real("Percentage4OperatorMove", 0.0))
     nsym = _int("NSymMove", 0)
     if nsym > 0:  # SymMove01 ... (Trace.F90:471-477)
         group.symmoves = np.array([[int(x) for x in _raw("SymMove%02d" % (i + 1)).split()]
@@ -237,7 +238,7 @@ def ctqmc_measure(iSector=1, iComponent=1):
 
 def _collect():
     global gtau, gtau_full, histo, occ, rho1, rho2, densitymatrix, mean_sign, gleg, gleg_full
-    global accadd, accrem, accglob, accshift, outersuperstatehisto, outerstatehisto, signhistosuperstates
+    global accadd, accrem, accadd4, accrem4, accglob, accshift, outersuperstatehisto, outerstatehisto, signhistosuperstates
     global signhistostates, tracecontribsuperstates, tracecontribstates, lhisto, rhisto
     global ssquare, ssquare_operator
     nd, ns, nf = _nd, _model.nstates, 2 * _nd
@@ -257,6 +258,8 @@ def _collect():
     accrem = np.zeros(NWormSectors)
     accadd[0] = cnt["acc_add"] / max(cnt["try_add"], 1)
     accrem[0] = cnt["acc_rem"] / max(cnt["try_rem"], 1)
+    accadd4 = mcnt["acc_add4"] / mcnt["try_add4"] if mcnt["try_add4"] else 0.0
+    accrem4 = mcnt["acc_rem4"] / mcnt["try_rem4"] if mcnt["try_rem4"] else 0.0
     accglob = mcnt["acc_glob"] / mcnt["try_glob"] if mcnt["try_glob"] else float("nan")
     accshift = mcnt["acc_shift"] / mcnt["try_shift"] if mcnt["try_shift"] else float("nan")
     gtau_full = np.zeros((nd, 2, nd, 2, gtau.shape[-1]))
