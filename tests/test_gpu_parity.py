@@ -307,8 +307,9 @@ def test_batched_chains_match_oracle_per_seed(lib):
 @pytest.mark.parametrize("warps", [-1, 7, 32])
 def test_phase_synchronous_schedule_matches_oracle(lib, warps):
     """The phase-synchronous schedule (blocks of `warps` chains, a partial
-    last block; global and tau-shift moves at 2 % each) runs every chain as
-    the reference chain of its own seed, and
+    last block; global and tau-shift moves at 2 % each, 4-operator moves at
+    10 % of the insertions and removals) runs every chain as the reference
+    chain of its own seed, and
     its measurements equal the independent-warp schedule's: histogram and
     sign exactly, G(tau) and the density matrix to 1e-12 relative (G(tau)
     bins are summed with atomics, whose order is not fixed)."""
@@ -318,7 +319,8 @@ def test_phase_synchronous_schedule_matches_oracle(lib, warps):
     runs = []
     for sched in (0, warps):
         b = E.Batch(mg, [E.Group(10.0, pr["ftau"], 20, nchains=n, seed0=300, taudiff_max=5.0,
-                                 kcap=64, opcap=512, ncorr=50, p_global=0.02, p_shift=0.02)])
+                                 kcap=64, opcap=512, ncorr=50, p_global=0.02, p_shift=0.02,
+                                 p_4op=0.1)])
         b.set_schedule(sched)
         b.warmup(2000)
         b.measure(20)
@@ -327,7 +329,7 @@ def test_phase_synchronous_schedule_matches_oracle(lib, warps):
     mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
     for c in (0, 6, 7, 44):
         co = O.Chain(mo, 10.0, pr["ftau"], 20, seed=300 + c, taudiff_max=5.0, ncorr=50,
-                     p_global=0.02, p_shift=0.02)
+                     p_global=0.02, p_shift=0.02, p_4op=0.1)
         co.warmup(2000)
         co.measure(20)
         t_o, *_ = co.get_config()
@@ -352,7 +354,8 @@ def test_graph_replay_and_autotune_keep_the_chains():
     runs = []
     for graphs in (False, True):
         b = E.Batch(mg, [E.Group(10.0, pr["ftau"], 20, nchains=40, seed0=500, taudiff_max=5.0,
-                                 kcap=64, opcap=512, ncorr=50, p_global=0.02, p_shift=0.02)])
+                                 kcap=64, opcap=512, ncorr=50, p_global=0.02, p_shift=0.02,
+                                 p_4op=0.1)])
         b.use_graphs(graphs)
         for _ in range(2):
             b.warmup(300)

@@ -3506,16 +3506,16 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
       h.try_add = h.acc_add = h.try_rem = h.acc_rem = h.qn_add = h.qn_rem = 0;
       h.try_glob = h.acc_glob = h.qn_glob = h.try_shift = h.acc_shift = 0;
       h.try_add4 = h.acc_add4 = h.try_rem4 = h.acc_rem4 = 0;
-    h.try_add4 = h.acc_add4 = h.try_rem4 = h.acc_rem4 = 0;
       h.nprop = 0;
     }
     __syncwarp();
     total = nmeas <= 0 ? nprop : (long long)nmeas * gp->ncorr;
   }
-  // One barrier after each phase: draw, set-up, superstate tree + QN check,
-  // state tree, determinant, trace, decision, accepted-move updates,
-  // bookkeeping and measurement.  A warp with nothing to do in a phase
-  // (proposal ended, chain finished, no chain) only meets the barrier.
+  // One barrier after each phase: set-up, superstate tree + QN check, state
+  // tree, determinant, trace, decision with the accepted move's updates,
+  // rare moves (only when one is pending), and bookkeeping + measurement +
+  // the next draw.  A warp with nothing to do in a phase (proposal ended,
+  // chain finished, no chain) only meets the barrier.
   long long i = 0;
 #ifdef CTHYB_PROFILE
   // prof[k]: work of phase k (0..8, phase 8 = bookkeeping); prof[9]: waits
@@ -3534,27 +3534,33 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
   SPROF(k);            \
   __syncthreads();     \
   SPROF(9);
-  for (;;) {
-    const bool mine = valid && i < total && c.h->status == ST_OK;
-    if (!__syncthreads_or(mine)) break;
-    SPROF(9);
-    if (mine) {
-      ph_draw(c, p);
-    } else if (lane == 0) {
-      p.alive = 0;
-      p.rare = 0;
-    }
-    SPROF(0);
-    __syncthreads();
+  // the next proposal's draw shares the segment of the previous one's
+  // bookkeeping; the barrier that follows also decides whether any chain of
+  // the block is left
+  bool mine = valid && i < total && c.h->status == ST_OK;
+  if (mine) {
+    ph_draw(c, p);
+  } else if (lane == 0) {
+    p.alive = 0;
+    p.rare = 0;
+  }
+  SPROF(0);
+  while (__syncthreads_or(mine)) {
     SPROF(9);
     PHASE(1, if (p.move == 0) ph_setup_add(c, p); else ph_setup_rem(c, p))
     PHASE(2, ph_tree_ss(c, p))
     PHASE(3, ph_tree_states(c, p))
     PHASE(4, ph_det(c, p))
     PHASE(5, ph_trace(c, p))
-    PHASE(6, ph_decide(c, p))
-    PHASE(7, if (p.move == 0) ph_accept_add(c, p); else ph_accept_rem(c, p))
-    if (__syncthreads_or(p.rare)) {  // global and tau-shift moves, rare
+    if (p.alive) {
+      ph_decide(c, p);
+      if (p.alive) {
+        if (p.move == 0) ph_accept_add(c, p);
+        else ph_accept_rem(c, p);
+      }
+    }
+    SPROF(6);
+    if (__syncthreads_or(p.rare)) {
       if (p.rare) {
         if (p.move == 2) ph_global(c, p);
         else if (p.move == 3) ph_shift(c, p);
@@ -3569,6 +3575,14 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
       if (nmeas > 0 && i % gp->ncorr == 0 && c.h->status == ST_OK) measure(c);
     }
     SPROF(8);
+    mine = valid && i < total && c.h->status == ST_OK;
+    if (mine) {
+      ph_draw(c, p);
+    } else if (lane == 0) {
+      p.alive = 0;
+      p.rare = 0;
+    }
+    SPROF(0);
   }
 #undef PHASE
 #undef SPROF
