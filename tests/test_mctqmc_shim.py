@@ -116,3 +116,52 @@ def test_solve_through_the_module_matches_the_oracle():
     assert np.array_equal(taus, t_o) and outer2 == outer
     ctqmc.dest_ctqmc()
     ctqmc.dest_paras()
+
+
+@pytest.mark.gpu
+def test_warm_start_files_for_all_chains(tmp_path):
+    """save_mc_configs / load_mc_configs keep each of GPUChains = 6 chains'
+    configuration across solves; a one-configuration file in the driver's
+    CtHybConfig npz layout (cthyb_solver.py:78-87) goes to every chain; the
+    warm-started chains keep running."""
+    pr = P.config_problem("dd3", beta=10.0)
+    nd = 3
+    ftau = pr["ftau"]
+    ftau_full = np.zeros((nd, 2, nd, 2, ftau.shape[-1]))
+    for b in range(nd):
+        for s in range(2):
+            ftau_full[b, s, b, s] = ftau[b, s]
+    umat = np.asarray(pr["umatrix"]).reshape((2 * nd,) * 4)
+    par = dict(BASE, GPUChains=6, Nmeas=5)
+
+    def solver():
+        ctqmc.init_rnd(3)
+        ctqmc.init_paras(pstring(par))
+        ctqmc.init_solver(umat, ftau_full, pr["muimp"], np.zeros_like(ftau_full), 1)
+        ctqmc.set_taudiffmax(BASE["TaudiffMax"])
+
+    solver()
+    ctqmc.ctqmc_warmup(1500)
+    before = ctqmc.get_mc_configs()
+    assert len(before["offsets"]) == 7 and before["offsets"][-1] > 0
+    ctqmc.save_mc_configs(tmp_path / "cfg.npz")
+    ctqmc.dest_ctqmc()
+    solver()
+    ctqmc.load_mc_configs(tmp_path / "cfg.npz")
+    after = ctqmc.get_mc_configs()
+    for k in ("offsets", "taus", "orbs", "spins", "cas", "outer_sst"):
+        assert np.array_equal(before[k], after[k]), k
+    # one configuration in the driver's layout
+    n = before["offsets"][1]
+    np.savez(tmp_path / "one.npz", taus=before["taus"][:n], orbs=before["orbs"][:n],
+             spins=before["spins"][:n], cas=before["cas"][:n], hashybs=np.ones(n, int),
+             outer_sst=np.array([before["outer_sst"][0]]), outer_state=np.array([1]))
+    ctqmc.load_mc_configs(tmp_path / "one.npz")
+    rep = ctqmc.get_mc_configs()
+    assert np.array_equal(rep["offsets"], np.arange(7) * n)
+    for c in range(6):
+        assert np.array_equal(rep["taus"][c * n:(c + 1) * n], before["taus"][:n])
+    ctqmc.ctqmc_measure(1, 1)
+    assert np.isfinite(ctqmc.gtau).all()
+    ctqmc.dest_ctqmc()
+    ctqmc.dest_paras()

@@ -30,15 +30,21 @@ matches the first parameter whose name starts with it).
 Beyond the reference: ``GPUChains = n`` in the parameter string runs n
 independent chains (seeds Nseed .. Nseed+n-1) in one batch and combines
 their measurements as one longer run would (sign-weighted), the form in
-which the GPU is used efficiently.
+which the GPU is used efficiently.  set_mc_config / set_empty_mc_config
+give every chain the configuration; get_mc_configs / set_mc_configs and
+save_mc_configs / load_mc_configs keep one configuration per chain across
+solves (the batch form of the driver's mc_config_inout warm start and its
+CtHybConfig npz files, cthyb_solver.py:24-87, 316-345).
 
-Parameters selecting moves or modes outside the engine (4-operator and worm
-moves, segment, off-diagonal hybridisation, state sampling, retarded
-interactions) raise NotImplementedError at init_solver.  The trace-recomputation histograms lhisto/rhisto describe the
-reference's list-walking implementation and are returned as zeros; outer
-trace contributions are measured for density-density (monomial) models.  Each init_solver seeds the chains
-from Nseed; the reference continues one global random stream across
-solves, so solves after the first draw different (equally valid) streams.
+Parameters selecting moves or modes outside the engine (worm and
+flavour-change moves, segment, off-diagonal hybridisation, state sampling,
+retarded interactions) raise NotImplementedError at init_solver.  The
+trace-recomputation histograms lhisto/rhisto describe the reference's
+list-walking implementation and are returned as zeros; outer trace
+contributions are measured for density-density (monomial) models.  Each
+init_solver seeds the chains from Nseed; the reference continues one global
+random stream across solves, so solves after the first draw different
+(equally valid) streams.
 """
 import time
 
@@ -317,18 +323,68 @@ def get_mc_config(N):
 
 
 def set_mc_config(N, taus, orbs, spins, cas, hashybs, outer_sst, outer_state):
+    """set_mc_config (CTQMC.F90:9378): the configuration goes to every chain
+    of the solver (one upload for all GPUChains chains)."""
     n = int(N)
     if np.any(np.asarray(hashybs)[:n] == 0):
         raise NotImplementedError("operators without hybridisation (worms) are not supported")
-    for c in range(_nchains):
-        _batch.set_config(c, np.asarray(taus)[:n], np.asarray(orbs)[:n], np.asarray(spins)[:n],
-                          np.asarray(cas)[:n], int(outer_sst))
+    arrs = [np.asarray(a)[:n] for a in (taus, orbs, spins, cas)]
+    _replicate(arrs, int(outer_sst))
 
 
 def set_empty_mc_config(outer_sst, outer_state):
-    for c in range(_nchains):
-        _batch.set_config(c, np.zeros(0), np.zeros(0, np.int32), np.zeros(0, np.int32),
-                          np.zeros(0, np.int32), int(outer_sst))
+    """set_empty_mc_config (CTQMC.F90:9391) for every chain."""
+    _replicate([np.zeros(0), np.zeros(0, np.int32), np.zeros(0, np.int32), np.zeros(0, np.int32)],
+               int(outer_sst))
+
+
+def _replicate(arrs, outer_sst):
+    n = len(arrs[0])
+    offs = np.arange(_nchains + 1, dtype=np.int32) * n
+    _batch.set_configs(offs, *[np.tile(a, _nchains) for a in arrs], np.full(_nchains, outer_sst, np.int32))
+
+
+def get_mc_configs():
+    """Every chain's configuration in one read (the batch form of
+    get_mc_config): dict of offsets (chain c's operators are entries
+    offsets[c] .. offsets[c+1]-1), taus, orbs, spins, cas, hashybs (1-based
+    as get_mc_config), outer_sst and outer_state per chain."""
+    offs, t, o, s, c, outer = _batch.get_configs()
+    return dict(offsets=offs, taus=t, orbs=o, spins=s, cas=c, hashybs=np.ones(len(t), np.int32),
+                outer_sst=outer, outer_state=np.ones(len(outer), np.int32))
+
+
+def set_mc_configs(cfg):
+    """Inverse of get_mc_configs: chain c takes configuration c (one upload)."""
+    offs = np.asarray(cfg["offsets"], np.int32)
+    if len(offs) != _nchains + 1:
+        raise ValueError(f"{len(offs) - 1} configurations for {_nchains} chains")
+    if np.any(np.asarray(cfg["hashybs"]) == 0):
+        raise NotImplementedError("operators without hybridisation (worms) are not supported")
+    _batch.set_configs(offs, cfg["taus"], cfg["orbs"], cfg["spins"], cfg["cas"], cfg["outer_sst"])
+
+
+def save_mc_configs(file):
+    """All chains' configurations to an npz file with the keys of the
+    driver's CtHybConfig.save_to_file (cthyb_solver.py:78-87) plus
+    `offsets`; outer_sst/outer_state hold one entry per chain."""
+    np.savez(file, **get_mc_configs())
+
+
+def load_mc_configs(file):
+    """Warm start from an npz file: a file of save_mc_configs gives chain c
+    its own configuration; a file of the driver's CtHybConfig (one
+    configuration, no `offsets`) goes to every chain like set_mc_config."""
+    with np.load(file) as f:
+        if "offsets" in f.files:
+            set_mc_configs({k: f[k] for k in f.files})
+        else:
+            t = f["taus"]
+            if t.size:
+                set_mc_config(t.size, t, f["orbs"], f["spins"], f["cas"], f["hashybs"],
+                              int(f["outer_sst"][0]), int(f["outer_state"][0]))
+            else:
+                set_empty_mc_config(int(f["outer_sst"][0]), int(f["outer_state"][0]))
 
 
 def dest_ctqmc():
