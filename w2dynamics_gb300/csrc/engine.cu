@@ -4102,14 +4102,17 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   int opcap = d.opcap > 0 ? d.opcap : std::max(64, std::min(nf * kcap * 2, (int)(64 + 16 * d.beta)));
   g.kcap = kcap;
   g.opcap = opcap;
-  // Default depth: two leaves up to 512 operators, then one level more per
-  // factor four (measured optimum of the proposal rate for density-density
-  // models: the leaf rebuild grows with the operators of a bin, the combine
-  // steps with the depth).
+  // Default depth: two leaves up to 512 operators, beyond that leaves of at
+  // most 128 operators of capacity (measured optimum of the phase-
+  // synchronous sweep for density-density models: at beta = 100 with
+  // opcap 1024 depth 3 beats depth 2 by 2 % of the batch rate, at beta = 50
+  // with opcap 512 depth 1 beats depth 2; the leaf rebuild grows with the
+  // operators of a bin, the combine steps with the depth).
   int L = d.tree_levels;
   if (L <= 0) {
     L = 1;
-    while ((512ll << (2 * (L - 1))) < opcap && L < 10) ++L;
+    if (opcap > 512)
+      while ((128ll << L) < opcap && L < 10) ++L;
   }
   if (L > 10) L = 10;  // the sweep keeps 2^(L+1) active bits per chain in shared memory
   g.L = L;
