@@ -435,6 +435,14 @@ struct Chain {
   long long try_add = 0, try_rem = 0, acc_add = 0, acc_rem = 0, accqn_add = 0, accqn_rem = 0;
   long long try_glob = 0, acc_glob = 0, accqn_glob = 0, try_shift = 0, acc_shift = 0;
   long long try_add4 = 0, acc_add4 = 0, try_rem4 = 0, acc_rem4 = 0;
+  // off-diagonal hybridisation (offdiag = 1): F for every flavour pair, one
+  // inverse matrix over all flavours in block order (flavour-major, time
+  // within a flavour; rows creators, columns annihilators), G for every
+  // flavour pair
+  bool offdiag = false;
+  std::vector<double> hybr_full;  // [(f1 * nf + f2) * nftau + t]
+  std::vector<double> minv_full;  // column-major, k_total x k_total
+  std::vector<double> gtau_full;  // [(f_annihilator * nf + f_creator) * ntau + bin]
   // measurements
   long long cnt_meas = 0;
   double meas_sign = 0;
@@ -504,11 +512,6 @@ static void shift_window(Chain& c) {
 }
 
 // Number of annihilators/creators with tau in [lo, hi] (sorted array)
-static int count_in(const std::vector<double>& v, double lo, double hi) {
-  auto a = std::lower_bound(v.begin(), v.end(), lo);
-  auto b = std::upper_bound(v.begin(), v.end(), hi);
-  return b > a ? int(b - a) : 0;
-}
 
 // ensure_valid_NPairs_diag, Trace.F90:1762-1803: pairs {x<y} of one flavour,
 // opposite CA, x.tau >= win_min, y.tau <= win_max, y.tau <= x.tau + tdm.
@@ -1898,6 +1901,420 @@ static void step_rem4(Chain& c) {
   record(c, r);
 }
 
+// ---------------------------------------------------------------------------
+// Off-diagonal hybridisation (offdiag = 1, fast updates): StepAdd / StepRem
+// with unconstrained flavours (pair_OperAdd force_diagonal = .false.),
+// get_HybrF_full, one inverse matrix over all flavours in block order
+// (get_LogDetRatPairAdd_full / get_LogDetRatPairRem_full with
+// add_ftau_offset, Trace.F90:2835-3040), removable pairs of any flavours
+// (ensure_valid_NPairs_offdiag / update_NPairs_offdiag, Trace.F90:1818-1992),
+// (2 Nd)^2 proposal factors (CTQMC.F90:3517-3523, 4050-4056), the sign
+// from recalc_sign (Trace.F90:3479-3545).
+
+// get_HybrF_full(tau, b1, s1, b2, s2): F of flavour pair (f1, f2)
+static inline double hybrf_full(const Chain& c, double tau, int f1, int f2) {
+  double sig;
+  if (tau < 0.0) {
+    tau = tau + c.p.beta;
+    sig = -1.0;
+  } else {
+    sig = 1.0;
+  }
+  const double* F = &c.hybr_full[((size_t)f1 * c.nf + f2) * c.p.nftau];
+  double n = tau / c.p.beta * double(c.p.nftau - 1);
+  int i = int(n);
+  if (i > c.p.nftau - 2) i = c.p.nftau - 2;
+  return sig * (F[i] + (n - double(int(n))) * (F[i + 1] - F[i]));
+}
+
+// 1-based position in block order of rank r (0-based) in flavour f's list
+// of creators (ca 0) or annihilators (ca 1) (add_ftau_offset)
+static int block_pos(const Chain& c, int f, int ca, int r) {
+  int o = 0;
+  for (int g = 0; g < f; ++g) o += (int)(ca == 0 ? c.tau_c[g] : c.tau_a[g]).size();
+  return o + r + 1;
+}
+static int total_creators(const Chain& c) {
+  int n = 0;
+  for (int f = 0; f < c.nf; ++f) n += (int)c.tau_c[f].size();
+  return n;
+}
+
+// ensure_valid_NPairs_offdiag: pairs x < y of opposite CA, any flavours,
+// x.tau >= win_min, y.tau <= win_max, y.tau <= x.tau + tdm
+static int count_pairs_offdiag(const Chain& c, const std::vector<Op>& ops) {
+  int n = 0;
+  const int K = (int)ops.size();
+  for (int i = 0; i < K; ++i) {
+    const Op& x = ops[i];
+    if (x.tau < c.tauwin_min) continue;
+    if (x.tau > c.tauwin_max) break;
+    for (int j = i + 1; j < K; ++j) {
+      const Op& y = ops[j];
+      if (y.tau > c.tauwin_max || y.tau > x.tau + c.taudiff_max) break;
+      if (y.ca != x.ca) ++n;
+    }
+  }
+  return n;
+}
+
+// recalc_sign (Trace.F90:3500-3545): exchange count of the operator keys
+// (3 - CA) * 100000 + Orbital * 10000 + Spin * 1000 + tau (1-based CA,
+// orbital, spin) under the reference's double loop, plus sum_{i < n/2} i.
+static int recalc_sign(const Chain& c) {
+  std::vector<double> op;
+  op.reserve(c.ops.size());
+  for (const Op& e : c.ops)
+    op.push_back(double(3 - (e.ca + 1)) * 100000.0 + double(e.b + 1) * 10000.0 + double(e.s + 1) * 1000.0 + e.tau);
+  long perm = 0;
+  const int n = (int)op.size();
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      if (op[i] > op[j]) {
+        std::swap(op[i], op[j]);
+        ++perm;
+      }
+  for (int i = 1; i <= n / 2 - 1; ++i) perm += i;
+  return (perm % 2) ? -1 : 1;
+}
+static double config_sign_offdiag(const Chain& c) {
+  return c.trace.sign * c.det.sign * double(recalc_sign(c));
+}
+
+// S - R.M.Q over the full matrix for a new creator oc and annihilator oa:
+// Q over the present annihilators, R over the present creators, both in
+// block order.  As the reference (Trace.F90:2892), Q passes the flavour
+// pair (creator, annihilator) to get_HybrF_full, R and S (annihilator,
+// creator).
+static double det_ratio_add_full(const Chain& c, const Op& oc, const Op& oa, std::vector<double>& Q,
+                                 std::vector<double>& R, double& S) {
+  const int fc = c.fi(oc.b, oc.s), fa = c.fi(oa.b, oa.s);
+  S = hybrf_full(c, oa.tau - oc.tau, fa, fc);
+  Q.clear();
+  R.clear();
+  for (int f = 0; f < c.nf; ++f)
+    for (double t : c.tau_a[f]) Q.push_back(hybrf_full(c, t - oc.tau, fc, f));
+  for (int f = 0; f < c.nf; ++f)
+    for (double t : c.tau_c[f]) R.push_back(hybrf_full(c, oa.tau - t, fa, f));
+  const int k = (int)R.size();
+  double r = S;
+  for (int i = 0; i < k; ++i)
+    for (int j = 0; j < k; ++j) r = r - R[i] * c.minv_full[(size_t)j * k + i] * Q[j];
+  return r;
+}
+
+// Full hybridisation matrix in block order (get_FullHybr_offdiag,
+// Trace.F90:2690-2770): H(pos_a, pos_c) = F(tau_a - tau_c; f_a, f_c),
+// column-major k x k.
+static std::vector<double> full_hybr_offdiag(const Chain& c) {
+  std::vector<std::pair<double, int>> cr, an;
+  for (int f = 0; f < c.nf; ++f) {
+    for (double t : c.tau_c[f]) cr.push_back({t, f});
+    for (double t : c.tau_a[f]) an.push_back({t, f});
+  }
+  const int k = (int)cr.size();
+  std::vector<double> H((size_t)k * k);
+  for (int ic = 0; ic < k; ++ic)
+    for (int ia = 0; ia < k; ++ia)
+      H[(size_t)ic * k + ia] = hybrf_full(c, an[ia].first - cr[ic].first, an[ia].second, cr[ic].second);
+  return H;
+}
+
+// Proposed list with the pair inserted and the 0-based positions of its
+// earlier and later operator.
+static std::vector<Op> with_pair(const Chain& c, const Op& o1, const Op& o2, int& q1, int& q2, int& p1,
+                                 int& p2old) {
+  const int K = (int)c.ops.size();
+  auto lb = [&](double t) {
+    return (int)(std::lower_bound(c.ops.begin(), c.ops.end(), t, [](const Op& e, double v) { return e.tau < v; }) -
+                 c.ops.begin());
+  };
+  p1 = lb(o1.tau);
+  p2old = lb(o2.tau);
+  std::vector<Op> nops;
+  nops.reserve(K + 2);
+  nops.insert(nops.end(), c.ops.begin(), c.ops.begin() + p1);
+  nops.push_back(o1);
+  nops.insert(nops.end(), c.ops.begin() + p1, c.ops.begin() + p2old);
+  nops.push_back(o2);
+  nops.insert(nops.end(), c.ops.begin() + p2old, c.ops.end());
+  q1 = p1;
+  q2 = p2old + 1;
+  return nops;
+}
+
+// StepAdd, CTQMC.F90:3353-3613, off-diagonal branch.
+static void step_add_offdiag(Chain& c, bool change_outer) {
+  c.try_add++;
+  Record r{};
+  r.move = 0;
+  r.change_outer = change_outer;
+  // pair_OperAdd(force_diagonal = .false.): annihilator at tau_ref with its
+  // own orbital and spin, creator within TaudiffMax with its own
+  double tdf = 1.0;
+  const double w = c.tauwin_max - c.tauwin_min;
+  const double tau_ref = c.tauwin_min + w * c.rng.grnd();
+  tdf = tdf * w;
+  const int orb_a = c.rng.randint(1, c.nd);
+  const int spin_a = c.rng.randint(1, 2);
+  const double tmin = std::max(tau_ref - c.taudiff_max, c.tauwin_min);
+  const double w2 = std::min(tau_ref + c.taudiff_max, c.tauwin_max) - tmin;
+  const double tau_c = tmin + w2 * c.rng.grnd();
+  tdf = tdf * w2;
+  const int orb_c = c.rng.randint(1, c.nd);
+  const int spin_c = c.rng.randint(1, 2);
+  const Op oa{tau_ref, orb_a - 1, spin_a - 1, 1}, oc{tau_c, orb_c - 1, spin_c - 1, 0};
+  const int fa = c.fi(oa.b, oa.s), fc = c.fi(oc.b, oc.s);
+  r.orb = fc + 1;  // creator and annihilator flavours (1-based)
+  r.spin = fa + 1;
+  r.tau_c = tau_c;
+  r.tau_a = tau_ref;
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  bool equal = (tau_ref == tau_c);
+  for (const Op& e : c.ops)
+    if (e.tau == tau_ref || e.tau == tau_c) equal = true;
+  if (equal) {
+    c.accqn_add++;
+    r.outcome = OUT_EQUALTIME;
+    record(c, r);
+    return;
+  }
+  const int rc = (int)(std::lower_bound(c.tau_c[fc].begin(), c.tau_c[fc].end(), tau_c) - c.tau_c[fc].begin());
+  const int ra = (int)(std::lower_bound(c.tau_a[fa].begin(), c.tau_a[fa].end(), tau_ref) - c.tau_a[fa].begin());
+  const int pos_c = block_pos(c, fc, 0, rc), pos_a = block_pos(c, fa, 1, ra);
+  r.fpos_c = pos_c;
+  r.fpos_a = pos_a;
+  const Op o1 = oa.tau < oc.tau ? oa : oc, o2 = oa.tau < oc.tau ? oc : oa;
+  int q1, q2, p1, p2old;
+  std::vector<Op> nops = with_pair(c, o1, o2, q1, q2, p1, p2old);
+  int new_outer = c.outer_sst;
+  bool qn_ok;
+  if (!change_outer) {
+    int bs = sector_before(c, p1);
+    int es = sector_before(c, p2old);
+    int wk = walk(c, nops, bs, q1, q2 + 1);
+    qn_ok = (bs >= 0 && wk >= 0 && wk == es);
+  } else {
+    int inside = sector_before(c, p2old);
+    int s2 = walk(c, nops, inside, q2, (int)nops.size());
+    new_outer = s2;
+    if (s2 < 0) qn_ok = false;
+    else {
+      int back = walk(c, nops, s2, 0, q1 + 1);
+      qn_ok = (back >= 0 && back == sector_before(c, p1));
+    }
+  }
+  if (!qn_ok) {
+    c.accqn_add++;
+    r.outcome = OUT_QN;
+    record(c, r);
+    return;
+  }
+  std::vector<double> Q, R;
+  double S;
+  const double dr = det_ratio_add_full(c, oc, oa, Q, R, S);
+  const double sig = double(1 - 2 * (std::abs(pos_c - pos_a) % 2));
+  const LogVal detrat{std::log(std::fabs(dr)), (dr >= 0 ? 1.0 : -1.0) * sig};
+  const bool fresh = change_outer && new_outer != c.outer_sst;
+  std::vector<Cache> mid, fb;
+  std::vector<LogVal> part;
+  const LogVal trnew = proposed_trace(c, nops, q1 + 1, q2 + 1, 2, fresh, new_outer, mid, &part, &fb);
+  const double rnd = c.rng.grnd();
+  const int np_new = count_pairs_offdiag(c, nops);
+  const LogVal trrat = ldiv(trnew, c.trace);
+  const double wr = std::exp(trrat.log + detrat.log);
+  const double n2 = 2.0 * c.nd;
+  const double prob = std::fabs(tdf * (n2 * n2) / double(np_new) * wr * 1.0);
+  r.det_log = detrat.log;
+  r.det_sign = detrat.sign;
+  r.tr_log = trnew.log;
+  r.tr_sign = trnew.sign;
+  r.prob = prob;
+  r.rand = rnd;
+  r.npairs = np_new;
+  if (rnd < prob) {
+    const int k = total_creators(c);
+    c.minv_full = mat_add(c.minv_full, k, Q, R, dr, pos_c, pos_a);
+    c.tau_c[fc].insert(c.tau_c[fc].begin() + rc, tau_c);
+    c.tau_a[fa].insert(c.tau_a[fa].begin() + ra, tau_ref);
+    c.ops.swap(nops);
+    c.det = lmul(detrat, c.det);
+    c.trace = trnew;
+    c.parttrace = part;
+    c.npairs = np_new;
+    std::vector<Cache> nk(c.ops.size() + 2), nb(c.ops.size() + 2);
+    const int Kn = (int)c.ops.size();
+    if (!fresh) {
+      for (int j = 0; j <= q1; ++j) nk[j] = std::move(c.kets[j]);
+      for (int j = q1 + 1; j <= q2 + 1; ++j) nk[j] = std::move(mid[j - (q1 + 1)]);
+      for (int j = q2 + 2; j <= Kn + 1; ++j) nb[j] = std::move(c.bras[j - 2]);
+    } else {
+      for (int j = 1; j <= q2 + 1; ++j) nk[j] = std::move(mid[j - 1]);
+      nk[0] = outer_identity(c, new_outer);
+      for (int j = q2 + 2; j <= Kn + 1; ++j) nb[j] = std::move(fb[j]);
+    }
+    c.kets.swap(nk);
+    c.bras.swap(nb);
+    c.kv = q2 + 1;
+    c.bv = q2 + 2;
+    c.outer_sst = new_outer;
+    c.cfgsign = -config_sign_offdiag(c);
+    c.acc_add++;
+    r.outcome = OUT_ACCEPT;
+  } else {
+    r.outcome = OUT_REJECT;
+  }
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  record(c, r);
+}
+
+// StepRem, CTQMC.F90:3892-4151, off-diagonal branch.
+static void step_rem_offdiag(Chain& c, bool change_outer) {
+  c.try_rem++;
+  Record r{};
+  r.move = 1;
+  r.change_outer = change_outer;
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  if (c.npairs == -1) c.npairs = count_pairs_offdiag(c, c.ops);
+  if (c.npairs <= 0) {
+    c.accqn_rem++;
+    r.outcome = OUT_NOPAIRS;
+    record(c, r);
+    return;
+  }
+  // gen_OperRemove, offdiag: the npair-th pair of opposite CA in the window
+  int npair = c.rng.randint(1, c.npairs);
+  int ix = -1, iy = -1;
+  const int K = (int)c.ops.size();
+  for (int i = 0; i < K && ix < 0; ++i) {
+    const Op& x = c.ops[i];
+    if (x.tau < c.tauwin_min) continue;
+    for (int j = i + 1; j < K; ++j) {
+      const Op& y = c.ops[j];
+      if (y.tau > c.tauwin_max || y.tau > x.tau + c.taudiff_max) break;
+      if (y.ca == x.ca) continue;
+      if (--npair <= 0) {
+        ix = i;
+        iy = j;
+        break;
+      }
+    }
+  }
+  const Op x = c.ops[ix], y = c.ops[iy];
+  const Op& oc = x.ca == 0 ? x : y;
+  const Op& oa = x.ca == 0 ? y : x;
+  const int fc = c.fi(oc.b, oc.s), fa = c.fi(oa.b, oa.s);
+  const int rc = (int)(std::lower_bound(c.tau_c[fc].begin(), c.tau_c[fc].end(), oc.tau) - c.tau_c[fc].begin());
+  const int ra = (int)(std::lower_bound(c.tau_a[fa].begin(), c.tau_a[fa].end(), oa.tau) - c.tau_a[fa].begin());
+  const int pos_c = block_pos(c, fc, 0, rc), pos_a = block_pos(c, fa, 1, ra);
+  const double hprf =
+      double(c.npairs) / ((c.tauwin_max - c.tauwin_min) *
+                          (std::min(oa.tau + c.taudiff_max, c.tauwin_max) - std::max(oa.tau - c.taudiff_max, c.tauwin_min)));
+  r.orb = fc + 1;
+  r.spin = fa + 1;
+  r.tau_c = oc.tau;
+  r.tau_a = oa.tau;
+  r.fpos_c = pos_c;
+  r.fpos_a = pos_a;
+  r.npairs = c.npairs;
+  std::vector<Op> nops;
+  nops.reserve(K);
+  for (int j = 0; j < K; ++j)
+    if (j != ix && j != iy) nops.push_back(c.ops[j]);
+  int new_outer = c.outer_sst;
+  bool qn_ok;
+  if (!change_outer) {
+    int bs = sector_before(c, ix);
+    int es = sector_before(c, iy + 1);
+    int wk = walk(c, nops, bs, ix, iy - 1);
+    qn_ok = (bs >= 0 && wk >= 0 && wk == es);
+  } else {
+    int inside = sector_before(c, iy);
+    int s2 = walk(c, nops, inside, iy - 1, (int)nops.size());
+    new_outer = s2;
+    if (s2 < 0) qn_ok = false;
+    else {
+      int back = walk(c, nops, s2, 0, ix);
+      qn_ok = (back >= 0 && back == sector_before(c, ix + 1));
+    }
+  }
+  if (!qn_ok) {
+    c.accqn_rem++;
+    r.outcome = OUT_QN;
+    record(c, r);
+    return;
+  }
+  const int k = total_creators(c);
+  const double dr = c.minv_full[(size_t)(pos_a - 1) * k + (pos_c - 1)];
+  const double sig = double(1 - 2 * (std::abs(pos_c - pos_a) % 2));
+  const LogVal detrat{std::log(std::fabs(dr)), (dr >= 0 ? 1.0 : -1.0) * sig};
+  const bool fresh = change_outer && new_outer != c.outer_sst;
+  std::vector<Cache> mid, fb;
+  std::vector<LogVal> part;
+  const int lo = ix + 1, hi = iy - 1;
+  LogVal trnew;
+  if (hi >= lo || fresh) {
+    trnew = proposed_trace(c, nops, fresh ? 1 : lo, fresh ? std::max(hi, 0) : hi, -2, fresh, new_outer, mid, &part, &fb);
+  } else {
+    extend_kets(c, ix);
+    extend_bras(c, iy + 2);
+    const double tauR = ix >= 1 ? c.ops[ix - 1].tau : 0.0;
+    const double tauL = iy + 1 < K ? c.ops[iy + 1].tau : c.p.beta;
+    trnew = close_trace(c, c.kets[ix], tauR, c.bras[iy + 2], tauL, &part);
+  }
+  const LogVal trrat = ldiv(trnew, c.trace);
+  const double wr = std::exp(trrat.log + detrat.log);
+  const double n2 = 2.0 * c.nd;
+  const double prob = std::fabs(hprf / (n2 * n2) * wr * 1.0);
+  const double rnd = c.rng.grnd();
+  r.det_log = detrat.log;
+  r.det_sign = detrat.sign;
+  r.tr_log = trnew.log;
+  r.tr_sign = trnew.sign;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    c.minv_full = mat_rem(c.minv_full, k, pos_c, pos_a);
+    c.tau_c[fc].erase(c.tau_c[fc].begin() + rc);
+    c.tau_a[fa].erase(c.tau_a[fa].begin() + ra);
+    const int Kn = K - 2;
+    std::vector<Cache> nk(Kn + 2), nb(Kn + 2);
+    if (!fresh) {
+      for (int j = 0; j <= ix; ++j) nk[j] = std::move(c.kets[j]);
+      for (int j = lo; j <= hi; ++j) nk[j] = std::move(mid[j - lo]);
+      for (int j = iy; j <= Kn + 1; ++j) nb[j] = std::move(c.bras[j + 2]);
+      c.kv = std::max(hi, ix);
+      c.bv = std::max(hi, ix) + 1;
+    } else {
+      nk[0] = outer_identity(c, new_outer);
+      const int h = std::max(hi, 0);
+      for (int j = 1; j <= h; ++j) nk[j] = std::move(mid[j - 1]);
+      for (int j = h + 1; j <= Kn + 1; ++j) nb[j] = std::move(fb[j]);
+      c.kv = h;
+      c.bv = h + 1;
+    }
+    c.ops.swap(nops);
+    c.kets.swap(nk);
+    c.bras.swap(nb);
+    c.det = lmul(detrat, c.det);
+    c.trace = trnew;
+    c.parttrace = part;
+    c.outer_sst = new_outer;
+    c.cfgsign = -config_sign_offdiag(c);
+    c.npairs = count_pairs_offdiag(c, c.ops);
+    c.acc_rem++;
+    r.outcome = OUT_ACCEPT;
+  } else {
+    r.outcome = OUT_REJECT;
+  }
+  r.outer_sst = c.outer_sst;
+  r.k_total = (int)c.ops.size();
+  record(c, r);
+}
+
 // one proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250)
 static int one_step(Chain& c) {
   double rand_num = c.rng.grnd();
@@ -1905,14 +2322,16 @@ static int one_step(Chain& c) {
   if (rand_num < p_add) {
     if (c.rng.grnd() >= c.p.p_4op) {
       bool co = c.rng.grnd() < c.p.p_outer;
-      step_add(c, co);
+      if (c.offdiag) step_add_offdiag(c, co);
+      else step_add(c, co);
     } else {
       step_add4(c);
     }
   } else if (rand_num <= 1.0 - c.p.p_shift - c.p.p_global) {
     if (c.rng.grnd() >= c.p.p_4op) {
       bool co = c.rng.grnd() < c.p.p_outer;
-      step_rem(c, co);
+      if (c.offdiag) step_rem_offdiag(c, co);
+      else step_rem(c, co);
     } else {
       step_rem4(c);
     }
@@ -1970,6 +2389,36 @@ static void meas_gtau(Chain& c) {
         }
       }
   }
+}
+
+// MeasGtauRem_full, CTQMC.F90:2475-2584: every creator (row pos1) with
+// every annihilator (column pos2) of the full inverse matrix, into the bin
+// of tau_a - tau_c (wrapped with a sign change), times the configuration
+// sign, at G(f_annihilator, f_creator).
+static void meas_gtau_full(Chain& c) {
+  const int nt = c.p.ntau, k = total_creators(c);
+  if (k == 0) return;
+  int p1 = 0;
+  for (int fcr = 0; fcr < c.nf; ++fcr)
+    for (double tc : c.tau_c[fcr]) {
+      int p2 = 0;
+      for (int fan = 0; fan < c.nf; ++fan)
+        for (double ta : c.tau_a[fan]) {
+          double M = c.minv_full[(size_t)p2 * k + p1];
+          int idt;
+          if (ta - tc > 0.0) {
+            idt = int((ta - tc) / c.p.beta * double(nt)) + 1;
+          } else {
+            idt = int((c.p.beta + ta - tc) / c.p.beta * double(nt)) + 1;
+            M = -M;
+          }
+          M = M * c.cfgsign;
+          if (idt > nt) idt = nt;
+          c.gtau_full[((size_t)fan * c.nf + fcr) * nt + (idt - 1)] += M;
+          ++p2;
+        }
+      ++p1;
+    }
 }
 
 // MeasOuterHistograms, CTQMC.F90:3285-3341 (no state sampling)
@@ -2150,6 +2599,36 @@ void* orc_chain_create(void* model, const Params* p, const double* hybr_fortran)
   }
   return c;
 }
+// Chain with off-diagonal hybridisation (offdiag = 1): F for every flavour
+// pair, Ftau_full(Nd,2,Nd,2,Nftau) in Fortran order.  Pair and
+// outer-superstate moves; global, tau-shift and 4-operator moves and the
+// Legendre measurement are not part of the restatement in this mode.
+void* orc_chain_create_full(void* model, const Params* p, const double* hybr_full_fortran) {
+  if (p->p_global > 0.0 || p->p_shift > 0.0 || p->p_4op > 0.0 || p->nleg > 0) {
+    g_err = "off-diagonal chains restate pair and outer-superstate moves only";
+    return nullptr;
+  }
+  Model* m = (Model*)model;
+  const int nd = m->nd, nf = 2 * nd;
+  std::vector<double> diag((size_t)nd * 2 * p->nftau);
+  for (int b = 0; b < nd; ++b)
+    for (int s = 0; s < 2; ++s)
+      for (int t = 0; t < p->nftau; ++t)
+        diag[b + nd * (s + 2 * (size_t)t)] =
+            hybr_full_fortran[b + nd * (s + 2 * (b + nd * (s + 2 * (size_t)t)))];
+  Chain* c = (Chain*)orc_chain_create(model, p, diag.data());
+  c->offdiag = true;
+  c->hybr_full.resize((size_t)nf * nf * p->nftau);
+  for (int b1 = 0; b1 < nd; ++b1)
+    for (int s1 = 0; s1 < 2; ++s1)
+      for (int b2 = 0; b2 < nd; ++b2)
+        for (int s2 = 0; s2 < 2; ++s2)
+          for (int t = 0; t < p->nftau; ++t)
+            c->hybr_full[((size_t)c->fi(b1, s1) * nf + c->fi(b2, s2)) * p->nftau + t] =
+                hybr_full_fortran[b1 + nd * (s1 + 2 * (b2 + nd * (s2 + 2 * (size_t)t)))];
+  c->gtau_full.assign((size_t)nf * nf * p->ntau, 0.0);
+  return c;
+}
 void orc_chain_destroy(void* c) { delete (Chain*)c; }
 
 void orc_chain_set_taudiffmax(void* cc, double tdm) { init_window(*(Chain*)cc, tdm); }
@@ -2186,14 +2665,15 @@ int orc_chain_measure(void* cc, long long nmeas) {
     c.cnt_meas++;
     c.meas_sign += c.cfgsign;  // MeasSign
     meas_outer(c);
-    for (int f = 0; f < c.nf; ++f) {  // MeasExpOrder
-      int k = (int)c.tau_c[f].size();
+    for (int f = 0; f < c.nf; ++f) {  // MeasExpOrder: NOSOper(b,s)/2
+      int k = int(c.tau_c[f].size() + c.tau_a[f].size()) / 2;
       int hmax = std::max(c.p.maxhisto, 1);
       if (k < hmax - 1) c.histo[(size_t)f * hmax + k] += 1.0;
       else c.histo[(size_t)f * hmax + hmax - 1] += 1.0;
     }
     if (c.p.meas_dm) meas_dm(c);
-    meas_gtau(c);
+    if (c.offdiag) meas_gtau_full(c);
+    else meas_gtau(c);
   }
   return 0;
 }
@@ -2324,6 +2804,24 @@ int orc_chain_set_config(void* cc, int n, const double* taus, const int* orbs, c
 }
 
 // sorted inverse hybridisation matrix of flavour f = 2b+s (k x k col-major)
+// The inverse matrix over all flavours (off-diagonal mode), block order,
+// column-major; returns its dimension.
+int orc_chain_minv_full(void* cc, double* out) {
+  Chain& c = *(Chain*)cc;
+  const int k = c.offdiag ? total_creators(c) : 0;
+  if (out && k) std::memcpy(out, c.minv_full.data(), sizeof(double) * (size_t)k * k);
+  return k;
+}
+// G for every flavour pair (off-diagonal mode), [f_annihilator][f_creator][bin],
+// normalised as Gtau_full (CTQMC.F90:8752-8753).
+void orc_chain_results_full(void* cc, double* gtau_full) {
+  Chain& c = *(Chain*)cc;
+  const double ms = c.meas_sign / double(c.cnt_meas);
+  const double zs = -1.0 / (double(c.cnt_meas) * ms);
+  const int nt = c.p.ntau;
+  for (size_t i = 0; i < c.gtau_full.size(); ++i)
+    gtau_full[i] = -c.gtau_full[i] * zs * double(nt) / (c.p.beta * c.p.beta);
+}
 int orc_chain_minv(void* cc, int f, double* out) {
   Chain& c = *(Chain*)cc;
   int k = (int)c.tau_c[f].size();
@@ -2342,6 +2840,14 @@ void orc_chain_full_trace(void* cc, double* out) {
 // log|det| and sign of the full rebuild (does not modify the chain)
 void orc_chain_full_det(void* cc, double* out) {
   Chain& c = *(Chain*)cc;
+  if (c.offdiag) {  // get_FullHybr_offdiag + get_MatLogDetFull
+    std::vector<double> H = full_hybr_offdiag(c);
+    bool sing;
+    LogVal d = lu_logdet_inverse(H, total_creators(c), sing);
+    out[0] = d.log;
+    out[1] = d.sign;
+    return;
+  }
   std::vector<std::vector<double>> save = c.minv;
   LogVal d = rebuild_minv(c);
   c.minv.swap(save);

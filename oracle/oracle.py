@@ -60,6 +60,10 @@ def lib():
         L.orc_model_evec.argtypes = [vp, C.c_int, dp]
         L.orc_chain_create.restype = vp
         L.orc_chain_create.argtypes = [vp, C.POINTER(Params), dp]
+        L.orc_chain_create_full.restype = vp
+        L.orc_chain_create_full.argtypes = [vp, C.POINTER(Params), dp]
+        L.orc_chain_minv_full.argtypes = [vp, dp]
+        L.orc_chain_results_full.argtypes = [vp, dp]
         L.orc_chain_destroy.argtypes = [vp]
         L.orc_chain_set_taudiffmax.argtypes = [vp, C.c_double]
         L.orc_chain_set_log.argtypes = [vp, C.c_void_p, C.c_longlong]
@@ -146,13 +150,16 @@ class Chain:
     def __init__(self, model, beta, ftau, ntau, seed, taudiff_max=-1.0, ncorr=100,
                  p_outer=0.0, maxhisto=500, meas_dm=1, p_global=0.0, p_shift=0.0, nleg=0,
                  symmoves=None, p_4op=0.0):
+        """ftau: (Nd, 2, Nftau) diagonal F, or (Nd, 2, Nd, 2, Nftau) for the
+        off-diagonal mode (offdiag = 1)."""
         L = lib()
         self.model = model
         nd = model.nd
         ftau = np.asarray(ftau, dtype=np.float64)
-        assert ftau.shape[:2] == (nd, 2)
+        self.offdiag = ftau.ndim == 5
+        assert ftau.shape[:2] == (nd, 2) and (not self.offdiag or ftau.shape[2:4] == (nd, 2))
         self._ftau = np.asfortranarray(ftau)
-        self.nftau = ftau.shape[2]
+        self.nftau = ftau.shape[-1]
         self.ntau = ntau
         self.maxhisto = maxhisto
         p = Params(beta=beta, nftau=self.nftau, ntau=ntau, ncorr=ncorr, seed=seed,
@@ -164,8 +171,27 @@ class Chain:
             p.nsym = self._sym.shape[0]
             p.symmoves = self._sym.ctypes.data_as(C.POINTER(C.c_int32))
         self.params = p
-        self.h = L.orc_chain_create(model.h, C.byref(p), _dp(self._ftau.ravel(order="F")))
+        create = L.orc_chain_create_full if self.offdiag else L.orc_chain_create
+        self.h = create(model.h, C.byref(p), _dp(self._ftau.ravel(order="F")))
+        if not self.h:
+            raise RuntimeError(L.orc_last_error().decode())
         self._log = None
+
+    def results_full(self):
+        """Off-diagonal mode: G for every flavour pair, (2Nd, 2Nd, Ntau) with
+        index [f_annihilator, f_creator], f = 2b + s (Gtau_full)."""
+        nf = 2 * self.model.nd
+        out = np.zeros(nf * nf * self.ntau)
+        lib().orc_chain_results_full(self.h, _dp(out))
+        return out.reshape(nf, nf, self.ntau)
+
+    def minv_full(self):
+        """Off-diagonal mode: the inverse matrix over all flavours in block
+        order (rows creators, columns annihilators)."""
+        k = lib().orc_chain_minv_full(self.h, None)
+        out = np.zeros(max(k, 1) ** 2)
+        lib().orc_chain_minv_full(self.h, _dp(out))
+        return out[:k * k].reshape((k, k), order="F")
 
     def set_taudiffmax(self, tdm):
         lib().orc_chain_set_taudiffmax(self.h, tdm)

@@ -82,3 +82,117 @@ def occupations(beta, mu, u, eps, v):
     p = np.exp(-beta * (w - w.min()))
     rho = (q * (p / p.sum())) @ q.T
     return (np.trace(rho @ num[0]), np.trace(rho @ num[1]), np.trace(rho @ num[0] @ num[1]))
+
+
+def ftau_full_bath(beta, eps, v, nftau):
+    """F_{s s'}(tau), shape (1, 2, 1, 2, nftau), of spinless bath levels eps_b
+    coupled to impurity spin s with amplitude v[b][s] (the bath-site formula
+    with V*_{b s} V_{b s'}, w2dyn/auxiliaries/transform.py:140-144)."""
+    tau = np.linspace(0.0, beta, nftau)
+    out = np.zeros((1, 2, 1, 2, nftau))
+    for b, e in enumerate(eps):
+        g = 1.0 / (np.exp(-tau * e) + np.exp((beta - tau) * e))
+        for s in range(2):
+            for s2 in range(2):
+                out[0, s, 0, s2] += v[b][s] * v[b][s2] * g
+    return out
+
+
+def offdiag_answers(beta, mu, u, eps, v, ntau, nsub=64):
+    """Exact <d+_s d_s'> (2 x 2), <n_up n_dn> and bin averages of
+    <d_s(tau) d+_s'(0)> (2, 2, ntau) for the impurity with spinless bath
+    levels of spin-dependent amplitudes v[b][s]."""
+    nb = len(eps)
+    ops = _fermions(2 + nb)
+    num = [x.T @ x for x in ops]
+    h = -mu * (num[0] + num[1]) + u * num[0] @ num[1]
+    for b in range(nb):
+        h = h + eps[b] * num[2 + b]
+        for s in range(2):
+            h = h + v[b][s] * (ops[s].T @ ops[2 + b] + ops[2 + b].T @ ops[s])
+    w, q = np.linalg.eigh(h)
+    w = w - w.min()
+    z = np.exp(-beta * w).sum()
+    rho = (q * (np.exp(-beta * w) / z)) @ q.T
+    rho1 = np.array([[np.trace(rho @ ops[a].T @ ops[b]) for b in range(2)] for a in range(2)])
+    dbl = np.trace(rho @ num[0] @ num[1])
+    d = [q.T @ ops[s] @ q for s in range(2)]
+    edges = np.linspace(0.0, beta, ntau + 1)
+    g = np.zeros((2, 2, ntau))
+    for i in range(ntau):
+        t = edges[i] + (np.arange(nsub) + 0.5) * (edges[i + 1] - edges[i]) / nsub
+        el = np.exp(-(beta - t)[:, None] * w[None, :])  # e^{-(beta - tau) w_m}
+        er = np.exp(-t[:, None] * w[None, :])           # e^{-tau w_n}
+        for a in range(2):
+            for b in range(2):
+                # Tr[e^{-(beta-tau)H} d_a e^{-tau H} d+_b] / Z
+                g[a, b, i] = np.mean(np.einsum("tm,mn,tn,nm->t", el, d[a], er, d[b].T)) / z
+    return dict(rho1=rho1, double_occ=dbl, gtau=g)
+
+
+def impurity_hamiltonian(nd, umatrix, muimp, ops):
+    """H_loc = sum_ij muimp_ij d+_i d_j + 1/2 sum_ijkl U_ijkl d+_i d+_j d_l d_k
+    on the first 2 nd modes of `ops` (flavour f = 2b + s), the solver's
+    convention for muimp (Nd,2,Nd,2) and the flat U matrix."""
+    nf = 2 * nd
+    u = np.asarray(umatrix, np.float64).reshape((nf,) * 4)
+    mu = np.asarray(muimp, np.float64).reshape(nd, 2, nd, 2)
+    d = ops[:nf]
+    h = 0.0
+    for i in range(nf):
+        for j in range(nf):
+            t = mu[i // 2, i % 2, j // 2, j % 2]
+            if t != 0.0:
+                h = h + t * d[i].T @ d[j]
+    for i in range(nf):
+        for j in range(nf):
+            for k in range(nf):
+                for l in range(nf):
+                    if u[i, j, k, l] != 0.0:
+                        h = h + 0.5 * u[i, j, k, l] * d[i].T @ d[j].T @ d[l] @ d[k]
+    return h
+
+
+def ftau_full_spinful(nd, beta, eps, v, nftau):
+    """F (Nd,2,Nd,2,nftau) of spinful bath levels eps_b coupled to orbital o
+    of either spin with amplitude v[b][o] (spin-diagonal, orbital-mixing)."""
+    tau = np.linspace(0.0, beta, nftau)
+    out = np.zeros((nd, 2, nd, 2, nftau))
+    for b, e in enumerate(eps):
+        g = 1.0 / (np.exp(-tau * e) + np.exp((beta - tau) * e))
+        for o1 in range(nd):
+            for o2 in range(nd):
+                for s in range(2):
+                    out[o1, s, o2, s] += v[b][o1] * v[b][o2] * g
+    return out
+
+
+def spinful_answers(nd, beta, umatrix, muimp, eps, v, ntau, nsub=32):
+    """Exact G_ab(tau) bin averages <d_a(tau) d+_b(0)> (2nd, 2nd, ntau) and
+    <n_a> for the impurity with spinful bath levels of ftau_full_spinful."""
+    nf, nb = 2 * nd, len(eps)
+    ops = _fermions(nf + 2 * nb)
+    h = impurity_hamiltonian(nd, umatrix, muimp, ops)
+    for b in range(nb):
+        for s in range(2):
+            cb = ops[nf + 2 * b + s]
+            h = h + eps[b] * cb.T @ cb
+            for o in range(nd):
+                f = 2 * o + s
+                h = h + v[b][o] * (ops[f].T @ cb + cb.T @ ops[f])
+    w, q = np.linalg.eigh(h)
+    w = w - w.min()
+    z = np.exp(-beta * w).sum()
+    rho = (q * (np.exp(-beta * w) / z)) @ q.T
+    occ = np.array([np.trace(rho @ ops[f].T @ ops[f]) for f in range(nf)])
+    d = [q.T @ ops[f] @ q for f in range(nf)]
+    edges = np.linspace(0.0, beta, ntau + 1)
+    g = np.zeros((nf, nf, ntau))
+    for i in range(ntau):
+        t = edges[i] + (np.arange(nsub) + 0.5) * (edges[i + 1] - edges[i]) / nsub
+        el = np.exp(-(beta - t)[:, None] * w[None, :])
+        er = np.exp(-t[:, None] * w[None, :])
+        for a in range(nf):
+            for b2 in range(nf):
+                g[a, b2, i] = np.mean(np.einsum("tm,mn,tn,nm->t", el, d[a], er, d[b2].T)) / z
+    return dict(occ=occ, gtau=g)
