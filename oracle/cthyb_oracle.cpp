@@ -1,9 +1,11 @@
 // cthyb_oracle.cpp -- TEST INFRASTRUCTURE ONLY (the oracle).
 //
-// CPU restatement of the w2dynamics CT-HYB pair-insertion/removal loop
-// (Fortran module `ctqmc`, matrix-vector path, diagonal hybridisation).
-// It is the checker for the GPU library and the timed CPU baseline; it is
-// never linked into, loaded by, or called from the product library.
+// CPU restatement of the w2dynamics CT-HYB Z-space loop (Fortran module
+// `ctqmc`, matrix-vector path): pair insertion/removal, outer-superstate,
+// global, tau-shift and 4-operator moves with diagonal hybridisation, and
+// pair moves with off-diagonal hybridisation (offdiag = 1).  It is the
+// checker for the GPU library and the timed CPU baseline; it is never
+// linked into, loaded by, or called from the product library.
 //
 // Parity status: the Fortran reference cannot be compiled here (no Fortran
 // compiler, no LAPACK), so this file restates it routine by routine.  It is
@@ -16,7 +18,9 @@
 // .F90:5-58, and U matrices generated by the reference's own
 // w2dyn/dmft/interaction.py.  Determinant ratios and traces are further
 // checked against dense FP64 recomputation (LU and full Fock-space
-// matrix exponentials) in the test suite.
+// matrix exponentials) in the test suite, and the sampled distributions
+// (expansion orders, occupations, G(tau) for every flavour pair) against
+// exact diagonalisation of an impurity with a discrete bath.
 //
 // Data layout follows the reference semantics with arrays instead of the
 // pointer lists of src/ctqmc_fortran/Trace.F90:27-62 (TOper): one globally

@@ -2,8 +2,10 @@
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
 this module.  It wraps oracle/cthyb_oracle.cpp, the CPU restatement of the
-w2dynamics pair-move CT-HYB loop (src/ctqmc_fortran/CTQMC.F90 StepAdd /
-StepRem and the MTrace / MMatrixUpdate routines they call).
+w2dynamics CT-HYB Z-space loop (src/ctqmc_fortran/CTQMC.F90 StepAdd /
+StepRem / StepAdd4 / StepRem4 / StepGlob / StepShiftTau and the MTrace /
+MMatrixUpdate routines they call; off-diagonal hybridisation for pair
+moves).
 """
 import ctypes as C
 import os
