@@ -99,6 +99,11 @@ typedef struct {
                               (b-1) + Nd*(s-1) + 1 (Trace.F90:471-477) */
   double p_4op;          /* Percentage4OperatorMove: share of insertions and removals made as
                             4-operator moves (StepAdd4 / StepRem4, CTQMC.F90:3615-3890, 4153-4431) */
+  const double* ftau_full; /* offdiag = 1: F for every flavour pair, (Nd,2,Nd,2,Nftau) Fortran
+                              order (NULL: diagonal hybridisation from ftau).  Pair and
+                              outer-superstate moves only; kcap then bounds the total number of
+                              pairs; the inverse matrix over all flavours is in the reference's
+                              block order (add_ftau_offset, Trace.F90:3002-3040). */
 } cthyb_group_desc;
 
 #define CTHYB_FLAG_DENSE 1  /* dense block trace even for monomial models */
@@ -194,6 +199,13 @@ int cthyb_batch_move_counters(cthyb_batch_t batch, int chain, int64_t* counters5
 /* 4-operator move counters since the last warmup/measure call:
  * TryAdd4, AccAdd4, TryRem4, AccRem4 (CTQMC.F90:134-136). */
 int cthyb_batch_move_counters4(cthyb_batch_t batch, int chain, int64_t* out4);
+/* Off-diagonal groups: G for every flavour pair, (2Nd, 2Nd, Ntau) with index
+ * [f_annihilator][f_creator][bin], f = 2(b-1)+(s-1), normalised as
+ * Gtau_full (CTQMC.F90:8752-8753; MeasGtauRem_full, CTQMC.F90:2475-2584). */
+int cthyb_batch_results_full(cthyb_batch_t batch, int chain, double* gtau_full);
+/* Off-diagonal groups: the inverse matrix over all flavours (rows creators,
+ * columns annihilators, block order, column-major k x k); k in *k. */
+int cthyb_batch_minv_full(cthyb_batch_t batch, int chain, int* k, double* out);
 
 /* Normalised results of one chain (CTQMC.F90:8676-8760):
  *   gtau (Nd,2,Ntau) Fortran order, mean_sign, densitymatrix in the

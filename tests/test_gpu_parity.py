@@ -538,3 +538,76 @@ def test_capacity_limit_and_invalid_configurations(lib):
     assert b2.state(0)["noper"] == 0
     b2.warmup(100)
     b2.sync()
+
+
+def _offdiag_problem(kind):
+    """One orbital with a spin-mixing bath ("Nt"), or two orbitals with
+    inter-orbital hopping (dense H_loc) and an orbital-mixing bath."""
+    import exact_bath as XB
+    if kind == "spin":
+        beta = 4.0
+        um = P.flat_umatrix(P.umatrix_density(1, 2.0, 2.0, 0.0))
+        muimp = P.muimp_solver(1, 1.3)
+        ff = XB.ftau_full_bath(beta, [-0.6, 0.9], [[0.6, 0.3], [0.5, -0.4]], 2000)
+        return 1, beta, um, muimp, ff, "Nt"
+    nd, beta = 2, 3.0
+    um = P.flat_umatrix(P.umatrix_density(nd, 2.0, 2.0, 0.0))
+    muimp = P.muimp_solver(nd, 1.0).copy()
+    for s in range(2):
+        muimp[0, s, 1, s] = muimp[1, s, 0, s] = -0.3
+    ff = XB.ftau_full_spinful(nd, beta, [-0.5, 0.7], [[0.6, 0.3], [0.4, -0.5]], 2000)
+    return nd, beta, um, muimp, ff, "Nt Szt"
+
+
+def _diag_of(ff):
+    nd = ff.shape[0]
+    return np.stack([np.stack([ff[b, s, b, s] for s in range(2)]) for b in range(nd)])
+
+
+@pytest.mark.parametrize("kind,tdm,pout,nprop,seed", [("spin", 1.5, 0.1, 20000, 5),
+                                                      ("spin", -1.0, 0.0, 10000, 9),
+                                                      ("orbital", -1.0, 0.1, 6000, 6),
+                                                      ("orbital", 1.0, 0.1, 6000, 8)])
+def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, nprop, seed):
+    """Off-diagonal hybridisation (offdiag = 1): the GPU chain proposes,
+    decides and updates like the oracle chain of the same seed, proposal by
+    proposal (flavours, block positions, pair counts, outcomes bit-exact;
+    ratios to 1e-10); then the measured G for every flavour pair, the
+    order histogram and the sign agree, and so do the final configuration
+    and the inverse matrix over all flavours."""
+    nd, beta, um, muimp, ff, qns = _offdiag_problem(kind)
+    ntau = 10
+    mo = O.Model(nd, um, muimp, qns)
+    co = O.Chain(mo, beta, ff, ntau, seed=seed, taudiff_max=tdm, p_outer=pout, ncorr=20, maxhisto=30)
+    co.start_log(nprop)
+    co.warmup(nprop)
+    ref = co.log()
+    mg = E.Model(nd, um, muimp, qns)
+    b = E.Batch(mg, [E.Group(beta, _diag_of(ff), ntau, nchains=1, seed0=seed, taudiff_max=tdm,
+                             p_outer=pout, ncorr=20, maxhisto=30, kcap=64, opcap=256,
+                             ftau_full=ff)])
+    b.set_log(nprop)
+    b.warmup(nprop)
+    b.sync()
+    got = b.log(0)
+    compare_logs(ref, got)
+    assert np.sum((ref["outcome"] == 4) & (ref["move"] == 0)) > 20
+    co.measure(300)
+    b.measure(300)
+    b.sync()
+    ro, rg = co.results(), b.results(0)
+    assert ro["mean_sign"] == rg["mean_sign"]
+    nf = 2 * nd
+    assert np.array_equal(ro["histo"], np.stack([rg["histo"][f // 2, f % 2] for f in range(nf)]))
+    go, gg = co.results_full(), b.results_full(0)
+    assert np.allclose(gg, go, rtol=1e-9, atol=1e-12 * np.abs(go).max())
+    t_o, *_ = co.get_config()
+    t_g, *_ = b.get_config(0)
+    assert np.array_equal(t_o, t_g)
+    mo_, mg_ = co.minv_full(), b.minv_full(0)
+    assert mo_.shape == mg_.shape
+    if mo_.size:
+        assert np.allclose(mg_, mo_, rtol=1e-9, atol=1e-9 * np.abs(mo_).max())
+    so, sg = co.state(), b.state(0)
+    assert so["cfgsign"] == sg["cfgsign"] and so["det_sign"] == sg["det_sign"]
+    assert abs(so["det_log"] - sg["det_log"]) < 1e-8

@@ -165,3 +165,36 @@ def test_warm_start_files_for_all_chains(tmp_path):
     assert np.isfinite(ctqmc.gtau).all()
     ctqmc.dest_ctqmc()
     ctqmc.dest_paras()
+
+
+@pytest.mark.gpu
+def test_offdiag_solve_through_the_module_matches_the_oracle():
+    """offdiag = 1 through the module (pair and outer-superstate moves): the
+    Gtau_full of the solve equals the oracle chain of the same seed."""
+    import exact_bath as XB
+    beta = 4.0
+    ff = XB.ftau_full_bath(beta, [-0.6, 0.9], [[0.6, 0.3], [0.5, -0.4]], 2000)
+    um = P.flat_umatrix(P.umatrix_density(1, 2.0, 2.0, 0.0))
+    muimp = P.muimp_solver(1, 1.3)
+    par = dict(BASE, beta=beta, Nd=1, Ntau=10, QuantumNumbers="Nt", offdiag=1, Nmeas=400,
+               NCorr=20, PercentageGlobalMove=0.0, PercentageTauShiftMove=0.0,
+               Percentage4OperatorMove=0.0, TaudiffMax=1.5, NSymMove=0, MeasSsquare=0)
+    ctqmc.init_rnd(17)
+    ctqmc.init_paras(pstring(par))
+    ctqmc.init_solver(np.asarray(um).reshape((2,) * 4), ff, muimp, np.zeros_like(ff), 1)
+    ctqmc.set_taudiffmax(1.5)
+    ctqmc.ctqmc_warmup(3000)
+    ctqmc.ctqmc_measure(1, 1)
+    mo = O.Model(1, um, muimp, "Nt")
+    co = O.Chain(mo, beta, ff, 10, seed=17, taudiff_max=1.5, ncorr=20, p_outer=0.1,
+                 maxhisto=par["MaxHisto"] + 1)
+    co.set_taudiffmax(1.5)
+    co.warmup(3000)
+    co.measure(400)
+    go = co.results_full()
+    got = np.array([[ctqmc.gtau_full[fa // 2, fa % 2, fc // 2, fc % 2] for fc in range(2)] for fa in range(2)])
+    assert np.allclose(got, go, rtol=1e-9, atol=1e-12 * np.abs(go).max())
+    assert np.abs(go[0, 1]).max() > 0.01
+    assert ctqmc.mean_sign == co.results()["mean_sign"]
+    ctqmc.dest_ctqmc()
+    ctqmc.dest_paras()

@@ -1452,6 +1452,12 @@ __device__ NOINL void ph_draw(Ctx& c, Prop& p) {
     if (move == 0) h.try_add++;
     else h.try_rem++;
   }
+  if (c.g->offdiag) {  // off-diagonal pair moves run in the rare-move phase
+    p.move = move + 7;
+    p.rare = 1;
+    __syncwarp();
+    return;
+  }
   p.alive = 1;
   __syncwarp();
 }
@@ -3025,6 +3031,608 @@ __device__ NOINL void ph_rem4(Ctx& c, Prop& p) {
   __syncwarp();
 }
 
+// ---------------------------------------------------------------------------
+// Off-diagonal hybridisation (offdiag = 1): StepAdd / StepRem with
+// unconstrained flavours (pair_OperAdd force_diagonal = .false.,
+// Trace.F90:3657-3702), F for every flavour pair (get_HybrF_full), one
+// inverse matrix over all flavours in the reference's block order
+// (flavour-major, time within a flavour; rows creators, columns
+// annihilators; get_LogDetRatPairAdd_full / get_LogDetRatPairRem_full with
+// add_ftau_offset, Trace.F90:2835-3040), removable pairs of any flavours
+// (Trace.F90:1818-1992), (2 Nd)^2 proposal factors (CTQMC.F90:3517-3523,
+// 4050-4056) and the configuration sign of recalc_sign (Trace.F90:3479-3545).
+// These proposals run in the rare-move phase: the proposed operator arrays
+// are written in place (old ones saved in the o_glob space), the tree is
+// rebuilt into the inactive slots and the full trace taken from it; the
+// determinant ratio is the fast S - R.M.Q over the full matrix, whose
+// accepted update inserts or removes one row and column in block order.
+
+// get_HybrF_full(tau; f1, f2)
+__device__ __forceinline__ double hybrf_full(const Ctx& c, double tau, int f1, int f2) {
+  const DGroup& g = *c.g;
+  const long long neg = __double_as_longlong(tau) & (long long)0x8000000000000000ll;
+  if (neg) tau = tau + g.beta;
+  const double n = tau * g.hscale;
+  const int in = (int)n;
+  const double fr = n - (double)in;
+  const int i = min(max(in, 0), g.nftau - 2);
+  const double* F = g.hybr_full + ((size_t)f1 * c.m->nf + f2) * g.nftau;
+  const double f0 = __ldg(F + i), f1v = __ldg(F + i + 1);
+  const double v = fma(fr, f1v - f0, f0);
+  return __longlong_as_double(__double_as_longlong(v) ^ neg);
+}
+
+__device__ __forceinline__ int conn_code(const DModel& m, int s, int code) {
+  return s < 0 ? -1 : m.connect[((size_t)s * m.nf + (code >> 1)) * 2 + (code & 1)];
+}
+
+// 1-based block position a new operator (code 2f + ca, time t) would take
+// among the present operators of its kind (creators ca 0, annihilators 1).
+__device__ NOINL int od_pos_new(Ctx& c, int code, double t) {
+  const int K = c.h->K, ca = code & 1, f = code >> 1;
+  int n = 0;
+  for (int j = c.lane; j < K; j += 32) {
+    const int cd = c.opcode[j];
+    if ((cd & 1) != ca) continue;
+    const int fj = cd >> 1;
+    n += fj < f || (fj == f && c.optau[j] < t);
+  }
+  return wsumi(n) + 1;
+}
+
+// Block position (0-based) of every present operator into pos[0..K).
+__device__ NOINL void od_positions(Ctx& c, int* pos) {
+  const int K = c.h->K, ncode = 2 * c.m->nf;
+  const unsigned lt = (1u << c.lane) - 1u;
+  int cnt[2 * NFMAX];
+  for (int q = 0; q < ncode; ++q) cnt[q] = 0;
+  for (int base = 0; base < K; base += 32) {  // operators of each code
+    const int i = base + c.lane;
+    const int mc = i < K ? c.opcode[i] : -1;
+    for (int q = 0; q < ncode; ++q) cnt[q] += __popc(__ballot_sync(FULL, mc == q));
+  }
+  int off[2 * NFMAX];  // block offset of each code: earlier flavours of the same kind
+  for (int q = 0; q < ncode; ++q) {
+    off[q] = 0;
+    for (int r = q & 1; r < q; r += 2) off[q] += cnt[r];
+  }
+  int run[2 * NFMAX];
+  for (int q = 0; q < ncode; ++q) run[q] = 0;
+  for (int base = 0; base < K; base += 32) {
+    const int i = base + c.lane;
+    const int mc = i < K ? c.opcode[i] : -1;
+    for (int q = 0; q < ncode; ++q) {
+      const unsigned bal = __ballot_sync(FULL, mc == q);
+      if (mc == q) pos[i] = off[q] + run[q] + __popc(bal & lt);
+      run[q] += __popc(bal);
+    }
+  }
+  __syncwarp();
+}
+
+// Removable pairs of any flavours in the present arrays
+// (ensure_valid_NPairs_offdiag, Trace.F90:1818-1856).
+__device__ NOINL int count_pairs_od(Ctx& c) {
+  const Hdr& h = *c.h;
+  const int K = h.K;
+  int tot = 0;
+  for (int i = c.lane; i < K; i += 32) {
+    const double x = c.optau[i];
+    if (x < h.tauwin_min || x > h.tauwin_max) continue;
+    const int cx = c.opcode[i] & 1;
+    const double hi = fmin(h.tauwin_max, __dadd_rn(x, h.taudiff_max));
+    for (int j = i + 1; j < K; ++j) {
+      if (c.optau[j] > hi) break;
+      tot += (c.opcode[j] & 1) != cx;
+    }
+  }
+  return wsumi(tot);
+}
+
+// The target-th removable pair (1-based) in the scan order of gen_OperRemove
+// with off-diagonal hybridisation (Trace.F90:4880-4910): ix < iy.
+__device__ NOINL bool select_pair_od(Ctx& c, int target, int& ix, int& iy) {
+  const Hdr& h = *c.h;
+  const int K = h.K;
+  const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  const int start = wlb(c.optau, K, wmin, c.lane);
+  for (int base = start; base < K; base += 32) {
+    const int i = base + c.lane;
+    int cnt = 0;
+    if (i < K) {
+      const int cx = c.opcode[i] & 1;
+      const double hi = fmin(wmax, __dadd_rn(c.optau[i], tdm));
+      for (int j = i + 1; j < K; ++j) {
+        if (c.optau[j] > hi) break;
+        cnt += (c.opcode[j] & 1) != cx;
+      }
+    }
+    int cum = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(FULL, cum, o);
+      if (c.lane >= o) cum += y;
+    }
+    const int total = __shfl_sync(FULL, cum, 31);
+    if (target <= total) {
+      const unsigned bal = __ballot_sync(FULL, cum >= target);
+      const int L0 = __ffs(bal) - 1;
+      const int before = __shfl_sync(FULL, cum - cnt, L0);
+      int jy = -1;
+      if (c.lane == L0) {
+        int want = target - before;
+        const int cx = c.opcode[i] & 1;
+        const double hi = fmin(wmax, __dadd_rn(c.optau[i], tdm));
+        for (int j = i + 1; j < K; ++j) {
+          if (c.optau[j] > hi) break;
+          if ((c.opcode[j] & 1) != cx && --want <= 0) {
+            jy = j;
+            break;
+          }
+        }
+      }
+      ix = base + L0;
+      iy = __shfl_sync(FULL, jy, L0);
+      return iy > ix;
+    }
+    target -= total;
+  }
+  return false;
+}
+
+// Configuration sign with off-diagonal hybridisation: -(trace sign x
+// determinant sign x recalc_sign).  recalc_sign's double loop sorts the keys
+// (3 - CA) * 100000 + Orbital * 10000 + Spin * 1000 + tau descending, so its
+// exchange count has the parity of the number of ascending key pairs; to it
+// the loop adds sum_{i < n/2} i.
+__device__ __forceinline__ double od_key(const Ctx& c, int j) {
+  const int cd = c.opcode[j], f = cd >> 1;
+  const double a = (double)(2 - (cd & 1)) * 100000.0 + (double)((f >> 1) + 1) * 10000.0 + (double)((f & 1) + 1) * 1000.0;
+  return __dadd_rn(a, c.optau[j]);
+}
+__device__ NOINL double od_cfgsign(Ctx& c) {
+  const Hdr& h = *c.h;
+  const int K = h.K;
+  int asc = 0;
+  for (int i = c.lane; i < K; i += 32) {
+    const double ki = od_key(c, i);
+    for (int j = i + 1; j < K; ++j) asc += ki < od_key(c, j);
+  }
+  asc = wsumi(asc);
+  const long long half = K / 2;
+  const long long perm = (long long)asc + (half >= 2 ? (half - 1) * half / 2 : 0);
+  const double rs = (perm & 1) ? -1.0 : 1.0;
+  return -(h.trace_sign * h.det_sign * rs);
+}
+
+// Copy of the present operator arrays into the o_glob space (K entries).
+__device__ __forceinline__ void od_save(Ctx& c, int K) {
+  double* t = glob_optau(c);
+  int* o = glob_opcode(c);
+  for (int i = c.lane; i < K; i += 32) {
+    t[i] = c.optau[i];
+    o[i] = c.opcode[i];
+  }
+  __syncwarp();
+}
+__device__ __forceinline__ void od_restore(Ctx& c, int K) {
+  const double* t = glob_optau(c);
+  const int* o = glob_opcode(c);
+  for (int i = c.lane; i < K; i += 32) {
+    c.optau[i] = t[i];
+    c.opcode[i] = o[i];
+  }
+  if (c.lane == 0) c.h->K = K;
+  __syncwarp();
+  bstart_build(c);
+}
+
+// Trace of the proposed arrays with outer superstate s0 from a full rebuild
+// of the tree into the inactive slots.
+__device__ __forceinline__ void od_trace(Ctx& c, int s0, double& lg, double& sg) {
+  bstart_build(c);
+  tree_build_inactive(c, true, false);
+  rebuilt_trace(c, s0, lg, sg);
+}
+
+// Installation of an accepted off-diagonal move: tree, weights, sign.
+__device__ NOINL void od_accept(Ctx& c, double det_lg, double det_sg, double tr_lg, double tr_sg, int new_outer,
+                                int np_new) {
+  Hdr& h = *c.h;
+  tree_flip_all(c);
+  if (c.g->o_chk) chk_invalidate(c);
+  if (c.lane == 0) {
+    h.det_log = h.det_log + det_lg;
+    h.det_sign = h.det_sign * det_sg;
+    h.trace_log = tr_lg;
+    h.trace_sign = tr_sg;
+    h.outer_sst = new_outer;
+    h.npairs = np_new;
+  }
+  __syncwarp();
+  const double cs = od_cfgsign(c);
+  if (c.lane == 0) h.cfgsign = cs;
+  __syncwarp();
+}
+
+// StepAdd, CTQMC.F90:3353-3613, off-diagonal branch.
+__device__ NOINL void ph_add_od(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  cthyb_record& r = *c.rec;
+  const int K = h.K;
+  const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  // pair_OperAdd(force_diagonal = .false.): the annihilator at tau_ref with
+  // its own orbital and spin, then the creator within TaudiffMax with its own
+  const double w = __dsub_rn(wmax, wmin);
+  const double tau_a = __dadd_rn(wmin, __dmul_rn(w, grnd(c)));
+  double tdf = __dmul_rn(1.0, w);
+  const int orb_a = randint(c, 1, m.nd);
+  const int spin_a = randint(c, 1, 2);
+  const double tmin = fmax(__dsub_rn(tau_a, tdm), wmin);
+  const double w2 = __dsub_rn(fmin(__dadd_rn(tau_a, tdm), wmax), tmin);
+  const double tau_c = __dadd_rn(tmin, __dmul_rn(w2, grnd(c)));
+  tdf = __dmul_rn(tdf, w2);
+  const int orb_c = randint(c, 1, m.nd);
+  const int spin_c = randint(c, 1, 2);
+  const int fa = 2 * (orb_a - 1) + (spin_a - 1), fc = 2 * (orb_c - 1) + (spin_c - 1);
+  const int code_a = 2 * fa + 1, code_c = 2 * fc;
+  r.orb = fc + 1;
+  r.spin = fa + 1;
+  r.tau_c = tau_c;
+  r.tau_a = tau_a;
+  const int k = K / 2;
+  if (K + 2 > c.g->opcap || k + 1 > c.kcap) {
+    set_status(c, ST_CAPACITY);
+    return;
+  }
+  bool equal = tau_a == tau_c;
+  for (int i = c.lane; i < K; i += 32) {
+    const double t = c.optau[i];
+    equal = equal || t == tau_a || t == tau_c;
+  }
+  if (__any_sync(FULL, equal)) {
+    if (c.lane == 0) h.qn_add++;
+    r.outcome = 0;
+    __syncwarp();
+    return;
+  }
+  const int pos_c = od_pos_new(c, code_c, tau_c), pos_a = od_pos_new(c, code_a, tau_a);
+  r.fpos_c = pos_c;
+  r.fpos_a = pos_a;
+  // quantum numbers on the present arrays (check_sst_sequence)
+  const bool afirst = tau_a < tau_c;
+  const double t1 = afirst ? tau_a : tau_c, t2 = afirst ? tau_c : tau_a;
+  const int c1 = afirst ? code_a : code_c, c2 = afirst ? code_c : code_a;
+  const int p1 = wlb(c.optau, K, t1, c.lane), p2 = wlb(c.optau, K, t2, c.lane);
+  const int none[4] = {-1, -1, -1, -1};
+  const int bs = old_prefix(c, h.outer_sst, t1);
+  int new_outer = h.outer_sst;
+  bool qn_ok;
+  if (!p.co) {
+    const int es = old_prefix(c, h.outer_sst, t2);
+    int wk = conn_code(m, bs, c1);
+    wk = wk < 0 ? -1 : walk_ops(c, wk, p1, p2, none);
+    wk = conn_code(m, wk, c2);
+    qn_ok = bs >= 0 && wk >= 0 && wk == es;
+  } else {
+    int s2 = conn_code(m, old_prefix(c, h.outer_sst, t2), c2);
+    s2 = s2 < 0 ? -1 : walk_ops(c, s2, p2, K, none);
+    new_outer = s2;
+    qn_ok = false;
+    if (s2 >= 0) {
+      int back = walk_ops(c, s2, 0, p1, none);
+      back = conn_code(m, back, c1);
+      qn_ok = back >= 0 && back == bs;
+    }
+  }
+  if (!qn_ok) {
+    if (c.lane == 0) h.qn_add++;
+    r.outcome = 1;
+    __syncwarp();
+    return;
+  }
+  // determinant ratio S - R.M.Q over the full matrix; Q over the present
+  // annihilators with the flavour pair (creator, annihilator) as the
+  // reference passes it (Trace.F90:2892), R over the present creators
+  double* Q = c.scr;
+  double* R = c.scr + c.kcap;
+  double* v = c.scr + 2 * c.kcap;
+  double* wv = c.scr + 3 * c.kcap;
+  int* pos = c.bcode[1];
+  od_positions(c, pos);
+  for (int i = c.lane; i < K; i += 32) {
+    const int cd = c.opcode[i], fi = cd >> 1;
+    const double t = c.optau[i];
+    if (cd & 1) Q[pos[i]] = hybrf_full(c, __dsub_rn(t, tau_c), fc, fi);
+    else R[pos[i]] = hybrf_full(c, __dsub_rn(tau_a, t), fa, fi);
+  }
+  const double S = hybrf_full(c, __dsub_rn(tau_a, tau_c), fa, fc);
+  __syncwarp();
+  const double* Mf = M_ptr(c, 0);
+  const int ld = c.kcap;
+  double part = 0.0;
+  for (int i = c.lane; i < k; i += 32) {
+    double acc = 0.0;
+    for (int j = 0; j < k; ++j) acc = fma(Mf[(size_t)j * ld + i], Q[j], acc);
+    v[i] = acc;
+    part = fma(R[i], acc, part);
+  }
+  const double ratio = S - wsum(part);
+  const double sig = ((pos_c - pos_a) & 1) ? -1.0 : 1.0;
+  const double det_lg = log(fabs(ratio)), det_sg = (ratio >= 0.0 ? 1.0 : -1.0) * sig;
+  // proposed arrays: the pair merged in
+  od_save(c, K);
+  {
+    const double* tau_old = glob_optau(c);
+    const int* opc_old = glob_opcode(c);
+    for (int i = c.lane; i < K; i += 32) {
+      const double t = tau_old[i];
+      const int d = (t1 < t) + (t2 < t);
+      c.optau[i + d] = t;
+      c.opcode[i + d] = opc_old[i];
+    }
+    if (c.lane == 0) {
+      c.optau[p1] = t1;
+      c.opcode[p1] = c1;
+      c.optau[p2 + 1] = t2;
+      c.opcode[p2 + 1] = c2;
+      h.K = K + 2;
+    }
+    __syncwarp();
+  }
+  double tr_lg, tr_sg;
+  od_trace(c, new_outer, tr_lg, tr_sg);
+  const double rnd = grnd(c);
+  const int np_new = count_pairs_od(c);
+  const double n2 = 2.0 * m.nd;
+  const double wr = exp(__dsub_rn(tr_lg, h.trace_log) + det_lg);
+  const double prob = fabs(__dmul_rn(__ddiv_rn(__dmul_rn(tdf, __dmul_rn(n2, n2)), (double)np_new), wr));
+  r.det_log = det_lg;
+  r.det_sign = det_sg;
+  r.tr_log = tr_lg;
+  r.tr_sign = tr_sg;
+  r.prob = prob;
+  r.rand = rnd;
+  r.npairs = np_new;
+  if (rnd < prob) {
+    // get_MatAdd in block order: new row pos_c, new column pos_a
+    for (int j = c.lane; j < k; j += 32) {
+      double acc = 0.0;
+      const double* col = Mf + (size_t)j * ld;
+      for (int i = 0; i < k; ++i) acc = fma(R[i], col[i], acc);
+      wv[j] = acc;
+    }
+    __syncwarp();
+    double* T = glob_minv(c);
+    const int pc = pos_c - 1, pa = pos_a - 1, kn = k + 1;
+    const double inv = 1.0 / ratio;
+    for (int e = c.lane; e < kn * kn; e += 32) {
+      const int in = e % kn, jn = e / kn;
+      double val;
+      if (in == pc && jn == pa) {
+        val = inv;
+      } else if (jn == pa) {
+        val = -v[in < pc ? in : in - 1] * inv;
+      } else if (in == pc) {
+        val = -wv[jn < pa ? jn : jn - 1] * inv;
+      } else {
+        const int io = in < pc ? in : in - 1, jo = jn < pa ? jn : jn - 1;
+        val = Mf[(size_t)jo * ld + io] + v[io] * wv[jo] * inv;
+      }
+      T[(size_t)jn * ld + in] = val;
+    }
+    __syncwarp();
+    double* Mw = M_ptr(c, 0);
+    for (int e = c.lane; e < kn * kn; e += 32) {
+      const size_t idx = (size_t)(e / kn) * ld + (e % kn);
+      Mw[idx] = T[idx];
+    }
+    __syncwarp();
+    od_accept(c, det_lg, det_sg, tr_lg, tr_sg, new_outer, np_new);
+    if (c.lane == 0) h.acc_add++;
+    r.outcome = 4;
+  } else {
+    od_restore(c, K);
+    r.outcome = 3;
+  }
+  r.outer_sst = h.outer_sst;
+  r.k_total = h.K;
+  __syncwarp();
+}
+
+// StepRem, CTQMC.F90:3892-4151, off-diagonal branch.
+__device__ NOINL void ph_rem_od(Ctx& c, Prop& p) {
+  Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  cthyb_record& r = *c.rec;
+  const int K = h.K;
+  if (h.npairs == -1) {
+    const int np = count_pairs_od(c);
+    if (c.lane == 0) h.npairs = np;
+    __syncwarp();
+  }
+  const int np = h.npairs;
+  if (np <= 0) {
+    if (c.lane == 0) h.qn_rem++;
+    r.outcome = 2;
+    __syncwarp();
+    return;
+  }
+  int ix, iy;
+  if (!select_pair_od(c, randint(c, 1, np), ix, iy)) {
+    set_status(c, ST_INTERNAL);
+    return;
+  }
+  const double tx = c.optau[ix], ty = c.optau[iy];
+  const int cx = c.opcode[ix], cy = c.opcode[iy];
+  const bool xc = (cx & 1) == 0;  // x is the creator
+  const double tau_c = xc ? tx : ty, tau_a = xc ? ty : tx;
+  const int code_c = xc ? cx : cy, code_a = xc ? cy : cx;
+  const int fc = code_c >> 1, fa = code_a >> 1;
+  int* pos = c.bcode[1];
+  od_positions(c, pos);
+  const int pos_c = pos[xc ? ix : iy] + 1, pos_a = pos[xc ? iy : ix] + 1;
+  const double hprf = __ddiv_rn((double)np, __dmul_rn(__dsub_rn(h.tauwin_max, h.tauwin_min),
+                                                      __dsub_rn(fmin(__dadd_rn(tau_a, h.taudiff_max), h.tauwin_max),
+                                                                fmax(__dsub_rn(tau_a, h.taudiff_max), h.tauwin_min))));
+  r.orb = fc + 1;
+  r.spin = fa + 1;
+  r.tau_c = tau_c;
+  r.tau_a = tau_a;
+  r.fpos_c = pos_c;
+  r.fpos_a = pos_a;
+  r.npairs = np;
+  // quantum numbers on the present arrays
+  const int none[4] = {-1, -1, -1, -1};
+  int new_outer = h.outer_sst;
+  bool qn_ok;
+  if (!p.co) {
+    const int bs = old_prefix(c, h.outer_sst, tx);
+    const int es = conn_code(m, old_prefix(c, h.outer_sst, ty), cy);
+    const int wk = bs < 0 ? -1 : walk_ops(c, bs, ix + 1, iy, none);
+    qn_ok = bs >= 0 && wk >= 0 && wk == es;
+  } else {
+    const int inside = old_prefix(c, h.outer_sst, ty);
+    const int s2 = inside < 0 ? -1 : walk_ops(c, inside, iy + 1, K, none);
+    new_outer = s2;
+    qn_ok = false;
+    if (s2 >= 0) {
+      const int back = walk_ops(c, s2, 0, ix, none);
+      const int target = conn_code(m, old_prefix(c, h.outer_sst, tx), cx);
+      qn_ok = back >= 0 && back == target;
+    }
+  }
+  if (!qn_ok) {
+    if (c.lane == 0) h.qn_rem++;
+    r.outcome = 1;
+    __syncwarp();
+    return;
+  }
+  const int k = K / 2, ld = c.kcap, pc = pos_c - 1, pa = pos_a - 1;
+  const double* Mf = M_ptr(c, 0);
+  const double dr = Mf[(size_t)pa * ld + pc];
+  const double sig = ((pos_c - pos_a) & 1) ? -1.0 : 1.0;
+  const double det_lg = log(fabs(dr)), det_sg = (dr >= 0.0 ? 1.0 : -1.0) * sig;
+  // proposed arrays without the pair
+  od_save(c, K);
+  {
+    const double* tau_old = glob_optau(c);
+    const int* opc_old = glob_opcode(c);
+    for (int i = c.lane; i < K; i += 32) {
+      if (i == ix || i == iy) continue;
+      const int d = (ix < i) + (iy < i);
+      c.optau[i - d] = tau_old[i];
+      c.opcode[i - d] = opc_old[i];
+    }
+    if (c.lane == 0) h.K = K - 2;
+    __syncwarp();
+  }
+  double tr_lg, tr_sg;
+  od_trace(c, new_outer, tr_lg, tr_sg);
+  const double n2 = 2.0 * m.nd;
+  const double wr = exp(__dsub_rn(tr_lg, h.trace_log) + det_lg);
+  const double prob = fabs(__dmul_rn(__ddiv_rn(hprf, __dmul_rn(n2, n2)), wr));
+  const double rnd = grnd(c);
+  r.det_log = det_lg;
+  r.det_sign = det_sg;
+  r.tr_log = tr_lg;
+  r.tr_sign = tr_sg;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    if (fabs(dr) < 1e-12) {  // CTQMC.F90:4062
+      od_restore(c, K);
+      set_status(c, ST_NUMERIC);
+      return;
+    }
+    // get_MatRem in block order: row pos_c and column pos_a leave
+    double* T = glob_minv(c);
+    const int kn = k - 1;
+    const double inv = 1.0 / dr;
+    for (int e = c.lane; e < kn * kn; e += 32) {
+      const int in = e % kn, jn = e / kn;
+      const int io = in < pc ? in : in + 1, jo = jn < pa ? jn : jn + 1;
+      T[(size_t)jn * ld + in] = Mf[(size_t)jo * ld + io] - Mf[(size_t)pa * ld + io] * Mf[(size_t)jo * ld + pc] * inv;
+    }
+    __syncwarp();
+    double* Mw = M_ptr(c, 0);
+    for (int e = c.lane; e < kn * kn; e += 32) {
+      const size_t idx = (size_t)(e / kn) * ld + (e % kn);
+      Mw[idx] = T[idx];
+    }
+    __syncwarp();
+    const int np_new = count_pairs_od(c);
+    od_accept(c, det_lg, det_sg, tr_lg, tr_sg, new_outer, np_new);
+    if (c.lane == 0) h.acc_rem++;
+    r.outcome = 4;
+  } else {
+    od_restore(c, K);
+    r.outcome = 3;
+  }
+  r.outer_sst = h.outer_sst;
+  r.k_total = h.K;
+  __syncwarp();
+}
+
+// MeasGtauRem_full (CTQMC.F90:2475-2584) and MeasExpOrder with
+// NOSOper(b,s)/2 = (creators + annihilators of the flavour) / 2.
+__device__ NOINL void measure_od(Ctx& c) {
+  const Hdr& h = *c.h;
+  const DModel& m = *c.m;
+  const DGroup& g = *c.g;
+  const int K = h.K, nf = m.nf, nt = g.ntau, k = K / 2, ld = c.kcap;
+  for (int f = 0; f < nf; ++f) {
+    int n = 0;
+    for (int i = c.lane; i < K; i += 32) n += (c.opcode[i] >> 1) == f;
+    n = wsumi(n) / 2;
+    if (c.lane == 0) c.histo[(size_t)f * g.maxhisto + (n < g.maxhisto - 1 ? n : g.maxhisto - 1)] += 1.0;
+  }
+  __syncwarp();
+  if (k == 0) return;
+  // times and flavours by block position
+  int* pos = c.bcode[1];
+  od_positions(c, pos);
+  double* ct = c.scr;
+  double* at = c.scr + c.kcap;
+  int* cf = (int*)(c.scr + 2 * c.kcap);
+  int* af = (int*)(c.scr + 3 * c.kcap);
+  for (int i = c.lane; i < K; i += 32) {
+    const int cd = c.opcode[i];
+    if (cd & 1) {
+      at[pos[i]] = c.optau[i];
+      af[pos[i]] = cd >> 1;
+    } else {
+      ct[pos[i]] = c.optau[i];
+      cf[pos[i]] = cd >> 1;
+    }
+  }
+  __syncwarp();
+  double* G = (double*)((char*)c.gtau - g.o_gtau + g.o_gfull);
+  const double* Mf = M_ptr(c, 0);
+  for (int e = c.lane; e < k * k; e += 32) {
+    const int i = e % k, j = e / k;  // creator row i, annihilator column j
+    double Mv = Mf[(size_t)j * ld + i];
+    const double ta = at[j], tc = ct[i];
+    double dt;
+    if (ta - tc > 0.0) {
+      dt = ta - tc;
+    } else {
+      dt = g.beta + ta - tc;
+      Mv = -Mv;
+    }
+    const double q = dt * g.gscale;
+    int idt = (int)q;
+    const double fr = q - (double)idt;
+    if (fr < 1e-9 || fr > 1.0 - 1e-9) idt = (int)__dmul_rn(__ddiv_rn(dt, g.beta), (double)nt);
+    idt += 1;
+    if (idt > nt) idt = nt;
+    Mv = Mv * h.cfgsign;
+    atomicAdd(&G[((size_t)af[j] * nf + cf[i]) * nt + idt - 1], Mv);
+  }
+  __syncwarp();
+}
+
 // One proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250) with
 // the phases back to back.
 __device__ void one_step(Ctx& c, Prop& p) {
@@ -3034,7 +3642,9 @@ __device__ void one_step(Ctx& c, Prop& p) {
     if (p.move == 2) ph_global(c, p);
     else if (p.move == 3) ph_shift(c, p);
     else if (p.move == 5) ph_add4(c, p);
-    else ph_rem4(c, p);
+    else if (p.move == 6) ph_rem4(c, p);
+    else if (p.move == 7) ph_add_od(c, p);
+    else ph_rem_od(c, p);
     if (c.h->status == ST_OK) ph_finish(c, p);
     return;
   }
@@ -3121,13 +3731,17 @@ __device__ NOINL void measure(Ctx& c) {
     h.cnt_meas++;
     h.meas_sign += h.cfgsign;  // MeasSign
   }
-  // MeasExpOrder
-  for (int f = c.lane; f < m.nf; f += 32) {
-    int k = h.k[f];
-    int hm = g.maxhisto;
-    c.histo[(size_t)f * hm + (k < hm - 1 ? k : hm - 1)] += 1.0;
+  // MeasExpOrder (off-diagonal groups: in measure_od with G)
+  if (g.offdiag) {
+    measure_od(c);
+  } else {
+    for (int f = c.lane; f < m.nf; f += 32) {
+      int k = h.k[f];
+      int hm = g.maxhisto;
+      c.histo[(size_t)f * hm + (k < hm - 1 ? k : hm - 1)] += 1.0;
+    }
+    __syncwarp();
   }
-  __syncwarp();
   // MeasDensityMatrix_beta_half from the two children of the root
   if (g.meas_dm && c.mono) {
     int s0 = h.outer_sst;
@@ -3565,7 +4179,9 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
         if (p.move == 2) ph_global(c, p);
         else if (p.move == 3) ph_shift(c, p);
         else if (p.move == 5) ph_add4(c, p);
-        else ph_rem4(c, p);
+        else if (p.move == 6) ph_rem4(c, p);
+        else if (p.move == 7) ph_add_od(c, p);
+        else ph_rem_od(c, p);
       }
       __syncthreads();
     }
@@ -3896,6 +4512,7 @@ struct GroupHost {
   DGroup g;
   std::vector<double> hybr;
   double* d_hybr = nullptr;
+  double* d_hybr_full = nullptr;
   double* d_empty = nullptr;
   double* d_score = nullptr;
   double* d_edges = nullptr;
@@ -4149,6 +4766,12 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   off = align_up(off + (size_t)(4 * kcap + 2 * (opcap + 2) + 2 * (opcap + 3)) * 8 + (size_t)2 * (opcap + 2) * 4, 256);
   g.o_gtau = off;
   off = align_up(off + (size_t)nf * d.ntau * 8, 256);
+  g.offdiag = d.ftau_full ? 1 : 0;
+  g.o_gfull = 0;
+  if (g.offdiag) {
+    g.o_gfull = off;
+    off = align_up(off + (size_t)nf * nf * d.ntau * 8, 256);
+  }
   g.o_histo = off;
   off = align_up(off + (size_t)nf * g.maxhisto * 8, 256);
   g.o_dm = off;  // diagonal (monomial models) or the superstate blocks of rho
@@ -4182,7 +4805,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   // work space of global, tau-shift and 4-operator moves: new inverse
   // matrices, new sorted lists, copy of the operator arrays
   g.o_glob = 0;
-  if (d.p_global > 0.0 || d.p_shift > 0.0 || d.p_4op > 0.0) {
+  if (d.p_global > 0.0 || d.p_shift > 0.0 || d.p_4op > 0.0 || d.ftau_full) {
     g.o_glob = off;
     off = align_up(off + ((size_t)nf * kcap * kcap + (size_t)nf * 2 * kcap + (opcap + 2)) * 8 +
                              (size_t)(opcap + 2) * 4,
@@ -4209,6 +4832,13 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
     if (G.desc.nchains < 1 || G.desc.nftau < 2 || G.desc.ntau < 1 || !(G.desc.beta > 0) || !G.desc.ftau) {
       delete B;
       return fail(CTHYB_ERR_ARG, "bad group description");
+    }
+    if (G.desc.ftau_full && (G.desc.p_global > 0.0 || G.desc.p_shift > 0.0 || G.desc.p_4op > 0.0 ||
+                             G.desc.nleg > 0 || (G.desc.nscore > 0 && G.desc.score_dE))) {
+      delete B;
+      return fail(CTHYB_ERR_UNSUPPORTED,
+                  "off-diagonal hybridisation: pair and outer-superstate moves only (no global, tau-shift "
+                  "or 4-operator moves, Legendre or score measurements)");
     }
     layout_group(B, G, 0);
     G.chain0 = B->nchains;
@@ -4248,6 +4878,19 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
           G.hybr[(size_t)(2 * b + s) * d.nftau + t] = d.ftau[b + hm.nd * (s + 2 * (size_t)t)];
     G.d_hybr = dev_upload(G.hybr, e);
     G.g.hybr = G.d_hybr;
+    G.g.hybr_full = nullptr;
+    if (d.ftau_full) {  // [f1][f2][t] with f = 2b + s
+      std::vector<double> hf((size_t)hm.nf * hm.nf * d.nftau);
+      for (int b1 = 0; b1 < hm.nd; ++b1)
+        for (int s1 = 0; s1 < 2; ++s1)
+          for (int b2 = 0; b2 < hm.nd; ++b2)
+            for (int s2 = 0; s2 < 2; ++s2)
+              for (int t = 0; t < d.nftau; ++t)
+                hf[((size_t)(2 * b1 + s1) * hm.nf + (2 * b2 + s2)) * d.nftau + t] =
+                    d.ftau_full[b1 + hm.nd * (s1 + 2 * (b2 + hm.nd * (s2 + 2 * (size_t)t)))];
+      G.d_hybr_full = dev_upload(hf, e);
+      G.g.hybr_full = G.d_hybr_full;
+    }
     std::vector<double> w;
     empty_trace_weights(hm, d.beta, w);
     G.d_empty = dev_upload(w, e);
@@ -4322,6 +4965,7 @@ int cthyb_batch_destroy(cthyb_batch_t B) {
   if (B->stream) cudaStreamSynchronize(B->stream);
   for (GroupHost& G : B->groups) {
     cudaFree(G.d_hybr);
+    cudaFree(G.d_hybr_full);
     cudaFree(G.d_empty);
     cudaFree(G.d_score);
     cudaFree(G.d_edges);
@@ -4936,10 +5580,20 @@ int cthyb_batch_set_config(cthyb_batch_t B, int chain, int n, const double* taus
   return cthyb_batch_set_configs(B, chain, 1, offs, taus, orbs, spins, cas, &outer_sst);
 }
 
+// Whether any group of the batch has off-diagonal hybridisation (the
+// per-flavour paths below -- set_mc_config, the LU refresh, gradients --
+// do not apply to it).
+static bool any_offdiag(cthyb_batch_t B) {
+  for (const GroupHost& G : B->groups)
+    if (G.g.offdiag) return true;
+  return false;
+}
+
 int cthyb_batch_set_configs(cthyb_batch_t B, int chain0, int nset, const int* offsets, const double* taus,
                             const int* orbs, const int* spins, const int* cas, const int* outer_sst) {
   if (!B || nset < 0 || chain0 < 0 || chain0 + nset > B->nchains || !offsets || !outer_sst || offsets[0] != 0)
     return fail(CTHYB_ERR_ARG, "bad chain range or offsets");
+  if (any_offdiag(B)) return fail(CTHYB_ERR_UNSUPPORTED, "set_mc_config with off-diagonal hybridisation");
   for (int i = 0; i < nset; ++i)
     if (offsets[i + 1] < offsets[i]) return fail(CTHYB_ERR_ARG, "offsets must not decrease");
   if (offsets[nset] > 0 && (!taus || !orbs || !spins || !cas)) return fail(CTHYB_ERR_ARG, "null operator arrays");
@@ -4994,6 +5648,7 @@ int cthyb_batch_gradients(cthyb_batch_t B, int nparams, const double* dE, double
                           double* log_weights) {
   if (!B || nparams < 0 || nparams > NPARMAX || (nparams > 0 && (!dE || !grad_params)))
     return fail(CTHYB_ERR_ARG, "bad arguments (nparams must be 0..32)");
+  if (any_offdiag(B)) return fail(CTHYB_ERR_UNSUPPORTED, "gradients with off-diagonal hybridisation");
   const HostModel& hm = B->model->hm;
   if (nparams > 0)
     for (GroupHost& G : B->groups)
@@ -5051,6 +5706,7 @@ int cthyb_batch_gradients_device(cthyb_batch_t B, int nparams, const double* dE_
   if (!B || nparams < 0 || nparams > NPARMAX || !grad_delta_dev || !log_weights_dev ||
       (nparams > 0 && (!dE_dev || !grad_params_dev)))
     return fail(CTHYB_ERR_ARG, "bad arguments (nparams must be 0..32)");
+  if (any_offdiag(B)) return fail(CTHYB_ERR_UNSUPPORTED, "gradients with off-diagonal hybridisation");
   if (nparams > 0)
     for (GroupHost& G : B->groups)
       if (G.g.o_chk) return fail(CTHYB_ERR_UNSUPPORTED, "trace gradients need a monomial (density-density) model");
@@ -5080,6 +5736,7 @@ int cthyb_batch_gradients_device(cthyb_batch_t B, int nparams, const double* dE_
 
 int cthyb_batch_refresh_minv(cthyb_batch_t B, int replace, double* maxdev) {
   if (!B) return fail(CTHYB_ERR_ARG, "null");
+  if (any_offdiag(B)) return fail(CTHYB_ERR_UNSUPPORTED, "LU refresh with off-diagonal hybridisation");
   CK(cudaMemsetAsync(B->d_dev, 0, sizeof(double), B->stream));
   for (GroupHost& G : B->groups) {
     if (2 * G.g.kcap * G.g.kcap > 2 * B->model->hm.nsmax * B->model->hm.nsmax &&
@@ -5109,6 +5766,7 @@ int cthyb_batch_set_log(cthyb_batch_t B, int64_t cap) {
     layout_group(B, G, cap);
     G.g.base = save.base;
     G.g.hybr = save.hybr;
+    G.g.hybr_full = save.hybr_full;
     G.g.empty_w = save.empty_w;
     G.g.err_flag = save.err_flag;
     G.g.edges = save.edges;
@@ -5174,6 +5832,45 @@ int cthyb_debug_phase_cycles(cthyb_batch_t B, int64_t* out10) {
       CK(cudaMemcpy(&h, G.g.base + (size_t)c * G.g.stride + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost));
       for (int i = 0; i < 10; ++i) out10[i] += h.prof[i];
     }
+  return CTHYB_OK;
+}
+
+int cthyb_batch_results_full(cthyb_batch_t B, int chain, double* gtau_full) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  if (!G->g.offdiag) return fail(CTHYB_ERR_ARG, "not an off-diagonal group");
+  if (!gtau_full) return fail(CTHYB_ERR_ARG, "null");
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  const int nf = B->model->hm.nf, nt = G->g.ntau;
+  std::vector<double> acc((size_t)nf * nf * nt);
+  CK(cudaMemcpy(acc.data(), G->g.base + (size_t)c * G->g.stride + G->g.o_gfull, acc.size() * 8,
+                cudaMemcpyDeviceToHost));
+  const double ms = h.cnt_meas ? h.meas_sign / (double)h.cnt_meas : 0.0;
+  const double scale = (h.cnt_meas && ms != 0.0) ? (double)nt / (G->g.beta * G->g.beta) / ((double)h.cnt_meas * ms) : 0.0;
+  for (size_t i = 0; i < acc.size(); ++i) gtau_full[i] = acc[i] * scale;  // -acc * zScaling * Ntau / beta^2
+  return CTHYB_OK;
+}
+
+int cthyb_batch_minv_full(cthyb_batch_t B, int chain, int* kout, double* out) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  if (!G->g.offdiag || !kout) return fail(CTHYB_ERR_ARG, "not an off-diagonal group");
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  const int k = h.K / 2, ld = G->g.kcap;
+  *kout = k;
+  if (!out || k == 0) return CTHYB_OK;
+  std::vector<double> M((size_t)ld * k);
+  CK(cudaMemcpy(M.data(), G->g.base + (size_t)c * G->g.stride + G->g.o_M, M.size() * 8, cudaMemcpyDeviceToHost));
+  for (int j = 0; j < k; ++j)
+    for (int i = 0; i < k; ++i) out[(size_t)j * k + i] = M[(size_t)j * ld + i];
   return CTHYB_OK;
 }
 

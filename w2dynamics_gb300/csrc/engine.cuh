@@ -68,6 +68,9 @@ struct DGroup {
   const double* score_dE;  // [nscore][ns]
   double p_outer, p_global, p_shift;  // PercentageOuterMove, PercentageGlobalMove, PercentageTauShiftMove
   double p_4op;                       // Percentage4OperatorMove
+  int offdiag;                        // off-diagonal hybridisation (offdiag = 1)
+  const double* hybr_full;            // offdiag: [f1][f2][nftau]
+  size_t o_gfull;                     // offdiag: G for every flavour pair [f_a][f_c][ntau]
   int kcap, opcap, L, dense, meas_dm;
   char* base;          // chain c at base + c*stride
   size_t stride;

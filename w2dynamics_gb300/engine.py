@@ -29,7 +29,7 @@ EXPORTS = (
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
     "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_autotune", "cthyb_batch_results",
-    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_move_counters4", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
+    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_move_counters4", "cthyb_batch_results_full", "cthyb_batch_minv_full", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_set_configs", "cthyb_batch_get_configs", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
     "cthyb_minv_rebuild_noalloc",
@@ -44,7 +44,8 @@ class GroupDesc(C.Structure):
                 ("opcap", C.c_int32), ("tree_levels", C.c_int32), ("maxhisto", C.c_int32),
                 ("flags", C.c_int32), ("p_global", C.c_double), ("p_shift", C.c_double),
                 ("nleg", C.c_int32), ("nscore", C.c_int32), ("score_dE", C.POINTER(C.c_double)),
-                ("nsym", C.c_int32), ("symmoves", C.POINTER(C.c_int32)), ("p_4op", C.c_double)]
+                ("nsym", C.c_int32), ("symmoves", C.POINTER(C.c_int32)), ("p_4op", C.c_double),
+                ("ftau_full", C.POINTER(C.c_double))]
 
 
 class EngineError(RuntimeError):
@@ -92,6 +93,8 @@ def load(build_if_missing=False):
     L.cthyb_batch_results.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_move_counters.argtypes = [vp, C.c_int, C.POINTER(i64)]
     L.cthyb_batch_move_counters4.argtypes = [vp, C.c_int, C.POINTER(i64)]
+    L.cthyb_batch_results_full.argtypes = [vp, C.c_int, dp]
+    L.cthyb_batch_minv_full.argtypes = [vp, C.c_int, ip, dp]
     L.cthyb_batch_results_extra.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp]
     L.cthyb_batch_gradients.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.cthyb_batch_results_score.argtypes = [vp, C.c_int, dp, dp]
@@ -179,7 +182,7 @@ class Group:
     def __init__(self, beta, ftau, ntau, nchains=1, seed0=0, seeds=None, taudiff_max=-1.0,
                  ncorr=100, p_outer=0.0, kcap=0, opcap=0, tree_levels=0, maxhisto=500,
                  dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0, score_dE=None,
-                 symmoves=None, p_4op=0.0):
+                 symmoves=None, p_4op=0.0, ftau_full=None):
         self.beta = float(beta)
         self.ftau = np.asfortranarray(np.asarray(ftau, np.float64))
         self.ntau = int(ntau)
@@ -191,6 +194,8 @@ class Group:
         self.p_outer = float(p_outer)
         self.p_global, self.p_shift = float(p_global), float(p_shift)
         self.p_4op = float(p_4op)
+        # off-diagonal hybridisation: F for every flavour pair (Nd,2,Nd,2,Nftau)
+        self.ftau_full = None if ftau_full is None else np.asfortranarray(np.asarray(ftau_full, np.float64))
         self.nleg = int(nleg)
         self.score_dE = None if score_dE is None else np.ascontiguousarray(score_dE, np.float64)
         # user symmetry moves: rows of 1-based target flavours in the reference's
@@ -218,6 +223,11 @@ class Group:
         d.flags = self.flags
         d.p_global, d.p_shift = self.p_global, self.p_shift
         d.p_4op = self.p_4op
+        if self.ftau_full is not None:
+            self._ffl = self.ftau_full.ravel(order="F")
+            d.ftau_full = _dp(self._ffl)
+        else:
+            d.ftau_full = None
         d.nleg = self.nleg
         d.nscore = 0 if self.score_dE is None else self.score_dE.shape[0]
         d.score_dE = _dp(self.score_dE) if self.score_dE is not None else None
@@ -423,6 +433,24 @@ class Batch:
         o, s, c = (np.ascontiguousarray(a, np.int32) for a in (orbs, spins, cas))
         _check(load().cthyb_batch_set_configs(self.h, chain0, len(outer), _ip(offs), _dp(t), _ip(o),
                                               _ip(s), _ip(c), _ip(outer)))
+
+    def results_full(self, chain):
+        """Off-diagonal groups: G for every flavour pair, (2Nd, 2Nd, Ntau)
+        indexed [f_annihilator, f_creator, bin] with f = 2b + s."""
+        g = self.groups[self._group_of[chain]]
+        nf = 2 * self.model.nd
+        out = np.zeros(nf * nf * g.ntau)
+        _check(load().cthyb_batch_results_full(self.h, chain, _dp(out)))
+        return out.reshape(nf, nf, g.ntau)
+
+    def minv_full(self, chain):
+        """Off-diagonal groups: the inverse matrix over all flavours in block
+        order (rows creators, columns annihilators)."""
+        k = C.c_int()
+        _check(load().cthyb_batch_minv_full(self.h, chain, C.byref(k), None))
+        out = np.zeros(max(k.value, 1) ** 2)
+        _check(load().cthyb_batch_minv_full(self.h, chain, C.byref(k), _dp(out)))
+        return out[:k.value ** 2].reshape((k.value, k.value), order="F")
 
     def minv(self, chain, f):
         k = C.c_int()

@@ -156,14 +156,17 @@ def _check_supported():
     bad = []
     if _real("PercentageWormInsert", 0.0) != 0.0:
         bad.append(f"PercentageWormInsert = {_real('PercentageWormInsert')}")
-    for key in ("segment", "offdiag", "statesampling", "Phonon", "Screening", "Uw",
-                "flavourchange_moves"):
+    for key in ("segment", "statesampling", "Phonon", "Screening", "Uw", "flavourchange_moves"):
         if _int(key, 0) != 0:
             bad.append(f"{key} = {_int(key)}")
     if _int("Eigenbasis", 1) == 0:
         bad.append("Eigenbasis = 0")
     if "All" in _str("QuantumNumbers", "").split():
         bad.append("QuantumNumbers = All")
+    if _int("offdiag", 0) != 0:  # off-diagonal F: pair and outer-superstate moves only
+        for key in ("PercentageGlobalMove", "PercentageTauShiftMove", "Percentage4OperatorMove"):
+            if _real(key, 0.0) != 0.0:
+                bad.append(f"{key} = {_real(key)} with offdiag = 1")
     if bad:
         raise NotImplementedError("outside the GPU pair-move engine: " + ", ".join(bad))
 
@@ -188,13 +191,16 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
     _nd, _beta = nd, _real("beta")
     _nchains = max(1, _int("GPUChains", 1))
     _model = E.Model(nd, um, mu, qns)
+    offdiag = _int("offdiag", 0) != 0
     group = E.Group(_beta, ftau, _int("Ntau"), nchains=_nchains, seed0=_seed,
                     taudiff_max=_real("TaudiffMax", -1.0), ncorr=_int("NCorr"),
                     p_outer=_real("PercentageOuterMove", 0.0), maxhisto=_int("MaxHisto", 500) + 1,
                     measure_dm=_int("MeasDensityMatrix", 1) != 0,
                     p_global=_real("PercentageGlobalMove", 0.0),
-                    p_shift=_real("PercentageTauShiftMove", 0.0), nleg=_int("NLegMax", 100),
-                    p_4op=_real("Percentage4OperatorMove", 0.0))
+                    p_shift=_real("PercentageTauShiftMove", 0.0),
+                    nleg=0 if offdiag else _int("NLegMax", 100),
+                    p_4op=_real("Percentage4OperatorMove", 0.0),
+                    ftau_full=ftau_full if offdiag else None)
     nsym = _int("NSymMove", 0)
     if nsym > 0:  # SymMove01 ... (Trace.F90:471-477)
         group.symmoves = np.array([[int(x) for x in _raw("SymMove%02d" % (i + 1)).split()]
@@ -269,9 +275,16 @@ def _collect():
     accglob = mcnt["acc_glob"] / mcnt["try_glob"] if mcnt["try_glob"] else float("nan")
     accshift = mcnt["acc_shift"] / mcnt["try_shift"] if mcnt["try_shift"] else float("nan")
     gtau_full = np.zeros((nd, 2, nd, 2, gtau.shape[-1]))
-    for b in range(nd):
-        for s in range(2):
-            gtau_full[b, s, b, s] = gtau[b, s]
+    if _batch.groups[0].ftau_full is not None:
+        # offdiag = 1: MeasGtauRem_full fills Gtau_full, Gtau stays zero
+        gf = sum(_batch.results_full(c) * s for c, s in zip(range(_nchains), signs)) / wsum
+        for fa in range(nf):
+            for fc in range(nf):
+                gtau_full[fa // 2, fa % 2, fc // 2, fc % 2] = gf[fa, fc]
+    else:
+        for b in range(nd):
+            for s in range(2):
+                gtau_full[b, s, b, s] = gtau[b, s]
     if _int("MeasDensityMatrix", 1) != 0:
         fk, evec = _model.basis()
         est = ES.from_density_matrix(nd, fk, evec, dm_eigen)
