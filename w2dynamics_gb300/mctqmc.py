@@ -37,8 +37,10 @@ solves (the batch form of the driver's mc_config_inout warm start and its
 CtHybConfig npz files, cthyb_solver.py:24-87, 316-345).
 
 Parameters selecting moves or modes outside the engine (worm and
-flavour-change moves, segment, off-diagonal hybridisation, state sampling,
-retarded interactions) raise NotImplementedError at init_solver.  The
+flavour-change moves, segment, state sampling, retarded interactions;
+global, tau-shift or 4-operator moves together with offdiag = 1) raise
+NotImplementedError at init_solver.  With offdiag = 1 the full Ftau_full is
+used and gtau_full holds G for every flavour pair (MeasGtauRem_full).  The
 trace-recomputation histograms lhisto/rhisto describe the reference's
 list-walking implementation and are returned as zeros; outer trace
 contributions are measured for density-density (monomial) models.  Each
