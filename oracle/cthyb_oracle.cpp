@@ -1306,6 +1306,11 @@ static void flavour_lists(const Chain& c, const std::vector<Op>& ops, std::vecto
   for (const Op& o : ops) (o.ca == 0 ? tc : ta)[c.fi(o.b, o.s)].push_back(o.tau);
 }
 
+// off-diagonal helpers (defined with the off-diagonal moves below)
+static std::vector<double> full_hybr_offdiag(const Chain& c);
+static int total_creators(const Chain& c);
+static double config_sign_offdiag(const Chain& c);
+
 // Number of superstates s with s -> s under the whole list, their list
 // (check_qn_all_ssts, Trace.F90:1399-1433; -1 for those that fail).
 static int fixed_ssts(const Chain& c, const std::vector<Op>& ops, std::vector<int>& ssts) {
@@ -1412,17 +1417,29 @@ static void step_glob(Chain& c) {
   flavour_lists(c, nops, tc, ta);
   c.tau_c = tc;
   c.tau_a = ta;
-  LogVal det_new = rebuild_minv(c);
-  std::vector<std::vector<double>> minv_new = c.minv;
-  LogVal det_minv_old{0.0, 1.0};
-  for (int f = 0; f < c.nf; ++f) {
-    int k = (int)tc_old[f].size();
-    if (k == 0) continue;
-    std::vector<double> A = minv_old[f];
+  LogVal det_new, detrat;
+  std::vector<std::vector<double>> minv_new;
+  std::vector<double> mfull_new;
+  if (c.offdiag) {
+    // get_FullHybr_offdiag + get_MatLogDetFull; DetRat = DetNew / Det
+    // (CTQMC.F90:4491-4494)
+    mfull_new = full_hybr_offdiag(c);
     bool sing;
-    det_minv_old = lmul(lu_logdet_inverse(A, k, sing), det_minv_old);
+    det_new = lu_logdet_inverse(mfull_new, total_creators(c), sing);
+    detrat = ldiv(det_new, c.det);
+  } else {
+    det_new = rebuild_minv(c);
+    minv_new = c.minv;
+    LogVal det_minv_old{0.0, 1.0};
+    for (int f = 0; f < c.nf; ++f) {
+      int k = (int)tc_old[f].size();
+      if (k == 0) continue;
+      std::vector<double> A = minv_old[f];
+      bool sing;
+      det_minv_old = lmul(lu_logdet_inverse(A, k, sing), det_minv_old);
+    }
+    detrat = lmul(det_new, det_minv_old);
   }
-  LogVal detrat = lmul(det_new, det_minv_old);
   // full trace of the new configuration
   std::vector<Op> ops_old = c.ops;
   int outer_old = c.outer_sst;
@@ -1443,8 +1460,13 @@ static void step_glob(Chain& c) {
     c.det = det_new;
     c.trace = trnew;
     c.parttrace = part;
-    c.minv = minv_new;
-    c.cfgsign = -config_sign(c);
+    if (c.offdiag) {
+      c.minv_full = mfull_new;
+      c.cfgsign = -config_sign_offdiag(c);
+    } else {
+      c.minv = minv_new;
+      c.cfgsign = -config_sign(c);
+    }
     c.acc_glob++;
     r.outcome = OUT_ACCEPT;
   } else {
@@ -1559,16 +1581,48 @@ static void step_shift(Chain& c) {
     c.trace = trnew;
     c.parttrace = part;
     double detrat = 1.0;
+    if (c.offdiag) {
+      // update_InvFullHybrShiftTau_offdiag (Trace.F90:2490-2600): per pair of
+      // (creator flavour, annihilator flavour) blocks the rows and columns
+      // rotate by the wrapped counts, an entry negated when exactly one of
+      // its row and column wrapped; sign (-1)^(size * wrapped) per block
+      const int k = total_creators(c);
+      std::vector<int> offc(c.nf + 1, 0), offa(c.nf + 1, 0);
+      for (int f = 0; f < c.nf; ++f) {
+        offc[f + 1] = offc[f] + (int)c.tau_c[f].size();
+        offa[f + 1] = offa[f] + (int)c.tau_a[f].size();
+      }
+      std::vector<double> N((size_t)k * k);
+      for (int fr = 0; fr < c.nf; ++fr) {
+        const int sr = offc[fr + 1] - offc[fr], wrr = wr_c[fr];
+        for (int fcl = 0; fcl < c.nf; ++fcl) {
+          const int sc = offa[fcl + 1] - offa[fcl], wcc = wr_a[fcl];
+          for (int j = 0; j < sc; ++j)
+            for (int i = 0; i < sr; ++i) {
+              const int oi = (i + wrr) % sr, oj = (j + wcc) % sc;
+              const bool ri = i >= sr - wrr, cj = j >= sc - wcc;
+              const double v = c.minv_full[(size_t)(offa[fcl] + oj) * k + (offc[fr] + oi)];
+              N[(size_t)(offa[fcl] + j) * k + (offc[fr] + i)] = (ri != cj) ? -v : v;
+            }
+        }
+        if ((sr * wrr) % 2 != 0) detrat = -detrat;
+      }
+      for (int f = 0; f < c.nf; ++f)
+        if (((offa[f + 1] - offa[f]) * wr_a[f]) % 2 != 0) detrat = -detrat;
+      c.minv_full = N;
+    }
     for (int f = 0; f < c.nf; ++f) {
       int k = (int)c.tau_c[f].size();
+      const int ka = (int)c.tau_a[f].size();  // differs from k only off-diagonal
       int w1 = wr_c[f], w2 = wr_a[f];
       std::vector<double> nc, na;
       for (int i = w1; i < k; ++i) nc.push_back(shifted(c.tau_c[f][i]));
       for (int i = 0; i < w1; ++i) nc.push_back(shifted(c.tau_c[f][i]));
-      for (int i = w2; i < k; ++i) na.push_back(shifted(c.tau_a[f][i]));
+      for (int i = w2; i < ka; ++i) na.push_back(shifted(c.tau_a[f][i]));
       for (int i = 0; i < w2; ++i) na.push_back(shifted(c.tau_a[f][i]));
       c.tau_c[f] = nc;
       c.tau_a[f] = na;
+      if (c.offdiag) continue;
       if (!((w1 == 0 && w2 == 0) || (w1 == k && w2 == k))) {
         const std::vector<double>& M = c.minv[f];
         std::vector<double> N((size_t)k * k);
@@ -1587,7 +1641,7 @@ static void step_shift(Chain& c) {
       if ((k % 2) != 0 && ((w1 + w2) % 2) != 0) detrat = -detrat;
     }
     c.det.sign = c.det.sign * detrat;
-    c.cfgsign = -config_sign(c);
+    c.cfgsign = c.offdiag ? -config_sign_offdiag(c) : -config_sign(c);
     c.acc_shift++;
     r.outcome = OUT_ACCEPT;
   } else {
@@ -1678,17 +1732,29 @@ static int full_rebuild_step(Chain& c, std::vector<Op>& nops, double factor, Rec
   flavour_lists(c, nops, tc, ta);
   c.tau_c = tc;
   c.tau_a = ta;
-  LogVal det_new = rebuild_minv(c);
-  std::vector<std::vector<double>> minv_new = c.minv;
-  LogVal det_minv_old{0.0, 1.0};
-  for (int f = 0; f < c.nf; ++f) {
-    int k = (int)tc_old[f].size();
-    if (k == 0) continue;
-    std::vector<double> A = minv_old[f];
+  LogVal det_new, detrat;
+  std::vector<std::vector<double>> minv_new;
+  std::vector<double> mfull_new;
+  if (c.offdiag) {
+    // get_FullHybr_offdiag + get_MatLogDetFull; DetRat = DetNew / Det
+    // (CTQMC.F90:4491-4494)
+    mfull_new = full_hybr_offdiag(c);
     bool sing;
-    det_minv_old = lmul(lu_logdet_inverse(A, k, sing), det_minv_old);
+    det_new = lu_logdet_inverse(mfull_new, total_creators(c), sing);
+    detrat = ldiv(det_new, c.det);
+  } else {
+    det_new = rebuild_minv(c);
+    minv_new = c.minv;
+    LogVal det_minv_old{0.0, 1.0};
+    for (int f = 0; f < c.nf; ++f) {
+      int k = (int)tc_old[f].size();
+      if (k == 0) continue;
+      std::vector<double> A = minv_old[f];
+      bool sing;
+      det_minv_old = lmul(lu_logdet_inverse(A, k, sing), det_minv_old);
+    }
+    detrat = lmul(det_new, det_minv_old);
   }
-  LogVal detrat = lmul(det_new, det_minv_old);
   std::vector<Op> ops_old = c.ops;
   c.ops = nops;
   std::vector<LogVal> part;
@@ -2604,12 +2670,12 @@ void* orc_chain_create(void* model, const Params* p, const double* hybr_fortran)
   return c;
 }
 // Chain with off-diagonal hybridisation (offdiag = 1): F for every flavour
-// pair, Ftau_full(Nd,2,Nd,2,Nftau) in Fortran order.  Pair and
-// outer-superstate moves; global, tau-shift and 4-operator moves and the
+// pair, Ftau_full(Nd,2,Nd,2,Nftau) in Fortran order.  Pair,
+// outer-superstate, global and tau-shift moves; 4-operator moves and the
 // Legendre measurement are not part of the restatement in this mode.
 void* orc_chain_create_full(void* model, const Params* p, const double* hybr_full_fortran) {
-  if (p->p_global > 0.0 || p->p_shift > 0.0 || p->p_4op > 0.0 || p->nleg > 0) {
-    g_err = "off-diagonal chains restate pair and outer-superstate moves only";
+  if (p->p_4op > 0.0 || p->nleg > 0) {
+    g_err = "off-diagonal chains restate pair, outer-superstate, global and tau-shift moves only";
     return nullptr;
   }
   Model* m = (Model*)model;

@@ -403,17 +403,22 @@ def test_offdiag_fast_updates_match_full_recompute():
     """Off-diagonal hybridisation (offdiag = 1): after every proposal the
     determinant and the inverse matrix over all flavours (block order:
     flavour-major, time within a flavour) equal a full rebuild from F for
-    every flavour pair, and the trace a full recompute.  (With a
+    every flavour pair, and the trace a full recompute, with global and
+    tau-shift moves (block rotation of the inverse matrix) at 10 % each and
+    both accepted.  (With a
     spin-conserving H_loc a pair of unlike flavours has zero trace, so
     accepted pairs are of like flavours; the up-down elements of F couple
     the flavours through the determinant.)"""
-    m, c = offdiag_chain(7, taudiff_max=1.5, p_outer=0.1)
+    m, c = offdiag_chain(7, taudiff_max=1.5, p_outer=0.1, p_global=0.1, p_shift=0.1)
     F = XB.ftau_full_bath(OFFDIAG["beta"], OFFDIAG["eps"], OFFDIAG["v"], 2000)[0, :, 0]
     beta = OFFDIAG["beta"]
     c.start_log(3000)
     mixed = 0
+    acc = {"acc_glob": 0, "acc_shift": 0}
     for i in range(3000):
         c.warmup(1)
+        for key in acc:
+            acc[key] += c.counters()[key]
         st = c.state()
         fd, ft = c.full_det(), c.full_trace()
         assert abs(fd[0] - st["det_log"]) < 1e-9 and fd[1] == st["det_sign"], i
@@ -427,6 +432,7 @@ def test_offdiag_fast_updates_match_full_recompute():
         assert np.allclose(c.minv_full(), np.linalg.inv(H), rtol=1e-9, atol=1e-9), i
         mixed += len(set(f for f, _ in cr)) == 2
     assert mixed > 100  # configurations with both flavours: cross blocks in H
+    assert acc["acc_glob"] > 0 and acc["acc_shift"] > 0, acc
     log = c.log()
     acc = log["outcome"] == 4
     assert np.sum(acc & (log["move"] == 0)) > 0 and np.sum(acc & (log["move"] == 1)) > 0
@@ -465,7 +471,8 @@ def test_offdiag_green_function_and_occupations_exact():
 def test_offdiag_two_orbitals_with_hopping_exact():
     """Off-diagonal mode with a sign problem: two orbitals with inter-orbital
     hopping in H_loc (dense superstate blocks) and bath levels coupling both
-    orbitals (orbital-mixing F): G(tau) for all 16 flavour pairs from 16
+    orbitals (orbital-mixing F), global and tau-shift moves at 5 % each:
+    G(tau) for all 16 flavour pairs from 16
     chains agrees with exact diagonalisation within 4.5 standard errors;
     the mean sign is about -0.7 (the configuration sign, recalc_sign, and
     the block order of the inverse matrix matter here)."""
@@ -480,7 +487,8 @@ def test_offdiag_two_orbitals_with_hopping_exact():
     m = O.Model(nd, um, muimp, "Nt Szt")
     G, S = [], []
     for seed in range(16):
-        c = O.Chain(m, beta, ff, 8, seed=seed, ncorr=20, p_outer=0.1, maxhisto=30)
+        c = O.Chain(m, beta, ff, 8, seed=seed, ncorr=20, p_outer=0.1, maxhisto=30,
+                    p_global=0.05, p_shift=0.05)
         c.warmup(2000)
         c.measure(10000)
         G.append(c.results_full())
