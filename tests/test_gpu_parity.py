@@ -564,34 +564,41 @@ def _diag_of(ff):
     return np.stack([np.stack([ff[b, s, b, s] for s in range(2)]) for b in range(nd)])
 
 
-@pytest.mark.parametrize("kind,tdm,pout,nprop,seed", [("spin", 1.5, 0.1, 20000, 5),
-                                                      ("spin", -1.0, 0.0, 10000, 9),
-                                                      ("orbital", -1.0, 0.1, 6000, 6),
-                                                      ("orbital", 1.0, 0.1, 6000, 8)])
-def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, nprop, seed):
+@pytest.mark.parametrize("kind,tdm,pout,nprop,seed,prare", [("spin", 1.5, 0.1, 20000, 5, 0.0),
+                                                            ("spin", -1.0, 0.0, 10000, 9, 0.0),
+                                                            ("orbital", -1.0, 0.1, 6000, 6, 0.0),
+                                                            ("orbital", 1.0, 0.1, 6000, 8, 0.0),
+                                                            ("spin", 1.5, 0.1, 12000, 11, 0.05),
+                                                            ("orbital", -1.0, 0.1, 6000, 12, 0.05)])
+def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, nprop, seed, prare):
     """Off-diagonal hybridisation (offdiag = 1): the GPU chain proposes,
     decides and updates like the oracle chain of the same seed, proposal by
     proposal (flavours, block positions, pair counts, outcomes bit-exact;
-    ratios to 1e-10); then the measured G for every flavour pair, the
-    order histogram and the sign agree, and so do the final configuration
-    and the inverse matrix over all flavours."""
+    ratios to 1e-10), with global and tau-shift moves at prare each where
+    given; then the measured G for every flavour pair, the order histogram
+    and the sign agree, and so do the final configuration and the inverse
+    matrix over all flavours."""
     nd, beta, um, muimp, ff, qns = _offdiag_problem(kind)
     ntau = 10
     mo = O.Model(nd, um, muimp, qns)
-    co = O.Chain(mo, beta, ff, ntau, seed=seed, taudiff_max=tdm, p_outer=pout, ncorr=20, maxhisto=30)
+    co = O.Chain(mo, beta, ff, ntau, seed=seed, taudiff_max=tdm, p_outer=pout, ncorr=20, maxhisto=30,
+                 p_global=prare, p_shift=prare)
     co.start_log(nprop)
     co.warmup(nprop)
     ref = co.log()
     mg = E.Model(nd, um, muimp, qns)
     b = E.Batch(mg, [E.Group(beta, _diag_of(ff), ntau, nchains=1, seed0=seed, taudiff_max=tdm,
                              p_outer=pout, ncorr=20, maxhisto=30, kcap=64, opcap=256,
-                             ftau_full=ff)])
+                             ftau_full=ff, p_global=prare, p_shift=prare)])
     b.set_log(nprop)
     b.warmup(nprop)
     b.sync()
     got = b.log(0)
     compare_logs(ref, got)
     assert np.sum((ref["outcome"] == 4) & (ref["move"] == 0)) > 20
+    if prare > 0:
+        for mv in (2, 3):
+            assert np.sum((ref["outcome"] == 4) & (ref["move"] == mv)) > 5
     co.measure(300)
     b.measure(300)
     b.sync()

@@ -1985,28 +1985,17 @@ __device__ __forceinline__ void tree_flip_all(Ctx& c) {
   __syncwarp();
 }
 
-// Gauss-Jordan inverse with partial pivoting (first maximal pivot) of
-// H(a_rank, c_rank) = Delta(tau_a - tau_c) for the sorted time lists sc/sa
-// of flavour f (get_InvFullHybr, Trace.F90:2279-2336); log|det| and sign are
-// accumulated into dlog/dsign (get_MatLogDetFull, MatrixUpdate.F90:41-99).
-// On return work + kcap^2 holds the inverse, element (c_rank, a_rank) at
-// [a_rank * kcap + c_rank].  Returns false for a singular matrix.
-__device__ NOINL bool gj_inverse(Ctx& c, int f, int k, const double* sc, const double* sa, double* work,
-                                 double& dlog, double& dsign) {
+// Gauss-Jordan inverse with partial pivoting (first maximal pivot) of the
+// k x k matrix H (column-major, leading dimension kcap) into I, which must
+// hold the identity on entry; log|det| and sign accumulate into dlog/dsign.
+// False for a singular matrix.
+__device__ NOINL bool gj_eliminate(Ctx& c, int k, double* H, double* I, double& dlog, double& dsign) {
   const int ld = c.kcap;
-  double* H = work;
-  double* I = work + (size_t)ld * ld;
-  for (int e = c.lane; e < k * k; e += 32) {
-    int ia = e % k, ic = e / k;
-    H[(size_t)ic * ld + ia] = hybrf(c, __dsub_rn(sa[ia], sc[ic]), f);
-    I[(size_t)ic * ld + ia] = (ia == ic) ? 1.0 : 0.0;
-  }
-  __syncwarp();
   for (int j = 0; j < k; ++j) {
     double best = -1.0;
     int bi = j;
     for (int i = j + c.lane; i < k; i += 32) {
-      double a = fabs(H[(size_t)j * ld + i]);
+      const double a = fabs(H[(size_t)j * ld + i]);
       if (a > best) {
         best = a;
         bi = i;
@@ -2014,8 +2003,8 @@ __device__ NOINL bool gj_inverse(Ctx& c, int f, int k, const double* sc, const d
     }
 #pragma unroll
     for (int o = 16; o; o >>= 1) {
-      double ob = __shfl_xor_sync(FULL, best, o);
-      int oi = __shfl_xor_sync(FULL, bi, o);
+      const double ob = __shfl_xor_sync(FULL, best, o);
+      const int oi = __shfl_xor_sync(FULL, bi, o);
       if (ob > best || (ob == best && oi < bi)) {
         best = ob;
         bi = oi;
@@ -2034,22 +2023,22 @@ __device__ NOINL bool gj_inverse(Ctx& c, int f, int k, const double* sc, const d
       dsign = -dsign;
     }
     __syncwarp();
-    double piv = H[(size_t)j * ld + j];
+    const double piv = H[(size_t)j * ld + j];
     dlog += log(fabs(piv));
     if (piv < 0) dsign = -dsign;
-    double ip = 1.0 / piv;
+    const double ip = 1.0 / piv;
     for (int col = c.lane; col < k; col += 32) {
       H[(size_t)col * ld + j] *= ip;
       I[(size_t)col * ld + j] *= ip;
     }
     __syncwarp();
     for (int col = 0; col < k; ++col) {
-      double hj = H[(size_t)col * ld + j];
-      double ij = I[(size_t)col * ld + j];
+      if (col == j) continue;
+      const double hj = H[(size_t)col * ld + j];
+      const double ij = I[(size_t)col * ld + j];
       for (int i = c.lane; i < k; i += 32) {
         if (i == j) continue;
-        double fct = H[(size_t)j * ld + i];
-        if (col == j) continue;
+        const double fct = H[(size_t)j * ld + i];
         H[(size_t)col * ld + i] -= fct * hj;
         I[(size_t)col * ld + i] -= fct * ij;
       }
@@ -2063,6 +2052,26 @@ __device__ NOINL bool gj_inverse(Ctx& c, int f, int k, const double* sc, const d
     __syncwarp();
   }
   return true;
+}
+
+// Gauss-Jordan inverse of H(a_rank, c_rank) = Delta(tau_a - tau_c) for the
+// sorted time lists sc/sa of flavour f (get_InvFullHybr, Trace.F90:2279-2336);
+// log|det| and sign are accumulated into dlog/dsign (get_MatLogDetFull,
+// MatrixUpdate.F90:41-99).  On return work + kcap^2 holds the inverse,
+// element (c_rank, a_rank) at [a_rank * kcap + c_rank].  Returns false for a
+// singular matrix.
+__device__ NOINL bool gj_inverse(Ctx& c, int f, int k, const double* sc, const double* sa, double* work,
+                                 double& dlog, double& dsign) {
+  const int ld = c.kcap;
+  double* H = work;
+  double* I = work + (size_t)ld * ld;
+  for (int e = c.lane; e < k * k; e += 32) {
+    int ia = e % k, ic = e / k;
+    H[(size_t)ic * ld + ia] = hybrf(c, __dsub_rn(sa[ia], sc[ic]), f);
+    I[(size_t)ic * ld + ia] = (ia == ic) ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  return gj_eliminate(c, k, H, I, dlog, dsign);
 }
 
 // log|det| and sign of the current inverse matrix of flavour f in rank order
@@ -2162,6 +2171,12 @@ __device__ NOINL void rebuilt_trace(Ctx& c, int s0, double& lg, double& sg) {
     dense_trace(c, md, s0, lg, sg);
   }
 }
+
+// off-diagonal branches of the global and tau-shift moves (defined with the
+// off-diagonal pair moves below)
+__device__ NOINL void global_od_tail(Ctx& c, int K, int new_outer, double factor, const int* opc_old);
+__device__ NOINL double shift_od_rotate(Ctx& c, const double* tau_old, const int* opc_old, int K, double dtau);
+__device__ NOINL double od_cfgsign(Ctx& c);
 
 // StepGlob, CTQMC.F90:4433-4554: spin flip (30 %, gen_SpinFlipUpdate),
 // creator/annihilator flip (30 %, gen_CAFlip), a user symmetry move or its
@@ -2269,6 +2284,10 @@ __device__ NOINL void ph_global(Ctx& c, Prop& p) {
     if (c.lane == 0) h.qn_glob++;
     r.outcome = 1;
     __syncwarp();
+    return;
+  }
+  if (c.g->offdiag) {  // one inverse matrix over all flavours
+    global_od_tail(c, K, new_outer, factor, opc_old);
     return;
   }
   // new sorted lists and inverse matrices
@@ -2474,7 +2493,8 @@ __device__ NOINL void ph_shift(Ctx& c, Prop& p) {
     double detrat = 1.0;
     double* tmp = glob_srt(c);
     short* tmps = (short*)glob_minv(c);
-    for (int f = 0; f < m.nf; ++f) {
+    if (c.g->offdiag) detrat = shift_od_rotate(c, tau_old, opc_old, K, dtau);
+    for (int f = 0; f < m.nf && !c.g->offdiag; ++f) {
       const int k = h.k[f];
       if (k == 0) continue;
       const double* tc = stau_ptr(c, f, 0);
@@ -2517,8 +2537,8 @@ __device__ NOINL void ph_shift(Ctx& c, Prop& p) {
       h.acc_shift++;
     }
     __syncwarp();
-    const double sgn = config_sign(c);
-    if (c.lane == 0) h.cfgsign = -sgn;
+    const double cs = c.g->offdiag ? od_cfgsign(c) : -config_sign(c);
+    if (c.lane == 0) h.cfgsign = cs;
     r.outcome = 4;
   } else {
     for (int i = c.lane; i < K; i += 32) {
@@ -3631,6 +3651,141 @@ __device__ NOINL void measure_od(Ctx& c) {
     atomicAdd(&G[((size_t)af[j] * nf + cf[i]) * nt + idt - 1], Mv);
   }
   __syncwarp();
+}
+
+// StepGlob with off-diagonal hybridisation (CTQMC.F90:4491-4494): the full
+// hybridisation matrix of the permuted operators in block order
+// (get_FullHybr_offdiag, Trace.F90:2690-2770), its inverse and determinant
+// (get_MatLogDetFull), DetRat = DetNew / Det; then the trace, the
+// Metropolis draw and the installation, or the old codes back.
+__device__ NOINL void global_od_tail(Ctx& c, int K, int new_outer, double factor, const int* opc_old) {
+  Hdr& h = *c.h;
+  cthyb_record& r = *c.rec;
+  const int k = K / 2, ld = c.kcap;
+  int* pos = c.bcode[1];
+  od_positions(c, pos);
+  double* ct = c.scr;
+  double* at = c.scr + ld;
+  int* cf = (int*)(c.scr + 2 * ld);
+  int* af = (int*)(c.scr + 3 * ld);
+  for (int i = c.lane; i < K; i += 32) {
+    const int cd = c.opcode[i];
+    if (cd & 1) {
+      at[pos[i]] = c.optau[i];
+      af[pos[i]] = cd >> 1;
+    } else {
+      ct[pos[i]] = c.optau[i];
+      cf[pos[i]] = cd >> 1;
+    }
+  }
+  __syncwarp();
+  double* H = c.dense;
+  double* I = c.dense + (size_t)ld * ld;
+  for (int e = c.lane; e < k * k; e += 32) {
+    const int ia = e % k, ic = e / k;
+    H[(size_t)ic * ld + ia] = hybrf_full(c, __dsub_rn(at[ia], ct[ic]), af[ia], cf[ic]);
+    I[(size_t)ic * ld + ia] = ia == ic ? 1.0 : 0.0;
+  }
+  __syncwarp();
+  double dlog = 0.0, dsign = 1.0;
+  const bool singular = !gj_eliminate(c, k, H, I, dlog, dsign);
+  // the new inverse kept in the o_glob space (the dense trace below reuses
+  // the dense work space)
+  double* Mn = glob_minv(c);
+  for (int e = c.lane; e < k * k && !singular; e += 32) {
+    const size_t idx = (size_t)(e / k) * ld + (e % k);
+    Mn[idx] = I[idx];
+  }
+  __syncwarp();
+  const double det_lg = singular ? -DHUGE : dlog - h.det_log;
+  const double det_sg = singular ? 0.0 : dsign * h.det_sign;
+  double tr_lg = -DHUGE, tr_sg = 0.0, prob = 0.0;
+  if (!singular) {
+    rebuilt_trace(c, new_outer, tr_lg, tr_sg);
+    prob = fabs(exp(__dsub_rn(tr_lg, h.trace_log) + det_lg) * factor);
+  }
+  const double rnd = grnd(c);
+  r.det_log = det_lg;
+  r.det_sign = det_sg;
+  r.tr_log = tr_lg;
+  r.tr_sign = tr_sg;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    double* Mw = M_ptr(c, 0);
+    for (int e = c.lane; e < k * k; e += 32) {
+      const size_t idx = (size_t)(e / k) * ld + (e % k);
+      Mw[idx] = Mn[idx];
+    }
+    __syncwarp();
+    tree_flip_all(c);
+    if (c.g->o_chk) chk_invalidate(c);
+    if (c.lane == 0) {
+      h.det_log = dlog;
+      h.det_sign = dsign;
+      h.trace_log = tr_lg;
+      h.trace_sign = tr_sg;
+      h.outer_sst = new_outer;
+      h.acc_glob++;
+    }
+    __syncwarp();
+    const double cs = od_cfgsign(c);
+    if (c.lane == 0) h.cfgsign = cs;
+    r.outcome = 4;
+  } else {
+    for (int i = c.lane; i < K; i += 32) c.opcode[i] = opc_old[i];
+    r.outcome = 3;
+  }
+  __syncwarp();
+}
+
+// Accepted tau shift with off-diagonal hybridisation
+// (update_InvFullHybrShiftTau_offdiag, Trace.F90:2490-2600): in every
+// (creator flavour, annihilator flavour) block the rows and columns rotate
+// by the flavour's wrapped creators / annihilators, an entry negated when
+// exactly one of its row and column wrapped.  Returns the determinant sign
+// change, (-1)^(size x wrapped) per flavour block.  tau_old/opc_old hold
+// the operators before the shift (K entries).
+__device__ NOINL double shift_od_rotate(Ctx& c, const double* tau_old, const int* opc_old, int K, double dtau) {
+  const int nf = c.m->nf, ld = c.kcap, k = K / 2;
+  int sz[2 * NFMAX], wr[2 * NFMAX], off[2 * NFMAX];
+  for (int q = 0; q < 2 * nf; ++q) {
+    int n = 0, w = 0;
+    for (int i = c.lane; i < K; i += 32) {
+      n += opc_old[i] == q;
+      w += opc_old[i] == q && tau_old[i] < dtau;
+    }
+    sz[q] = wsumi(n);
+    wr[q] = wsumi(w);
+  }
+  double detrat = 1.0;
+  for (int q = 0; q < 2 * nf; ++q) {
+    off[q] = 0;
+    for (int t = q & 1; t < q; t += 2) off[q] += sz[t];
+    if ((sz[q] * wr[q]) & 1) detrat = -detrat;
+  }
+  const double* Mf = M_ptr(c, 0);
+  double* T = glob_minv(c);
+  for (int e = c.lane; e < k * k; e += 32) {
+    const int row = e % k, col = e / k;
+    int fr = 0, fc = 0;
+    while (fr + 1 < nf && off[2 * (fr + 1)] <= row) ++fr;
+    while (fc + 1 < nf && off[2 * (fc + 1) + 1] <= col) ++fc;
+    const int qr = 2 * fr, qc = 2 * fc + 1;
+    const int i = row - off[qr], j = col - off[qc];
+    const int oi = (i + wr[qr]) % sz[qr], oj = (j + wr[qc]) % sz[qc];
+    const bool ri = i >= sz[qr] - wr[qr], cj = j >= sz[qc] - wr[qc];
+    const double v = Mf[(size_t)(off[qc] + oj) * ld + (off[qr] + oi)];
+    T[(size_t)col * ld + row] = ri != cj ? -v : v;
+  }
+  __syncwarp();
+  double* Mw = M_ptr(c, 0);
+  for (int e = c.lane; e < k * k; e += 32) {
+    const size_t idx = (size_t)(e / k) * ld + (e % k);
+    Mw[idx] = T[idx];
+  }
+  __syncwarp();
+  return detrat;
 }
 
 // One proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250) with
@@ -4833,12 +4988,10 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
       delete B;
       return fail(CTHYB_ERR_ARG, "bad group description");
     }
-    if (G.desc.ftau_full && (G.desc.p_global > 0.0 || G.desc.p_shift > 0.0 || G.desc.p_4op > 0.0 ||
-                             G.desc.nleg > 0 || (G.desc.nscore > 0 && G.desc.score_dE))) {
+    if (G.desc.ftau_full && (G.desc.p_4op > 0.0 || G.desc.nleg > 0 || (G.desc.nscore > 0 && G.desc.score_dE))) {
       delete B;
       return fail(CTHYB_ERR_UNSUPPORTED,
-                  "off-diagonal hybridisation: pair and outer-superstate moves only (no global, tau-shift "
-                  "or 4-operator moves, Legendre or score measurements)");
+                  "off-diagonal hybridisation: no 4-operator moves, Legendre or score measurements");
     }
     layout_group(B, G, 0);
     G.chain0 = B->nchains;
