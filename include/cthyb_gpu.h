@@ -100,9 +100,9 @@ typedef struct {
   double p_4op;          /* Percentage4OperatorMove: share of insertions and removals made as
                             4-operator moves (StepAdd4 / StepRem4, CTQMC.F90:3615-3890, 4153-4431) */
   const double* ftau_full; /* offdiag = 1: F for every flavour pair, (Nd,2,Nd,2,Nftau) Fortran
-                              order (NULL: diagonal hybridisation from ftau).  Pair and
-                              outer-superstate moves only; kcap then bounds the total number of
-                              pairs; the inverse matrix over all flavours is in the reference's
+                              order (NULL: diagonal hybridisation from ftau).  Pair,
+                              outer-superstate, global and tau-shift moves (p_4op = 0, nleg = 0);
+                              kcap then bounds the total number of pairs; the inverse matrix over all flavours is in the reference's
                               block order (add_ftau_offset, Trace.F90:3002-3040). */
 } cthyb_group_desc;
 

@@ -56,6 +56,12 @@ def test_supported_configuration_passes_the_check():
     ctqmc.dest_paras()
 
 
+def test_offdiag_with_global_and_shift_moves_passes_the_check():
+    ctqmc.init_paras(pstring(dict(BASE, offdiag=1, Percentage4OperatorMove=0.0)))
+    ctqmc._check_supported()
+    ctqmc.dest_paras()
+
+
 @pytest.mark.gpu
 def test_solve_through_the_module_matches_the_oracle():
     """init_rnd/init_paras/init_solver/set_taudiffmax/ctqmc_warmup/

@@ -38,7 +38,7 @@ CtHybConfig npz files, cthyb_solver.py:24-87, 316-345).
 
 Parameters selecting moves or modes outside the engine (worm and
 flavour-change moves, segment, state sampling, retarded interactions;
-global, tau-shift or 4-operator moves together with offdiag = 1) raise
+4-operator moves together with offdiag = 1) raise
 NotImplementedError at init_solver.  With offdiag = 1 the full Ftau_full is
 used and gtau_full holds G for every flavour pair (MeasGtauRem_full).  The
 trace-recomputation histograms lhisto/rhisto describe the reference's
@@ -165,10 +165,9 @@ def _check_supported():
         bad.append("Eigenbasis = 0")
     if "All" in _str("QuantumNumbers", "").split():
         bad.append("QuantumNumbers = All")
-    if _int("offdiag", 0) != 0:  # off-diagonal F: pair and outer-superstate moves only
-        for key in ("PercentageGlobalMove", "PercentageTauShiftMove", "Percentage4OperatorMove"):
-            if _real(key, 0.0) != 0.0:
-                bad.append(f"{key} = {_real(key)} with offdiag = 1")
+    if _int("offdiag", 0) != 0 and _real("Percentage4OperatorMove", 0.0) != 0.0:
+        # off-diagonal F: pair, outer-superstate, global and tau-shift moves
+        bad.append(f"Percentage4OperatorMove = {_real('Percentage4OperatorMove')} with offdiag = 1")
     if bad:
         raise NotImplementedError("outside the GPU pair-move engine: " + ", ".join(bad))
 
