@@ -2925,6 +2925,20 @@ void orc_chain_full_det(void* cc, double* out) {
   out[1] = d.sign;
 }
 
+// get_MatLogDetFull (MatrixUpdate.F90:41-99) on a k x k column-major matrix:
+// out = (log|det|, sign), the matrix replaced by its inverse; a singular
+// matrix gives (-huge, 0) and is left in its factorised form.  Returns 1
+// for a singular matrix, else 0.
+int orc_mat_logdet_full(int k, double* mat, double* out) {
+  std::vector<double> A(mat, mat + (size_t)k * k);
+  bool sing;
+  LogVal d = lu_logdet_inverse(A, k, sing);
+  out[0] = d.log;
+  out[1] = d.sign;
+  if (!sing) std::copy(A.begin(), A.end(), mat);
+  return sing ? 1 : 0;
+}
+
 // RNG stream (pins the standard-library engine against random.cc)
 void orc_rng_stream(unsigned seed, int n, double* reals, int nint, int lo, int hi, int* ints) {
   Rng r(seed);

@@ -83,6 +83,7 @@ def lib():
         L.orc_chain_full_trace.argtypes = [vp, dp]
         L.orc_chain_full_det.argtypes = [vp, dp]
         L.orc_rng_stream.argtypes = [C.c_uint, C.c_int, dp, C.c_int, C.c_int, C.c_int, ip]
+        L.orc_mat_logdet_full.argtypes = [C.c_int, dp, dp]
         assert L.orc_record_size() == RECORD_DTYPE.itemsize
         assert L.orc_params_size() == C.sizeof(Params)
         _lib = L
@@ -301,3 +302,14 @@ def rng_stream(seed, n, nint, lo, hi):
     ints = np.zeros(nint, np.int32)
     lib().orc_rng_stream(seed, n, _dp(reals), nint, lo, hi, _ip(ints))
     return reals, ints
+
+
+def mat_logdet_full(mat):
+    """get_MatLogDetFull: (log|det|, sign, inverse or None when singular)."""
+    a = np.array(mat, np.float64, order="F", copy=True)
+    k = a.shape[0]
+    out = np.zeros(2)
+    flat = a.ravel(order="F").copy()
+    sing = lib().orc_mat_logdet_full(k, _dp(flat), _dp(out))
+    inv = None if sing else flat.reshape((k, k), order="F")
+    return out[0], out[1], inv

@@ -94,6 +94,34 @@ def test_time_evolve_known_answer():
     assert abs(c.state()["trace_log"] - expect) < 1e-14
 
 
+def test_mat_logdet_full_reference_case_and_known_answers():
+    """get_MatLogDetFull (MatrixUpdate.F90:41-99): the reference test's
+    rank-2 matrix N(i, j) = i + j, k = 10 (testsuite/ctqmc.tests/
+    1-get-MatFull.F90, which only requires the call to return) goes through
+    without error and is singular to working precision; k = 0 gives
+    (log 0, sign 1); well-conditioned matrices give numpy's slogdet and
+    inverse."""
+    k = 10
+    n = np.array([[i + j for j in range(1, k + 1)] for i in range(1, k + 1)], np.float64)
+    lg, sg, inv = O.mat_logdet_full(n)
+    hadamard = np.sum(np.log(np.linalg.norm(n, axis=0)))
+    assert sg == 0.0 or lg < hadamard - 25.0  # |det| below 1e-11 of the Hadamard bound
+    assert O.mat_logdet_full(np.zeros((0, 0)))[:2] == (0.0, 1.0)
+    one = O.mat_logdet_full(np.array([[-2.5]]))
+    assert one[1] == -1.0 and abs(one[0] - np.log(2.5)) < 1e-15 and one[2][0, 0] == -0.4
+    rng = np.random.default_rng(4)
+    for k in (2, 7, 40):
+        a = rng.normal(size=(k, k)) + 3.0 * np.eye(k) * rng.choice([-1.0, 1.0], size=k)
+        lg, sg, inv = O.mat_logdet_full(a)
+        s_np, l_np = np.linalg.slogdet(a)
+        assert sg == s_np and abs(lg - l_np) < 1e-12 * max(1.0, abs(l_np))
+        assert np.allclose(inv @ a, np.eye(k), atol=1e-12)
+    z = np.ones((3, 3))
+    z[:, 1] = 0.0  # a zero column: exact zero pivot, (-huge, 0)
+    lg, sg, inv = O.mat_logdet_full(z)
+    assert sg == 0.0 and lg == -np.finfo(np.float64).max and inv is None
+
+
 def _hyb(F, beta, t):
     s = 1.0
     if t < 0:
