@@ -1668,6 +1668,13 @@ static void step_shift(Chain& c) {
 // is in `skip` (ensure_valid_NPairs_diag, Trace.F90:1762-1803, on the list
 // without them); the incremental update_NPairs_diag (Trace.F90:1862-1922)
 // gives the same count for operators inside the window.
+// Operators that can form a removable pair: opposite CA, and with diagonal
+// hybridisation the same flavour (is_rempair_diag / is_rempair_offdiag,
+// Trace.F90:2006-2030).
+static inline bool pair_kind(const Chain& c, const Op& x, const Op& y) {
+  return x.ca != y.ca && (c.offdiag || (x.b == y.b && x.s == y.s));
+}
+
 static int count_pairs_list(const Chain& c, const std::vector<Op>& ops, const std::vector<int>& skip) {
   auto skipped = [&](int i) { return std::find(skip.begin(), skip.end(), i) != skip.end(); };
   int n = 0;
@@ -1681,7 +1688,7 @@ static int count_pairs_list(const Chain& c, const std::vector<Op>& ops, const st
       const Op& y = ops[j];
       if (y.tau > c.tauwin_max || y.tau > x.tau + c.taudiff_max) break;
       if (skipped(j)) continue;
-      if (y.b == x.b && y.s == x.s && y.ca != x.ca) ++n;
+      if (pair_kind(c, x, y)) ++n;
     }
   }
   return n;
@@ -1701,7 +1708,7 @@ static void select_pair(const Chain& c, const std::vector<Op>& ops, const std::v
     for (int j = i + 1; j < K; ++j) {
       const Op& y = ops[j];
       if (y.tau > c.tauwin_max || y.tau > x.tau + c.taudiff_max) break;
-      if (skipped(j) || y.b != x.b || y.s != x.s || y.ca == x.ca) continue;
+      if (skipped(j) || !pair_kind(c, x, y)) continue;
       if (--npair <= 0) {
         ix = i;
         iy = j;
@@ -1711,9 +1718,9 @@ static void select_pair(const Chain& c, const std::vector<Op>& ops, const std::v
   }
 }
 
-// is_rempair_diag (Trace.F90:2006-2030)
+// is_rempair (Trace.F90:1994-2030)
 static bool is_rempair(const Chain& c, const Op& x, const Op& y) {
-  return x.b == y.b && x.s == y.s && x.ca != y.ca && x.tau >= c.tauwin_min && x.tau <= c.tauwin_max &&
+  return pair_kind(c, x, y) && x.tau >= c.tauwin_min && x.tau <= c.tauwin_max &&
          y.tau >= c.tauwin_min && y.tau <= c.tauwin_max && std::fabs(x.tau - y.tau) <= c.taudiff_max;
 }
 
@@ -1772,9 +1779,14 @@ static int full_rebuild_step(Chain& c, std::vector<Op>& nops, double factor, Rec
     c.det = det_new;
     c.trace = trnew;
     c.parttrace = part;
-    c.minv = minv_new;
     c.npairs = npairs_new;
-    c.cfgsign = -config_sign(c);
+    if (c.offdiag) {
+      c.minv_full = mfull_new;
+      c.cfgsign = -config_sign_offdiag(c);
+    } else {
+      c.minv = minv_new;
+      c.cfgsign = -config_sign(c);
+    }
     return OUT_ACCEPT;
   }
   c.ops = ops_old;
@@ -1798,9 +1810,11 @@ static void step_add4(Chain& c) {
   r.move = MOVE_ADD4;
   r.outer_sst = c.outer_sst;
   r.k_total = (int)c.ops.size();
-  // pair_OperAdd with N = 4, force_diagonal (Trace.F90:3657-3702): per
-  // pair the annihilator at tau_ref in the window, orbital and spin, the
-  // creator within TaudiffMax; process_OperAdd puts each pair in time order
+  // pair_OperAdd with N = 4 (Trace.F90:3657-3702): per pair the annihilator
+  // at tau_ref in the window, orbital and spin, the creator within
+  // TaudiffMax with the annihilator's flavour (force_diagonal) or, with
+  // off-diagonal hybridisation, its own; process_OperAdd puts each pair in
+  // time order
   Op nw[4];
   double tdf = 1.0;
   for (int pr = 0; pr < 2; ++pr) {
@@ -1813,7 +1827,12 @@ static void step_add4(Chain& c) {
     const double w2 = std::min(tau_ref + c.taudiff_max, c.tauwin_max) - tmin;
     const double tcr = tmin + w2 * c.rng.grnd();
     tdf = tdf * w2;
-    Op a{tau_ref, orb - 1, spin - 1, 1}, cr{tcr, orb - 1, spin - 1, 0};
+    int orb_c = orb, spin_c = spin;
+    if (c.offdiag) {
+      orb_c = c.rng.randint(1, c.nd);
+      spin_c = c.rng.randint(1, 2);
+    }
+    Op a{tau_ref, orb - 1, spin - 1, 1}, cr{tcr, orb_c - 1, spin_c - 1, 0};
     nw[2 * pr] = a.tau < cr.tau ? a : cr;
     nw[2 * pr + 1] = a.tau < cr.tau ? cr : a;
   }
@@ -1877,8 +1896,10 @@ static void step_add4(Chain& c) {
     record(c, r);
     return;
   }
-  const double n2 = 2.0 * c.nd;
-  r.outcome = full_rebuild_step(c, all, tdf * n2 * n2 * rf, r, np_all);
+  // (2 Nd)^4 with off-diagonal hybridisation (both flavours of both pairs
+  // drawn), (2 Nd)^2 otherwise (CTQMC.F90:3822-3827)
+  const double n2 = 2.0 * c.nd, fl = c.offdiag ? n2 * n2 * n2 * n2 : n2 * n2;
+  r.outcome = full_rebuild_step(c, all, tdf * fl * rf, r, np_all);
   if (r.outcome == OUT_ACCEPT) c.acc_add4++;
   r.outer_sst = c.outer_sst;
   r.k_total = (int)c.ops.size();
@@ -1963,8 +1984,8 @@ static void step_rem4(Chain& c) {
     record(c, r);
     return;
   }
-  const double n2 = 2.0 * c.nd;
-  r.outcome = full_rebuild_step(c, nops, 1.0 / (n2 * n2) / tdf / rf, r, np_new);
+  const double n2 = 2.0 * c.nd, fl = c.offdiag ? n2 * n2 * n2 * n2 : n2 * n2;  // CTQMC.F90:4352-4357
+  r.outcome = full_rebuild_step(c, nops, 1.0 / fl / tdf / rf, r, np_new);
   if (r.outcome == OUT_ACCEPT) c.acc_rem4++;
   r.outer_sst = c.outer_sst;
   r.k_total = (int)c.ops.size();
@@ -2671,11 +2692,11 @@ void* orc_chain_create(void* model, const Params* p, const double* hybr_fortran)
 }
 // Chain with off-diagonal hybridisation (offdiag = 1): F for every flavour
 // pair, Ftau_full(Nd,2,Nd,2,Nftau) in Fortran order.  Pair,
-// outer-superstate, global and tau-shift moves; 4-operator moves and the
-// Legendre measurement are not part of the restatement in this mode.
+// outer-superstate, global, tau-shift and 4-operator moves; the Legendre
+// measurement is not part of the restatement in this mode.
 void* orc_chain_create_full(void* model, const Params* p, const double* hybr_full_fortran) {
-  if (p->p_4op > 0.0 || p->nleg > 0) {
-    g_err = "off-diagonal chains restate pair, outer-superstate, global and tau-shift moves only";
+  if (p->nleg > 0) {
+    g_err = "off-diagonal chains: no Legendre measurement";
     return nullptr;
   }
   Model* m = (Model*)model;

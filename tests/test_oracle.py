@@ -427,22 +427,24 @@ def offdiag_chain(seed, **kw):
     return m, O.Chain(m, b["beta"], ff, 10, seed=seed, **kw)
 
 
-def test_offdiag_fast_updates_match_full_recompute():
+@pytest.mark.parametrize("p_4op", [0.0, 0.3])
+def test_offdiag_fast_updates_match_full_recompute(p_4op):
     """Off-diagonal hybridisation (offdiag = 1): after every proposal the
     determinant and the inverse matrix over all flavours (block order:
     flavour-major, time within a flavour) equal a full rebuild from F for
     every flavour pair, and the trace a full recompute, with global and
     tau-shift moves (block rotation of the inverse matrix) at 10 % each and
-    both accepted.  (With a
-    spin-conserving H_loc a pair of unlike flavours has zero trace, so
-    accepted pairs are of like flavours; the up-down elements of F couple
-    the flavours through the determinant.)"""
-    m, c = offdiag_chain(7, taudiff_max=1.5, p_outer=0.1, p_global=0.1, p_shift=0.1)
+    both accepted, and with 4-operator moves of any flavours.  (With a
+    spin-conserving H_loc a single pair of unlike flavours has zero trace,
+    so accepted pairs are of like flavours; the up-down elements of F couple
+    the flavours through the determinant, and a 4-operator move can insert
+    two unlike pairs at once.)"""
+    m, c = offdiag_chain(7, taudiff_max=1.5, p_outer=0.1, p_global=0.1, p_shift=0.1, p_4op=p_4op)
     F = XB.ftau_full_bath(OFFDIAG["beta"], OFFDIAG["eps"], OFFDIAG["v"], 2000)[0, :, 0]
     beta = OFFDIAG["beta"]
     c.start_log(3000)
     mixed = 0
-    acc = {"acc_glob": 0, "acc_shift": 0}
+    acc = {"acc_glob": 0, "acc_shift": 0, "acc_add4": 0, "acc_rem4": 0}
     for i in range(3000):
         c.warmup(1)
         for key in acc:
@@ -461,23 +463,28 @@ def test_offdiag_fast_updates_match_full_recompute():
         mixed += len(set(f for f, _ in cr)) == 2
     assert mixed > 100  # configurations with both flavours: cross blocks in H
     assert acc["acc_glob"] > 0 and acc["acc_shift"] > 0, acc
+    if p_4op > 0:
+        assert acc["acc_add4"] > 10 and acc["acc_rem4"] > 10, acc
     log = c.log()
     acc = log["outcome"] == 4
     assert np.sum(acc & (log["move"] == 0)) > 0 and np.sum(acc & (log["move"] == 1)) > 0
     assert np.sum((log["move"] == 0) & (log["orb"] != log["spin"])) > 0  # unlike pairs proposed
 
 
-def test_offdiag_green_function_and_occupations_exact():
+@pytest.mark.parametrize("p_4op", [0.0, 0.3])
+def test_offdiag_green_function_and_occupations_exact(p_4op):
     """Known answer for the off-diagonal mode: G(tau) for every spin pair
     (Gtau_full, including the off-diagonal up-down element) and the
     occupations and double occupancy from the density matrix of 16 chains
     agree with exact diagonalisation of impurity + bath within 4.5 standard
-    errors."""
+    errors, also with 30 % of the insertions and removals made as
+    4-operator moves ((2 Nd)^4 proposal factors, removable pairs of any
+    flavours)."""
     b = OFFDIAG
     ex = XB.offdiag_answers(b["beta"], b["mu"], b["u"], b["eps"], b["v"], 10)
     G, occ = [], []
     for seed in range(16):
-        m, c = offdiag_chain(seed, taudiff_max=1.0, ncorr=20, p_outer=0.1, maxhisto=30)
+        m, c = offdiag_chain(seed, taudiff_max=1.0, ncorr=20, p_outer=0.1, maxhisto=30, p_4op=p_4op)
         c.warmup(2000)
         c.measure(5000)
         G.append(c.results_full())
