@@ -2441,7 +2441,26 @@ static void init_counters(Chain& c) {
   c.try_add4 = c.acc_add4 = c.try_rem4 = c.acc_rem4 = 0;
 }
 
-// MeasGtauRem(.false.), CTQMC.F90:2252-2440 (tau bins only)
+// Legendre coefficients of one inverse-matrix element (CTQMC.F90:2368-2389
+// and 2533-2555): out[l] += M P_l(x) by the three-term recurrence.
+static void add_legendre(double M, double x, int nleg, double* out) {
+  double plx = 0.0, plm1x = 0.0, plp1x;
+  for (int l = 0; l < nleg; ++l) {
+    if (l == 0) {
+      plp1x = 1.0;
+    } else if (l == 1) {
+      plp1x = x;
+    } else {
+      int ll = l - 1;
+      plp1x = (2.0 * double(ll) + 1.0) / double(ll + 1) * x * plx - double(ll) / double(ll + 1) * plm1x;
+    }
+    out[l] += M * plp1x;
+    plm1x = plx;
+    plx = plp1x;
+  }
+}
+
+// MeasGtauRem(.false.), CTQMC.F90:2252-2440
 static void meas_gtau(Chain& c) {
   int nt = c.p.ntau;
   for (int f = 0; f < c.nf; ++f) {
@@ -2460,23 +2479,9 @@ static void meas_gtau(Chain& c) {
         M = M * c.cfgsign;
         if (idt > nt) idt = nt;
         c.gtau[(size_t)f * nt + (idt - 1)] += M;
-        // Legendre coefficients (CTQMC.F90:2368-2389)
         if (c.p.nleg > 0) {
           double x = ta - tc > 0.0 ? 2.0 / c.p.beta * (ta - tc) - 1.0 : 2.0 / c.p.beta * (c.p.beta + ta - tc) - 1.0;
-          double plx = 0.0, plm1x = 0.0, plp1x;
-          for (int l = 0; l < c.p.nleg; ++l) {
-            if (l == 0) {
-              plp1x = 1.0;
-            } else if (l == 1) {
-              plp1x = x;
-            } else {
-              int ll = l - 1;
-              plp1x = (2.0 * double(ll) + 1.0) / double(ll + 1) * x * plx - double(ll) / double(ll + 1) * plm1x;
-            }
-            c.gleg[(size_t)f * c.p.nleg + l] += M * plp1x;
-            plm1x = plx;
-            plx = plp1x;
-          }
+          add_legendre(M, x, c.p.nleg, &c.gleg[(size_t)f * c.p.nleg]);
         }
       }
   }
@@ -2506,6 +2511,11 @@ static void meas_gtau_full(Chain& c) {
           M = M * c.cfgsign;
           if (idt > nt) idt = nt;
           c.gtau_full[((size_t)fan * c.nf + fcr) * nt + (idt - 1)] += M;
+          if (c.p.nleg > 0) {  // GLeg_full (CTQMC.F90:2533-2555)
+            const double x =
+                ta - tc > 0.0 ? 2.0 / c.p.beta * (ta - tc) - 1.0 : 2.0 / c.p.beta * (c.p.beta + ta - tc) - 1.0;
+            add_legendre(M, x, c.p.nleg, &c.gleg[((size_t)fan * c.nf + fcr) * c.p.nleg]);
+          }
           ++p2;
         }
       ++p1;
@@ -2692,13 +2702,9 @@ void* orc_chain_create(void* model, const Params* p, const double* hybr_fortran)
 }
 // Chain with off-diagonal hybridisation (offdiag = 1): F for every flavour
 // pair, Ftau_full(Nd,2,Nd,2,Nftau) in Fortran order.  Pair,
-// outer-superstate, global, tau-shift and 4-operator moves; the Legendre
-// measurement is not part of the restatement in this mode.
+// outer-superstate, global, tau-shift and 4-operator moves; G and its
+// Legendre coefficients for every flavour pair.
 void* orc_chain_create_full(void* model, const Params* p, const double* hybr_full_fortran) {
-  if (p->nleg > 0) {
-    g_err = "off-diagonal chains: no Legendre measurement";
-    return nullptr;
-  }
   Model* m = (Model*)model;
   const int nd = m->nd, nf = 2 * nd;
   std::vector<double> diag((size_t)nd * 2 * p->nftau);
@@ -2708,6 +2714,7 @@ void* orc_chain_create_full(void* model, const Params* p, const double* hybr_ful
         diag[b + nd * (s + 2 * (size_t)t)] =
             hybr_full_fortran[b + nd * (s + 2 * (b + nd * (s + 2 * (size_t)t)))];
   Chain* c = (Chain*)orc_chain_create(model, p, diag.data());
+  if (!c) return nullptr;
   c->offdiag = true;
   c->hybr_full.resize((size_t)nf * nf * p->nftau);
   for (int b1 = 0; b1 < nd; ++b1)
@@ -2718,6 +2725,7 @@ void* orc_chain_create_full(void* model, const Params* p, const double* hybr_ful
             c->hybr_full[((size_t)c->fi(b1, s1) * nf + c->fi(b2, s2)) * p->nftau + t] =
                 hybr_full_fortran[b1 + nd * (s1 + 2 * (b2 + nd * (s2 + 2 * (size_t)t)))];
   c->gtau_full.assign((size_t)nf * nf * p->ntau, 0.0);
+  c->gleg.assign((size_t)nf * nf * std::max(p->nleg, 0), 0.0);
   return c;
 }
 void orc_chain_destroy(void* c) { delete (Chain*)c; }
@@ -2912,6 +2920,15 @@ void orc_chain_results_full(void* cc, double* gtau_full) {
   const int nt = c.p.ntau;
   for (size_t i = 0; i < c.gtau_full.size(); ++i)
     gtau_full[i] = -c.gtau_full[i] * zs * double(nt) / (c.p.beta * c.p.beta);
+}
+// GLeg_full [f_annihilator][f_creator][nleg], normalised as CTQMC.F90:8767-8771
+void orc_chain_gleg_full(void* cc, double* gleg_full) {
+  Chain& c = *(Chain*)cc;
+  const double ms = c.meas_sign / double(c.cnt_meas);
+  const double zs = -1.0 / (double(c.cnt_meas) * ms);
+  const int nl = c.p.nleg;
+  for (size_t i = 0; i < (size_t)c.nf * c.nf * std::max(nl, 0); ++i)
+    gleg_full[i] = -(c.gleg[i] * std::sqrt(double(2 * (i % nl)) + 1.0) / c.p.beta) * zs;
 }
 int orc_chain_minv(void* cc, int f, double* out) {
   Chain& c = *(Chain*)cc;

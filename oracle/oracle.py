@@ -66,6 +66,7 @@ def lib():
         L.orc_chain_create_full.argtypes = [vp, C.POINTER(Params), dp]
         L.orc_chain_minv_full.argtypes = [vp, dp]
         L.orc_chain_results_full.argtypes = [vp, dp]
+        L.orc_chain_gleg_full.argtypes = [vp, dp]
         L.orc_chain_destroy.argtypes = [vp]
         L.orc_chain_set_taudiffmax.argtypes = [vp, C.c_double]
         L.orc_chain_set_log.argtypes = [vp, C.c_void_p, C.c_longlong]
@@ -187,6 +188,15 @@ class Chain:
         out = np.zeros(nf * nf * self.ntau)
         lib().orc_chain_results_full(self.h, _dp(out))
         return out.reshape(nf, nf, self.ntau)
+
+    def gleg_full(self):
+        """Off-diagonal mode: Legendre coefficients of G for every flavour
+        pair, (2Nd, 2Nd, NLegMax), index [f_annihilator, f_creator, l]
+        (GLeg_full)."""
+        nf, nl = 2 * self.model.nd, self.params.nleg
+        out = np.zeros(max(nf * nf * nl, 1))
+        lib().orc_chain_gleg_full(self.h, _dp(out))
+        return out[:nf * nf * nl].reshape(nf, nf, nl)
 
     def minv_full(self):
         """Off-diagonal mode: the inverse matrix over all flavours in block

@@ -196,3 +196,40 @@ def spinful_answers(nd, beta, umatrix, muimp, eps, v, ntau, nsub=32):
             for b2 in range(nf):
                 g[a, b2, i] = np.mean(np.einsum("tm,mn,tn,nm->t", el, d[a], er, d[b2].T)) / z
     return dict(occ=occ, gtau=g)
+
+
+def legendre_answers(beta, h, ops_a, nleg, nquad=400):
+    """Legendre coefficients G_l = sqrt(2l + 1) int_0^beta P_l(2 tau/beta - 1)
+    <d_a(tau) d+_b(0)> dtau (the normalisation of the solver's GLeg) for the
+    annihilators ops_a of a finite Hamiltonian h, by Gauss-Legendre
+    quadrature; shape (n, n, nleg)."""
+    w, q = np.linalg.eigh(h)
+    w = w - w.min()
+    z = np.exp(-beta * w).sum()
+    d = [q.T @ o @ q for o in ops_a]
+    x, wq = np.polynomial.legendre.leggauss(nquad)
+    t = 0.5 * beta * (x + 1.0)
+    el = np.exp(-(beta - t)[:, None] * w[None, :])
+    er = np.exp(-t[:, None] * w[None, :])
+    n = len(ops_a)
+    g = np.zeros((n, n, nquad))
+    for a in range(n):
+        for b in range(n):
+            g[a, b] = np.einsum("tm,mn,tn,nm->t", el, d[a], er, d[b].T) / z
+    pl = np.stack([np.polynomial.legendre.legval(x, np.eye(nleg)[l]) for l in range(nleg)])
+    gl = 0.5 * beta * np.einsum("abt,lt,t->abl", g, pl, wq)
+    return gl * np.sqrt(2.0 * np.arange(nleg) + 1.0)
+
+
+def offdiag_hamiltonian(mu, u, eps, v):
+    """Impurity (2 spin modes) + spinless bath levels with spin-dependent
+    amplitudes v[b][s]: (h, the two impurity annihilators)."""
+    nb = len(eps)
+    ops = _fermions(2 + nb)
+    num = [x.T @ x for x in ops]
+    h = -mu * (num[0] + num[1]) + u * num[0] @ num[1]
+    for b in range(nb):
+        h = h + eps[b] * num[2 + b]
+        for s in range(2):
+            h = h + v[b][s] * (ops[s].T @ ops[2 + b] + ops[2 + b].T @ ops[s])
+    return h, ops[:2]

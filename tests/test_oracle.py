@@ -503,6 +503,30 @@ def test_offdiag_green_function_and_occupations_exact(p_4op):
     assert np.abs(zo).max() < 4.5, zo
 
 
+def test_offdiag_legendre_coefficients_exact():
+    """GLeg_full (MeasGtauRem_full, CTQMC.F90:2533-2555, normalised as
+    8767-8771): the Legendre coefficients of G for every spin pair from 16
+    off-diagonal chains agree with the exact coefficients of impurity + bath
+    within 4.5 standard errors, and the l = 0 coefficient is the integral of
+    the measured G(tau) bins (sqrt(1) x beta x bin mean)."""
+    b = OFFDIAG
+    nleg = 8
+    h, dd = XB.offdiag_hamiltonian(b["mu"], b["u"], b["eps"], b["v"])
+    ex = XB.legendre_answers(b["beta"], h, dd, nleg)
+    GL, G0 = [], []
+    for seed in range(16):
+        m, c = offdiag_chain(seed, taudiff_max=1.0, ncorr=20, p_outer=0.1, maxhisto=30, nleg=nleg)
+        c.warmup(2000)
+        c.measure(5000)
+        GL.append(c.gleg_full())
+        G0.append(c.results_full())
+    GL, G0 = np.array(GL), np.array(G0)
+    z = (GL.mean(0) - ex) / np.maximum(GL.std(0, ddof=1) / 4.0, 1e-12)
+    assert np.abs(z).max() < 4.5, z
+    assert np.abs(ex[0, 1]).max() > 0.05  # a real off-diagonal G_l
+    assert np.allclose(GL[..., 0], G0.mean(-1) * b["beta"], rtol=1e-9, atol=1e-12)
+
+
 def test_offdiag_two_orbitals_with_hopping_exact():
     """Off-diagonal mode with a sign problem: two orbitals with inter-orbital
     hopping in H_loc (dense superstate blocks) and bath levels coupling both
