@@ -2918,8 +2918,8 @@ __device__ NOINL void ph_add4(Ctx& c, Prop& p) {
     __syncwarp();
     return;
   }
-  const double n2 = 2.0 * m.nd;
-  const double factor = __dmul_rn(__dmul_rn(__dmul_rn(tdf, n2), n2), rf);
+  const double n2 = 2.0 * m.nd;  // taudiff_factor * (2 NBands)**2 * rempair_factor, left to right
+  const double factor = __dmul_rn(__dmul_rn(tdf, __dmul_rn(n2, n2)), rf);
   r.outcome = rebuild4_decide(c, fa, fb, factor, K, np_all);
   if (r.outcome == 4 && c.lane == 0) h.acc_add4++;
   r.outer_sst = h.outer_sst;
