@@ -13,7 +13,11 @@ Writes
   * rng_streams.npz: uniform reals and bounded integers drawn through the
     reference's src/mtrng/random.cc (compiled unchanged from the reference
     sources into oracle/_ref/) for several seeds and ranges, including an
-    interleaved sequence shaped like the draws of one pair proposal.
+    interleaved sequence shaped like the draws of one pair proposal;
+  * bath_legendre.npz: F(tau) of the discrete baths of the exact-
+    diagonalisation tests from the reference's
+    w2dyn/auxiliaries/transform.py (hybr_from_sites), and its Legendre-to-tau
+    matrix (leg2tau), which fixes the G_l normalisation.
 """
 import ctypes as C
 import os
@@ -84,7 +88,34 @@ def rng_streams():
     return out
 
 
+def bath_legendre():
+    sys.path.insert(0, REF)
+    import w2dyn.auxiliaries.transform as T  # reference code, used only here
+    beta, ntau = 4.0, 201
+    tau = np.linspace(0.0, beta, ntau)
+    iw = T.matfreq(beta, "fermi", 10)
+    eps = np.array([-0.6, 0.9])
+    out = {}
+    # one orbital, both spins coupled with V_b to every level (rows: levels)
+    out["single"] = T.hybr_from_sites(eps, np.array([[0.6], [0.8]]), iw, tau, beta)[1]
+    # spinless levels with spin-dependent amplitudes V_{b s}
+    out["offdiag"] = T.hybr_from_sites(eps, np.array([[0.6, 0.3], [0.5, -0.4]]), iw, tau, beta)[1]
+    # two orbitals, spinful levels eps_b: mode (b, s) couples to flavour
+    # 2 o + s with V_{b o}
+    eps2, v2 = np.array([-0.5, 0.7]), [[0.6, 0.3], [0.4, -0.5]]
+    vki = np.zeros((4, 4))
+    for b in range(2):
+        for s in range(2):
+            for o in range(2):
+                vki[2 * b + s, 2 * o + s] = v2[b][o]
+    out["spinful"] = T.hybr_from_sites(np.repeat(eps2, 2), vki, iw, tau, beta)[1]
+    out["leg2tau"] = T.leg2tau(beta, 40, np.linspace(0.0, beta, 41))
+    out["beta"] = np.array(beta)
+    return out
+
+
 if __name__ == "__main__":
     np.savez_compressed(os.path.join(HERE, "umatrices.npz"), **umatrices())
     np.savez_compressed(os.path.join(HERE, "rng_streams.npz"), **rng_streams())
+    np.savez_compressed(os.path.join(HERE, "bath_legendre.npz"), **bath_legendre())
     print("written")

@@ -15,7 +15,13 @@
   (half-filled Bethe lattice self-consistency), atomic-limit density matrix,
   and detailed balance: the sampled expansion-order distribution and
   occupations of a single-orbital impurity with a discrete asymmetric bath
-  equal exact diagonalisation of impurity + bath (tests/exact_bath.py).
+  equal exact diagonalisation of impurity + bath (tests/exact_bath.py);
+  the baths' F(tau) and the Legendre convention of those known answers
+  against the reference's w2dyn/auxiliaries/transform.py (golden fixture).
+* get_MatLogDetFull on the matrix of testsuite/ctqmc.tests/1-get-MatFull.F90.
+* off-diagonal mode (offdiag = 1): fast updates, G for every flavour pair,
+  its Legendre coefficients and the occupations against exact
+  diagonalisation, with global, tau-shift and 4-operator moves.
 """
 import os
 
@@ -72,6 +78,36 @@ def test_reference_rng_live_if_built():
 def test_umatrix_matches_reference_interaction(key, fn, args):
     z = np.load(os.path.join(GOLD, "umatrices.npz"))
     assert np.array_equal(P.flat_umatrix(fn(*args)), z[key])
+
+
+def test_bath_functions_and_legendre_convention_match_reference_transform():
+    """The F(tau) of the exact-diagonalisation baths equal the reference's
+    hybr_from_sites (w2dyn/auxiliaries/transform.py:114-146, golden
+    fixture) for the one-orbital, the spin-mixing and the orbital-mixing
+    bath; the exact Legendre coefficients used as known answers for GLeg
+    follow the reference's convention: its leg2tau matrix
+    (transform.py:148-179) maps them back onto the exact G(tau)."""
+    z = np.load(os.path.join(GOLD, "bath_legendre.npz"))
+    beta = float(z["beta"])
+    eps = [-0.6, 0.9]
+    assert np.allclose(XB.ftau_bath(beta, eps, [0.6, 0.8], 201), z["single"][0, 0], rtol=1e-13, atol=0)
+    ff = XB.ftau_full_bath(beta, eps, [[0.6, 0.3], [0.5, -0.4]], 201)[0, :, 0, :]
+    assert np.allclose(ff, z["offdiag"], rtol=1e-13, atol=1e-16)
+    fs = XB.ftau_full_spinful(2, beta, [-0.5, 0.7], [[0.6, 0.3], [0.4, -0.5]], 201).reshape(4, 4, 201)
+    assert np.allclose(fs, z["spinful"], rtol=1e-13, atol=1e-16)
+    assert np.abs(z["spinful"][0, 2]).max() > 0.05 and np.abs(z["offdiag"][0, 1]).max() > 0.05
+    h, dd = XB.offdiag_hamiltonian(1.3, 2.0, eps, [[0.6, 0.3], [0.5, -0.4]])
+    gl = XB.legendre_answers(beta, h, dd, 40)
+    w, q = np.linalg.eigh(h)
+    w = w - w.min()
+    zz = np.exp(-beta * w).sum()
+    d = [q.T @ o @ q for o in dd]
+    taus = np.linspace(0.0, beta, 41)
+    el = np.exp(-(beta - taus)[:, None] * w[None, :])
+    er = np.exp(-taus[:, None] * w[None, :])
+    g = np.array([[np.einsum("tm,mn,tn,nm->t", el, d[a], er, d[b].T) / zz for b in range(2)] for a in range(2)])
+    rec = np.einsum("il,abl->abi", z["leg2tau"], gl)
+    assert np.abs(rec - g).max() < 1e-8 * np.abs(g).max()
 
 
 def test_time_evolve_known_answer():
