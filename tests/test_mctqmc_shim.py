@@ -62,6 +62,91 @@ def test_offdiag_with_global_and_shift_moves_passes_the_check():
     ctqmc.dest_paras()
 
 
+class _OracleBatch:
+    """The batch calls of ctqmc_calibrate served by oracle chains."""
+
+    def __init__(self, chains):
+        self.chains = chains
+        self.logcap = None
+
+    def set_log(self, cap):
+        self.logcap = cap
+        for c in self.chains:
+            c.start_log(cap)
+
+    def warmup(self, n):
+        for c in self.chains:
+            c.warmup(n)
+
+    def sync(self):
+        pass
+
+    def log(self, i):
+        return self.chains[i].log()
+
+    def set_taudiffmax(self, group, tdm):
+        for c in self.chains:
+            c.set_taudiffmax(tdm)
+
+
+def _calibration_chains(offdiag, n, seed0):
+    if offdiag:
+        import exact_bath as XB
+        beta, nd = 4.0, 1
+        ff = XB.ftau_full_bath(beta, [-0.6, 0.9], [[0.6, 0.3], [0.5, -0.4]], 2000)
+        m = O.Model(1, P.flat_umatrix(P.umatrix_density(1, 2.0, 2.0, 0.0)), P.muimp_solver(1, 1.3), "Nt")
+        return beta, nd, [O.Chain(m, beta, ff, 10, seed=seed0 + i, p_outer=0.1) for i in range(n)]
+    pr = P.config_problem("dd3", beta=10.0)
+    m = O.Model(3, pr["umatrix"], pr["muimp"], "Nt Szt")
+    return 10.0, 3, [O.Chain(m, 10.0, pr["ftau"], 20, seed=seed0 + i, p_outer=0.1, p_global=0.01,
+                             p_shift=0.01) for i in range(n)]
+
+
+def _first_accepted_dtau(chain, n, nprop):
+    chain.start_log(nprop)
+    chain.warmup(nprop)
+    r = chain.log()
+    r = r[(r["outcome"] == 4) & ((r["move"] == 0) | (r["move"] == 1))]
+    return np.abs(r["tau_a"] - r["tau_c"])[:n]
+
+
+@pytest.mark.parametrize("offdiag", [0, 1])
+def test_window_calibration_on_oracle_chains(monkeypatch, offdiag):
+    """ctqmc_calibrate as cthyb_solver.calibrate_taudiff_max calls it
+    (cthyb_solver.py:899-922), run on oracle chains behind the batch calls:
+    phase 1 gives the time differences of the first accepted pair moves of
+    the chains in turn (the same as one long run of identical chains);
+    phase 2 fills the per-flavour histogram over [0, taudiff_max) until
+    every flavour has phase2pairnum entries; a calibration that cannot
+    finish raises; the proposal records are switched off afterwards."""
+    beta, nd, chains = _calibration_chains(offdiag, 3, 40)
+    fake = _OracleBatch(chains)
+    monkeypatch.setattr(ctqmc, "_batch", fake)
+    monkeypatch.setattr(ctqmc, "_nchains", 3)
+    monkeypatch.setattr(ctqmc, "_nd", nd)
+    monkeypatch.setattr(ctqmc, "_beta", beta)
+    monkeypatch.setattr(ctqmc, "_taudiffmax", beta)
+    ctqmc.init_paras(pstring(dict(BASE, offdiag=offdiag)))
+    ctqmc.ctqmc_calibrate(True, 500, 20, 300, 100000, chunk=400)
+    assert fake.logcap == 0
+    want = np.concatenate([_first_accepted_dtau(c, 167, 20000)
+                           for c in _calibration_chains(offdiag, 3, 40)[2]])[:500]
+    assert ctqmc.accpairtau.shape == (500,)
+    assert np.array_equal(ctqmc.accpairtau, want)
+    tdm = float(np.sort(ctqmc.accpairtau)[int(0.995 * 500)])
+    assert 0.0 < tdm <= beta
+    ctqmc.set_taudiffmax(tdm)
+    assert ctqmc._taudiffmax == tdm
+    ctqmc.ctqmc_calibrate(False, 500, 10, 200, 100000, chunk=400)
+    assert ctqmc.accpair.shape == (nd, 2, 10)
+    assert ctqmc.accpair.reshape(2 * nd, 10).sum(axis=1).min() >= 200
+    assert ctqmc.accpair[..., 0].sum() > ctqmc.accpair[..., -1].sum()  # acceptance falls with the distance
+    with pytest.raises(RuntimeError, match="calibration"):
+        ctqmc.ctqmc_calibrate(False, 500, 10, 10 ** 9, 100000, chunk=50, max_chunks=2)
+    assert fake.logcap == 0
+    ctqmc.dest_paras()
+
+
 @pytest.mark.gpu
 def test_solve_through_the_module_matches_the_oracle():
     """init_rnd/init_paras/init_solver/set_taudiffmax/ctqmc_warmup/

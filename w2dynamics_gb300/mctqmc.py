@@ -43,7 +43,11 @@ NotImplementedError at init_solver.  With offdiag = 1 the full Ftau_full is
 used and gtau_full holds G for every flavour pair (MeasGtauRem_full).  The
 trace-recomputation histograms lhisto/rhisto describe the reference's
 list-walking implementation and are returned as zeros; outer trace
-contributions are measured for density-density (monomial) models.  Each
+contributions are measured for density-density (monomial) models.  The
+window calibration (ctqmc_calibrate, run by the driver for TaudiffMax <= 0)
+fills accpairtau and accpair from the engine's proposal records; after a
+measurement accpair (accepted pairs by time difference, a diagnostic) is
+returned as zeros of its (Nd, 2, Ntau) shape.  Each
 init_solver seeds the chains from Nseed; the reference continues one global
 random stream across solves, so solves after the first draw different
 (equally valid) streams.
@@ -64,6 +68,7 @@ _batch = None
 _nd = 0
 _beta = 0.0
 _nchains = 1
+_taudiffmax = 0.0     # the window's taudiff_max (beta for TaudiffMax <= 0, init_window)
 
 # module variables read by the driver (reset by dest_ctqmc)
 gtau = gtau_full = histo = occ = rho1 = rho2 = densitymatrix = None
@@ -175,7 +180,7 @@ def _check_supported():
 # ------------------------------------------------------------------- solver
 def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
     """Model and chain(s) for one solve (init_solver, CTQMC.F90:7894-8086)."""
-    global _model, _batch, _nd, _beta, _nchains
+    global _model, _batch, _nd, _beta, _nchains, _taudiffmax
     global statessuperstates, eigenstatesenergies, occbasismapping
     _check_supported()
     ftau_full = np.asarray(Ftau_full, np.float64)
@@ -191,6 +196,7 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
     dest_ctqmc()
     _nd, _beta = nd, _real("beta")
     _nchains = max(1, _int("GPUChains", 1))
+    _taudiffmax = _real("TaudiffMax", -1.0) if _real("TaudiffMax", -1.0) > 0.0 else _beta
     _model = E.Model(nd, um, mu, qns)
     offdiag = _int("offdiag", 0) != 0
     group = E.Group(_beta, ftau, _int("Ntau"), nchains=_nchains, seed0=_seed,
@@ -221,7 +227,75 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
 
 
 def set_taudiffmax(x):
+    global _taudiffmax
     _batch.set_taudiffmax(0, float(x))
+    _taudiffmax = float(x) if float(x) > 0.0 else _beta
+
+
+def _accepted_pairs(rec, offdiag):
+    """Flavours f = 2(b-1) + (s-1) and time differences of the accepted pair
+    insertions and removals in proposal records, in proposal order: the
+    entries StepAdd / StepRem add to AccPair and AccPairTau
+    (CTQMC.F90:3579-3587, 4112-4127).  The flavour is that of the earlier
+    operator of an inserted pair and of the creator of a removed pair; with
+    diagonal hybridisation both operators have it."""
+    r = rec[(rec["outcome"] == 4) & ((rec["move"] == 0) | (rec["move"] == 1))]
+    dt = np.abs(r["tau_a"] - r["tau_c"])
+    if not offdiag:  # orb, spin 1-based
+        f = 2 * (r["orb"] - 1) + (r["spin"] - 1)
+    else:  # orb = creator flavour + 1, spin = annihilator flavour + 1
+        fc, fa = r["orb"] - 1, r["spin"] - 1
+        f = np.where((r["move"] == 0) & (r["tau_a"] < r["tau_c"]), fa, fc)
+    return f.astype(np.int64), dt
+
+
+def ctqmc_calibrate(list_, phase1pairnum, phase2taugrid, phase2pairnum, nprogress=100000, chunk=1000,
+                    max_chunks=10000):
+    """Window calibration (ctqmc_calibrate, CTQMC.F90:8088-8175): Z-space
+    proposals of every chain until, with list_, phase1pairnum accepted pair
+    moves have given their time differences (accpairtau, taken from the
+    chains in turn), or else until every flavour has phase2pairnum accepted
+    pairs in the histogram accpair (Nd, 2, phase2taugrid) of time differences
+    over [0, taudiff_max).  The proposals advance the chains like a warm-up.
+    The engine's proposal records are read back after every `chunk`
+    proposals of each chain; RuntimeError after max_chunks chunks (the
+    reference would loop forever, e.g. for a flavour without accepted
+    pairs).  nprogress only paces the reference's progress output."""
+    global accpairtau, accpair
+    offdiag = _int("offdiag", 0) != 0
+    nf = 2 * _nd
+    if list_:
+        per_chain = -(-int(phase1pairnum) // _nchains)
+        got = [[] for _ in range(_nchains)]
+    else:
+        hist = np.zeros((nf, int(phase2taugrid)), np.int64)
+    try:
+        for _ in range(max_chunks):
+            _batch.set_log(chunk)
+            _batch.warmup(chunk)
+            _batch.sync()
+            for c in range(_nchains):
+                if list_ and len(got[c]) >= per_chain:
+                    continue
+                f, dt = _accepted_pairs(_batch.log(c), offdiag)
+                if list_:
+                    got[c].extend(dt[:per_chain - len(got[c])].tolist())
+                else:
+                    # min(NAccPair, floor(dtau / AccPairMax * NAccPair) + 1), 1-based
+                    b = np.minimum(int(phase2taugrid), np.floor(dt / _taudiffmax * phase2taugrid).astype(np.int64) + 1)
+                    np.add.at(hist, (f, b - 1), 1)
+                    if hist.sum(axis=1).min() >= phase2pairnum:
+                        break
+            if list_ and all(len(g) >= per_chain for g in got):
+                accpairtau = np.concatenate([np.asarray(g) for g in got])[:int(phase1pairnum)]
+                return
+            if not list_ and hist.sum(axis=1).min() >= phase2pairnum:
+                accpair = hist.reshape(_nd, 2, int(phase2taugrid))
+                return
+        raise RuntimeError("window calibration did not complete within %d x %d proposals per chain"
+                           % (max_chunks, chunk))
+    finally:
+        _batch.set_log(0)
 
 
 def ctqmc_warmup(N):
@@ -251,7 +325,7 @@ def ctqmc_measure(iSector=1, iComponent=1):
 
 def _collect():
     global gtau, gtau_full, histo, occ, rho1, rho2, densitymatrix, mean_sign, gleg, gleg_full
-    global accadd, accrem, accadd4, accrem4, accglob, accshift, outersuperstatehisto, outerstatehisto, signhistosuperstates
+    global accadd, accrem, accadd4, accrem4, accglob, accshift, accpair, outersuperstatehisto, outerstatehisto, signhistosuperstates
     global signhistostates, tracecontribsuperstates, tracecontribstates, lhisto, rhisto
     global ssquare, ssquare_operator
     nd, ns, nf = _nd, _model.nstates, 2 * _nd
@@ -318,6 +392,7 @@ def _collect():
     tracecontribstates = sum(x["contrib_state"] for x in ext) / _nchains
     lhisto = np.zeros(1)
     rhisto = np.zeros(1)
+    accpair = np.zeros((nd, 2, _int("Ntau")), np.int64)
 
 
 # ------------------------------------------------------ configuration access
