@@ -147,6 +147,96 @@ def test_window_calibration_on_oracle_chains(monkeypatch, offdiag):
     ctqmc.dest_paras()
 
 
+class _OracleSolveBatch(_OracleBatch):
+    """The batch calls of ctqmc_warmup / ctqmc_measure and the result
+    collection, served by oracle chains (results in the engine's layout)."""
+
+    class _G:
+        ftau_full = None
+
+    def __init__(self, chains, nd):
+        super().__init__(chains)
+        self.nd = nd
+        self.groups = [self._G()]
+
+    def measure(self, n):
+        for c in self.chains:
+            c.measure(n)
+
+    def reset_measurements(self):
+        pass
+
+    def results(self, i):
+        r = self.chains[i].results()
+        cnt = self.chains[i].counters()
+        return dict(gtau=r["gtau"].reshape(self.nd, 2, -1), mean_sign=r["mean_sign"],
+                    densitymatrix=r["densitymatrix"], histo=r["histo"].reshape(self.nd, 2, -1),
+                    counters={k: cnt[k] for k in ("try_add", "acc_add", "try_rem", "acc_rem")})
+
+    def results_extra(self, i):
+        x = self.chains[i].results_extra()
+        x["gleg"] = x["gleg"].reshape(self.nd, 2, -1)
+        return x
+
+    def move_counters(self, i):
+        cnt = self.chains[i].counters()
+        return {k: cnt[k] for k in ("try_glob", "acc_glob", "try_shift", "acc_shift", "try_add4",
+                                    "acc_add4", "try_rem4", "acc_rem4")}
+
+
+# module variables cthyb_solver.get_resultset reads in every Z-space run
+# (cthyb_solver.py:946-977); it copies each with .copy() (1028-1030)
+RESULTSET = ["gtau", "gtau_full", "rhisto", "lhisto", "histo", "statessuperstates",
+             "eigenstatesenergies", "occbasismapping", "outersuperstatehisto", "outerstatehisto",
+             "signhistosuperstates", "signhistostates", "tracecontribsuperstates",
+             "tracecontribstates", "occ", "gleg", "gleg_full", "accadd", "accadd4", "accrem",
+             "accrem4", "accpair", "accglob", "accshift", "accflavc", "mean_sign", "time_warmup",
+             "time_sim", "time_sim_steps", "ssquare_operator", "densitymatrix", "rho2", "rho1",
+             "ssquare"]
+
+
+def test_module_results_on_oracle_chains(monkeypatch):
+    """ctqmc_warmup / ctqmc_measure and the result collection of the module
+    with two oracle chains behind the batch calls (the host model set-up is
+    the engine's own, which needs no GPU): every module variable the
+    driver's get_resultset reads exists and copies like an f2py variable,
+    with the driver's shapes, and G(tau), the sign and the histogram are the
+    sign-weighted combination of the chains."""
+    from w2dynamics_gb300 import engine as E
+    pr = P.config_problem("dd3", beta=10.0)
+    nd, ntau = 3, BASE["Ntau"]
+    par = dict(BASE, Nmeas=40, GPUChains=2)
+    ctqmc.init_paras(pstring(par))
+    mo = O.Model(nd, pr["umatrix"], pr["muimp"], "Nt Szt")
+    chains = [O.Chain(mo, 10.0, pr["ftau"], ntau, seed=11 + i, taudiff_max=5.0, ncorr=BASE["NCorr"],
+                      p_outer=0.1, maxhisto=BASE["MaxHisto"] + 1, p_global=0.005, p_shift=0.005,
+                      nleg=BASE["NLegMax"], symmoves=[[2, 3, 1, 5, 6, 4]], p_4op=0.1)
+              for i in range(2)]
+    fake = _OracleSolveBatch(chains, nd)
+    model = E.Model(nd, pr["umatrix"], pr["muimp"], "Nt Szt")
+    for key, val in (("_batch", fake), ("_model", model), ("_nd", nd), ("_nchains", 2), ("_beta", 10.0)):
+        monkeypatch.setattr(ctqmc, key, val)
+    ctqmc._model_tables()
+    ctqmc.ctqmc_warmup(500)
+    ctqmc.ctqmc_measure(1, 1)
+    for name in RESULTSET:
+        v = getattr(ctqmc, name)
+        assert isinstance(v, np.ndarray), name
+        v.copy()
+    assert ctqmc.gtau.shape == (nd, 2, ntau) and ctqmc.gtau_full.shape == (nd, 2, nd, 2, ntau)
+    assert ctqmc.gleg_full.shape == (nd, 2, nd, 2, BASE["NLegMax"])
+    assert ctqmc.accpair.shape == (nd, 2, ntau)
+    assert ctqmc.rho1.size == (2 * nd) ** 2 and ctqmc.rho2.size == (2 * nd) ** 4
+    rs = [c.results() for c in chains]
+    s = np.array([r["mean_sign"] for r in rs])
+    want = sum(r["gtau"] * w for r, w in zip(rs, s)) / s.sum()
+    assert np.allclose(ctqmc.gtau.reshape(2 * nd, ntau), want, rtol=1e-13, atol=0)
+    assert ctqmc.mean_sign == s.mean()
+    assert np.array_equal(ctqmc.histo.reshape(2 * nd, -1), sum(r["histo"] for r in rs) / 2)
+    assert 0.0 < float(ctqmc.accadd4) < 1.0
+    ctqmc.dest_paras()
+
+
 @pytest.mark.gpu
 def test_solve_through_the_module_matches_the_oracle():
     """init_rnd/init_paras/init_solver/set_taudiffmax/ctqmc_warmup/

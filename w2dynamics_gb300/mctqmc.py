@@ -78,12 +78,14 @@ outersuperstatehisto = outerstatehisto = signhistosuperstates = signhistostates 
 tracecontribsuperstates = tracecontribstates = None
 lhisto = rhisto = None
 ssquare = ssquare_operator = None
-mean_sign = 0.0
+# scalars are 0-d arrays, as f2py exposes them (the driver copies every
+# result with .copy(), cthyb_solver.py:1028-1030)
+mean_sign = np.array(0.0)
 accadd = np.zeros(NWormSectors)
 accrem = np.zeros(NWormSectors)
-accadd4 = accrem4 = accglob = accshift = accflavc = 0.0
+accadd4, accrem4, accglob, accshift, accflavc = (np.array(0.0) for _ in range(5))
 accpair = accpairtau = None
-time_warmup = time_sim = time_sim_steps = 0.0
+time_warmup, time_sim, time_sim_steps = (np.array(0.0) for _ in range(3))
 aborted = 0
 simid = 0
 fancy_prog = False
@@ -181,7 +183,6 @@ def _check_supported():
 def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
     """Model and chain(s) for one solve (init_solver, CTQMC.F90:7894-8086)."""
     global _model, _batch, _nd, _beta, _nchains, _taudiffmax
-    global statessuperstates, eigenstatesenergies, occbasismapping
     _check_supported()
     ftau_full = np.asarray(Ftau_full, np.float64)
     nd = ftau_full.shape[0]
@@ -213,7 +214,14 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
         group.symmoves = np.array([[int(x) for x in _raw("SymMove%02d" % (i + 1)).split()]
                                    for i in range(nsym)], np.int32)
     _batch = E.Batch(_model, [group])
-    ns = _model.nstates
+    _model_tables()
+
+
+def _model_tables():
+    """statessuperstates, eigenstatesenergies and occbasismapping of the
+    present model (init_solver)."""
+    global statessuperstates, eigenstatesenergies, occbasismapping
+    ns, nd = _model.nstates, _nd
     statessuperstates = np.zeros(ns, np.int32)
     for s in range(_model.nsst):
         o, n = _model.sst_offset[s], _model.sst_size[s]
@@ -303,7 +311,7 @@ def ctqmc_warmup(N):
     t0 = time.perf_counter()
     _batch.warmup(int(N))
     _batch.sync()
-    time_warmup = time.perf_counter() - t0
+    time_warmup = np.array(time.perf_counter() - t0)
 
 
 def init_counters():
@@ -319,7 +327,8 @@ def ctqmc_measure(iSector=1, iComponent=1):
     _batch.reset_measurements()
     _batch.measure(_int("Nmeas"))
     _batch.sync()
-    time_sim = time_sim_steps = time.perf_counter() - t0
+    time_sim = np.array(time.perf_counter() - t0)
+    time_sim_steps = time_sim.copy()
     _collect()
 
 
@@ -336,7 +345,7 @@ def _collect():
     # combined run is the sign-weighted average
     gtau = sum(r["gtau"] * s for r, s in zip(res, signs)) / wsum
     dm_eigen = sum(r["densitymatrix"] * s for r, s in zip(res, signs)) / wsum
-    mean_sign = float(signs.mean())
+    mean_sign = np.array(signs.mean())
     histo = sum(r["histo"] for r in res) / _nchains
     cnt = {k: sum(r["counters"][k] for r in res) for k in res[0]["counters"]}
     mc = [_batch.move_counters(c) for c in range(_nchains)]
@@ -345,10 +354,10 @@ def _collect():
     accrem = np.zeros(NWormSectors)
     accadd[0] = cnt["acc_add"] / max(cnt["try_add"], 1)
     accrem[0] = cnt["acc_rem"] / max(cnt["try_rem"], 1)
-    accadd4 = mcnt["acc_add4"] / mcnt["try_add4"] if mcnt["try_add4"] else 0.0
-    accrem4 = mcnt["acc_rem4"] / mcnt["try_rem4"] if mcnt["try_rem4"] else 0.0
-    accglob = mcnt["acc_glob"] / mcnt["try_glob"] if mcnt["try_glob"] else float("nan")
-    accshift = mcnt["acc_shift"] / mcnt["try_shift"] if mcnt["try_shift"] else float("nan")
+    accadd4 = np.array(mcnt["acc_add4"] / mcnt["try_add4"] if mcnt["try_add4"] else 0.0)
+    accrem4 = np.array(mcnt["acc_rem4"] / mcnt["try_rem4"] if mcnt["try_rem4"] else 0.0)
+    accglob = np.array(mcnt["acc_glob"] / mcnt["try_glob"] if mcnt["try_glob"] else float("nan"))
+    accshift = np.array(mcnt["acc_shift"] / mcnt["try_shift"] if mcnt["try_shift"] else float("nan"))
     gtau_full = np.zeros((nd, 2, nd, 2, gtau.shape[-1]))
     if _batch.groups[0].ftau_full is not None:
         # offdiag = 1: MeasGtauRem_full fills Gtau_full, Gtau stays zero
