@@ -2,8 +2,9 @@
 //
 // CPU restatement of the w2dynamics CT-HYB Z-space loop (Fortran module
 // `ctqmc`, matrix-vector path): pair insertion/removal, outer-superstate,
-// global, tau-shift and 4-operator moves with diagonal hybridisation, and
-// pair moves with off-diagonal hybridisation (offdiag = 1).  It is the
+// global, tau-shift and 4-operator moves with diagonal and with
+// off-diagonal hybridisation (offdiag = 1), and the Z-space estimators
+// (G(tau), GLeg, GLeg_full, Gtau_full, rho at beta/2, histograms).  It is the
 // checker for the GPU library and the timed CPU baseline; it is never
 // linked into, loaded by, or called from the product library.
 //
@@ -16,7 +17,10 @@
 // testsuite/ctqmc.tests/3-operator-list-stress-test.F90:111-268, the
 // time-evolution identity of testsuite/ctqmc.tests/2-time-evolve-in-eigenbasis
 // .F90:5-58, and U matrices generated by the reference's own
-// w2dyn/dmft/interaction.py.  Determinant ratios and traces are further
+// w2dyn/dmft/interaction.py, the get_MatLogDetFull conventions on the matrix
+// of testsuite/ctqmc.tests/1-get-MatFull.F90, and the bath F(tau) and
+// Legendre normalisation of the known answers against the reference's
+// w2dyn/auxiliaries/transform.py.  Determinant ratios and traces are further
 // checked against dense FP64 recomputation (LU and full Fock-space
 // matrix exponentials) in the test suite, and the sampled distributions
 // (expansion orders, occupations, G(tau) for every flavour pair) against
