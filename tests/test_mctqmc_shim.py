@@ -154,10 +154,14 @@ class _OracleSolveBatch(_OracleBatch):
     class _G:
         ftau_full = None
 
-    def __init__(self, chains, nd):
+    def __init__(self, chains, nd, ftau_full=None):
         super().__init__(chains)
         self.nd = nd
         self.groups = [self._G()]
+        self.groups[0].ftau_full = ftau_full
+
+    def results_full(self, i):
+        return self.chains[i].results_full()
 
     def measure(self, n):
         for c in self.chains:
@@ -234,6 +238,43 @@ def test_module_results_on_oracle_chains(monkeypatch):
     assert ctqmc.mean_sign == s.mean()
     assert np.array_equal(ctqmc.histo.reshape(2 * nd, -1), sum(r["histo"] for r in rs) / 2)
     assert 0.0 < float(ctqmc.accadd4) < 1.0
+    ctqmc.dest_paras()
+
+
+def test_offdiag_module_results_on_oracle_chains(monkeypatch):
+    """offdiag = 1 through the module's result collection with two oracle
+    chains: gtau_full[b, s, b', s'] is the sign-weighted Gtau_full of the
+    chains at (flavour 2b + s, flavour 2b' + s'), including the spin-mixing
+    element."""
+    import exact_bath as XB
+    from w2dynamics_gb300 import engine as E
+    beta, ntau = 4.0, 10
+    ff = XB.ftau_full_bath(beta, [-0.6, 0.9], [[0.6, 0.3], [0.5, -0.4]], 2000)
+    um = P.flat_umatrix(P.umatrix_density(1, 2.0, 2.0, 0.0))
+    muimp = P.muimp_solver(1, 1.3)
+    par = dict(BASE, beta=beta, Nd=1, Ntau=ntau, QuantumNumbers="Nt", offdiag=1, Nmeas=300, NCorr=20,
+               PercentageGlobalMove=0.05, PercentageTauShiftMove=0.05, Percentage4OperatorMove=0.0,
+               NSymMove=0, MeasSsquare=0, NLegMax=0)
+    ctqmc.init_paras(pstring(par))
+    ctqmc._check_supported()
+    mo = O.Model(1, um, muimp, "Nt")
+    chains = [O.Chain(mo, beta, ff, ntau, seed=3 + i, taudiff_max=1.5, ncorr=20, p_outer=0.1,
+                      maxhisto=BASE["MaxHisto"] + 1, p_global=0.05, p_shift=0.05) for i in range(2)]
+    fake = _OracleSolveBatch(chains, 1, ftau_full=ff)
+    model = E.Model(1, um, muimp, "Nt")
+    for key, val in (("_batch", fake), ("_model", model), ("_nd", 1), ("_nchains", 2), ("_beta", beta)):
+        monkeypatch.setattr(ctqmc, key, val)
+    ctqmc._model_tables()
+    ctqmc.ctqmc_warmup(2000)
+    ctqmc.ctqmc_measure(1, 1)
+    s = np.array([c.results()["mean_sign"] for c in chains])
+    want = sum(c.results_full() * w for c, w in zip(chains, s)) / s.sum()
+    got = np.array([[ctqmc.gtau_full[fa // 2, fa % 2, fc // 2, fc % 2] for fc in range(2)] for fa in range(2)])
+    assert np.allclose(got, want, rtol=1e-13, atol=0)
+    assert np.abs(got[0, 1]).max() > 0.01
+    for name in RESULTSET:
+        if name not in ("ssquare", "ssquare_operator"):
+            getattr(ctqmc, name).copy()
     ctqmc.dest_paras()
 
 
