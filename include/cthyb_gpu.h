@@ -104,7 +104,15 @@ typedef struct {
                               outer-superstate, global and tau-shift moves (p_4op = 0, nleg = 0);
                               kcap then bounds the total number of pairs; the inverse matrix over all flavours is in the reference's
                               block order (add_ftau_offset, Trace.F90:3002-3040). */
+  int32_t refresh_every; /* drift control (no counterpart in the reference, which rebuilds M
+                            exactly only in global moves and set_mc_config): after this many
+                            accepted pair updates a chain rebuilds all its inverse matrices from
+                            the operator times by Gauss-Jordan elimination (get_InvFullHybr,
+                            Trace.F90:2279-2336) and continues with them; 0: every
+                            CTHYB_REFRESH_DEFAULT updates, < 0: never.  See cthyb_batch_drift. */
 } cthyb_group_desc;
+
+#define CTHYB_REFRESH_DEFAULT 1000
 
 #define CTHYB_FLAG_DENSE 1  /* dense block trace even for monomial models */
 #define CTHYB_FLAG_NO_DM 2  /* skip the beta/2 density-matrix measurement */
@@ -256,6 +264,15 @@ int cthyb_batch_minv(cthyb_batch_t batch, int chain, int f, int* k, double* out)
  * replace != 0 also installs the rebuilt matrices. */
 int cthyb_batch_refresh_minv(cthyb_batch_t batch, int replace, double* maxdev);
 
+/* Drift of the fast updates, over all chains since creation or the last
+ * reset (no counterpart in the reference): the largest |M_fast - M_rebuilt|
+ * element and |log|det H| fast - rebuilt| seen at the periodic rebuilds
+ * (refresh_every), the number of rebuilds and of rebuilds whose determinant
+ * sign disagreed with the fast-updated one.  reset != 0 clears them after
+ * reading.  Any output pointer may be NULL. */
+int cthyb_batch_drift(cthyb_batch_t batch, double* max_dev_m, double* max_dev_logdet, int64_t* refreshes,
+                      int64_t* sign_errors, int reset);
+
 /* Per-proposal records (layout cthyb_record below) for parity checks:
  * cap records per chain; 0 disables. */
 int cthyb_batch_set_log(cthyb_batch_t batch, int64_t cap_per_chain);
@@ -266,9 +283,12 @@ typedef struct {
   double tau_c, tau_a, det_log, det_sign, tr_log, tr_sign, prob, rand;
 } cthyb_record;
 
-/* Device-side bookkeeping statistics for the roofline: bytes of M and
- * operator arrays touched and flops of the determinant ratios and updates,
- * summed over all chains since the last reset (8 int64). */
+/* Device-side bookkeeping statistics for the roofline, summed over all
+ * chains since the last reset (8 int64): bytes of M touched, flops of the
+ * determinant ratios and updates, bytes of the operator arrays touched,
+ * time-bin tree nodes rebuilt, pair proposals, accepted pair proposals,
+ * FP64 flops of the dense-block trace products and bytes of their
+ * operands. */
 int cthyb_batch_work_counters(cthyb_batch_t batch, int64_t* out8, int reset);
 
 /* Allocation-free inverse hybridisation matrix of one flavour -- no
@@ -285,8 +305,10 @@ int cthyb_batch_work_counters(cthyb_batch_t batch, int64_t* out8, int reset);
  * and logdet[2] = log|det H|, sign of H(a,c) = F(tau_a - tau_c).
  * Asynchronous on `stream` (cudaStream_t, NULL for the default stream).
  * The first call on a device resolves the array's device address with that
- * device current and should come before any stream capture.  Calls share
- * the array: calls whose kernels overlap on the GPU race. */
+ * device current and should come before any stream capture; the address is
+ * then kept for the life of the process, so it is not valid after a
+ * cudaDeviceReset of that device (do not use this entry point after one).
+ * Calls share the array: calls whose kernels overlap on the GPU race. */
 int cthyb_minv_rebuild_noalloc(int k, const double* tau_c, const double* tau_a, const double* ftau,
                                int nftau, double beta, double* minv, double* logdet, void* stream);
 

@@ -1,10 +1,11 @@
 """Generate the golden fixtures in tests/golden/ from the w2dynamics reference.
 
-Run in a container where the reference sources are mounted at
-/root/reference (they are not needed afterwards):
+Run where the reference sources are present (they are not needed
+afterwards); their root directory comes from --reference-root, else the
+environment variable W2DYNAMICS_SRC, else /root/reference:
 
-    python oracle/build_oracle.py        # builds oracle/_ref/librandom_ref.so
-    python tests/golden/make_golden.py
+    python oracle/build_oracle.py [--reference-root DIR]    # oracle/_ref/librandom_ref.so
+    python tests/golden/make_golden.py [--reference-root DIR]
 
 Writes
   * umatrices.npz: U matrices produced by the reference's own
@@ -25,7 +26,7 @@ import sys
 
 import numpy as np
 
-REF = "/root/reference"
+REF = os.environ.get("W2DYNAMICS_SRC") or "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 
@@ -115,6 +116,12 @@ def bath_legendre():
 
 
 if __name__ == "__main__":
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference-root", default=None, help="root of the w2dynamics sources")
+    a = ap.parse_args()
+    if a.reference_root:
+        REF = a.reference_root
     np.savez_compressed(os.path.join(HERE, "umatrices.npz"), **umatrices())
     np.savez_compressed(os.path.join(HERE, "rng_streams.npz"), **rng_streams())
     np.savez_compressed(os.path.join(HERE, "bath_legendre.npz"), **bath_legendre())

@@ -16,8 +16,6 @@ import pytest
 from w2dynamics_gb300 import engine as E
 from w2dynamics_gb300 import problems as P
 
-pytestmark = pytest.mark.gpu
-
 
 def _reference(pr, beta, taus_c, taus_a, b, s):
     """M and log|det| from the regular entry points (one flavour only)."""
@@ -53,12 +51,12 @@ def _noalloc(torch, lib, beta, taus_c, taus_a, F):
     return minv[:k * k].cpu().numpy().reshape((k, k), order="F"), logdet.cpu().numpy()
 
 
+@pytest.mark.gpu
 def test_noalloc_matches_regular_entry_point_twice():
     torch = pytest.importorskip("torch")
     lib = E.load(build_if_missing=True)
     beta = 10.0
     pr = P.config_problem("dd3", beta=beta)
-    F = pr["ftau"][1, 0]
     rng = np.random.default_rng(7)
     for k, (b, s) in ((6, (1, 0)), (17, (2, 1))):  # two calls in a row, different sizes
         taus = np.sort(rng.uniform(0.0, beta, 2 * k))
@@ -69,10 +67,11 @@ def test_noalloc_matches_regular_entry_point_twice():
         assert np.allclose(M, M_ref, rtol=1e-9, atol=1e-9 * np.abs(M_ref).max())
         assert abs(ld[0] - dlog_ref) <= 1e-10 * max(1.0, abs(dlog_ref))
         assert ld[1] == dsign_ref
-    _ = F
 
 
 def test_noalloc_rejects_oversized_k():
+    """Host-side argument check only (no kernel is launched), so it runs
+    without a GPU as well."""
     lib = E.load(build_if_missing=True)
     rc = lib.cthyb_minv_rebuild_noalloc(257, None, None, None, 10, 1.0, None, None, None)
     assert rc == -3

@@ -314,15 +314,20 @@ __device__ __forceinline__ int sub(const double* ad, int n, double x) {
 __device__ __forceinline__ bool teq(double a, double b) { return tkey(a) == tkey(b); }
 
 // ---------------------------------------------------------------------------
-// Hybridisation function: get_HybrF, Trace.F90:1014-1033, with the
-// reference's operation order and no fused multiply-adds.
+// Hybridisation function: the linear interpolation of get_HybrF,
+// Trace.F90:1014-1033.  The grid coordinate is tau * ((Nftau - 1) / beta)
+// (the reference divides first: tau / beta * (Nftau - 1)) and the
+// interpolation is one fused multiply-add, so the value agrees with the
+// reference's to within a few units in the last place -- far inside the
+// 1e-10 tolerance of the ratios -- at one FP64 multiply instead of a
+// division per call.
 __device__ __forceinline__ double hybrf(const Ctx& c, double tau, int f) {
   const DGroup& g = *c.g;
   // tau is a difference of distinct times, never -0.0, so the sign bit
   // decides the antiperiodic branch
   const long long neg = __double_as_longlong(tau) & (long long)0x8000000000000000ll;
   if (neg) tau = tau + g.beta;
-  double n = tau * g.hscale;  // tau / beta * (Nftau - 1)
+  double n = tau * g.hscale;  // hscale = (Nftau - 1) / beta
   int in = (int)n;
   double fr = n - (double)in;
   int i = min(max(in, 0), g.nftau - 2);
@@ -950,6 +955,10 @@ __device__ NOINL void dense_trace(Ctx& c, const Mod& md, int s0, double& lg, dou
     __syncwarp();
     int nn = m.sst_n[nxt];
     const double* B = m.blk + m.blk_off[((size_t)cur * m.nf + f) * 2 + ca];
+    if (c.lane == 0) {
+      c.h->w_tflops += 2ll * nn * ncur * n0;
+      c.h->w_tbytes += 8ll * (nn * ncur + ncur * n0 + nn * n0);
+    }
     double mx = 0.0;
     for (int e = c.lane; e < nn * n0; e += 32) {
       int i = e % nn, col = e / nn;
@@ -1079,6 +1088,10 @@ __device__ bool col_step(Ctx& c, int& sst, int& rows, int cols, double*& v, doub
   col_evolve(c, sst, rows, cols, v, lg, dt);
   const int nn = m.sst_n[nxt];
   const double* B = m.blk + m.blk_off[((size_t)sst * m.nf + f) * 2 + ca];
+  if (c.lane == 0) {
+    c.h->w_tflops += 2ll * nn * rows * cols;
+    c.h->w_tbytes += 8ll * (nn * rows + rows * cols + nn * cols);
+  }
   for (int e = c.lane; e < nn * cols; e += 32) {
     const int i = e % nn, col = e / nn;
     double acc = 0.0;
@@ -1854,6 +1867,7 @@ __device__ NOINL void ph_accept_add(Ctx& c, Prop& p) {
     h.npairs = p.np;
     h.outer_sst = p.snew;
     h.acc_add++;
+    h.acc_since_refresh++;
     h.w_opbytes += 24ll * (K - p.p1) + 40ll * k;
   }
   __syncwarp();
@@ -1923,6 +1937,7 @@ __device__ NOINL void ph_accept_rem(Ctx& c, Prop& p) {
     h.trace_sign = p.tr_sign;
     h.outer_sst = p.snew;
     h.acc_rem++;
+    h.acc_since_refresh++;
     h.w_opbytes += 24ll * (K - p.ix) + 40ll * k;
     // update_NPairs(-1): the pair and the partners of its members
     const double* oppx = srt_ptr(c, f, 1 - p.cax);
@@ -3268,6 +3283,7 @@ __device__ NOINL void od_accept(Ctx& c, double det_lg, double det_sg, double tr_
     h.trace_sign = tr_sg;
     h.outer_sst = new_outer;
     h.npairs = np_new;
+    h.acc_since_refresh++;
   }
   __syncwarp();
   const double cs = od_cfgsign(c);
@@ -3653,14 +3669,12 @@ __device__ NOINL void measure_od(Ctx& c) {
   __syncwarp();
 }
 
-// StepGlob with off-diagonal hybridisation (CTQMC.F90:4491-4494): the full
-// hybridisation matrix of the permuted operators in block order
-// (get_FullHybr_offdiag, Trace.F90:2690-2770), its inverse and determinant
-// (get_MatLogDetFull), DetRat = DetNew / Det; then the trace, the
-// Metropolis draw and the installation, or the old codes back.
-__device__ NOINL void global_od_tail(Ctx& c, int K, int new_outer, double factor, const int* opc_old) {
-  Hdr& h = *c.h;
-  cthyb_record& r = *c.rec;
+// Inverse of the full hybridisation matrix of the configuration in the
+// operator arrays (K operators) in block order (get_FullHybr_offdiag,
+// Trace.F90:2690-2770, inverted by Gauss-Jordan): on return
+// c.dense + kcap^2 holds element (creator position, annihilator position)
+// at [a * kcap + c]; log|det| and sign in dlog/dsign.  False when singular.
+__device__ NOINL bool od_full_inverse(Ctx& c, int K, double& dlog, double& dsign) {
   const int k = K / 2, ld = c.kcap;
   int* pos = c.bcode[1];
   od_positions(c, pos);
@@ -3687,8 +3701,23 @@ __device__ NOINL void global_od_tail(Ctx& c, int K, int new_outer, double factor
     I[(size_t)ic * ld + ia] = ia == ic ? 1.0 : 0.0;
   }
   __syncwarp();
-  double dlog = 0.0, dsign = 1.0;
-  const bool singular = !gj_eliminate(c, k, H, I, dlog, dsign);
+  dlog = 0.0;
+  dsign = 1.0;
+  return gj_eliminate(c, k, H, I, dlog, dsign);
+}
+
+// StepGlob with off-diagonal hybridisation (CTQMC.F90:4491-4494): the full
+// hybridisation matrix of the permuted operators in block order
+// (get_FullHybr_offdiag, Trace.F90:2690-2770), its inverse and determinant
+// (get_MatLogDetFull), DetRat = DetNew / Det; then the trace, the
+// Metropolis draw and the installation, or the old codes back.
+__device__ NOINL void global_od_tail(Ctx& c, int K, int new_outer, double factor, const int* opc_old) {
+  Hdr& h = *c.h;
+  cthyb_record& r = *c.rec;
+  const int k = K / 2, ld = c.kcap;
+  double dlog, dsign;
+  const bool singular = !od_full_inverse(c, K, dlog, dsign);
+  const double* I = c.dense + (size_t)ld * ld;
   // the new inverse kept in the o_glob space (the dense trace below reuses
   // the dense work space)
   double* Mn = glob_minv(c);
@@ -3788,6 +3817,18 @@ __device__ NOINL double shift_od_rotate(Ctx& c, const double* tau_old, const int
   return detrat;
 }
 
+// Drift control (no counterpart in the reference, which rebuilds M exactly
+// only in global moves and set_mc_config): after every `refresh_every`
+// accepted pair updates a chain rebuilds all its inverse matrices by
+// Gauss-Jordan elimination from the operator times, records the largest
+// deviation of the fast-updated matrices and log-determinant from the
+// rebuilt ones, and continues with the rebuilt ones.  The proposal stream is
+// unchanged: the rebuild draws no random numbers.
+__device__ __forceinline__ bool refresh_due(const Ctx& c) {
+  return c.g->refresh_every > 0 && c.h->status == ST_OK && c.h->acc_since_refresh >= c.g->refresh_every;
+}
+__device__ NOINL void ph_refresh(Ctx& c);
+
 // One proposal of the Z-space loop (CTQMC.F90:8435-8476 / 8212-8250) with
 // the phases back to back.
 __device__ void one_step(Ctx& c, Prop& p) {
@@ -3800,6 +3841,7 @@ __device__ void one_step(Ctx& c, Prop& p) {
     else if (p.move == 6) ph_rem4(c, p);
     else if (p.move == 7) ph_add_od(c, p);
     else ph_rem_od(c, p);
+    if (refresh_due(c)) ph_refresh(c);
     if (c.h->status == ST_OK) ph_finish(c, p);
     return;
   }
@@ -3820,6 +3862,7 @@ __device__ void one_step(Ctx& c, Prop& p) {
     if (p.move == 0) ph_accept_add(c, p);
     else ph_accept_rem(c, p);
   }
+  if (refresh_due(c)) ph_refresh(c);
   PROF_MARK(5);
   if (c.h->status == ST_OK) ph_finish(c, p);
   PROF_MARK(6);
@@ -3967,11 +4010,13 @@ __device__ NOINL void measure(Ctx& c) {
         const double* blg = chk_lg(bh);
         double* D = c.dm + m.dm_off[sst];
         const double sgn = h.trace_sign * (-h.cfgsign);
+        double* wcol = dwork(c, 3);  // per-column weight, one exponential each
+        for (int col = c.lane; col < cols; col += 32) wcol[col] = exp(klg[col] + blg[col] - h.trace_log);
+        __syncwarp();
         for (int e = c.lane; e < n * n; e += 32) {
           const int s1 = e % n, s2 = e / n;
           double acc = 0.0;
-          for (int col = 0; col < cols; ++col)
-            acc += bv[(size_t)col * ld + s1] * kv[(size_t)col * ld + s2] * exp(klg[col] + blg[col] - h.trace_log);
+          for (int col = 0; col < cols; ++col) acc += bv[(size_t)col * ld + s1] * kv[(size_t)col * ld + s2] * wcol[col];
           D[(size_t)s2 * n + s1] += acc * sgn;
         }
         __syncwarp();
@@ -4329,7 +4374,8 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
       }
     }
     SPROF(6);
-    if (__syncthreads_or(p.rare)) {
+    // rare moves and the periodic rebuilds of M share one optional phase
+    if (__syncthreads_or(p.rare || (mine && refresh_due(c)))) {
       if (p.rare) {
         if (p.move == 2) ph_global(c, p);
         else if (p.move == 3) ph_shift(c, p);
@@ -4338,6 +4384,7 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
         else if (p.move == 7) ph_add_od(c, p);
         else ph_rem_od(c, p);
       }
+      if (mine && refresh_due(c)) ph_refresh(c);
       __syncthreads();
     }
     if (mine && c.h->status == ST_OK) {
@@ -4460,6 +4507,46 @@ __device__ void rebuild_minv(Ctx& c, double* maxdev, bool replace, double& dlog,
     if (maxdev && c.lane == 0) *maxdev = fmax(*maxdev, dev);
     __syncwarp();
   }
+}
+
+// The periodic rebuild (see refresh_due): per-flavour inverse matrices, or
+// the full matrix in block order for off-diagonal groups.
+__device__ NOINL void ph_refresh(Ctx& c) {
+  Hdr& h = *c.h;
+  double dlog = 0.0, dsign = 1.0;
+  if (c.g->offdiag) {
+    const int K = h.K, k = K / 2, ld = c.kcap;
+    if (k > 0) {
+      if (od_full_inverse(c, K, dlog, dsign)) {
+        const double* I = c.dense + (size_t)ld * ld;
+        double* Mw = M_ptr(c, 0);
+        double dev = 0.0;
+        for (int e = c.lane; e < k * k; e += 32) {
+          const size_t idx = (size_t)(e / k) * ld + (e % k);
+          dev = fmax(dev, fabs(Mw[idx] - I[idx]));
+          Mw[idx] = I[idx];
+        }
+        dev = wmax(dev);
+        if (c.lane == 0) h.drift_m = fmax(h.drift_m, dev);
+      } else {
+        dlog = -DHUGE;
+        dsign = 0.0;
+      }
+    }
+  } else {
+    rebuild_minv(c, &h.drift_m, true, dlog, dsign);
+  }
+  if (c.lane == 0) {
+    h.acc_since_refresh = 0;
+    h.n_refresh++;
+    if (dsign != 0.0) {  // a singular rebuild keeps the fast-updated weights
+      h.drift_det = fmax(h.drift_det, fabs(dlog - h.det_log));
+      if (dsign != h.det_sign) h.refresh_sign_err++;
+      h.det_log = dlog;
+      h.det_sign = dsign;
+    }
+  }
+  __syncwarp();
 }
 
 // set_mc_config for chains chain0 .. chain0 + nset - 1 of a group, one warp
@@ -4587,6 +4674,24 @@ __global__ void __launch_bounds__(WPB * 32) k_refresh(const __grid_constant__ DM
     unsigned long long* p = (unsigned long long*)maxdev;
     unsigned long long v = __double_as_longlong(dev[warp]);
     atomicMax(p, v);  // non-negative doubles order like their bit patterns
+  }
+}
+
+// Drift statistics of every chain of a group into out (max |dM|, max
+// |d log det| as bit patterns, refreshes, sign errors); reset clears them.
+__global__ void k_drift(const __grid_constant__ DGroup g, unsigned long long* out, int reset) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.nchains) return;
+  Hdr* h = (Hdr*)(g.base + (size_t)c * g.stride + g.o_hdr);
+  atomicMax(&out[0], (unsigned long long)__double_as_longlong(h->drift_m));  // non-negative
+  atomicMax(&out[1], (unsigned long long)__double_as_longlong(h->drift_det));
+  atomicAdd(&out[2], (unsigned long long)h->n_refresh);
+  atomicAdd(&out[3], (unsigned long long)h->refresh_sign_err);
+  if (reset) {
+    h->drift_m = 0.0;
+    h->drift_det = 0.0;
+    h->n_refresh = 0;
+    h->refresh_sign_err = 0;
   }
 }
 
@@ -4868,6 +4973,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.p_shift = d.p_shift;
   g.p_4op = d.p_4op;
   g.dense = (d.flags & CTHYB_FLAG_DENSE) ? 1 : 0;
+  g.refresh_every = d.refresh_every == 0 ? CTHYB_REFRESH_DEFAULT : (d.refresh_every < 0 ? 0 : d.refresh_every);
   g.meas_dm = (d.flags & CTHYB_FLAG_NO_DM) ? 0 : 1;
   int kcap = d.kcap > 0 ? d.kcap : std::max(32, (int)std::min(4096.0, 32.0 * std::ceil(d.beta * 1.0 / 32.0 + 1.0)));
   kcap = (kcap + 3) / 4 * 4;
@@ -5906,6 +6012,36 @@ int cthyb_batch_refresh_minv(cthyb_batch_t B, int replace, double* maxdev) {
   return CTHYB_OK;
 }
 
+int cthyb_batch_drift(cthyb_batch_t B, double* max_dev_m, double* max_dev_logdet, int64_t* refreshes,
+                      int64_t* sign_errors, int reset) {
+  if (!B) return fail(CTHYB_ERR_ARG, "null");
+  unsigned long long* d = nullptr;
+  CK(cudaMallocAsync((void**)&d, 4 * sizeof(unsigned long long), B->stream));
+  cudaError_t e = cudaMemsetAsync(d, 0, 4 * sizeof(unsigned long long), B->stream);
+  for (GroupHost& G : B->groups) {
+    if (e != cudaSuccess) break;
+    k_drift<<<(G.desc.nchains + 127) / 128, 128, 0, B->stream>>>(G.g, d, reset);
+    e = cudaGetLastError();
+  }
+  unsigned long long hbuf[4] = {0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hbuf, d, sizeof(hbuf), cudaMemcpyDeviceToHost, B->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+  cudaFreeAsync(d, B->stream);
+  CK(e);
+  double v;
+  if (max_dev_m) {
+    std::memcpy(&v, &hbuf[0], 8);
+    *max_dev_m = v;
+  }
+  if (max_dev_logdet) {
+    std::memcpy(&v, &hbuf[1], 8);
+    *max_dev_logdet = v;
+  }
+  if (refreshes) *refreshes = (int64_t)hbuf[2];
+  if (sign_errors) *sign_errors = (int64_t)hbuf[3];
+  return CTHYB_OK;
+}
+
 int cthyb_batch_set_log(cthyb_batch_t B, int64_t cap) {
   if (!B || cap < 0) return fail(CTHYB_ERR_ARG, "bad arguments");
   // re-layout is only possible right after creation: the log area is the
@@ -6075,8 +6211,10 @@ int cthyb_batch_work_counters(cthyb_batch_t B, int64_t* out8, int reset) {
       out8[3] += h.w_nodes;
       out8[4] += h.try_add + h.try_rem;
       out8[5] += h.acc_add + h.acc_rem;
+      out8[6] += h.w_tflops;
+      out8[7] += h.w_tbytes;
       if (reset) {
-        h.w_mbytes = h.w_mflops = h.w_opbytes = h.w_nodes = 0;
+        h.w_mbytes = h.w_mflops = h.w_opbytes = h.w_nodes = h.w_tflops = h.w_tbytes = 0;
         CK(cudaMemcpy(p, &h, sizeof(Hdr), cudaMemcpyHostToDevice));
       }
     }
@@ -6102,8 +6240,10 @@ namespace cthyb {
 constexpr int NOALLOC_KMAX = 256;  // largest k accepted (2 * 256^2 doubles = 1 MiB)
 static __device__ __align__(256) double g_noalloc_scratch[2 * NOALLOC_KMAX * NOALLOC_KMAX];
 
-// One warp: H(a, c) = F(tau_a - tau_c) with the reference's interpolation
-// (get_HybrF, Trace.F90:1014-1033), Gauss-Jordan elimination with partial
+// One warp: H(a, c) = F(tau_a - tau_c) by the linear interpolation of
+// get_HybrF (Trace.F90:1014-1033; grid coordinate tau * ((Nftau - 1) / beta),
+// equal to the reference's tau / beta * (Nftau - 1) to within rounding),
+// Gauss-Jordan elimination with partial
 // pivoting on [H | 1] in the scratch array, M = H^{-1} written with rows =
 // creators and columns = annihilators, log|det H| and its sign.
 __global__ void k_minv_noalloc(double* scratch, int k, const double* __restrict__ tau_c,

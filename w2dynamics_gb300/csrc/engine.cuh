@@ -53,6 +53,15 @@ struct Hdr {
   int k[NFMAX];
   // work counters for the roofline: M bytes, M flops, op-array bytes, tree node updates
   long long w_mbytes, w_mflops, w_opbytes, w_nodes;
+  // dense-block trace work: FP64 flops of the block products and bytes of
+  // their operands (block, input and output matrices)
+  long long w_tflops, w_tbytes;
+  // drift control: largest |M_fast - M_rebuilt| and |log|det| fast - rebuilt|
+  // seen at the periodic full rebuilds, rebuilds done, determinant-sign
+  // disagreements, accepted pair updates since the last rebuild
+  double drift_m, drift_det;
+  long long n_refresh, refresh_sign_err;
+  int acc_since_refresh, pad_refresh;
   // cycles per proposal phase (only with -DCTHYB_PROFILE)
   long long prof[10];
 };
@@ -72,6 +81,7 @@ struct DGroup {
   const double* hybr_full;            // offdiag: [f1][f2][nftau]
   size_t o_gfull;                     // offdiag: G for every flavour pair [f_a][f_c][ntau]
   int kcap, opcap, L, dense, meas_dm;
+  int refresh_every;   // accepted pair updates between full rebuilds of M (0: never)
   char* base;          // chain c at base + c*stride
   size_t stride;
   size_t o_hdr, o_mt, o_optau, o_opcode, o_srt_tau, o_srt_slot, o_slot_tau, o_M, o_tree, o_act, o_bstart,

@@ -32,7 +32,7 @@ EXPORTS = (
     "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_move_counters4", "cthyb_batch_results_full", "cthyb_batch_minv_full", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_set_configs", "cthyb_batch_get_configs", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
-    "cthyb_minv_rebuild_noalloc",
+    "cthyb_batch_drift", "cthyb_minv_rebuild_noalloc",
 )
 
 
@@ -45,7 +45,7 @@ class GroupDesc(C.Structure):
                 ("flags", C.c_int32), ("p_global", C.c_double), ("p_shift", C.c_double),
                 ("nleg", C.c_int32), ("nscore", C.c_int32), ("score_dE", C.POINTER(C.c_double)),
                 ("nsym", C.c_int32), ("symmoves", C.POINTER(C.c_int32)), ("p_4op", C.c_double),
-                ("ftau_full", C.POINTER(C.c_double))]
+                ("ftau_full", C.POINTER(C.c_double)), ("refresh_every", C.c_int32)]
 
 
 class EngineError(RuntimeError):
@@ -110,6 +110,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_set_log.argtypes = [vp, i64]
     L.cthyb_batch_get_log.argtypes = [vp, C.c_int, C.c_void_p, C.POINTER(i64)]
     L.cthyb_batch_work_counters.argtypes = [vp, C.POINTER(i64), C.c_int]
+    L.cthyb_batch_drift.argtypes = [vp, dp, dp, C.POINTER(i64), C.POINTER(i64), C.c_int]
     L.cthyb_minv_rebuild_noalloc.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_double, vp, vp, vp]
     _lib = L
     return L
@@ -182,7 +183,7 @@ class Group:
     def __init__(self, beta, ftau, ntau, nchains=1, seed0=0, seeds=None, taudiff_max=-1.0,
                  ncorr=100, p_outer=0.0, kcap=0, opcap=0, tree_levels=0, maxhisto=500,
                  dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0, score_dE=None,
-                 symmoves=None, p_4op=0.0, ftau_full=None):
+                 symmoves=None, p_4op=0.0, ftau_full=None, refresh_every=0):
         self.beta = float(beta)
         self.ftau = np.asfortranarray(np.asarray(ftau, np.float64))
         self.ntau = int(ntau)
@@ -204,6 +205,9 @@ class Group:
         self.kcap, self.opcap, self.tree_levels = int(kcap), int(opcap), int(tree_levels)
         self.maxhisto = int(maxhisto)
         self.flags = (FLAG_DENSE if dense else 0) | (0 if measure_dm else FLAG_NO_DM)
+        # accepted pair updates between full rebuilds of the inverse matrices
+        # (0: the library default, negative: never)
+        self.refresh_every = int(refresh_every)
 
     def desc(self):
         d = GroupDesc()
@@ -231,6 +235,7 @@ class Group:
         d.nleg = self.nleg
         d.nscore = 0 if self.score_dE is None else self.score_dE.shape[0]
         d.score_dE = _dp(self.score_dE) if self.score_dE is not None else None
+        d.refresh_every = self.refresh_every
         d.nsym = 0 if self.symmoves is None else self.symmoves.shape[0]
         d.symmoves = self.symmoves.ctypes.data_as(C.POINTER(C.c_int32)) if self.symmoves is not None else None
         return d
@@ -464,6 +469,17 @@ class Batch:
         _check(load().cthyb_batch_refresh_minv(self.h, 1 if replace else 0, _dp(d)))
         return float(d[0])
 
+    def drift(self, reset=False):
+        """Drift of the fast updates at the periodic rebuilds of M, over all
+        chains: max |M_fast - M_rebuilt|, max |log|det| fast - rebuilt|,
+        number of rebuilds and of determinant-sign disagreements."""
+        dm, dd = np.zeros(1), np.zeros(1)
+        n, se = np.zeros(1, np.int64), np.zeros(1, np.int64)
+        _check(load().cthyb_batch_drift(self.h, _dp(dm), _dp(dd), n.ctypes.data_as(C.POINTER(C.c_int64)),
+                                        se.ctypes.data_as(C.POINTER(C.c_int64)), 1 if reset else 0))
+        return dict(max_dev_m=float(dm[0]), max_dev_logdet=float(dd[0]), refreshes=int(n[0]),
+                    sign_errors=int(se[0]))
+
     def set_log(self, cap):
         _check(load().cthyb_batch_set_log(self.h, int(cap)))
         self._logcap = int(cap)
@@ -482,7 +498,7 @@ class Batch:
         _check(load().cthyb_batch_work_counters(self.h, out.ctypes.data_as(C.POINTER(C.c_int64)),
                                                 1 if reset else 0))
         return dict(zip(("m_bytes", "m_flops", "op_bytes", "tree_nodes", "proposals",
-                         "accepted", "r6", "r7"), out.tolist()))
+                         "accepted", "trace_flops", "trace_bytes"), out.tolist()))
 
     def close(self):
         if getattr(self, "h", None):
