@@ -4,20 +4,31 @@ Workload (the batched configuration): 4096 independent chains of the
 3-orbital density-density model (U=4, J=0.6, U'=U-2J, mu=3.3 for filling
 2/6, QuantumNumbers "Nt Szt"), 1024 chains at each beta in {10,25,50,100},
 semicircular bath (D=1) with F(tau) on Ntau=Nftau=2000 points, seed = chain
-index, TaudiffMax=5, NCorr=100.  One step = one measurement cycle of every
-chain: NCorr pair proposals (StepAdd/StepRem, CTQMC.F90:8428-8476) and the
-Z-space measurements (sign, order histogram, density matrix at beta/2,
-G(tau)).  1 MC update = 1 proposed pair insertion or removal.
+index, TaudiffMax=5, NCorr=100, and the reference's default move mix
+(PercentageGlobalMove = PercentageTauShiftMove = 0.005, configspec:81-82),
+which makes every chain ergodic over the superstate sectors.  One step = one
+measurement cycle of every chain: NCorr proposals (StepAdd/StepRem and the
+rare global / tau-shift moves, CTQMC.F90:8428-8476) and the Z-space
+measurements (sign, order histogram, density matrix at beta/2, G(tau)).
+1 MC update = 1 proposal.
+
+Footing: every chain is thermalised for THERMALIZE proposals (the GPU run
+reports the mean expansion order of each beta group after every round of
+THERM_ROUND proposals, so the plateau is visible), then the schedule
+autotuner runs (its proposals are further warm-up), then W warm-up steps;
+the timed window is the next K steps.  The CPU arms run their chains
+through exactly the same proposal window and report their mean orders too.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 --impl reference times the oracle (the C++ restatement of the reference's
-Fortran loop, which cannot be built here) on the host cores, one chain per
-process, on a bounded sample of the same workload.
+Fortran loop, which cannot be built here) on all host cores.
 """
 import argparse
+import hashlib
 import json
 import os
+import re
 import subprocess
 import sys
 import threading
@@ -33,36 +44,34 @@ CHAINS_PER_BETA = 1024  # 4096 chains, 1024 at each beta
 NTAU = 2000
 NCORR = 100
 TDM = 5.0
-THERMALIZE = 2000  # proposals per chain before timing (not timed)
-E2E_WARMUP = 1000  # re-thermalisation proposals per chain of the warm-started end-to-end solve
-TUNE = 200         # of them, per candidate schedule of the autotuner (10 candidates)
-CPU_SAMPLE_MEAS = 100  # measurement cycles per host core and round of the bounded CPU sample
-# dense-block workload (--workload kanamori5): 5-orbital Kanamori with
-# spin-flip and pair hopping, 1024 chains, one window (TaudiffMax <= 0)
-K5_BETA, K5_CHAINS, K5_THERM = 40.0, 1024, 2000
+MOVES = dict(p_global=0.005, p_shift=0.005)  # the reference's default move mix
+THERM_ROUND = 2000   # proposals per chain between order read-outs
+THERMALIZE = 20000   # thermalisation proposals per chain (10 rounds)
+TUNE = 200           # autotuner proposals per candidate (10 candidates, 2 interleaved passes)
+E2E_WARMUP = 1000    # re-thermalisation proposals of the warm-started end-to-end solve
+CPU_CHAINS_PER_CORE = 16  # chains per host core in the bounded CPU sample (beta cycling)
+ONE_CHAIN_BLOCKS, ONE_CHAIN_MEAS = 16, 30  # one-chain form: blocks x measurement cycles per beta
+# dense-block workload: 5-orbital Kanamori with spin-flip and pair hopping
+K5_BETA, K5_CHAINS, K5_THERM, K5_STEPS = 40.0, 1024, 2000, 2
 METRIC = "MC updates/sec on 1 GB300, batched vs one-chain form, at equal G(tau) error"
-# From one ncu capture (--set full) of a one-cycle sweep launch of this
-# workload: DRAM bytes read + written, FP64-pipe and issue utilisation.
-TRAFFIC_PER_STEP = 373.3e6
-NCU_FP64_PIPE = 0.372
-NCU_ISSUE_ACTIVE = 0.229
+PROFILE = os.path.join(ROOT, "profiles", "k_sweep_sync_bench_4096chains.md")
 
 
 def workload_desc(chains_per_beta):
     return {"workload": f"{len(BETAS) * chains_per_beta} chains, 3-orbital density-density "
                         f"U=4 J=0.6 mu=3.3 (Nt Szt), beta in {list(BETAS)}, "
-                        f"Ntau=Nftau={NTAU}, TaudiffMax={TDM}, NCorr={NCORR}",
+                        f"Ntau=Nftau={NTAU}, TaudiffMax={TDM}, NCorr={NCORR}, "
+                        f"PercentageGlobalMove={MOVES['p_global']}, "
+                        f"PercentageTauShiftMove={MOVES['p_shift']}",
             "chains": len(BETAS) * chains_per_beta, "betas": list(BETAS), "ncorr": NCORR,
             "step": "NCorr proposals per chain + measurement",
+            "window": f"proposals {THERMALIZE + 10 * TUNE} + W*{NCORR} ... + K*{NCORR} of every chain",
             "l2_flush": "inputs (chain state, ~GBs) larger than L2"}
 
 
 def problems():
     from w2dynamics_gb300 import problems as P
-    out = []
-    for b in BETAS:
-        out.append(P.config_problem("dd3", beta=b))
-    return out
+    return [P.config_problem("dd3", beta=b) for b in BETAS]
 
 
 class ClockSampler:
@@ -122,16 +131,63 @@ class ClockSampler:
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(sm)}
 
 
-def measured_peaks():
+def hbm_peak():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
         with open(p) as f:
             d = json.load(f)
-        return float(d.get("hbm_gbs", 6800.0)), "measured"
+        return float(d.get("hbm_gbs", 6800.0)), "measured (MEASURED_PEAKS.json hbm_gbs)"
     return 6800.0, "fallback"
 
 
-def build_batch(E, probs, cpb, rank=0):
+def engine_sha():
+    h = hashlib.sha256()
+    for name in ("engine.cu", "engine.cuh", "model.cpp", "model.h"):
+        with open(os.path.join(ROOT, "w2dynamics_gb300", "csrc", name), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def profile_keys():
+    """The machine-readable line of the committed ncu summary of the sweep
+    kernel (`bench-keys: {...}`), and whether it was taken on this build."""
+    try:
+        with open(PROFILE) as f:
+            for line in f:
+                m = re.match(r"bench-keys:\s*(\{.*\})\s*$", line.strip())
+                if m:
+                    d = json.loads(m.group(1))
+                    d["profile"] = os.path.relpath(PROFILE, ROOT)
+                    d["same_build"] = d.get("engine_sha") == engine_sha()
+                    return d
+    except OSError:
+        pass
+    return None
+
+
+def mean_orders(batch, ngroups):
+    return [float(batch.chain_stats(g)["noper"].mean()) for g in range(ngroups)]
+
+
+def thermalise(batch, ngroups, total, rnd=THERM_ROUND):
+    """`total` proposals per chain in rounds of `rnd`; the mean operator
+    count of each group after every round."""
+    hist = []
+    for _ in range(max(1, total // rnd)):
+        batch.warmup(rnd)
+        batch.sync()
+        hist.append([round(x, 2) for x in mean_orders(batch, ngroups)])
+    return hist
+
+
+def sigma2_of_mean(per_chain_g):
+    """Mean over (flavour, tau) of the variance of the chain-averaged G:
+    per-chain estimates are independent, so var = var_c / n_chains."""
+    g = np.asarray(per_chain_g).reshape(len(per_chain_g), -1)
+    return float(np.mean(g.var(axis=0, ddof=1) / len(g)))
+
+
+def build_batch(E, probs, cpb, rank=0, moves=MOVES):
     """Model and `cpb` chains per beta for one GPU, from host arrays; seed =
     chain index of the whole job (rank r holds chains r*4*cpb ...)."""
     pr0 = probs[0]
@@ -141,24 +197,56 @@ def build_batch(E, probs, cpb, rank=0):
         groups.append(E.Group(pr["beta"], pr["ftau"], pr["ntau"], nchains=cpb,
                               seed0=(rank * len(probs) + i) * cpb, taudiff_max=TDM, ncorr=NCORR,
                               kcap=32 if pr["beta"] <= 25 else 64,
-                              opcap=256 if pr["beta"] <= 25 else (512 if pr["beta"] <= 50 else 1024)))
+                              opcap=256 if pr["beta"] <= 25 else (512 if pr["beta"] <= 50 else 1024),
+                              **moves))
     h2d = sum(g.ftau.nbytes for g in groups) + pr0["umatrix"].nbytes + pr0["muimp"].nbytes
     return model, groups, E.Batch(model, groups), h2d
 
 
+def one_chain_forms(E, model, probs):
+    """The plain drop-in form (one chain, as one Fortran process runs it) at
+    each beta: thermalised like the batch, then ONE_CHAIN_BLOCKS blocks of
+    ONE_CHAIN_MEAS measurement cycles; device time (CUDA events on the
+    batch's stream) of the measured blocks and the variance of its G(tau)
+    mean from the spread of the block averages."""
+    import torch
+    out = []
+    for pr in probs:
+        b = E.Batch(model, [E.Group(pr["beta"], pr["ftau"], NTAU, nchains=1, seed0=0, taudiff_max=TDM,
+                                    ncorr=NCORR, kcap=64, opcap=1024, **MOVES)])
+        b.warmup(THERMALIZE + 10 * TUNE)
+        b.sync()
+        stream = torch.cuda.ExternalStream(b.stream())
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ms, blocks, k0 = 0.0, [], b.state(0)["noper"]
+        for _ in range(ONE_CHAIN_BLOCKS):
+            b.reset_measurements()
+            ev0.record(stream)
+            b.measure(ONE_CHAIN_MEAS)
+            ev1.record(stream)
+            ev1.synchronize()
+            ms += ev0.elapsed_time(ev1)
+            blocks.append(b.group_gtau(0)[0])
+        props = ONE_CHAIN_BLOCKS * ONE_CHAIN_MEAS * NCORR
+        out.append({"beta": pr["beta"], "value": props / (ms / 1e3), "device_s": ms / 1e3,
+                    "proposals": props, "sigma2_G": sigma2_of_mean(blocks),
+                    "mean_order": [k0, b.state(0)["noper"]]})
+        b.close()
+    return out
+
+
 def measure_backward(E, model, pr, args):
-    """The differentiation configuration: 2048 chains of the same model at
-    beta = 50; one forward step (NCorr proposals + measurement) against one
-    backward pass (d log|w| of every chain w.r.t. the F(tau) grid and the
-    2Nd + 2 parameters eps_f, U, J), both device-timed with CUDA events on the
-    batch's stream."""
+    """The differentiation configuration: 2048 thermalised chains of the same
+    model at beta = 50; one forward step (NCorr proposals + measurement)
+    against one backward pass (d log|w| of every chain w.r.t. the F(tau)
+    grid and the 2Nd + 2 parameters eps_f, U, J), both device-timed with CUDA
+    events on the batch's stream."""
     import torch
     from w2dynamics_gb300 import gradients as GR
     n = 2048
     b = E.Batch(model, [E.Group(pr["beta"], pr["ftau"], pr["ntau"], nchains=n, seed0=0, taudiff_max=TDM,
-                                ncorr=NCORR, kcap=64, opcap=512)])
-    b.autotune(TUNE)
-    b.warmup(THERMALIZE - 10 * TUNE)
+                                ncorr=NCORR, kcap=64, opcap=512, **MOVES)])
+    b.warmup(THERMALIZE)
     b.sync()
     dev = torch.device("cuda")
     dE = torch.tensor(GR.density_density_directions(model.nd, model.fock_states), dtype=torch.float64, device=dev)
@@ -190,52 +278,49 @@ def measure_backward(E, model, pr, args):
             "forward_step_ms": fwd, "backward_ms": bwd, "backward_over_forward": bwd / fwd}
 
 
-def run_gpu_k5(args):
+def run_k5(E, args, fp64_peak):
     """Dense-block workload: 1024 chains of the 5-orbital Kanamori model
-    (U=3, J=0.7, crystal field, beta=40, 1024 states in 36 (N,Sz) blocks up
-    to 100x100), Ntau = Nftau = 4000, NCorr = 100, seed = chain index.  The
-    chains are thermalised for K5_THERM proposals only (orders still
-    growing); the CPU sample runs the oracle on the same footing."""
+    (U=3, J=0.7, crystal field +-0.2, beta=40, 1024 states in 36 (N,Sz)
+    blocks up to 100x100), Ntau = Nftau = 4000, one window, NCorr = 100,
+    seed = chain index, K5_THERM thermalisation proposals; K5_STEPS timed
+    steps.  Roofline: FP64 flops of the trace's block products (counted at
+    run time from the recomputed products) against the live DFMA peak."""
     import torch
-    from w2dynamics_gb300 import engine as E
     from w2dynamics_gb300 import problems as P
     pr = P.config_problem("kanamori5", beta=K5_BETA)
     model = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
     b = E.Batch(model, [E.Group(K5_BETA, pr["ftau"], pr["ntau"], nchains=K5_CHAINS, seed0=0, taudiff_max=-1.0,
                                 ncorr=NCORR, kcap=64, opcap=1024, tree_levels=4)])
     b.warmup(K5_THERM)
+    b.measure(1)
     b.sync()
+    st = b.chain_stats(0)
+    outer = np.array([b.state(c)["outer_sst"] for c in range(K5_CHAINS)], int)
+    sizes = model.sst_size[outer]
+    b.work_counters(reset=True)
     stream = torch.cuda.ExternalStream(b.stream())
     start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(args.warmup):
-        b.measure(1)
-    b.sync()
-    with ClockSampler() as clocks:
-        start.record(stream)
-        for _ in range(args.steps):
-            b.measure(1)
-        stop.record(stream)
-        stop.synchronize()
+    start.record(stream)
+    b.measure(K5_STEPS)
+    stop.record(stream)
+    stop.synchronize()
     ms = start.elapsed_time(stop)
-    value = K5_CHAINS * NCORR * args.steps / (ms / 1e3)
-    korder = float(np.mean([b.state(c)["noper"] for c in range(0, K5_CHAINS, 64)]))
+    wc = b.work_counters()
+    k_end = float(b.chain_stats(0)["noper"].mean())
     b.close()
-    cores = os.cpu_count() or 1
-    cpu_value, cpu_wall = oracle_rate(cores, 2, 2, 0, workload="kanamori5")
-    line = {
-        "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (semicircular bath D=2, seeded chains)",
-        "config": {"workload": f"{K5_CHAINS} chains, 5-orbital Kanamori U=3 J=0.7 crystal field +-0.2, "
-                               f"beta={K5_BETA}, Ntau=Nftau=4000, Nt Szt blocks, NCorr={NCORR}, "
-                               f"{K5_THERM} thermalisation proposals",
-                   "mean_operators_per_chain": korder},
-        "cpu_baseline": {"value": cpu_value, "unit": "MC updates/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} chains (one per host core), {K5_THERM} thermalisation "
-                                   f"proposals, 2 rounds of 2 x {NCORR} proposals ({cpu_wall:.1f} s)"},
-        "gpu_launches": args.steps, "clocks": clocks.summary(),
-    }
-    print(json.dumps(line))
+    value = K5_CHAINS * NCORR * K5_STEPS / (ms / 1e3)
+    achieved = wc["trace_flops"] / (ms / 1e3) / 1e9
+    return {"workload": f"{K5_CHAINS} chains, 5-orbital Kanamori U=3 J=0.7 crystal field +-0.2, beta={K5_BETA}, "
+                        f"Ntau=Nftau=4000, Nt Szt blocks (largest 100), one window, NCorr={NCORR}, "
+                        f"{K5_THERM} thermalisation proposals (orders still growing), {K5_STEPS} timed steps",
+            "value": value, "unit": "MC updates/s", "ms_per_step": ms / K5_STEPS,
+            "mean_order": [float(st["noper"].mean()), k_end],
+            "outer_superstate_sizes": {int(k): int(v) for k, v in zip(*np.unique(sizes, return_counts=True))},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "GFLOP/s",
+                         "frac": achieved / fp64_peak,
+                         "note": "FP64 flops of the dense block products of the trace, counted at run time, "
+                                 "over the device time; peak = live DFMA probe (cthyb_probe_fp64)",
+                         "trace_flops_per_proposal": wc["trace_flops"] / max(1, wc["proposals"])}}
 
 
 def run_gpu(args, rank=0, world=1):
@@ -245,15 +330,18 @@ def run_gpu(args, rank=0, world=1):
 
     cpb = args.chains_per_beta
     probs = problems()
+    ng = len(probs)
     model, groups, batch, _ = build_batch(E, probs, cpb, rank)
-    sched = batch.autotune(TUNE)  # thermalisation doubles as schedule tuning
-    batch.warmup(THERMALIZE - 10 * TUNE)
-    batch.sync()
+    therm = thermalise(batch, ng, THERMALIZE)
+    sched = batch.autotune(TUNE)  # after thermalisation; its proposals are more warm-up
     stream = torch.cuda.ExternalStream(batch.stream())
     for _ in range(args.warmup):
         batch.measure(1)
     batch.sync()
+    batch.reset_measurements()
     batch.work_counters(reset=True)
+    batch.drift(reset=True)
+    order_start = mean_orders(batch, ng)
     start = torch.cuda.Event(enable_timing=True)
     stop = torch.cuda.Event(enable_timing=True)
     nchains = world * len(BETAS) * cpb  # the whole job (weak scaling: fixed chains per GPU)
@@ -273,7 +361,10 @@ def run_gpu(args, rank=0, world=1):
     ms = shard.max_over_ranks(start.elapsed_time(stop))
     props = nchains * NCORR * args.steps
     value = props / (ms / 1e3)
+    order_end = mean_orders(batch, ng)
     wc = batch.work_counters(reset=False)
+    drift = batch.drift()
+    sig2_b = [sigma2_of_mean(batch.group_gtau(g)) for g in range(ng)]
     # the thermalised configurations: what one DMFT iteration hands the next
     # through mc_config_inout (cthyb_solver.py:329-345)
     cfg = batch.get_configs()
@@ -292,7 +383,8 @@ def run_gpu(args, rank=0, world=1):
     model2, groups2, b2, h2d = build_batch(E, probs, cpb, rank)
     b2.set_configs(*cfg)
     h2d += sum(a.nbytes for a in cfg)
-    b2.warmup(E2E_WARMUP)  # automatic schedule (the autotuner's choice above on this workload)
+    b2.set_schedule(sched)
+    b2.warmup(E2E_WARMUP)
     b2.use_graphs(True)
     d2h = 0
     for _ in range(args.steps):
@@ -308,24 +400,25 @@ def run_gpu(args, rank=0, world=1):
     e2e_value = nchains * (E2E_WARMUP + NCORR * args.steps) / t_e2e
     if rank != 0:
         return
-    # plain one-chain drop-in form on the same model (beta=50 problem)
-    single = E.Batch(model, [E.Group(probs[2]["beta"], probs[2]["ftau"], NTAU, nchains=1, seed0=0,
-                                     taudiff_max=TDM, ncorr=NCORR, kcap=64, opcap=512)])
-    single.warmup(THERMALIZE)
-    single.sync()
-    s_steps = max(3, args.steps)
-    s0 = time.perf_counter()
-    for _ in range(s_steps):
-        single.measure(1)
-    single.sync()
-    s_time = time.perf_counter() - s0
-    single_value = s_steps * NCORR / s_time
+    # plain one-chain drop-in form at each beta, and the equal-error ratio:
+    # the one-chain form needs t1 * sigma2_1 / sigma2_b to reach the batch's
+    # G(tau) error at that beta; the batch reaches all four in its K steps
+    ones = one_chain_forms(E, model, probs)
+    t_batch = ms / 1e3
+    t_equal = [o["device_s"] * o["sigma2_G"] / s2 for o, s2 in zip(ones, sig2_b)]
+    one_rate = float(np.mean([o["value"] for o in ones]))
     backward = measure_backward(E, model, probs[2], args)
+    fp64_dfma, fp64_dmma = E.probe_fp64()
+    k5 = run_k5(E, args, fp64_dfma) if not args.skip_k5 else None
     cores = os.cpu_count() or 1
-    cpu_value, cpu_wall = oracle_rate(cores, CPU_SAMPLE_MEAS, 3, 1)
-    hbm, peak_kind = measured_peaks()
+    cpu = oracle_rate(cores, args.steps, args.warmup)
+    if k5 is not None:
+        k5["cpu_baseline"] = oracle_rate_k5(cores)
+    hbm, hbm_kind = hbm_peak()
     bytes_per_step = (wc["m_bytes"] + wc["op_bytes"]) / max(1, args.steps)
     achieved = bytes_per_step / (ms / 1e3 / args.steps) / 1e9
+    fp64_achieved = wc["m_flops"] / (ms / 1e3) / 1e9
+    prof = profile_keys()
     line = {
         "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -340,27 +433,43 @@ def run_gpu(args, rank=0, world=1):
                          f"per chain, {args.steps} steps each with G(tau) sums read back, "
                          f"configurations read back; bytes per step = per-call bytes / steps",
                 "wall_s": t_e2e},
-        "one_chain_form": {"value": single_value, "unit": "MC updates/s",
-                           "batched_over_one_chain": value / single_value},
+        "footing": {"thermalisation_proposals": THERMALIZE, "autotune_proposals": 10 * TUNE,
+                    "mean_order_per_round": therm, "mean_order_start": order_start,
+                    "mean_order_end": order_end},
+        "equal_error": {
+            "sigma2_G_batched": sig2_b,
+            "one_chain": ones,
+            "one_chain_seconds_to_batched_error": t_equal,
+            "batched_seconds": t_batch,
+            "batched_over_one_chain_at_equal_error": float(sum(t_equal) / t_batch),
+            "note": "sigma2_G = mean over (flavour, tau bin) of the variance of the G(tau) mean: batched from "
+                    "the spread of the per-chain estimates (1024 independent chains per beta), one-chain from "
+                    "the spread of block averages; the one-chain form needs t1*sigma2_1/sigma2_b to reach "
+                    "the batched error at each beta, the batch reaches all four betas in batched_seconds"},
+        "one_chain_form": {"value": one_rate, "unit": "MC updates/s",
+                           "batched_over_one_chain": value / one_rate},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": TRAFFIC_PER_STEP, "peak_kind": peak_kind,
-                     "note": "per step (one measurement cycle, NCorr proposals a chain): "
-                             "algorithmic bytes of M and operator arrays; traffic = ncu DRAM "
-                             "bytes of a one-cycle launch; the kernel is bound by barrier "
-                             "waits, load latency and the FP64 pipe, not HBM",
-                     "ncu": {"fp64_pipe_busy": NCU_FP64_PIPE, "issue_active": NCU_ISSUE_ACTIVE}},
-        "cpu_baseline": {"value": cpu_value, "unit": "MC updates/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} chains (one per host core, beta cycling over {list(BETAS)}), "
-                                   f"{THERMALIZE} thermalisation proposals, then 3 rounds of "
-                                   f"{CPU_SAMPLE_MEAS} measurement cycles x {NCORR} proposals per chain "
-                                   f"({cpu_wall:.1f} s wall)"},
+                     "frac": achieved / hbm,
+                     "traffic": (prof or {}).get("dram_bytes_per_step"), "peak_kind": hbm_kind,
+                     "note": "per step (one measurement cycle, NCorr proposals a chain): algorithmic bytes of "
+                             "M and operator arrays over the device time; traffic = ncu DRAM bytes of one "
+                             "cycle from the committed profile (see ncu.same_build)",
+                     "fp64": {"achieved": fp64_achieved, "peak": fp64_dfma, "unit": "GFLOP/s",
+                              "frac": fp64_achieved / fp64_dfma,
+                              "peak_kind": "live DFMA probe (cthyb_probe_fp64)", "dmma_peak": fp64_dmma,
+                              "note": "algorithmic determinant flops (ratios and updates) only"},
+                     "ncu": prof},
+        "cpu_baseline": cpu,
         "backward": backward,
+        "drift": dict(drift, refresh_every=1000),
+        "dense_block": k5,
         "work": wc,
-        "schedule": {"warps_per_block": sched, "chosen_by": "autotuner (cthyb_batch_autotune)",
+        "schedule": {"warps_per_block": sched, "chosen_by": "autotuner (cthyb_batch_autotune) after thermalisation",
                      "cuda_graphs": "end-to-end solve (one launch per step); the device-timed "
                                     "steps run as one measure(K) call"},
         "gpu_launches": (args.steps + 199) // 200,
         "clocks": clocks.summary(),
+        "engine_sha": engine_sha(),
     }
     print(json.dumps(line))
 
@@ -368,79 +477,124 @@ def run_gpu(args, rank=0, world=1):
 _WORKER = {}
 
 
-def _worker_init(name, beta, seed, ftau, therm):
-    """One oracle chain per process, built and thermalised once."""
+def _worker_init(specs):
+    """The oracle chains of one host core (test infrastructure only)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     from w2dynamics_gb300 import problems as P
-    pr = P.config_problem(name, beta=beta)
-    m = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
-    tdm = TDM if name == "dd3" else -1.0
-    c = O.Chain(m, beta, ftau, 100, seed=seed, taudiff_max=tdm, ncorr=NCORR)
-    c.warmup(therm)
-    _WORKER["chain"], _WORKER["model"] = c, m
+    chains = []
+    models = {}
+    for name, beta, seed, ftau, tdm, moves, tree in specs:
+        if name not in models:
+            pr = P.config_problem(name, beta=beta)
+            models[name] = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+        chains.append((beta, O.Chain(models[name], beta, ftau, NTAU if name == "dd3" else 4000, seed=seed,
+                                     taudiff_max=tdm, ncorr=NCORR, **moves)))
+    _WORKER["chains"], _WORKER["models"] = chains, models
 
 
-def _worker_run(nmeas):
-    c = _WORKER["chain"]
+def _worker_warm(n):
+    for _, c in _WORKER["chains"]:
+        c.warmup(n)
+    return [(b, c.state()["noper"]) for b, c in _WORKER["chains"]]
+
+
+def _worker_run(nsteps):
+    """nsteps measurement cycles of every chain of this core, timed."""
     t0 = time.perf_counter()
-    c.measure(nmeas)
-    return time.perf_counter() - t0, nmeas * NCORR
+    for _, c in _WORKER["chains"]:
+        c.measure(nsteps)
+    t = time.perf_counter() - t0
+    return t, nsteps * NCORR * len(_WORKER["chains"]), [(b, c.state()["noper"]) for b, c in _WORKER["chains"]]
 
 
-def oracle_rate(cores, meas, rounds, warm_rounds, workload="batched"):
+def _per_beta(pairs):
+    out = {}
+    for b, k in pairs:
+        out.setdefault(b, []).append(k)
+    return [round(float(np.mean(out[b])), 2) for b in sorted(out)]
+
+
+def oracle_rate(cores, steps, warmup):
     """MC updates/s of the oracle (C++ restatement of the Fortran loop) on
-    `cores` host cores, one chain per core (beta cycling over the groups of
-    the batched workload), each round `meas` measurement cycles per chain;
-    median over rounds."""
+    `cores` host cores with CPU_CHAINS_PER_CORE chains each (beta cycling
+    over the groups, seeds = chain index), through the GPU run's proposal
+    window: THERMALIZE + 10 * TUNE + warmup * NCORR untimed proposals, then
+    `steps` timed measurement cycles per chain."""
     import multiprocessing as mp
     from w2dynamics_gb300 import problems as P
-    if workload == "kanamori5":
-        specs = [("kanamori5", K5_BETA, P.config_problem("kanamori5", beta=K5_BETA)["ftau"], K5_THERM)]
-    else:
-        specs = [("dd3", b, P.semicircle_ftau(3, b, 1.0, NTAU), THERMALIZE) for b in BETAS]
+    ftaus = {b: P.semicircle_ftau(3, b, 1.0, NTAU) for b in BETAS}
     ctx = mp.get_context("spawn")
     pools = []
     for i in range(cores):
-        name, b, ft, th = specs[i % len(specs)]
-        pools.append(ctx.Pool(1, initializer=_worker_init, initargs=(name, b, i, ft, th)))
+        specs = []
+        for j in range(CPU_CHAINS_PER_CORE):
+            b = BETAS[(i * CPU_CHAINS_PER_CORE + j) % len(BETAS)]
+            specs.append(("dd3", b, i * CPU_CHAINS_PER_CORE + j, ftaus[b], TDM, MOVES, 0))
+        pools.append(ctx.Pool(1, initializer=_worker_init, initargs=(specs,)))
     try:
-        for _ in range(warm_rounds):
-            for r in [p.apply_async(_worker_run, (max(1, meas // 4),)) for p in pools]:
-                r.get()
-        vals = []
+        warm = THERMALIZE + 10 * TUNE + warmup * NCORR
+        k0 = sum((r.get() for r in [p.apply_async(_worker_warm, (warm,)) for p in pools]), [])
         t0 = time.perf_counter()
-        for _ in range(rounds):
-            res = [r.get() for r in [p.apply_async(_worker_run, (meas,)) for p in pools]]
-            vals.append(sum(n for _, n in res) / max(t for t, _ in res))
+        res = [r.get() for r in [p.apply_async(_worker_run, (steps,)) for p in pools]]
         wall = time.perf_counter() - t0
     finally:
         for p in pools:
             p.terminate()
-    return float(np.median(vals)), wall
+    tmax = max(t for t, _, _ in res)
+    nprop = sum(n for _, n, _ in res)
+    k1 = sum((k for _, _, k in res), [])
+    return {"value": nprop / tmax, "unit": "MC updates/s", "cores": cores, "kind": "port",
+            "sample": f"{cores * CPU_CHAINS_PER_CORE} chains ({CPU_CHAINS_PER_CORE} per host core, beta cycling "
+                      f"over {list(BETAS)}), {warm} untimed proposals each (the GPU run's thermalisation, "
+                      f"autotuning and warm-up), then {steps} timed measurement cycles of {NCORR} proposals "
+                      f"each ({tmax:.2f} s per core, {wall:.2f} s wall)",
+            "mean_order_start": _per_beta(k0), "mean_order_end": _per_beta(k1)}
+
+
+def oracle_rate_k5(cores):
+    """The oracle on the dense-block workload through the GPU run's window:
+    one chain per host core (seeds 0..cores-1), K5_THERM + NCORR untimed
+    proposals, then K5_STEPS timed measurement cycles."""
+    import multiprocessing as mp
+    from w2dynamics_gb300 import problems as P
+    pr = P.config_problem("kanamori5", beta=K5_BETA)
+    ctx = mp.get_context("spawn")
+    pools = [ctx.Pool(1, initializer=_worker_init,
+                      initargs=([("kanamori5", K5_BETA, i, pr["ftau"], -1.0, {}, 0)],)) for i in range(cores)]
+    try:
+        for r in [p.apply_async(_worker_warm, (K5_THERM + NCORR,)) for p in pools]:
+            r.get()
+        res = [r.get() for r in [p.apply_async(_worker_run, (K5_STEPS,)) for p in pools]]
+    finally:
+        for p in pools:
+            p.terminate()
+    tmax = max(t for t, _, _ in res)
+    return {"value": sum(n for _, n, _ in res) / tmax, "unit": "MC updates/s", "cores": cores, "kind": "port",
+            "sample": f"{cores} chains (one per host core), {K5_THERM + NCORR} untimed proposals, then "
+                      f"{K5_STEPS} timed measurement cycles ({tmax:.2f} s)"}
 
 
 def run_reference(args):
-    """Oracle (C++ restatement of the Fortran loop) on all host cores, one
-    chain per core; each step runs `ref_meas` measurement cycles per chain."""
+    """Oracle (C++ restatement of the Fortran loop) on all host cores through
+    the GPU run's proposal window (see oracle_rate)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    value, wall = oracle_rate(cores, args.ref_meas if args.workload == "batched" else 2, args.steps,
-                              args.warmup, workload=args.workload)
+    t0 = time.perf_counter()
+    cpu = oracle_rate(cores, args.steps, args.warmup)
     line = {
-        "metric": METRIC, "value": value, "unit": "MC updates/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3,
+        "metric": METRIC, "value": cpu["value"], "unit": "MC updates/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * CPU_CHAINS_PER_CORE * cores * NCORR / cpu["value"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (semicircular bath, seeded chains)",
         "config": workload_desc(args.chains_per_beta), "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": "MC updates/s", "cores": cores, "kind": "port",
-                         "sample": f"{cores} chains (one per core, beta cycling over {list(BETAS)}), "
-                                   f"{args.ref_meas} measurement cycles of {NCORR} proposals per chain "
-                                   f"and step after {THERMALIZE} thermalisation proposals"},
-        "e2e": {"value": value, "unit": "MC updates/s", "h2d_bytes_per_step": 0,
+        "cpu_baseline": cpu,
+        "e2e": {"value": cpu["value"], "unit": "MC updates/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t0,
     }
     print(json.dumps(line))
 
@@ -452,16 +606,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--chains-per-beta", type=int, default=CHAINS_PER_BETA)
-    ap.add_argument("--workload", default="batched", choices=("batched", "kanamori5"),
-                    help="batched: the 4096-chain benchmark; kanamori5: dense-block 5-orbital model")
-    ap.add_argument("--ref-meas", type=int, default=100,
-                    help="measurement cycles per chain and step of the CPU reference arm")
+    ap.add_argument("--skip-k5", action="store_true", help="leave out the dense-block (5-orbital) line")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
-        return
-    if args.workload == "kanamori5":
-        run_gpu_k5(args)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

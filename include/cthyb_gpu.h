@@ -152,9 +152,11 @@ int cthyb_batch_use_graphs(cthyb_batch_t batch, int on);
  * phase together.  Per-chain results do not depend on the schedule. */
 int cthyb_batch_set_schedule(cthyb_batch_t batch, int warps_per_block);
 /* Time `nprop` warmup proposals per chain under each schedule (independent
- * warps; phase-synchronous blocks of 4..32 chains) and keep the fastest;
- * the proposals are real warmup steps of the chains (no reference
- * counterpart).  *best receives the chosen warps per block. */
+ * warps; phase-synchronous blocks of 4..32 chains), in two interleaved
+ * passes (forward, then reverse order) of nprop/2 each, and keep the
+ * fastest; the proposals are real warmup steps of the chains (no reference
+ * counterpart), so call it after thermalisation.  *best receives the chosen
+ * warps per block. */
 int cthyb_batch_autotune(cthyb_batch_t batch, int64_t nprop, int* best);
 
 /* The remaining Z-space estimators of one chain, normalised as in
@@ -264,6 +266,17 @@ int cthyb_batch_minv(cthyb_batch_t batch, int chain, int f, int* k, double* out)
  * replace != 0 also installs the rebuilt matrices. */
 int cthyb_batch_refresh_minv(cthyb_batch_t batch, int replace, double* maxdev);
 
+/* Per-chain summary of one group (no reference counterpart; what the
+ * reference's per-rank outputs hold, for all chains in one copy): out[4*c
+ * + 0..3] = operators in the configuration, measurements, sum of the
+ * measured signs, proposals since the last warmup/measure call. */
+int cthyb_batch_chain_stats(cthyb_batch_t batch, int group, double* out);
+/* The raw G(tau) accumulators of every chain of one group in one copy:
+ * out[(c * 2Nd + f) * Ntau + bin], f = 2(b-1) + (s-1); chain c's G of
+ * cthyb_batch_results is -(raw / cnt) / (-sign_sum / cnt) * Ntau / beta^2
+ * with cnt and sign_sum from cthyb_batch_chain_stats (CTQMC.F90:8730). */
+int cthyb_batch_group_gtau_raw(cthyb_batch_t batch, int group, double* out);
+
 /* Drift of the fast updates, over all chains since creation or the last
  * reset (no counterpart in the reference): the largest |M_fast - M_rebuilt|
  * element and |log|det H| fast - rebuilt| seen at the periodic rebuilds
@@ -290,6 +303,13 @@ typedef struct {
  * FP64 flops of the dense-block trace products and bytes of their
  * operands. */
 int cthyb_batch_work_counters(cthyb_batch_t batch, int64_t* out8, int reset);
+
+/* FP64 throughput of the running device (no reference counterpart; the
+ * denominator of the FP64 rooflines the benchmark reports): GFLOP/s of
+ * independent fused multiply-adds on the CUDA cores and of m8n8k4 FP64
+ * tensor-core MMAs, best of three timed launches each.  Either pointer may
+ * be NULL.  Synchronises the device. */
+int cthyb_probe_fp64(double* dfma_gflops, double* dmma_gflops);
 
 /* Allocation-free inverse hybridisation matrix of one flavour -- no
  * counterpart in the reference.  For callers that cannot call cudaMalloc

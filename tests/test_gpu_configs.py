@@ -123,8 +123,10 @@ def test_three_orbital_beta50_config_parity(lib):
     assert abs(so["det_log"] - sg["det_log"]) < 1e-8 and so["cfgsign"] == sg["cfgsign"]
 
 
-@pytest.mark.parametrize("qns,seed,nwarm,nlog", [("Nt Szt", 4, 2000, 1000), ("Nt Szt", 1, 2000, 1000),
-                                                 ("Nt", 4, 150, 100)])
+# seeds whose initial outer superstate has 100 (seed 0), 50 (seed 7) and 5
+# (seed 4) states under "Nt Szt"; 210 states (seed 4) under "Nt"
+@pytest.mark.parametrize("qns,seed,nwarm,nlog", [("Nt Szt", 0, 1500, 1000), ("Nt Szt", 7, 2000, 1000),
+                                                 ("Nt Szt", 4, 2000, 1000), ("Nt", 4, 150, 100)])
 def test_kanamori5_config_parity(lib, qns, seed, nwarm, nlog):
     """5-orbital Kanamori model with spin-flip and pair hopping, beta = 40,
     Nftau = Ntau = 4000, one window: dense blocks of up to 100 x 100 ("Nt
@@ -179,7 +181,9 @@ def _coarse(g, nbin):
 
 def test_anderson_impurity_statistics_two_sigma(lib):
     """GPU: 32 chains x 1000 measurements of NCorr = 100 proposals; oracle:
-    8 chains x 4000 measurements with other seeds (equal total samples).
+    32 chains x 1000 measurements with other seeds (equal total samples;
+    as many independent chains on both sides, so the z-scores are close to
+    normal).
     Occupancies and double occupancy, G(tau) on 1000 bins (90 % within 2
     sigma, all within 5) and G averaged over 50-bin windows, by the 2-sigma
     criterion of _check_z."""
@@ -201,10 +205,10 @@ def test_anderson_impurity_statistics_two_sigma(lib):
     mo = O.Model(nd, pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
     ev = _oracle_evec(mo)
     cg, cn, cd = [], [], []
-    for c in range(8):
+    for c in range(32):
         co = O.Chain(mo, beta, pr["ftau"], ntau, seed=9000 + c, taudiff_max=beta, ncorr=100)
         co.warmup(10000)
-        co.measure(4000)
+        co.measure(1000)
         r = co.results()
         cg.append(r["gtau"])
         n, d = _occupations(nd, r["densitymatrix"], mo.fock_states, ev)
@@ -221,8 +225,8 @@ def test_anderson_impurity_statistics_two_sigma(lib):
 
 def test_mixed_beta_batch_statistics_two_sigma(lib):
     """The batched configuration's model with beta in {10, 25, 50, 100} in
-    ONE launch (16 chains per beta) against 8 oracle chains per beta with 2x
-    the measurements (equal total samples): occupancies and double
+    ONE launch (16 chains per beta) against 16 oracle chains per beta with
+    the same measurements (equal total samples): occupancies and double
     occupancies of all betas, and G(tau) averaged over 100-bin windows, by
     the 2-sigma criterion of _check_z."""
     betas = (10.0, 25.0, 50.0, 100.0)
@@ -250,11 +254,11 @@ def test_mixed_beta_batch_statistics_two_sigma(lib):
             gn.append(n)
             gd.append(d)
         cg, cn, cd = [], [], []
-        for c in range(nch // 2):
+        for c in range(nch):
             co = O.Chain(mo, bb, pr["ftau"], ntau, seed=7000 + 100 * i + c, taudiff_max=5.0, ncorr=ncorr,
                          **moves)
             co.warmup(nwarm)
-            co.measure(2 * nmeas)
+            co.measure(nmeas)
             r = co.results()
             cg.append(r["gtau"])
             n, d = _occupations(nd, r["densitymatrix"], mo.fock_states, ev)
@@ -266,5 +270,5 @@ def test_mixed_beta_batch_statistics_two_sigma(lib):
         zs.append(np.concatenate([zn, zd]))
         zcs.append(np.ravel(zc))
     print(f"\nmixed-beta batch statistics (occupancy z, double occupancy z, coarse G max |z|): {report}")
-    _check_z(np.concatenate(zs), "occupancies and double occupancies")
+    _check_z(np.concatenate(zs), "occupancies and double occupancies", zmax=4.0)
     _check_z(np.concatenate(zcs), "G(tau) 100-bin windows")

@@ -4695,6 +4695,34 @@ __global__ void k_drift(const __grid_constant__ DGroup g, unsigned long long* ou
   }
 }
 
+// Clear the measurement accumulators of every chain of a group (block c =
+// chain c): the region from G(tau) to the dense work space (G, G_full,
+// histogram, density matrix, Legendre, outer histograms, score sums) and
+// the header's measurement count and sign sum (init_counters' measurement
+// part, CTQMC.F90:847-899).
+__global__ void k_reset_meas(const __grid_constant__ DGroup g) {
+  char* base = g.base + (size_t)blockIdx.x * g.stride;
+  unsigned long long* p = (unsigned long long*)(base + g.o_gtau);
+  const size_t n = (g.o_dense - g.o_gtau) / 8;  // both offsets 256-byte aligned
+  for (size_t i = threadIdx.x; i < n; i += blockDim.x) p[i] = 0ull;
+  if (threadIdx.x == 0) {
+    Hdr* h = (Hdr*)(base + g.o_hdr);
+    h->cnt_meas = 0;
+    h->meas_sign = 0.0;
+  }
+}
+
+// Per-chain summary of a group: operators, measurements, sign sum, proposals.
+__global__ void k_chain_stats(const __grid_constant__ DGroup g, double* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.nchains) return;
+  const Hdr* h = (const Hdr*)(g.base + (size_t)c * g.stride + g.o_hdr);
+  out[4 * (size_t)c + 0] = (double)h->K;
+  out[4 * (size_t)c + 1] = (double)h->cnt_meas;
+  out[4 * (size_t)c + 2] = h->meas_sign;
+  out[4 * (size_t)c + 3] = (double)h->nprop;
+}
+
 // Sum of the G(tau) accumulators, signs and measurement counts over the
 // chains of a group (one thread per bin, chains strided).
 __global__ void k_group_sum(const __grid_constant__ DGroup g, int nbins, double* out, double* sign_out,
@@ -5391,30 +5419,40 @@ int cthyb_batch_measure(cthyb_batch_t B, int64_t nmeas) {
 int cthyb_batch_autotune(cthyb_batch_t B, int64_t nprop, int* best_out) {
   if (!B || nprop < 1) return fail(CTHYB_ERR_ARG, "bad arguments");
   const int cands[] = {0, 4, 8, 12, 14, 16, 20, 24, 28, 32};
+  const int ncand = (int)(sizeof(cands) / sizeof(cands[0]));
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   const int saved = B->sync_warps;
   int best = saved;
-  float best_ms = 3.4e38f;
+  // two passes over the candidates, the second in reverse order, half the
+  // proposals each: a drift of the chains' cost during tuning (expansion
+  // orders still growing) then weighs on every candidate alike
+  float tot[ncand] = {0.f};
   int rc = CTHYB_OK;
-  for (int nw : cands) {
-    B->sync_warps = nw;
-    cudaEventRecord(e0, B->stream);
-    rc = issue_sweeps(B, nprop, false);
-    if (rc) break;
-    cudaEventRecord(e1, B->stream);
-    if (cudaEventSynchronize(e1) != cudaSuccess) {
-      rc = fail(CTHYB_ERR_CUDA, "autotune launch failed");
-      break;
+  const long long half = std::max<long long>(1, nprop / 2);
+  for (int pass = 0; pass < 2 && rc == CTHYB_OK; ++pass)
+    for (int q = 0; q < ncand; ++q) {
+      const int ci = pass == 0 ? q : ncand - 1 - q;
+      B->sync_warps = cands[ci];
+      cudaEventRecord(e0, B->stream);
+      rc = issue_sweeps(B, half, false);
+      if (rc) break;
+      cudaEventRecord(e1, B->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        rc = fail(CTHYB_ERR_CUDA, "autotune launch failed");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      tot[ci] += ms;
     }
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    if (ms < best_ms) {
-      best_ms = ms;
-      best = nw;
+  float best_ms = 3.4e38f;
+  for (int q = 0; q < ncand && rc == CTHYB_OK; ++q)
+    if (tot[q] < best_ms) {
+      best_ms = tot[q];
+      best = cands[q];
     }
-  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   B->sync_warps = rc ? saved : best;
@@ -5425,18 +5463,8 @@ int cthyb_batch_autotune(cthyb_batch_t B, int64_t nprop, int* best_out) {
 int cthyb_batch_reset_measurements(cthyb_batch_t B) {
   if (!B) return fail(CTHYB_ERR_ARG, "null");
   for (GroupHost& G : B->groups) {
-    for (int c = 0; c < G.desc.nchains; ++c) {
-      char* base = G.g.base + (size_t)c * G.g.stride;
-      CK(cudaMemsetAsync(base + G.g.o_gtau, 0, G.g.o_dense - G.g.o_gtau, B->stream));
-      // header measurement fields: cnt_meas, meas_sign
-      Hdr hz;
-      CK(cudaMemcpyAsync(&hz, base + G.g.o_hdr, sizeof(Hdr), cudaMemcpyDeviceToHost, B->stream));
-      CK(cudaStreamSynchronize(B->stream));
-      hz.cnt_meas = 0;
-      hz.meas_sign = 0.0;
-      CK(cudaMemcpyAsync(base + G.g.o_hdr, &hz, sizeof(Hdr), cudaMemcpyHostToDevice, B->stream));
-      CK(cudaStreamSynchronize(B->stream));
-    }
+    k_reset_meas<<<G.desc.nchains, 256, 0, B->stream>>>(G.g);
+    CK(cudaGetLastError());
   }
   return CTHYB_OK;
 }
@@ -6012,6 +6040,31 @@ int cthyb_batch_refresh_minv(cthyb_batch_t B, int replace, double* maxdev) {
   return CTHYB_OK;
 }
 
+int cthyb_batch_chain_stats(cthyb_batch_t B, int group, double* out) {
+  if (!B || !out || group < 0 || group >= (int)B->groups.size()) return fail(CTHYB_ERR_ARG, "bad arguments");
+  GroupHost& G = B->groups[group];
+  const int n = G.desc.nchains;
+  double* d = nullptr;
+  CK(cudaMallocAsync((void**)&d, (size_t)4 * n * sizeof(double), B->stream));
+  k_chain_stats<<<(n + 127) / 128, 128, 0, B->stream>>>(G.g, d);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, d, (size_t)4 * n * sizeof(double), cudaMemcpyDeviceToHost, B->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
+  cudaFreeAsync(d, B->stream);
+  CK(e);
+  return CTHYB_OK;
+}
+
+int cthyb_batch_group_gtau_raw(cthyb_batch_t B, int group, double* out) {
+  if (!B || !out || group < 0 || group >= (int)B->groups.size()) return fail(CTHYB_ERR_ARG, "bad arguments");
+  GroupHost& G = B->groups[group];
+  const size_t row = (size_t)B->model->hm.nf * G.g.ntau * sizeof(double);
+  CK(cudaMemcpy2DAsync(out, row, G.g.base + G.g.o_gtau, G.g.stride, row, G.desc.nchains, cudaMemcpyDeviceToHost,
+                       B->stream));
+  CK(cudaStreamSynchronize(B->stream));
+  return CTHYB_OK;
+}
+
 int cthyb_batch_drift(cthyb_batch_t B, double* max_dev_m, double* max_dev_logdet, int64_t* refreshes,
                       int64_t* sign_errors, int reset) {
   if (!B) return fail(CTHYB_ERR_ARG, "null");
@@ -6222,6 +6275,80 @@ int cthyb_batch_work_counters(cthyb_batch_t B, int64_t* out8, int reset) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// FP64 peak of the running device, the denominator of the FP64 rooflines:
+// independent fused multiply-adds on the CUDA cores (eight chains a
+// thread) and m8n8k4 FP64 tensor-core MMAs (four accumulators a warp), each
+// over a grid of 8 blocks of 256 threads per multiprocessor.  Every thread
+// writes one double of `out` (grid x block entries).
+namespace cthyb {
+__global__ void __launch_bounds__(256) k_peak_dfma(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) x[j] = threadIdx.x * 1e-9 + j;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) x[j] = fma(x[j], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += x[j];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+__device__ __forceinline__ void dmma_884(double& d0, double& d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+__global__ void __launch_bounds__(256) k_peak_dmma(double* out, int iters, double a, double b) {
+  double c[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) c[j] = threadIdx.x * 1e-9 + j;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) dmma_884(c[2 * j], c[2 * j + 1], a, b);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) s += c[j];
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+}  // namespace cthyb
+
+extern "C" int cthyb_probe_fp64(double* dfma_gflops, double* dmma_gflops) {
+  using namespace cthyb;
+  int dev = 0, nsm = 0;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int block = 256, grid = 8 * nsm, iters = 4096;
+  double* out = nullptr;
+  CK(cudaMalloc(&out, sizeof(double) * (size_t)grid * block));
+  cudaEvent_t e0, e1;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  float best[2] = {3.4e38f, 3.4e38f};
+  for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep)
+    for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
+      cudaEventRecord(e0);
+      if (kind == 0) k_peak_dfma<<<grid, block>>>(out, iters, 0.999, 1e-3);
+      else k_peak_dmma<<<grid, block>>>(out, iters, 0.999, 1e-3);
+      cudaEventRecord(e1);
+      e = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best[kind]) best[kind] = ms;
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  CK(e);
+  const double threads = (double)grid * block;
+  // DFMA: 8 FMAs a thread and iteration; DMMA: 4 MMAs of 8x8x4 FMAs a warp
+  if (dfma_gflops) *dfma_gflops = 2.0 * 8 * iters * threads / (best[0] * 1e6);
+  if (dmma_gflops) *dmma_gflops = 2.0 * 256 * 4 * iters * (threads / 32) / (best[1] * 1e6);
+  return CTHYB_OK;
+}
 
 // ---------------------------------------------------------------------------
 // Allocation-free inverse hybridisation matrix.

@@ -32,7 +32,8 @@ EXPORTS = (
     "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_move_counters4", "cthyb_batch_results_full", "cthyb_batch_minv_full", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_set_configs", "cthyb_batch_get_configs", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
-    "cthyb_batch_drift", "cthyb_minv_rebuild_noalloc",
+    "cthyb_batch_drift", "cthyb_batch_chain_stats", "cthyb_batch_group_gtau_raw", "cthyb_probe_fp64",
+    "cthyb_minv_rebuild_noalloc",
 )
 
 
@@ -110,6 +111,9 @@ def load(build_if_missing=False):
     L.cthyb_batch_set_log.argtypes = [vp, i64]
     L.cthyb_batch_get_log.argtypes = [vp, C.c_int, C.c_void_p, C.POINTER(i64)]
     L.cthyb_batch_work_counters.argtypes = [vp, C.POINTER(i64), C.c_int]
+    L.cthyb_probe_fp64.argtypes = [dp, dp]
+    L.cthyb_batch_chain_stats.argtypes = [vp, C.c_int, dp]
+    L.cthyb_batch_group_gtau_raw.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_drift.argtypes = [vp, dp, dp, C.POINTER(i64), C.POINTER(i64), C.c_int]
     L.cthyb_minv_rebuild_noalloc.argtypes = [C.c_int, vp, vp, vp, C.c_int, C.c_double, vp, vp, vp]
     _lib = L
@@ -119,6 +123,13 @@ def load(build_if_missing=False):
 def _check(rc):
     if rc != 0:
         raise EngineError(f"cthyb error {rc}: {load().cthyb_last_error().decode()}")
+
+
+def probe_fp64():
+    """(DFMA, DMMA) FP64 GFLOP/s of the running device."""
+    a, b = C.c_double(), C.c_double()
+    _check(load().cthyb_probe_fp64(C.byref(a), C.byref(b)))
+    return a.value, b.value
 
 
 def _dp(a):
@@ -468,6 +479,31 @@ class Batch:
         d = np.zeros(1)
         _check(load().cthyb_batch_refresh_minv(self.h, 1 if replace else 0, _dp(d)))
         return float(d[0])
+
+    def chain_stats(self, group):
+        """Per chain of a group: operators, measurements, sign sum and
+        proposals since the last warmup/measure call (one copy)."""
+        g = self.groups[group]
+        out = np.zeros(4 * g.nchains)
+        _check(load().cthyb_batch_chain_stats(self.h, group, _dp(out)))
+        out = out.reshape(g.nchains, 4)
+        return dict(noper=out[:, 0].astype(np.int64), cnt_meas=out[:, 1].astype(np.int64),
+                    sign_sum=out[:, 2], proposals=out[:, 3].astype(np.int64))
+
+    def group_gtau(self, group):
+        """G(tau) of every chain of a group, normalised as results():
+        (nchains, Nd, 2, Ntau); chains without measurements give zeros."""
+        g = self.groups[group]
+        nd, nt = self.model.nd, g.ntau
+        raw = np.zeros(g.nchains * 2 * nd * nt)
+        _check(load().cthyb_batch_group_gtau_raw(self.h, group, _dp(raw)))
+        raw = raw.reshape(g.nchains, nd, 2, nt)  # f = 2b + s is (b, s) in C order
+        st = self.chain_stats(group)
+        cnt = st["cnt_meas"].astype(np.float64)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ms = np.where(cnt > 0, st["sign_sum"] / cnt, 0.0)
+            fac = np.where(cnt > 0, 1.0 / (cnt * ms), 0.0) * nt / (g.beta * g.beta)
+        return raw * fac[:, None, None, None]
 
     def drift(self, reset=False):
         """Drift of the fast updates at the periodic rebuilds of M, over all
