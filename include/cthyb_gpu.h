@@ -101,7 +101,8 @@ typedef struct {
                             4-operator moves (StepAdd4 / StepRem4, CTQMC.F90:3615-3890, 4153-4431) */
   const double* ftau_full; /* offdiag = 1: F for every flavour pair, (Nd,2,Nd,2,Nftau) Fortran
                               order (NULL: diagonal hybridisation from ftau).  Pair,
-                              outer-superstate, global and tau-shift moves (p_4op = 0, nleg = 0);
+                              outer-superstate, global and tau-shift moves (p_4op = 0), GLeg_full
+                              for nleg > 0;
                               kcap then bounds the total number of pairs; the inverse matrix over all flavours is in the reference's
                               block order (add_ftau_offset, Trace.F90:3002-3040). */
   int32_t refresh_every; /* drift control (no counterpart in the reference, which rebuilds M
@@ -116,6 +117,8 @@ typedef struct {
 
 #define CTHYB_FLAG_DENSE 1  /* dense block trace even for monomial models */
 #define CTHYB_FLAG_NO_DM 2  /* skip the beta/2 density-matrix measurement */
+#define CTHYB_FLAG_DMMA 4   /* dense-block trace: blocks of >= 16 x 16 on the FP64 tensor cores
+                               (mma m8n8k4) instead of FP64 fused multiply-adds */
 
 /* Create chains for all groups and initialise them like init_Trace
  * (Trace.F90:340-701): window from TaudiffMax, outer superstate drawn with
@@ -151,12 +154,22 @@ int cthyb_batch_use_graphs(cthyb_batch_t batch, int on);
  * phase-synchronous blocks of n chains whose proposals advance phase by
  * phase together.  Per-chain results do not depend on the schedule. */
 int cthyb_batch_set_schedule(cthyb_batch_t batch, int warps_per_block);
-/* Time `nprop` warmup proposals per chain under each schedule (independent
- * warps; phase-synchronous blocks of 4..32 chains), in two interleaved
- * passes (forward, then reverse order) of nprop/2 each, and keep the
- * fastest; the proposals are real warmup steps of the chains (no reference
- * counterpart), so call it after thermalisation.  *best receives the chosen
- * warps per block. */
+/* Team sweep (no reference counterpart): 0 = off (the schedule of
+ * cthyb_batch_set_schedule); T in 1..8 = blocks of T warps, each advancing
+ * one chain at a time, chains taken from a cost-ordered queue (largest
+ * operators x outer-superstate size first) as blocks become free; the T
+ * warps evaluate the dense-block trace together.  Per-chain results do not
+ * depend on it.  cthyb_batch_set_schedule switches it off. */
+int cthyb_batch_set_team(cthyb_batch_t batch, int warps_per_chain);
+/* Time `nprop` warmup proposals per chain under each schedule
+ * (independent warps; phase-synchronous blocks of 4..32 chains; for
+ * dense-block models phase-synchronous blocks of 1..8 chains and team
+ * sweeps of 1..8 warps per chain), in two interleaved passes (forward,
+ * then reverse order) of nprop/2 each, and keep the fastest; the proposals
+ * are real warmup steps of the chains (no reference counterpart), so call
+ * it after thermalisation.  *best receives the choice: warps per block of
+ * the phase-synchronous schedule (0: independent warps) or 100 + T for a
+ * team sweep of T warps per chain. */
 int cthyb_batch_autotune(cthyb_batch_t batch, int64_t nprop, int* best);
 
 /* The remaining Z-space estimators of one chain, normalised as in
@@ -195,6 +208,13 @@ int cthyb_batch_gradients(cthyb_batch_t batch, int nparams, const double* dE, do
 int cthyb_batch_gradients_device(cthyb_batch_t batch, int nparams, const double* dE_dev, double* grad_delta_dev,
                                  double* grad_params_dev, double* log_weights_dev, void* stream);
 
+/* log|det H| and the absolute log|trace| of every chain's current
+ * configuration, (nchains, 2) in device memory, from the weights the chains
+ * carry (no kernel walk; the forward value of a torch.autograd.Function
+ * whose backward calls cthyb_batch_gradients_device).  Enqueued on `stream`
+ * (NULL: the batch's stream) after the batch's queued work. */
+int cthyb_batch_log_weights_device(cthyb_batch_t batch, double* lw_dev, void* stream);
+
 /* Score-function estimate of dG(tau)/dtheta_p for the group's parameter
  * directions (nscore > 0): dgtau (nscore, Nd, 2, Ntau), each direction in
  * Fortran order, = <G g_p> - <G><g_p> with g_p = d log|trace| / dtheta_p of
@@ -213,6 +233,13 @@ int cthyb_batch_move_counters4(cthyb_batch_t batch, int chain, int64_t* out4);
  * [f_annihilator][f_creator][bin], f = 2(b-1)+(s-1), normalised as
  * Gtau_full (CTQMC.F90:8752-8753; MeasGtauRem_full, CTQMC.F90:2475-2584). */
 int cthyb_batch_results_full(cthyb_batch_t batch, int chain, double* gtau_full);
+/* Off-diagonal groups with nleg > 0: Legendre coefficients of G for every
+ * flavour pair, (2Nd, 2Nd, nleg) with index [f_annihilator][f_creator][l],
+ * normalised as GLeg_full (CTQMC.F90:8766-8771; measured by
+ * MeasGtauRem_full, CTQMC.F90:2533-2555).  The diagonal gleg of
+ * cthyb_batch_results_extra stays zero for these groups, as in the
+ * reference. */
+int cthyb_batch_results_gleg_full(cthyb_batch_t batch, int chain, double* gleg_full);
 /* Off-diagonal groups: the inverse matrix over all flavours (rows creators,
  * columns annihilators, block order, column-major k x k); k in *k. */
 int cthyb_batch_minv_full(cthyb_batch_t batch, int chain, int* k, double* out);

@@ -575,21 +575,22 @@ def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, np
     decides and updates like the oracle chain of the same seed, proposal by
     proposal (flavours, block positions, pair counts, outcomes bit-exact;
     ratios to 1e-10), with global and tau-shift moves at prare each where
-    given; then the measured G for every flavour pair, the order histogram
-    and the sign agree, and so do the final configuration and the inverse
-    matrix over all flavours."""
+    given; then the measured G for every flavour pair and its Legendre
+    coefficients (GLeg_full), the order histogram and the sign agree, and
+    so do the final configuration and the inverse matrix over all
+    flavours."""
     nd, beta, um, muimp, ff, qns = _offdiag_problem(kind)
     ntau = 10
     mo = O.Model(nd, um, muimp, qns)
     co = O.Chain(mo, beta, ff, ntau, seed=seed, taudiff_max=tdm, p_outer=pout, ncorr=20, maxhisto=30,
-                 p_global=prare, p_shift=prare)
+                 p_global=prare, p_shift=prare, nleg=6)
     co.start_log(nprop)
     co.warmup(nprop)
     ref = co.log()
     mg = E.Model(nd, um, muimp, qns)
     b = E.Batch(mg, [E.Group(beta, _diag_of(ff), ntau, nchains=1, seed0=seed, taudiff_max=tdm,
                              p_outer=pout, ncorr=20, maxhisto=30, kcap=64, opcap=256,
-                             ftau_full=ff, p_global=prare, p_shift=prare)])
+                             ftau_full=ff, p_global=prare, p_shift=prare, nleg=6)])
     b.set_log(nprop)
     b.warmup(nprop)
     b.sync()
@@ -608,6 +609,9 @@ def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, np
     assert np.array_equal(ro["histo"], np.stack([rg["histo"][f // 2, f % 2] for f in range(nf)]))
     go, gg = co.results_full(), b.results_full(0)
     assert np.allclose(gg, go, rtol=1e-9, atol=1e-12 * np.abs(go).max())
+    lo, lg = co.gleg_full(), b.results_gleg_full(0)  # GLeg_full, CTQMC.F90:2533-2555
+    assert np.allclose(lg, lo, rtol=1e-9, atol=1e-12 * np.abs(lo).max())
+    assert not np.any(b.results_extra(0)["gleg"])
     t_o, *_ = co.get_config()
     t_g, *_ = b.get_config(0)
     assert np.array_equal(t_o, t_g)

@@ -180,7 +180,12 @@ class _OracleSolveBatch(_OracleBatch):
     def results_extra(self, i):
         x = self.chains[i].results_extra()
         x["gleg"] = x["gleg"].reshape(self.nd, 2, -1)
+        if self.groups[0].ftau_full is not None:
+            x["gleg"] = np.zeros_like(x["gleg"])  # offdiag = 1: GLeg stays zero
         return x
+
+    def results_gleg_full(self, i):
+        return self.chains[i].gleg_full()
 
     def move_counters(self, i):
         cnt = self.chains[i].counters()
@@ -254,12 +259,12 @@ def test_offdiag_module_results_on_oracle_chains(monkeypatch):
     muimp = P.muimp_solver(1, 1.3)
     par = dict(BASE, beta=beta, Nd=1, Ntau=ntau, QuantumNumbers="Nt", offdiag=1, Nmeas=300, NCorr=20,
                PercentageGlobalMove=0.05, PercentageTauShiftMove=0.05, Percentage4OperatorMove=0.0,
-               NSymMove=0, MeasSsquare=0, NLegMax=0)
+               NSymMove=0, MeasSsquare=0, NLegMax=8)
     ctqmc.init_paras(pstring(par))
     ctqmc._check_supported()
     mo = O.Model(1, um, muimp, "Nt")
     chains = [O.Chain(mo, beta, ff, ntau, seed=3 + i, taudiff_max=1.5, ncorr=20, p_outer=0.1,
-                      maxhisto=BASE["MaxHisto"] + 1, p_global=0.05, p_shift=0.05) for i in range(2)]
+                      maxhisto=BASE["MaxHisto"] + 1, p_global=0.05, p_shift=0.05, nleg=8) for i in range(2)]
     fake = _OracleSolveBatch(chains, 1, ftau_full=ff)
     model = E.Model(1, um, muimp, "Nt")
     for key, val in (("_batch", fake), ("_model", model), ("_nd", 1), ("_nchains", 2), ("_beta", beta)):
@@ -272,6 +277,11 @@ def test_offdiag_module_results_on_oracle_chains(monkeypatch):
     got = np.array([[ctqmc.gtau_full[fa // 2, fa % 2, fc // 2, fc % 2] for fc in range(2)] for fa in range(2)])
     assert np.allclose(got, want, rtol=1e-13, atol=0)
     assert np.abs(got[0, 1]).max() > 0.01
+    # GLeg_full of every flavour pair, GLeg zero (MeasGtauRem_full only)
+    wl = sum(c.gleg_full() * w for c, w in zip(chains, s)) / s.sum()
+    gl = np.array([[ctqmc.gleg_full[fa // 2, fa % 2, fc // 2, fc % 2] for fc in range(2)] for fa in range(2)])
+    assert gl.shape == (2, 2, 8) and np.allclose(gl, wl, rtol=1e-13, atol=0)
+    assert np.abs(gl[0, 1]).max() > 0.0 and not np.any(ctqmc.gleg)
     for name in RESULTSET:
         if name not in ("ssquare", "ssquare_operator"):
             getattr(ctqmc, name).copy()

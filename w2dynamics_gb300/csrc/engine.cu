@@ -892,10 +892,48 @@ __device__ __forceinline__ double weight_ratio(double mx, double sum, double old
 }
 
 // ---------------------------------------------------------------------------
-// Dense-block trace: time-ordered product of exp(-dtau (E-Egs)) and c/c+
-// blocks for the outer superstate s0, recomputed over the whole proposed
-// configuration (get_Trace_EB_fullmatrix, Trace.F90:5734-6100, evaluated as
-// a matrix over all outer states at once with one log scale).
+// Dense-block trace: time-ordered products of exp(-dtau (E - Egs)) and the
+// c/c+ blocks in the H_loc eigenbasis (get_Trace_EB_fullmatrix,
+// Trace.F90:5734-6100), evaluated for all outer states at once: every outer
+// state is one column of a matrix propagated through the operators, each
+// column with its own log scale (the role of split_log, Trace.F90:5341-5348).
+//
+// Teams.  The threads that evaluate one chain's dense-block trace together:
+// one warp (the chain's own warp in the phase-synchronous and independent-
+// warp sweeps, and every leader-only path) or a whole block of T warps (the
+// team sweep, k_sweep_team).  Values the team shares are written by its
+// thread 0 and read after a team barrier; `red` is shared scratch of one
+// double per warp for team reductions.
+struct Team {
+  int tid, nth;
+  double* red;
+};
+__device__ __forceinline__ Team solo_team(const Ctx& c) { return Team{c.lane, 32, nullptr}; }
+__device__ __forceinline__ void tsync(const Team& t) {
+  if (t.nth == 32) __syncwarp();
+  else __syncthreads();
+}
+__device__ __forceinline__ double tsum(const Team& t, double x) {
+  x = wsum(x);
+  if (t.nth == 32) return x;
+  if ((t.tid & 31) == 0) t.red[t.tid >> 5] = x;
+  __syncthreads();
+  double s = 0.0;
+  for (int w = 0; w < (t.nth >> 5); ++w) s += t.red[w];
+  __syncthreads();
+  return s;
+}
+__device__ __forceinline__ double tmax(const Team& t, double x) {
+  x = wmax(x);
+  if (t.nth == 32) return x;
+  if ((t.tid & 31) == 0) t.red[t.tid >> 5] = x;
+  __syncthreads();
+  double s = -DHUGE;
+  for (int w = 0; w < (t.nth >> 5); ++w) s = fmax(s, t.red[w]);
+  __syncthreads();
+  return s;
+}
+
 struct OpIter {
   int j, K, stage;  // stage: number of inserted ops consumed
 };
@@ -920,99 +958,16 @@ __device__ __forceinline__ bool next_op(const Ctx& c, const Mod& md, OpIter& it,
     return true;
   }
 }
-__device__ NOINL void dense_trace(Ctx& c, const Mod& md, int s0, double& lg, double& sg) {
-  const DModel& m = *c.m;
-  const int ld = m.nsmax;
-  double* X = c.dense;
-  double* Y = c.dense + (size_t)ld * ld;
-  int n0 = m.sst_n[s0];
-  for (int e = c.lane; e < n0 * n0; e += 32) {
-    int r = e % n0, col = e / n0;
-    X[(size_t)col * ld + r] = (r == col) ? 1.0 : 0.0;
-  }
-  __syncwarp();
-  int cur = s0, ncur = n0;
-  double t = 0.0, l = 0.0;
-  OpIter it{0, c.h->K, 0};
-  double tau;
-  int code;
-  bool zero = false;
-  while (next_op(c, md, it, tau, code)) {
-    int f = code >> 1, ca = code & 1;
-    int nxt = m.connect[((size_t)cur * m.nf + f) * 2 + ca];
-    if (nxt < 0) {
-      zero = true;
-      break;
-    }
-    double dt = tau - t;
-    const double* E = m.eval + m.sst_off[cur];
-    double e0 = E[0];
-    for (int e = c.lane; e < ncur * n0; e += 32) {
-      int r = e % ncur, col = e / ncur;
-      X[(size_t)col * ld + r] *= exp(-(E[r] - e0) * dt);
-    }
-    l += -(e0 - m.egs) * dt;
-    __syncwarp();
-    int nn = m.sst_n[nxt];
-    const double* B = m.blk + m.blk_off[((size_t)cur * m.nf + f) * 2 + ca];
-    if (c.lane == 0) {
-      c.h->w_tflops += 2ll * nn * ncur * n0;
-      c.h->w_tbytes += 8ll * (nn * ncur + ncur * n0 + nn * n0);
-    }
-    double mx = 0.0;
-    for (int e = c.lane; e < nn * n0; e += 32) {
-      int i = e % nn, col = e / nn;
-      double acc = 0.0;
-      for (int r = 0; r < ncur; ++r) acc += B[(size_t)r * nn + i] * X[(size_t)col * ld + r];
-      Y[(size_t)col * ld + i] = acc;
-      mx = fmax(mx, fabs(acc));
-    }
-    mx = wmax(mx);
-    __syncwarp();
-    if (mx == 0.0) {
-      zero = true;
-      break;
-    }
-    double inv = 1.0 / mx;
-    for (int e = c.lane; e < nn * n0; e += 32) {
-      int i = e % nn, col = e / nn;
-      Y[(size_t)col * ld + i] *= inv;
-    }
-    l += log(mx);
-    __syncwarp();
-    double* T = X;
-    X = Y;
-    Y = T;
-    cur = nxt;
-    ncur = nn;
-    t = tau;
-  }
-  if (zero || cur != s0) {
-    lg = -DHUGE;
-    sg = 0.0;
-    return;
-  }
-  double dt = c.g->beta - t;
-  const double* E = m.eval + m.sst_off[cur];
-  double e0 = E[0];
-  l += -(e0 - m.egs) * dt;
-  double tr = 0.0;
-  for (int i = c.lane; i < n0; i += 32) tr += exp(-(E[i] - e0) * dt) * X[(size_t)i * ld + i];
-  tr = wsum(tr);
-  lg = l + log(fabs(tr));
-  sg = tr >= 0.0 ? 1.0 : -1.0;
-}
 
 // ---------------------------------------------------------------------------
-// Dense-block trace with checkpoints at the bin edges: the reference's
-// cached kets/bras with lazy extension (get_Trace_EB, Trace.F90:5354-5546,
-// and the R/L loops of get_Trace_EB_fullmatrix, Trace.F90:5734-6100), kept at
-// the 2^L + 1 time-bin edges.  Ket checkpoint j: every outer state
-// propagated from tau = 0 through the operators before edge j and evolved to
-// the edge; bra checkpoint j: from beta through the operators after edge j.
-// A pair move in bins b1 <= b2 needs kets up to b1 and bras from b2 + 1 and
-// recomputes only bins b1..b2; acceptance keeps those checkpoints.  Each
-// column (outer state) carries its own log scale.
+// Checkpoints at the bin edges: the reference's cached kets/bras with lazy
+// extension (get_Trace_EB, Trace.F90:5354-5546, and the R/L loops of
+// get_Trace_EB_fullmatrix), kept at the 2^L + 1 time-bin edges.  Ket
+// checkpoint j: every outer state propagated from tau = 0 through the
+// operators before edge j and evolved to the edge; bra checkpoint j: from
+// beta through the operators after edge j.  A pair move in bins b1 <= b2
+// needs kets up to b1 and bras from b2 + 1 and recomputes only bins
+// b1..b2; acceptance keeps those checkpoints.
 struct ChkHead {
   int sst, rows, cols, pad;
 };
@@ -1023,21 +978,23 @@ __device__ __forceinline__ ChkHead* chk_head(const Ctx& c, int dir, int j) {
 __device__ __forceinline__ double* chk_lg(ChkHead* p) { return (double*)(p + 1); }
 __device__ __forceinline__ double* chk_v(const Ctx& c, ChkHead* p) { return chk_lg(p) + c.m->nsmax; }
 
+// work space of the dense trace: two nsmax x nsmax matrices (0, 1) and two
+// nsmax vectors (2: column logs, 3: per-row / per-column factors)
 __device__ __forceinline__ double* dwork(const Ctx& c, int i) {
   const size_t n2 = (size_t)c.m->nsmax * c.m->nsmax;
   return i < 2 ? c.dense + i * n2 : c.dense + 2 * n2 + (size_t)(i - 2) * c.m->nsmax;
 }
-// Column-wise renormalisation, the role of split_log (Trace.F90:5341-5348):
-// each column is scaled by the power of two at or below its largest
-// magnitude (exact), whose exponent goes into the column's log.  One column
-// at a time, warp-parallel over its rows; the maximum is taken on the bit
-// patterns (order-preserving for magnitudes), so no FP64 compares.
-__device__ void col_split(Ctx& c, int rows, int cols, double* v, double* lg) {
-  const int ld = c.m->nsmax;
-  for (int col = 0; col < cols; ++col) {
+// Column-wise renormalisation: each column is scaled by the power of two at
+// or below its largest magnitude (exact), whose exponent goes into the
+// column's log.  One warp per column (columns strided over the team's
+// warps), the maximum taken on the bit patterns (order-preserving for
+// magnitudes), so no FP64 compares.
+__device__ void col_split(Ctx& c, int rows, int cols, double* v, double* lg, const Team& t) {
+  const int ld = c.m->nsmax, lane = t.tid & 31;
+  for (int col = t.tid >> 5; col < cols; col += t.nth >> 5) {
     double* vc = v + (size_t)col * ld;
     long long mk = 0;
-    for (int i = c.lane; i < rows; i += 32) {
+    for (int i = lane; i < rows; i += 32) {
       const long long k = __double_as_longlong(vc[i]) & 0x7FFFFFFFFFFFFFFFll;
       mk = k > mk ? k : mk;
     }
@@ -1051,193 +1008,292 @@ __device__ void col_split(Ctx& c, int rows, int cols, double* v, double* lg) {
     const int e = ef - 1023 > 1022 ? 1022 : ef - 1023;  // keep 2^-e a normal number
     if (e == 0) continue;
     const double sc = __longlong_as_double((long long)(1023 - e) << 52);  // 2^-e
-    for (int i = c.lane; i < rows; i += 32) vc[i] *= sc;
-    if (c.lane == 0) lg[col] += (double)e * 0.69314718055994530942;  // e ln 2
+    for (int i = lane; i < rows; i += 32) vc[i] *= sc;
+    if (lane == 0) lg[col] += (double)e * 0.69314718055994530942;  // e ln 2
   }
-  __syncwarp();
+  tsync(t);
 }
 // exp(-(E - E0) dt) on the rows of superstate sst, E0 - Egs into the logs
-__device__ void col_evolve(Ctx& c, int sst, int rows, int cols, double* v, double* lg, double dt) {
+__device__ void col_evolve(Ctx& c, int sst, int rows, int cols, double* v, double* lg, double dt, const Team& t) {
   const DModel& m = *c.m;
   const int ld = m.nsmax;
   const double* E = m.eval + m.sst_off[sst];
   const double e0 = E[0];
   if (rows > 1) {
     double* fac = dwork(c, 3);  // one exponential per row, shared by the columns
-    for (int i = c.lane; i < rows; i += 32) fac[i] = exp(-(E[i] - e0) * dt);
-    __syncwarp();
-    for (int e = c.lane; e < rows * cols; e += 32) {
+    for (int i = t.tid; i < rows; i += t.nth) fac[i] = exp(-(E[i] - e0) * dt);
+    tsync(t);
+    for (int e = t.tid; e < rows * cols; e += t.nth) {
       const int i = e % rows, col = e / rows;
       v[(size_t)col * ld + i] *= fac[i];
     }
   }
-  for (int col = c.lane; col < cols; col += 32) lg[col] += -(e0 - m.egs) * dt;
-  __syncwarp();
-  if (rows > 1) col_split(c, rows, cols, v, lg);
+  for (int col = t.tid; col < cols; col += t.nth) lg[col] += -(e0 - m.egs) * dt;
+  tsync(t);
+  if (rows > 1) col_split(c, rows, cols, v, lg, t);
 }
+
+// out (nn x cols) = B^T v with B the block stored as B[r * nn + i] (rows r
+// of v, rows i of out), leading dimension ld for v and out.  CUDA cores:
+// each thread accumulates one output row over four columns (four
+// independent FMA chains; the block element is loaded once for the four).
+__device__ __forceinline__ void block_gemm_fma(const double* __restrict__ B, int nn, int rows,
+                                               const double* __restrict__ v, int cols, double* __restrict__ out,
+                                               int ld, const Team& t) {
+  const int ncb = (cols + 3) >> 2;
+  for (int e = t.tid; e < nn * ncb; e += t.nth) {
+    const int i = e % nn, c0 = (e / nn) * 4;
+    const double* vp = v + (size_t)c0 * ld;
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    if (c0 + 4 <= cols) {
+#pragma unroll 4
+      for (int r = 0; r < rows; ++r) {
+        const double b = B[(size_t)r * nn + i];
+        a0 = fma(b, vp[r], a0);
+        a1 = fma(b, vp[ld + r], a1);
+        a2 = fma(b, vp[2 * ld + r], a2);
+        a3 = fma(b, vp[3 * ld + r], a3);
+      }
+      double* op = out + (size_t)c0 * ld + i;
+      op[0] = a0;
+      op[ld] = a1;
+      op[2 * ld] = a2;
+      op[3 * ld] = a3;
+    } else {
+      const int nc = cols - c0;
+      for (int r = 0; r < rows; ++r) {
+        const double b = B[(size_t)r * nn + i];
+        a0 = fma(b, vp[r], a0);
+        if (nc > 1) a1 = fma(b, vp[ld + r], a1);
+        if (nc > 2) a2 = fma(b, vp[2 * ld + r], a2);
+      }
+      double* op = out + (size_t)c0 * ld + i;
+      op[0] = a0;
+      if (nc > 1) op[ld] = a1;
+      if (nc > 2) op[2 * ld] = a2;
+    }
+  }
+}
+// The same on the FP64 tensor cores: m8n8k4 MMAs, each warp computing an
+// 8 x 16 strip of out (two 8 x 8 accumulator tiles sharing the A
+// fragment) over k-steps of 4, strips strided over the team's warps.
+// Fragment layouts of mma.m8n8k4.f64 (PTX ISA): A row = lane / 4, k =
+// lane % 4; B k = lane % 4, column = lane / 4; C row = lane / 4, columns
+// 2 (lane % 4) + {0, 1}.  Out-of-range rows, columns and k are zero.
+__device__ __forceinline__ void dmma_884(double& d0, double& d1, double a, double b) {
+  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+               : "+d"(d0), "+d"(d1)
+               : "d"(a), "d"(b));
+}
+__device__ __forceinline__ void block_gemm_mma(const double* __restrict__ B, int nn, int rows,
+                                               const double* __restrict__ v, int cols, double* __restrict__ out,
+                                               int ld, const Team& t) {
+  const int lane = t.tid & 31, warp = t.tid >> 5, nw = t.nth >> 5;
+  const int ti = (nn + 7) >> 3, tj = (cols + 15) >> 4;
+  const int fr = lane >> 2, fk = lane & 3;
+  for (int s = warp; s < ti * tj; s += nw) {
+    const int i0 = (s % ti) * 8, j0 = (s / ti) * 16;
+    const int ia = i0 + fr, jb0 = j0 + fr, jb1 = j0 + 8 + fr;
+    double d0 = 0.0, d1 = 0.0, d2 = 0.0, d3 = 0.0;
+    for (int k0 = 0; k0 < rows; k0 += 4) {
+      const int k = k0 + fk;
+      const bool kin = k < rows;
+      const double a = (kin && ia < nn) ? B[(size_t)k * nn + ia] : 0.0;
+      const double b0 = (kin && jb0 < cols) ? v[(size_t)jb0 * ld + k] : 0.0;
+      const double b1 = (kin && jb1 < cols) ? v[(size_t)jb1 * ld + k] : 0.0;
+      dmma_884(d0, d1, a, b0);
+      dmma_884(d2, d3, a, b1);
+    }
+    const int orow = i0 + fr, oc = j0 + 2 * fk;
+    if (orow < nn) {
+      if (oc < cols) out[(size_t)oc * ld + orow] = d0;
+      if (oc + 1 < cols) out[(size_t)(oc + 1) * ld + orow] = d1;
+      if (oc + 8 < cols) out[(size_t)(oc + 8) * ld + orow] = d2;
+      if (oc + 9 < cols) out[(size_t)(oc + 9) * ld + orow] = d3;
+    }
+  }
+}
+
 // One operator: evolve by dt in superstate *sst, apply the block of
 // (code, ca-flip for bras) into `out`, split.  Returns false when the
-// superstate sequence breaks.
+// superstate sequence breaks.  Blocks of at least 16 x 16 go to the FP64
+// tensor cores when the group asks for them (CTHYB_FLAG_DMMA).
 __device__ bool col_step(Ctx& c, int& sst, int& rows, int cols, double*& v, double*& out, double* lg, int code,
-                         bool bra, double dt) {
+                         bool bra, double dt, const Team& t) {
   const DModel& m = *c.m;
   const int ld = m.nsmax;
   const int f = code >> 1, ca = bra ? 1 - (code & 1) : (code & 1);
   const int nxt = m.connect[((size_t)sst * m.nf + f) * 2 + ca];
   if (nxt < 0) return false;
-  col_evolve(c, sst, rows, cols, v, lg, dt);
+  col_evolve(c, sst, rows, cols, v, lg, dt, t);
   const int nn = m.sst_n[nxt];
   const double* B = m.blk + m.blk_off[((size_t)sst * m.nf + f) * 2 + ca];
-  if (c.lane == 0) {
+  if (t.tid == 0) {
     c.h->w_tflops += 2ll * nn * rows * cols;
     c.h->w_tbytes += 8ll * (nn * rows + rows * cols + nn * cols);
   }
-  for (int e = c.lane; e < nn * cols; e += 32) {
-    const int i = e % nn, col = e / nn;
-    double acc = 0.0;
-    for (int r = 0; r < rows; ++r) acc = fma(B[(size_t)r * nn + i], v[(size_t)col * ld + r], acc);
-    out[(size_t)col * ld + i] = acc;
-  }
-  __syncwarp();
-  if (nn > 1 || rows > 1) col_split(c, nn, cols, out, lg);
-  double* t = v;
+  if (c.g->dmma && nn >= 16 && rows >= 16) block_gemm_mma(B, nn, rows, v, cols, out, ld, t);
+  else block_gemm_fma(B, nn, rows, v, cols, out, ld, t);
+  tsync(t);
+  if (nn > 1 || rows > 1) col_split(c, nn, cols, out, lg, t);
+  double* tmp = v;
   v = out;
-  out = t;
+  out = tmp;
   sst = nxt;
   rows = nn;
   return true;
 }
-__device__ void chk_load(Ctx& c, ChkHead* h, int& sst, int& rows, int& cols, double* v, double* lg) {
+__device__ void chk_load(Ctx& c, ChkHead* h, int& sst, int& rows, int& cols, double* v, double* lg, const Team& t) {
   sst = h->sst;
   rows = h->rows;
   cols = h->cols;
   const int ld = c.m->nsmax;
   const double* src = chk_v(c, h);
-  for (int e = c.lane; e < rows * cols; e += 32) v[(size_t)(e / rows) * ld + e % rows] = src[(size_t)(e / rows) * ld + e % rows];
-  for (int col = c.lane; col < cols; col += 32) lg[col] = chk_lg(h)[col];
-  __syncwarp();
+  for (int e = t.tid; e < rows * cols; e += t.nth) {
+    const size_t x = (size_t)(e / rows) * ld + e % rows;
+    v[x] = src[x];
+  }
+  for (int col = t.tid; col < cols; col += t.nth) lg[col] = chk_lg(h)[col];
+  tsync(t);
 }
-__device__ void chk_store(Ctx& c, ChkHead* h, int sst, int rows, int cols, const double* v, const double* lg) {
+__device__ void chk_store(Ctx& c, ChkHead* h, int sst, int rows, int cols, const double* v, const double* lg,
+                          const Team& t) {
   const int ld = c.m->nsmax;
   double* dst = chk_v(c, h);
-  for (int e = c.lane; e < rows * cols; e += 32) dst[(size_t)(e / rows) * ld + e % rows] = v[(size_t)(e / rows) * ld + e % rows];
-  for (int col = c.lane; col < cols; col += 32) chk_lg(h)[col] = lg[col];
-  if (c.lane == 0) {
+  for (int e = t.tid; e < rows * cols; e += t.nth) {
+    const size_t x = (size_t)(e / rows) * ld + e % rows;
+    dst[x] = v[x];
+  }
+  for (int col = t.tid; col < cols; col += t.nth) chk_lg(h)[col] = lg[col];
+  if (t.tid == 0) {
     h->sst = sst;
     h->rows = rows;
     h->cols = cols;
   }
-  __syncwarp();
+  tsync(t);
 }
-__device__ void chk_identity(Ctx& c, ChkHead* h, int s0) {
+__device__ void chk_identity(Ctx& c, ChkHead* h, int s0, const Team& t) {
   const int ld = c.m->nsmax, n0 = c.m->sst_n[s0];
   double* dst = chk_v(c, h);
-  for (int e = c.lane; e < n0 * n0; e += 32) dst[(size_t)(e / n0) * ld + e % n0] = (e / n0 == e % n0) ? 1.0 : 0.0;
-  for (int col = c.lane; col < n0; col += 32) chk_lg(h)[col] = 0.0;
-  if (c.lane == 0) {
+  for (int e = t.tid; e < n0 * n0; e += t.nth) dst[(size_t)(e / n0) * ld + e % n0] = (e / n0 == e % n0) ? 1.0 : 0.0;
+  for (int col = t.tid; col < n0; col += t.nth) chk_lg(h)[col] = 0.0;
+  if (t.tid == 0) {
     h->sst = s0;
     h->rows = n0;
     h->cols = n0;
   }
-  __syncwarp();
+  tsync(t);
 }
 // Kets valid up to edge `upto` (current configuration).
-__device__ NOINL bool ensure_kets(Ctx& c, int upto) {
+__device__ NOINL bool ensure_kets(Ctx& c, int upto, const Team& t) {
   Hdr& h = *c.h;
   if (h.kv < 0) {
-    chk_identity(c, chk_head(c, 0, 0), h.outer_sst);
-    if (c.lane == 0) h.kv = 0;
-    __syncwarp();
+    chk_identity(c, chk_head(c, 0, 0), h.outer_sst, t);
+    if (t.tid == 0) h.kv = 0;
+    tsync(t);
   }
   double *v = dwork(c, 0), *o = dwork(c, 1), *lg = dwork(c, 2);
   while (h.kv < upto) {
     const int j = h.kv;
     int sst, rows, cols;
-    chk_load(c, chk_head(c, 0, j), sst, rows, cols, v, lg);
-    double t = bin_edge(c, j);
+    chk_load(c, chk_head(c, 0, j), sst, rows, cols, v, lg, t);
+    double tt = bin_edge(c, j);
     for (int i = c.bstart[j]; i < c.bstart[j + 1]; ++i) {
       const double tau = c.optau[i];
-      if (!col_step(c, sst, rows, cols, v, o, lg, c.opcode[i], false, tau - t)) return false;
-      t = tau;
+      if (!col_step(c, sst, rows, cols, v, o, lg, c.opcode[i], false, tau - tt, t)) return false;
+      tt = tau;
     }
-    col_evolve(c, sst, rows, cols, v, lg, bin_edge(c, j + 1) - t);
-    chk_store(c, chk_head(c, 0, j + 1), sst, rows, cols, v, lg);
-    if (c.lane == 0) h.kv = j + 1;
-    __syncwarp();
+    col_evolve(c, sst, rows, cols, v, lg, bin_edge(c, j + 1) - tt, t);
+    chk_store(c, chk_head(c, 0, j + 1), sst, rows, cols, v, lg, t);
+    if (t.tid == 0) h.kv = j + 1;
+    tsync(t);
   }
   return true;
 }
 // Bras valid from edge `from` (current configuration).
-__device__ NOINL bool ensure_bras(Ctx& c, int from) {
+__device__ NOINL bool ensure_bras(Ctx& c, int from, const Team& t) {
   Hdr& h = *c.h;
   const int nb = 1 << c.g->L;
   if (h.bv > nb) {
-    chk_identity(c, chk_head(c, 1, nb), h.outer_sst);
-    if (c.lane == 0) h.bv = nb;
-    __syncwarp();
+    chk_identity(c, chk_head(c, 1, nb), h.outer_sst, t);
+    if (t.tid == 0) h.bv = nb;
+    tsync(t);
   }
   double *v = dwork(c, 0), *o = dwork(c, 1), *lg = dwork(c, 2);
   while (h.bv > from) {
     const int j = h.bv;
     int sst, rows, cols;
-    chk_load(c, chk_head(c, 1, j), sst, rows, cols, v, lg);
-    double t = bin_edge(c, j);
+    chk_load(c, chk_head(c, 1, j), sst, rows, cols, v, lg, t);
+    double tt = bin_edge(c, j);
     for (int i = c.bstart[j] - 1; i >= c.bstart[j - 1]; --i) {
       const double tau = c.optau[i];
-      if (!col_step(c, sst, rows, cols, v, o, lg, c.opcode[i], true, t - tau)) return false;
-      t = tau;
+      if (!col_step(c, sst, rows, cols, v, o, lg, c.opcode[i], true, tt - tau, t)) return false;
+      tt = tau;
     }
-    col_evolve(c, sst, rows, cols, v, lg, t - bin_edge(c, j - 1));
-    chk_store(c, chk_head(c, 1, j - 1), sst, rows, cols, v, lg);
-    if (c.lane == 0) h.bv = j - 1;
-    __syncwarp();
+    col_evolve(c, sst, rows, cols, v, lg, tt - bin_edge(c, j - 1), t);
+    chk_store(c, chk_head(c, 1, j - 1), sst, rows, cols, v, lg, t);
+    if (t.tid == 0) h.bv = j - 1;
+    tsync(t);
   }
   return true;
 }
-// <bra|ket> per column at one edge, summed over the outer states in log
-// form (addLogTr, Trace.F90:298-309).
-__device__ void chk_close(Ctx& c, int sst, int rows, int cols, const double* v, const double* lg, ChkHead* bh,
-                          double& out_lg, double& out_sg) {
+// Sum over the outer states (columns) of d[col] * exp(lg[col]) in log form
+// (the sum of addLogTr, Trace.F90:298-309): log|sum| and its sign.
+__device__ void col_logsum(const double* d, const double* lg, int cols, const Team& t, double& out_lg,
+                           double& out_sg) {
+  double mx = -DHUGE;
+  for (int col = t.tid; col < cols; col += t.nth)
+    if (d[col] != 0.0) mx = fmax(mx, lg[col] + log(fabs(d[col])));
+  mx = tmax(t, mx);
+  out_lg = -DHUGE;
+  out_sg = 0.0;
+  if (mx == -DHUGE) return;
+  double s = 0.0;
+  for (int col = t.tid; col < cols; col += t.nth)
+    if (d[col] != 0.0) s += (d[col] > 0.0 ? 1.0 : -1.0) * exp(lg[col] + log(fabs(d[col])) - mx);
+  s = tsum(t, s);
+  if (s == 0.0) return;
+  out_lg = mx + log(fabs(s));
+  out_sg = s > 0.0 ? 1.0 : -1.0;
+}
+// <bra|ket> per column at one edge, summed over the outer states in log form.
+__device__ void chk_close(Ctx& c, int sst, int rows, int cols, const double* v, double* lg, ChkHead* bh,
+                          double& out_lg, double& out_sg, const Team& t) {
   out_lg = -DHUGE;
   out_sg = 0.0;
   if (bh->sst != sst) return;
-  const int ld = c.m->nsmax;
+  const int ld = c.m->nsmax, lane = t.tid & 31;
   const double* bv = chk_v(c, bh);
   const double* blg = chk_lg(bh);
-  for (int col = 0; col < cols; ++col) {
+  double* d = dwork(c, 3);  // per-column <bra|ket>
+  for (int col = t.tid >> 5; col < cols; col += t.nth >> 5) {
     double part = 0.0;
-    for (int i = c.lane; i < rows; i += 32) part = fma(v[(size_t)col * ld + i], bv[(size_t)col * ld + i], part);
-    const double bk = wsum(part);
-    if (bk == 0.0) continue;
-    const double l = lg[col] + blg[col] + log(fabs(bk));
-    const double sg = bk >= 0.0 ? 1.0 : -1.0;
-    if (out_sg == 0.0) {
-      out_lg = l;
-      out_sg = sg;
-    } else if (out_lg >= l) {
-      out_lg = out_lg + log(1.0 + out_sg * sg * exp(l - out_lg));
-    } else {
-      const double nl = l + log(1.0 + out_sg * sg * exp(out_lg - l));
-      out_lg = nl;
-      out_sg = sg;
-    }
+    for (int i = lane; i < rows; i += 32) part = fma(v[(size_t)col * ld + i], bv[(size_t)col * ld + i], part);
+    part = wsum(part);
+    if (lane == 0) d[col] = part;
   }
+  tsync(t);
+  // column logs of ket and bra together (lg is the trace's work vector,
+  // free to update here)
+  for (int col = t.tid; col < cols; col += t.nth) lg[col] += blg[col];
+  tsync(t);
+  col_logsum(d, lg, cols, t, out_lg, out_sg);
 }
 // Trace of a proposed pair move for the current outer superstate from the
 // checkpoints: kets at edge b1, the proposed operators of bins b1..b2 (the
 // gathered leaves for b1/b2, the current lists in between), bras at b2 + 1.
-__device__ NOINL void chk_trace(Ctx& c, const Mod& md, double& out_lg, double& out_sg) {
+__device__ NOINL void chk_trace(Ctx& c, const Mod& md, double& out_lg, double& out_sg, const Team& t) {
   out_lg = -DHUGE;
   out_sg = 0.0;
   const int b1 = md.b1, b2 = md.b2;
-  if (!ensure_kets(c, b1) || !ensure_bras(c, b2 + 1)) {
-    set_status(c, ST_INTERNAL);
+  if (!ensure_kets(c, b1, t) || !ensure_bras(c, b2 + 1, t)) {
+    if (t.tid < 32) set_status(c, ST_INTERNAL);
     return;
   }
   double *v = dwork(c, 0), *o = dwork(c, 1), *lg = dwork(c, 2);
   int sst, rows, cols;
-  chk_load(c, chk_head(c, 0, b1), sst, rows, cols, v, lg);
-  double t = bin_edge(c, b1);
+  chk_load(c, chk_head(c, 0, b1), sst, rows, cols, v, lg, t);
+  double tt = bin_edge(c, b1);
   for (int b = b1; b <= b2; ++b) {
     const bool gathered = b == b1 || b == b2;
     const int buf = b == b1 ? 0 : 1;
@@ -1245,13 +1301,13 @@ __device__ NOINL void chk_trace(Ctx& c, const Mod& md, double& out_lg, double& o
     for (int q = 0; q < n; ++q) {
       const double tau = gathered ? c.btau[buf][q] : c.optau[c.bstart[b] + q];
       const int code = gathered ? c.bcode[buf][q] : c.opcode[c.bstart[b] + q];
-      if (!col_step(c, sst, rows, cols, v, o, lg, code, false, tau - t)) return;
-      t = tau;
+      if (!col_step(c, sst, rows, cols, v, o, lg, code, false, tau - tt, t)) return;
+      tt = tau;
     }
-    col_evolve(c, sst, rows, cols, v, lg, bin_edge(c, b + 1) - t);
-    t = bin_edge(c, b + 1);
+    col_evolve(c, sst, rows, cols, v, lg, bin_edge(c, b + 1) - tt, t);
+    tt = bin_edge(c, b + 1);
   }
-  chk_close(c, sst, rows, cols, v, lg, chk_head(c, 1, b2 + 1), out_lg, out_sg);
+  chk_close(c, sst, rows, cols, v, lg, chk_head(c, 1, b2 + 1), out_lg, out_sg, t);
 }
 __device__ __forceinline__ void chk_invalidate(Ctx& c) {
   if (c.lane == 0) {
@@ -1273,6 +1329,34 @@ __device__ __forceinline__ void chk_keep(Ctx& c, const Mod& md, int new_outer) {
     if (c.h->bv < md.b2 + 1) c.h->bv = md.b2 + 1;
   }
   __syncwarp();
+}
+
+// Dense-block trace from scratch for outer superstate s0 over the whole
+// proposed configuration: the identity for the outer states propagated from
+// tau = 0 through every operator and evolved to beta; the trace is the sum
+// of the diagonal elements with their column scales.  log|trace| and sign.
+__device__ NOINL void dense_trace(Ctx& c, const Mod& md, int s0, double& lg, double& sg, const Team& t) {
+  const int ld = c.m->nsmax, n0 = c.m->sst_n[s0];
+  double *v = dwork(c, 0), *o = dwork(c, 1), *lgc = dwork(c, 2);
+  for (int e = t.tid; e < n0 * n0; e += t.nth) v[(size_t)(e / n0) * ld + e % n0] = (e / n0 == e % n0) ? 1.0 : 0.0;
+  for (int col = t.tid; col < n0; col += t.nth) lgc[col] = 0.0;
+  tsync(t);
+  lg = -DHUGE;
+  sg = 0.0;
+  int sst = s0, rows = n0;
+  double tprev = 0.0, tau;
+  int code;
+  OpIter it{0, c.h->K, 0};
+  while (next_op(c, md, it, tau, code)) {
+    if (!col_step(c, sst, rows, n0, v, o, lgc, code, false, tau - tprev, t)) return;
+    tprev = tau;
+  }
+  if (sst != s0) return;
+  col_evolve(c, sst, rows, n0, v, lgc, c.g->beta - tprev, t);
+  double* d = dwork(c, 3);
+  for (int col = t.tid; col < n0; col += t.nth) d[col] = v[(size_t)col * ld + col];
+  tsync(t);
+  col_logsum(d, lgc, n0, t, lg, sg);
 }
 
 // ---------------------------------------------------------------------------
@@ -1384,13 +1468,13 @@ __device__ NOINL void write_record(Ctx& c, const cthyb_record& r) {
 
 // Trace of the proposed configuration for outer superstate s0.
 // Trace of the proposed configuration as sum * exp(mx).
-__device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum) {
+__device__ void proposed_trace(Ctx& c, Mod& md, int s0, double& mx, double& sum, const Team& t) {
   if (c.mono) {
     root_trace(c, 1 - c.act[1], s0, mx, sum, c.h->trace_log);  // state tree rebuilt after the QN check
   } else if (s0 == c.h->outer_sst && c.g->o_chk) {
-    chk_trace(c, md, mx, sum);  // log|trace| and its sign from the checkpoints
+    chk_trace(c, md, mx, sum, t);  // log|trace| and its sign from the checkpoints
   } else {
-    dense_trace(c, md, s0, mx, sum);  // new outer superstate: from scratch
+    dense_trace(c, md, s0, mx, sum, t);  // new outer superstate: from scratch
   }
 }
 
@@ -1732,10 +1816,26 @@ __device__ NOINL void ph_det(Ctx& c, Prop& p) {
 // and the Metropolis decision (CTQMC.F90:3508-3524, 4050-4058).
 __device__ NOINL void ph_trace(Ctx& c, Prop& p) {
   double tr_mx, tr_sum;
-  proposed_trace(c, p.md, p.snew, tr_mx, tr_sum);
+  proposed_trace(c, p.md, p.snew, tr_mx, tr_sum, solo_team(c));
   p.tr_mx = tr_mx;
   p.tr_sum = tr_sum;
   __syncwarp();
+}
+// The same evaluated by a team of warps (dense-block models in the team
+// sweep; monomial traces stay with the chain's own warp, thread 0's warp).
+__device__ NOINL void ph_trace_team(Ctx& c, Prop& p, const Team& t) {
+  if (c.mono) {
+    if (t.tid < 32) ph_trace(c, p);
+    __syncthreads();
+    return;
+  }
+  double tr_mx, tr_sum;
+  proposed_trace(c, p.md, p.snew, tr_mx, tr_sum, t);
+  if (t.tid == 0) {
+    p.tr_mx = tr_mx;
+    p.tr_sum = tr_sum;
+  }
+  __syncthreads();
 }
 __device__ NOINL void ph_decide(Ctx& c, Prop& p) {
   Hdr& h = *c.h;
@@ -2183,7 +2283,7 @@ __device__ NOINL void rebuilt_trace(Ctx& c, int s0, double& lg, double& sg) {
   } else {
     Mod md;
     md.type = 0;
-    dense_trace(c, md, s0, lg, sg);
+    dense_trace(c, md, s0, lg, sg, solo_team(c));
   }
 }
 
@@ -2415,7 +2515,7 @@ __device__ NOINL void ph_change_outer(Ctx& c, Prop& p) {
     } else {
       Mod md;
       md.type = 0;
-      dense_trace(c, md, s0, lg, sg);
+      dense_trace(c, md, s0, lg, sg, solo_team(c));
     }
   }
   if (!(lg > -DHUGE)) {
@@ -3611,6 +3711,29 @@ __device__ NOINL void ph_rem_od(Ctx& c, Prop& p) {
   __syncwarp();
 }
 
+// ---------------------------------------------------------------------------
+// Legendre coefficients of one G sample: lsum[l] += M P_l(x), P_l by the
+// three-term recurrence in the reference's operation order
+// (CTQMC.F90:2368-2389, 2533-2555).
+__device__ __forceinline__ void legendre_add(double Mv, double x, int nleg, double* lsum) {
+  double plx = 0.0, plm1 = 0.0;
+  for (int l = 0; l < nleg; ++l) {
+    double p;
+    if (l == 0) {
+      p = 1.0;
+    } else if (l == 1) {
+      p = x;
+    } else {
+      const int ll = l - 1;
+      p = __dsub_rn(__dmul_rn(__dmul_rn(__ddiv_rn(2.0 * ll + 1.0, (double)(ll + 1)), x), plx),
+                    __dmul_rn(__ddiv_rn((double)ll, (double)(ll + 1)), plm1));
+    }
+    lsum[l] = __dadd_rn(lsum[l], __dmul_rn(Mv, p));
+    plm1 = plx;
+    plx = p;
+  }
+}
+
 // MeasGtauRem_full (CTQMC.F90:2475-2584) and MeasExpOrder with
 // NOSOper(b,s)/2 = (creators + annihilators of the flavour) / 2.
 __device__ NOINL void measure_od(Ctx& c) {
@@ -3667,6 +3790,50 @@ __device__ NOINL void measure_od(Ctx& c) {
     atomicAdd(&G[((size_t)af[j] * nf + cf[i]) * nt + idt - 1], Mv);
   }
   __syncwarp();
+  // GLeg_full (CTQMC.F90:2533-2555): per (annihilator flavour, creator
+  // flavour) block of the inverse matrix, lane partial sums reduced over
+  // the warp
+  const int nleg = g.nleg;
+  if (nleg <= 0) return;
+  int offc[NFMAX + 1], offa[NFMAX + 1];
+  offc[0] = offa[0] = 0;
+  for (int f = 0; f < nf; ++f) {
+    int nc = 0, na = 0;
+    for (int i = c.lane; i < K; i += 32) {
+      nc += c.opcode[i] == 2 * f;
+      na += c.opcode[i] == 2 * f + 1;
+    }
+    offc[f + 1] = offc[f] + wsumi(nc);
+    offa[f + 1] = offa[f] + wsumi(na);
+  }
+  double* GL = (double*)((char*)c.gtau - g.o_gtau + g.o_gleg);  // [fa][fc][l]
+  double* lsum = (double*)((char*)c.gtau - g.o_gtau + g.o_glscr) + (size_t)c.lane * nleg;
+  for (int fa = 0; fa < nf; ++fa)
+    for (int fc = 0; fc < nf; ++fc) {
+      const int na = offa[fa + 1] - offa[fa], nc = offc[fc + 1] - offc[fc];
+      if (na == 0 || nc == 0) continue;
+      for (int l = 0; l < nleg; ++l) lsum[l] = 0.0;
+      for (int e = c.lane; e < na * nc; e += 32) {
+        const int i = offc[fc] + e % nc, j = offa[fa] + e / nc;
+        double Mv = Mf[(size_t)j * ld + i];
+        const double ta = at[j], tc = ct[i];
+        double dt;
+        if (ta - tc > 0.0) {
+          dt = ta - tc;
+        } else {
+          dt = g.beta + ta - tc;
+          Mv = -Mv;
+        }
+        legendre_add(Mv * h.cfgsign, __dsub_rn(__dmul_rn(__ddiv_rn(2.0, g.beta), dt), 1.0), nleg, lsum);
+      }
+      __syncwarp();
+      double* dst = GL + ((size_t)fa * nf + fc) * nleg;
+      for (int l = 0; l < nleg; ++l) {
+        const double v = wsum(lsum[l]);
+        if (c.lane == 0) dst[l] += v;
+      }
+      __syncwarp();
+    }
 }
 
 // Inverse of the full hybridisation matrix of the configuration in the
@@ -3999,7 +4166,7 @@ __device__ NOINL void measure(Ctx& c) {
   // state (CTQMC.F90:3088-3150)
   if (g.meas_dm && !c.mono && g.o_chk) {
     const int mid = 1 << (g.L - 1);
-    if (ensure_kets(c, mid) && ensure_bras(c, mid)) {
+    if (ensure_kets(c, mid, solo_team(c)) && ensure_bras(c, mid, solo_team(c))) {
       ChkHead* kh = chk_head(c, 0, mid);
       ChkHead* bh = chk_head(c, 1, mid);
       if (kh->sst == bh->sst) {
@@ -4068,26 +4235,7 @@ __device__ NOINL void measure(Ctx& c) {
         if (idt > nt) idt = nt;
         atomicAdd(&G[idt - 1], Mv);
         for (int p = 0; p < nsc; ++p) atomicAdd(&sacc[nsc + ((size_t)p * m.nf + f) * nt + idt - 1], Mv * score[p]);
-        if (nleg > 0) {
-          // P_l by the three-term recurrence, as evaluated in the reference
-          const double x = __dsub_rn(__dmul_rn(__ddiv_rn(2.0, g.beta), dt), 1.0);
-          double plx = 0.0, plm1 = 0.0;
-          for (int l = 0; l < nleg; ++l) {
-            double p;
-            if (l == 0) {
-              p = 1.0;
-            } else if (l == 1) {
-              p = x;
-            } else {
-              const int ll = l - 1;
-              p = __dsub_rn(__dmul_rn(__dmul_rn(__ddiv_rn(2.0 * ll + 1.0, (double)(ll + 1)), x), plx),
-                            __dmul_rn(__ddiv_rn((double)ll, (double)(ll + 1)), plm1));
-            }
-            lsum[l] = __dadd_rn(lsum[l], __dmul_rn(Mv, p));
-            plm1 = plx;
-            plx = p;
-          }
-        }
+        if (nleg > 0) legendre_add(Mv, __dsub_rn(__dmul_rn(__ddiv_rn(2.0, g.beta), dt), 1.0), nleg, lsum);
       }
     }
     if (nleg > 0) {
@@ -4208,7 +4356,7 @@ __global__ void __launch_bounds__(WPB * 32) k_init(const __grid_constant__ DMode
   } else {
     Mod md;
     md.type = 0;
-    dense_trace(c, md, h.outer_sst, lg, sg);
+    dense_trace(c, md, h.outer_sst, lg, sg, solo_team(c));
   }
   if (c.lane == 0) {
     h.trace_log = lg;
@@ -4415,6 +4563,161 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
   }
 }
 
+// Team sweep: each block is a team of T warps that advances one chain at a
+// time; chains are taken in the order of `order` through a global counter,
+// so a block that finishes early picks up the next chain (the order puts
+// the largest estimated cost first: longest-processing-time-first list
+// scheduling over the blocks).  Warp 0 runs the scalar phases of every
+// proposal with the same functions as the other sweeps, so each chain's
+// proposal stream is unchanged; the whole team evaluates the dense-block
+// trace (block products, renormalisation, checkpoints).
+#ifndef TEAM_MAX_THREADS
+#define TEAM_MAX_THREADS 256  // teams of up to 8 warps
+#define TEAM_MIN_BLOCKS 4     // register budget: 64 per thread
+#endif
+__global__ void __launch_bounds__(TEAM_MAX_THREADS, TEAM_MIN_BLOCKS)
+    k_sweep_team(const __grid_constant__ DModel m, const DGroup* __restrict__ groups, int ngroups, int ntotal,
+                 long long nprop, int nmeas, int reset, const int* __restrict__ order, int* counter) {
+  extern __shared__ __align__(16) unsigned char dyn[];
+  Hdr* hs = (Hdr*)dyn;
+  cthyb_record* rec = (cthyb_record*)(hs + 1);
+  Prop* pp = (Prop*)(rec + 1);
+  double* red = (double*)(pp + 1);                   // one double per warp
+  unsigned char* act = (unsigned char*)(red + 32);   // tree active bits
+  __shared__ int next;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const Team team{(int)threadIdx.x, (int)blockDim.x, red};
+  Prop& p = *pp;
+  while (true) {
+    if (threadIdx.x == 0) next = atomicAdd(counter, 1);
+    __syncthreads();
+    const int slot = next;
+    __syncthreads();
+    if (slot >= ntotal) break;
+    const int gchain = order[slot];
+    int gi = 0;
+    while (gi + 1 < ngroups && gchain >= groups[gi + 1].chain0) ++gi;
+    const DGroup* gp = &groups[gi];
+    const int chain = gchain - gp->chain0;
+    Ctx c = make_ctx(&m, gp, hs, chain, rec);
+    Hdr* gh = (Hdr*)(gp->base + (size_t)chain * gp->stride + gp->o_hdr);
+    unsigned char* gact = c.act;
+    const int nact4 = (2 << gp->L) / 4;
+    c.act = act;
+    if (warp == 0) {
+      load_hdr(c.h, gh, lane);
+      for (int i = lane; i < nact4; i += 32) ((uint32_t*)c.act)[i] = ((const uint32_t*)gact)[i];
+      __syncwarp();
+      mt_refill(c, c.h->mt_idx);
+      if (reset && lane == 0) {  // init_counters, CTQMC.F90:847-899
+        Hdr& h = *c.h;
+        h.try_add = h.acc_add = h.try_rem = h.acc_rem = h.qn_add = h.qn_rem = 0;
+        h.try_glob = h.acc_glob = h.qn_glob = h.try_shift = h.acc_shift = 0;
+        h.try_add4 = h.acc_add4 = h.try_rem4 = h.acc_rem4 = 0;
+        h.nprop = 0;
+      }
+      __syncwarp();
+    }
+    __syncthreads();
+    const long long total = nmeas <= 0 ? nprop : (long long)nmeas * gp->ncorr;
+    for (long long i = 0; i < total; ++i) {
+      if (c.h->status != ST_OK) break;  // the shared header, read after a block barrier
+      if (warp == 0) {
+        ph_draw(c, p);
+        if (p.rare) {
+          if (p.move == 2) ph_global(c, p);
+          else if (p.move == 3) ph_shift(c, p);
+          else if (p.move == 5) ph_add4(c, p);
+          else if (p.move == 6) ph_rem4(c, p);
+          else if (p.move == 7) ph_add_od(c, p);
+          else ph_rem_od(c, p);
+          if (refresh_due(c)) ph_refresh(c);
+          if (c.h->status == ST_OK) ph_finish(c, p);
+        } else if (p.alive) {
+          if (p.move == 0) ph_setup_add(c, p);
+          else ph_setup_rem(c, p);
+          if (p.alive) ph_tree_ss(c, p);
+          if (p.alive) ph_tree_states(c, p);
+          if (p.alive) ph_det(c, p);
+        }
+      }
+      __syncthreads();
+      if (!p.rare && p.alive) ph_trace_team(c, p, team);  // the whole team; ends with a barrier
+      if (warp == 0) {
+        if (!p.rare) {
+          if (p.alive) ph_decide(c, p);
+          if (p.alive) {
+            if (p.move == 0) ph_accept_add(c, p);
+            else ph_accept_rem(c, p);
+          }
+          if (refresh_due(c)) ph_refresh(c);
+          if (c.h->status == ST_OK) ph_finish(c, p);
+        }
+        if (nmeas > 0 && (i + 1) % gp->ncorr == 0 && c.h->status == ST_OK) measure(c);
+      }
+      __syncthreads();
+    }
+    if (warp == 0) {
+      if (lane == 0) {
+        c.h->mt_idx = mt_index(c);
+        if (c.h->status != ST_OK) atomicMax(gp->err_flag, c.h->status);
+      }
+      __syncwarp();
+      for (int i2 = lane; i2 < nact4; i2 += 32) ((uint32_t*)gact)[i2] = ((const uint32_t*)c.act)[i2];
+      store_hdr(gh, c.h, lane);
+    }
+    __syncthreads();
+  }
+}
+
+// Order of the chains for the team sweep: estimated cost of a proposal
+// descending (operators + 8, times the outer superstate's size for dense-
+// block models: the trace's block products scale with both), ties by
+// chain index; one block, bitonic sort of (cost, index) keys in shared
+// memory for up to 8192 chains, the identity beyond.
+constexpr int ORDER_MAX = 8192;
+__global__ void __launch_bounds__(1024) k_order(const __grid_constant__ DModel m, const DGroup* __restrict__ groups,
+                                                int ngroups, int ntotal, int* __restrict__ order) {
+  extern __shared__ unsigned long long keys[];
+  int n2 = 1;
+  while (n2 < ntotal) n2 <<= 1;
+  if (n2 > ORDER_MAX) {
+    for (int i = threadIdx.x; i < ntotal; i += blockDim.x) order[i] = i;
+    return;
+  }
+  for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+    unsigned long long v = ~0ull;
+    if (i < ntotal) {
+      int gi = 0;
+      while (gi + 1 < ngroups && i >= groups[gi + 1].chain0) ++gi;
+      const DGroup& g = groups[gi];
+      const Hdr* h = (const Hdr*)(g.base + (size_t)(i - g.chain0) * g.stride + g.o_hdr);
+      long long cost = (long long)h->K + 8;
+      if (!(m.monomial && !g.dense)) cost *= m.sst_n[h->outer_sst];
+      const long long key = cost < 0x7fffffffll ? cost : 0x7fffffffll;
+      v = ((unsigned long long)(0x7fffffffll - key) << 32) | (unsigned)i;
+    }
+    keys[i] = v;
+  }
+  __syncthreads();
+  for (int k = 2; k <= n2; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int i = threadIdx.x; i < n2; i += blockDim.x) {
+        const int ixj = i ^ j;
+        if (ixj > i) {
+          const bool up = (i & k) == 0;
+          const unsigned long long a = keys[i], b = keys[ixj];
+          if ((a > b) == up) {
+            keys[i] = b;
+            keys[ixj] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int i = threadIdx.x; i < ntotal; i += blockDim.x) order[i] = (int)(keys[i] & 0xffffffffull);
+}
+
 // Gradients of log|w| of each chain's current configuration (no reference
 // counterpart).  Determinant part: d log|det H| / dH(a, c) = M(c, a), and
 // H(a, c) = Delta_f(tau_a - tau_c) interpolates the grid linearly
@@ -4610,7 +4913,7 @@ __global__ void __launch_bounds__(WPB * 32) k_set_configs(const __grid_constant_
   } else {
     Mod md;
     md.type = 0;
-    dense_trace(c, md, h.outer_sst, lg, sg);
+    dense_trace(c, md, h.outer_sst, lg, sg, solo_team(c));
   }
   double dlog, dsign;
   rebuild_minv(c, nullptr, true, dlog, dsign);
@@ -4710,6 +5013,16 @@ __global__ void k_reset_meas(const __grid_constant__ DGroup g) {
     h->cnt_meas = 0;
     h->meas_sign = 0.0;
   }
+}
+
+// log|det H| and the absolute log|trace| (the stored trace is relative to
+// exp(-beta Egs)) of every chain of a group from the chain headers.
+__global__ void k_log_weights(const __grid_constant__ DModel m, const __grid_constant__ DGroup g, double* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.nchains) return;
+  const Hdr* h = (const Hdr*)(g.base + (size_t)c * g.stride + g.o_hdr);
+  out[2 * (size_t)(g.chain0 + c)] = h->det_log;
+  out[2 * (size_t)(g.chain0 + c) + 1] = h->trace_log - g.beta * m.egs;
 }
 
 // Per-chain summary of a group: operators, measurements, sign sum, proposals.
@@ -4831,6 +5144,10 @@ struct cthyb_batch_s {
     int sched = -2;
     cudaGraphExec_t exec = nullptr;
   } gwarm, gmeas;
+  int team = 0;         // > 0: team sweep with `team` warps per chain (k_sweep_team)
+  int* d_order = nullptr;   // chain order of the team sweep
+  int* d_counter = nullptr; // its fetch counter
+  int team_attr = 0;        // shared memory the team kernels are opted in for
   int nsm = 0;          // multiprocessors of the device
   long long logcap = 0;
   bool counters_reset_pending = false;
@@ -5001,6 +5318,7 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.p_shift = d.p_shift;
   g.p_4op = d.p_4op;
   g.dense = (d.flags & CTHYB_FLAG_DENSE) ? 1 : 0;
+  g.dmma = (d.flags & CTHYB_FLAG_DMMA) ? 1 : 0;
   g.refresh_every = d.refresh_every == 0 ? CTHYB_REFRESH_DEFAULT : (d.refresh_every < 0 ? 0 : d.refresh_every);
   g.meas_dm = (d.flags & CTHYB_FLAG_NO_DM) ? 0 : 1;
   int kcap = d.kcap > 0 ? d.kcap : std::max(32, (int)std::min(4096.0, 32.0 * std::ceil(d.beta * 1.0 / 32.0 + 1.0)));
@@ -5066,8 +5384,8 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.o_dm = off;  // diagonal (monomial models) or the superstate blocks of rho
   off = align_up(off + (size_t)(mono ? hm.ns : hm.dm_size) * 8, 256);
   g.nleg = d.nleg > 0 ? d.nleg : 0;
-  g.o_gleg = off;
-  off = align_up(off + (size_t)nf * g.nleg * 8, 256);
+  g.o_gleg = off;  // GLeg (nf x nleg), or GLeg_full (nf x nf x nleg) for off-diagonal groups
+  off = align_up(off + (size_t)nf * (d.ftau_full ? nf : 1) * g.nleg * 8, 256);
   g.o_outer = off;  // outer superstate/state histograms, signs, trace contributions
   off = align_up(off + (size_t)3 * (hm.nss + hm.ns) * 8, 256);
   g.nscore = (d.nscore > 0 && d.score_dE && mono) ? std::min(d.nscore, 32) : 0;
@@ -5122,10 +5440,9 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
       delete B;
       return fail(CTHYB_ERR_ARG, "bad group description");
     }
-    if (G.desc.ftau_full && (G.desc.p_4op > 0.0 || G.desc.nleg > 0 || (G.desc.nscore > 0 && G.desc.score_dE))) {
+    if (G.desc.ftau_full && (G.desc.p_4op > 0.0 || (G.desc.nscore > 0 && G.desc.score_dE))) {
       delete B;
-      return fail(CTHYB_ERR_UNSUPPORTED,
-                  "off-diagonal hybridisation: no 4-operator moves, Legendre or score measurements");
+      return fail(CTHYB_ERR_UNSUPPORTED, "off-diagonal hybridisation: no 4-operator moves or score measurements");
     }
     layout_group(B, G, 0);
     G.chain0 = B->nchains;
@@ -5265,6 +5582,8 @@ int cthyb_batch_destroy(cthyb_batch_t B) {
   cudaFree(B->d_err);
   cudaFree(B->d_dev);
   if (B->d_red) cudaFree(B->d_red);
+  if (B->d_order) cudaFree(B->d_order);
+  if (B->d_counter) cudaFree(B->d_counter);
   if (B->d_groups) cudaFree(B->d_groups);
   if (B->gwarm.exec) cudaGraphExecDestroy(B->gwarm.exec);
   if (B->gmeas.exec) cudaGraphExecDestroy(B->gmeas.exec);
@@ -5327,7 +5646,40 @@ static int sync_attributes(cthyb_batch_t B, size_t smem) {
   return CTHYB_OK;
 }
 
+// Team sweep: order the chains by estimated cost (k_order), reset the
+// fetch counter, and launch one persistent grid of `team`-warp blocks
+// (as many as fit on the device, at most one per chain).
+static int launch_team(cthyb_batch_t B, long long nprop, int nmeas, int reset) {
+  int Lmax = 1;
+  for (GroupHost& G : B->groups) Lmax = std::max(Lmax, G.g.L);
+  const int threads = 32 * B->team;
+  const size_t smem = sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + 32 * sizeof(double) + (2 << Lmax);
+  int n2 = 1;
+  while (n2 < B->nchains) n2 <<= 1;
+  const size_t osmem = n2 <= ORDER_MAX ? (size_t)n2 * 8 : 0;
+  if (!B->d_order) {
+    CK(cudaMalloc(&B->d_order, sizeof(int) * (size_t)B->nchains));
+    CK(cudaMalloc(&B->d_counter, sizeof(int)));
+  }
+  if (!B->team_attr) {
+    CK(cudaFuncSetAttribute(k_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(ORDER_MAX * 8)));
+    CK(cudaFuncSetAttribute(k_sweep_team, cudaFuncAttributeMaxDynamicSharedMemorySize, 48 * 1024));
+    B->team_attr = 1;
+  }
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_team, threads, smem));
+  const int grid = std::max(1, std::min(B->nchains, std::max(per_sm, 1) * std::max(B->nsm, 1)));
+  k_order<<<1, 1024, osmem, B->stream>>>(B->model->dm, B->d_groups, (int)B->groups.size(), B->nchains, B->d_order);
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(B->d_counter, 0, sizeof(int), B->stream));
+  k_sweep_team<<<grid, threads, smem, B->stream>>>(B->model->dm, B->d_groups, (int)B->groups.size(), B->nchains,
+                                                  nprop, nmeas, reset, B->d_order, B->d_counter);
+  CK(cudaGetLastError());
+  return CTHYB_OK;
+}
+
 static int launch_sweeps(cthyb_batch_t B, long long nprop, int nmeas, int reset) {
+  if (B->team > 0) return launch_team(B, nprop, nmeas, reset);
   int Lmax = 1;
   for (GroupHost& G : B->groups) Lmax = std::max(Lmax, G.g.L);
   const int actbytes = 2 << Lmax;
@@ -5352,6 +5704,14 @@ static int launch_sweeps(cthyb_batch_t B, long long nprop, int nmeas, int reset)
 int cthyb_batch_set_schedule(cthyb_batch_t B, int warps_per_block) {
   if (!B || warps_per_block < -1 || warps_per_block > 32) return fail(CTHYB_ERR_ARG, "warps_per_block must be -1..32");
   B->sync_warps = warps_per_block;
+  B->team = 0;
+  return CTHYB_OK;
+}
+
+int cthyb_batch_set_team(cthyb_batch_t B, int warps_per_chain) {
+  if (!B || warps_per_chain < 0 || warps_per_chain > TEAM_MAX_THREADS / 32)
+    return fail(CTHYB_ERR_ARG, "warps_per_chain must be 0..8");
+  B->team = warps_per_chain;
   return CTHYB_OK;
 }
 
@@ -5372,7 +5732,7 @@ static int issue_sweeps(cthyb_batch_t B, long long n, bool meas) {
 
 // Capture the launch sequence once per (n, schedule) and replay it.
 static int graph_sweeps(cthyb_batch_t B, cthyb_batch_s::Graph& G, long long n, bool meas) {
-  const int sched = schedule_of(B);
+  const int sched = B->team > 0 ? 100 + B->team : schedule_of(B);
   if (!G.exec || G.n != n || G.sched != sched) {
     if (G.exec) {
       CK(cudaGraphExecDestroy(G.exec));
@@ -5381,8 +5741,15 @@ static int graph_sweeps(cthyb_batch_t B, cthyb_batch_s::Graph& G, long long n, b
     // kernel attributes are set outside the capture
     int Lmax = 1;
     for (GroupHost& g : B->groups) Lmax = std::max(Lmax, g.g.L);
-    const size_t smem = (size_t)sched * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + (2 << Lmax));
-    if (sched > 0) {
+    if (B->team > 0) {
+      // attributes, order and counter buffers set up by one eager launch
+      // sequence outside the capture
+      if (!B->d_order || !B->team_attr) {
+        int rc = launch_team(B, 0, 0, 0);
+        if (rc) return rc;
+      }
+    } else if (sched > 0) {
+      const size_t smem = (size_t)sched * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + (2 << Lmax));
       int rc = sync_attributes(B, smem);
       if (rc) return rc;
     }
@@ -5418,23 +5785,31 @@ int cthyb_batch_measure(cthyb_batch_t B, int64_t nmeas) {
 
 int cthyb_batch_autotune(cthyb_batch_t B, int64_t nprop, int* best_out) {
   if (!B || nprop < 1) return fail(CTHYB_ERR_ARG, "bad arguments");
-  const int cands[] = {0, 4, 8, 12, 14, 16, 20, 24, 28, 32};
-  const int ncand = (int)(sizeof(cands) / sizeof(cands[0]));
+  // candidates: phase-synchronous blocks of n chains (0: independent
+  // warps) and, for dense-block models, team sweeps of T warps per chain
+  // (encoded 100 + T)
+  bool dense = false;
+  for (GroupHost& G : B->groups) dense = dense || !(B->model->hm.monomial && !G.g.dense);
+  std::vector<int> cl = {0, 4, 8, 12, 14, 16, 20, 24, 28, 32};
+  if (dense) cl = {0, 1, 2, 4, 8, 101, 102, 104, 108};
+  const int ncand = (int)cl.size();
+  const int* cands = cl.data();
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  const int saved = B->sync_warps;
-  int best = saved;
+  const int saved = B->sync_warps, saved_team = B->team;
+  int best = saved_team > 0 ? 100 + saved_team : saved;
   // two passes over the candidates, the second in reverse order, half the
   // proposals each: a drift of the chains' cost during tuning (expansion
   // orders still growing) then weighs on every candidate alike
-  float tot[ncand] = {0.f};
+  std::vector<float> tot(ncand, 0.f);
   int rc = CTHYB_OK;
   const long long half = std::max<long long>(1, nprop / 2);
   for (int pass = 0; pass < 2 && rc == CTHYB_OK; ++pass)
     for (int q = 0; q < ncand; ++q) {
       const int ci = pass == 0 ? q : ncand - 1 - q;
-      B->sync_warps = cands[ci];
+      B->team = cands[ci] >= 100 ? cands[ci] - 100 : 0;
+      B->sync_warps = cands[ci] >= 100 ? saved : cands[ci];
       cudaEventRecord(e0, B->stream);
       rc = issue_sweeps(B, half, false);
       if (rc) break;
@@ -5455,8 +5830,14 @@ int cthyb_batch_autotune(cthyb_batch_t B, int64_t nprop, int* best_out) {
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  B->sync_warps = rc ? saved : best;
-  if (best_out) *best_out = B->sync_warps;
+  if (rc) {
+    B->sync_warps = saved;
+    B->team = saved_team;
+  } else {
+    B->team = best >= 100 ? best - 100 : 0;
+    B->sync_warps = best >= 100 ? saved : best;
+  }
+  if (best_out) *best_out = B->team > 0 ? 100 + B->team : B->sync_warps;
   return rc;
 }
 
@@ -5540,7 +5921,10 @@ int cthyb_batch_results_extra(cthyb_batch_t B, int chain, double* gleg, double* 
   const int nf = hm.nf, nleg = G->g.nleg, nss = hm.nss, ns = hm.ns;
   const double cnt = (double)h.cnt_meas;
   const double ms = h.cnt_meas ? h.meas_sign / cnt : 0.0;
-  if (gleg && nleg > 0) {
+  if (gleg && nleg > 0 && G->g.offdiag) {
+    // MeasGtauRem_full fills GLeg_full only (CTQMC.F90:8561-8566)
+    std::fill(gleg, gleg + (size_t)nf * nleg, 0.0);
+  } else if (gleg && nleg > 0) {
     std::vector<double> raw((size_t)nf * nleg);
     CK(cudaMemcpy(raw.data(), base + G->g.o_gleg, raw.size() * 8, cudaMemcpyDeviceToHost));
     const double zs = h.cnt_meas ? -1.0 / (cnt * ms) : 0.0;
@@ -5682,6 +6066,8 @@ int cthyb_batch_group_sums(cthyb_batch_t B, int group, double* gsum, double* sig
   const int nt = G.g.ntau, nf = hm.nf, nbins = nf * nt;
   if ((int)B->red_host.size() < nbins + 2) {
     if (B->d_red) cudaFree(B->d_red);
+  if (B->d_order) cudaFree(B->d_order);
+  if (B->d_counter) cudaFree(B->d_counter);
     B->d_red = nullptr;
     CK(cudaMalloc(&B->d_red, (size_t)(nbins + 2) * 8));
     B->red_host.assign(nbins + 2, 0.0);
@@ -6040,6 +6426,24 @@ int cthyb_batch_refresh_minv(cthyb_batch_t B, int replace, double* maxdev) {
   return CTHYB_OK;
 }
 
+int cthyb_batch_log_weights_device(cthyb_batch_t B, double* lw_dev, void* stream) {
+  if (!B || !lw_dev) return fail(CTHYB_ERR_ARG, "null");
+  cudaStream_t st = stream ? (cudaStream_t)stream : B->stream;
+  if (st != B->stream) {  // after the batch's queued work
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    cudaError_t e = cudaEventRecord(ev, B->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ev, 0);
+    cudaEventDestroy(ev);
+    CK(e);
+  }
+  for (GroupHost& G : B->groups) {
+    k_log_weights<<<(G.desc.nchains + 127) / 128, 128, 0, st>>>(B->model->dm, G.g, lw_dev);
+    CK(cudaGetLastError());
+  }
+  return CTHYB_OK;
+}
+
 int cthyb_batch_chain_stats(cthyb_batch_t B, int group, double* out) {
   if (!B || !out || group < 0 || group >= (int)B->groups.size()) return fail(CTHYB_ERR_ARG, "bad arguments");
   GroupHost& G = B->groups[group];
@@ -6197,6 +6601,29 @@ int cthyb_batch_results_full(cthyb_batch_t B, int chain, double* gtau_full) {
   return CTHYB_OK;
 }
 
+int cthyb_batch_results_gleg_full(cthyb_batch_t B, int chain, double* gleg_full) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  if (!G->g.offdiag) return fail(CTHYB_ERR_ARG, "not an off-diagonal group");
+  if (!gleg_full) return fail(CTHYB_ERR_ARG, "null");
+  const int nf = B->model->hm.nf, nleg = G->g.nleg;
+  if (nleg <= 0) return CTHYB_OK;
+  Hdr h;
+  rc = read_hdr(B, G, c, h);
+  if (rc) return rc;
+  std::vector<double> raw((size_t)nf * nf * nleg);
+  CK(cudaMemcpy(raw.data(), G->g.base + (size_t)c * G->g.stride + G->g.o_gleg, raw.size() * 8,
+                cudaMemcpyDeviceToHost));
+  const double cnt = (double)h.cnt_meas, ms = h.cnt_meas ? h.meas_sign / cnt : 0.0;
+  const double zs = h.cnt_meas ? -1.0 / (cnt * ms) : 0.0;
+  // GLeg_full * sqrt(2l+1)/beta, then -GLeg_full * zScaling (CTQMC.F90:8766-8771)
+  for (size_t i = 0; i < raw.size(); ++i)
+    gleg_full[i] = -(raw[i] * std::sqrt(2.0 * (double)(i % nleg) + 1.0) / G->g.beta) * zs;
+  return CTHYB_OK;
+}
+
 int cthyb_batch_minv_full(cthyb_batch_t B, int chain, int* kout, double* out) {
   GroupHost* G;
   int c;
@@ -6295,11 +6722,6 @@ __global__ void __launch_bounds__(256) k_peak_dfma(double* out, int iters, doubl
 #pragma unroll
   for (int j = 0; j < 8; ++j) s += x[j];
   out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
-}
-__device__ __forceinline__ void dmma_884(double& d0, double& d1, double a, double b) {
-  asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
-               : "+d"(d0), "+d"(d1)
-               : "d"(a), "d"(b));
 }
 __global__ void __launch_bounds__(256) k_peak_dmma(double* out, int iters, double a, double b) {
   double c[8];

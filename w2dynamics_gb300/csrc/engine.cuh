@@ -81,6 +81,7 @@ struct DGroup {
   const double* hybr_full;            // offdiag: [f1][f2][nftau]
   size_t o_gfull;                     // offdiag: G for every flavour pair [f_a][f_c][ntau]
   int kcap, opcap, L, dense, meas_dm;
+  int dmma;            // dense blocks of >= 16 x 16 on the FP64 tensor cores (m8n8k4 MMA)
   int refresh_every;   // accepted pair updates between full rebuilds of M (0: never)
   char* base;          // chain c at base + c*stride
   size_t stride;

@@ -21,6 +21,7 @@ RECORD_DTYPE = np.dtype([
 
 FLAG_DENSE = 1
 FLAG_NO_DM = 2
+FLAG_DMMA = 4
 
 EXPORTS = (
     "cthyb_last_error", "cthyb_model_create", "cthyb_model_destroy", "cthyb_model_info",
@@ -28,11 +29,11 @@ EXPORTS = (
     "cthyb_batch_destroy",
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
-    "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_autotune", "cthyb_batch_results",
-    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_move_counters4", "cthyb_batch_results_full", "cthyb_batch_minv_full", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
+    "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_set_team", "cthyb_batch_autotune", "cthyb_batch_results",
+    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_move_counters4", "cthyb_batch_results_full", "cthyb_batch_results_gleg_full", "cthyb_batch_minv_full", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_set_configs", "cthyb_batch_get_configs", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
-    "cthyb_batch_drift", "cthyb_batch_chain_stats", "cthyb_batch_group_gtau_raw", "cthyb_probe_fp64",
+    "cthyb_batch_drift", "cthyb_batch_chain_stats", "cthyb_batch_group_gtau_raw", "cthyb_probe_fp64", "cthyb_batch_log_weights_device",
     "cthyb_minv_rebuild_noalloc",
 )
 
@@ -90,12 +91,14 @@ def load(build_if_missing=False):
     L.cthyb_batch_stream.argtypes = [vp, C.POINTER(vp)]
     L.cthyb_batch_use_graphs.argtypes = [vp, C.c_int]
     L.cthyb_batch_set_schedule.argtypes = [vp, C.c_int]
+    L.cthyb_batch_set_team.argtypes = [vp, C.c_int]
     L.cthyb_batch_autotune.argtypes = [vp, i64, C.POINTER(C.c_int)]
     L.cthyb_batch_results.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_move_counters.argtypes = [vp, C.c_int, C.POINTER(i64)]
     L.cthyb_batch_move_counters4.argtypes = [vp, C.c_int, C.POINTER(i64)]
     L.cthyb_batch_results_full.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_minv_full.argtypes = [vp, C.c_int, ip, dp]
+    L.cthyb_batch_results_gleg_full.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_results_extra.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp]
     L.cthyb_batch_gradients.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.cthyb_batch_results_score.argtypes = [vp, C.c_int, dp, dp]
@@ -112,6 +115,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_get_log.argtypes = [vp, C.c_int, C.c_void_p, C.POINTER(i64)]
     L.cthyb_batch_work_counters.argtypes = [vp, C.POINTER(i64), C.c_int]
     L.cthyb_probe_fp64.argtypes = [dp, dp]
+    L.cthyb_batch_log_weights_device.argtypes = [vp, vp, vp]
     L.cthyb_batch_chain_stats.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_group_gtau_raw.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_drift.argtypes = [vp, dp, dp, C.POINTER(i64), C.POINTER(i64), C.c_int]
@@ -194,7 +198,7 @@ class Group:
     def __init__(self, beta, ftau, ntau, nchains=1, seed0=0, seeds=None, taudiff_max=-1.0,
                  ncorr=100, p_outer=0.0, kcap=0, opcap=0, tree_levels=0, maxhisto=500,
                  dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0, score_dE=None,
-                 symmoves=None, p_4op=0.0, ftau_full=None, refresh_every=0):
+                 symmoves=None, p_4op=0.0, ftau_full=None, refresh_every=0, dmma=False):
         self.beta = float(beta)
         self.ftau = np.asfortranarray(np.asarray(ftau, np.float64))
         self.ntau = int(ntau)
@@ -215,7 +219,7 @@ class Group:
         self.symmoves = None if symmoves is None else np.ascontiguousarray(np.atleast_2d(symmoves), np.int32)
         self.kcap, self.opcap, self.tree_levels = int(kcap), int(opcap), int(tree_levels)
         self.maxhisto = int(maxhisto)
-        self.flags = (FLAG_DENSE if dense else 0) | (0 if measure_dm else FLAG_NO_DM)
+        self.flags = (FLAG_DENSE if dense else 0) | (0 if measure_dm else FLAG_NO_DM) | (FLAG_DMMA if dmma else 0)
         # accepted pair updates between full rebuilds of the inverse matrices
         # (0: the library default, negative: never)
         self.refresh_every = int(refresh_every)
@@ -296,9 +300,15 @@ class Batch:
         """-1: automatic; 0: independent warps; n (1..32): phase-synchronous blocks of n chains."""
         _check(load().cthyb_batch_set_schedule(self.h, int(warps_per_block)))
 
+    def set_team(self, warps_per_chain):
+        """0: off; T (1..8): team sweep, blocks of T warps per chain taken
+        from a cost-ordered queue (the warps share the dense-block trace)."""
+        _check(load().cthyb_batch_set_team(self.h, int(warps_per_chain)))
+
     def autotune(self, nprop):
         """Pick the fastest schedule on `nprop` warmup proposals per candidate;
-        returns the chosen warps per block (0: independent warps)."""
+        returns the chosen warps per block (0: independent warps) or 100 + T
+        for a team sweep of T warps per chain."""
         best = C.c_int()
         _check(load().cthyb_batch_autotune(self.h, int(nprop), C.byref(best)))
         return best.value
@@ -341,6 +351,12 @@ class Batch:
         npar = 0 if dE_dev is None else int(dE_dev.shape[0])
         _check(load().cthyb_batch_gradients_device(self.h, npar, ptr(dE_dev), ptr(grad_delta), ptr(grad_params),
                                                    ptr(log_weights), C.c_void_p(stream) if stream else None))
+
+    def log_weights_device(self, out, stream=None):
+        """log|det| and absolute log|trace| of every chain, (nchains, 2)
+        into a device tensor (or raw pointer); enqueued, not synchronised."""
+        ptr = C.c_void_p(out.data_ptr() if hasattr(out, "data_ptr") else int(out))
+        _check(load().cthyb_batch_log_weights_device(self.h, ptr, C.c_void_p(stream) if stream else None))
 
     def results_score(self, chain):
         """Score-function dG(tau)/dtheta (nscore, Nd, 2, Ntau) and <g> (nscore)."""
@@ -458,6 +474,15 @@ class Batch:
         out = np.zeros(nf * nf * g.ntau)
         _check(load().cthyb_batch_results_full(self.h, chain, _dp(out)))
         return out.reshape(nf, nf, g.ntau)
+
+    def results_gleg_full(self, chain):
+        """Off-diagonal groups: Legendre coefficients of G for every flavour
+        pair, (2Nd, 2Nd, nleg) indexed [f_annihilator, f_creator, l]."""
+        g = self.groups[self._group_of[chain]]
+        nf = 2 * self.model.nd
+        out = np.zeros(max(1, nf * nf * g.nleg))
+        _check(load().cthyb_batch_results_gleg_full(self.h, chain, _dp(out)))
+        return out[:nf * nf * g.nleg].reshape(nf, nf, g.nleg)
 
     def minv_full(self, chain):
         """Off-diagonal groups: the inverse matrix over all flavours in block

@@ -68,7 +68,14 @@ class _LogWeightFn:
 def LogWeight():
     """torch.autograd.Function: log_w = LogWeight().apply(ftau, theta, batch, dE)
     with ftau the (Nd, 2, Nftau) grid and theta the parameters the batch was
-    built with (their values are the batch's; they carry the gradient)."""
+    built with (their values are the batch's; they carry the gradient), dE
+    the (nparams, nstates) energy derivatives of the parameter directions
+    (numpy or torch, or None).  Everything runs on the device: the forward
+    value comes from the weights the chains carry
+    (cthyb_batch_log_weights_device, no kernel walk); the backward launches
+    the gradient kernel into device tensors (cthyb_batch_gradients_device)
+    only when a gradient is requested and contracts with grad_out on the
+    device.  Gradients are returned on the devices of ftau and theta."""
     if _LogWeightFn.cls is not None:
         return _LogWeightFn.cls
     torch = _torch()
@@ -76,16 +83,29 @@ def LogWeight():
     class Fn(torch.autograd.Function):
         @staticmethod
         def forward(ctx, ftau, theta, batch, dE):
-            gd, gp, lw = batch.gradients(dE)
-            ctx.save_for_backward(torch.as_tensor(gd, dtype=ftau.dtype), torch.as_tensor(gp, dtype=theta.dtype))
-            return torch.as_tensor(lw.sum(axis=1), dtype=ftau.dtype)
+            dev = torch.device("cuda")
+            lw = torch.empty((batch.nchains, 2), dtype=torch.float64, device=dev)
+            batch.log_weights_device(lw, stream=torch.cuda.current_stream().cuda_stream)
+            ctx.batch = batch
+            ctx.dE = None if dE is None else torch.as_tensor(dE, dtype=torch.float64).to(dev)
+            ctx.fshape, ctx.fdev, ctx.tdev = ftau.shape, ftau.device, theta.device
+            return lw.sum(dim=1).to(ftau.device, ftau.dtype)
 
         @staticmethod
         def backward(ctx, grad_out):
-            gd, gp = ctx.saved_tensors
-            g_f = (grad_out[:, None, None, None] * gd).sum(0)
-            g_t = (grad_out[:, None] * gp).sum(0)
-            return g_f, g_t, None, None
+            b, dE = ctx.batch, ctx.dE
+            dev = torch.device("cuda")
+            n = b.nchains
+            nf, nft = 2 * ctx.fshape[0], ctx.fshape[2]
+            npar = 0 if dE is None else int(dE.shape[0])
+            gd = torch.empty((n, nf, nft), dtype=torch.float64, device=dev)
+            gp = torch.empty((n, max(npar, 1)), dtype=torch.float64, device=dev)
+            lw = torch.empty((n, 2), dtype=torch.float64, device=dev)
+            b.gradients_device(dE, gd, gp if npar else None, lw, stream=torch.cuda.current_stream().cuda_stream)
+            go = grad_out.to(dev, torch.float64)
+            g_f = torch.einsum("c,cfj->fj", go, gd).reshape(ctx.fshape)
+            g_t = go @ gp[:, :npar] if npar else torch.zeros(0, dtype=torch.float64, device=dev)
+            return g_f.to(ctx.fdev), g_t.to(ctx.tdev), None, None
 
     _LogWeightFn.cls = Fn
     return Fn

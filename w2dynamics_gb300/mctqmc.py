@@ -206,7 +206,7 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
                     measure_dm=_int("MeasDensityMatrix", 1) != 0,
                     p_global=_real("PercentageGlobalMove", 0.0),
                     p_shift=_real("PercentageTauShiftMove", 0.0),
-                    nleg=0 if offdiag else _int("NLegMax", 100),
+                    nleg=_int("NLegMax", 100),
                     p_4op=_real("Percentage4OperatorMove", 0.0),
                     ftau_full=ftau_full if offdiag else None)
     nsym = _int("NSymMove", 0)
@@ -386,9 +386,16 @@ def _collect():
     gleg = sum(x["gleg"] * s for x, s in zip(ext, signs)) / wsum
     nleg = gleg.shape[-1]
     gleg_full = np.zeros((nd, 2, nd, 2, nleg))
-    for b in range(nd):
-        for s in range(2):
-            gleg_full[b, s, b, s] = gleg[b, s]
+    if _batch.groups[0].ftau_full is not None and nleg > 0:
+        # offdiag = 1: MeasGtauRem_full fills GLeg_full, GLeg stays zero
+        glf = sum(_batch.results_gleg_full(c) * s for c, s in zip(range(_nchains), signs)) / wsum
+        for fa in range(nf):
+            for fc in range(nf):
+                gleg_full[fa // 2, fa % 2, fc // 2, fc % 2] = glf[fa, fc]
+    else:
+        for b in range(nd):
+            for s in range(2):
+                gleg_full[b, s, b, s] = gleg[b, s]
     outersuperstatehisto = sum(x["outer_sst_histo"] for x in ext) / _nchains
     outerstatehisto = sum(x["outer_state_histo"] for x in ext) / _nchains
     with np.errstate(invalid="ignore", divide="ignore"):
