@@ -52,7 +52,8 @@ E2E_WARMUP = 1000    # re-thermalisation proposals of the warm-started end-to-en
 CPU_CHAINS_PER_CORE = 16  # chains per host core in the bounded CPU sample (beta cycling)
 ONE_CHAIN_BLOCKS, ONE_CHAIN_MEAS = 16, 30  # one-chain form: blocks x measurement cycles per beta
 # dense-block workload: 5-orbital Kanamori with spin-flip and pair hopping
-K5_BETA, K5_CHAINS, K5_THERM, K5_STEPS = 40.0, 1024, 2000, 2
+K5_BETA, K5_CHAINS, K5_THERM, K5_STEPS, K5_TUNE = 40.0, 1024, 2000, 2, 20
+K5_TUNE_PROPS = 9 * 2 * K5_TUNE  # the autotuner's dense-model candidates x 2 K5_TUNE proposals
 METRIC = "MC updates/sec on 1 GB300, batched vs one-chain form, at equal G(tau) error"
 PROFILE = os.path.join(ROOT, "profiles", "k_sweep_sync_bench_4096chains.md")
 
@@ -289,13 +290,16 @@ def run_k5(E, args, fp64_peak):
     from w2dynamics_gb300 import problems as P
     pr = P.config_problem("kanamori5", beta=K5_BETA)
     model = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
-    b = E.Batch(model, [E.Group(K5_BETA, pr["ftau"], pr["ntau"], nchains=K5_CHAINS, seed0=0, taudiff_max=-1.0,
+    nch = args.k5_chains
+    b = E.Batch(model, [E.Group(K5_BETA, pr["ftau"], pr["ntau"], nchains=nch, seed0=0, taudiff_max=-1.0,
                                 ncorr=NCORR, kcap=64, opcap=1024, tree_levels=4)])
-    b.warmup(K5_THERM)
+    b.set_team(8)
+    b.warmup(K5_THERM - K5_TUNE_PROPS)
+    sched = b.autotune(2 * K5_TUNE)  # its proposals are the rest of the thermalisation
     b.measure(1)
     b.sync()
     st = b.chain_stats(0)
-    outer = np.array([b.state(c)["outer_sst"] for c in range(K5_CHAINS)], int)
+    outer = np.array([b.state(c)["outer_sst"] for c in range(nch)], int)
     sizes = model.sst_size[outer]
     b.work_counters(reset=True)
     stream = torch.cuda.ExternalStream(b.stream())
@@ -308,13 +312,17 @@ def run_k5(E, args, fp64_peak):
     wc = b.work_counters()
     k_end = float(b.chain_stats(0)["noper"].mean())
     b.close()
-    value = K5_CHAINS * NCORR * K5_STEPS / (ms / 1e3)
+    value = nch * NCORR * K5_STEPS / (ms / 1e3)
     achieved = wc["trace_flops"] / (ms / 1e3) / 1e9
-    return {"workload": f"{K5_CHAINS} chains, 5-orbital Kanamori U=3 J=0.7 crystal field +-0.2, beta={K5_BETA}, "
+    return {"workload": f"{nch} chains, 5-orbital Kanamori U=3 J=0.7 crystal field +-0.2, beta={K5_BETA}, "
                         f"Ntau=Nftau=4000, Nt Szt blocks (largest 100), one window, NCorr={NCORR}, "
-                        f"{K5_THERM} thermalisation proposals (orders still growing), {K5_STEPS} timed steps",
+                        f"{K5_THERM} thermalisation proposals (the last {K5_TUNE_PROPS} of them the schedule "
+                        f"autotuner's; orders still growing), {K5_STEPS} timed steps",
             "value": value, "unit": "MC updates/s", "ms_per_step": ms / K5_STEPS,
             "mean_order": [float(st["noper"].mean()), k_end],
+            "schedule": {"autotuner_choice": sched,
+                         "meaning": "100 + T + 1000 x blocks per SM: team sweep of T warps per chain"
+                                    if sched >= 100 else "phase-synchronous warps per block"},
             "outer_superstate_sizes": {int(k): int(v) for k, v in zip(*np.unique(sizes, return_counts=True))},
             "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "GFLOP/s",
                          "frac": achieved / fp64_peak,
@@ -607,6 +615,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--chains-per-beta", type=int, default=CHAINS_PER_BETA)
     ap.add_argument("--skip-k5", action="store_true", help="leave out the dense-block (5-orbital) line")
+    ap.add_argument("--k5-chains", type=int, default=K5_CHAINS, help="chains of the dense-block line")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

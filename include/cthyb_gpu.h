@@ -154,22 +154,25 @@ int cthyb_batch_use_graphs(cthyb_batch_t batch, int on);
  * phase-synchronous blocks of n chains whose proposals advance phase by
  * phase together.  Per-chain results do not depend on the schedule. */
 int cthyb_batch_set_schedule(cthyb_batch_t batch, int warps_per_block);
-/* Team sweep (no reference counterpart): 0 = off (the schedule of
- * cthyb_batch_set_schedule); T in 1..8 = blocks of T warps, each advancing
- * one chain at a time, chains taken from a cost-ordered queue (largest
- * operators x outer-superstate size first) as blocks become free; the T
- * warps evaluate the dense-block trace together.  Per-chain results do not
- * depend on it.  cthyb_batch_set_schedule switches it off. */
-int cthyb_batch_set_team(cthyb_batch_t batch, int warps_per_chain);
+/* Team sweep (no reference counterpart): warps_per_chain 0 = off (the
+ * schedule of cthyb_batch_set_schedule); T in 1..16 = blocks of T warps,
+ * each advancing one chain at a time, chains taken from a cost-ordered
+ * queue (largest operators x outer-superstate size first) as blocks become
+ * free; the T warps evaluate the dense-block trace together.
+ * blocks_per_sm bounds the resident blocks per multiprocessor (0: as many
+ * as fit), so that blocks take several chains each from the queue.
+ * Per-chain results do not depend on it.  cthyb_batch_set_schedule
+ * switches it off. */
+int cthyb_batch_set_team(cthyb_batch_t batch, int warps_per_chain, int blocks_per_sm);
 /* Time `nprop` warmup proposals per chain under each schedule
  * (independent warps; phase-synchronous blocks of 4..32 chains; for
  * dense-block models phase-synchronous blocks of 1..8 chains and team
- * sweeps of 1..8 warps per chain), in two interleaved passes (forward,
+ * sweeps of 4..16 warps per chain), in two interleaved passes (forward,
  * then reverse order) of nprop/2 each, and keep the fastest; the proposals
  * are real warmup steps of the chains (no reference counterpart), so call
  * it after thermalisation.  *best receives the choice: warps per block of
- * the phase-synchronous schedule (0: independent warps) or 100 + T for a
- * team sweep of T warps per chain. */
+ * the phase-synchronous schedule (0: independent warps) or
+ * 100 + T + 1000 x blocks_per_sm for a team sweep. */
 int cthyb_batch_autotune(cthyb_batch_t batch, int64_t nprop, int* best);
 
 /* The remaining Z-space estimators of one chain, normalised as in
@@ -183,6 +186,15 @@ int cthyb_batch_results_extra(cthyb_batch_t batch, int chain, double* gleg, doub
                               double* outer_state_histo, double* sign_sst, double* sign_state,
                               double* contrib_sst, double* contrib_state);
 
+/* Hamiltonian directions theta_p for the trace gradients of dense-block
+ * models (no reference counterpart): dH/dtheta_p = sum dmuimp_p c+c +
+ * 1/2 sum dU_p c+c+cc, the operator strings of the local Hamiltonian
+ * (Operator.F90:482-546, 1042-1108); dumatrix: nparams x (2Nd)^4, each in
+ * the layout of cthyb_model_create's umatrix, dmuimp: nparams x
+ * (Nd,2,Nd,2) Fortran order (either may be NULL).  Stored in the model as
+ * blocks in the eigenbasis of each superstate; nparams <= 32, 0 clears. */
+int cthyb_model_set_directions(cthyb_model_t model, int nparams, const double* dumatrix, const double* dmuimp);
+
 /* Per-configuration gradients of log|w| = log|det H| + log|trace| of every
  * chain's current configuration (no reference counterpart: the reference
  * has no derivatives).
@@ -190,9 +202,13 @@ int cthyb_batch_results_extra(cthyb_batch_t batch, int chain, double* gleg, doub
  *               d log|det H| / d F(b, s, tau_j), F entering H through the
  *               linear interpolation of get_HybrF (Trace.F90:1014-1033);
  *   grad_params (nchains, nparams): d log|trace| / d theta_p for parameter
- *               directions given by per-eigenstate energy derivatives
- *               dE (nparams x nstates, row-major, p slowest) -- monomial
- *               (density-density) models only, nparams <= 32;
+ *               directions given, for monomial (density-density) models,
+ *               by per-eigenstate energy derivatives dE (nparams x
+ *               nstates, row-major, p slowest); for dense-block models
+ *               dE = NULL and the directions of cthyb_model_set_directions
+ *               (exact derivative of each segment propagator in the
+ *               eigenbasis, adjoint sweep from the checkpoints);
+ *               nparams <= 32;
  *   log_weights (nchains, 2): log|det H| and the absolute log|trace|
  *               (energies not shifted by the ground-state energy).
  * grad_params/dE may be NULL with nparams = 0. */
@@ -219,7 +235,11 @@ int cthyb_batch_log_weights_device(cthyb_batch_t batch, double* lw_dev, void* st
  * directions (nscore > 0): dgtau (nscore, Nd, 2, Ntau), each direction in
  * Fortran order, = <G g_p> - <G><g_p> with g_p = d log|trace| / dtheta_p of
  * the measured configuration, normalised like G(tau); mean_score (nscore)
- * = <g_p>.  Assumes a sign-free model (configuration sign constant). */
+ * = <g_p>.  Averages over this chain's measurements: for an estimate over
+ * several chains combine <G g_p> = dgtau + G <g_p> and G, <g_p> of every
+ * chain before subtracting (the covariance of the chains' means belongs to
+ * the derivative).  Assumes a sign-free model (configuration sign
+ * constant). */
 int cthyb_batch_results_score(cthyb_batch_t batch, int chain, double* dgtau, double* mean_score);
 
 /* Global and tau-shift move counters of one chain since the last warmup or

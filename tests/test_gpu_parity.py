@@ -564,18 +564,21 @@ def _diag_of(ff):
     return np.stack([np.stack([ff[b, s, b, s] for s in range(2)]) for b in range(nd)])
 
 
-@pytest.mark.parametrize("kind,tdm,pout,nprop,seed,prare", [("spin", 1.5, 0.1, 20000, 5, 0.0),
-                                                            ("spin", -1.0, 0.0, 10000, 9, 0.0),
-                                                            ("orbital", -1.0, 0.1, 6000, 6, 0.0),
-                                                            ("orbital", 1.0, 0.1, 6000, 8, 0.0),
-                                                            ("spin", 1.5, 0.1, 12000, 11, 0.05),
-                                                            ("orbital", -1.0, 0.1, 6000, 12, 0.05)])
-def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, nprop, seed, prare):
+@pytest.mark.parametrize("kind,tdm,pout,nprop,seed,prare,p4", [("spin", 1.5, 0.1, 20000, 5, 0.0, 0.0),
+                                                               ("spin", -1.0, 0.0, 10000, 9, 0.0, 0.0),
+                                                               ("orbital", -1.0, 0.1, 6000, 6, 0.0, 0.0),
+                                                               ("orbital", 1.0, 0.1, 6000, 8, 0.0, 0.0),
+                                                               ("spin", 1.5, 0.1, 12000, 11, 0.05, 0.0),
+                                                               ("orbital", -1.0, 0.1, 6000, 12, 0.05, 0.0),
+                                                               ("spin", 1.5, 0.1, 12000, 21, 0.02, 0.3),
+                                                               ("orbital", -1.0, 0.1, 6000, 22, 0.02, 0.3)])
+def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, nprop, seed, prare, p4):
     """Off-diagonal hybridisation (offdiag = 1): the GPU chain proposes,
     decides and updates like the oracle chain of the same seed, proposal by
     proposal (flavours, block positions, pair counts, outcomes bit-exact;
     ratios to 1e-10), with global and tau-shift moves at prare each where
-    given; then the measured G for every flavour pair and its Legendre
+    given and 4-operator moves at p4; then the measured G for every flavour
+    pair and its Legendre
     coefficients (GLeg_full), the order histogram and the sign agree, and
     so do the final configuration and the inverse matrix over all
     flavours."""
@@ -583,14 +586,14 @@ def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, np
     ntau = 10
     mo = O.Model(nd, um, muimp, qns)
     co = O.Chain(mo, beta, ff, ntau, seed=seed, taudiff_max=tdm, p_outer=pout, ncorr=20, maxhisto=30,
-                 p_global=prare, p_shift=prare, nleg=6)
+                 p_global=prare, p_shift=prare, nleg=6, p_4op=p4)
     co.start_log(nprop)
     co.warmup(nprop)
     ref = co.log()
     mg = E.Model(nd, um, muimp, qns)
     b = E.Batch(mg, [E.Group(beta, _diag_of(ff), ntau, nchains=1, seed0=seed, taudiff_max=tdm,
                              p_outer=pout, ncorr=20, maxhisto=30, kcap=64, opcap=256,
-                             ftau_full=ff, p_global=prare, p_shift=prare, nleg=6)])
+                             ftau_full=ff, p_global=prare, p_shift=prare, nleg=6, p_4op=p4)])
     b.set_log(nprop)
     b.warmup(nprop)
     b.sync()
@@ -600,6 +603,9 @@ def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, np
     if prare > 0:
         for mv in (2, 3):
             assert np.sum((ref["outcome"] == 4) & (ref["move"] == mv)) > 5
+    if p4 > 0:  # 4-operator moves with off-diagonal F (CTQMC.F90:3647-3651, 3822-3827, 4352-4357)
+        for mv in (5, 6):
+            assert np.sum((ref["outcome"] == 4) & (ref["move"] == mv)) > 5, mv
     co.measure(300)
     b.measure(300)
     b.sync()

@@ -36,6 +36,7 @@ def _oracle_log(name, beta, qns, tdm, ntau, nprop, seed, moves):
 
 @pytest.mark.parametrize("name,beta,qns,tdm,nprop,seeds,team,dmma,moves", [
     ("kanamori5", 40.0, None, -1.0, 600, [0], 4, False, {}),          # 100-state outer superstate
+    ("kanamori5", 40.0, None, -1.0, 600, [0], 16, False, {}),
     ("kanamori5", 40.0, None, -1.0, 600, [0], 4, True, {}),
     ("kanamori5", 40.0, None, -1.0, 600, [7, 4, 0], 2, True, {}),     # three chains, 50/5/100 states
     ("kanamori5", 40.0, None, -1.0, 600, [7], 0, True, {}),           # MMA blocks, one-warp sweep
@@ -86,3 +87,29 @@ def test_team_sweep_measurements_match_the_warp_sweep(lib):
         assert ra["mean_sign"] == rb["mean_sign"]
         assert np.allclose(ra["gtau"], rb["gtau"], rtol=1e-9, atol=1e-12)
         assert np.allclose(ra["densitymatrix"], rb["densitymatrix"], rtol=1e-8, atol=1e-12)
+
+
+def test_team_blocks_take_several_chains_from_the_queue(lib):
+    """More chains than resident team blocks (one block per multiprocessor):
+    blocks take further chains from the cost-ordered queue; every chain
+    ends exactly where the phase-synchronous sweep leaves it."""
+    pr = P.config_problem("kanamori5", beta=4.0)
+    mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    n = 400
+    out = []
+    for team in (0, 8):
+        b = E.Batch(mg, [E.Group(4.0, pr["ftau"], 20, nchains=n, seed0=1000, taudiff_max=-1.0, kcap=32,
+                                 opcap=256, tree_levels=2)])
+        if team:
+            b.set_team(team, 1)
+        b.warmup(300)
+        b.measure(2)
+        b.sync()
+        out.append((b.get_configs(), [b.results(c)["mean_sign"] for c in range(n)],
+                    b.group_gtau(0)))
+        b.close()
+    (ca, sa, ga), (cb, sb, gb) = out
+    for x, y in zip(ca, cb):
+        assert np.array_equal(x, y)
+    assert sa == sb
+    assert np.allclose(ga, gb, rtol=1e-9, atol=1e-12, equal_nan=True)  # NaN: chains with zero sign sum

@@ -293,8 +293,11 @@ def test_gradients_100_configurations_beta50():
 @pytest.mark.gpu
 def test_score_function_dG_dU_three_orbital():
     """dG(tau)/dU of the 3-orbital model (beta = 50, 2048 chains) from the
-    score-function estimator against central differences of G(tau) from
-    independent runs at U +- 0.05."""
+    score-function estimator <G g> - <G><g> over all measurements of all
+    chains (per-chain covariances alone would drop the covariance between
+    the chains' means, which is large where a chain keeps its sector for a
+    long time) against central differences of G(tau) from independent runs
+    at U +- 0.05."""
     from w2dynamics_gb300 import engine as E
     beta, nd, u0, j, du, n, nt = 50.0, 3, 4.0, 0.6, 0.05, 2048, 8
     pr = P.config_problem("dd3", beta=beta)
@@ -309,19 +312,29 @@ def test_score_function_dG_dU_three_orbital():
         b.measure(400)
         b.sync()
         G = b.group_gtau(0).reshape(n, 2 * nd, nt).mean(axis=1)  # average over the degenerate flavours
-        dG = None
-        if score:
-            # results_score: (nscore, Nd, 2, Ntau); average over the flavours
-            dG = np.array([b.results_score(c)[0][0].reshape(2 * nd, nt).mean(axis=0) for c in range(n)])
-        return G, dG
+        if not score:
+            return G, None, None
+        # per chain: the within-chain covariance <G g>_c - <G>_c <g>_c and <g>_c
+        sc = [b.results_score(c) for c in range(n)]
+        cov = np.array([x[0][0].reshape(2 * nd, nt).mean(axis=0) for x in sc])
+        g = np.array([x[1][0] for x in sc])
+        return G, cov + G * g[:, None], g  # <G g>_c
 
-    _, dG = run(u0, 0, True)
-    Gp, _ = run(u0 + du, 10000, False)
-    Gm, _ = run(u0 - du, 20000, False)
+    G0, Gg, g = run(u0, 0, True)
+    Gp, _, _ = run(u0 + du, 10000, False)
+    Gm, _, _ = run(u0 - du, 20000, False)
     fd = (Gp.mean(0) - Gm.mean(0)) / (2 * du)
     efd = np.sqrt(Gp.var(0, ddof=1) / n + Gm.var(0, ddof=1) / n) / (2 * du)
-    sf = dG.mean(0)
-    esf = dG.std(0, ddof=1) / np.sqrt(n)
+
+    # the score-function estimate over all measurements of all chains (equal
+    # measurement counts): <G g> - <G><g>, which keeps the between-chain
+    # covariance; error by jackknife over the chains
+    def est(sel):
+        return Gg[sel].mean(0) - G0[sel].mean(0) * g[sel].mean()
+
+    sf = est(np.ones(n, bool))
+    jk = np.array([est(np.arange(n) != c) for c in range(n)])
+    esf = np.sqrt((n - 1) / n * ((jk - jk.mean(0)) ** 2).sum(0))
     z = (sf - fd) / np.sqrt(efd ** 2 + esf ** 2)
     print(f"\ndG/dU 3-orbital: score {sf}, finite differences {fd}, z {z}")
     assert np.abs(z).max() < 4.0, (z, sf, fd)
@@ -355,3 +368,59 @@ def test_device_log_weight_function():
     assert ftau.grad.is_cuda and theta.grad.is_cuda
     assert np.allclose(ftau.grad.cpu().numpy(), np.tensordot(w, gd, axes=1), rtol=1e-10, atol=1e-12)
     assert np.allclose(theta.grad.cpu().numpy(), w @ gp, rtol=1e-10, atol=1e-12)
+
+
+def _kan3(u, j):
+    return P.flat_umatrix(P.umatrix_kanamori(3, u, u - 2 * j, j))
+
+
+@pytest.mark.gpu
+def test_dense_block_trace_gradients_against_dense_reference():
+    """Dense-block models (3-orbital Kanamori with spin flip and pair
+    hopping, "Nt Szt" blocks): the adjoint trace gradient along U, J and
+    one level eps_0 (directions set on the model as dU / dmuimp) equals the
+    dense Frechet-expm reference on every chain, and central differences of
+    the oracle's full trace on two of them."""
+    from w2dynamics_gb300 import engine as E
+    beta, nd, u, j = 10.0, 3, 4.0, 0.6
+    muimp = P.muimp_solver(nd, 3.0)
+    ft = P.semicircle_ftau(nd, beta, 1.0, 1000)
+    mg = E.Model(nd, _kan3(u, j), muimp, "Nt Szt")
+    assert not mg.monomial
+    d_eps = np.zeros((nd, 2, nd, 2))
+    d_eps[0, 0, 0, 0] = 1.0
+    dirs_u = [_kan3(1.0, 0.0), _kan3(0.0, 1.0), np.zeros((6,) * 4)]
+    dirs_mu = [np.zeros((nd, 2, nd, 2)), np.zeros((nd, 2, nd, 2)), d_eps]
+    mg.set_directions(dirs_u, dirs_mu)
+    n = 8
+    b = E.Batch(mg, [E.Group(beta, ft, 20, nchains=n, seed0=60, taudiff_max=-1.0, kcap=64, opcap=512,
+                             tree_levels=3)])
+    b.warmup(3000)
+    b.sync()
+    gd, gp, lw = b.gradients()
+    assert gp.shape == (n, 3)
+    occ_fock, _ = mg.basis()
+    C = DR.fock_operators(nd, occ_fock)
+    H = DR.hamiltonian(nd, _kan3(u, j), muimp, C)
+    V = [DR.hamiltonian(nd, du, dm, C) for du, dm in zip(dirs_u, dirs_mu)]
+    worst = 0.0
+    for ch in range(n):
+        taus, orbs, spins, cas, outer = b.get_config(ch)
+        states = np.arange(mg.sst_offset[outer], mg.sst_offset[outer] + mg.sst_size[outer])
+        lt, gt = DR.logtrace_and_grad(H, V, C, beta, taus, orbs, spins, cas, states)
+        assert abs(lt - lw[ch, 1]) < 1e-9 * max(1.0, abs(lt)), (ch, lt, lw[ch, 1])
+        err = np.abs(gt - gp[ch]).max() / max(1.0, np.abs(gt).max())
+        worst = max(worst, err)
+        assert err < 1e-8, (ch, gt, gp[ch])
+    print(f"\ndense-block trace gradients: worst relative error against the dense reference {worst:.2e}")
+    h = 1e-6
+    for ch in (0, 5):
+        cfg = b.get_config(ch)
+        for p, (du, dj) in enumerate([(1, 0), (0, 1)]):
+            def tr(sig):
+                mo = O.Model(nd, _kan3(u + sig * h * du, j + sig * h * dj), muimp, "Nt Szt")
+                co = O.Chain(mo, beta, ft, 20, seed=1, taudiff_max=beta)
+                co.set_config(*cfg[:4], cfg[4])
+                return co.full_trace()[0] - beta * mo.egs
+            fd = (tr(1) - tr(-1)) / (2 * h)
+            assert abs(fd - gp[ch, p]) < 1e-5 * max(1.0, abs(fd)), (ch, p, fd, gp[ch, p])

@@ -41,8 +41,7 @@ def test_parameter_string_rules():
 
 
 @pytest.mark.parametrize("key,val", [("flavourchange_moves", 1), ("segment", 1),
-                                     ("PercentageWormInsert", 0.1),
-                                     ("offdiag", 1), ("statesampling", 1)])
+                                     ("PercentageWormInsert", 0.1), ("statesampling", 1)])
 def test_unsupported_modes_are_rejected(key, val):
     ctqmc.init_paras(pstring(dict(BASE, **{key: val})))
     with pytest.raises(NotImplementedError, match=key):
@@ -56,8 +55,8 @@ def test_supported_configuration_passes_the_check():
     ctqmc.dest_paras()
 
 
-def test_offdiag_with_global_and_shift_moves_passes_the_check():
-    ctqmc.init_paras(pstring(dict(BASE, offdiag=1, Percentage4OperatorMove=0.0)))
+def test_offdiag_with_global_shift_and_four_operator_moves_passes_the_check():
+    ctqmc.init_paras(pstring(dict(BASE, offdiag=1, Percentage4OperatorMove=0.1)))
     ctqmc._check_supported()
     ctqmc.dest_paras()
 

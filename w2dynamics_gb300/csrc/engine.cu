@@ -2686,6 +2686,12 @@ __device__ NOINL void ph_shift(Ctx& c, Prop& p) {
 // Removable pairs of the operator arrays (time order, K entries) without the
 // entries skip[0..3] (-1: unused) (ensure_valid_NPairs_diag,
 // Trace.F90:1762-1803, on the list without them).
+// A creator/annihilator pair of codes cx, cy: opposite kinds, and the same
+// flavour unless the hybridisation is off-diagonal (is_rempair_diag /
+// is_rempair_offdiag, Trace.F90:1994-2030).
+__device__ __forceinline__ bool pair_codes(const Ctx& c, int cx, int cy) {
+  return ((cx & 1) != (cy & 1)) && (c.g->offdiag || (cx >> 1) == (cy >> 1));
+}
 __device__ NOINL int count_pairs_skip(Ctx& c, const double* tau, const int* code, int K, const int* skip) {
   const Hdr& h = *c.h;
   const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
@@ -2700,7 +2706,7 @@ __device__ NOINL int count_pairs_skip(Ctx& c, const double* tau, const int* code
       if (tau[j] > hi) break;
       if (j == skip[0] || j == skip[1] || j == skip[2] || j == skip[3]) continue;
       const int cy = code[j];
-      tot += ((cy >> 1) == (cx >> 1)) && ((cy & 1) != (cx & 1));
+      tot += pair_codes(c, cx, cy);
     }
   }
   return wsumi(tot);
@@ -2725,7 +2731,7 @@ __device__ NOINL bool select_pair_skip(Ctx& c, const double* tau, const int* cod
         if (tau[j] > hi) break;
         if (j == skip[0] || j == skip[1] || j == skip[2] || j == skip[3]) continue;
         const int cy = code[j];
-        cnt += ((cy >> 1) == (cx >> 1)) && ((cy & 1) != (cx & 1));
+        cnt += pair_codes(c, cx, cy);
       }
     }
     int cum = cnt;
@@ -2748,7 +2754,7 @@ __device__ NOINL bool select_pair_skip(Ctx& c, const double* tau, const int* cod
           if (tau[j] > hi) break;
           if (j == skip[0] || j == skip[1] || j == skip[2] || j == skip[3]) continue;
           const int cy = code[j];
-          if (((cy >> 1) == (cx >> 1)) && ((cy & 1) != (cx & 1)) && --want <= 0) {
+          if (pair_codes(c, cx, cy) && --want <= 0) {
             jy = j;
             break;
           }
@@ -2763,9 +2769,9 @@ __device__ NOINL bool select_pair_skip(Ctx& c, const double* tau, const int* cod
   return false;
 }
 
-// is_rempair_diag (Trace.F90:2006-2030) for (time, code) operators.
-__device__ __forceinline__ bool rempair4(const Hdr& h, double tx, int cx, double ty, int cy) {
-  return (cx >> 1) == (cy >> 1) && (cx & 1) != (cy & 1) && tx >= h.tauwin_min && tx <= h.tauwin_max &&
+// is_rempair (Trace.F90:1994-2030) for (time, code) operators.
+__device__ __forceinline__ bool rempair4(const Ctx& c, const Hdr& h, double tx, int cx, double ty, int cy) {
+  return pair_codes(c, cx, cy) && tx >= h.tauwin_min && tx <= h.tauwin_max &&
          ty >= h.tauwin_min && ty <= h.tauwin_max && fabs(__dsub_rn(tx, ty)) <= h.taudiff_max;
 }
 
@@ -2892,6 +2898,58 @@ __device__ NOINL int rebuild4_decide(Ctx& c, int fa, int fb, double factor, int 
   return 3;
 }
 
+// The same for off-diagonal hybridisation: the full matrix of the proposed
+// arrays in block order inverted by Gauss-Jordan, DetRat = DetNew / Det
+// (full_rebuild of StepAdd4 / StepRem4 with get_FullHybr_offdiag,
+// CTQMC.F90:3822-3827, 4352-4357), the trace from the rebuilt tree, the
+// Metropolis draw, installation or the old arrays back.
+__device__ NOINL bool od_full_inverse(Ctx& c, int K, double& dlog, double& dsign);
+__device__ NOINL void od_trace(Ctx& c, int s0, double& lg, double& sg);
+__device__ NOINL int count_pairs_od(Ctx& c);
+__device__ NOINL void od_restore(Ctx& c, int K);
+__device__ NOINL void od_accept(Ctx& c, double det_lg, double det_sg, double tr_lg, double tr_sg, int new_outer,
+                                int np_new);
+__device__ NOINL int rebuild4_decide_od(Ctx& c, double factor, int K_old, int np_new) {
+  Hdr& h = *c.h;
+  cthyb_record& r = *c.rec;
+  const int K = h.K, k = K / 2, ld = c.kcap;
+  double dlog = 0.0, dsign = 1.0;
+  const bool singular = !od_full_inverse(c, K, dlog, dsign);
+  double* Mn = glob_minv(c);  // the new inverse (the trace below reuses the dense work space)
+  const double* I = c.dense + (size_t)ld * ld;
+  for (int e = c.lane; e < k * k && !singular; e += 32) {
+    const size_t idx = (size_t)(e / k) * ld + (e % k);
+    Mn[idx] = I[idx];
+  }
+  __syncwarp();
+  const double det_lg = singular ? -DHUGE : dlog - h.det_log;
+  const double det_sg = singular ? 0.0 : dsign * h.det_sign;
+  double tr_lg = -DHUGE, tr_sg = 0.0, prob = 0.0;
+  if (!singular) {
+    od_trace(c, h.outer_sst, tr_lg, tr_sg);
+    prob = fabs(__dmul_rn(factor, exp(__dsub_rn(tr_lg, h.trace_log) + det_lg)));
+  }
+  const double rnd = grnd(c);
+  r.det_log = det_lg;
+  r.det_sign = det_sg;
+  r.tr_log = tr_lg;
+  r.tr_sign = tr_sg;
+  r.prob = prob;
+  r.rand = rnd;
+  if (rnd < prob) {
+    double* Mw = M_ptr(c, 0);
+    for (int e = c.lane; e < k * k; e += 32) {
+      const size_t idx = (size_t)(e / k) * ld + (e % k);
+      Mw[idx] = Mn[idx];
+    }
+    __syncwarp();
+    od_accept(c, det_lg, det_sg, tr_lg, tr_sg, h.outer_sst, np_new);
+    return 4;
+  }
+  od_restore(c, K_old);
+  return 3;
+}
+
 // StepAdd4, CTQMC.F90:3615-3890.
 __device__ NOINL void ph_add4(Ctx& c, Prop& p) {
   Hdr& h = *c.h;
@@ -2917,11 +2975,17 @@ __device__ NOINL void ph_add4(Ctx& c, Prop& p) {
     const double tcr = __dadd_rn(tmin, __dmul_rn(w2, grnd(c)));
     tdf = __dmul_rn(tdf, w2);
     const int f = 2 * (orb - 1) + (spin - 1);
+    int fcr = f;  // the creator's flavour: drawn as well with off-diagonal hybridisation
+    if (c.g->offdiag) {
+      const int orb_c = randint(c, 1, m.nd);
+      const int spin_c = randint(c, 1, 2);
+      fcr = 2 * (orb_c - 1) + (spin_c - 1);
+    }
     const bool afirst = tref < tcr;
     nt[2 * pr] = afirst ? tref : tcr;
-    nc[2 * pr] = 2 * f + (afirst ? 1 : 0);
+    nc[2 * pr] = afirst ? 2 * f + 1 : 2 * fcr;
     nt[2 * pr + 1] = afirst ? tcr : tref;
-    nc[2 * pr + 1] = 2 * f + (afirst ? 0 : 1);
+    nc[2 * pr + 1] = afirst ? 2 * fcr : 2 * f + 1;
   }
   const int fa = nc[0] >> 1, fb = nc[2] >> 1;
   r.orb = fa + 1;
@@ -2929,7 +2993,8 @@ __device__ NOINL void ph_add4(Ctx& c, Prop& p) {
   r.tau_c = nt[0];
   r.tau_a = nt[1];
   const int dk = fa == fb ? 2 : 1;
-  if (K + 4 > c.g->opcap || h.k[fa] + dk > c.kcap || h.k[fb] + dk > c.kcap) {
+  if (K + 4 > c.g->opcap ||
+      (c.g->offdiag ? K / 2 + 2 > c.kcap : (h.k[fa] + dk > c.kcap || h.k[fb] + dk > c.kcap))) {
     set_status(c, ST_CAPACITY);
     return;
   }
@@ -2942,7 +3007,7 @@ __device__ NOINL void ph_add4(Ctx& c, Prop& p) {
   }
   equal = __any_sync(FULL, equal);
   if (h.npairs == -1) {  // ensure_valid_NPairs
-    const int np = count_npairs(c);
+    const int np = c.g->offdiag ? count_pairs_od(c) : count_npairs(c);
     if (c.lane == 0) h.npairs = np;
     __syncwarp();
   }
@@ -2989,7 +3054,7 @@ __device__ NOINL void ph_add4(Ctx& c, Prop& p) {
   const int np_all = count_pairs_skip(c, c.optau, c.opcode, Kn, none);
   double rf;
   int branch = 0;
-  if (rempair4(h, nt[0], nc[0], nt[3], nc[3]) && rempair4(h, nt[1], nc[1], nt[2], nc[2])) {
+  if (rempair4(c, h, nt[0], nc[0], nt[3], nc[3]) && rempair4(c, h, nt[1], nc[1], nt[2], nc[2])) {
     branch = 1;
     const int sa[4] = {q[0], q[3], -1, -1}, sb[4] = {q[1], q[2], -1, -1};
     const int np_23 = count_pairs_skip(c, c.optau, c.opcode, Kn, sa);
@@ -2999,7 +3064,7 @@ __device__ NOINL void ph_add4(Ctx& c, Prop& p) {
                                        __ddiv_rn(1.0, (double)np_14)),
                              __ddiv_rn(1.0, (double)np_23)));
     tdf = __ddiv_rn(tdf, 4.0);
-  } else if (rempair4(h, nt[0], nc[0], nt[2], nc[2]) && rempair4(h, nt[1], nc[1], nt[3], nc[3])) {
+  } else if (rempair4(c, h, nt[0], nc[0], nt[2], nc[2]) && rempair4(c, h, nt[1], nc[1], nt[3], nc[3])) {
     branch = 2;
     const int sa[4] = {q[0], q[2], -1, -1}, sb[4] = {q[1], q[3], -1, -1};
     const int np_23 = count_pairs_skip(c, c.optau, c.opcode, Kn, sa);
@@ -3033,9 +3098,13 @@ __device__ NOINL void ph_add4(Ctx& c, Prop& p) {
     __syncwarp();
     return;
   }
-  const double n2 = 2.0 * m.nd;  // taudiff_factor * (2 NBands)**2 * rempair_factor, left to right
-  const double factor = __dmul_rn(__dmul_rn(tdf, __dmul_rn(n2, n2)), rf);
-  r.outcome = rebuild4_decide(c, fa, fb, factor, K, np_all);
+  // taudiff_factor * (2 NBands)**2 * rempair_factor, left to right; (2
+  // NBands)**4 with off-diagonal hybridisation (both flavours of both pairs
+  // drawn, CTQMC.F90:3822-3827)
+  const double n2 = 2.0 * m.nd;
+  const double fl = c.g->offdiag ? __dmul_rn(__dmul_rn(__dmul_rn(n2, n2), n2), n2) : __dmul_rn(n2, n2);
+  const double factor = __dmul_rn(__dmul_rn(tdf, fl), rf);
+  r.outcome = c.g->offdiag ? rebuild4_decide_od(c, factor, K, np_all) : rebuild4_decide(c, fa, fb, factor, K, np_all);
   if (r.outcome == 4 && c.lane == 0) h.acc_add4++;
   r.outer_sst = h.outer_sst;
   r.k_total = h.K;
@@ -3051,7 +3120,7 @@ __device__ NOINL void ph_rem4(Ctx& c, Prop& p) {
   __syncwarp();
   const int K = h.K;
   if (h.npairs == -1) {
-    const int np = count_npairs(c);
+    const int np = c.g->offdiag ? count_pairs_od(c) : count_npairs(c);
     if (c.lane == 0) h.npairs = np;
     __syncwarp();
   }
@@ -3090,7 +3159,7 @@ __device__ NOINL void ph_rem4(Ctx& c, Prop& p) {
   const int np_12 = count_pairs_skip(c, c.optau, c.opcode, K, sB);
   double rf;
   int branch = 0;
-  if (rempair4(h, ta1, ca1, tb2, cb2) && rempair4(h, ta2, ca2, tb1, cb1)) {
+  if (rempair4(c, h, ta1, ca1, tb2, cb2) && rempair4(c, h, ta2, ca2, tb1, cb1)) {
     branch = 1;
     const int sa[4] = {a1, b2, -1, -1}, sb[4] = {a2, b1, -1, -1};
     const int np_23 = count_pairs_skip(c, c.optau, c.opcode, K, sa);
@@ -3100,7 +3169,7 @@ __device__ NOINL void ph_rem4(Ctx& c, Prop& p) {
                                        __ddiv_rn(1.0, (double)np_14)),
                              __ddiv_rn(1.0, (double)np_23)));
     tdf = __ddiv_rn(tdf, 4.0);
-  } else if (rempair4(h, ta1, ca1, tb1, cb1) && rempair4(h, ta2, ca2, tb2, cb2)) {
+  } else if (rempair4(c, h, ta1, ca1, tb1, cb1) && rempair4(c, h, ta2, ca2, tb2, cb2)) {
     branch = 2;
     const int sa[4] = {a1, b1, -1, -1}, sb[4] = {a2, b2, -1, -1};
     const int np_23 = count_pairs_skip(c, c.optau, c.opcode, K, sa);
@@ -3157,9 +3226,10 @@ __device__ NOINL void ph_rem4(Ctx& c, Prop& p) {
   }
   if (c.lane == 0) h.K = K - 4;
   __syncwarp();
-  const double n2 = 2.0 * m.nd;
-  const double factor = __ddiv_rn(__ddiv_rn(__ddiv_rn(1.0, __dmul_rn(n2, n2)), tdf), rf);
-  r.outcome = rebuild4_decide(c, fa, fb, factor, K, np_new);
+  const double n2 = 2.0 * m.nd;  // (2 NBands)**4 with off-diagonal hybridisation (CTQMC.F90:4352-4357)
+  const double fl = c.g->offdiag ? __dmul_rn(__dmul_rn(__dmul_rn(n2, n2), n2), n2) : __dmul_rn(n2, n2);
+  const double factor = __ddiv_rn(__ddiv_rn(__ddiv_rn(1.0, fl), tdf), rf);
+  r.outcome = c.g->offdiag ? rebuild4_decide_od(c, factor, K, np_new) : rebuild4_decide(c, fa, fb, factor, K, np_new);
   if (r.outcome == 4 && c.lane == 0) h.acc_rem4++;
   r.outer_sst = h.outer_sst;
   r.k_total = h.K;
@@ -3350,7 +3420,7 @@ __device__ __forceinline__ void od_save(Ctx& c, int K) {
   }
   __syncwarp();
 }
-__device__ __forceinline__ void od_restore(Ctx& c, int K) {
+__device__ NOINL void od_restore(Ctx& c, int K) {
   const double* t = glob_optau(c);
   const int* o = glob_opcode(c);
   for (int i = c.lane; i < K; i += 32) {
@@ -3364,7 +3434,7 @@ __device__ __forceinline__ void od_restore(Ctx& c, int K) {
 
 // Trace of the proposed arrays with outer superstate s0 from a full rebuild
 // of the tree into the inactive slots.
-__device__ __forceinline__ void od_trace(Ctx& c, int s0, double& lg, double& sg) {
+__device__ NOINL void od_trace(Ctx& c, int s0, double& lg, double& sg) {
   bstart_build(c);
   tree_build_inactive(c, true, false);
   rebuilt_trace(c, s0, lg, sg);
@@ -4572,8 +4642,8 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
 // proposal stream is unchanged; the whole team evaluates the dense-block
 // trace (block products, renormalisation, checkpoints).
 #ifndef TEAM_MAX_THREADS
-#define TEAM_MAX_THREADS 256  // teams of up to 8 warps
-#define TEAM_MIN_BLOCKS 4     // register budget: 64 per thread
+#define TEAM_MAX_THREADS 512  // teams of up to 16 warps
+#define TEAM_MIN_BLOCKS 2     // register budget: 64 per thread
 #endif
 __global__ void __launch_bounds__(TEAM_MAX_THREADS, TEAM_MIN_BLOCKS)
     k_sweep_team(const __grid_constant__ DModel m, const DGroup* __restrict__ groups, int ngroups, int ntotal,
@@ -4653,7 +4723,17 @@ __global__ void __launch_bounds__(TEAM_MAX_THREADS, TEAM_MIN_BLOCKS)
           if (refresh_due(c)) ph_refresh(c);
           if (c.h->status == ST_OK) ph_finish(c, p);
         }
-        if (nmeas > 0 && (i + 1) % gp->ncorr == 0 && c.h->status == ST_OK) measure(c);
+      }
+      if (nmeas > 0 && (i + 1) % gp->ncorr == 0) {
+        // dense-block models: the team extends the checkpoints to the
+        // middle edge first, so the density-matrix measurement at beta/2
+        // finds them valid
+        __syncthreads();
+        if (gp->meas_dm && !c.mono && gp->o_chk && c.h->status == ST_OK) {
+          const int mid = 1 << (gp->L - 1);
+          if (ensure_kets(c, mid, team)) ensure_bras(c, mid, team);
+        }
+        if (warp == 0 && c.h->status == ST_OK) measure(c);
       }
       __syncthreads();
     }
@@ -4770,6 +4850,133 @@ __global__ void __launch_bounds__(WPB * 32) k_grad(const __grid_constant__ DMode
     for (int p = 0; p < npar; ++p) gpar[(size_t)chain * npar + p] = score[p];
   // absolute log|trace| (the stored trace is relative to exp(-beta Egs))
   if (c.lane == 0) logw[2 * (size_t)chain + 1] = ltr - g.beta * m.egs;
+}
+
+// Trace gradients of dense-block models along Hamiltonian directions
+// dH/dtheta_p, given as blocks V_p in the eigenbasis of each superstate:
+// d log|Tr| / dtheta_p = (1/Tr) sum over the segments between operators of
+// Tr[bra_seg^T dP_seg ket_seg], with dP(a, b) = -V_p(a, b) psi(E_a, E_b)
+// the exact derivative of the segment propagator exp(-dtau H) in its
+// eigenbasis (psi = (exp(-dtau E_a) - exp(-dtau E_b)) / (E_b - E_a), dtau
+// exp(-dtau E_a) for E_a = E_b; no eigenvector derivatives are needed,
+// the trace being basis-independent).  The adjoint sweep recomputes from
+// the checkpoints: per time bin the kets after each operator are stored
+// (forward from the ket checkpoint at the bin's start) and the bra is
+// propagated backwards from the bra checkpoint at its end.  One block (a
+// team of warps) per chain; `scr` holds maxseg + 1 matrices per chain.
+__global__ void __launch_bounds__(128) k_grad_dense(const __grid_constant__ DModel m, const __grid_constant__ DGroup g,
+                                                    int chain0, const double* __restrict__ vblk, int npar,
+                                                    double* gpar, double* logw, double* scr, size_t scr_stride,
+                                                    int maxseg) {
+  __shared__ Hdr hs;
+  __shared__ double red[4];
+  const int chain = chain0 + blockIdx.x;
+  if (chain >= g.nchains) return;
+  const Team t{(int)threadIdx.x, (int)blockDim.x, red};
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  Ctx c = make_ctx(&m, &g, &hs, chain);
+  Hdr* gh = (Hdr*)(g.base + (size_t)chain * g.stride + g.o_hdr);
+  if (warp == 0) load_hdr(c.h, gh, lane);
+  __syncthreads();
+  const int nb = 1 << g.L, ld = m.nsmax;
+  double* S = scr + (size_t)blockIdx.x * scr_stride;  // stored kets (maxseg + 1) x nsmax^2, then their logs
+  double* Slg = S + (size_t)(maxseg + 1) * ld * ld;
+  int* Ssst = (int*)(Slg + (size_t)(maxseg + 1) * ld);
+  double acc[NPARMAX];
+  for (int q = 0; q < npar; ++q) acc[q] = 0.0;
+  bool ok = ensure_kets(c, nb, t) && ensure_bras(c, 0, t);
+  double trlg = -DHUGE, trsg = 0.0;
+  if (ok) {
+    // the trace at beta: the full ket against the identity bra
+    double *v = dwork(c, 0), *lg = dwork(c, 2);
+    int sst, rows, cols;
+    chk_load(c, chk_head(c, 0, nb), sst, rows, cols, v, lg, t);
+    chk_close(c, sst, rows, cols, v, lg, chk_head(c, 1, nb), trlg, trsg, t);
+    ok = trsg != 0.0;
+  }
+  for (int b = 0; b < nb && ok; ++b) {
+    const int j0 = c.bstart[b], nops = c.bstart[b + 1] - j0;
+    if (nops > maxseg) {
+      ok = false;
+      break;
+    }
+    // forward: S[0] = ket at edge b, S[j] = ket after the j-th operator of the bin
+    double *v = dwork(c, 0), *o = dwork(c, 1), *lg = dwork(c, 2);
+    int sst, rows, cols;
+    chk_load(c, chk_head(c, 0, b), sst, rows, cols, v, lg, t);
+    double tt = bin_edge(c, b);
+    for (int j = 0; j <= nops; ++j) {
+      double* Sj = S + (size_t)j * ld * ld;
+      for (int e = t.tid; e < rows * cols; e += t.nth) {
+        const size_t x = (size_t)(e / rows) * ld + e % rows;
+        Sj[x] = v[x];
+      }
+      for (int col = t.tid; col < cols; col += t.nth) Slg[(size_t)j * ld + col] = lg[col];
+      if (t.tid == 0) Ssst[j] = sst;
+      tsync(t);
+      if (j == nops) break;
+      const double tau = c.optau[j0 + j];
+      if (!col_step(c, sst, rows, cols, v, o, lg, c.opcode[j0 + j], false, tau - tt, t)) {
+        ok = false;
+        break;
+      }
+      tt = tau;
+    }
+    if (!ok) break;
+    // backward: the bra at the end of each segment, from the checkpoint at edge b + 1
+    int bsst, brows, bcols;
+    chk_load(c, chk_head(c, 1, b + 1), bsst, brows, bcols, v, lg, t);
+    for (int j = nops; j >= 0 && ok; --j) {
+      const double ta = j == 0 ? bin_edge(c, b) : c.optau[j0 + j - 1];
+      const double te = j == nops ? bin_edge(c, b + 1) : c.optau[j0 + j];
+      const double dt = te - ta;
+      const int s = Ssst[j];
+      if (s != bsst) {
+        ok = false;
+        break;
+      }
+      const int n = m.sst_n[s];
+      const double* E = m.eval + m.sst_off[s];
+      const double e0 = E[0];
+      const double* Sj = S + (size_t)j * ld * ld;
+      const double* Sl = Slg + (size_t)j * ld;
+      double* w = dwork(c, 3);  // per-column weight exp(log ket + log bra - (e0 - Egs) dt - log Tr)
+      for (int col = t.tid; col < cols; col += t.nth) w[col] = exp(Sl[col] + lg[col] - (e0 - m.egs) * dt - trlg);
+      tsync(t);
+      // sum over (b, a) of W(b, a) psi(a, b) (-V_p(a, b)), W = ket w bra^T
+      for (int e = t.tid; e < n * n; e += t.nth) {
+        const int ib = e % n, ia = e / n;
+        double wba = 0.0;
+        for (int col = 0; col < cols; ++col) wba = fma(Sj[(size_t)col * ld + ib] * w[col], v[(size_t)col * ld + ia], wba);
+        const double d = E[ib] - E[ia];
+        const double ea = exp(-(E[ia] - e0) * dt);
+        const double psi = d == 0.0 ? dt * ea : ea * (-expm1(-dt * d)) / d;
+        const double x = wba * psi;
+        for (int q = 0; q < npar; ++q) acc[q] -= vblk[(size_t)q * m.dm_size + m.dm_off[s] + (size_t)ib * n + ia] * x;
+      }
+      if (j == 0) break;
+      // bra across segment j and through the j-th operator (transposed)
+      if (!col_step(c, bsst, brows, bcols, v, o, lg, c.opcode[j0 + j - 1], true, dt, t)) ok = false;
+    }
+  }
+  // team sums of the per-thread partials
+  for (int q = 0; q < npar; ++q) {
+    const double sum = tsum(t, acc[q]) * trsg;  // d log|Tr| = dTr / Tr, Tr = trsg exp(trlg)
+    if (t.tid == 0) gpar[(size_t)chain * npar + q] = ok ? sum : 0.0;
+  }
+  if (t.tid == 0) logw[2 * (size_t)chain + 1] = ok ? trlg - g.beta * m.egs : -DHUGE;
+  // the checkpoints extended here stay valid for the configuration
+  if (warp == 0) store_hdr(gh, c.h, lane);
+}
+
+// Largest operator count of a time bin over the chains of a group.
+__global__ void k_max_bin(const __grid_constant__ DGroup g, int* out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.nchains) return;
+  const int* bs = (const int*)(g.base + (size_t)c * g.stride + g.o_bstart);
+  int mx = 0;
+  for (int b = 0; b < (1 << g.L); ++b) mx = max(mx, bs[b + 1] - bs[b]);
+  atomicMax(out, mx);
 }
 
 // set_mc_config: operator arrays from a time-ordered list already written
@@ -5106,6 +5313,8 @@ struct cthyb_model_s {
   DModel dm;
   std::vector<void*> allocs;
   bool uploaded = false;
+  int ndir = 0;                 // Hamiltonian directions set by cthyb_model_set_directions
+  double* d_dir = nullptr;      // their eigenbasis blocks on the device (ndir x dm_size)
 };
 
 struct GroupHost {
@@ -5145,6 +5354,7 @@ struct cthyb_batch_s {
     cudaGraphExec_t exec = nullptr;
   } gwarm, gmeas;
   int team = 0;         // > 0: team sweep with `team` warps per chain (k_sweep_team)
+  int team_bps = 0;     // resident team blocks per multiprocessor (0: as many as fit)
   int* d_order = nullptr;   // chain order of the team sweep
   int* d_counter = nullptr; // its fetch counter
   int team_attr = 0;        // shared memory the team kernels are opted in for
@@ -5245,8 +5455,27 @@ static int model_upload(cthyb_model_t M) {
   return CTHYB_OK;
 }
 
+int cthyb_model_set_directions(cthyb_model_t m, int nparams, const double* dumatrix, const double* dmuimp) {
+  if (!m || nparams < 0 || nparams > NPARMAX || (nparams > 0 && !dumatrix && !dmuimp))
+    return fail(CTHYB_ERR_ARG, "bad arguments (nparams must be 0..32)");
+  std::vector<double> blocks;
+  direction_blocks(m->hm, nparams, dumatrix, dmuimp, blocks);
+  if (m->d_dir) {
+    CK(cudaFree(m->d_dir));
+    m->d_dir = nullptr;
+  }
+  m->ndir = 0;
+  if (nparams > 0) {
+    CK(cudaMalloc(&m->d_dir, blocks.size() * sizeof(double)));
+    CK(cudaMemcpy(m->d_dir, blocks.data(), blocks.size() * sizeof(double), cudaMemcpyHostToDevice));
+    m->ndir = nparams;
+  }
+  return CTHYB_OK;
+}
+
 int cthyb_model_destroy(cthyb_model_t m) {
   if (!m) return CTHYB_OK;
+  if (m->d_dir) cudaFree(m->d_dir);
   for (void* p : m->allocs) cudaFree(p);
   delete m;
   return CTHYB_OK;
@@ -5440,9 +5669,9 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
       delete B;
       return fail(CTHYB_ERR_ARG, "bad group description");
     }
-    if (G.desc.ftau_full && (G.desc.p_4op > 0.0 || (G.desc.nscore > 0 && G.desc.score_dE))) {
+    if (G.desc.ftau_full && G.desc.nscore > 0 && G.desc.score_dE) {
       delete B;
-      return fail(CTHYB_ERR_UNSUPPORTED, "off-diagonal hybridisation: no 4-operator moves or score measurements");
+      return fail(CTHYB_ERR_UNSUPPORTED, "off-diagonal hybridisation: no score measurements");
     }
     layout_group(B, G, 0);
     G.chain0 = B->nchains;
@@ -5668,7 +5897,9 @@ static int launch_team(cthyb_batch_t B, long long nprop, int nmeas, int reset) {
   }
   int per_sm = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sweep_team, threads, smem));
-  const int grid = std::max(1, std::min(B->nchains, std::max(per_sm, 1) * std::max(B->nsm, 1)));
+  per_sm = std::max(per_sm, 1);
+  if (B->team_bps > 0) per_sm = std::min(per_sm, B->team_bps);
+  const int grid = std::max(1, std::min(B->nchains, per_sm * std::max(B->nsm, 1)));
   k_order<<<1, 1024, osmem, B->stream>>>(B->model->dm, B->d_groups, (int)B->groups.size(), B->nchains, B->d_order);
   CK(cudaGetLastError());
   CK(cudaMemsetAsync(B->d_counter, 0, sizeof(int), B->stream));
@@ -5708,10 +5939,11 @@ int cthyb_batch_set_schedule(cthyb_batch_t B, int warps_per_block) {
   return CTHYB_OK;
 }
 
-int cthyb_batch_set_team(cthyb_batch_t B, int warps_per_chain) {
-  if (!B || warps_per_chain < 0 || warps_per_chain > TEAM_MAX_THREADS / 32)
-    return fail(CTHYB_ERR_ARG, "warps_per_chain must be 0..8");
+int cthyb_batch_set_team(cthyb_batch_t B, int warps_per_chain, int blocks_per_sm) {
+  if (!B || warps_per_chain < 0 || warps_per_chain > TEAM_MAX_THREADS / 32 || blocks_per_sm < 0)
+    return fail(CTHYB_ERR_ARG, "warps_per_chain must be 0..16, blocks_per_sm >= 0");
   B->team = warps_per_chain;
+  B->team_bps = blocks_per_sm;
   return CTHYB_OK;
 }
 
@@ -5732,7 +5964,7 @@ static int issue_sweeps(cthyb_batch_t B, long long n, bool meas) {
 
 // Capture the launch sequence once per (n, schedule) and replay it.
 static int graph_sweeps(cthyb_batch_t B, cthyb_batch_s::Graph& G, long long n, bool meas) {
-  const int sched = B->team > 0 ? 100 + B->team : schedule_of(B);
+  const int sched = B->team > 0 ? 100 + B->team + 1000 * B->team_bps : schedule_of(B);
   if (!G.exec || G.n != n || G.sched != sched) {
     if (G.exec) {
       CK(cudaGraphExecDestroy(G.exec));
@@ -5791,14 +6023,16 @@ int cthyb_batch_autotune(cthyb_batch_t B, int64_t nprop, int* best_out) {
   bool dense = false;
   for (GroupHost& G : B->groups) dense = dense || !(B->model->hm.monomial && !G.g.dense);
   std::vector<int> cl = {0, 4, 8, 12, 14, 16, 20, 24, 28, 32};
-  if (dense) cl = {0, 1, 2, 4, 8, 101, 102, 104, 108};
+  // team candidates: 100 + T warps per chain + 1000 x resident blocks per
+  // multiprocessor (0: as many as fit)
+  if (dense) cl = {0, 1, 104, 108, 2108, 4108, 116, 1116, 2116};
   const int ncand = (int)cl.size();
   const int* cands = cl.data();
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  const int saved = B->sync_warps, saved_team = B->team;
-  int best = saved_team > 0 ? 100 + saved_team : saved;
+  const int saved = B->sync_warps, saved_team = B->team, saved_bps = B->team_bps;
+  int best = saved_team > 0 ? 100 + saved_team + 1000 * saved_bps : saved;
   // two passes over the candidates, the second in reverse order, half the
   // proposals each: a drift of the chains' cost during tuning (expansion
   // orders still growing) then weighs on every candidate alike
@@ -5808,7 +6042,8 @@ int cthyb_batch_autotune(cthyb_batch_t B, int64_t nprop, int* best_out) {
   for (int pass = 0; pass < 2 && rc == CTHYB_OK; ++pass)
     for (int q = 0; q < ncand; ++q) {
       const int ci = pass == 0 ? q : ncand - 1 - q;
-      B->team = cands[ci] >= 100 ? cands[ci] - 100 : 0;
+      B->team = cands[ci] >= 100 ? cands[ci] % 1000 - 100 : 0;
+      B->team_bps = cands[ci] >= 100 ? cands[ci] / 1000 : 0;
       B->sync_warps = cands[ci] >= 100 ? saved : cands[ci];
       cudaEventRecord(e0, B->stream);
       rc = issue_sweeps(B, half, false);
@@ -5833,11 +6068,13 @@ int cthyb_batch_autotune(cthyb_batch_t B, int64_t nprop, int* best_out) {
   if (rc) {
     B->sync_warps = saved;
     B->team = saved_team;
+    B->team_bps = saved_bps;
   } else {
-    B->team = best >= 100 ? best - 100 : 0;
+    B->team = best >= 100 ? best % 1000 - 100 : 0;
+    B->team_bps = best >= 100 ? best / 1000 : 0;
     B->sync_warps = best >= 100 ? saved : best;
   }
-  if (best_out) *best_out = B->team > 0 ? 100 + B->team : B->sync_warps;
+  if (best_out) *best_out = B->team > 0 ? 100 + B->team + 1000 * B->team_bps : B->sync_warps;
   return rc;
 }
 
@@ -6317,18 +6554,59 @@ int cthyb_batch_minv(cthyb_batch_t B, int chain, int f, int* kout, double* out) 
   return CTHYB_OK;
 }
 
+// Dense-block trace gradients of the chains of one group (directions of
+// cthyb_model_set_directions) into device arrays gp (chains of the group x
+// nparams) and lw[2c + 1], in chunks of chains that keep the stored kets
+// within 2 GiB; enqueued on st (synchronises once for the largest bin).
+static int dense_group_gradients(cthyb_batch_t B, GroupHost& G, int nparams, double* gp, double* lw,
+                                 cudaStream_t st) {
+  const HostModel& hm = B->model->hm;
+  const int n = G.desc.nchains;
+  int* d_mx = nullptr;
+  CK(cudaMalloc(&d_mx, sizeof(int)));
+  int mx = 0;
+  cudaError_t e = cudaMemsetAsync(d_mx, 0, sizeof(int), st);
+  if (e == cudaSuccess) {
+    k_max_bin<<<(n + 127) / 128, 128, 0, st>>>(G.g, d_mx);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, d_mx, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaFree(d_mx);
+  const size_t ld = hm.nsmax;
+  const size_t stride = align_up(((size_t)mx + 1) * (ld * ld + ld) + (size_t)mx + 2, 32);
+  const int chunk = (int)std::max<size_t>(1, std::min<size_t>(n, ((size_t)2 << 30) / (stride * 8)));
+  double* scr = nullptr;
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)&scr, (size_t)chunk * stride * 8, st);
+  for (int c0 = 0; c0 < n && e == cudaSuccess; c0 += chunk) {
+    k_grad_dense<<<std::min(chunk, n - c0), 128, 0, st>>>(B->model->dm, G.g, c0, B->model->d_dir, nparams, gp, lw,
+                                                          scr, stride, mx);
+    e = cudaGetLastError();
+  }
+  if (scr) cudaFreeAsync(scr, st);
+  if (e != cudaSuccess) return fail(CTHYB_ERR_CUDA, std::string("dense trace gradients: ") + cudaGetErrorString(e));
+  return CTHYB_OK;
+}
+
+static bool any_dense(cthyb_batch_t B) {
+  for (GroupHost& G : B->groups)
+    if (G.g.o_chk) return true;
+  return false;
+}
+
 int cthyb_batch_gradients(cthyb_batch_t B, int nparams, const double* dE, double* grad_delta, double* grad_params,
                           double* log_weights) {
-  if (!B || nparams < 0 || nparams > NPARMAX || (nparams > 0 && (!dE || !grad_params)))
+  const bool dense = B && any_dense(B);
+  if (!B || nparams < 0 || nparams > NPARMAX || (nparams > 0 && !grad_params) ||
+      (nparams > 0 && !dense && !dE))
     return fail(CTHYB_ERR_ARG, "bad arguments (nparams must be 0..32)");
   if (any_offdiag(B)) return fail(CTHYB_ERR_UNSUPPORTED, "gradients with off-diagonal hybridisation");
   const HostModel& hm = B->model->hm;
-  if (nparams > 0)
-    for (GroupHost& G : B->groups)
-      if (G.g.o_chk) return fail(CTHYB_ERR_UNSUPPORTED, "trace gradients need a monomial (density-density) model");
+  if (nparams > 0 && dense && (dE || B->model->ndir != nparams))
+    return fail(CTHYB_ERR_ARG, "dense-block models: pass dE = NULL and set the directions with cthyb_model_set_directions");
   CK(cudaStreamSynchronize(B->stream));
   double* d_dE = nullptr;
-  if (nparams > 0) {
+  if (nparams > 0 && !dense) {
     CK(cudaMalloc(&d_dE, sizeof(double) * (size_t)nparams * hm.ns));
     CK(cudaMemcpy(d_dE, dE, sizeof(double) * (size_t)nparams * hm.ns, cudaMemcpyHostToDevice));
   }
@@ -6342,8 +6620,19 @@ int cthyb_batch_gradients(cthyb_batch_t B, int nparams, const double* dE, double
     if (e == cudaSuccess) e = cudaMemsetAsync(gd, 0, sizeof(double) * (size_t)n * nf * nft, B->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(lw, 0, sizeof(double) * (size_t)n * 2, B->stream);
     if (e == cudaSuccess) {
-      k_grad<<<(n + WPB - 1) / WPB, WPB * 32, 0, B->stream>>>(B->model->dm, G.g, d_dE, nparams, gd, gp, lw);
+      k_grad<<<(n + WPB - 1) / WPB, WPB * 32, 0, B->stream>>>(B->model->dm, G.g, d_dE, dense ? 0 : nparams, gd, gp,
+                                                              lw);
       e = cudaGetLastError();
+    }
+    if (e == cudaSuccess && dense && nparams > 0) {
+      const int rc2 = dense_group_gradients(B, G, nparams, gp, lw, B->stream);
+      if (rc2) {
+        cudaFree(gd);
+        cudaFree(gp);
+        cudaFree(lw);
+        if (d_dE) cudaFree(d_dE);
+        return rc2;
+      }
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
     if (e == cudaSuccess) {
@@ -6376,13 +6665,13 @@ int cthyb_batch_gradients(cthyb_batch_t B, int nparams, const double* dE, double
 
 int cthyb_batch_gradients_device(cthyb_batch_t B, int nparams, const double* dE_dev, double* grad_delta_dev,
                                  double* grad_params_dev, double* log_weights_dev, void* stream) {
+  const bool dense = B && any_dense(B);
   if (!B || nparams < 0 || nparams > NPARMAX || !grad_delta_dev || !log_weights_dev ||
-      (nparams > 0 && (!dE_dev || !grad_params_dev)))
+      (nparams > 0 && (!grad_params_dev || (!dense && !dE_dev))))
     return fail(CTHYB_ERR_ARG, "bad arguments (nparams must be 0..32)");
   if (any_offdiag(B)) return fail(CTHYB_ERR_UNSUPPORTED, "gradients with off-diagonal hybridisation");
-  if (nparams > 0)
-    for (GroupHost& G : B->groups)
-      if (G.g.o_chk) return fail(CTHYB_ERR_UNSUPPORTED, "trace gradients need a monomial (density-density) model");
+  if (nparams > 0 && dense && (dE_dev || B->model->ndir != nparams))
+    return fail(CTHYB_ERR_ARG, "dense-block models: pass dE = NULL and set the directions with cthyb_model_set_directions");
   const int nft = B->groups[0].g.nftau, nf = B->model->hm.nf;
   for (GroupHost& G : B->groups)
     if (G.g.nftau != nft) return fail(CTHYB_ERR_ARG, "gradients need one Nftau for all groups");
@@ -6397,12 +6686,17 @@ int cthyb_batch_gradients_device(cthyb_batch_t B, int nparams, const double* dE_
   CK(cudaMemsetAsync(grad_delta_dev, 0, sizeof(double) * (size_t)B->nchains * nf * nft, st));
   for (GroupHost& G : B->groups) {
     const int n = G.desc.nchains;
-    k_grad<<<(n + WPB - 1) / WPB, WPB * 32, 0, st>>>(B->model->dm, G.g, dE_dev, nparams,
+    k_grad<<<(n + WPB - 1) / WPB, WPB * 32, 0, st>>>(B->model->dm, G.g, dE_dev, dense ? 0 : nparams,
                                                      grad_delta_dev + (size_t)G.chain0 * nf * nft,
                                                      grad_params_dev ? grad_params_dev + (size_t)G.chain0 * nparams
                                                                      : nullptr,
                                                      log_weights_dev + (size_t)G.chain0 * 2);
     CK(cudaGetLastError());
+    if (dense && nparams > 0) {
+      const int rc = dense_group_gradients(B, G, nparams, grad_params_dev + (size_t)G.chain0 * nparams,
+                                           log_weights_dev + (size_t)G.chain0 * 2, st);
+      if (rc) return rc;
+    }
   }
   return CTHYB_OK;
 }

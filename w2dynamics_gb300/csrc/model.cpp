@@ -365,6 +365,96 @@ bool build_model(int nd, const double* umat, const double* muimp, const char* qn
   return true;
 }
 
+void direction_blocks(const HostModel& m, int np, const double* dumat, const double* dmuimp,
+                      std::vector<double>& out) {
+  const int nd = m.nd, nf = m.nf, ns = m.ns, nss = m.nss;
+  out.assign((size_t)np * m.dm_size, 0.0);
+  // occupation basis: global index of each Fock state, its superstate
+  std::vector<int> idx_of(ns, -1), sst_of(ns, -1);
+  for (int s = 0; s < nss; ++s)
+    for (int i = 0; i < m.sst_n[s]; ++i) {
+      idx_of[m.occ_fock[m.sst_off[s] + i]] = m.sst_off[s] + i;
+      sst_of[m.occ_fock[m.sst_off[s] + i]] = s;
+    }
+  auto bit_of = [&](int fl) { return (fl / 2) + nd * (fl % 2); };
+  for (int p = 0; p < np; ++p) {
+    // D in the occupation basis, superstate blocks (entries leaving a block
+    // are dropped, as for H)
+    std::vector<std::vector<double>> D(nss);
+    for (int s = 0; s < nss; ++s) D[s].assign((size_t)m.sst_n[s] * m.sst_n[s], 0.0);
+    auto add = [&](int from, int to, double v) {
+      const int s = sst_of[from];
+      if (sst_of[to] != s) return;
+      const int n = m.sst_n[s];
+      D[s][(size_t)(idx_of[from] - m.sst_off[s]) * n + (idx_of[to] - m.sst_off[s])] += v;
+    };
+    if (dmuimp) {
+      const double* mu = dmuimp + (size_t)p * nf * nf;
+      for (int f1 = 0; f1 < nf; ++f1)
+        for (int f2 = 0; f2 < nf; ++f2) {
+          const int b1 = f1 / 2, s1 = f1 % 2, b2 = f2 / 2, s2 = f2 % 2;
+          const double v = mu[b1 + nd * (s1 + 2 * (b2 + nd * s2))];
+          if (v == 0.0) continue;
+          for (int st = 0; st < ns; ++st) {
+            double sg = 1.0;
+            const int a = apply_op(st, bit_of(f2), true, sg);
+            if (a < 0) continue;
+            const int c = apply_op(a, bit_of(f1), false, sg);
+            if (c < 0) continue;
+            add(st, c, v * sg);
+          }
+        }
+    }
+    if (dumat) {
+      const double* um = dumat + (size_t)p * nf * nf * nf * nf;
+      for (int i = 0; i < nf; ++i)
+        for (int j = 0; j < nf; ++j)
+          for (int k = 0; k < nf; ++k)
+            for (int l = 0; l < nf; ++l) {
+              const double u = um[i + nf * (j + nf * (k + nf * l))];
+              if (u == 0.0) continue;
+              for (int st = 0; st < ns; ++st) {
+                double sg = 1.0;
+                int x = apply_op(st, bit_of(k), true, sg);
+                if (x < 0) continue;
+                x = apply_op(x, bit_of(l), true, sg);
+                if (x < 0) continue;
+                x = apply_op(x, bit_of(j), false, sg);
+                if (x < 0) continue;
+                x = apply_op(x, bit_of(i), false, sg);
+                if (x < 0) continue;
+                add(st, x, 0.5 * u * sg);
+              }
+            }
+    }
+    // rotate into the eigenbasis: V^T D V (D symmetrised like H)
+    for (int s = 0; s < nss; ++s) {
+      const int n = m.sst_n[s];
+      const double* V = m.evec.data() + m.evec_off[s];
+      std::vector<double>& d = D[s];
+      for (int i = 0; i < n; ++i)
+        for (int j = i + 1; j < n; ++j) {
+          const double a = 0.5 * (d[(size_t)j * n + i] + d[(size_t)i * n + j]);
+          d[(size_t)j * n + i] = d[(size_t)i * n + j] = a;
+        }
+      std::vector<double> DV((size_t)n * n, 0.0);
+      for (int j = 0; j < n; ++j)
+        for (int k = 0; k < n; ++k) {
+          const double v = V[(size_t)j * n + k];
+          if (v == 0.0) continue;
+          for (int i = 0; i < n; ++i) DV[(size_t)j * n + i] += d[(size_t)k * n + i] * v;
+        }
+      double* o = out.data() + (size_t)p * m.dm_size + m.dm_off[s];
+      for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) {
+          double acc = 0.0;
+          for (int k = 0; k < n; ++k) acc += V[(size_t)i * n + k] * DV[(size_t)j * n + k];
+          o[(size_t)j * n + i] = acc;
+        }
+    }
+  }
+}
+
 // Normalised empty-trace weights per superstate (init_Trace's choice of the
 // outer superstate, Trace.F90:611-669): sum_i exp(-(E_i - Egs) beta)
 // accumulated in log form over the states of each superstate.

@@ -29,5 +29,12 @@ struct HostModel {
 bool build_model(int nd, const double* umat, const double* muimp, const char* qns, HostModel& m,
                  std::string& err);
 void empty_trace_weights(const HostModel& m, double beta, std::vector<double>& w);
+// Hamiltonian directions dH/dtheta_p = sum dmuimp_p c+c + 1/2 sum dU_p
+// c+c+cc (the operator strings of H) as blocks in the eigenbasis of each
+// superstate: out[p * dm_size + dm_off[s] + j * n_s + i] = (V_s^T D_p V_s)(i, j)
+// with V_s the eigenvectors.  dumat: np x (2Nd)^4 (each as the U matrix of
+// build_model), dmuimp: np x (Nd,2,Nd,2) Fortran order; either may be NULL.
+void direction_blocks(const HostModel& m, int np, const double* dumat, const double* dmuimp,
+                      std::vector<double>& out);
 
 }  // namespace cthyb

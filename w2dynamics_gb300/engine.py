@@ -25,7 +25,7 @@ FLAG_DMMA = 4
 
 EXPORTS = (
     "cthyb_last_error", "cthyb_model_create", "cthyb_model_destroy", "cthyb_model_info",
-    "cthyb_model_states", "cthyb_model_basis", "cthyb_model_connect", "cthyb_batch_create",
+    "cthyb_model_states", "cthyb_model_basis", "cthyb_model_connect", "cthyb_model_set_directions", "cthyb_batch_create",
     "cthyb_batch_destroy",
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
@@ -80,6 +80,7 @@ def load(build_if_missing=False):
     L.cthyb_model_states.argtypes = [vp, ip, ip, ip, dp]
     L.cthyb_model_connect.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
     L.cthyb_model_basis.argtypes = [vp, ip, dp]
+    L.cthyb_model_set_directions.argtypes = [vp, C.c_int, dp, dp]
     L.cthyb_batch_create.argtypes = [vp, C.c_int, C.POINTER(GroupDesc), C.POINTER(vp)]
     L.cthyb_batch_destroy.argtypes = [vp]
     L.cthyb_batch_nchains.argtypes = [vp]
@@ -91,7 +92,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_stream.argtypes = [vp, C.POINTER(vp)]
     L.cthyb_batch_use_graphs.argtypes = [vp, C.c_int]
     L.cthyb_batch_set_schedule.argtypes = [vp, C.c_int]
-    L.cthyb_batch_set_team.argtypes = [vp, C.c_int]
+    L.cthyb_batch_set_team.argtypes = [vp, C.c_int, C.c_int]
     L.cthyb_batch_autotune.argtypes = [vp, i64, C.POINTER(C.c_int)]
     L.cthyb_batch_results.argtypes = [vp, C.c_int, dp, dp, dp, dp, C.POINTER(i64)]
     L.cthyb_batch_move_counters.argtypes = [vp, C.c_int, C.POINTER(i64)]
@@ -179,6 +180,21 @@ class Model:
         ev = np.zeros(self.nstates * self.nstates)
         _check(load().cthyb_model_basis(self.h, _ip(fk), _dp(ev)))
         return fk, ev.reshape((self.nstates, self.nstates), order="F")
+
+    def set_directions(self, dumatrix=None, dmuimp=None):
+        """Hamiltonian directions for the trace gradients of dense-block
+        models: dumatrix (nparams, 2Nd, 2Nd, 2Nd, 2Nd) and/or dmuimp
+        (nparams, Nd, 2, Nd, 2), dH/dtheta_p in the operator strings of
+        H_loc."""
+        nd, nf = self.nd, 2 * self.nd
+        n = len(dumatrix) if dumatrix is not None else len(dmuimp)
+        du = None if dumatrix is None else np.concatenate(
+            [np.asfortranarray(np.asarray(u, np.float64).reshape((nf,) * 4)).ravel(order="F") for u in dumatrix])
+        dm = None if dmuimp is None else np.concatenate(
+            [np.asfortranarray(np.asarray(x, np.float64).reshape(nd, 2, nd, 2)).ravel(order="F") for x in dmuimp])
+        _check(load().cthyb_model_set_directions(self.h, n, _dp(du) if du is not None else None,
+                                                 _dp(dm) if dm is not None else None))
+        self.ndir = n
 
     def close(self):
         if getattr(self, "h", None):
@@ -300,15 +316,16 @@ class Batch:
         """-1: automatic; 0: independent warps; n (1..32): phase-synchronous blocks of n chains."""
         _check(load().cthyb_batch_set_schedule(self.h, int(warps_per_block)))
 
-    def set_team(self, warps_per_chain):
-        """0: off; T (1..8): team sweep, blocks of T warps per chain taken
-        from a cost-ordered queue (the warps share the dense-block trace)."""
-        _check(load().cthyb_batch_set_team(self.h, int(warps_per_chain)))
+    def set_team(self, warps_per_chain, blocks_per_sm=0):
+        """0: off; T (1..16): team sweep, blocks of T warps per chain taken
+        from a cost-ordered queue (the warps share the dense-block trace);
+        blocks_per_sm bounds the resident blocks (0: as many as fit)."""
+        _check(load().cthyb_batch_set_team(self.h, int(warps_per_chain), int(blocks_per_sm)))
 
     def autotune(self, nprop):
         """Pick the fastest schedule on `nprop` warmup proposals per candidate;
-        returns the chosen warps per block (0: independent warps) or 100 + T
-        for a team sweep of T warps per chain."""
+        returns the chosen warps per block (0: independent warps) or
+        100 + T + 1000 x blocks_per_sm for a team sweep of T warps per chain."""
         best = C.c_int()
         _check(load().cthyb_batch_autotune(self.h, int(nprop), C.byref(best)))
         return best.value
@@ -348,7 +365,7 @@ class Batch:
         pointers): grad_delta (nchains, 2Nd, Nftau), grad_params (nchains,
         nparams), log_weights (nchains, 2); enqueued, not synchronised."""
         ptr = lambda t: None if t is None else C.c_void_p(t.data_ptr() if hasattr(t, "data_ptr") else int(t))
-        npar = 0 if dE_dev is None else int(dE_dev.shape[0])
+        npar = getattr(self.model, "ndir", 0) if dE_dev is None else int(dE_dev.shape[0])
         _check(load().cthyb_batch_gradients_device(self.h, npar, ptr(dE_dev), ptr(grad_delta), ptr(grad_params),
                                                    ptr(log_weights), C.c_void_p(stream) if stream else None))
 
@@ -376,7 +393,8 @@ class Batch:
         nft = self.groups[0].ftau.shape[2]
         if any(g.ftau.shape[2] != nft for g in self.groups):
             raise ValueError("gradients need one Nftau for all groups")
-        npar = 0 if dE is None else int(np.asarray(dE).shape[0])
+        # dense-block models: dE None, the directions set on the model
+        npar = getattr(self.model, "ndir", 0) if dE is None else int(np.asarray(dE).shape[0])
         dEc = None if dE is None else np.ascontiguousarray(dE, np.float64)
         gd = np.zeros((self.nchains, nd * 2 * nft))
         gp = np.zeros((self.nchains, max(npar, 1)))

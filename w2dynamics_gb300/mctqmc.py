@@ -172,9 +172,6 @@ def _check_supported():
         bad.append("Eigenbasis = 0")
     if "All" in _str("QuantumNumbers", "").split():
         bad.append("QuantumNumbers = All")
-    if _int("offdiag", 0) != 0 and _real("Percentage4OperatorMove", 0.0) != 0.0:
-        # off-diagonal F: pair, outer-superstate, global and tau-shift moves
-        bad.append(f"Percentage4OperatorMove = {_real('Percentage4OperatorMove')} with offdiag = 1")
     if bad:
         raise NotImplementedError("outside the GPU pair-move engine: " + ", ".join(bad))
 
