@@ -49,7 +49,7 @@ THERM_ROUND = 2000   # proposals per chain between order read-outs
 THERMALIZE = 20000   # thermalisation proposals per chain (10 rounds)
 TUNE = 200           # autotuner proposals per candidate (10 candidates, 2 interleaved passes)
 E2E_WARMUP = 1000    # re-thermalisation proposals of the warm-started end-to-end solve
-CPU_CHAINS_PER_CORE = 16  # chains per host core in the bounded CPU sample (beta cycling)
+CPU_CHAINS_PER_CORE = 64  # chains per host core in the bounded CPU sample (beta cycling)
 ONE_CHAIN_BLOCKS, ONE_CHAIN_MEAS = 16, 30  # one-chain form: blocks x measurement cycles per beta
 # dense-block workload: 5-orbital Kanamori with spin-flip and pair hopping
 K5_BETA, K5_CHAINS, K5_THERM, K5_STEPS, K5_TUNE = 40.0, 1024, 2000, 2, 20
@@ -485,20 +485,29 @@ def run_gpu(args, rank=0, world=1):
 _WORKER = {}
 
 
-def _worker_init(specs):
-    """The oracle chains of one host core (test infrastructure only)."""
+def _worker_init(model_args, specs):
+    """The oracle chains of one host core (test infrastructure only):
+    model_args = (nd, umatrix, muimp, quantum_numbers), specs one (beta,
+    seed, ftau, taudiff_max, moves) per chain."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    from w2dynamics_gb300 import problems as P
+    model = O.Model(*model_args)
     chains = []
-    models = {}
-    for name, beta, seed, ftau, tdm, moves, tree in specs:
-        if name not in models:
-            pr = P.config_problem(name, beta=beta)
-            models[name] = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
-        chains.append((beta, O.Chain(models[name], beta, ftau, NTAU if name == "dd3" else 4000, seed=seed,
-                                     taudiff_max=tdm, ncorr=NCORR, **moves)))
-    _WORKER["chains"], _WORKER["models"] = chains, models
+    for beta, seed, ftau, tdm, moves in specs:
+        chains.append((beta, O.Chain(model, beta, ftau, ftau.shape[-1], seed=seed, taudiff_max=tdm, ncorr=NCORR,
+                                     **moves)))
+    _WORKER["chains"], _WORKER["model"] = chains, model
+
+
+def _spawn_pools(model_args, specs_per_core):
+    """One single-process pool per host core.  The children do no numpy
+    linear algebra of their own (F(tau) comes from the parent), and their
+    BLAS runs single-threaded so that the cores are not oversubscribed."""
+    import multiprocessing as mp
+    for var in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS", "MKL_NUM_THREADS"):
+        os.environ[var] = "1"
+    ctx = mp.get_context("spawn")
+    return [ctx.Pool(1, initializer=_worker_init, initargs=(model_args, specs)) for specs in specs_per_core]
 
 
 def _worker_warm(n):
@@ -529,17 +538,16 @@ def oracle_rate(cores, steps, warmup):
     over the groups, seeds = chain index), through the GPU run's proposal
     window: THERMALIZE + 10 * TUNE + warmup * NCORR untimed proposals, then
     `steps` timed measurement cycles per chain."""
-    import multiprocessing as mp
-    from w2dynamics_gb300 import problems as P
-    ftaus = {b: P.semicircle_ftau(3, b, 1.0, NTAU) for b in BETAS}
-    ctx = mp.get_context("spawn")
-    pools = []
+    probs = {pr["beta"]: pr for pr in problems()}
+    pr0 = probs[BETAS[0]]
+    model_args = (pr0["nd"], pr0["umatrix"], pr0["muimp"], pr0["quantum_numbers"])
+    specs = []
     for i in range(cores):
-        specs = []
+        specs.append([])
         for j in range(CPU_CHAINS_PER_CORE):
             b = BETAS[(i * CPU_CHAINS_PER_CORE + j) % len(BETAS)]
-            specs.append(("dd3", b, i * CPU_CHAINS_PER_CORE + j, ftaus[b], TDM, MOVES, 0))
-        pools.append(ctx.Pool(1, initializer=_worker_init, initargs=(specs,)))
+            specs[-1].append((b, i * CPU_CHAINS_PER_CORE + j, probs[b]["ftau"], TDM, MOVES))
+    pools = _spawn_pools(model_args, specs)
     try:
         warm = THERMALIZE + 10 * TUNE + warmup * NCORR
         k0 = sum((r.get() for r in [p.apply_async(_worker_warm, (warm,)) for p in pools]), [])
@@ -564,12 +572,10 @@ def oracle_rate_k5(cores):
     """The oracle on the dense-block workload through the GPU run's window:
     one chain per host core (seeds 0..cores-1), K5_THERM + NCORR untimed
     proposals, then K5_STEPS timed measurement cycles."""
-    import multiprocessing as mp
     from w2dynamics_gb300 import problems as P
     pr = P.config_problem("kanamori5", beta=K5_BETA)
-    ctx = mp.get_context("spawn")
-    pools = [ctx.Pool(1, initializer=_worker_init,
-                      initargs=([("kanamori5", K5_BETA, i, pr["ftau"], -1.0, {}, 0)],)) for i in range(cores)]
+    model_args = (pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    pools = _spawn_pools(model_args, [[(K5_BETA, i, pr["ftau"], -1.0, {})] for i in range(cores)])
     try:
         for r in [p.apply_async(_worker_warm, (K5_THERM + NCORR,)) for p in pools]:
             r.get()
