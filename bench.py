@@ -4,13 +4,16 @@ Workload (the batched configuration): 4096 independent chains of the
 3-orbital density-density model (U=4, J=0.6, U'=U-2J, mu=3.3 for filling
 2/6, QuantumNumbers "Nt Szt"), 1024 chains at each beta in {10,25,50,100},
 semicircular bath (D=1) with F(tau) on Ntau=Nftau=2000 points, seed = chain
-index, TaudiffMax=5, NCorr=100, and the reference's default move mix
-(PercentageGlobalMove = PercentageTauShiftMove = 0.005, configspec:81-82),
-which makes every chain ergodic over the superstate sectors.  One step = one
-measurement cycle of every chain: NCorr proposals (StepAdd/StepRem and the
-rare global / tau-shift moves, CTQMC.F90:8428-8476) and the Z-space
-measurements (sign, order histogram, density matrix at beta/2, G(tau)).
-1 MC update = 1 proposal.
+index, TaudiffMax=5, NCorr=100, and PercentageOuterMove = 0.1: pair
+insertions and removals (StepAdd/StepRem, CTQMC.F90:8428-8476), a tenth of
+them also moving the outer superstate, which makes every chain ergodic over
+the superstate sectors (pair moves alone keep a chain in the sector it
+starts in, so the G(tau) errors of the two forms would not compare).  One
+step = one measurement cycle of every chain: NCorr proposals and the
+Z-space measurements (sign, order histogram, density matrix at beta/2,
+G(tau)).  1 MC update = 1 proposal.  The line also times the reference's
+default move mix (PercentageGlobalMove = PercentageTauShiftMove = 0.005,
+configspec:81-82), whose rare global moves rebuild every inverse matrix.
 
 Footing: every chain is thermalised for THERMALIZE proposals (the GPU run
 reports the mean expansion order of each beta group after every round of
@@ -44,7 +47,8 @@ CHAINS_PER_BETA = 1024  # 4096 chains, 1024 at each beta
 NTAU = 2000
 NCORR = 100
 TDM = 5.0
-MOVES = dict(p_global=0.005, p_shift=0.005)  # the reference's default move mix
+MOVES = dict(p_outer=0.1)  # PercentageOuterMove: pair moves that may change the outer superstate
+DEFAULT_MOVES = dict(p_global=0.005, p_shift=0.005)  # the reference's default mix (configspec:81-82)
 THERM_ROUND = 2000   # proposals per chain between order read-outs
 THERMALIZE = 20000   # thermalisation proposals per chain (10 rounds)
 TUNE = 200           # autotuner proposals per candidate (10 candidates, 2 interleaved passes)
@@ -62,8 +66,7 @@ def workload_desc(chains_per_beta):
     return {"workload": f"{len(BETAS) * chains_per_beta} chains, 3-orbital density-density "
                         f"U=4 J=0.6 mu=3.3 (Nt Szt), beta in {list(BETAS)}, "
                         f"Ntau=Nftau={NTAU}, TaudiffMax={TDM}, NCorr={NCORR}, "
-                        f"PercentageGlobalMove={MOVES['p_global']}, "
-                        f"PercentageTauShiftMove={MOVES['p_shift']}",
+                        f"PercentageOuterMove={MOVES['p_outer']}",
             "chains": len(BETAS) * chains_per_beta, "betas": list(BETAS), "ncorr": NCORR,
             "step": "NCorr proposals per chain + measurement",
             "window": f"proposals {THERMALIZE + 10 * TUNE} + W*{NCORR} ... + K*{NCORR} of every chain",
@@ -202,6 +205,30 @@ def build_batch(E, probs, cpb, rank=0, moves=MOVES):
                               **moves))
     h2d = sum(g.ftau.nbytes for g in groups) + pr0["umatrix"].nbytes + pr0["muimp"].nbytes
     return model, groups, E.Batch(model, groups), h2d
+
+
+def default_mix(E, probs, cpb, steps):
+    """The same batch with the reference's default move mix (0.5 % global
+    and 0.5 % tau-shift moves, no outer moves): THERMALIZE proposals, then
+    `steps` device-timed steps (CUDA events on the batch's stream)."""
+    import torch
+    model, groups, b, _ = build_batch(E, probs, cpb, moves=DEFAULT_MOVES)
+    b.warmup(THERMALIZE)
+    b.autotune(TUNE)
+    b.measure(1)
+    b.sync()
+    stream = torch.cuda.ExternalStream(b.stream())
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    b.measure(steps)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    mc = [b.move_counters(c) for c in range(0, b.nchains, 64)]
+    b.close()
+    return {"moves": "PercentageGlobalMove=0.005, PercentageTauShiftMove=0.005 (pair moves otherwise)",
+            "value": b.nchains * NCORR * steps / (ms / 1e3), "unit": "MC updates/s", "ms_per_step": ms / steps,
+            "global_accepted_over_tried": float(sum(x["acc_glob"] for x in mc) / max(1, sum(x["try_glob"] for x in mc)))}
 
 
 def one_chain_forms(E, model, probs):
@@ -416,6 +443,7 @@ def run_gpu(args, rank=0, world=1):
     t_equal = [o["device_s"] * o["sigma2_G"] / s2 for o, s2 in zip(ones, sig2_b)]
     one_rate = float(np.mean([o["value"] for o in ones]))
     backward = measure_backward(E, model, probs[2], args)
+    dmix = default_mix(E, probs, cpb, args.steps)
     fp64_dfma, fp64_dmma = E.probe_fp64()
     k5 = run_k5(E, args, fp64_dfma) if not args.skip_k5 else None
     cores = os.cpu_count() or 1
@@ -469,6 +497,7 @@ def run_gpu(args, rank=0, world=1):
                      "ncu": prof},
         "cpu_baseline": cpu,
         "backward": backward,
+        "default_move_mix": dmix,
         "drift": dict(drift, refresh_every=1000),
         "dense_block": k5,
         "work": wc,

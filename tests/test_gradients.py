@@ -301,14 +301,17 @@ def test_score_function_dG_dU_three_orbital():
     from w2dynamics_gb300 import engine as E
     beta, nd, u0, j, du, n, nt = 50.0, 3, 4.0, 0.6, 0.05, 2048, 8
     pr = P.config_problem("dd3", beta=beta)
-    moves = dict(p_global=0.005, p_shift=0.005)
+    # outer-superstate, global and tau-shift moves equilibrate the chains
+    # over the superstate sectors, which the initial draw (empty-trace
+    # weights, U dependent) does not
+    moves = dict(p_outer=0.1, p_global=0.01, p_shift=0.01)
 
     def run(u, seed0, score):
         mg = E.Model(nd, _dd3_umatrix(u, j), pr["muimp"], pr["quantum_numbers"])
         dE = GR.density_density_directions(nd, mg.fock_states)[2 * nd:2 * nd + 1] if score else None
         b = E.Batch(mg, [E.Group(beta, pr["ftau"], nt, nchains=n, seed0=seed0, taudiff_max=5.0, ncorr=50,
                                  kcap=64, opcap=512, score_dE=dE, **moves)])
-        b.warmup(20000)
+        b.warmup(40000)
         b.measure(400)
         b.sync()
         G = b.group_gtau(0).reshape(n, 2 * nd, nt).mean(axis=1)  # average over the degenerate flavours

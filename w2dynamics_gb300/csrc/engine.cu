@@ -2100,12 +2100,34 @@ __device__ __forceinline__ void tree_flip_all(Ctx& c) {
   __syncwarp();
 }
 
+// Running product of pivot magnitudes kept as a mantissa in [1, 2) and a
+// binary exponent: one FP64 multiply per pivot and one logarithm per matrix
+// instead of a logarithm per pivot (each costs tens of dependent FP64
+// operations).  A product that would leave the normal range falls back to
+// adding log(x) directly.
+__device__ __forceinline__ void pivot_mul(double& m, long long& e, double& dlog, double x) {
+  const double y = m * x;
+  const long long b = __double_as_longlong(y);
+  const int ef = (int)((b >> 52) & 0x7FF);
+  if (ef == 0 || ef == 0x7FF) {
+    dlog += log(x);
+    return;
+  }
+  e += ef - 1023;
+  m = __longlong_as_double((b & 0x000FFFFFFFFFFFFFll) | 0x3FF0000000000000ll);
+}
+__device__ __forceinline__ double pivot_log(double m, long long e) {
+  return log(m) + (double)e * 0.69314718055994530942;
+}
+
 // Gauss-Jordan inverse with partial pivoting (first maximal pivot) of the
 // k x k matrix H (column-major, leading dimension kcap) into I, which must
 // hold the identity on entry; log|det| and sign accumulate into dlog/dsign.
 // False for a singular matrix.
 __device__ NOINL bool gj_eliminate(Ctx& c, int k, double* H, double* I, double& dlog, double& dsign) {
   const int ld = c.kcap;
+  double pm = 1.0;
+  long long pe = 0;
   for (int j = 0; j < k; ++j) {
     double best = -1.0;
     int bi = j;
@@ -2139,7 +2161,7 @@ __device__ NOINL bool gj_eliminate(Ctx& c, int k, double* H, double* I, double& 
     }
     __syncwarp();
     const double piv = H[(size_t)j * ld + j];
-    dlog += log(fabs(piv));
+    pivot_mul(pm, pe, dlog, fabs(piv));
     if (piv < 0) dsign = -dsign;
     const double ip = 1.0 / piv;
     for (int col = c.lane; col < k; col += 32) {
@@ -2147,16 +2169,15 @@ __device__ NOINL bool gj_eliminate(Ctx& c, int k, double* H, double* I, double& 
       I[(size_t)col * ld + j] *= ip;
     }
     __syncwarp();
-    for (int col = 0; col < k; ++col) {
-      if (col == j) continue;
-      const double hj = H[(size_t)col * ld + j];
-      const double ij = I[(size_t)col * ld + j];
-      for (int i = c.lane; i < k; i += 32) {
-        if (i == j) continue;
-        const double fct = H[(size_t)j * ld + i];
-        H[(size_t)col * ld + i] -= fct * hj;
-        I[(size_t)col * ld + i] -= fct * ij;
-      }
+    // rank-one elimination of every (row i, column col) outside row and
+    // column j, the lanes over all k x k elements at once (column j and row
+    // j are only read here)
+    for (int e = c.lane; e < k * k; e += 32) {
+      const int i = e % k, col = e / k;
+      if (i == j || col == j) continue;
+      const double fct = H[(size_t)j * ld + i];
+      H[(size_t)col * ld + i] -= fct * H[(size_t)col * ld + j];
+      I[(size_t)col * ld + i] -= fct * I[(size_t)col * ld + j];
     }
     __syncwarp();
     for (int i = c.lane; i < k; i += 32)
@@ -2166,6 +2187,7 @@ __device__ NOINL bool gj_eliminate(Ctx& c, int k, double* H, double* I, double& 
       }
     __syncwarp();
   }
+  dlog += pivot_log(pm, pe);
   return true;
 }
 
@@ -2204,6 +2226,8 @@ __device__ NOINL void lu_logdet_minv(Ctx& c, int f, double* work, double& dlog, 
     A[(size_t)ra * ld + rc] = Mf[(size_t)sla[ra] * ld + slc[rc]];
   }
   __syncwarp();
+  double pm = 1.0;
+  long long pe = 0;
   for (int j = 0; j < k; ++j) {
     double best = -1.0;
     int bi = j;
@@ -2238,16 +2262,18 @@ __device__ NOINL void lu_logdet_minv(Ctx& c, int f, double* work, double& dlog, 
     }
     __syncwarp();
     const double piv = A[(size_t)j * ld + j];
-    dlog += log(fabs(piv));
+    pivot_mul(pm, pe, dlog, fabs(piv));
     if (piv < 0) dsign = -dsign;
     for (int i = j + 1 + c.lane; i < k; i += 32) A[(size_t)j * ld + i] /= piv;
     __syncwarp();
-    for (int col = j + 1; col < k; ++col) {
-      const double ajc = A[(size_t)col * ld + j];
-      for (int i = j + 1 + c.lane; i < k; i += 32) A[(size_t)col * ld + i] -= A[(size_t)j * ld + i] * ajc;
+    const int r = k - j - 1;  // trailing block, the lanes over all its r x r elements
+    for (int e = c.lane; e < r * r; e += 32) {
+      const int i = j + 1 + e % r, col = j + 1 + e / r;
+      A[(size_t)col * ld + i] -= A[(size_t)j * ld + i] * A[(size_t)col * ld + j];
     }
     __syncwarp();
   }
+  dlog += pivot_log(pm, pe);
 }
 
 // Per-flavour sorted time lists of the current operator arrays into
@@ -4954,6 +4980,7 @@ __global__ void __launch_bounds__(128) k_grad_dense(const __grid_constant__ DMod
         const double x = wba * psi;
         for (int q = 0; q < npar; ++q) acc[q] -= vblk[(size_t)q * m.dm_size + m.dm_off[s] + (size_t)ib * n + ia] * x;
       }
+      tsync(t);  // the bra and the weights are read above and overwritten below
       if (j == 0) break;
       // bra across segment j and through the j-th operator (transposed)
       if (!col_step(c, bsst, brows, bcols, v, o, lg, c.opcode[j0 + j - 1], true, dt, t)) ok = false;
