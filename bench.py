@@ -319,7 +319,7 @@ def run_k5(E, args, fp64_peak):
     model = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
     nch = args.k5_chains
     b = E.Batch(model, [E.Group(K5_BETA, pr["ftau"], pr["ntau"], nchains=nch, seed0=0, taudiff_max=-1.0,
-                                ncorr=NCORR, kcap=64, opcap=1024, tree_levels=4)])
+                                ncorr=NCORR, kcap=64, opcap=1024, tree_levels=4, dmma=args.k5_dmma)])
     b.set_team(8)
     b.warmup(K5_THERM - K5_TUNE_PROPS)
     sched = b.autotune(2 * K5_TUNE)  # its proposals are the rest of the thermalisation
@@ -345,6 +345,7 @@ def run_k5(E, args, fp64_peak):
                         f"Ntau=Nftau=4000, Nt Szt blocks (largest 100), one window, NCorr={NCORR}, "
                         f"{K5_THERM} thermalisation proposals (the last {K5_TUNE_PROPS} of them the schedule "
                         f"autotuner's; orders still growing), {K5_STEPS} timed steps",
+            "block_products": "FP64 tensor cores (mma m8n8k4)" if args.k5_dmma else "FP64 fused multiply-adds",
             "value": value, "unit": "MC updates/s", "ms_per_step": ms / K5_STEPS,
             "mean_order": [float(st["noper"].mean()), k_end],
             "schedule": {"autotuner_choice": sched,
@@ -651,6 +652,8 @@ def main():
     ap.add_argument("--chains-per-beta", type=int, default=CHAINS_PER_BETA)
     ap.add_argument("--skip-k5", action="store_true", help="leave out the dense-block (5-orbital) line")
     ap.add_argument("--k5-chains", type=int, default=K5_CHAINS, help="chains of the dense-block line")
+    ap.add_argument("--k5-dmma", action="store_true",
+                    help="dense-block line with the block products on the FP64 tensor cores (A/B)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

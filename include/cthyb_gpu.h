@@ -119,6 +119,7 @@ typedef struct {
 #define CTHYB_FLAG_NO_DM 2  /* skip the beta/2 density-matrix measurement */
 #define CTHYB_FLAG_DMMA 4   /* dense-block trace: blocks of >= 16 x 16 on the FP64 tensor cores
                                (mma m8n8k4) instead of FP64 fused multiply-adds */
+#define CTHYB_FLAG_ACCPAIR 8  /* count accepted pair moves by time difference (AccPair) */
 
 /* Create chains for all groups and initialise them like init_Trace
  * (Trace.F90:340-701): window from TaudiffMax, outer superstate drawn with
@@ -253,6 +254,14 @@ int cthyb_batch_move_counters4(cthyb_batch_t batch, int chain, int64_t* out4);
  * [f_annihilator][f_creator][bin], f = 2(b-1)+(s-1), normalised as
  * Gtau_full (CTQMC.F90:8752-8753; MeasGtauRem_full, CTQMC.F90:2475-2584). */
 int cthyb_batch_results_full(cthyb_batch_t batch, int chain, double* gtau_full);
+/* Groups with CTHYB_FLAG_ACCPAIR: accepted pair insertions and removals by
+ * flavour and time difference, (Nd, 2, Ntau) Fortran order, bin
+ * min(Ntau, floor(dtau / beta * Ntau) + 1) (AccPair of the warmup and
+ * measurement loops, CTQMC.F90:3579-3582, 4112-4122, 8203-8204; the flavour
+ * of the earlier operator of an insertion, of the creator of a removal);
+ * counts since the last cthyb_batch_reset_measurements. */
+int cthyb_batch_results_accpair(cthyb_batch_t batch, int chain, double* accpair);
+
 /* Off-diagonal groups with nleg > 0: Legendre coefficients of G for every
  * flavour pair, (2Nd, 2Nd, nleg) with index [f_annihilator][f_creator][l],
  * normalised as GLeg_full (CTQMC.F90:8766-8771; measured by

@@ -628,3 +628,33 @@ def test_offdiag_proposal_stream_and_measurement_parity(lib, kind, tdm, pout, np
     so, sg = co.state(), b.state(0)
     assert so["cfgsign"] == sg["cfgsign"] and so["det_sign"] == sg["det_sign"]
     assert abs(so["det_log"] - sg["det_log"]) < 1e-8
+
+
+def test_accepted_pair_histogram(lib):
+    """AccPair of the measurement loop (CTQMC.F90:3579-3582, 4112-4122):
+    the device histogram of accepted pair moves by flavour and time
+    difference equals the one built from the oracle's proposal records of
+    the same run (bin min(Ntau, floor(dtau / beta * Ntau) + 1))."""
+    beta, ntau, nprop = 10.0, 40, 6000
+    pr = P.config_problem("dd3", beta=beta)
+    mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    co = O.Chain(mo, beta, pr["ftau"], ntau, seed=31, taudiff_max=5.0, ncorr=50)
+    co.start_log(nprop)
+    co.warmup(nprop)
+    ref = co.log()
+    mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    b = E.Batch(mg, [E.Group(beta, pr["ftau"], ntau, nchains=1, seed0=31, taudiff_max=5.0, ncorr=50,
+                             kcap=64, opcap=512, measure_accpair=True)])
+    b.warmup(nprop)
+    b.sync()
+    got = b.results_accpair(0)
+    acc = ref[(ref["outcome"] == 4) & (ref["move"] <= 1)]
+    want = np.zeros((3, 2, ntau))
+    for r in acc:
+        dt = abs(r["tau_a"] - r["tau_c"])
+        k = min(ntau, int(np.floor(dt / beta * ntau)) + 1)
+        want[r["orb"] - 1, r["spin"] - 1, k - 1] += 1
+    assert want.sum() > 500
+    assert np.array_equal(got, want)
+    b.reset_measurements()
+    assert not np.any(b.results_accpair(0))

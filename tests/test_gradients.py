@@ -297,7 +297,11 @@ def test_score_function_dG_dU_three_orbital():
     chains (per-chain covariances alone would drop the covariance between
     the chains' means, which is large where a chain keeps its sector for a
     long time) against central differences of G(tau) from independent runs
-    at U +- 0.05."""
+    at U +- 0.05.  At beta = 50 the sector populations settle slowly and
+    the finite differences of runs that start from U-dependent initial
+    sectors carry that: 4e4 thermalisation proposals leave them 3 sigma
+    above the score estimate, 1.5e5 proposals bring them within about one
+    sigma, so the runs thermalise for 1.5e5 proposals."""
     from w2dynamics_gb300 import engine as E
     beta, nd, u0, j, du, n, nt = 50.0, 3, 4.0, 0.6, 0.05, 2048, 8
     pr = P.config_problem("dd3", beta=beta)
@@ -311,7 +315,7 @@ def test_score_function_dG_dU_three_orbital():
         dE = GR.density_density_directions(nd, mg.fock_states)[2 * nd:2 * nd + 1] if score else None
         b = E.Batch(mg, [E.Group(beta, pr["ftau"], nt, nchains=n, seed0=seed0, taudiff_max=5.0, ncorr=50,
                                  kcap=64, opcap=512, score_dE=dE, **moves)])
-        b.warmup(40000)
+        b.warmup(150000)
         b.measure(400)
         b.sync()
         G = b.group_gtau(0).reshape(n, 2 * nd, nt).mean(axis=1)  # average over the degenerate flavours

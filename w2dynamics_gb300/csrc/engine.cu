@@ -1919,6 +1919,18 @@ __device__ NOINL void ph_decide(Ctx& c, Prop& p) {
   if (!accept) prop_end(c, p, 3);
 }
 
+// AccPair (CTQMC.F90:3579-3582, 4112-4122): an accepted pair insertion or
+// removal of flavour f whose operators are dt apart, binned as
+// min(Ntau, floor(dt / beta * Ntau) + 1) (NAccPair = NGtau, AccPairMax =
+// beta in the warmup and measurement loops, CTQMC.F90:8203-8204).
+__device__ __forceinline__ void count_accpair(const Ctx& c, int f, double dt) {
+  if (!c.g->o_accpair || c.lane != 0) return;
+  const int nt = c.g->ntau;
+  int bin = (int)floor(__dmul_rn(__ddiv_rn(dt, c.g->beta), (double)nt)) + 1;
+  bin = bin > nt ? nt : (bin < 1 ? 1 : bin);
+  ((double*)(c.g->base + (size_t)c.chain * c.g->stride + c.g->o_accpair))[(size_t)f * nt + bin - 1] += 1.0;
+}
+
 // Phase 5: accepted insertion: get_MatAdd in slot order (w = R^T M, rank-one
 // update, new row and column), sorted and operator arrays, tree flip, sign.
 __device__ NOINL void ph_accept_add(Ctx& c, Prop& p) {
@@ -1969,6 +1981,7 @@ __device__ NOINL void ph_accept_add(Ctx& c, Prop& p) {
     h.acc_add++;
     h.acc_since_refresh++;
     h.w_opbytes += 24ll * (K - p.p1) + 40ll * k;
+    count_accpair(c, f, __dsub_rn(md.t2, md.t1));
   }
   __syncwarp();
   double sgn = config_sign(c);
@@ -2038,6 +2051,7 @@ __device__ NOINL void ph_accept_rem(Ctx& c, Prop& p) {
     h.outer_sst = p.snew;
     h.acc_rem++;
     h.acc_since_refresh++;
+    count_accpair(c, f, __dsub_rn(p.ty, p.tx));
     h.w_opbytes += 24ll * (K - p.ix) + 40ll * k;
     // update_NPairs(-1): the pair and the partners of its members
     const double* oppx = srt_ptr(c, f, 1 - p.cax);
@@ -3662,6 +3676,7 @@ __device__ NOINL void ph_add_od(Ctx& c, Prop& p) {
     }
     __syncwarp();
     od_accept(c, det_lg, det_sg, tr_lg, tr_sg, new_outer, np_new);
+    count_accpair(c, c1 >> 1, __dsub_rn(t2, t1));
     if (c.lane == 0) h.acc_add++;
     r.outcome = 4;
   } else {
@@ -3796,6 +3811,7 @@ __device__ NOINL void ph_rem_od(Ctx& c, Prop& p) {
     __syncwarp();
     const int np_new = count_pairs_od(c);
     od_accept(c, det_lg, det_sg, tr_lg, tr_sg, new_outer, np_new);
+    count_accpair(c, code_c >> 1, __dsub_rn(ty, tx));
     if (c.lane == 0) h.acc_rem++;
     r.outcome = 4;
   } else {
@@ -5647,6 +5663,11 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   g.nscore = (d.nscore > 0 && d.score_dE && mono) ? std::min(d.nscore, 32) : 0;
   g.o_score = off;
   off = align_up(off + (size_t)g.nscore * (1 + (size_t)nf * d.ntau) * 8, 256);
+  g.o_accpair = 0;
+  if (d.flags & CTHYB_FLAG_ACCPAIR) {
+    g.o_accpair = off;
+    off = align_up(off + (size_t)nf * d.ntau * 8, 256);
+  }
   g.o_dense = off;
   size_t dense = std::max((size_t)2 * hm.nsmax * hm.nsmax + 2 * hm.nsmax, (size_t)2 * kcap * kcap) * 8;
   off = align_up(off + dense, 256);
@@ -6919,6 +6940,22 @@ int cthyb_batch_results_full(cthyb_batch_t B, int chain, double* gtau_full) {
   const double ms = h.cnt_meas ? h.meas_sign / (double)h.cnt_meas : 0.0;
   const double scale = (h.cnt_meas && ms != 0.0) ? (double)nt / (G->g.beta * G->g.beta) / ((double)h.cnt_meas * ms) : 0.0;
   for (size_t i = 0; i < acc.size(); ++i) gtau_full[i] = acc[i] * scale;  // -acc * zScaling * Ntau / beta^2
+  return CTHYB_OK;
+}
+
+int cthyb_batch_results_accpair(cthyb_batch_t B, int chain, double* accpair) {
+  GroupHost* G;
+  int c;
+  int rc = find_chain(B, chain, &G, &c);
+  if (rc) return rc;
+  if (!G->g.o_accpair) return fail(CTHYB_ERR_ARG, "the group does not measure accepted pairs (CTHYB_FLAG_ACCPAIR)");
+  if (!accpair) return fail(CTHYB_ERR_ARG, "null");
+  const int nf = B->model->hm.nf, nt = G->g.ntau, nd = B->model->hm.nd;
+  std::vector<double> raw((size_t)nf * nt);
+  CK(cudaMemcpy(raw.data(), G->g.base + (size_t)c * G->g.stride + G->g.o_accpair, raw.size() * 8,
+                cudaMemcpyDeviceToHost));
+  for (int f = 0; f < nf; ++f)
+    for (int t = 0; t < nt; ++t) accpair[(f / 2) + nd * ((f % 2) + 2 * (size_t)t)] = raw[(size_t)f * nt + t];
   return CTHYB_OK;
 }
 

@@ -89,7 +89,8 @@ struct DGroup {
       o_scr, o_gtau, o_histo, o_dm, o_gleg, o_outer, o_dense, o_log, o_glob,  // o_glob: 0 without global/shift moves
       o_glscr,  // per-lane Legendre partial sums (0 when nleg == 0)
       o_chk,    // dense-block models: ket and bra checkpoints at the 2^L + 1 bin edges
-      o_score;  // score sums [nscore] and G * score sums [nscore][nf][ntau]
+      o_score,  // score sums [nscore] and G * score sums [nscore][nf][ntau]
+      o_accpair;  // accepted pairs by time difference [nf][ntau] (0: not measured)
   size_t chk_bytes;  // bytes of one checkpoint
   size_t node_bytes;   // bytes of one node slot
   long long logcap;

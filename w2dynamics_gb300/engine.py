@@ -22,6 +22,7 @@ RECORD_DTYPE = np.dtype([
 FLAG_DENSE = 1
 FLAG_NO_DM = 2
 FLAG_DMMA = 4
+FLAG_ACCPAIR = 8
 
 EXPORTS = (
     "cthyb_last_error", "cthyb_model_create", "cthyb_model_destroy", "cthyb_model_info",
@@ -30,7 +31,7 @@ EXPORTS = (
     "cthyb_batch_nchains", "cthyb_batch_set_taudiffmax", "cthyb_batch_warmup",
     "cthyb_batch_measure", "cthyb_batch_reset_measurements", "cthyb_batch_sync",
     "cthyb_batch_stream", "cthyb_batch_use_graphs", "cthyb_batch_set_schedule", "cthyb_batch_set_team", "cthyb_batch_autotune", "cthyb_batch_results",
-    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_move_counters4", "cthyb_batch_results_full", "cthyb_batch_results_gleg_full", "cthyb_batch_minv_full", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
+    "cthyb_batch_group_sums", "cthyb_batch_move_counters", "cthyb_batch_move_counters4", "cthyb_batch_results_full", "cthyb_batch_results_gleg_full", "cthyb_batch_results_accpair", "cthyb_batch_minv_full", "cthyb_batch_results_extra", "cthyb_batch_gradients", "cthyb_batch_gradients_device", "cthyb_batch_results_score", "cthyb_batch_state", "cthyb_batch_get_config",
     "cthyb_batch_set_config", "cthyb_batch_set_configs", "cthyb_batch_get_configs", "cthyb_batch_minv", "cthyb_batch_refresh_minv",
     "cthyb_batch_set_log", "cthyb_batch_get_log", "cthyb_batch_work_counters",
     "cthyb_batch_drift", "cthyb_batch_chain_stats", "cthyb_batch_group_gtau_raw", "cthyb_probe_fp64", "cthyb_batch_log_weights_device",
@@ -100,6 +101,7 @@ def load(build_if_missing=False):
     L.cthyb_batch_results_full.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_minv_full.argtypes = [vp, C.c_int, ip, dp]
     L.cthyb_batch_results_gleg_full.argtypes = [vp, C.c_int, dp]
+    L.cthyb_batch_results_accpair.argtypes = [vp, C.c_int, dp]
     L.cthyb_batch_results_extra.argtypes = [vp, C.c_int, dp, dp, dp, dp, dp, dp, dp]
     L.cthyb_batch_gradients.argtypes = [vp, C.c_int, dp, dp, dp, dp]
     L.cthyb_batch_results_score.argtypes = [vp, C.c_int, dp, dp]
@@ -214,7 +216,7 @@ class Group:
     def __init__(self, beta, ftau, ntau, nchains=1, seed0=0, seeds=None, taudiff_max=-1.0,
                  ncorr=100, p_outer=0.0, kcap=0, opcap=0, tree_levels=0, maxhisto=500,
                  dense=False, measure_dm=True, p_global=0.0, p_shift=0.0, nleg=0, score_dE=None,
-                 symmoves=None, p_4op=0.0, ftau_full=None, refresh_every=0, dmma=False):
+                 symmoves=None, p_4op=0.0, ftau_full=None, refresh_every=0, dmma=False, measure_accpair=False):
         self.beta = float(beta)
         self.ftau = np.asfortranarray(np.asarray(ftau, np.float64))
         self.ntau = int(ntau)
@@ -235,7 +237,8 @@ class Group:
         self.symmoves = None if symmoves is None else np.ascontiguousarray(np.atleast_2d(symmoves), np.int32)
         self.kcap, self.opcap, self.tree_levels = int(kcap), int(opcap), int(tree_levels)
         self.maxhisto = int(maxhisto)
-        self.flags = (FLAG_DENSE if dense else 0) | (0 if measure_dm else FLAG_NO_DM) | (FLAG_DMMA if dmma else 0)
+        self.flags = ((FLAG_DENSE if dense else 0) | (0 if measure_dm else FLAG_NO_DM) | (FLAG_DMMA if dmma else 0)
+                      | (FLAG_ACCPAIR if measure_accpair else 0))
         # accepted pair updates between full rebuilds of the inverse matrices
         # (0: the library default, negative: never)
         self.refresh_every = int(refresh_every)
@@ -492,6 +495,15 @@ class Batch:
         out = np.zeros(nf * nf * g.ntau)
         _check(load().cthyb_batch_results_full(self.h, chain, _dp(out)))
         return out.reshape(nf, nf, g.ntau)
+
+    def results_accpair(self, chain):
+        """Accepted pair moves by flavour and time difference, (Nd, 2, Ntau)
+        (groups built with measure_accpair=True)."""
+        g = self.groups[self._group_of[chain]]
+        nd = self.model.nd
+        out = np.zeros(nd * 2 * g.ntau)
+        _check(load().cthyb_batch_results_accpair(self.h, chain, _dp(out)))
+        return out.reshape((nd, 2, g.ntau), order="F")
 
     def results_gleg_full(self, chain):
         """Off-diagonal groups: Legendre coefficients of G for every flavour

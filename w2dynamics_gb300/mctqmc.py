@@ -37,17 +37,17 @@ solves (the batch form of the driver's mc_config_inout warm start and its
 CtHybConfig npz files, cthyb_solver.py:24-87, 316-345).
 
 Parameters selecting moves or modes outside the engine (worm and
-flavour-change moves, segment, state sampling, retarded interactions;
-4-operator moves together with offdiag = 1) raise
-NotImplementedError at init_solver.  With offdiag = 1 the full Ftau_full is
-used and gtau_full holds G for every flavour pair (MeasGtauRem_full).  The
+flavour-change moves, segment, state sampling, retarded interactions)
+raise NotImplementedError at init_solver.  With offdiag = 1 the full
+Ftau_full is used and gtau_full / gleg_full hold G and its Legendre
+coefficients for every flavour pair (MeasGtauRem_full).  The
 trace-recomputation histograms lhisto/rhisto describe the reference's
 list-walking implementation and are returned as zeros; outer trace
 contributions are measured for density-density (monomial) models.  The
 window calibration (ctqmc_calibrate, run by the driver for TaudiffMax <= 0)
 fills accpairtau and accpair from the engine's proposal records; after a
-measurement accpair (accepted pairs by time difference, a diagnostic) is
-returned as zeros of its (Nd, 2, Ntau) shape.  Each
+measurement accpair holds the accepted pairs of the measurement run by
+flavour and time difference (Nd, 2, Ntau), counted on the device.  Each
 init_solver seeds the chains from Nseed; the reference continues one global
 random stream across solves, so solves after the first draw different
 (equally valid) streams.
@@ -205,7 +205,7 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
                     p_shift=_real("PercentageTauShiftMove", 0.0),
                     nleg=_int("NLegMax", 100),
                     p_4op=_real("Percentage4OperatorMove", 0.0),
-                    ftau_full=ftau_full if offdiag else None)
+                    ftau_full=ftau_full if offdiag else None, measure_accpair=True)
     nsym = _int("NSymMove", 0)
     if nsym > 0:  # SymMove01 ... (Trace.F90:471-477)
         group.symmoves = np.array([[int(x) for x in _raw("SymMove%02d" % (i + 1)).split()]
@@ -405,7 +405,11 @@ def _collect():
     tracecontribstates = sum(x["contrib_state"] for x in ext) / _nchains
     lhisto = np.zeros(1)
     rhisto = np.zeros(1)
-    accpair = np.zeros((nd, 2, _int("Ntau")), np.int64)
+    if hasattr(_batch, "results_accpair"):
+        # AccPair of the measurement run (NAccPair = Ntau bins over [0, beta))
+        accpair = sum(_batch.results_accpair(c) for c in range(_nchains)).astype(np.int64)
+    else:
+        accpair = np.zeros((nd, 2, _int("Ntau")), np.int64)
 
 
 # ------------------------------------------------------ configuration access
