@@ -58,6 +58,9 @@ ONE_CHAIN_BLOCKS, ONE_CHAIN_MEAS = 16, 30  # one-chain form: blocks x measuremen
 # dense-block workload: 5-orbital Kanamori with spin-flip and pair hopping
 K5_BETA, K5_CHAINS, K5_THERM, K5_STEPS, K5_TUNE = 40.0, 1024, 2000, 2, 20
 K5_TUNE_PROPS = 9 * 2 * K5_TUNE  # the autotuner's dense-model candidates x 2 K5_TUNE proposals
+# off-diagonal hybridisation workload: the 3-orbital model with an orbital-mixing bath
+OD_BETA, OD_CHAINS, OD_THERM, OD_STEPS, OD_MIX = 25.0, 1024, 10000, 20, 0.3
+OD_CPU_CHAINS_PER_CORE, OD_CPU_STEPS = 8, 100
 METRIC = "MC updates/sec on 1 GB300, batched vs one-chain form, at equal G(tau) error"
 PROFILE = os.path.join(ROOT, "profiles", "k_sweep_sync_bench_4096chains.md")
 
@@ -359,6 +362,79 @@ def run_k5(E, args, fp64_peak):
                          "trace_flops_per_proposal": wc["trace_flops"] / max(1, wc["proposals"])}}
 
 
+def od_problem():
+    """The batched workload's 3-orbital model at beta = OD_BETA with an
+    orbital-mixing bath: F_{bs,b's'}(tau) = delta_ss' A_bb' F(tau), F the
+    semicircular bath's, A = (1 - OD_MIX) 1 + OD_MIX (all ones), positive
+    definite (offdiag = 1: one inverse matrix over all six flavours)."""
+    from w2dynamics_gb300 import problems as P
+    pr = P.config_problem("dd3", beta=OD_BETA)
+    nd = pr["nd"]
+    A = (1.0 - OD_MIX) * np.eye(nd) + OD_MIX * np.ones((nd, nd))
+    ff = np.zeros((nd, 2, nd, 2, pr["ntau"]))
+    for b in range(nd):
+        for b2 in range(nd):
+            for s in range(2):
+                ff[b, s, b2, s] = A[b, b2] * pr["ftau"][0, 0]
+    pr["ftau_full"] = ff
+    return pr
+
+
+def run_od(E):
+    """Off-diagonal workload: OD_CHAINS chains (seed = chain index),
+    TaudiffMax = TDM, NCorr = NCORR, PercentageOuterMove as the headline,
+    OD_THERM thermalisation proposals, then OD_STEPS timed steps."""
+    import torch
+    pr = od_problem()
+    model = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    b = E.Batch(model, [E.Group(OD_BETA, pr["ftau"], pr["ntau"], nchains=OD_CHAINS, seed0=0, taudiff_max=TDM,
+                                ncorr=NCORR, kcap=64, opcap=256, ftau_full=pr["ftau_full"], **MOVES)])
+    b.warmup(OD_THERM)
+    b.measure(1)
+    b.sync()
+    k0 = float(b.chain_stats(0)["noper"].mean())
+    stream = torch.cuda.ExternalStream(b.stream())
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    b.measure(OD_STEPS)
+    stop.record(stream)
+    stop.synchronize()
+    ms = start.elapsed_time(stop)
+    b.sync()
+    st = b.chain_stats(0)
+    _, ssum, cnt = b.group_sums(0)
+    b.close()
+    return {"workload": f"{OD_CHAINS} chains, 3-orbital density-density U=4 J=0.6 mu=3.3 (Nt Szt), beta={OD_BETA}, "
+                        f"orbital-mixing bath F_bb' = (delta_bb' (1-{OD_MIX}) + {OD_MIX}) F_semicircle, offdiag=1, "
+                        f"Ntau=Nftau=2000, TaudiffMax={TDM}, NCorr={NCORR}, PercentageOuterMove=0.1, "
+                        f"{OD_THERM} thermalisation proposals, {OD_STEPS} timed steps",
+            "value": OD_CHAINS * NCORR * OD_STEPS / (ms / 1e3), "unit": "MC updates/s", "ms_per_step": ms / OD_STEPS,
+            "mean_order": [k0, float(st["noper"].mean())], "mean_sign": ssum / max(1, cnt)}
+
+
+def oracle_rate_od(cores):
+    """The oracle on the off-diagonal workload through the GPU run's window:
+    OD_CPU_CHAINS_PER_CORE chains per host core, OD_THERM + NCORR untimed
+    proposals, then OD_CPU_STEPS timed measurement cycles."""
+    pr = od_problem()
+    model_args = (pr["nd"], pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
+    specs = [[(OD_BETA, i * OD_CPU_CHAINS_PER_CORE + j, pr["ftau_full"], TDM, MOVES)
+              for j in range(OD_CPU_CHAINS_PER_CORE)] for i in range(cores)]
+    pools = _spawn_pools(model_args, specs)
+    try:
+        k0 = sum((r.get() for r in [p.apply_async(_worker_warm, (OD_THERM + NCORR,)) for p in pools]), [])
+        res = [r.get() for r in [p.apply_async(_worker_run, (OD_CPU_STEPS,)) for p in pools]]
+    finally:
+        for p in pools:
+            p.terminate()
+    tmax = max(t for t, _, _ in res)
+    return {"value": sum(n for _, n, _ in res) / tmax, "unit": "MC updates/s", "cores": cores, "kind": "port",
+            "sample": f"{cores * OD_CPU_CHAINS_PER_CORE} chains ({OD_CPU_CHAINS_PER_CORE} per host core), "
+                      f"{OD_THERM + NCORR} untimed proposals, then {OD_CPU_STEPS} timed measurement cycles "
+                      f"({tmax:.2f} s per core)",
+            "mean_order_start": _per_beta(k0), "mean_order_end": _per_beta(sum((k for _, _, k in res), []))}
+
+
 def run_gpu(args, rank=0, world=1):
     import torch
     from w2dynamics_gb300 import engine as E
@@ -447,10 +523,13 @@ def run_gpu(args, rank=0, world=1):
     dmix = default_mix(E, probs, cpb, args.steps)
     fp64_dfma, fp64_dmma = E.probe_fp64()
     k5 = run_k5(E, args, fp64_dfma) if not args.skip_k5 else None
+    od = run_od(E) if not args.skip_od else None
     cores = os.cpu_count() or 1
     cpu = oracle_rate(cores, args.steps, args.warmup)
     if k5 is not None:
         k5["cpu_baseline"] = oracle_rate_k5(cores)
+    if od is not None:
+        od["cpu_baseline"] = oracle_rate_od(cores)
     hbm, hbm_kind = hbm_peak()
     bytes_per_step = (wc["m_bytes"] + wc["op_bytes"]) / max(1, args.steps)
     achieved = bytes_per_step / (ms / 1e3 / args.steps) / 1e9
@@ -501,6 +580,7 @@ def run_gpu(args, rank=0, world=1):
         "default_move_mix": dmix,
         "drift": dict(drift, refresh_every=1000),
         "dense_block": k5,
+        "offdiag": od,
         "work": wc,
         "schedule": {"warps_per_block": sched, "chosen_by": "autotuner (cthyb_batch_autotune) after thermalisation",
                      "cuda_graphs": "end-to-end solve (one launch per step); the device-timed "
@@ -651,6 +731,7 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--chains-per-beta", type=int, default=CHAINS_PER_BETA)
     ap.add_argument("--skip-k5", action="store_true", help="leave out the dense-block (5-orbital) line")
+    ap.add_argument("--skip-od", action="store_true", help="leave out the off-diagonal hybridisation line")
     ap.add_argument("--k5-chains", type=int, default=K5_CHAINS, help="chains of the dense-block line")
     ap.add_argument("--k5-dmma", action="store_true",
                     help="dense-block line with the block products on the FP64 tensor cores (A/B)")

@@ -3450,16 +3450,7 @@ __device__ NOINL double od_cfgsign(Ctx& c) {
   return -(h.trace_sign * h.det_sign * rs);
 }
 
-// Copy of the present operator arrays into the o_glob space (K entries).
-__device__ __forceinline__ void od_save(Ctx& c, int K) {
-  double* t = glob_optau(c);
-  int* o = glob_opcode(c);
-  for (int i = c.lane; i < K; i += 32) {
-    t[i] = c.optau[i];
-    o[i] = c.opcode[i];
-  }
-  __syncwarp();
-}
+// The present operator arrays back from their copy in the o_glob space.
 __device__ NOINL void od_restore(Ctx& c, int K) {
   const double* t = glob_optau(c);
   const int* o = glob_opcode(c);
@@ -3486,6 +3477,73 @@ __device__ NOINL void od_accept(Ctx& c, double det_lg, double det_sg, double tr_
   Hdr& h = *c.h;
   tree_flip_all(c);
   if (c.g->o_chk) chk_invalidate(c);
+  if (c.lane == 0) {
+    h.det_log = h.det_log + det_lg;
+    h.det_sign = h.det_sign * det_sg;
+    h.trace_log = tr_lg;
+    h.trace_sign = tr_sg;
+    h.outer_sst = new_outer;
+    h.npairs = np_new;
+    h.acc_since_refresh++;
+  }
+  __syncwarp();
+  const double cs = od_cfgsign(c);
+  if (c.lane == 0) h.cfgsign = cs;
+  __syncwarp();
+}
+
+// Off-diagonal pair moves evaluate the proposed configuration like the
+// diagonal ones: the two changed leaves of the time-bin tree and their
+// ancestors are rebuilt into the inactive slots (quantum numbers from the
+// superstate maps, the trace from the state maps or the dense-block
+// checkpoints), and the operator arrays change only on acceptance.
+
+// Quantum-number check of the proposal md (check_sst_sequence,
+// Trace.F90:1243-1304) on the proposed superstate tree; snew: the outer
+// superstate of the proposed configuration (a new one with change_outer).
+__device__ NOINL bool od_tree_qn(Ctx& c, Mod& md, bool co, int& snew) {
+  tree_propose(c, md, true, false, true);
+  const int root_new = 1 - c.act[1];
+  const int s0 = c.h->outer_sst;
+  snew = s0;
+  if (!co) return node_ss(c, 1, root_new)[s0] == s0;
+  const int inside = old_prefix(c, s0, md.t2);
+  snew = inside >= 0 ? new_suffix(c, md, inside, md.t2) : -1;
+  return snew >= 0 && node_ss(c, 1, root_new)[snew] == snew;
+}
+
+// Removable pairs (update_NPairs with off-diagonal hybridisation) that the
+// two operators of an insertion add: present operators of the other kind
+// (creator/annihilator, any flavour) whose earlier member lies in the window
+// and whose later member lies within TaudiffMax of it and inside the
+// window, and the inserted pair itself.
+__device__ NOINL int od_new_pairs(Ctx& c, const Mod& md) {
+  const Hdr& h = *c.h;
+  const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  int n = 0;
+  for (int i = c.lane; i < h.K; i += 32) {
+    const double t = c.optau[i];
+    const int ca = c.opcode[i] & 1;
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const double tn = q ? md.t2 : md.t1;
+      if (((q ? md.c2 : md.c1) & 1) == ca) continue;
+      const double e = fmin(t, tn), l = fmax(t, tn);
+      n += e >= wmin && e <= wmax && l <= fmin(wmax, __dadd_rn(e, tdm));
+    }
+  }
+  n = wsumi(n);
+  return n + (md.t1 >= wmin && md.t1 <= wmax && md.t2 <= fmin(wmax, __dadd_rn(md.t1, tdm)));
+}
+
+// Installation of an accepted off-diagonal pair move whose operator arrays,
+// inverse matrix and bin starts are already updated: tree flip of the
+// changed path, checkpoints, weights, pairs, sign.
+__device__ NOINL void od_accept_pair(Ctx& c, const Mod& md, double det_lg, double det_sg, double tr_lg,
+                                     double tr_sg, int new_outer, int np_new) {
+  Hdr& h = *c.h;
+  tree_accept(c, md);
+  chk_keep(c, md, new_outer);
   if (c.lane == 0) {
     h.det_log = h.det_log + det_lg;
     h.det_sign = h.det_sign * det_sg;
@@ -3532,12 +3590,18 @@ __device__ NOINL void ph_add_od(Ctx& c, Prop& p) {
     set_status(c, ST_CAPACITY);
     return;
   }
-  bool equal = tau_a == tau_c;
-  for (int i = c.lane; i < K; i += 32) {
-    const double t = c.optau[i];
-    equal = equal || t == tau_a || t == tau_c;
-  }
-  if (__any_sync(FULL, equal)) {
+  const bool afirst = tau_a < tau_c;
+  Mod& md = p.md;
+  md.type = 1;
+  md.t1 = afirst ? tau_a : tau_c;
+  md.t2 = afirst ? tau_c : tau_a;
+  md.c1 = afirst ? code_a : code_c;
+  md.c2 = afirst ? code_c : code_a;
+  md.ix = md.iy = -1;
+  md.b1 = bin_of(c, md.t1);
+  md.b2 = bin_of(c, md.t2);
+  const int p1 = op_lower_bound(c, md.b1, md.t1), p2 = op_lower_bound(c, md.b2, md.t2);
+  if (teq(tau_a, tau_c) || (p1 < K && teq(c.optau[p1], md.t1)) || (p2 < K && teq(c.optau[p2], md.t2))) {
     if (c.lane == 0) h.qn_add++;
     r.outcome = 0;
     __syncwarp();
@@ -3546,41 +3610,20 @@ __device__ NOINL void ph_add_od(Ctx& c, Prop& p) {
   const int pos_c = od_pos_new(c, code_c, tau_c), pos_a = od_pos_new(c, code_a, tau_a);
   r.fpos_c = pos_c;
   r.fpos_a = pos_a;
-  // quantum numbers on the present arrays (check_sst_sequence)
-  const bool afirst = tau_a < tau_c;
-  const double t1 = afirst ? tau_a : tau_c, t2 = afirst ? tau_c : tau_a;
-  const int c1 = afirst ? code_a : code_c, c2 = afirst ? code_c : code_a;
-  const int p1 = wlb(c.optau, K, t1, c.lane), p2 = wlb(c.optau, K, t2, c.lane);
-  const int none[4] = {-1, -1, -1, -1};
-  const int bs = old_prefix(c, h.outer_sst, t1);
-  int new_outer = h.outer_sst;
-  bool qn_ok;
-  if (!p.co) {
-    const int es = old_prefix(c, h.outer_sst, t2);
-    int wk = conn_code(m, bs, c1);
-    wk = wk < 0 ? -1 : walk_ops(c, wk, p1, p2, none);
-    wk = conn_code(m, wk, c2);
-    qn_ok = bs >= 0 && wk >= 0 && wk == es;
-  } else {
-    int s2 = conn_code(m, old_prefix(c, h.outer_sst, t2), c2);
-    s2 = s2 < 0 ? -1 : walk_ops(c, s2, p2, K, none);
-    new_outer = s2;
-    qn_ok = false;
-    if (s2 >= 0) {
-      int back = walk_ops(c, s2, 0, p1, none);
-      back = conn_code(m, back, c1);
-      qn_ok = back >= 0 && back == bs;
-    }
-  }
-  if (!qn_ok) {
+  int snew;
+  if (!od_tree_qn(c, md, p.co, snew)) {
     if (c.lane == 0) h.qn_add++;
     r.outcome = 1;
     __syncwarp();
     return;
   }
+  if (c.mono) tree_propose(c, md, false, true, false);
+  double tr_mx, tr_sum;
+  proposed_trace(c, md, snew, tr_mx, tr_sum, solo_team(c));
   // determinant ratio S - R.M.Q over the full matrix; Q over the present
   // annihilators with the flavour pair (creator, annihilator) as the
   // reference passes it (Trace.F90:2892), R over the present creators
+  // (the block positions reuse the gathered-leaf buffer, no longer needed)
   double* Q = c.scr;
   double* R = c.scr + c.kcap;
   double* v = c.scr + 2 * c.kcap;
@@ -3606,34 +3649,27 @@ __device__ NOINL void ph_add_od(Ctx& c, Prop& p) {
   }
   const double ratio = S - wsum(part);
   const double sig = ((pos_c - pos_a) & 1) ? -1.0 : 1.0;
-  const double det_lg = log(fabs(ratio)), det_sg = (ratio >= 0.0 ? 1.0 : -1.0) * sig;
-  // proposed arrays: the pair merged in
-  od_save(c, K);
-  {
-    const double* tau_old = glob_optau(c);
-    const int* opc_old = glob_opcode(c);
-    for (int i = c.lane; i < K; i += 32) {
-      const double t = tau_old[i];
-      const int d = (t1 < t) + (t2 < t);
-      c.optau[i + d] = t;
-      c.opcode[i + d] = opc_old[i];
-    }
-    if (c.lane == 0) {
-      c.optau[p1] = t1;
-      c.opcode[p1] = c1;
-      c.optau[p2 + 1] = t2;
-      c.opcode[p2 + 1] = c2;
-      h.K = K + 2;
-    }
+  const double det_sg = (ratio >= 0.0 ? 1.0 : -1.0) * sig;
+  if (c.lane == 0) {
+    h.w_mbytes += 8ll * k * k + 32ll * k;
+    h.w_mflops += 2ll * k * k + 2ll * k;
+  }
+  if (h.npairs == -1) {
+    const int np = count_pairs_od(c);
+    if (c.lane == 0) h.npairs = np;
     __syncwarp();
   }
-  double tr_lg, tr_sg;
-  od_trace(c, new_outer, tr_lg, tr_sg);
+  const int np_new = h.npairs + od_new_pairs(c, md);
   const double rnd = grnd(c);
-  const int np_new = count_pairs_od(c);
   const double n2 = 2.0 * m.nd;
-  const double wr = exp(__dsub_rn(tr_lg, h.trace_log) + det_lg);
+  const double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(ratio));
   const double prob = fabs(__dmul_rn(__ddiv_rn(__dmul_rn(tdf, __dmul_rn(n2, n2)), (double)np_new), wr));
+  const bool accept = rnd < prob;
+  double det_lg = 0.0, tr_lg = 0.0, tr_sg = 0.0;
+  if (accept || c.log) {
+    det_lg = log(fabs(ratio));
+    trace_log(tr_mx, tr_sum, tr_lg, tr_sg);
+  }
   r.det_log = det_lg;
   r.det_sign = det_sg;
   r.tr_log = tr_lg;
@@ -3641,7 +3677,7 @@ __device__ NOINL void ph_add_od(Ctx& c, Prop& p) {
   r.prob = prob;
   r.rand = rnd;
   r.npairs = np_new;
-  if (rnd < prob) {
+  if (accept) {
     // get_MatAdd in block order: new row pos_c, new column pos_a
     for (int j = c.lane; j < k; j += 32) {
       double acc = 0.0;
@@ -3674,13 +3710,21 @@ __device__ NOINL void ph_add_od(Ctx& c, Prop& p) {
       const size_t idx = (size_t)(e / kn) * ld + (e % kn);
       Mw[idx] = T[idx];
     }
+    if (c.lane == 0) {
+      h.w_mbytes += 24ll * kn * kn + 16ll * k * k;
+      h.w_mflops += 4ll * kn * kn;
+      h.w_opbytes += 24ll * (K - p1);
+    }
     __syncwarp();
-    od_accept(c, det_lg, det_sg, tr_lg, tr_sg, new_outer, np_new);
-    count_accpair(c, c1 >> 1, __dsub_rn(t2, t1));
+    ops_insert2(c, p1, p2, md.t1, md.c1, md.t2, md.c2);
+    if (c.lane == 0) h.K = K + 2;
+    __syncwarp();
+    bstart_shift(c, md.b1, md.b2, +1);
+    od_accept_pair(c, md, det_lg, det_sg, tr_lg, tr_sg, snew, np_new);
+    count_accpair(c, md.c1 >> 1, __dsub_rn(md.t2, md.t1));
     if (c.lane == 0) h.acc_add++;
     r.outcome = 4;
   } else {
-    od_restore(c, K);
     r.outcome = 3;
   }
   r.outer_sst = h.outer_sst;
@@ -3715,11 +3759,12 @@ __device__ NOINL void ph_rem_od(Ctx& c, Prop& p) {
   const int cx = c.opcode[ix], cy = c.opcode[iy];
   const bool xc = (cx & 1) == 0;  // x is the creator
   const double tau_c = xc ? tx : ty, tau_a = xc ? ty : tx;
-  const int code_c = xc ? cx : cy, code_a = xc ? cy : cx;
-  const int fc = code_c >> 1, fa = code_a >> 1;
+  const int code_c = xc ? cx : cy;
+  const int fc = code_c >> 1, fa = (xc ? cy : cx) >> 1;
   int* pos = c.bcode[1];
   od_positions(c, pos);
   const int pos_c = pos[xc ? ix : iy] + 1, pos_a = pos[xc ? iy : ix] + 1;
+  __syncwarp();
   const double hprf = __ddiv_rn((double)np, __dmul_rn(__dsub_rn(h.tauwin_max, h.tauwin_min),
                                                       __dsub_rn(fmin(__dadd_rn(tau_a, h.taudiff_max), h.tauwin_max),
                                                                 fmax(__dsub_rn(tau_a, h.taudiff_max), h.tauwin_min))));
@@ -3730,66 +3775,48 @@ __device__ NOINL void ph_rem_od(Ctx& c, Prop& p) {
   r.fpos_c = pos_c;
   r.fpos_a = pos_a;
   r.npairs = np;
-  // quantum numbers on the present arrays
-  const int none[4] = {-1, -1, -1, -1};
-  int new_outer = h.outer_sst;
-  bool qn_ok;
-  if (!p.co) {
-    const int bs = old_prefix(c, h.outer_sst, tx);
-    const int es = conn_code(m, old_prefix(c, h.outer_sst, ty), cy);
-    const int wk = bs < 0 ? -1 : walk_ops(c, bs, ix + 1, iy, none);
-    qn_ok = bs >= 0 && wk >= 0 && wk == es;
-  } else {
-    const int inside = old_prefix(c, h.outer_sst, ty);
-    const int s2 = inside < 0 ? -1 : walk_ops(c, inside, iy + 1, K, none);
-    new_outer = s2;
-    qn_ok = false;
-    if (s2 >= 0) {
-      const int back = walk_ops(c, s2, 0, ix, none);
-      const int target = conn_code(m, old_prefix(c, h.outer_sst, tx), cx);
-      qn_ok = back >= 0 && back == target;
-    }
-  }
-  if (!qn_ok) {
+  Mod& md = p.md;
+  md.type = 2;
+  md.ix = ix;
+  md.iy = iy;
+  md.t1 = tx;
+  md.t2 = ty;
+  md.c1 = md.c2 = 0;
+  md.b1 = bin_of(c, tx);
+  md.b2 = bin_of(c, ty);
+  int snew;
+  if (!od_tree_qn(c, md, p.co, snew)) {
     if (c.lane == 0) h.qn_rem++;
     r.outcome = 1;
     __syncwarp();
     return;
   }
+  if (c.mono) tree_propose(c, md, false, true, false);
+  double tr_mx, tr_sum;
+  proposed_trace(c, md, snew, tr_mx, tr_sum, solo_team(c));
   const int k = K / 2, ld = c.kcap, pc = pos_c - 1, pa = pos_a - 1;
   const double* Mf = M_ptr(c, 0);
   const double dr = Mf[(size_t)pa * ld + pc];
   const double sig = ((pos_c - pos_a) & 1) ? -1.0 : 1.0;
-  const double det_lg = log(fabs(dr)), det_sg = (dr >= 0.0 ? 1.0 : -1.0) * sig;
-  // proposed arrays without the pair
-  od_save(c, K);
-  {
-    const double* tau_old = glob_optau(c);
-    const int* opc_old = glob_opcode(c);
-    for (int i = c.lane; i < K; i += 32) {
-      if (i == ix || i == iy) continue;
-      const int d = (ix < i) + (iy < i);
-      c.optau[i - d] = tau_old[i];
-      c.opcode[i - d] = opc_old[i];
-    }
-    if (c.lane == 0) h.K = K - 2;
-    __syncwarp();
-  }
-  double tr_lg, tr_sg;
-  od_trace(c, new_outer, tr_lg, tr_sg);
+  const double det_sg = (dr >= 0.0 ? 1.0 : -1.0) * sig;
   const double n2 = 2.0 * m.nd;
-  const double wr = exp(__dsub_rn(tr_lg, h.trace_log) + det_lg);
+  const double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(dr));
   const double prob = fabs(__dmul_rn(__ddiv_rn(hprf, __dmul_rn(n2, n2)), wr));
   const double rnd = grnd(c);
+  const bool accept = rnd < prob;
+  double det_lg = 0.0, tr_lg = 0.0, tr_sg = 0.0;
+  if (accept || c.log) {
+    det_lg = log(fabs(dr));
+    trace_log(tr_mx, tr_sum, tr_lg, tr_sg);
+  }
   r.det_log = det_lg;
   r.det_sign = det_sg;
   r.tr_log = tr_lg;
   r.tr_sign = tr_sg;
   r.prob = prob;
   r.rand = rnd;
-  if (rnd < prob) {
+  if (accept) {
     if (fabs(dr) < 1e-12) {  // CTQMC.F90:4062
-      od_restore(c, K);
       set_status(c, ST_NUMERIC);
       return;
     }
@@ -3808,14 +3835,22 @@ __device__ NOINL void ph_rem_od(Ctx& c, Prop& p) {
       const size_t idx = (size_t)(e / kn) * ld + (e % kn);
       Mw[idx] = T[idx];
     }
+    if (c.lane == 0) {
+      h.w_mbytes += 24ll * kn * kn + 16ll * kn;
+      h.w_mflops += 2ll * kn * kn;
+      h.w_opbytes += 24ll * (K - ix);
+    }
     __syncwarp();
+    ops_remove2(c, ix, iy);
+    if (c.lane == 0) h.K = K - 2;
+    __syncwarp();
+    bstart_shift(c, md.b1, md.b2, -1);
     const int np_new = count_pairs_od(c);
-    od_accept(c, det_lg, det_sg, tr_lg, tr_sg, new_outer, np_new);
-    count_accpair(c, code_c >> 1, __dsub_rn(ty, tx));
+    od_accept_pair(c, md, det_lg, det_sg, tr_lg, tr_sg, snew, np_new);
+    count_accpair(c, fc, __dsub_rn(ty, tx));
     if (c.lane == 0) h.acc_rem++;
     r.outcome = 4;
   } else {
-    od_restore(c, K);
     r.outcome = 3;
   }
   r.outer_sst = h.outer_sst;
@@ -3823,7 +3858,6 @@ __device__ NOINL void ph_rem_od(Ctx& c, Prop& p) {
   __syncwarp();
 }
 
-// ---------------------------------------------------------------------------
 // Legendre coefficients of one G sample: lsum[l] += M P_l(x), P_l by the
 // three-term recurrence in the reference's operation order
 // (CTQMC.F90:2368-2389, 2533-2555).
