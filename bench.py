@@ -13,7 +13,10 @@ step = one measurement cycle of every chain: NCorr proposals and the
 Z-space measurements (sign, order histogram, density matrix at beta/2,
 G(tau)).  1 MC update = 1 proposal.  The line also times the reference's
 default move mix (PercentageGlobalMove = PercentageTauShiftMove = 0.005,
-configspec:81-82), whose rare global moves rebuild every inverse matrix.
+configspec:81-82), whose rare global moves rebuild every inverse matrix,
+the dense-block workload (1024 chains of the 5-orbital Kanamori model) and
+an off-diagonal-hybridisation workload (offdiag = 1), each with its own CPU
+baseline.
 
 Footing: every chain is thermalised for THERMALIZE proposals (the GPU run
 reports the mean expansion order of each beta group after every round of
@@ -55,11 +58,16 @@ TUNE = 200           # autotuner proposals per candidate (10 candidates, 2 inter
 E2E_WARMUP = 1000    # re-thermalisation proposals of the warm-started end-to-end solve
 CPU_CHAINS_PER_CORE = 64  # chains per host core in the bounded CPU sample (beta cycling)
 ONE_CHAIN_BLOCKS, ONE_CHAIN_MEAS = 16, 30  # one-chain form: blocks x measurement cycles per beta
+# time-bin tree depth per beta (-1: one leaf; 0: the engine's default from the
+# operator capacity), the measured optima at the thermalised expansion orders
+# (about 14, 36, 74, 148 operators at beta 10, 25, 50, 100)
+BATCH_TREE_LEVELS = {10.0: -1, 25.0: -1, 50.0: 0, 100.0: 0}
+ONE_CHAIN_TREE_LEVELS = {10.0: -1, 25.0: 2, 50.0: 3, 100.0: 4}
 # dense-block workload: 5-orbital Kanamori with spin-flip and pair hopping
 K5_BETA, K5_CHAINS, K5_THERM, K5_STEPS, K5_TUNE = 40.0, 1024, 2000, 2, 20
 K5_TUNE_PROPS = 9 * 2 * K5_TUNE  # the autotuner's dense-model candidates x 2 K5_TUNE proposals
 # off-diagonal hybridisation workload: the 3-orbital model with an orbital-mixing bath
-OD_BETA, OD_CHAINS, OD_THERM, OD_STEPS, OD_MIX = 25.0, 1024, 10000, 20, 0.3
+OD_BETA, OD_CHAINS, OD_THERM, OD_STEPS, OD_MIX = 25.0, 4096, 10000, 20, 0.3
 OD_CPU_CHAINS_PER_CORE, OD_CPU_STEPS = 8, 100
 METRIC = "MC updates/sec on 1 GB300, batched vs one-chain form, at equal G(tau) error"
 PROFILE = os.path.join(ROOT, "profiles", "k_sweep_sync_bench_4096chains.md")
@@ -205,7 +213,7 @@ def build_batch(E, probs, cpb, rank=0, moves=MOVES):
                               seed0=(rank * len(probs) + i) * cpb, taudiff_max=TDM, ncorr=NCORR,
                               kcap=32 if pr["beta"] <= 25 else 64,
                               opcap=256 if pr["beta"] <= 25 else (512 if pr["beta"] <= 50 else 1024),
-                              **moves))
+                              tree_levels=BATCH_TREE_LEVELS.get(pr["beta"], 0), **moves))
     h2d = sum(g.ftau.nbytes for g in groups) + pr0["umatrix"].nbytes + pr0["muimp"].nbytes
     return model, groups, E.Batch(model, groups), h2d
 
@@ -244,7 +252,8 @@ def one_chain_forms(E, model, probs):
     out = []
     for pr in probs:
         b = E.Batch(model, [E.Group(pr["beta"], pr["ftau"], NTAU, nchains=1, seed0=0, taudiff_max=TDM,
-                                    ncorr=NCORR, kcap=64, opcap=1024, **MOVES)])
+                                    ncorr=NCORR, kcap=64, opcap=1024,
+                                    tree_levels=ONE_CHAIN_TREE_LEVELS.get(pr["beta"], 0), **MOVES)])
         b.warmup(THERMALIZE + 10 * TUNE)
         b.sync()
         stream = torch.cuda.ExternalStream(b.stream())

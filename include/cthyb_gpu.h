@@ -84,7 +84,7 @@ typedef struct {
   double p_outer;        /* PercentageOuterMove */
   int32_t kcap;          /* max pairs per flavour (0: automatic) */
   int32_t opcap;         /* max operators in a configuration (0: automatic) */
-  int32_t tree_levels;   /* time-bin tree depth, 2^levels leaves (0: automatic) */
+  int32_t tree_levels;   /* time-bin tree depth, 2^levels leaves (0: automatic, -1: one leaf) */
   int32_t maxhisto;      /* expansion-order histogram bins (MaxHisto) */
   int32_t flags;         /* CTHYB_FLAG_* */
   double p_global;       /* PercentageGlobalMove: spin flip, CA flip, random

@@ -27,7 +27,7 @@ def lib():
 
 
 def run_pair(name, beta, tdm, p_outer, nprop, seed, dense=False, qns=None, ntau=50, p_global=0.0,
-             p_shift=0.0, symmoves=None, p_4op=0.0):
+             p_shift=0.0, symmoves=None, p_4op=0.0, tree_levels=0):
     pr = P.config_problem(name, beta=beta)
     q = qns or pr["quantum_numbers"]
     mo = O.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
@@ -39,7 +39,7 @@ def run_pair(name, beta, tdm, p_outer, nprop, seed, dense=False, qns=None, ntau=
     mg = E.Model(pr["nd"], pr["umatrix"], pr["muimp"], q)
     grp = E.Group(beta, pr["ftau"], ntau, nchains=1, seed0=seed, taudiff_max=tdm,
                   p_outer=p_outer, dense=dense, kcap=64, opcap=512, p_global=p_global,
-                  p_shift=p_shift, symmoves=symmoves, p_4op=p_4op)
+                  p_shift=p_shift, symmoves=symmoves, p_4op=p_4op, tree_levels=tree_levels)
     b = E.Batch(mg, [grp])
     b.set_log(nprop)
     b.warmup(nprop)
@@ -105,6 +105,29 @@ GLOBAL_CASES = [
     ("dd3", 10.0, 4.0, 0.1, 2000, 15, True, None),
     ("dd3", 8.0, 8.0, 0.0, 3000, 16, False, "Nt"),
 ]
+
+
+@pytest.mark.parametrize("name,beta,levels,dense,nprop,moves", [
+    ("dd3", 10.0, -1, False, 6000, dict(p_global=0.05, p_shift=0.05)),
+    ("dd3", 25.0, -1, False, 6000, dict(p_4op=0.1)),
+    ("dd3", 10.0, -1, True, 2000, dict(p_global=0.05, p_shift=0.05)),
+    ("dd3", 50.0, 4, False, 8000, dict(p_global=0.02, p_shift=0.02)),
+    ("kanamori5", 2.0, -1, False, 300, {}),
+])
+def test_tree_depth_keeps_the_proposal_stream(lib, name, beta, levels, dense, nprop, moves):
+    """The time-bin tree's depth is a schedule choice: a single leaf (every
+    proposal walks all operators, no combine steps) and a deep tree leave
+    the proposal stream equal to the oracle's, global, tau-shift and
+    4-operator moves included (one-chain batches also run with their chain
+    state in shared memory)."""
+    ref, got, co, b = run_pair(name, beta, 4.0 if beta <= 25 else 5.0, 0.1, nprop, 31, dense=dense,
+                               tree_levels=levels, **moves)
+    F = P.config_problem(name, beta=beta)["ftau"][0, 0]
+    compare_logs(ref, got, F, beta)
+    assert (ref["outcome"] == 4).sum() > 20
+    so, sg = co.state(), b.state(0)
+    assert so["noper"] == sg["noper"] and so["outer_sst"] == sg["outer_sst"]
+    assert abs(so["trace_log"] - sg["trace_log"]) <= 1e-9 * max(1.0, abs(so["trace_log"]))
 
 
 @pytest.mark.parametrize("name,beta,tdm,pout,nprop,seed,dense,qns", GLOBAL_CASES)

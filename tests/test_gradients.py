@@ -227,7 +227,7 @@ def test_dense_reference_against_oracle_weights():
 
 @pytest.mark.gpu
 def test_gradients_100_configurations_beta50():
-    """Config 5 checks: 100 thermalised configurations of the 3-orbital
+    """Gradient checks: 100 thermalised configurations of the 3-orbital
     model at beta = 50; the kernel's gradients against central finite
     differences (step 1e-6) of the oracle's full LU determinant and full
     trace (the two grid points of largest d log|det| and all 8 parameter
@@ -287,7 +287,7 @@ def test_gradients_100_configurations_beta50():
             worst["det_dense"] = max(worst["det_dense"], e1)
             worst["trace_dense"] = max(worst["trace_dense"], e2)
             assert e1 < 1e-9 and e2 < 1e-9, (ch, e1, e2)
-    print(f"\nconfig-5 gradient checks, worst relative errors: {worst}")
+    print(f"\ngradient checks (100 configurations, beta = 50), worst relative errors: {worst}")
 
 
 @pytest.mark.gpu

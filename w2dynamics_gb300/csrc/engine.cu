@@ -460,6 +460,7 @@ struct Mod {
   int ix, iy;       // removed indices (ix < iy)
   int b1, b2;       // affected leaves
   int n1, n2;       // gathered operator counts of leaves b1, b2 (buffers 0, 1)
+  int p1, p2;       // insertion: lower bounds of t1, t2 in the operator array
 };
 
 // Bin edges beta * j / 2^L (tabulated per group) and the bin of a time by
@@ -559,6 +560,71 @@ __device__ NOINL int gather_bin(Ctx& c, const Mod& md, int b, int buf) {
   }
   __syncwarp();
   return n;
+}
+
+// The operators of the proposal's one or two leaves (bins md.b1, md.b2) of
+// the proposed configuration gathered together into buffers 0 and 1, with
+// their time steps: the same buffers as gather_bin for each bin, with one
+// pass over both bins instead of one after the other.  Leaf 0 holds t1 (and
+// t2 when both are in one bin), leaf 1 holds t2; the inserted operators go
+// to their lower bounds md.p1, md.p2 in the operator array.
+__device__ NOINL void gather_leaves(Ctx& c, Mod& md, int nleaf) {
+  const int nb = 1 << c.g->L;
+  const int lo0 = c.bstart[md.b1], hi0 = c.bstart[md.b1 + 1];
+  const int lo1 = c.bstart[md.b2], hi1 = c.bstart[md.b2 + 1];
+  const int len0 = hi0 - lo0, len1 = nleaf > 1 ? hi1 - lo1 : 0;
+  const bool ins = md.type == 1, rem = md.type == 2;
+  for (int t = c.lane; t < len0 + len1; t += 32) {
+    const int q = t >= len0 ? 1 : 0;
+    const int lo = q ? lo1 : lo0;
+    const int j = lo + t - q * len0;
+    const double tau = c.optau[j];
+    const int code = c.opcode[j];
+    int r = j - lo;
+    if (ins) {
+      r += (q == 0 && md.t1 < tau) + ((q == 1 || nleaf == 1) && md.t2 < tau);
+    } else if (rem) {
+      if (j == md.ix || j == md.iy) continue;
+      r -= (md.ix >= lo && md.ix < j) + (md.iy >= lo && md.iy < j);
+    }
+    c.btau[q][r] = tau;
+    c.bcode[q][r] = code;
+  }
+  int n0 = len0, n1 = len1;
+  if (rem) {
+    n0 -= (md.ix >= lo0 && md.ix < hi0) + (md.iy >= lo0 && md.iy < hi0);
+    if (nleaf > 1) n1 -= (md.ix >= lo1 && md.ix < hi1) + (md.iy >= lo1 && md.iy < hi1);
+  }
+  if (ins) {
+    if (c.lane == 0) {
+      c.btau[0][md.p1 - lo0] = md.t1;
+      c.bcode[0][md.p1 - lo0] = md.c1;
+      const int q2 = nleaf > 1 ? 1 : 0;
+      const int p2 = md.p2 - (q2 ? lo1 : lo0) + (q2 ? 0 : 1);
+      c.btau[q2][p2] = md.t2;
+      c.bcode[q2][p2] = md.c2;
+    }
+    if (nleaf > 1) {
+      n0 += 1;
+      n1 += 1;
+    } else {
+      n0 += 2;
+    }
+  }
+  md.n1 = n0;
+  md.n2 = nleaf > 1 ? n1 : n0;
+  __syncwarp();
+  // time steps: before operator j from the previous one (bin start for
+  // j = 0), and from the last operator to the bin end (index n)
+  const int m0 = n0 + 1, tot = m0 + (nleaf > 1 ? n1 + 1 : 0);
+  for (int t = c.lane; t < tot; t += 32) {
+    const int q = t >= m0 ? 1 : 0, j = t - q * m0, n = q ? n1 : n0, b = q ? md.b2 : md.b1;
+    const double* bt = c.btau[q];
+    const double prev = j > 0 ? bt[j - 1] : bin_edge(c, b);
+    const double cur = j < n ? bt[j] : (b + 1 < nb ? bin_edge(c, b + 1) : c.g->beta);
+    c.bdt[q][j] = cur - prev;
+  }
+  __syncwarp();
 }
 
 // Leaf of bin b from the gathered operators (n of them), written to `slot`:
@@ -690,14 +756,7 @@ __device__ __forceinline__ void combine_body(Ctx& c, int n, int sl, int sr, int 
 __device__ NOINL void tree_propose(Ctx& c, Mod& md, bool do_ss, bool do_states, bool gather) {
   const int L = c.g->L, nb = 1 << L;
   const int nleaf = md.b2 != md.b1 ? 2 : 1;
-  if (gather) {
-    for (int q = 0; q < nleaf; ++q) {
-      int n = gather_bin(c, md, q ? md.b2 : md.b1, q);
-      if (q) md.n2 = n;
-      else md.n1 = n;
-    }
-    if (nleaf == 1) md.n2 = md.n1;
-  }
+  if (gather) gather_leaves(c, md, nleaf);
   for (int q = 0; q < nleaf; ++q) {
     int b = q ? md.b2 : md.b1;
     leaf_body(c, b, q ? md.n2 : md.n1, 1 - c.act[nb + b], do_ss, do_states, q);
@@ -1609,6 +1668,8 @@ __device__ NOINL void ph_setup_add(Ctx& c, Prop& p) {
   md.b2 = a_first ? bc : ba;
   p.p1 = a_first ? pa : pc;
   p.p2 = a_first ? pc : pa;
+  md.p1 = p.p1;
+  md.p2 = p.p2;
   p.f = f;
   p.k = k;
   p.K = K;
@@ -3601,6 +3662,8 @@ __device__ NOINL void ph_add_od(Ctx& c, Prop& p) {
   md.b1 = bin_of(c, md.t1);
   md.b2 = bin_of(c, md.t2);
   const int p1 = op_lower_bound(c, md.b1, md.t1), p2 = op_lower_bound(c, md.b2, md.t2);
+  md.p1 = p1;
+  md.p2 = p2;
   if (teq(tau_a, tau_c) || (p1 < K && teq(c.optau[p1], md.t1)) || (p2 < K && teq(c.optau[p2], md.t2))) {
     if (c.lane == 0) h.qn_add++;
     r.outcome = 0;
@@ -4532,7 +4595,7 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
   load_hdr(c.h, gh, c.lane);
   // the tree's active bits live in shared memory during the sweep
   unsigned char* gact = c.act;
-  const int nact4 = (2 << g.L) / 4;
+  const int nact4 = ((2 << g.L) + 3) / 4;  // whole words (a one-leaf tree has 2 bytes)
   c.act = dyn_act + (size_t)warp * actbytes;
   for (int i = c.lane; i < nact4; i += 32) ((uint32_t*)c.act)[i] = ((const uint32_t*)gact)[i];
   __syncwarp();
@@ -4577,9 +4640,62 @@ __global__ void __launch_bounds__(WPB * 32, SWEEP_MIN_BLOCKS)
 #define SYNC_MAX_THREADS 1024  // register budget: 64 per thread, 32 chain warps per SM
 #define SYNC_MIN_BLOCKS 1
 #endif
+// Shared-memory residence of one chain (blocks of one chain warp): three
+// contiguous ranges of the chain's slab -- operator arrays and sorted lists
+// [o_optau, o_M), the time-bin tree [o_tree, o_act), bin starts and scratch
+// [o_bstart, o_gtau) -- are copied into the block's shared memory and the
+// context's pointers redirected there; on leaving, the ranges go back.  The
+// inverse matrices, accumulators, checkpoints and rare-move space stay in
+// global memory.  Every access to these ranges in the sweep goes through
+// the context's pointers.
+__host__ __device__ inline size_t resident_bytes(const DGroup& g) {
+  return (g.o_M - g.o_optau) + (g.o_act - g.o_tree) + (g.o_gtau - g.o_bstart);
+}
+__device__ __forceinline__ void copy16(void* dst, const void* src, size_t bytes, int lane) {
+  uint4* d = (uint4*)dst;
+  const uint4* sp = (const uint4*)src;
+  for (size_t i = lane; i < bytes / 16; i += 32) d[i] = sp[i];
+}
+__device__ NOINL void resident_enter(Ctx& c, unsigned char* sm) {
+  const DGroup& g = *c.g;
+  const char* b = g.base + (size_t)c.chain * g.stride;
+  const size_t la = g.o_M - g.o_optau, lt = g.o_act - g.o_tree, ls = g.o_gtau - g.o_bstart;
+  char* sa = (char*)sm;
+  char* st = sa + la;
+  char* ss = st + lt;
+  copy16(sa, b + g.o_optau, la, c.lane);
+  copy16(st, b + g.o_tree, lt, c.lane);
+  copy16(ss, b + g.o_bstart, ls, c.lane);
+  __syncwarp();
+  c.optau = (double*)(sa);
+  c.opcode = (int*)(sa + (g.o_opcode - g.o_optau));
+  c.srt_tau = (double*)(sa + (g.o_srt_tau - g.o_optau));
+  c.srt_slot = (short*)(sa + (g.o_srt_slot - g.o_optau));
+  c.slot_tau = (double*)(sa + (g.o_slot_tau - g.o_optau));
+  c.tree = st;
+  c.bstart = (int*)ss;
+  c.scr = (double*)(ss + (g.o_scr - g.o_bstart));
+  c.btau[0] = c.scr + 4 * g.kcap;
+  c.btau[1] = c.btau[0] + g.opcap + 2;
+  c.bdt[0] = c.btau[1] + g.opcap + 2;
+  c.bdt[1] = c.bdt[0] + g.opcap + 3;
+  c.bcode[0] = (int*)(c.bdt[1] + g.opcap + 3);
+  c.bcode[1] = c.bcode[0] + g.opcap + 2;
+}
+__device__ NOINL void resident_leave(Ctx& c, const unsigned char* sm) {
+  const DGroup& g = *c.g;
+  char* b = g.base + (size_t)c.chain * g.stride;
+  const size_t la = g.o_M - g.o_optau, lt = g.o_act - g.o_tree;
+  const char* sa = (const char*)sm;
+  copy16(b + g.o_optau, sa, la, c.lane);
+  copy16(b + g.o_tree, sa + la, lt, c.lane);
+  copy16(b + g.o_bstart, sa + la + lt, g.o_gtau - g.o_bstart, c.lane);
+  __syncwarp();
+}
+
 __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
     k_sweep_sync(const __grid_constant__ DModel m, const DGroup* __restrict__ groups, int ngroups, int ntotal,
-                 long long nprop, int nmeas, int reset, int actbytes) {
+                 long long nprop, int nmeas, int reset, int actbytes, int resident_off) {
   extern __shared__ __align__(16) unsigned char dyn[];
   const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   Hdr* hs = (Hdr*)dyn;
@@ -4604,10 +4720,11 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
     gh = (Hdr*)(gp->base + (size_t)chain * gp->stride + gp->o_hdr);
     load_hdr(c.h, gh, lane);
     gact = c.act;
-    nact4 = (2 << gp->L) / 4;
+    nact4 = ((2 << gp->L) + 3) / 4;
     c.act = acts + (size_t)warp * actbytes;
     for (int i = lane; i < nact4; i += 32) ((uint32_t*)c.act)[i] = ((const uint32_t*)gact)[i];
     __syncwarp();
+    if (resident_off) resident_enter(c, dyn + resident_off);
     mt_refill(c, c.h->mt_idx);
     if (reset && lane == 0) {  // init_counters, CTQMC.F90:847-899
       Hdr& h = *c.h;
@@ -4704,6 +4821,7 @@ __global__ void __launch_bounds__(SYNC_MAX_THREADS, SYNC_MIN_BLOCKS)
       if (c.h->status != ST_OK) atomicMax(gp->err_flag, c.h->status);
     }
     __syncwarp();
+    if (resident_off) resident_leave(c, dyn + resident_off);
     for (int i2 = lane; i2 < nact4; i2 += 32) ((uint32_t*)gact)[i2] = ((const uint32_t*)c.act)[i2];
     store_hdr(gh, c.h, lane);
   }
@@ -4748,7 +4866,7 @@ __global__ void __launch_bounds__(TEAM_MAX_THREADS, TEAM_MIN_BLOCKS)
     Ctx c = make_ctx(&m, gp, hs, chain, rec);
     Hdr* gh = (Hdr*)(gp->base + (size_t)chain * gp->stride + gp->o_hdr);
     unsigned char* gact = c.act;
-    const int nact4 = (2 << gp->L) / 4;
+    const int nact4 = ((2 << gp->L) + 3) / 4;
     c.act = act;
     if (warp == 0) {
       load_hdr(c.h, gh, lane);
@@ -5421,8 +5539,8 @@ struct cthyb_batch_s {
   int use_graphs = 0;
   int sync_warps = -1;  // -1: automatic; 0: independent warps (k_sweep); n: phase-synchronous blocks of n warps
   size_t sync_smem = 48 * 1024;  // dynamic shared memory the sync kernel is opted in for
-  int sync_carve = -1;           // shared-memory carveout (percent) last set for the sync kernel
   int smem_sm = 0, smem_rsv = 0; // shared memory per multiprocessor and reserved per block (bytes)
+  int smem_optin = 0;           // opt-in shared memory per block (bytes)
   // captured launch sequences of warmup(n) / measure(n), replayed while n and
   // the schedule stay the same
   struct Graph {
@@ -5639,7 +5757,9 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   // with opcap 512 depth 1 beats depth 2; the leaf rebuild grows with the
   // operators of a bin, the combine steps with the depth).
   int L = d.tree_levels;
-  if (L <= 0) {
+  if (L < 0) {
+    L = 0;  // one leaf: every proposal rewalks all operators, no combine steps
+  } else if (L == 0) {
     L = 1;
     if (opcap > 512)
       while ((128ll << L) < opcap && L < 10) ++L;
@@ -5773,6 +5893,7 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&B->nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&B->smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&B->smem_rsv, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&B->smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   }
   if (e != cudaSuccess) {
     cthyb_batch_destroy(B);
@@ -5936,22 +6057,40 @@ static int schedule_of(cthyb_batch_t B) {
   return nw;
 }
 
+// One chain per block and at most one block per multiprocessor: the
+// chain's operator arrays, sorted lists, tree, bin starts and scratch live
+// in the block's shared memory for the launch (resident_enter).  Returns
+// the bytes of that area (0: not resident) and aligns `smem`, the per-warp
+// area in front of it.
+static size_t sync_resident(cthyb_batch_t B, int nw, size_t& smem) {
+  size_t resident = 0;
+  if (nw == 1 && B->nchains <= B->nsm) {
+    for (GroupHost& G : B->groups) resident = std::max(resident, resident_bytes(G.g));
+    smem = align_up(smem, 16);
+    if (smem + resident > (size_t)B->smem_optin) resident = 0;
+  }
+  return resident;
+}
+
 // Shared memory of the sync kernel: opt in for `smem` bytes a block and
-// ask for the smallest carveout that holds two such blocks, leaving the
+// ask for the smallest carveout that holds `blocks` such blocks (two; one
+// for a resident chain, whose warp's stack then keeps L1), leaving the
 // rest of the multiprocessor's 256 KB to the L1 cache (the chains' hot
 // arrays live there; a carveout of 10 % against the default measured +1 %,
 // 50 % -3 %, 100 % -17 % on the 4096-chain batch).
-static int sync_attributes(cthyb_batch_t B, size_t smem) {
+static int sync_attributes(cthyb_batch_t B, size_t smem, int blocks) {
   if (smem > B->sync_smem) {
     CK(cudaFuncSetAttribute(k_sweep_sync, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     B->sync_smem = smem;
   }
   if (B->smem_sm > 0) {
-    const size_t need = 2 * (smem + (size_t)B->smem_rsv);
+    const size_t need = (size_t)blocks * (smem + (size_t)B->smem_rsv);
     const int pct = (int)std::min<size_t>(100, (100 * need + B->smem_sm - 1) / B->smem_sm + 1);
-    if (pct != B->sync_carve) {
+    // a function attribute: the last value set by any batch of the process
+    static int carve = -1;
+    if (pct != carve) {
       CK(cudaFuncSetAttribute(k_sweep_sync, cudaFuncAttributePreferredSharedMemoryCarveout, pct));
-      B->sync_carve = pct;
+      carve = pct;
     }
   }
   return CTHYB_OK;
@@ -5999,11 +6138,13 @@ static int launch_sweeps(cthyb_batch_t B, long long nprop, int nmeas, int reset)
   const int nw = schedule_of(B);
   if (nw > 0) {
     const int nblk = (B->nchains + nw - 1) / nw;
-    const size_t smem = (size_t)nw * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + actbytes);
-    int rc = sync_attributes(B, smem);
+    size_t smem = (size_t)nw * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + actbytes);
+    const size_t resident = sync_resident(B, nw, smem);
+    int rc = sync_attributes(B, smem + resident, resident ? 1 : 2);
     if (rc) return rc;
-    k_sweep_sync<<<nblk, nw * 32, smem, B->stream>>>(B->model->dm, B->d_groups, (int)B->groups.size(), B->nchains,
-                                                     nprop, nmeas, reset, actbytes);
+    k_sweep_sync<<<nblk, nw * 32, smem + resident, B->stream>>>(B->model->dm, B->d_groups, (int)B->groups.size(),
+                                                                B->nchains, nprop, nmeas, reset, actbytes,
+                                                                resident ? (int)smem : 0);
   } else {
     const int nblk = (B->nchains + WPB - 1) / WPB;
     k_sweep<<<nblk, WPB * 32, (size_t)WPB * actbytes, B->stream>>>(B->model->dm, B->d_groups,
@@ -6063,8 +6204,9 @@ static int graph_sweeps(cthyb_batch_t B, cthyb_batch_s::Graph& G, long long n, b
         if (rc) return rc;
       }
     } else if (sched > 0) {
-      const size_t smem = (size_t)sched * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + (2 << Lmax));
-      int rc = sync_attributes(B, smem);
+      size_t smem = (size_t)sched * (sizeof(Hdr) + sizeof(cthyb_record) + sizeof(Prop) + (2 << Lmax));
+      const size_t resident = sync_resident(B, sched, smem);
+      int rc = sync_attributes(B, smem + resident, resident ? 1 : 2);
       if (rc) return rc;
     }
     CK(cudaStreamBeginCapture(B->stream, cudaStreamCaptureModeThreadLocal));
