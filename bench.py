@@ -573,16 +573,21 @@ def run_gpu(args, rank=0, world=1):
                     "the batched error at each beta, the batch reaches all four betas in batched_seconds"},
         "one_chain_form": {"value": one_rate, "unit": "MC updates/s",
                            "batched_over_one_chain": value / one_rate},
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm,
-                     "traffic": (prof or {}).get("dram_bytes_per_step"), "peak_kind": hbm_kind,
-                     "note": "per step (one measurement cycle, NCorr proposals a chain): algorithmic bytes of "
-                             "M and operator arrays over the device time; traffic = ncu DRAM bytes of one "
-                             "cycle from the committed profile (see ncu.same_build)",
-                     "fp64": {"achieved": fp64_achieved, "peak": fp64_dfma, "unit": "GFLOP/s",
-                              "frac": fp64_achieved / fp64_dfma,
-                              "peak_kind": "live DFMA probe (cthyb_probe_fp64)", "dmma_peak": fp64_dmma,
-                              "note": "algorithmic determinant flops (ratios and updates) only"},
+        "roofline": {"bound": "fp64", "achieved": fp64_achieved, "peak": fp64_dfma, "unit": "GFLOP/s",
+                     "frac": fp64_achieved / fp64_dfma,
+                     "peak_kind": "live DFMA probe (cthyb_probe_fp64) on this GPU",
+                     "note": "algorithmic FP64 flops of the determinant ratios and fast updates (counted at run "
+                             "time) over the device time of the K steps; the kernel is latency-bound (see "
+                             "binding), so both this and the HBM fraction are small by the nature of the workload",
+                     "dmma_peak": fp64_dmma,
+                     "fp64_pipe_active": (prof or {}).get("fp64_pipe_active"),
+                     "binding": (prof or {}).get("binding"),
+                     "hbm": {"achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                             "traffic": (prof or {}).get("dram_bytes_per_step"), "peak_kind": hbm_kind,
+                             "note": "per step (one measurement cycle, NCorr proposals a chain): algorithmic "
+                                     "bytes of M and operator arrays over the device time; traffic = ncu DRAM "
+                                     "bytes per step of the timed launch from the committed profile "
+                                     "(see ncu.same_build)"},
                      "ncu": prof},
         "cpu_baseline": cpu,
         "backward": backward,
