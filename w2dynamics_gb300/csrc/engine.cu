@@ -399,6 +399,32 @@ __device__ __forceinline__ int cnt_earlier(const double* opp, int n, double t, d
   int a = slb(opp, n, lo), b = slb(opp, n, t);
   return b > a ? b - a : 0;
 }
+// Partners of two operators (times t1, t2) among the opposite-CA lists
+// opp1, opp2 (n1, n2 entries): cnt_later + cnt_earlier of each, the eight
+// binary searches run by lanes 0..7 at once instead of one after the
+// other.  Warp-uniform result.
+__device__ __forceinline__ int partner_counts(const Ctx& c, const double* opp1, int n1, double t1,
+                                              const double* opp2, int n2, double t2, double wmin, double wmax,
+                                              double tdm) {
+  const int l = c.lane;
+  int r = 0;
+  if (l < 8) {
+    const bool second = l >= 4;
+    const double* opp = second ? opp2 : opp1;
+    const int n = second ? n2 : n1;
+    const double t = second ? t2 : t1;
+    const int q = l & 3;
+    if (q == 0) r = sub(opp, n, t);                               // later: lower end
+    else if (q == 1) r = sub(opp, n, fmin(wmax, __dadd_rn(t, tdm)));  // later: upper end
+    else if (q == 2) r = slb(opp, n, fmax(wmin, __dsub_rn(t, tdm)));  // earlier: lower end
+    else r = slb(opp, n, t);                                      // earlier: upper end
+  }
+  const int up = __shfl_down_sync(FULL, r, 1);
+  int d = (l < 8 && (l & 1) == 0 && up > r) ? up - r : 0;
+  d += __shfl_down_sync(FULL, d, 2);
+  d += __shfl_down_sync(FULL, d, 4);
+  return __shfl_sync(FULL, d, 0);
+}
 __device__ NOINL int count_npairs(Ctx& c) {
   Hdr& h = *c.h;
   int K = h.K;
@@ -1936,15 +1962,10 @@ __device__ NOINL void ph_decide(Ctx& c, Prop& p) {
       }
       np = tot + __shfl_sync(FULL, n, 0);
     } else {
-      int n = 0;
-      if (c.lane == 0) {
-        const double* opp1 = srt_ptr(c, f, 1 - (md.c1 & 1));
-        const double* opp2 = srt_ptr(c, f, 1 - (md.c2 & 1));
-        n += cnt_later(opp1, k, md.t1, wmax, tdm) + cnt_earlier(opp1, k, md.t1, wmin, tdm);
-        if (md.t2 <= wmax && md.t2 <= __dadd_rn(md.t1, tdm)) n += 1;
-        n += cnt_later(opp2, k, md.t2, wmax, tdm) + cnt_earlier(opp2, k, md.t2, wmin, tdm);
-      }
-      np = h.npairs + __shfl_sync(FULL, n, 0);
+      int n = partner_counts(c, srt_ptr(c, f, 1 - (md.c1 & 1)), k, md.t1, srt_ptr(c, f, 1 - (md.c2 & 1)), k, md.t2,
+                             wmin, wmax, tdm);
+      if (md.t2 <= wmax && md.t2 <= __dadd_rn(md.t1, tdm)) n += 1;
+      np = h.npairs + n;
     }
     double wr = weight_ratio(tr_mx, tr_sum, h.trace_log, fabs(p.ratio));
     prob = fabs(p.tdf * (double)(2 * m.nd) / (double)np * wr);
@@ -2102,6 +2123,9 @@ __device__ NOINL void ph_accept_rem(Ctx& c, Prop& p) {
   tree_accept(c, md);
   chk_keep(c, md, p.snew);
   const double wmin = h.tauwin_min, wmax = h.tauwin_max, tdm = h.taudiff_max;
+  // update_NPairs(-1): the pair and the partners of its members
+  const int gone = 1 + partner_counts(c, srt_ptr(c, f, 1 - p.cax), k - 1, p.tx, srt_ptr(c, f, p.cax), k - 1, p.ty,
+                                      wmin, wmax, tdm);
   if (c.lane == 0) {
     h.k[f] = k - 1;
     h.K = K - 2;
@@ -2114,11 +2138,7 @@ __device__ NOINL void ph_accept_rem(Ctx& c, Prop& p) {
     h.acc_since_refresh++;
     count_accpair(c, f, __dsub_rn(p.ty, p.tx));
     h.w_opbytes += 24ll * (K - p.ix) + 40ll * k;
-    // update_NPairs(-1): the pair and the partners of its members
-    const double* oppx = srt_ptr(c, f, 1 - p.cax);
-    const double* oppy = srt_ptr(c, f, p.cax);
-    h.npairs -= 1 + cnt_later(oppx, k - 1, p.tx, wmax, tdm) + cnt_earlier(oppx, k - 1, p.tx, wmin, tdm) +
-                cnt_later(oppy, k - 1, p.ty, wmax, tdm) + cnt_earlier(oppy, k - 1, p.ty, wmin, tdm);
+    h.npairs -= gone;
   }
   __syncwarp();
   double sgn = config_sign(c);
@@ -5853,6 +5873,28 @@ static int layout_group(cthyb_batch_s* B, GroupHost& G, long long logcap) {
   return CTHYB_OK;
 }
 
+// Chain slabs come from the device's stream-ordered memory pool, which is
+// told to keep freed memory for the process (release threshold at its
+// maximum): a driver that creates a batch per solve (one per DMFT
+// iteration) reuses the previous slab instead of mapping gigabytes anew.
+static cudaError_t slab_alloc(char** p, size_t n, cudaStream_t s) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  cudaMemPool_t pool;
+  if (e == cudaSuccess) e = cudaDeviceGetDefaultMemPool(&pool, dev);
+  if (e == cudaSuccess) {
+    uint64_t keep = ~0ull;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  }
+  if (e == cudaSuccess) e = cudaMallocAsync((void**)p, n, s);
+  return e;
+}
+static void slab_free(char* p, cudaStream_t s) {
+  if (!p) return;
+  cudaFreeAsync(p, s);
+  cudaStreamSynchronize(s);
+}
+
 int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc* groups, cthyb_batch_t* out) {
   if (!model || ngroups < 1 || !groups || !out) return fail(CTHYB_ERR_ARG, "bad arguments");
   {
@@ -5882,7 +5924,7 @@ int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc*
     total += (size_t)G.desc.nchains * G.g.stride;
   }
   cudaError_t e = cudaStreamCreateWithFlags(&B->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaMalloc(&B->slab, total);
+  if (e == cudaSuccess) e = slab_alloc(&B->slab, total, B->stream);
   if (e == cudaSuccess) e = cudaMemsetAsync(B->slab, 0, total, B->stream);
   if (e == cudaSuccess) e = cudaMalloc(&B->d_err, sizeof(int));
   if (e == cudaSuccess) e = cudaMemsetAsync(B->d_err, 0, sizeof(int), B->stream);
@@ -6010,7 +6052,7 @@ int cthyb_batch_destroy(cthyb_batch_t B) {
     cudaFree(G.d_seeds);
     cudaFree(G.d_tdm);
   }
-  cudaFree(B->slab);
+  if (B->stream) slab_free(B->slab, B->stream);
   cudaFree(B->d_err);
   cudaFree(B->d_dev);
   if (B->d_red) cudaFree(B->d_red);
@@ -7041,8 +7083,9 @@ int cthyb_batch_set_log(cthyb_batch_t B, int64_t cap) {
     total += (size_t)G.desc.nchains * G.g.stride;
   }
   char* slab = nullptr;
-  CK(cudaMalloc(&slab, total));
-  CK(cudaMemset(slab, 0, total));
+  CK(slab_alloc(&slab, total, B->stream));
+  CK(cudaMemsetAsync(slab, 0, total, B->stream));
+  CK(cudaStreamSynchronize(B->stream));
   size_t off = 0;
   for (size_t gi = 0; gi < B->groups.size(); ++gi) {
     GroupHost& G = B->groups[gi];
@@ -7063,7 +7106,7 @@ int cthyb_batch_set_log(cthyb_batch_t B, int64_t cap) {
       CK(cudaMemcpy(nb + (size_t)c * G.g.stride + G.g.o_hdr, &h, sizeof(Hdr), cudaMemcpyHostToDevice));
     }
   }
-  cudaFree(B->slab);
+  slab_free(B->slab, B->stream);
   B->slab = slab;
   B->logcap = cap;
   return upload_groups(B);
