@@ -126,7 +126,10 @@ typedef struct {
  * one uniform number in proportion to the empty trace, NSlide
  * (CTQMC.F90:8069).  Chains are numbered consecutively over groups.
  * Replaces init_solver's init_Trace / init_CTQMC for one process
- * (one chain) or for a batch of independent chains. */
+ * (one chain) or for a batch of independent chains.  The chains' device
+ * memory comes from the device's default stream-ordered memory pool, whose
+ * release threshold is raised to its maximum so that the next batch of the
+ * process reuses it (a process-wide setting of that pool). */
 int cthyb_batch_create(cthyb_model_t model, int ngroups, const cthyb_group_desc* groups,
                        cthyb_batch_t* out);
 int cthyb_batch_destroy(cthyb_batch_t batch);
