@@ -180,9 +180,10 @@ def _coarse(g, nbin):
 
 
 def test_anderson_impurity_statistics_two_sigma(lib):
-    """GPU: 32 chains x 1000 measurements of NCorr = 100 proposals; oracle:
-    32 chains x 1000 measurements with other seeds (equal total samples;
-    as many independent chains on both sides, so the z-scores are close to
+    """GPU: 100 chains x 1000 measurements of NCorr = 100 proposals (1e5
+    measurement cycles, 1e7 proposals after thermalisation); oracle: 100
+    chains x 1000 measurements with other seeds (equal total samples; as
+    many independent chains on both sides, so the z-scores are close to
     normal).
     Occupancies and double occupancy, G(tau) on 1000 bins (90 % within 2
     sigma, all within 5) and G averaged over 50-bin windows, by the 2-sigma
@@ -191,12 +192,13 @@ def test_anderson_impurity_statistics_two_sigma(lib):
     nd, beta, ntau = 1, 10.0, 1000
     mg = E.Model(nd, pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
     fk, evec = mg.basis()
-    b = E.Batch(mg, [E.Group(beta, pr["ftau"], ntau, nchains=32, seed0=100, taudiff_max=beta, ncorr=100)])
+    nch = 100
+    b = E.Batch(mg, [E.Group(beta, pr["ftau"], ntau, nchains=nch, seed0=100, taudiff_max=beta, ncorr=100)])
     b.warmup(10000)
     b.measure(1000)
     b.sync()
     gg, gn, gd = [], [], []
-    for c in range(32):
+    for c in range(nch):
         r = b.results(c)
         gg.append(np.stack([r["gtau"][f // 2, f % 2] for f in range(2 * nd)]))
         n, d = _occupations(nd, r["densitymatrix"], fk, evec)
@@ -205,7 +207,7 @@ def test_anderson_impurity_statistics_two_sigma(lib):
     mo = O.Model(nd, pr["umatrix"], pr["muimp"], pr["quantum_numbers"])
     ev = _oracle_evec(mo)
     cg, cn, cd = [], [], []
-    for c in range(32):
+    for c in range(nch):
         co = O.Chain(mo, beta, pr["ftau"], ntau, seed=9000 + c, taudiff_max=beta, ncorr=100)
         co.warmup(10000)
         co.measure(1000)
