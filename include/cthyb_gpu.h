@@ -45,7 +45,10 @@ const char* cthyb_last_error(void);
  * Replaces init_States / qns2substates / init_Psi / oneparticle_hamiltonian /
  * u_hamiltonian / diag_Operator / transform_Psis called from init_solver
  * (CTQMC.F90:7894-8000; States.F90:58-186; Operator.F90:115-300,482-546,
- * 637-735,1042-1172). */
+ * 637-735,1042-1172).  A string containing "All" partitions the superstates
+ * of the other quantum numbers automatically (analyze_hamiltonian,
+ * Operator.F90:303-442); an "EPSBLOCK=x" token in the string sets its
+ * threshold relative to the largest entry of muimp and U (default 1e-13). */
 int cthyb_model_create(int nd, const double* umatrix, const double* muimp,
                        const char* quantum_numbers, cthyb_model_t* out);
 int cthyb_model_destroy(cthyb_model_t model);

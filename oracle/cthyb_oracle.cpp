@@ -35,6 +35,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -227,38 +228,140 @@ static std::string g_err;
 // init_States + qns2substates + init_substates + init_Psi + Hamiltonian +
 // diagonalisation + transform_Psis (the init_solver sequence,
 // CTQMC.F90:7894-8000).
+static Model* build_model_partition(int nd, const double* umat, const double* muimp, bool useSzt,
+                                    const std::vector<int>& sst_of_state, int nss);
+
+// analyze_hamiltonian, Operator.F90:303-442 (QuantumNumbers containing
+// "All"; threshold EPSBLOCK relative to the largest entry of muimp and U,
+// CTQMC.F90:7971-7990).  m0 is the model of the partition by the other
+// quantum numbers (its ham blocks: the symmetrised Hamiltonian in the
+// occupation basis).  First every superstate splits into the nets of its
+// Hamiltonian: from the first unassigned state, states joined by entries
+// above the threshold, in the order they are reached, each net a new
+// substate.  Then, while some creator or annihilator maps two states of one
+// substate into two different substates, the bigger of those two substates
+// joins the smaller and the numbers above it close the gap (restarting the
+// scan after every join).  Returns the new partition.
+static int analyze_hamiltonian(const Model& m0, double threshold, std::vector<int>& s2s) {
+  const int ns = m0.ns, nd = m0.nd;
+  s2s.assign(ns, -1);
+  int nsub = -1;
+  for (int sst = 0; sst < m0.nss; ++sst) {
+    const int n = m0.nst[sst];
+    const Block& H = m0.ham[sst];
+    std::vector<std::vector<int>> nets(1, std::vector<int>(1, 0));
+    ++nsub;
+    s2s[m0.states[sst][0]] = nsub;
+    for (size_t net = 0; net < nets.size(); ++net) {
+      for (size_t node = 0; node < nets[net].size(); ++node) {
+        const int row = nets[net][node];
+        for (int edge = 0; edge < n; ++edge) {
+          const double h = H.at(row, edge);
+          if (h != 0.0 && std::fabs(h) > threshold &&
+              std::find(nets[net].begin(), nets[net].end(), edge) == nets[net].end()) {
+            nets[net].push_back(edge);
+            s2s[m0.states[sst][edge]] = nsub;
+          }
+        }
+      }
+      for (int node = 0; node < n; ++node)
+        if (s2s[m0.states[sst][node]] == -1) {
+          nets.push_back(std::vector<int>(1, node));
+          ++nsub;
+          s2s[m0.states[sst][node]] = nsub;
+          break;
+        }
+    }
+  }
+  // states in the order of the superstates (StatesSStates)
+  std::vector<int> order;
+  for (int sst = 0; sst < m0.nss; ++sst)
+    for (int st : m0.states[sst]) order.push_back(st);
+  bool change = true;
+  while (change) {
+    change = false;
+    for (int ib = 0; ib < nd && !change; ++ib)
+      for (int is = 0; is < 2 && !change; ++is)
+        for (int ca = 0; ca < 2 && !change; ++ca) {
+          const int bit = ib + nd * is;
+          // first target substate seen in each substate
+          std::vector<int> first(ns, -1);
+          for (int st : order) {
+            const bool occ = (st >> bit) & 1;
+            int c = -1;
+            if (!occ && ca == 0) c = st | (1 << bit);
+            else if (occ && ca == 1) c = st & ~(1 << bit);
+            if (c < 0) continue;
+            const int src = s2s[st], tg = s2s[c];
+            if (first[src] < 0) {
+              first[src] = tg;
+            } else if (first[src] != tg) {
+              const int big = std::max(first[src], tg), small = std::min(first[src], tg);
+              for (int x = 0; x < ns; ++x) {
+                if (s2s[x] == big) s2s[x] = small;
+                if (s2s[x] > big) s2s[x] -= 1;
+              }
+              change = true;
+              break;
+            }
+          }
+        }
+  }
+  return *std::max_element(s2s.begin(), s2s.end()) + 1;
+}
+
 static Model* build_model(int nd, const double* umat, const double* muimp, const char* qns) {
-  std::unique_ptr<Model> m(new Model);
-  m->nd = nd;
-  m->nf = 2 * nd;
-  m->ns = 1 << (2 * nd);
+  const int ns = 1 << (2 * nd);
   std::string q(qns ? qns : "");
-  if (q.find("All") != std::string::npos) {
-    g_err = "QuantumNumbers 'All' (automatic partitioning) is not supported";
-    return nullptr;
+  const bool all = q.find("All") != std::string::npos;
+  double epsblock = 1e-13;  // EPSBLOCK default (configspec)
+  {
+    const size_t e = q.find("EPSBLOCK=");
+    if (e != std::string::npos) epsblock = std::strtod(q.c_str() + e + 9, nullptr);
   }
   bool useNt = q.find("Nt") != std::string::npos, useSzt = q.find("Szt") != std::string::npos;
-  m->has_szt = useSzt;
   bool useQzt = q.find("Qzt") != std::string::npos, useAzt = q.find("Azt") != std::string::npos;
   bool useLzt = q.find("Lzt") != std::string::npos, useJzt = q.find("Jzt") != std::string::npos;
   // qns2substates, States.F90:149-186
-  m->sst_of_state.assign(m->ns, -1);
+  std::vector<int> sst_of_state(ns, -1);
   int nss = 0;
-  for (int s1 = 0; s1 < m->ns; ++s1) {
-    if (m->sst_of_state[s1] != -1) continue;
+  for (int s1 = 0; s1 < ns; ++s1) {
+    if (sst_of_state[s1] != -1) continue;
     ++nss;
-    m->sst_of_state[s1] = nss - 1;
-    for (int s2 = s1; s2 < m->ns; ++s2) {
-      if (m->sst_of_state[s2] != -1) continue;
+    sst_of_state[s1] = nss - 1;
+    for (int s2 = s1; s2 < ns; ++s2) {
+      if (sst_of_state[s2] != -1) continue;
       if (useNt && nt_of(s1, nd) != nt_of(s2, nd)) continue;
       if (useSzt && !feq(szt_of(s1, nd), szt_of(s2, nd))) continue;
       if (useQzt && !feq(qzt_of(s1, nd), qzt_of(s2, nd))) continue;
       if (useAzt && !feq(azt_of(s1, nd), azt_of(s2, nd))) continue;
       if (useLzt && !feq(lzt_of(s1, nd), lzt_of(s2, nd))) continue;
       if (useJzt && !feq(lzt_of(s1, nd) + szt_of(s1, nd), lzt_of(s2, nd) + szt_of(s2, nd))) continue;
-      m->sst_of_state[s2] = nss - 1;
+      sst_of_state[s2] = nss - 1;
     }
   }
+  if (all) {
+    std::unique_ptr<Model> m0(build_model_partition(nd, umat, muimp, useSzt, sst_of_state, nss));
+    if (!m0) return nullptr;
+    const int nf = 2 * nd;
+    double mx = 0.0;
+    for (int i = 0; i < nf * nf; ++i) mx = std::max(mx, std::fabs(muimp[i]));
+    for (int i = 0; i < nf * nf * nf * nf; ++i) mx = std::max(mx, std::fabs(umat[i]));
+    nss = analyze_hamiltonian(*m0, epsblock * mx, sst_of_state);
+  }
+  return build_model_partition(nd, umat, muimp, useSzt, sst_of_state, nss);
+}
+
+// init_SubStates + init_Psi + Hamiltonian + diagonalisation + transform_Psis
+// for a given partition of the Fock states into superstates.
+static Model* build_model_partition(int nd, const double* umat, const double* muimp, bool useSzt,
+                                    const std::vector<int>& sst_of_state, int nss) {
+  std::unique_ptr<Model> m(new Model);
+  m->nd = nd;
+  m->nf = 2 * nd;
+  m->ns = 1 << (2 * nd);
+  m->has_szt = useSzt;
+  m->sst_of_state = sst_of_state;
   m->nss = nss;
   m->states.assign(nss, {});
   for (int st = 0; st < m->ns; ++st) m->states[m->sst_of_state[st]].push_back(st);

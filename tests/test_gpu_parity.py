@@ -130,6 +130,34 @@ def test_tree_depth_keeps_the_proposal_stream(lib, name, beta, levels, dense, np
     assert abs(so["trace_log"] - sg["trace_log"]) <= 1e-9 * max(1.0, abs(so["trace_log"]))
 
 
+def test_automatic_partition_proposal_stream(lib):
+    """QuantumNumbers "Nt All" (automatic block partitioning) for two
+    orbitals with inter-orbital hopping in H_loc (dense blocks): the
+    superstates of the engine and the oracle agree and the proposal stream
+    with outer-superstate, global and tau-shift moves matches proposal by
+    proposal."""
+    nd, beta, ntau = 2, 8.0, 20
+    um = P.flat_umatrix(P.umatrix_density(nd, 2.0, 2.0, 0.0))
+    mu = P.muimp_solver(nd, 1.0).copy()
+    for sp in range(2):
+        mu[0, sp, 1, sp] = mu[1, sp, 0, sp] = -0.3
+    ff = P.semicircle_ftau(nd, beta, 1.0, 1000)
+    moves = dict(p_outer=0.1, p_global=0.02, p_shift=0.02)
+    mo = O.Model(nd, um, mu, "Nt All")
+    co = O.Chain(mo, beta, ff, ntau, seed=41, taudiff_max=4.0, **moves)
+    co.start_log(4000)
+    co.warmup(4000)
+    ref = co.log()
+    mg = E.Model(nd, um, mu, "Nt All")
+    assert mg.nsst == mo.nsst == 9 and np.array_equal(mg.sst_size, mo.sst_size)
+    b = E.Batch(mg, [E.Group(beta, ff, ntau, nchains=1, seed0=41, taudiff_max=4.0, kcap=64, opcap=512, **moves)])
+    b.set_log(4000)
+    b.warmup(4000)
+    b.sync()
+    compare_logs(ref, b.log(0), ff[0, 0], beta)
+    assert (ref["outcome"] == 4).sum() > 100
+
+
 @pytest.mark.parametrize("name,beta,tdm,pout,nprop,seed,dense,qns", GLOBAL_CASES)
 def test_global_and_shift_move_parity(lib, name, beta, tdm, pout, nprop, seed, dense, qns):
     """Global moves (StepGlob) and tau-shift moves (StepShiftTau) at 5 %

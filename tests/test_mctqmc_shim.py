@@ -53,6 +53,11 @@ def test_supported_configuration_passes_the_check():
     ctqmc.init_paras(pstring(BASE))
     ctqmc._check_supported()
     ctqmc.dest_paras()
+    # automatic block partitioning (the driver's choice for custom U
+    # matrices and for off-diagonal H_loc) is supported
+    ctqmc.init_paras(pstring(dict(BASE, QuantumNumbers="Nt All", EPSBLOCK=1e-12)))
+    ctqmc._check_supported()
+    ctqmc.dest_paras()
 
 
 def test_offdiag_with_global_shift_and_four_operator_moves_passes_the_check():

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -114,6 +115,159 @@ void jacobi(int n, std::vector<double>& a, std::vector<double>& w, std::vector<d
   v.swap(vs);
 }
 
+// H = sum muimp c+c + 1/2 sum U c+c+cc in the occupation basis, one block
+// per superstate of the partition `sst_of` (states of each superstate in
+// `members` order), by applying each operator string to bit patterns.
+// As the reference assembles H from its superstate connections
+// (Operator.F90:482-546, 1042-1108), every operator of a string must move
+// the state to another superstate (a superstate's Connect entry is never
+// the superstate itself, Operator.F90:146), and entries that leave a
+// superstate are dropped (Operator.F90:1077-1084).  Under quantum numbers
+// that include Nt every operator changes the superstate, so only the
+// second rule ever applies there.
+void assemble_h(int nd, const double* umat, const double* muimp, const std::vector<int>& sst_of,
+                const std::vector<std::vector<uint32_t>>& members, std::vector<std::vector<double>>& H) {
+  const int nf = 2 * nd, ns = 1 << (2 * nd), nss = (int)members.size();
+  std::vector<int> pos_in_sst(ns);
+  for (int s = 0; s < nss; ++s)
+    for (size_t i = 0; i < members[s].size(); ++i) pos_in_sst[members[s][i]] = (int)i;
+  H.assign(nss, {});
+  for (int s = 0; s < nss; ++s) H[s].assign(members[s].size() * members[s].size(), 0.0);
+  auto add_entry = [&](uint32_t from, int to, double v) {
+    const int sf = sst_of[from];
+    if (sst_of[to] != sf) return;
+    const size_t n = members[sf].size();
+    H[sf][(size_t)pos_in_sst[from] * n + pos_in_sst[to]] += v;
+  };
+  auto bit_of = [&](int fl) { return (fl / 2) + nd * (fl % 2); };
+  for (int f1 = 0; f1 < nf; ++f1)
+    for (int f2 = 0; f2 < nf; ++f2) {
+      // muimp(b1,s1,b2,s2) Fortran order
+      const int b1 = f1 / 2, s1 = f1 % 2, b2 = f2 / 2, s2 = f2 % 2;
+      const double v = muimp[b1 + nd * (s1 + 2 * (b2 + nd * s2))];
+      if (v == 0.0) continue;
+      for (int st = 0; st < ns; ++st) {
+        double sg = 1.0;
+        const int a = apply_op(st, bit_of(f2), true, sg);
+        if (a < 0 || sst_of[a] == sst_of[st]) continue;
+        const int c = apply_op(a, bit_of(f1), false, sg);
+        if (c < 0 || sst_of[c] == sst_of[a]) continue;
+        add_entry(st, c, v * sg);
+      }
+    }
+  for (int i = 0; i < nf; ++i)
+    for (int j = 0; j < nf; ++j)
+      for (int k = 0; k < nf; ++k)
+        for (int l = 0; l < nf; ++l) {
+          const double u = umat[i + nf * (j + nf * (k + nf * l))];
+          if (u == 0.0) continue;
+          // 1/2 U_ijkl c+_i c+_j c_l c_k
+          for (int st = 0; st < ns; ++st) {
+            double sg = 1.0;
+            int x = apply_op(st, bit_of(k), true, sg);
+            if (x < 0 || sst_of[x] == sst_of[st]) continue;
+            int y = apply_op(x, bit_of(l), true, sg);
+            if (y < 0 || sst_of[y] == sst_of[x]) continue;
+            x = apply_op(y, bit_of(j), false, sg);
+            if (x < 0 || sst_of[x] == sst_of[y]) continue;
+            y = apply_op(x, bit_of(i), false, sg);
+            if (y < 0 || sst_of[y] == sst_of[x]) continue;
+            add_entry(st, y, 0.5 * u * sg);
+          }
+        }
+  // force_hermitian
+  for (int s = 0; s < nss; ++s) {
+    const size_t n = members[s].size();
+    std::vector<double>& h = H[s];
+    for (size_t i = 0; i < n; ++i)
+      for (size_t j = i + 1; j < n; ++j) {
+        const double a = 0.5 * (h[j * n + i] + h[i * n + j]);
+        h[j * n + i] = h[i * n + j] = a;
+      }
+  }
+}
+
+// QuantumNumbers containing "All": automatic block partitioning
+// (analyze_hamiltonian, Operator.F90:303-442, called by init_solver,
+// CTQMC.F90:7971-7990).  Each superstate of the given partition splits
+// into the connected components of its Hamiltonian (entries of magnitude
+// above `threshold`), numbered in order of discovery from the lowest
+// unassigned state; then blocks are joined until every creator and
+// annihilator maps each block into a single block (the targets of two
+// states of one block are merged).  Joining keeps the lower number and
+// closes the gaps, so the final blocks are numbered by the smallest
+// component number they contain; here the joins run on a union-find forest
+// to the same fixed point.  States of a block in ascending order.
+void partition_all(int nd, const double* umat, const double* muimp, double threshold, std::vector<int>& sst_of,
+                   std::vector<std::vector<uint32_t>>& members) {
+  const int ns = 1 << (2 * nd);
+  std::vector<std::vector<double>> H;
+  assemble_h(nd, umat, muimp, sst_of, members, H);
+  std::vector<int> comp(ns, -1);
+  int ncomp = 0;
+  for (size_t s = 0; s < members.size(); ++s) {
+    const int n = (int)members[s].size();
+    std::vector<int> local(n, -1);
+    for (int start = 0; start < n; ++start) {
+      if (local[start] >= 0) continue;
+      const int id = ncomp++;
+      std::vector<int> net = {start};
+      local[start] = id;
+      for (size_t q = 0; q < net.size(); ++q) {
+        const int node = net[q];
+        for (int e = 0; e < n; ++e) {
+          const double h = H[s][(size_t)node * n + e];
+          if (h != 0.0 && std::fabs(h) > threshold && local[e] < 0) {
+            local[e] = id;
+            net.push_back(e);
+          }
+        }
+      }
+    }
+    for (int i = 0; i < n; ++i) comp[members[s][i]] = local[i];
+  }
+  std::vector<int> parent(ncomp);
+  for (int i = 0; i < ncomp; ++i) parent[i] = i;
+  auto find = [&](int x) {
+    while (parent[x] != x) x = parent[x] = parent[parent[x]];
+    return x;
+  };
+  bool change = true;
+  while (change) {
+    change = false;
+    for (int bit = 0; bit < 2 * nd; ++bit)
+      for (int ann = 0; ann < 2; ++ann) {
+        // first target block seen for each source block
+        std::vector<int> tgt(ncomp, -1);
+        for (int st = 0; st < ns; ++st) {
+          double sg = 1.0;
+          const int r = apply_op(st, bit, ann == 1, sg);
+          if (r < 0) continue;
+          const int a = find(comp[st]), t = find(comp[r]);
+          if (tgt[a] < 0) {
+            tgt[a] = t;
+          } else if (find(tgt[a]) != t) {
+            const int u = find(tgt[a]);
+            parent[std::max(u, t)] = std::min(u, t);
+            change = true;
+          }
+        }
+      }
+  }
+  // final numbering: blocks ordered by their smallest component number
+  std::vector<int> rank(ncomp, -1);
+  int nb = 0;
+  for (int c = 0; c < ncomp; ++c) {
+    const int r = find(c);
+    if (rank[r] < 0) rank[r] = nb++;
+  }
+  members.assign(nb, {});
+  for (int st = 0; st < ns; ++st) {
+    sst_of[st] = rank[find(comp[st])];
+    members[sst_of[st]].push_back((uint32_t)st);
+  }
+}
+
 }  // namespace
 
 bool build_model(int nd, const double* umat, const double* muimp, const char* qns, HostModel& m,
@@ -126,9 +280,11 @@ bool build_model(int nd, const double* umat, const double* muimp, const char* qn
   m.nf = 2 * nd;
   m.ns = 1 << (2 * nd);
   std::string q(qns ? qns : "");
-  if (q.find("All") != std::string::npos) {
-    err = "QuantumNumbers 'All' (automatic block partitioning) is not supported";
-    return false;
+  const bool all = q.find("All") != std::string::npos;
+  double epsblock = 1e-13;  // EPSBLOCK default (configspec)
+  {
+    const size_t e = q.find("EPSBLOCK=");
+    if (e != std::string::npos) epsblock = std::strtod(q.c_str() + e + 9, nullptr);
   }
   QN qf;
   qf.nt = q.find("Nt") != std::string::npos;
@@ -158,6 +314,13 @@ bool build_model(int nd, const double* umat, const double* muimp, const char* qn
         members[id].push_back((uint32_t)s2);
       }
     }
+  }
+  if (all) {
+    // threshold relative to the largest entry of muimp and U (CTQMC.F90:7972-7975)
+    double mx = 0.0;
+    for (int i = 0; i < nf * nf; ++i) mx = std::max(mx, std::fabs(muimp[i]));
+    for (int i = 0; i < nf * nf * nf * nf; ++i) mx = std::max(mx, std::fabs(umat[i]));
+    partition_all(nd, umat, muimp, epsblock * mx, sst_of, members);
   }
   const int nss = (int)members.size();
   m.nss = nss;
@@ -191,71 +354,20 @@ bool build_model(int nd, const double* umat, const double* muimp, const char* qn
             }
             tgt = t;
           }
-          m.connect[((size_t)s * nf + f) * 2 + ca] = tgt;
+          // a superstate never connects to itself (Operator.F90:146)
+          m.connect[((size_t)s * nf + f) * 2 + ca] = tgt == s ? -1 : tgt;
         }
-  // Hamiltonian blocks by acting on bit patterns
-  std::vector<std::vector<double>> H(nss);
-  for (int s = 0; s < nss; ++s) H[s].assign((size_t)m.sst_n[s] * m.sst_n[s], 0.0);
-  auto add_entry = [&](uint32_t from, int to, double v) {
-    int s = sst_of[from];
-    if (sst_of[to] != s) return false;
-    int n = m.sst_n[s];
-    H[s][(size_t)pos_in_sst[from] * n + pos_in_sst[to]] += v;
-    return true;
-  };
+  // Hamiltonian blocks by acting on bit patterns (symmetrised)
+  std::vector<std::vector<double>> H;
+  assemble_h(nd, umat, muimp, sst_of, members, H);
   auto bit_of = [&](int fl) { return (fl / 2) + nd * (fl % 2); };
-  bool blocked = true;
-  for (int f1 = 0; f1 < nf; ++f1)
-    for (int f2 = 0; f2 < nf; ++f2) {
-      // muimp(b1,s1,b2,s2) Fortran order
-      int b1 = f1 / 2, s1 = f1 % 2, b2 = f2 / 2, s2 = f2 % 2;
-      double v = muimp[b1 + nd * (s1 + 2 * (b2 + nd * s2))];
-      if (v == 0.0) continue;
-      for (int st = 0; st < ns; ++st) {
-        double sg = 1.0;
-        int a = apply_op(st, bit_of(f2), true, sg);
-        if (a < 0) continue;
-        int c = apply_op(a, bit_of(f1), false, sg);
-        if (c < 0) continue;
-        if (!add_entry(st, c, v * sg)) blocked = false;
-      }
-    }
-  for (int i = 0; i < nf; ++i)
-    for (int j = 0; j < nf; ++j)
-      for (int k = 0; k < nf; ++k)
-        for (int l = 0; l < nf; ++l) {
-          double u = umat[i + nf * (j + nf * (k + nf * l))];
-          if (u == 0.0) continue;
-          // 1/2 U_ijkl c+_i c+_j c_l c_k
-          for (int st = 0; st < ns; ++st) {
-            double sg = 1.0;
-            int x = apply_op(st, bit_of(k), true, sg);
-            if (x < 0) continue;
-            x = apply_op(x, bit_of(l), true, sg);
-            if (x < 0) continue;
-            x = apply_op(x, bit_of(j), false, sg);
-            if (x < 0) continue;
-            x = apply_op(x, bit_of(i), false, sg);
-            if (x < 0) continue;
-            if (!add_entry(st, x, 0.5 * u * sg)) blocked = false;
-          }
-        }
-  if (!blocked) {
-    // the reference silently ignores entries that break the blocking
-    // (Operator.F90:1077-1084); keep that behaviour
-  }
-  // symmetrise (force_hermitian) and diagonalise
+  // diagonalise
   m.eval.assign(ns, 0.0);
   std::vector<std::vector<double>> V(nss);
   m.egs = 1e300;
   for (int s = 0; s < nss; ++s) {
     int n = m.sst_n[s];
     std::vector<double>& h = H[s];
-    for (int i = 0; i < n; ++i)
-      for (int j = i + 1; j < n; ++j) {
-        double a = 0.5 * (h[(size_t)j * n + i] + h[(size_t)i * n + j]);
-        h[(size_t)j * n + i] = h[(size_t)i * n + j] = a;
-      }
     std::vector<double> w;
     jacobi(n, h, w, V[s]);
     for (int i = 0; i < n; ++i) m.eval[m.sst_off[s] + i] = w[i];

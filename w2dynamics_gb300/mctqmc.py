@@ -170,8 +170,6 @@ def _check_supported():
             bad.append(f"{key} = {_int(key)}")
     if _int("Eigenbasis", 1) == 0:
         bad.append("Eigenbasis = 0")
-    if "All" in _str("QuantumNumbers", "").split():
-        bad.append("QuantumNumbers = All")
     if bad:
         raise NotImplementedError("outside the GPU pair-move engine: " + ", ".join(bad))
 
@@ -191,6 +189,8 @@ def init_solver(u_matrix, Ftau_full, muimp_full, screening, iter_no):
     mu = np.asarray(muimp_full, np.float64).reshape(nd, 2, nd, 2)
     um = np.asarray(u_matrix, np.float64).reshape((2 * nd,) * 4)
     qns = _str("QuantumNumbers", "Nt Szt")
+    if "All" in qns.split():  # automatic partitioning with the EPSBLOCK threshold
+        qns = f"{qns} EPSBLOCK={_real('EPSBLOCK', 1e-13)!r}"
     dest_ctqmc()
     _nd, _beta = nd, _real("beta")
     _nchains = max(1, _int("GPUChains", 1))
